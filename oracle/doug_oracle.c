@@ -1,0 +1,2076 @@
+/*
+ * doug_oracle.c -- CPU restatement of DOUG's solve path.
+ *
+ * TEST INFRASTRUCTURE ONLY: the parity tests, the smoke check and the CPU
+ * baseline of the benchmark use this file as the checker.  The product
+ * (doug_gb300/) never links, loads or calls it.
+ *
+ * Every routine below cites the reference routine it restates
+ * (file:line relative to the DOUG source tree).  Arrays are 1-based (element
+ * 0 unused) so that each loop maps one-to-one onto the Fortran it follows.
+ * Compile with -ffp-contract=off: the reference arithmetic is evaluated in
+ * source order without fused multiply-adds, and the aggregation of the coarse
+ * level depends on the exact bits of the Galerkin product.
+ *
+ * Parity pin: tests/test_oracle.py checks the solutions of the reference
+ * fixtures tests/assembled/lap4x4 and tests/assembled/lap16x16.
+ */
+#include "doug_oracle.h"
+
+#include <ctype.h>
+#include <limits.h>
+#include <math.h>
+#include <setjmp.h>
+#include <stdarg.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+#include <time.h>
+
+/* ------------------------------------------------------------------ */
+/* error handling: DOUG_abort (DOUG_utils.F90:254-286) becomes a longjmp */
+/* back to the API entry, which returns a negative status.              */
+/* ------------------------------------------------------------------ */
+static jmp_buf g_jmp;
+static char g_err[512];
+
+static void orc_abort(const char *fmt, ...) {
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(g_err, sizeof g_err, fmt, ap);
+  va_end(ap);
+  longjmp(g_jmp, 1);
+}
+
+static void *xcalloc(size_t n, size_t sz) {
+  void *p = calloc(n ? n : 1, sz);
+  if (!p) orc_abort("out of memory (%zu x %zu)", n, sz);
+  return p;
+}
+#define NEWI(n) ((int *)xcalloc((size_t)(n) + 1, sizeof(int)))
+#define NEWD(n) ((double *)xcalloc((size_t)(n) + 1, sizeof(double)))
+#define NEWB(n) ((char *)xcalloc((size_t)(n) + 1, 1))
+
+static double now_s(void) {
+  struct timespec ts;
+  clock_gettime(CLOCK_MONOTONIC, &ts);
+  return ts.tv_sec + 1e-9 * ts.tv_nsec;
+}
+
+/* parameters.F90:99-102 */
+#define D_MAXINT 2147483647
+#define D_AGGREGATED D_MAXINT
+#define D_PENDING (D_MAXINT / 2)
+
+enum { ARR_NO = 0, ARR_ROWS = 1, ARR_COLS = 2 };
+enum { SCALE_UNDEF = -1, SCALE_NO = 0, SCALE_DIAG = 1 };
+
+/* ------------------------------------------------------------------ */
+/* control data: globals.F90:85-154, controls.F90:159-246               */
+/* ------------------------------------------------------------------ */
+typedef struct {
+  int solver, method, fine_method, num_iters, coarse_method, num_subdomains,
+      levels, overlap, smoothers, input_type, grid_size, matrix_type,
+      initial_guess, number_of_blocks, radius1, radius2, minasize1, minasize2,
+      maxasize1, maxasize2, debug, verbose, plotting;
+  double strong1, strong2, solve_tolerance;
+  int solve_maxiters;
+  int symmstruct, symmnumeric;
+  int interpolation_type;
+  /* master data */
+  char assembled_mtx_file[300];
+  int assembled_mtx_format;
+  char assembled_rhs_file[300];
+  int assembled_rhs_format;
+  char solution_file[300];
+  int solution_format;
+  int start_vec_type;
+} ctl_t;
+
+static void ctl_defaults(ctl_t *c) {
+  memset(c, 0, sizeof *c);
+  c->solver = c->method = c->fine_method = c->num_iters = c->coarse_method = -1;
+  c->num_subdomains = c->levels = c->overlap = c->smoothers = -1;
+  c->input_type = c->grid_size = c->matrix_type = c->initial_guess = -1;
+  c->number_of_blocks = c->radius1 = c->radius2 = c->minasize1 = -1;
+  c->minasize2 = c->maxasize1 = c->maxasize2 = c->debug = c->verbose = -1;
+  c->plotting = -1;
+  c->strong1 = c->strong2 = c->solve_tolerance = -1.0;
+  c->solve_maxiters = -1;
+  c->interpolation_type = -1;
+  c->assembled_mtx_format = -1;
+  c->assembled_rhs_format = -1;
+  c->solution_format = -1;
+  c->start_vec_type = -1;
+}
+
+/* Fortran internal READ with edit descriptor I10: the first 10 characters,
+ * blanks ignored (BLANK='NULL'), optional sign. DOUG_utils.F90:731ff. */
+int orc_parse_i10(const char *s, int *out) {
+  char buf[11];
+  int k = 0, i;
+  for (i = 0; i < 10 && s[i]; i++)
+    if (s[i] != ' ') buf[k++] = s[i];
+  buf[k] = 0;
+  if (k == 0) { *out = 0; return 0; }
+  char *end;
+  long v = strtol(buf, &end, 10);
+  if (*end) return -1;
+  *out = (int)v;
+  return 0;
+}
+
+/* Fortran internal READ with F10.5: first 10 characters, blanks ignored;
+ * without a decimal point the digits carry 5 implied decimals
+ * (so "8" reads as 8e-5). Used for strong1/strong2/solve_tolerance
+ * (DOUG_utils.F90:914-936). */
+int orc_parse_f10_5(const char *s, double *out) {
+  char buf[11];
+  int k = 0, i;
+  for (i = 0; i < 10 && s[i]; i++)
+    if (s[i] != ' ') buf[k++] = s[i];
+  buf[k] = 0;
+  if (k == 0) { *out = 0.0; return 0; }
+  /* split mantissa / exponent */
+  int p = 0, neg = 0;
+  if (buf[p] == '+' || buf[p] == '-') { neg = buf[p] == '-'; p++; }
+  char mant[16]; int m = 0, has_dot = 0, ndig = 0;
+  while (buf[p] && (isdigit((unsigned char)buf[p]) || buf[p] == '.')) {
+    if (buf[p] == '.') { if (has_dot) return -1; has_dot = 1; }
+    else ndig++;
+    mant[m++] = buf[p++];
+  }
+  mant[m] = 0;
+  int expo = 0;
+  if (buf[p]) {
+    if (buf[p] == 'e' || buf[p] == 'E' || buf[p] == 'd' || buf[p] == 'D') p++;
+    if (!(buf[p] == '+' || buf[p] == '-' || isdigit((unsigned char)buf[p]))) return -1;
+    char *end;
+    long e = strtol(buf + p, &end, 10);
+    if (*end) return -1;
+    expo = (int)e;
+  }
+  if (ndig == 0) return -1;
+  char num[48];
+  if (has_dot)
+    snprintf(num, sizeof num, "%se%d", mant, expo);
+  else
+    snprintf(num, sizeof num, "%se%d", mant, expo - 5);
+  double v = strtod(num, NULL);
+  *out = neg ? -v : v;
+  return 0;
+}
+
+/* L1: first character T/t true, F/f false. */
+int orc_parse_l1(const char *s, int *out) {
+  char c = s[0];
+  if (c == 'T' || c == 't') { *out = 1; return 0; }
+  if (c == 'F' || c == 'f') { *out = 0; return 0; }
+  if (c == '.' && (s[1] == 'T' || s[1] == 't')) { *out = 1; return 0; }
+  if (c == '.' && (s[1] == 'F' || s[1] == 'f')) { *out = 0; return 0; }
+  return -1;
+}
+
+/* getword (DOUG_utils.F90:1518-1544): words are separated by blanks only. */
+static int getword(const char *line, int num, char *word, size_t wsz) {
+  int n = (int)strlen(line);
+  while (n > 0 && (line[n - 1] == ' ' || line[n - 1] == '\n' || line[n - 1] == '\r')) n--;
+  int j = 0, k = 0, i;
+  for (i = 1; i <= num; i++) {
+    while (j < n && line[j] == ' ') j++;
+    if (j >= n) { word[0] = 0; return 0; }
+    k = j;
+    while (j < n && line[j] != ' ') j++;
+  }
+  int len = j - k;
+  if ((size_t)len >= wsz) len = (int)wsz - 1;
+  memcpy(word, line + k, (size_t)len);
+  word[len] = 0;
+  return len;
+}
+
+/* util_actionOnCtrlArg (DOUG_utils.F90:703-1150): the first occurrence of a
+ * word wins (later repeats only warn); unknown words are ignored. */
+#define SETI(name) if (!strcmp(w1, #name)) { if (c->name == -1) { if (orc_parse_i10(w2, &c->name)) orc_abort("bad integer for %s: '%s'", w1, w2); } return; }
+#define SETR(name) if (!strcmp(w1, #name)) { if (c->name == -1.0) { if (orc_parse_f10_5(w2, &c->name)) orc_abort("bad real for %s: '%s'", w1, w2); } return; }
+#define SETL(name) if (!strcmp(w1, #name)) { int _v; if (orc_parse_l1(w2, &_v)) orc_abort("bad logical for %s: '%s'", w1, w2); c->name = _v; return; }
+#define SETS(name) if (!strcmp(w1, #name)) { if (!c->name[0]) snprintf(c->name, sizeof c->name, "%s", w2); return; }
+static void ctl_action(ctl_t *c, const char *w1, const char *w2) {
+  SETI(solver) SETI(method) SETI(fine_method) SETI(num_iters) SETI(grid_size)
+  SETI(coarse_method) SETI(num_subdomains) SETI(levels) SETI(overlap)
+  SETI(smoothers) SETI(input_type) SETI(matrix_type) SETI(initial_guess)
+  SETI(number_of_blocks) SETI(radius1) SETI(radius2) SETI(minasize1)
+  SETI(minasize2) SETI(maxasize1) SETI(maxasize2) SETI(debug) SETI(verbose)
+  SETI(plotting)
+  SETR(strong1) SETR(strong2) SETR(solve_tolerance)
+  SETI(solve_maxiters)
+  SETL(symmstruct) SETL(symmnumeric)
+  SETI(interpolation_type)
+  SETS(assembled_mtx_file) SETI(assembled_mtx_format)
+  SETS(assembled_rhs_file) SETI(assembled_rhs_format)
+  SETS(solution_file) SETI(solution_format) SETI(start_vec_type)
+}
+
+/* CtrlData_initFromFile (DOUG_utils.F90:629-696), on text. */
+static void ctl_parse_text(ctl_t *c, const char *text) {
+  const char *p = text;
+  char line[512], w1[320], w2[320];
+  while (p && *p) {
+    const char *e = strchr(p, '\n');
+    size_t len = e ? (size_t)(e - p) : strlen(p);
+    if (len > 300) len = 300;
+    memcpy(line, p, len);
+    line[len] = 0;
+    p = e ? e + 1 : NULL;
+    int lt = (int)strlen(line);
+    while (lt > 0 && (line[lt - 1] == ' ' || line[lt - 1] == '\r')) lt--;
+    line[lt] = 0;
+    if (lt > 0 && line[0] != '#') {
+      getword(line, 1, w1, sizeof w1);
+      for (char *q = w1; *q; q++)
+        if (*q >= 'A' && *q <= 'Z') *q = (char)(*q + 32);
+      getword(line, 2, w2, sizeof w2);
+      ctl_action(c, w1, w2);
+    }
+  }
+}
+
+static void ctl_finish(ctl_t *c) {
+  if (c->solve_maxiters == -1) c->solve_maxiters = 100; /* DOUG_utils.F90:676-678 */
+}
+
+/* ------------------------------------------------------------------ */
+/* sparse matrix in DOUG's COO + bounds form (SpMtx_class.F90:69-146)  */
+/* ------------------------------------------------------------------ */
+typedef struct {
+  int nnz, nrows, ncols;
+  int *indi, *indj;
+  double *val;
+  int arrange;
+  int *mbound;
+  int mbound_len; /* number of entries in mbound (n+1) */
+  double *diag;
+  int scaling;
+  char *strong;
+  int *srow, *scol;
+  int symmstruct, symmnumeric;
+} spm;
+
+static spm spm_new(int nnz, int nrows, int ncols) {
+  spm m;
+  memset(&m, 0, sizeof m);
+  m.nnz = nnz; m.nrows = nrows; m.ncols = ncols;
+  m.indi = NEWI(nnz); m.indj = NEWI(nnz); m.val = NEWD(nnz);
+  m.arrange = ARR_NO;
+  m.scaling = SCALE_NO;
+  return m;
+}
+
+static void spm_free(spm *m) {
+  free(m->indi); free(m->indj); free(m->val); free(m->mbound); free(m->diag);
+  free(m->strong); free(m->srow); free(m->scol);
+  memset(m, 0, sizeof *m);
+}
+
+static spm spm_copy(const spm *a) { /* SpMtx_Copy, SpMtx_class.F90:680-699 */
+  spm m = spm_new(a->nnz, a->nrows, a->ncols);
+  memcpy(m.indi + 1, a->indi + 1, sizeof(int) * (size_t)a->nnz);
+  memcpy(m.indj + 1, a->indj + 1, sizeof(int) * (size_t)a->nnz);
+  memcpy(m.val + 1, a->val + 1, sizeof(double) * (size_t)a->nnz);
+  m.arrange = a->arrange;
+  if (a->arrange != ARR_NO) {
+    m.mbound_len = a->mbound_len;
+    m.mbound = NEWI(a->mbound_len);
+    memcpy(m.mbound + 1, a->mbound + 1, sizeof(int) * (size_t)a->mbound_len);
+  }
+  return m;
+}
+
+static int imax_arr(const int *a, int n) {
+  int m = INT_MIN, i;
+  for (i = 1; i <= n; i++) if (a[i] > m) m = a[i];
+  return m;
+}
+
+/* SpMtx_arrange (SpMtx_arrangement.F90:58-252): stable bucketing by row or
+ * column; with sort=.true. an insertion sort by the other index. */
+static void spm_arrange(spm *M, int at, int sort, int nnz_o, int nrows_o, int ncols_o) {
+  int Mnnz = nnz_o > 0 ? nnz_o : M->nnz;
+  int Mnrows = nrows_o > 0 ? nrows_o : M->nrows;
+  int Mncols = ncols_o > 0 ? ncols_o : M->ncols;
+  int columnwise = (at == ARR_COLS);
+  int ok = (M->arrange == at);
+  if (ok) {
+    int need = columnwise ? Mncols + 1 : Mnrows + 1;
+    if (!M->mbound || M->mbound_len != need) ok = 0;
+  }
+  if (ok) return; /* "arrange not needed" */
+  M->arrange = at;
+  int nb = columnwise ? Mncols : Mnrows;
+  int *el = NEWI(nb);
+  free(M->mbound);
+  M->mbound = NEWI(nb + 1);
+  M->mbound_len = nb + 1;
+  int i, k;
+  for (i = 1; i <= Mnnz; i++) {
+    k = columnwise ? M->indj[i] : M->indi[i];
+    if (k < 1 || k > nb) orc_abort("arrange: index %d out of range 1..%d", k, nb);
+    el[k]++;
+  }
+  M->mbound[1] = 1;
+  for (i = 1; i <= nb; i++) M->mbound[i + 1] = M->mbound[i] + el[i];
+  int *ni = NEWI(Mnnz), *nj = NEWI(Mnnz);
+  double *nv = NEWD(Mnnz);
+  if (sort) {
+    int *sortref = NEWI(Mnnz);
+    memset(el, 0, sizeof(int) * (size_t)(nb + 1));
+    for (i = 1; i <= Mnnz; i++) {
+      k = columnwise ? M->indj[i] : M->indi[i];
+      int ind_beg = M->mbound[k];
+      if (el[k] == 0) {
+        sortref[ind_beg] = i;
+        el[k] = 1;
+      } else {
+        int ind = M->mbound[k] + el[k];
+        int j = ind_beg;
+        for (;;) {
+          if (j == ind) { sortref[j] = i; el[k]++; break; }
+          int other_i = columnwise ? M->indi[i] : M->indj[i];
+          int other_s = columnwise ? M->indi[sortref[j]] : M->indj[sortref[j]];
+          if (other_i < other_s) {
+            int kk;
+            for (kk = ind; kk >= j + 1; kk--) sortref[kk] = sortref[kk - 1];
+            sortref[j] = i;
+            el[k]++;
+            break;
+          }
+          j++;
+        }
+      }
+    }
+    for (i = 1; i <= Mnnz; i++) {
+      int ind = sortref[i];
+      ni[i] = M->indi[ind]; nj[i] = M->indj[ind]; nv[i] = M->val[ind];
+    }
+    free(sortref);
+  } else {
+    memset(el, 0, sizeof(int) * (size_t)(nb + 1));
+    for (i = 1; i <= Mnnz; i++) {
+      k = columnwise ? M->indj[i] : M->indi[i];
+      int ind = M->mbound[k] + el[k];
+      el[k]++;
+      ni[ind] = M->indi[i]; nj[ind] = M->indj[i]; nv[ind] = M->val[i];
+    }
+  }
+  memcpy(M->indi + 1, ni + 1, sizeof(int) * (size_t)Mnnz);
+  memcpy(M->indj + 1, nj + 1, sizeof(int) * (size_t)Mnnz);
+  memcpy(M->val + 1, nv + 1, sizeof(double) * (size_t)Mnnz);
+  free(ni); free(nj); free(nv); free(el);
+  free(M->strong); M->strong = NULL; /* "destroy strong" :249-250 */
+}
+
+/* SpMtx_scale (SpMtx_arrangement.F90:298-346). */
+static void spm_scale(spm *M) {
+  if (!(M->scaling == SCALE_NO || M->scaling == SCALE_UNDEF)) return;
+  int ndiags = M->nrows > M->ncols ? M->nrows : M->ncols;
+  int i;
+  if (!M->diag) M->diag = NEWD(ndiags);
+  double *s = NEWD(ndiags);
+  for (i = 1; i <= M->nnz; i++)
+    if (M->indi[i] == M->indj[i]) M->diag[M->indi[i]] = M->val[i];
+  if (M->symmstruct && M->symmnumeric) {
+    for (i = 1; i <= ndiags; i++) s[i] = sqrt(fabs(M->diag[i]));
+    for (i = 1; i <= M->nnz; i++) {
+      M->val[i] = M->val[i] / s[M->indi[i]];
+      M->val[i] = M->val[i] / s[M->indj[i]];
+    }
+  } else {
+    for (i = 1; i <= ndiags; i++) s[i] = fabs(M->diag[i]);
+    for (i = 1; i <= M->nnz; i++) M->val[i] = M->val[i] / s[M->indi[i]];
+  }
+  free(s);
+  M->scaling = SCALE_DIAG;
+}
+
+/* SpMtx_unscale (SpMtx_arrangement.F90:350-388). */
+static void spm_unscale(spm *M) {
+  if (M->scaling != SCALE_DIAG) return;
+  int ndiags = M->nrows > M->ncols ? M->nrows : M->ncols;
+  int i;
+  double *s = NEWD(ndiags);
+  if (M->symmstruct && M->symmnumeric) {
+    for (i = 1; i <= ndiags; i++) s[i] = sqrt(fabs(M->diag[i]));
+    for (i = 1; i <= M->nnz; i++) {
+      M->val[i] = M->val[i] * s[M->indi[i]];
+      M->val[i] = M->val[i] * s[M->indj[i]];
+    }
+  } else {
+    for (i = 1; i <= ndiags; i++) s[i] = fabs(M->diag[i]);
+    for (i = 1; i <= M->nnz; i++) M->val[i] = M->val[i] * s[M->indi[i]];
+  }
+  free(s);
+  free(M->diag); M->diag = NULL;
+  M->scaling = SCALE_NO;
+}
+
+/* SpMtx_find_strong (SpMtx_aggregation.F90:829-900), symmetrise off. */
+static void spm_find_strong(spm *A, double alpha) {
+  if (A->scaling == SCALE_NO || A->scaling == SCALE_UNDEF) spm_scale(A);
+  spm_arrange(A, ARR_ROWS, 0, 0, 0, 0);
+  if (!A->strong) A->strong = NEWB(A->nnz);
+  int i, j;
+  for (i = 1; i <= A->nrows; i++) {
+    int start = A->mbound[i], ending = A->mbound[i + 1] - 1;
+    double maxndiag = (double)(-1.0e15f); /* default-real literal */
+    for (j = start; j <= ending; j++)
+      if (A->indj[j] != i) {
+        double aa = fabs(A->val[j]);
+        if (maxndiag < aa) maxndiag = aa;
+      }
+    maxndiag = maxndiag * alpha;
+    for (j = start; j <= ending; j++) {
+      double aa = fabs(A->val[j]);
+      if (A->indj[j] != i)
+        A->strong[j] = aa > maxndiag;
+      else
+        A->strong[j] = A->diag[i] > maxndiag; /* unscaled diagonal, :886 */
+    }
+  }
+}
+
+/* SpMtx_build_refs_symm with sortdown (SpMtx_arrangement.F90:461-568). */
+static void spm_build_refs_symm(spm *A) {
+  int nn = A->nrows, nnz = A->nnz, i;
+  int *cnt = NEWI(nn);
+  for (i = 1; i <= nnz; i++)
+    if (A->strong[i]) {
+      int ii = A->indi[i], jj = A->indj[i];
+      if (ii != jj && jj <= nn) cnt[ii]++;
+    }
+  free(A->srow);
+  A->srow = NEWI(nn + 1);
+  A->srow[1] = 1;
+  for (i = 1; i <= nn; i++) A->srow[i + 1] = A->srow[i] + cnt[i];
+  int noff = A->srow[nn + 1] - 1;
+  free(A->scol);
+  A->scol = NEWI(noff);
+  memset(cnt, 0, sizeof(int) * (size_t)(nn + 1));
+  int *sortref = NEWI(noff);
+  for (i = 1; i <= nnz; i++) {
+    if (!A->strong[i]) continue;
+    int ii = A->indi[i], jj = A->indj[i];
+    if (ii == jj || jj > nn) continue;
+    int ind_beg = A->srow[ii];
+    if (cnt[ii] == 0) {
+      sortref[ind_beg] = i;
+      cnt[ii] = 1;
+    } else {
+      int ind = A->srow[ii] + cnt[ii] - 1;
+      int j = ind_beg;
+      for (;;) {
+        if (j == ind + 1) { sortref[j] = i; cnt[ii]++; break; }
+        if (fabs(A->val[i]) > fabs(A->val[sortref[j]])) {
+          int k;
+          for (k = ind + 1; k >= j + 1; k--) sortref[k] = sortref[k - 1];
+          sortref[j] = i;
+          cnt[ii]++;
+          break;
+        }
+        j++;
+      }
+    }
+  }
+  for (i = 1; i <= noff; i++) A->scol[i] = A->indj[sortref[i]];
+  free(sortref);
+  free(cnt);
+}
+
+/* ------------------------------------------------------------------ */
+/* aggregates (Aggregate_mod.F90)                                       */
+/* ------------------------------------------------------------------ */
+typedef struct {
+  int nagr, radius, nisolated, n;
+  int *num, *starts, *nodes;
+} aggrs;
+
+static void aggrs_free(aggrs *a) {
+  free(a->num); free(a->starts); free(a->nodes);
+  memset(a, 0, sizeof *a);
+}
+
+/* Form_Aggr (Aggregate_mod.F90:82-125). */
+static void form_aggr(aggrs *ag, int nagrs, int n, int radius, int nisolated,
+                      const int *aggrnum) {
+  int i, j;
+  int *starts = NEWI(nagrs + 1), *stat = NEWI(nagrs);
+  for (i = 1; i <= n; i++) {
+    j = aggrnum[i];
+    if (j > 0) stat[j]++;
+  }
+  starts[1] = 1;
+  for (i = 1; i <= nagrs; i++) {
+    starts[i + 1] = starts[i] + stat[i];
+    stat[i] = starts[i];
+  }
+  int *nodes = NEWI(starts[nagrs + 1] - 1);
+  for (i = 1; i <= n; i++) {
+    j = aggrnum[i];
+    if (j > 0) { nodes[stat[j]] = i; stat[j]++; }
+  }
+  ag->nagr = nagrs; ag->radius = radius; ag->nisolated = nisolated; ag->n = n;
+  ag->num = NEWI(n);
+  memcpy(ag->num + 1, aggrnum + 1, sizeof(int) * (size_t)n);
+  ag->starts = starts;
+  ag->nodes = nodes;
+  free(stat);
+}
+
+/* SAVE variables of the reference that persist across calls. */
+static int g_allmind = D_MAXINT;  /* Aggregate_mod.F90:348 (integer,save) */
+static double g_beta = 1.0e-5;    /* SpMtx_aggregation.F90:81 (initialised => SAVE) */
+
+typedef struct {
+  int *inlayer, *newlayer, *roundernodes;
+  int cap, rcap;
+  int neighood, minasize, maxasize;
+  int *stat, *distance, *rowstart, *colnrs, *nodes;
+  int nodes_cap;
+} colour_ctx;
+
+#define CHK(idx, cap) do { if ((idx) > (cap)) orc_abort("aggregation work array overflow (%d > %d)", (idx), (cap)); } while (0)
+
+/* can_add_roundlayer (Aggregate_mod.F90:323-497). */
+static int can_add_roundlayer(colour_ctx *c, int layer, int *ninnodes, int *nneigs) {
+  int nxtlayer = layer + 1, layerfits = 1, ntoadd = 0;
+  int i, j, k, d, rs, re, cn, layernode, nrounders = 0, mind, maxd;
+  int neighood = c->neighood, maxasize = c->maxasize;
+  int *stat = c->stat, *distance = c->distance, *inlayer = c->inlayer,
+      *newlayer = c->newlayer;
+  if (layerfits && layer <= 2 * neighood) {
+    for (k = 1; k <= *ninnodes; k++) {
+      layernode = inlayer[k];
+      rs = c->rowstart[layernode];
+      re = c->rowstart[layernode + 1] - 1;
+      for (i = rs; i <= re; i++) {
+        cn = c->colnrs[i];
+        if (stat[cn] <= 0) {
+          if (stat[cn] == 0) {
+            ntoadd++;
+            CHK(ntoadd, c->cap);
+            newlayer[ntoadd] = cn;
+            distance[cn] = distance[layernode] + 1;
+          }
+          stat[cn] = stat[cn] - 1;
+        }
+      }
+    }
+  }
+  if (layerfits && layer <= neighood) {
+    nrounders = 0;
+    mind = D_MAXINT;
+    maxd = 0;
+    for (k = 1; k <= ntoadd; k++) {
+      d = -stat[newlayer[k]];
+      if (d < mind) mind = d;
+      if (d > maxd) maxd = d;
+    }
+    if (mind < g_allmind) g_allmind = mind;
+    if (mind < maxd || mind > g_allmind) {
+      for (k = 1; k <= ntoadd; k++) {
+        if (stat[newlayer[k]] == -maxd) {
+          nrounders++;
+          if (*nneigs + *ninnodes + 1 > maxasize) { layerfits = 0; break; }
+          (*ninnodes)++;
+          CHK(*ninnodes, c->cap);
+          inlayer[*ninnodes] = newlayer[k];
+          CHK(nrounders, c->rcap);
+          c->roundernodes[nrounders] = newlayer[k];
+          newlayer[k] = -1;
+        }
+      }
+    }
+    if (!layerfits) nrounders = 0;
+    j = 0;
+    for (i = 1; i <= ntoadd; i++)
+      if (newlayer[i] != -1) {
+        j++;
+        if (j < i) newlayer[j] = newlayer[i];
+      }
+    ntoadd = j;
+    for (k = 1; k <= nrounders; k++) {
+      layernode = c->roundernodes[k];
+      rs = c->rowstart[layernode];
+      re = c->rowstart[layernode + 1] - 1;
+      for (i = rs; i <= re; i++) {
+        cn = c->colnrs[i];
+        if (stat[cn] == 0) {
+          ntoadd++;
+          CHK(ntoadd, c->cap);
+          newlayer[ntoadd] = cn;
+          distance[cn] = distance[layernode] + 1;
+        }
+      }
+    }
+  }
+  if (layer <= neighood && *nneigs + *ninnodes > maxasize) layerfits = 0;
+  if (layerfits) {
+    for (k = 1; k <= *ninnodes; k++) {
+      stat[inlayer[k]] = layer + 1;
+      (*nneigs)++;
+      CHK(*nneigs, c->nodes_cap);
+      c->nodes[*nneigs] = inlayer[k];
+    }
+    if (layer <= 2 * neighood) {
+      for (k = 1; k <= ntoadd; k++) stat[newlayer[k]] = D_PENDING - 1;
+      *ninnodes = ntoadd;
+      for (k = 1; k <= ntoadd; k++) inlayer[k] = newlayer[k];
+      return can_add_roundlayer(c, nxtlayer, ninnodes, nneigs);
+    }
+    return 3;
+  }
+  for (k = 1; k <= *ninnodes; k++) distance[inlayer[k]] = 0;
+  for (k = 1; k <= ntoadd; k++) distance[newlayer[k]] = 0;
+  for (k = 1; k <= *nneigs; k++) distance[c->nodes[k]] = 0;
+  for (k = 1; k <= *ninnodes; k++) {
+    (*nneigs)++;
+    CHK(*nneigs, c->nodes_cap);
+    c->nodes[*nneigs] = inlayer[k];
+  }
+  if (*nneigs > 0) return layer > neighood ? 2 : 1;
+  return 0;
+}
+
+/* lets_colour (Aggregate_mod.F90:287-321). */
+static int lets_colour(colour_ctx *c, int innode, int *nneigs) {
+  *nneigs = 0;
+  long virt = 2L * c->maxasize * c->maxasize;
+  if (virt > 50000000L) orc_abort("maxasize too large");
+  c->cap = (int)virt;
+  c->rcap = c->maxasize;
+  c->inlayer = NEWI(c->cap);
+  c->newlayer = NEWI(c->cap);
+  c->roundernodes = NEWI(c->rcap);
+  c->stat[innode] = 1;
+  c->distance[innode] = 0;
+  int ninnodes = 1;
+  c->inlayer[1] = innode;
+  int ok = can_add_roundlayer(c, 0, &ninnodes, nneigs);
+  free(c->inlayer); free(c->newlayer); free(c->roundernodes);
+  return ok;
+}
+
+/* SpMtx_aggregate (SpMtx_aggregation.F90:49-641), numprocs==1. */
+static void spm_aggregate(spm *A, aggrs *inner, aggrs *full, int neighood,
+                          int minaggrsize, int maxaggrsize, double alpha,
+                          int coarse) {
+  int n = A->nrows, nn = n, i, j, k, kk, kkk, node;
+  int toosmall = 0, nagrs = 0, nisolated = 0, unaggregated = 0;
+  int *aggrnum = NEWI(nn), *fullaggrnum = NEWI(n);
+  int sn = (int)sqrtf((float)n); /* default-real sqrt, :123 */
+  int minasize, maxasize, maxasizelargest;
+  (void)unaggregated;
+  minasize = minaggrsize;
+  maxasize = maxaggrsize;
+  if (alpha >= 0 || sn * sn != n) {
+    if (!A->srow) spm_build_refs_symm(A);
+    int *stat = NEWI(n), *nodes = NEWI(n), *distance = NEWI(n);
+    if (!coarse) maxasizelargest = maxasize + 4 * (2 * neighood);
+    else maxasizelargest = 3 * maxasize;
+    if (!coarse) g_beta = alpha / 4.0;
+    int ngoodstarts = 0;
+    int *nextgoodstart = NEWI(n);
+    int firstwocol = 1;
+    colour_ctx c;
+    memset(&c, 0, sizeof c);
+    c.neighood = neighood; c.minasize = minasize; c.maxasize = maxasize;
+    c.stat = stat; c.distance = distance; c.rowstart = A->srow;
+    c.colnrs = A->scol; c.nodes = nodes; c.nodes_cap = n;
+    while (firstwocol <= n) {
+      int startnode, nneigs, ok, mindistance, nouters, next_start_layer;
+      if (ngoodstarts > 0) {
+        j = 0;
+        for (i = 1; i <= ngoodstarts; i++)
+          if (stat[nextgoodstart[i]] < D_PENDING) {
+            j++;
+            if (j < i) nextgoodstart[j] = nextgoodstart[i];
+          }
+        ngoodstarts = j;
+      }
+      if (ngoodstarts == 0) {
+        int done = 0;
+        while (stat[firstwocol] >= D_PENDING) {
+          firstwocol++;
+          if (firstwocol > n) { done = 1; break; }
+        }
+        if (done) break;
+        startnode = firstwocol;
+      } else {
+        startnode = 0;
+        for (i = 2; i <= ngoodstarts && !startnode; i++)
+          for (j = 1; j <= i - 1; j++)
+            if (nextgoodstart[i] == nextgoodstart[j]) { startnode = nextgoodstart[i]; break; }
+        if (startnode == 0) startnode = nextgoodstart[1];
+      }
+      ok = lets_colour(&c, startnode, &nneigs);
+      mindistance = D_MAXINT;
+      if (ok <= 0) orc_abort("aggregation found nothing at node %d", startnode);
+      nagrs++;
+      nouters = 0;
+      if (ok == 3) {
+        int *layerlen = NEWI(2 * neighood + 2);
+        int maxlayer = 0;
+        if (!toosmall && nneigs < minasize) toosmall = 1;
+        for (j = nneigs; j >= 1; j--) {
+          k = stat[nodes[j]];
+          if (k > maxlayer) maxlayer = k;
+          if (k <= neighood + 1) break;
+          if (k > 2 * neighood + 2) orc_abort("layer index out of range");
+          layerlen[k]++;
+        }
+        next_start_layer = neighood + 2;
+        k = layerlen[neighood + 2];
+        for (j = neighood + 3; j <= maxlayer; j++)
+          if (k < layerlen[j]) { k = layerlen[j]; next_start_layer = j; }
+        free(layerlen);
+      } else if (ok == 2) {
+        next_start_layer = neighood + 2;
+        if (!toosmall && nneigs < minasize) toosmall = 1;
+      } else {
+        next_start_layer = 0;
+      }
+      for (j = 1; j <= nneigs; j++) {
+        node = nodes[j];
+        if (stat[node] <= neighood + 1 && j <= maxasize) {
+          stat[node] = D_AGGREGATED;
+          aggrnum[node] = nagrs;
+        } else if (next_start_layer > neighood + 1) {
+          if (stat[node] == next_start_layer) {
+            if (distance[node] < mindistance) mindistance = distance[node];
+            nouters++;
+            nextgoodstart[n - nouters + 1] = node;
+          }
+        }
+      }
+      for (j = 1; j <= nouters; j++)
+        if (distance[nextgoodstart[n - j + 1]] == mindistance) {
+          ngoodstarts++;
+          nextgoodstart[ngoodstarts] = nextgoodstart[n - j + 1];
+        }
+      for (j = 1; j <= nneigs; j++) {
+        node = nodes[j];
+        if (stat[node] != D_AGGREGATED) { distance[node] = 0; stat[node] = 0; }
+      }
+    }
+    free(nextgoodstart); free(distance); free(nodes); free(stat);
+  } else {
+    /* Cartesian aggregates (:332-346) */
+    int nsa = (sn + neighood - 1) / neighood;
+    k = 0;
+    for (i = 1; i <= sn; i++)
+      for (j = 1; j <= sn; j++) {
+        k++;
+        aggrnum[k] = ((i + neighood - 1) / neighood - 1) * nsa + (j + neighood - 1) / neighood;
+      }
+    nagrs = imax_arr(aggrnum, n);
+    nisolated = 0;
+    maxasizelargest = maxasize + 4 * (2 * neighood);
+  }
+  int full_nagrs_new;
+  if (!toosmall) {
+    for (i = 1; i <= n; i++) fullaggrnum[i] = aggrnum[i];
+    full_nagrs_new = imax_arr(fullaggrnum, n);
+    if (full_nagrs_new < 0) full_nagrs_new = 0;
+    form_aggr(inner, nagrs, n, neighood, nisolated, aggrnum);
+  } else {
+    /* repair of too small aggregates (:369-591) */
+    int *aggrsize = NEWI(nagrs);
+    for (i = 1; i <= n; i++) { j = aggrnum[i]; aggrsize[j]++; }
+    int maxstructlen = maxasizelargest;
+    for (i = 1; i <= nagrs; i++) if (aggrsize[i] > maxstructlen) maxstructlen = aggrsize[i];
+    int **structnodes = (int **)xcalloc((size_t)nagrs + 1, sizeof(int *));
+    for (i = 1; i <= nagrs; i++) structnodes[i] = NEWI(maxstructlen);
+    memset(aggrsize, 0, sizeof(int) * (size_t)(nagrs + 1));
+    for (i = 1; i <= n; i++) {
+      j = aggrnum[i];
+      aggrsize[j]++;
+      structnodes[j][aggrsize[j]] = i;
+    }
+    int mnstructneigs = 4 * maxasize;
+    spm_arrange(A, ARR_ROWS, 0, 0, 0, 0);
+    int *colsaround = NEWI(mnstructneigs);
+    double *connweightsums = NEWD(mnstructneigs);
+    int nagrs_new = nagrs;
+    for (i = 1; i <= nagrs; i++) {
+      if (aggrsize[i] >= minasize) continue;
+      int ncolsaround = 0;
+      memset(colsaround, 0, sizeof(int) * (size_t)(mnstructneigs + 1));
+      for (k = 1; k <= aggrsize[i]; k++) {
+        kkk = structnodes[i][k];
+        int rs = A->mbound[kkk], re = A->mbound[kkk + 1] - 1;
+        for (j = rs; j <= re; j++) {
+          int cn = A->indj[j];
+          if (cn <= n) {
+            int colr = aggrnum[cn];
+            if (colr > 0 && colr != i) {
+              for (kk = 1; kk <= ncolsaround; kk++)
+                if (colr == colsaround[kk]) {
+                  connweightsums[kk] = connweightsums[kk] + fabs(A->val[j]);
+                  break;
+                }
+              if (kk > ncolsaround) {
+                ncolsaround++;
+                if (ncolsaround > mnstructneigs) orc_abort("mnstructneigs too small");
+                connweightsums[kk] = fabs(A->val[j]);
+                colsaround[kk] = colr;
+              }
+            }
+          }
+        }
+      }
+      double maxconnweightsum = 0.0;
+      int eater = 0;
+      for (j = 1; j <= ncolsaround; j++)
+        if (maxconnweightsum < connweightsums[j])
+          if (aggrsize[colsaround[j]] + aggrsize[i] <= maxasize) {
+            maxconnweightsum = connweightsums[j];
+            eater = colsaround[j];
+          }
+      if (maxconnweightsum >= alpha || (coarse && maxconnweightsum >= g_beta)) {
+        if (eater == 0) orc_abort("aggregate repair without an eater (alpha <= 0)");
+        for (j = 1; j <= aggrsize[i]; j++) {
+          aggrsize[eater]++;
+          if (aggrsize[eater] > maxstructlen) orc_abort("structnodes overflow");
+          structnodes[eater][aggrsize[eater]] = structnodes[i][j];
+          aggrnum[structnodes[i][j]] = eater;
+        }
+        aggrsize[i] = 0;
+        nagrs_new--;
+      } else {
+        int nleft = aggrsize[i], reduced = 1;
+        while (nleft > 0 && reduced) {
+          reduced = 0;
+          for (k = aggrsize[i]; k >= 1; k--) {
+            kkk = structnodes[i][k];
+            if (kkk > 0) {
+              int rs = A->mbound[kkk], re = A->mbound[kkk + 1] - 1;
+              for (j = rs; j <= re; j++) {
+                int cn = A->indj[j];
+                if (cn <= n) {
+                  int colr = aggrnum[cn];
+                  if (colr != i) {
+                    if (colr < 1) orc_abort("repair: unaggregated neighbour");
+                    if (aggrsize[colr] < maxasizelargest && fabs(A->val[j]) >= g_beta) {
+                      aggrsize[colr]++;
+                      if (aggrsize[colr] > maxstructlen) orc_abort("structnodes overflow");
+                      structnodes[colr][aggrsize[colr]] = structnodes[i][k];
+                      aggrnum[structnodes[i][k]] = colr;
+                      structnodes[i][k] = -1;
+                      nleft--;
+                      reduced = 1;
+                      break;
+                    }
+                  }
+                }
+              }
+            }
+          }
+        }
+        if (nleft > 0 && nleft < aggrsize[i]) {
+          k = 0;
+          for (j = 1; j <= aggrsize[i]; j++)
+            if (structnodes[i][j] > 0) {
+              k++;
+              if (k > 0 && k < j) structnodes[i][k] = structnodes[i][j];
+            }
+          aggrsize[i] = nleft;
+        } else if (nleft == 0) {
+          aggrsize[i] = 0;
+          nagrs_new--;
+        }
+      }
+    }
+    int naggregatednodes = 0;
+    for (i = 1; i <= nagrs; i++) naggregatednodes += aggrsize[i];
+    full_nagrs_new = nagrs_new;
+    int cnt = imax_arr(aggrnum, n);
+    if (cnt > nagrs_new) {
+      int *st = NEWI(cnt), col = 0;
+      for (i = 1; i <= n; i++)
+        if (aggrnum[i] > 0) {
+          int thiscol;
+          if (st[aggrnum[i]] == 0) { col++; st[aggrnum[i]] = col; thiscol = col; }
+          else thiscol = st[aggrnum[i]];
+          aggrnum[i] = thiscol;
+        }
+      free(st);
+    }
+    if (n == naggregatednodes) {
+      for (i = 1; i <= n; i++) fullaggrnum[i] = aggrnum[i];
+      full_nagrs_new = imax_arr(fullaggrnum, n);
+    } else {
+      for (i = 1; i <= n; i++) {
+        if (aggrnum[i] > 0) fullaggrnum[i] = aggrnum[i];
+        else { full_nagrs_new++; fullaggrnum[i] = full_nagrs_new; }
+      }
+    }
+    form_aggr(inner, nagrs_new, n, neighood, n - naggregatednodes, aggrnum);
+    free(connweightsums); free(colsaround);
+    for (i = 1; i <= nagrs; i++) free(structnodes[i]);
+    free(structnodes); free(aggrsize);
+    nagrs = nagrs_new;
+  }
+  form_aggr(full, full_nagrs_new, n, neighood, nisolated, fullaggrnum);
+  free(fullaggrnum); free(aggrnum);
+}
+
+/* Get_aggregate_nodes (Aggregate_mod.F90:162-190). */
+static int get_aggregate_nodes(int cAggr, const aggrs *cA, const aggrs *fA,
+                               int maxnodes, int *nodes) {
+  int *nodeLoc = NEWI(maxnodes), nnodes = 0, ifa, inode;
+  for (ifa = cA->starts[cAggr]; ifa <= cA->starts[cAggr + 1] - 1; ifa++) {
+    int fAggr = cA->nodes[ifa];
+    for (inode = fA->starts[fAggr]; inode <= fA->starts[fAggr + 1] - 1; inode++) {
+      int node = fA->nodes[inode];
+      if (nodeLoc[node] == 0) {
+        nnodes++;
+        nodeLoc[node] = nnodes;
+        nodes[nnodes] = node;
+      }
+    }
+  }
+  free(nodeLoc);
+  return nnodes;
+}
+
+/* ------------------------------------------------------------------ */
+/* SpMtx_AB (SpMtx_op_AB.f90:39-200): Gustavson row by row, dense       */
+/* marker, output columns in first-touch order, zeros kept.             */
+/* ------------------------------------------------------------------ */
+static spm spm_AB(spm *A, spm *B, int AT, int BT) {
+  int *Aindi, *Aindj, *Bindi, *Bindj;
+  int Anrows, Ancols, Bnrows, Bncols;
+  (void)Aindi; (void)Bindi;
+  if (AT) {
+    Aindi = A->indj; Aindj = A->indi;
+    Anrows = A->ncols > imax_arr(A->indj, A->nnz) ? A->ncols : imax_arr(A->indj, A->nnz);
+    Ancols = A->nrows > imax_arr(A->indi, A->nnz) ? A->nrows : imax_arr(A->indi, A->nnz);
+    spm_arrange(A, ARR_COLS, 0, A->nnz, Ancols, Anrows);
+  } else {
+    Aindi = A->indi; Aindj = A->indj;
+    Anrows = A->nrows > imax_arr(A->indi, A->nnz) ? A->nrows : imax_arr(A->indi, A->nnz);
+    Ancols = A->ncols > imax_arr(A->indj, A->nnz) ? A->ncols : imax_arr(A->indj, A->nnz);
+    spm_arrange(A, ARR_ROWS, 0, A->nnz, Anrows, Ancols);
+  }
+  if (BT) {
+    Bindi = B->indj; Bindj = B->indi;
+    Bnrows = B->ncols > imax_arr(B->indj, B->nnz) ? B->ncols : imax_arr(B->indj, B->nnz);
+    Bncols = B->nrows > imax_arr(B->indi, B->nnz) ? B->nrows : imax_arr(B->indi, B->nnz);
+    spm_arrange(B, ARR_COLS, 0, B->nnz, Bncols, Bnrows);
+  } else {
+    Bindi = B->indi; Bindj = B->indj;
+    Bnrows = B->nrows > imax_arr(B->indi, B->nnz) ? B->nrows : imax_arr(B->indi, B->nnz);
+    Bncols = B->ncols > imax_arr(B->indj, B->nnz) ? B->ncols : imax_arr(B->indj, B->nnz);
+    spm_arrange(B, ARR_ROWS, 0, B->nnz, Bnrows, Bncols);
+  }
+  if (Ancols != Bnrows) orc_abort("A*B is impossible: %d vs %d", Ancols, Bnrows);
+  /* after arrange the index pointers may have moved */
+  if (AT) { Aindj = A->indi; } else { Aindj = A->indj; }
+  if (BT) { Bindj = B->indi; } else { Bindj = B->indj; }
+  int *indeces = NEWI(Bncols), *coladder = NEWI(Bncols);
+  /* first pass: count output nnz (the reference grows its estimate and
+   * retries; the result is the same) */
+  long total = 0;
+  int i, k, j;
+  for (i = 1; i <= Anrows; i++) {
+    int nind = 0;
+    for (k = A->mbound[i]; k <= A->mbound[i + 1] - 1; k++) {
+      int kk = Aindj[k];
+      for (j = B->mbound[kk]; j <= B->mbound[kk + 1] - 1; j++) {
+        int jj = Bindj[j];
+        if (coladder[jj] != i) { coladder[jj] = i; nind++; }
+      }
+    }
+    total += nind;
+  }
+  if (total > INT_MAX / 2) orc_abort("SpMtx_AB output too large");
+  int nnz = (int)total;
+  spm AB = spm_new(nnz, Anrows, Bncols);
+  AB.arrange = ARR_ROWS;
+  AB.mbound = NEWI(Anrows + 1);
+  AB.mbound_len = Anrows + 1;
+  memset(coladder, 0, sizeof(int) * (size_t)(Bncols + 1));
+  int counter = 1;
+  for (i = 1; i <= Anrows; i++) {
+    AB.mbound[i] = counter;
+    int nind = 0;
+    for (k = A->mbound[i]; k <= A->mbound[i + 1] - 1; k++) {
+      int kk = Aindj[k];
+      for (j = B->mbound[kk]; j <= B->mbound[kk + 1] - 1; j++) {
+        int jj = Bindj[j];
+        if (coladder[jj] != i) {
+          coladder[jj] = i;
+          nind++;
+          indeces[jj] = nind;
+          AB.indi[counter + nind - 1] = i;
+          AB.indj[counter + nind - 1] = jj;
+          AB.val[counter + nind - 1] = A->val[k] * B->val[j];
+        } else {
+          int kkk = indeces[jj];
+          AB.val[counter + kkk - 1] = AB.val[counter + kkk - 1] + A->val[k] * B->val[j];
+        }
+      }
+    }
+    counter += nind;
+  }
+  AB.mbound[Anrows + 1] = counter;
+  free(indeces); free(coladder);
+  return AB;
+}
+
+/* KeepGivenColumnIndeces (SpMtx_util.f90:232-286) for inds = 1..ninner. */
+static void keep_columns_upto(spm *A, int ninner, int keepShape) {
+  int i, nz = 0;
+  for (i = 1; i <= A->nnz; i++)
+    if (A->indj[i] >= 1 && A->indj[i] <= ninner) {
+      nz++;
+      A->indi[nz] = A->indi[i]; A->indj[nz] = A->indj[i]; A->val[nz] = A->val[i];
+    }
+  if (nz < A->nnz) {
+    A->nnz = nz;
+    if (!keepShape) A->ncols = imax_arr(A->indj, nz);
+  }
+  if (A->arrange != ARR_NO) {
+    free(A->mbound); A->mbound = NULL; A->mbound_len = 0;
+    A->arrange = ARR_NO;
+  }
+}
+
+/* Build one Jacobi-type smoother S (CoarseMtx.F90:154-233 for S with
+ * diag accumulated from 0; :236-301 for S2 whose diagonal is assigned). */
+static spm build_smoother(const spm *A, double omega, int assign_diag) {
+  int N = A->nrows > A->ncols ? A->nrows : A->ncols, i;
+  double *diag = NEWD(N);
+  for (i = 1; i <= A->nnz; i++) {
+    if (A->indi[i] == A->indj[i]) {
+      if (assign_diag) diag[A->indi[i]] = A->val[i];
+      else diag[A->indi[i]] = diag[A->indi[i]] + A->val[i];
+    } else if (!A->strong[i]) {
+      diag[A->indi[i]] = diag[A->indi[i]] + A->val[i];
+    }
+  }
+  spm S = spm_new(A->nnz, A->nrows, A->nrows);
+  int nz = 0;
+  for (i = 1; i <= A->nnz; i++) {
+    nz++;
+    S.indi[nz] = A->indi[i];
+    S.indj[nz] = A->indj[i];
+    if (A->indi[i] == A->indj[i]) S.val[nz] = 1.0 - omega;
+    else if (A->strong[i]) S.val[nz] = -(omega / diag[A->indi[i]] * A->val[i]);
+    else S.val[nz] = 0.0;
+  }
+  free(diag);
+  return S;
+}
+
+/* IntRestBuild (CoarseMtx.F90:50-474), np=1 (no ghost matrix). */
+static spm int_rest_build(const spm *A, const aggrs *ag, int smoothers) {
+  const double omega = 0.33333333333333;  /* :64 */
+  const double omega2 = 0.33333333333333; /* :67 */
+  int Tnrows = A->nrows, i, j, k;
+  int nz = ag->starts[ag->nagr + 1] - 1, nagr = ag->nagr;
+  spm T = spm_new(nz, nagr, Tnrows);
+  for (i = 1; i <= nagr; i++)
+    for (j = ag->starts[i]; j <= ag->starts[i + 1] - 1; j++) T.indi[j] = i;
+  for (k = 1; k <= nz; k++) { T.indj[k] = ag->nodes[k]; T.val[k] = 1.0; }
+  if (smoothers == 0) return T; /* :82-127, arrange_type NO */
+  if (smoothers < 0) orc_abort("smoothers=%d not supported", smoothers);
+  spm S = build_smoother(A, omega, 0);
+  spm R;
+  if (smoothers == 1) {
+    R = spm_AB(&T, &S, 0, 1);
+  } else {
+    spm S2 = build_smoother(A, omega2, 1);
+    spm SS = spm_AB(&S2, &S, 0, 0);
+    if (smoothers == 3) {
+      spm SSS = spm_AB(&SS, &S2, 0, 0);
+      R = spm_AB(&T, &SSS, 0, 0);
+      spm_free(&SSS);
+    } else if (smoothers == 4) {
+      spm SSSS = spm_AB(&SS, &SS, 0, 0);
+      R = spm_AB(&T, &SSSS, 0, 0);
+      spm_free(&SSSS);
+    } else if (smoothers == 5) {
+      spm SSSS = spm_AB(&SS, &SS, 0, 0);
+      spm SSS = spm_AB(&SSSS, &S2, 0, 0);
+      R = spm_AB(&T, &SSS, 0, 0);
+      spm_free(&SSSS); spm_free(&SSS);
+    } else if (smoothers == 6) {
+      spm SSSS = spm_AB(&SS, &SS, 0, 0);
+      spm SSS = spm_AB(&SSSS, &SS, 0, 0);
+      R = spm_AB(&T, &SSS, 0, 0);
+      spm_free(&SSSS); spm_free(&SSS);
+    } else if (smoothers == 7) {
+      spm SSSS = spm_AB(&SS, &SS, 0, 0);
+      spm SSS = spm_AB(&SSSS, &SS, 0, 0);
+      spm_free(&SSSS);
+      SSSS = spm_AB(&SSS, &S2, 0, 0);
+      spm_free(&SSS);
+      R = spm_AB(&T, &SSSS, 0, 0);
+      spm_free(&SSSS);
+    } else if (smoothers == 8) {
+      spm SSSS = spm_AB(&SS, &SS, 0, 0);
+      spm SSS = spm_AB(&SSSS, &SSSS, 0, 0);
+      R = spm_AB(&T, &SSS, 0, 0);
+      spm_free(&SSSS); spm_free(&SSS);
+    } else { /* 2, and >8 which the reference performs as 2 */
+      R = spm_AB(&T, &SS, 0, 1);
+    }
+    spm_free(&SS); spm_free(&S2);
+  }
+  spm_free(&S); spm_free(&T);
+  return R;
+}
+
+/* CoarseMtxBuild (CoarseMtx.F90:476-516), np=1: T=A*R^T, AC=R*T. It
+ * re-arranges R by columns as a side effect, exactly as the reference. */
+static spm coarse_mtx_build(const spm *A, spm *R, int ninner) {
+  spm TT = spm_copy(A);
+  spm T = spm_AB(&TT, R, 0, 1);
+  spm_free(&TT);
+  spm RT = spm_copy(R);
+  keep_columns_upto(&RT, ninner, 1);
+  spm AC = spm_AB(&RT, &T, 0, 0);
+  spm_free(&RT); spm_free(&T);
+  return AC;
+}
+
+/* Add_layers (Decomposition.f90:56-99). nodes has room for nlf entries. */
+static int add_layers(const int *adjBounds, const int *adjValues, int *nodes,
+                      int nnodes, int nlayers, int nlf) {
+  int *frontstart = (int *)xcalloc((size_t)nlayers + 1, sizeof(int));
+  int *frontend = (int *)xcalloc((size_t)nlayers + 1, sizeof(int));
+  int *onfront = NEWI(nlf), i, j, layer;
+  for (i = 1; i <= nnodes; i++) onfront[nodes[i]] = -1;
+  frontstart[0] = 1;
+  int nfront = nnodes;
+  frontend[0] = nfront;
+  for (layer = 1; layer <= nlayers; layer++) {
+    frontstart[layer] = nfront;
+    for (i = frontstart[layer - 1]; i <= frontend[layer - 1]; i++) {
+      int node = nodes[i];
+      for (j = adjBounds[node]; j <= adjBounds[node + 1] - 1; j++) {
+        int neigh = adjValues[j];
+        if (onfront[neigh] == 0) {
+          onfront[neigh] = layer;
+          nfront++;
+          nodes[nfront] = neigh;
+        }
+      }
+    }
+    frontend[layer] = nfront;
+  }
+  int onn = frontend[nlayers];
+  free(frontstart); free(frontend); free(onfront);
+  return onn;
+}
+
+/* ------------------------------------------------------------------ */
+/* exact SPD solver: reverse Cuthill-McKee + profile (envelope)         */
+/* Cholesky.  Stands in for UMFPACK's exact LU (Fact.F90:102-159); both */
+/* are exact solves, so results agree to rounding.                      */
+/* ------------------------------------------------------------------ */
+typedef struct {
+  int n;
+  int *perm;      /* new -> old (0-based) */
+  int *iperm;     /* old -> new */
+  long *rowptr;   /* start of row i in env (0-based), n+1 */
+  int *first;     /* first column of row i */
+  double *env;    /* row i holds L(i, first[i]..i) */
+} profchol;
+
+static void pc_free(profchol *f) {
+  free(f->perm); free(f->iperm); free(f->rowptr); free(f->first); free(f->env);
+  memset(f, 0, sizeof *f);
+}
+
+/* Build a factor from 0-based COO (duplicates summed, as umf4triplet2col). */
+static void pc_factor(profchol *f, int n, int nnz, const int *ii, const int *jj,
+                      const double *vv) {
+  int i, k;
+  memset(f, 0, sizeof *f);
+  f->n = n;
+  /* symmetric adjacency (CSR, deduplicated) for RCM */
+  int *deg = (int *)xcalloc((size_t)n + 1, sizeof(int));
+  for (k = 0; k < nnz; k++)
+    if (ii[k] != jj[k]) { deg[ii[k]]++; deg[jj[k]]++; }
+  int *adjp = (int *)xcalloc((size_t)n + 1, sizeof(int));
+  for (i = 0; i < n; i++) adjp[i + 1] = adjp[i] + deg[i];
+  int *adj = (int *)xcalloc((size_t)adjp[n] + 1, sizeof(int));
+  int *fill = (int *)xcalloc((size_t)n + 1, sizeof(int));
+  for (k = 0; k < nnz; k++)
+    if (ii[k] != jj[k]) {
+      adj[adjp[ii[k]] + fill[ii[k]]++] = jj[k];
+      adj[adjp[jj[k]] + fill[jj[k]]++] = ii[k];
+    }
+  /* dedupe each list */
+  int *mark = (int *)xcalloc((size_t)n + 1, sizeof(int));
+  for (i = 0; i < n; i++) mark[i] = -1;
+  int *udeg = (int *)xcalloc((size_t)n + 1, sizeof(int));
+  for (i = 0; i < n; i++) {
+    int w = adjp[i];
+    for (k = adjp[i]; k < adjp[i] + fill[i]; k++)
+      if (mark[adj[k]] != i) { mark[adj[k]] = i; adj[w++] = adj[k]; }
+    udeg[i] = w - adjp[i];
+  }
+  /* RCM: BFS from a minimum-degree unvisited node, neighbours by degree */
+  int *order = (int *)xcalloc((size_t)n + 1, sizeof(int));
+  char *vis = (char *)xcalloc((size_t)n + 1, 1);
+  int head = 0, tail = 0;
+  int *tmp = (int *)xcalloc((size_t)n + 1, sizeof(int));
+  while (tail < n) {
+    int s = -1, bestd = INT_MAX;
+    for (i = 0; i < n; i++)
+      if (!vis[i] && udeg[i] < bestd) { bestd = udeg[i]; s = i; }
+    /* one pseudo-peripheral refinement: farthest node of a BFS */
+    {
+      int h = tail, t = tail, last = s;
+      order[t++] = s; vis[s] = 1;
+      while (h < t) {
+        int v = order[h++]; last = v;
+        for (k = adjp[v]; k < adjp[v] + udeg[v]; k++)
+          if (!vis[adj[k]]) { vis[adj[k]] = 1; order[t++] = adj[k]; }
+      }
+      for (k = tail; k < t; k++) vis[order[k]] = 0;
+      s = last;
+    }
+    order[tail++] = s; vis[s] = 1; head = tail - 1;
+    while (head < tail) {
+      int v = order[head++], nt = 0;
+      for (k = adjp[v]; k < adjp[v] + udeg[v]; k++)
+        if (!vis[adj[k]]) { vis[adj[k]] = 1; tmp[nt++] = adj[k]; }
+      /* insertion sort by degree (stable) */
+      int a, b;
+      for (a = 1; a < nt; a++) {
+        int x = tmp[a];
+        for (b = a - 1; b >= 0 && udeg[tmp[b]] > udeg[x]; b--) tmp[b + 1] = tmp[b];
+        tmp[b + 1] = x;
+      }
+      for (a = 0; a < nt; a++) order[tail++] = tmp[a];
+    }
+  }
+  f->perm = (int *)xcalloc((size_t)n + 1, sizeof(int));
+  f->iperm = (int *)xcalloc((size_t)n + 1, sizeof(int));
+  for (i = 0; i < n; i++) f->perm[i] = order[n - 1 - i];
+  for (i = 0; i < n; i++) f->iperm[f->perm[i]] = i;
+  /* envelope */
+  f->first = (int *)xcalloc((size_t)n + 1, sizeof(int));
+  for (i = 0; i < n; i++) f->first[i] = i;
+  for (k = 0; k < nnz; k++) {
+    int r = f->iperm[ii[k]], c = f->iperm[jj[k]];
+    if (c > r) { int t2 = r; r = c; c = t2; }
+    if (c < f->first[r]) f->first[r] = c;
+  }
+  f->rowptr = (long *)xcalloc((size_t)n + 1, sizeof(long));
+  for (i = 0; i < n; i++) f->rowptr[i + 1] = f->rowptr[i] + (i - f->first[i] + 1);
+  f->env = (double *)xcalloc((size_t)f->rowptr[n] + 1, sizeof(double));
+  for (k = 0; k < nnz; k++) {
+    int r = f->iperm[ii[k]], c = f->iperm[jj[k]];
+    if (c > r) continue; /* lower triangle only (matrix is symmetric) */
+    f->env[f->rowptr[r] + (c - f->first[r])] += vv[k];
+  }
+  /* row-oriented Cholesky on the envelope */
+  for (i = 0; i < n; i++) {
+    double *Li = f->env + f->rowptr[i];
+    int fi = f->first[i], j;
+    for (j = fi; j < i; j++) {
+      double *Lj = f->env + f->rowptr[j];
+      int fj = f->first[j];
+      int k0 = fi > fj ? fi : fj;
+      double s = Li[j - fi];
+      for (k = k0; k < j; k++) s -= Li[k - fi] * Lj[k - fj];
+      Li[j - fi] = s / Lj[j - fj];
+    }
+    double s = Li[i - fi];
+    for (k = fi; k < i; k++) s -= Li[k - fi] * Li[k - fi];
+    if (!(s > 0.0)) orc_abort("matrix not positive definite (pivot %d: %g)", i, s);
+    Li[i - fi] = sqrt(s);
+  }
+  free(deg); free(adjp); free(adj); free(fill); free(mark); free(udeg);
+  free(order); free(vis); free(tmp);
+}
+
+/* x = A^-1 b (0-based vectors in the original numbering) */
+static void pc_solve(const profchol *f, const double *b, double *x, double *w) {
+  int n = f->n, i, k;
+  for (i = 0; i < n; i++) w[i] = b[f->perm[i]];
+  for (i = 0; i < n; i++) {
+    const double *Li = f->env + f->rowptr[i];
+    int fi = f->first[i];
+    double s = w[i];
+    for (k = fi; k < i; k++) s -= Li[k - fi] * w[k];
+    w[i] = s / Li[i - fi];
+  }
+  for (i = n - 1; i >= 0; i--) {
+    const double *Li = f->env + f->rowptr[i];
+    int fi = f->first[i];
+    w[i] = w[i] / Li[i - fi];
+    double wi = w[i];
+    for (k = fi; k < i; k++) w[k] -= Li[k - fi] * wi;
+  }
+  for (i = 0; i < n; i++) x[f->perm[i]] = w[i];
+}
+
+int orc_spd_solve(int n, int nnz, const int *ii, const int *jj, const double *vv,
+                  const double *b, double *x) {
+  if (setjmp(g_jmp)) return -1;
+  profchol f;
+  pc_factor(&f, n, nnz, ii, jj, vv);
+  double *w = (double *)xcalloc((size_t)n + 1, sizeof(double));
+  pc_solve(&f, b, x, w);
+  free(w);
+  pc_free(&f);
+  return 0;
+}
+
+/* ------------------------------------------------------------------ */
+/* eigenvalues of the Lanczos tridiagonal: CalculateEigenvalues and the */
+/* EISPACK QL method tql1 (pcg.F90:465-641; Bowdler, Martin, Reinsch &  */
+/* Wilkinson, Num. Math. 11 (1968) 293-306).                            */
+/* ------------------------------------------------------------------ */
+static double pythag(double a, double b) {
+  double p = fmax(fabs(a), fabs(b)), r, s, t, u;
+  if (p == 0.0) return p;
+  r = fmin(fabs(a), fabs(b)) / p;
+  r = r * r;
+  for (;;) {
+    t = 4.0 + r;
+    if (t == 4.0) break;
+    s = r / t;
+    u = 1.0 + 2.0 * s;
+    p = u * p;
+    r = (s / u) * (s / u) * r;
+  }
+  return p;
+}
+
+static int tql1(int n, double *d, double *e) { /* 1-based d, e */
+  int i, j, l, m, ii, l1, l2, mml;
+  double c, c2, c3 = 0, dl1, el1, f, g, h, p, r, s, s2 = 0, tst1, tst2;
+  if (n == 1) return 0;
+  for (i = 2; i <= n; i++) e[i - 1] = e[i];
+  f = 0.0; tst1 = 0.0; e[n] = 0.0;
+  for (l = 1; l <= n; l++) {
+    j = 0;
+    h = fabs(d[l]) + fabs(e[l]);
+    if (tst1 < h) tst1 = h;
+    for (m = l; m <= n; m++) {
+      tst2 = tst1 + fabs(e[m]);
+      if (tst2 == tst1) break;
+    }
+    if (m > n) m = n;
+    if (m != l) {
+      do {
+        if (j == 30) return l;
+        j++;
+        l1 = l + 1; l2 = l1 + 1;
+        g = d[l];
+        p = (d[l1] - g) / (2.0 * e[l]);
+        r = pythag(p, 1.0);
+        d[l] = e[l] / (p + copysign(r, p));
+        d[l1] = e[l] * (p + copysign(r, p));
+        dl1 = d[l1];
+        h = g - d[l];
+        for (i = l2; i <= n; i++) d[i] -= h;
+        f += h;
+        p = d[m]; c = 1.0; c2 = c; el1 = e[l1]; s = 0.0;
+        mml = m - l;
+        for (ii = 1; ii <= mml; ii++) {
+          c3 = c2; c2 = c; s2 = s;
+          i = m - ii;
+          g = c * e[i];
+          h = c * p;
+          r = pythag(p, e[i]);
+          e[i + 1] = s * r;
+          s = e[i] / r;
+          c = p / r;
+          p = c * d[i] - s * g;
+          d[i + 1] = h + s * (c * g + s * d[i]);
+        }
+        p = -s * s2 * c3 * el1 * e[l] / dl1;
+        e[l] = s * p;
+        d[l] = c * p;
+        tst2 = tst1 + fabs(e[l]);
+      } while (tst2 > tst1);
+    }
+    p = d[l] + f;
+    for (ii = 2; ii <= l; ii++) {
+      i = l + 2 - ii;
+      if (p >= d[i - 1]) goto found;
+      d[i] = d[i - 1];
+    }
+    i = 1;
+  found:
+    d[i] = p;
+  }
+  return 0;
+}
+
+static double calc_cond(int it, const double *alpha, const double *beta) {
+  if (it < 1) return 0.0;
+  double *dd = NEWD(it), *ee = NEWD(it);
+  int i;
+  dd[1] = 1.0 / alpha[1];
+  ee[1] = 0.0;
+  for (i = 2; i <= it; i++) {
+    if (alpha[i] == 0 || beta[i] < 0) { free(dd); free(ee); return 0.0; }
+    dd[i] = 1.0 / alpha[i] + beta[i] / alpha[i - 1];
+    ee[i] = -sqrt(beta[i]) / alpha[i - 1];
+  }
+  tql1(it, dd, ee);
+  double c = dd[it] / dd[1];
+  free(dd); free(ee);
+  return c;
+}
+
+/* ------------------------------------------------------------------ */
+/* the whole np=1 path                                                  */
+/* ------------------------------------------------------------------ */
+typedef struct {
+  ctl_t ctl;
+  spm A;
+  double *rhs;
+  int n;
+  aggrs fine_inner, fine_full, coarse_inner, coarse_full;
+  int have_coarse;
+  spm R, AC;
+  int have_R;
+  int nsubd;
+  int *sd_start, *sd_nodes; /* 0-based starts, 1-based node ids */
+  int ol;
+  double strong1, strong2;
+  int r1, r2, min1, max1, min2, max2;
+} state;
+
+static void state_free(state *s) {
+  spm_free(&s->A); free(s->rhs);
+  aggrs_free(&s->fine_inner); aggrs_free(&s->fine_full);
+  aggrs_free(&s->coarse_inner); aggrs_free(&s->coarse_full);
+  spm_free(&s->R); spm_free(&s->AC);
+  free(s->sd_start); free(s->sd_nodes);
+}
+
+/* aggr.F90:131-215 for numprocs==1 (or an imported partition). */
+static void run_setup(state *s, const int *part, int nparts) {
+  ctl_t *c = &s->ctl;
+  int n = s->n, i;
+  /* Partitionings_aggr_InitFine (Partitioning_aggr.F90:33-117) */
+  s->strong1 = (c->strong1 != 0.0) ? c->strong1 : 0.67;
+  s->r1 = (c->radius1 > 0) ? c->radius1 : 2;
+  s->min1 = (c->minasize1 > 0) ? c->minasize1 : (int)(0.5 * (double)((2 * s->r1 + 1) * (2 * s->r1 + 1)));
+  s->max1 = (c->maxasize1 > 0) ? c->maxasize1 : (2 * s->r1 + 1) * (2 * s->r1 + 1);
+  g_allmind = D_MAXINT;
+  g_beta = 1.0e-5;
+  spm_find_strong(&s->A, s->strong1);
+  spm_aggregate(&s->A, &s->fine_inner, &s->fine_full, s->r1, s->min1, s->max1, s->strong1, 0);
+  spm_unscale(&s->A);
+  /* CoarsePreconditioner_smooth_Init (CoarsePreconditioner_smooth.F90:47-89) */
+  if (c->coarse_method > 1) orc_abort("coarse_method %d not supported", c->coarse_method);
+  if (c->smoothers > c->radius1) c->smoothers = c->radius1; /* CoarseMtx.F90:75-78 */
+  s->R = int_rest_build(&s->A, &s->fine_inner, c->smoothers);
+  s->have_R = 1;
+  s->AC = coarse_mtx_build(&s->A, &s->R, n);
+  /* Partitionings_aggr_InitCoarse (Partitioning_aggr.F90:120-193) */
+  s->strong2 = (c->strong2 > 0) ? c->strong2 : s->strong1 / 2.0;
+  spm_find_strong(&s->AC, s->strong2);
+  if (c->radius2 > 0) s->r2 = c->radius2;
+  else {
+    int nn = (int)sqrt(1.0 * (double)s->A.nrows);
+    s->r2 = (int)lround(3.0 * sqrt((double)nn) / (double)(2 * s->r1 + 1) - 1.0);
+  }
+  if (c->minasize2 > 0) s->min2 = c->minasize2;
+  else if (c->radius2 > 0) s->min2 = 2 * c->radius2 + 1;
+  else s->min2 = (int)(0.5 * (double)((2 * s->r2 + 1) * (2 * s->r2 + 1)));
+  s->max2 = (c->maxasize2 > 0) ? c->maxasize2 : (2 * s->r2 + 1) * (2 * s->r2 + 1);
+  spm_aggregate(&s->AC, &s->coarse_inner, &s->coarse_full, s->r2, s->min2, s->max2, s->strong2, 1);
+  spm_unscale(&s->AC);
+  s->have_coarse = 1;
+  /* subdomains: coarse partitions (+ overlap), Preconditioner_base.F90:96-123 */
+  s->ol = (c->overlap < 0) ? (c->smoothers > 0 ? c->smoothers : 0) : c->overlap;
+  spm_arrange(&s->A, ARR_ROWS, 0, 0, 0, 0);
+  int *nodes = NEWI(n);
+  int np = part ? nparts : s->coarse_full.nagr;
+  s->nsubd = np;
+  s->sd_start = (int *)xcalloc((size_t)np + 2, sizeof(int));
+  long cap = 16L * n + 16;
+  s->sd_nodes = (int *)xcalloc((size_t)cap, sizeof(int));
+  long fill = 0;
+  int ip;
+  for (ip = 1; ip <= np; ip++) {
+    int nnodes = 0;
+    if (part) { /* Get_nodes (Decomposition.f90:35-53) on an imported partition */
+      for (i = 1; i <= n; i++) if (part[i - 1] == ip) nodes[++nnodes] = i;
+    } else {
+      nnodes = get_aggregate_nodes(ip, &s->coarse_full, &s->fine_full, n, nodes);
+    }
+    int nexp = add_layers(s->A.mbound, s->A.indj, nodes, nnodes, s->ol, n);
+    if (fill + nexp > cap) {
+      cap = 2 * (fill + nexp);
+      s->sd_nodes = (int *)realloc(s->sd_nodes, sizeof(int) * (size_t)cap);
+      if (!s->sd_nodes) orc_abort("out of memory");
+    }
+    s->sd_start[ip - 1] = (int)fill;
+    memcpy(s->sd_nodes + fill, nodes + 1, sizeof(int) * (size_t)nexp);
+    fill += nexp;
+  }
+  s->sd_start[np] = (int)fill;
+  free(nodes);
+}
+
+/* y = A x with DOUG's row-arranged loop (SpMtx_op_Ax.f90:82-87) */
+static void spmv_rows(const spm *A, const double *x, double *y) {
+  int i, j;
+  for (i = 1; i <= A->nrows; i++) {
+    double s = 0.0;
+    for (j = A->mbound[i]; j <= A->mbound[i + 1] - 1; j++) s = s + A->val[j] * x[A->indj[j]];
+    y[i] = s;
+  }
+}
+
+/* restriction / prolongation with R in its final (column-arranged or
+ * unarranged) form, following SpMtx_Ax (SpMtx_op_Ax.f90:44-101). */
+static void spmv_R(const spm *R, const double *x, double *y, int transp, int ny) {
+  int i, j;
+  for (i = 1; i <= ny; i++) y[i] = 0.0;
+  int at = R->arrange;
+  const int *indi = transp ? R->indj : R->indi;
+  const int *indj = transp ? R->indi : R->indj;
+  if (transp) at = (at == ARR_ROWS) ? ARR_COLS : (at == ARR_COLS ? ARR_ROWS : at);
+  if (at == ARR_NO) {
+    for (j = 1; j <= R->nnz; j++) y[indi[j]] = y[indi[j]] + R->val[j] * x[indj[j]];
+  } else if (at == ARR_ROWS) {
+    int nr = transp ? R->ncols : R->nrows;
+    for (i = 1; i <= nr; i++)
+      for (j = R->mbound[i]; j <= R->mbound[i + 1] - 1; j++) y[i] = y[i] + R->val[j] * x[indj[j]];
+  } else {
+    int nc = transp ? R->nrows : R->ncols;
+    for (j = 1; j <= nc; j++)
+      for (i = R->mbound[j]; i <= R->mbound[j + 1] - 1; i++) y[indi[i]] = y[indi[i]] + R->val[i] * x[j];
+  }
+}
+
+static double dotp(const double *a, const double *b, int n) {
+  double s = 0.0;
+  int i;
+  for (i = 1; i <= n; i++) s = s + a[i] * b[i];
+  return s;
+}
+
+/* pcg_weigs (pcg.F90:289-462) with preconditioner (pcg.F90:216-270). */
+static void run_pcg(state *s, orc_result *res) {
+  ctl_t *c = &s->ctl;
+  int n = s->n, i, sd;
+  int levels = c->levels;
+  int method = c->method;
+  if (c->fine_method != 1 && c->fine_method != 0)
+    orc_abort("Wrong fine method %d", c->fine_method); /* aggr.F90:216-226 */
+  double t0 = now_s();
+  /* Factorise_subdomains (subsolvers.F90:78-163) */
+  profchol *fact = NULL;
+  int maxsd = 1;
+  if (c->fine_method == 1) {
+    fact = (profchol *)xcalloc((size_t)s->nsubd + 1, sizeof(profchol));
+    int *floc = NEWI(n);
+    for (sd = 0; sd < s->nsubd; sd++) {
+      int b0 = s->sd_start[sd], m = s->sd_start[sd + 1] - b0, k;
+      if (m > maxsd) maxsd = m;
+      for (k = 0; k < m; k++) floc[s->sd_nodes[b0 + k]] = k + 1;
+      int cnt = 0;
+      for (k = 1; k <= s->A.nnz; k++)
+        if (floc[s->A.indi[k]] > 0 && floc[s->A.indj[k]] > 0) cnt++;
+      int *si = (int *)xcalloc((size_t)cnt + 1, sizeof(int));
+      int *sj = (int *)xcalloc((size_t)cnt + 1, sizeof(int));
+      double *sv = (double *)xcalloc((size_t)cnt + 1, sizeof(double));
+      cnt = 0;
+      for (k = 1; k <= s->A.nnz; k++)
+        if (floc[s->A.indi[k]] > 0 && floc[s->A.indj[k]] > 0) {
+          si[cnt] = floc[s->A.indi[k]] - 1;
+          sj[cnt] = floc[s->A.indj[k]] - 1;
+          sv[cnt] = s->A.val[k];
+          cnt++;
+        }
+      pc_factor(&fact[sd], m, cnt, si, sj, sv);
+      free(si); free(sj); free(sv);
+      for (k = 0; k < m; k++) floc[s->sd_nodes[b0 + k]] = 0;
+    }
+    free(floc);
+  }
+  profchol cfact;
+  memset(&cfact, 0, sizeof cfact);
+  int nc = s->AC.nrows;
+  if (levels > 1) {
+    int *ci = (int *)xcalloc((size_t)s->AC.nnz + 1, sizeof(int));
+    int *cj = (int *)xcalloc((size_t)s->AC.nnz + 1, sizeof(int));
+    int k;
+    for (k = 0; k < s->AC.nnz; k++) { ci[k] = s->AC.indi[k + 1] - 1; cj[k] = s->AC.indj[k + 1] - 1; }
+    pc_factor(&cfact, nc, s->AC.nnz, ci, cj, s->AC.val + 1);
+    free(ci); free(cj);
+  }
+  double t1 = now_s();
+  res->t_factor = t1 - t0;
+
+  double *x = NEWD(n), *r = NEWD(n), *p = NEWD(n), *q = NEWD(n), *z = NEWD(n);
+  double *subrhs = NEWD(maxsd), *subsol = NEWD(maxsd), *work = NEWD(maxsd);
+  double *crhs = NEWD(nc), *csol = NEWD(nc), *cw = NEWD(nc), *tmpsol = NEWD(n);
+  double tol = c->solve_tolerance;
+  int maxit = c->solve_maxiters;
+  if (maxit == -1) maxit = 100000;
+  double *alpha = NEWD(maxit + 1), *beta = NEWD(maxit + 1);
+  res->res_hist = (double *)xcalloc((size_t)maxit + 1, sizeof(double));
+  spmv_rows(&s->A, x, r);
+  for (i = 1; i <= n; i++) r[i] = s->rhs[i - 1] - r[i];
+  double init_norm = dotp(r, r, n);
+  if (init_norm == 0.0) init_norm = 1.0;
+  res->init_norm = sqrt(init_norm);
+  int it = 0;
+  double ratio_norm = 1.0, rho_prev = 0.0;
+  while (ratio_norm > tol * tol && it < maxit) {
+    it++;
+    /* preconditioner */
+    if (method == 0) {
+      for (i = 1; i <= n; i++) z[i] = r[i];
+    } else {
+      for (i = 1; i <= n; i++) z[i] = 0.0;
+      if (c->fine_method == 0) { /* FinePreconditioner_Apply, type NONE (Preconditioner.F90:38-39) */
+        for (i = 1; i <= n; i++) z[i] = r[i];
+      } else { /* Solve_subdomains (subsolvers.F90:54-76) */
+        for (sd = 0; sd < s->nsubd; sd++) {
+          int b0 = s->sd_start[sd], m = s->sd_start[sd + 1] - b0, k;
+          for (k = 0; k < m; k++) subrhs[k] = r[s->sd_nodes[b0 + k]];
+          pc_solve(&fact[sd], subrhs, subsol, work);
+          for (k = 0; k < m; k++) z[s->sd_nodes[b0 + k]] = z[s->sd_nodes[b0 + k]] + subsol[k];
+        }
+      }
+      if (levels > 1) { /* prec2Level (pcg.F90:144-209), method 1 */
+        spmv_R(&s->R, r, crhs, 0, nc);
+        pc_solve(&cfact, crhs + 1, csol + 1, cw);
+        spmv_R(&s->R, csol, tmpsol, 1, n);
+        if (method == 1)
+          for (i = 1; i <= n; i++) z[i] = z[i] + tmpsol[i];
+      }
+    }
+    double rho_curr = dotp(r, z, n);
+    if (it == 1) {
+      for (i = 1; i <= n; i++) p[i] = z[i];
+    } else {
+      beta[it] = rho_curr / rho_prev;
+      for (i = 1; i <= n; i++) p[i] = z[i] + beta[it] * p[i];
+    }
+    spmv_rows(&s->A, p, q);
+    alpha[it] = rho_curr / dotp(p, q, n);
+    for (i = 1; i <= n; i++) x[i] = x[i] + alpha[it] * p[i];
+    for (i = 1; i <= n; i++) r[i] = r[i] - alpha[it] * q[i];
+    rho_prev = rho_curr;
+    double res_norm = dotp(r, r, n);
+    ratio_norm = res_norm / init_norm;
+    res->res_hist[it - 1] = sqrt(res_norm);
+  }
+  res->t_solve = now_s() - t1;
+  res->iterations = it;
+  res->cond_num = calc_cond(it, alpha, beta);
+  res->x = (double *)xcalloc((size_t)n, sizeof(double));
+  memcpy(res->x, x + 1, sizeof(double) * (size_t)n);
+  if (fact) {
+    for (sd = 0; sd < s->nsubd; sd++) pc_free(&fact[sd]);
+    free(fact);
+  }
+  pc_free(&cfact);
+  free(x); free(r); free(p); free(q); free(z); free(subrhs); free(subsol); free(work);
+  free(crhs); free(csol); free(cw); free(tmpsol); free(alpha); free(beta);
+}
+
+static int *dup0(const int *a1, int n) { /* 1-based -> 0-based copy */
+  int *o = (int *)xcalloc((size_t)n + 1, sizeof(int));
+  if (n > 0) memcpy(o, a1 + 1, sizeof(int) * (size_t)n);
+  return o;
+}
+static double *dupd0(const double *a1, int n) {
+  double *o = (double *)xcalloc((size_t)n + 1, sizeof(double));
+  if (n > 0) memcpy(o, a1 + 1, sizeof(double) * (size_t)n);
+  return o;
+}
+
+static void export_setup(const state *s, orc_result *r) {
+  r->n = s->n;
+  r->nagr_fine = s->fine_inner.nagr;
+  r->aggr_fine = dup0(s->fine_inner.num, s->n);
+  r->nagr_fine_full = s->fine_full.nagr;
+  r->aggr_fine_full = dup0(s->fine_full.num, s->n);
+  if (s->have_coarse) {
+    r->nagr_coarse = s->coarse_inner.nagr;
+    r->aggr_coarse = dup0(s->coarse_inner.num, s->coarse_inner.n);
+    r->nagr_coarse_full = s->coarse_full.nagr;
+    r->aggr_coarse_full = dup0(s->coarse_full.num, s->coarse_full.n);
+  }
+  r->nsubd = s->nsubd;
+  r->subd_starts = (int *)xcalloc((size_t)s->nsubd + 1, sizeof(int));
+  memcpy(r->subd_starts, s->sd_start, sizeof(int) * (size_t)(s->nsubd + 1));
+  int tot = s->sd_start[s->nsubd];
+  r->subd_nodes = (int *)xcalloc((size_t)tot + 1, sizeof(int));
+  memcpy(r->subd_nodes, s->sd_nodes, sizeof(int) * (size_t)tot);
+  r->R_nrows = s->R.nrows; r->R_ncols = s->R.ncols; r->R_nnz = s->R.nnz;
+  r->R_i = dup0(s->R.indi, s->R.nnz); r->R_j = dup0(s->R.indj, s->R.nnz);
+  r->R_v = dupd0(s->R.val, s->R.nnz);
+  r->AC_n = s->AC.nrows; r->AC_nnz = s->AC.nnz;
+  r->AC_i = dup0(s->AC.indi, s->AC.nnz); r->AC_j = dup0(s->AC.indj, s->AC.nnz);
+  r->AC_v = dupd0(s->AC.val, s->AC.nnz);
+  r->overlap = s->ol; r->smoothers = s->ctl.smoothers; r->levels = s->ctl.levels;
+  r->method = s->ctl.method;
+  r->strong1 = s->strong1; r->strong2 = s->strong2;
+  r->radius1 = s->r1; r->radius2 = s->r2;
+  r->minasize1 = s->min1; r->maxasize1 = s->max1;
+  r->minasize2 = s->min2; r->maxasize2 = s->max2;
+  r->tol = s->ctl.solve_tolerance; r->maxit = s->ctl.solve_maxiters;
+}
+
+static void load_coo(state *s, int n, int nnz, const int *ii, const int *jj,
+                     const double *vv) {
+  /* ReadInSparseAssembled (SpMtx_class.F90:410-453) after the file read */
+  if (n > nnz) { int t = n; n = nnz; nnz = t; }
+  s->n = n;
+  s->A = spm_new(nnz, n, n);
+  int k, shift = (nnz > 0 && ii[0] == 0) ? 1 : 0;
+  for (k = 0; k < nnz; k++) {
+    s->A.indi[k + 1] = ii[k] + shift;
+    s->A.indj[k + 1] = jj[k] + shift;
+    s->A.val[k + 1] = vv[k];
+    if (s->A.indi[k + 1] < 1 || s->A.indi[k + 1] > n || s->A.indj[k + 1] < 1 ||
+        s->A.indj[k + 1] > n)
+      orc_abort("matrix index out of range at entry %d", k + 1);
+  }
+  s->A.symmstruct = s->ctl.symmstruct;
+  s->A.symmnumeric = s->A.symmstruct ? s->ctl.symmnumeric : 0;
+  s->A.scaling = SCALE_NO;
+}
+
+static int run_common(int n, int nnz, const int *ii, const int *jj, const double *vv,
+                      const double *rhs, const char *ctl_text, const int *part,
+                      int nparts, int do_solve, orc_result **out) {
+  orc_result *r = (orc_result *)calloc(1, sizeof(orc_result));
+  state *s = (state *)calloc(1, sizeof(state));
+  *out = r;
+  if (setjmp(g_jmp)) {
+    r->status = -1;
+    snprintf(r->errmsg, sizeof r->errmsg, "%s", g_err);
+    state_free(s); free(s);
+    return -1;
+  }
+  ctl_defaults(&s->ctl);
+  ctl_parse_text(&s->ctl, ctl_text ? ctl_text : "");
+  ctl_finish(&s->ctl);
+  load_coo(s, n, nnz, ii, jj, vv);
+  s->rhs = (double *)xcalloc((size_t)s->n + 1, sizeof(double));
+  int i;
+  for (i = 0; i < s->n; i++) s->rhs[i] = rhs ? rhs[i] : 1.0;
+  double t0 = now_s();
+  run_setup(s, part, nparts);
+  r->t_setup = now_s() - t0;
+  export_setup(s, r);
+  r->b = (double *)xcalloc((size_t)s->n + 1, sizeof(double));
+  memcpy(r->b, s->rhs, sizeof(double) * (size_t)s->n);
+  if (do_solve) run_pcg(s, r);
+  state_free(s); free(s);
+  return 0;
+}
+
+int orc_run_coo(int n, int nnz, const int *ii, const int *jj, const double *vv,
+                const double *rhs, const char *ctl_text, const int *part,
+                int nparts, orc_result **out) {
+  return run_common(n, nnz, ii, jj, vv, rhs, ctl_text, part, nparts, 1, out);
+}
+
+int orc_setup_coo(int n, int nnz, const int *ii, const int *jj, const double *vv,
+                  const char *ctl_text, const int *part, int nparts,
+                  orc_result **out) {
+  return run_common(n, nnz, ii, jj, vv, NULL, ctl_text, part, nparts, 0, out);
+}
+
+void orc_free(orc_result *r) {
+  if (!r) return;
+  free(r->x); free(r->b); free(r->res_hist); free(r->aggr_fine);
+  free(r->aggr_fine_full); free(r->aggr_coarse); free(r->aggr_coarse_full);
+  free(r->subd_starts); free(r->subd_nodes); free(r->R_i); free(r->R_j);
+  free(r->R_v); free(r->AC_i); free(r->AC_j); free(r->AC_v);
+  free(r);
+}
+
+/* ------------------------------------------------------------------ */
+/* file formats (SpMtx_class.F90:410-617, Vect.F90:840-947,             */
+/* DOUG_utils.F90:1598-1700)                                            */
+/* ------------------------------------------------------------------ */
+static unsigned char *slurp(const char *path, long *len) {
+  FILE *f = fopen(path, "rb");
+  if (!f) return NULL;
+  fseek(f, 0, SEEK_END);
+  long L = ftell(f);
+  fseek(f, 0, SEEK_SET);
+  unsigned char *buf = (unsigned char *)malloc((size_t)L + 1);
+  if (!buf) { fclose(f); return NULL; }
+  if (L > 0 && fread(buf, 1, (size_t)L, f) != (size_t)L) { fclose(f); free(buf); return NULL; }
+  buf[L] = 0;
+  fclose(f);
+  *len = L;
+  return buf;
+}
+
+static uint32_t be32(const unsigned char *p) {
+  return ((uint32_t)p[0] << 24) | ((uint32_t)p[1] << 16) | ((uint32_t)p[2] << 8) | p[3];
+}
+static double bed(const unsigned char *p) {
+  uint64_t u = ((uint64_t)be32(p) << 32) | be32(p + 4);
+  double d;
+  memcpy(&d, &u, 8);
+  return d;
+}
+static uint32_t le32(const unsigned char *p) {
+  return ((uint32_t)p[3] << 24) | ((uint32_t)p[2] << 16) | ((uint32_t)p[1] << 8) | p[0];
+}
+static double led(const unsigned char *p) {
+  uint64_t u = ((uint64_t)le32(p + 4) << 32) | le32(p);
+  double d;
+  memcpy(&d, &u, 8);
+  return d;
+}
+
+/* Fortran unformatted sequential record (4-byte little-endian markers,
+ * gfortran sub-records for lengths beyond 2^31-1). */
+static const unsigned char *fort_record(const unsigned char *buf, long len, long *pos,
+                                        long *rlen, unsigned char **owned) {
+  *owned = NULL;
+  if (*pos + 4 > len) return NULL;
+  int32_t m = (int32_t)le32(buf + *pos);
+  if (m >= 0) {
+    if (*pos + 8 + m > len) return NULL;
+    const unsigned char *d = buf + *pos + 4;
+    *rlen = m;
+    *pos += 8 + m;
+    return d;
+  }
+  /* sub-records: concatenate */
+  long total = 0, p = *pos;
+  unsigned char *acc = NULL;
+  for (;;) {
+    if (p + 4 > len) { free(acc); return NULL; }
+    int32_t mm = (int32_t)le32(buf + p);
+    long l = mm < 0 ? -(long)mm : mm;
+    if (p + 8 + l > len) { free(acc); return NULL; }
+    acc = (unsigned char *)realloc(acc, (size_t)(total + l + 1));
+    memcpy(acc + total, buf + p + 4, (size_t)l);
+    total += l;
+    p += 8 + l;
+    if (mm >= 0 && p != *pos + 8 + l) break;
+    if (mm > 0) break;
+    if (mm < 0 && total == l && p - 8 - l == *pos) continue;
+    if (mm < 0) continue;
+    break;
+  }
+  *pos = p;
+  *rlen = total;
+  *owned = acc;
+  return acc;
+}
+
+int orc_read_assembled(const char *path, int format, int *n, int *nnz, int **ii,
+                       int **jj, double **vv) {
+  long len = 0;
+  unsigned char *buf = slurp(path, &len);
+  if (!buf) return -1;
+  int N = 0, NNZ = 0, k;
+  if (format == 0) {
+    char *p = (char *)buf, *e;
+    long a = strtol(p, &e, 10); if (e == p) { free(buf); return -2; } p = e;
+    long b = strtol(p, &e, 10); if (e == p) { free(buf); return -2; } p = e;
+    N = (int)a; NNZ = (int)b;
+    int cnt = N > NNZ ? N : NNZ;
+    *ii = (int *)malloc(sizeof(int) * (size_t)(cnt + 1));
+    *jj = (int *)malloc(sizeof(int) * (size_t)(cnt + 1));
+    *vv = (double *)malloc(sizeof(double) * (size_t)(cnt + 1));
+    for (k = 0; k < cnt; k++) {
+      while (*p == ',' || isspace((unsigned char)*p)) p++;
+      long i1 = strtol(p, &e, 10); if (e == p) { free(buf); return -3; } p = e;
+      while (*p == ',' || isspace((unsigned char)*p)) p++;
+      long j1 = strtol(p, &e, 10); if (e == p) { free(buf); return -3; } p = e;
+      while (*p == ',' || isspace((unsigned char)*p)) p++;
+      for (char *q = p; *q && !isspace((unsigned char)*q); q++) if (*q == 'd' || *q == 'D') *q = 'e';
+      double v = strtod(p, &e); if (e == p) { free(buf); return -3; } p = e;
+      (*ii)[k] = (int)i1; (*jj)[k] = (int)j1; (*vv)[k] = v;
+    }
+  } else if (format == 1) {
+    long pos = 0, rl;
+    unsigned char *own;
+    const unsigned char *d = fort_record(buf, len, &pos, &rl, &own);
+    if (!d || rl < 8) { free(buf); return -2; }
+    N = (int)le32(d); NNZ = (int)le32(d + 4);
+    free(own);
+    int cnt = N > NNZ ? N : NNZ;
+    d = fort_record(buf, len, &pos, &rl, &own);
+    if (!d || rl < 16L * cnt) { free(buf); return -3; }
+    *ii = (int *)malloc(sizeof(int) * (size_t)(cnt + 1));
+    *jj = (int *)malloc(sizeof(int) * (size_t)(cnt + 1));
+    *vv = (double *)malloc(sizeof(double) * (size_t)(cnt + 1));
+    for (k = 0; k < cnt; k++) {
+      (*ii)[k] = (int)le32(d + 16L * k);
+      (*jj)[k] = (int)le32(d + 16L * k + 4);
+      (*vv)[k] = led(d + 16L * k + 8);
+    }
+    free(own);
+  } else if (format == 2) {
+    if (len < 8) { free(buf); return -2; }
+    N = (int)be32(buf); NNZ = (int)be32(buf + 4);
+    int cnt = N > NNZ ? N : NNZ;
+    if (len < 8 + 16L * cnt) { free(buf); return -3; }
+    *ii = (int *)malloc(sizeof(int) * (size_t)(cnt + 1));
+    *jj = (int *)malloc(sizeof(int) * (size_t)(cnt + 1));
+    *vv = (double *)malloc(sizeof(double) * (size_t)(cnt + 1));
+    for (k = 0; k < cnt; k++) {
+      (*ii)[k] = (int)be32(buf + 8 + 16L * k);
+      (*jj)[k] = (int)be32(buf + 8 + 16L * k + 4);
+      (*vv)[k] = bed(buf + 8 + 16L * k + 8);
+    }
+  } else {
+    free(buf);
+    return -4;
+  }
+  free(buf);
+  *n = N;
+  *nnz = NNZ;
+  return 0;
+}
+
+int orc_read_vector(const char *path, int format, int n, double *x) {
+  long len = 0;
+  unsigned char *buf = slurp(path, &len);
+  if (!buf) return -1;
+  int k;
+  if (format == 0) { /* '(i9)' count then '(e23.16)' per line */
+    char *p = (char *)buf, *e;
+    long m = strtol(p, &e, 10);
+    if (e == p || m != n) { free(buf); return -2; }
+    p = e;
+    for (k = 0; k < n; k++) {
+      while (isspace((unsigned char)*p)) p++;
+      for (char *q = p; *q && !isspace((unsigned char)*q); q++) if (*q == 'd' || *q == 'D') *q = 'e';
+      x[k] = strtod(p, &e);
+      if (e == p) { free(buf); return -3; }
+      p = e;
+    }
+  } else if (format == 1) {
+    long pos = 0, rl;
+    unsigned char *own;
+    const unsigned char *d = fort_record(buf, len, &pos, &rl, &own);
+    if (!d || rl < 8L * n) { free(buf); return -3; }
+    for (k = 0; k < n; k++) x[k] = led(d + 8L * k);
+    free(own);
+  } else if (format == 2) {
+    if (len < 4 || (int)be32(buf) != n || len < 4 + 8L * n) { free(buf); return -2; }
+    for (k = 0; k < n; k++) x[k] = bed(buf + 4 + 8L * k);
+  } else {
+    free(buf);
+    return -4;
+  }
+  free(buf);
+  return 0;
+}
+
+int orc_write_solution(const char *path, int format, int n, const double *x) {
+  FILE *f = fopen(path, "wb");
+  if (!f) return -1;
+  int k;
+  if (format == 0) {
+    fprintf(f, "%6d\n", n);
+    for (k = 0; k < n; k++) fprintf(f, "%21.14E\n", x[k]);
+  } else if (format == 1) {
+    uint32_t m = (uint32_t)(8 * n);
+    fwrite(&m, 4, 1, f);
+    for (k = 0; k < n; k++) fwrite(&x[k], 8, 1, f);
+    fwrite(&m, 4, 1, f);
+  } else if (format == 2) {
+    unsigned char b[8];
+    uint32_t m = (uint32_t)n;
+    b[0] = (unsigned char)(m >> 24); b[1] = (unsigned char)(m >> 16);
+    b[2] = (unsigned char)(m >> 8); b[3] = (unsigned char)m;
+    fwrite(b, 1, 4, f);
+    for (k = 0; k < n; k++) {
+      uint64_t u;
+      memcpy(&u, &x[k], 8);
+      int q;
+      for (q = 0; q < 8; q++) b[q] = (unsigned char)(u >> (56 - 8 * q));
+      fwrite(b, 1, 8, f);
+    }
+  } else {
+    fclose(f);
+    return -4;
+  }
+  fclose(f);
+  return 0;
+}
+
+int orc_run_ctl(const char *ctl_path, const char *overrides, orc_result **out) {
+  *out = NULL;
+  long len = 0;
+  unsigned char *txt = slurp(ctl_path, &len);
+  if (!txt) {
+    orc_result *r = (orc_result *)calloc(1, sizeof(orc_result));
+    r->status = -1;
+    snprintf(r->errmsg, sizeof r->errmsg, "Unable to open DOUG control file: %s", ctl_path);
+    *out = r;
+    return -1;
+  }
+  size_t ol = overrides ? strlen(overrides) : 0;
+  char *all = (char *)malloc(ol + (size_t)len + 2);
+  memcpy(all, overrides ? overrides : "", ol);
+  all[ol] = '\n';
+  memcpy(all + ol + 1, txt, (size_t)len);
+  all[ol + 1 + len] = 0;
+  free(txt);
+  /* resolve input files relative to the control file's directory */
+  char dir[1024];
+  snprintf(dir, sizeof dir, "%s", ctl_path);
+  char *slash = strrchr(dir, '/');
+  if (slash) *slash = 0; else snprintf(dir, sizeof dir, ".");
+  ctl_t c;
+  int rc;
+  orc_result *r = NULL;
+  if (setjmp(g_jmp)) {
+    r = (orc_result *)calloc(1, sizeof(orc_result));
+    r->status = -1;
+    snprintf(r->errmsg, sizeof r->errmsg, "%s", g_err);
+    *out = r;
+    free(all);
+    return -1;
+  }
+  ctl_defaults(&c);
+  ctl_parse_text(&c, all);
+  if (c.input_type != 2) orc_abort("input_type %d not supported by the oracle", c.input_type);
+  char mpath[1400], rpath[1400];
+  if (c.assembled_mtx_file[0] == '/') snprintf(mpath, sizeof mpath, "%s", c.assembled_mtx_file);
+  else snprintf(mpath, sizeof mpath, "%s/%s", dir, c.assembled_mtx_file);
+  int n, nnz, *ii, *jj;
+  double *vv;
+  rc = orc_read_assembled(mpath, c.assembled_mtx_format < 0 ? 0 : c.assembled_mtx_format,
+                          &n, &nnz, &ii, &jj, &vv);
+  if (rc) orc_abort("Unable to read assembled file: %s (%d)", mpath, rc);
+  int nn = n > nnz ? nnz : n;
+  double *rhs = NULL;
+  if (c.assembled_rhs_file[0]) {
+    if (c.assembled_rhs_file[0] == '/') snprintf(rpath, sizeof rpath, "%s", c.assembled_rhs_file);
+    else snprintf(rpath, sizeof rpath, "%s/%s", dir, c.assembled_rhs_file);
+    rhs = (double *)malloc(sizeof(double) * (size_t)nn);
+    rc = orc_read_vector(rpath, c.assembled_rhs_format < 0 ? 1 : c.assembled_rhs_format, nn, rhs);
+    if (rc) orc_abort("Unable to read rhs file: %s (%d)", rpath, rc);
+  }
+  int nz2 = n > nnz ? n : nnz;
+  rc = orc_run_coo(nn, nz2, ii, jj, vv, rhs, all, NULL, 0, &r);
+  free(ii); free(jj); free(vv); free(rhs); free(all);
+  *out = r;
+  return rc;
+}
