@@ -1,0 +1,253 @@
+"""doug_gb300 -- GB300-native solve path of DOUG (Domain decomposition On
+Unstructured Grids): PCG with a two-level additive Schwarz preconditioner
+(overlapping subdomain solves + smoothed-aggregation coarse grid).
+
+The Python side is a thin host mirror of the reference's solver entry over the
+C ABI in ``include/doug_gpu.h`` (``doug_gb300/_build/libdouggpu.so``):
+
+* control words and control files as in ``doug_aggr -f DOUG.ctl``
+  (src/utils/DOUG_utils.F90:629-1150),
+* assembled input (src/datatypes/SpMtx/SpMtx_class.F90:410-617),
+* ``setup()`` = aggregation + coarse space + subdomains (src/main/aggr.F90:131-226),
+* ``solve()`` = ``pcg_weigs`` (src/solvers/pcg.F90:289-462) on the GPU.
+
+There is no CPU fallback: without the built library or without a CUDA device
+the calls raise.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from dataclasses import dataclass
+
+import numpy as np
+
+from .build import LIB as _LIB_PATH, build as build_library
+
+__all__ = ["DougSolver", "DougError", "SolveStats", "load_library", "build_library",
+           "DG_OK", "DG_NOT_CONVERGED", "DG_BREAKDOWN", "DG_SINGULAR", "DG_BAD_INPUT",
+           "DG_CUDA_ERROR", "DG_NO_DEVICE", "DG_NOT_READY", "EXPORTED_SYMBOLS"]
+
+DG_OK, DG_NOT_CONVERGED, DG_BREAKDOWN, DG_SINGULAR = 0, 1, 2, 3
+DG_BAD_INPUT, DG_CUDA_ERROR, DG_NO_DEVICE, DG_NOT_READY = 4, 5, 6, 7
+_STATUS_NAMES = {0: "DG_OK", 1: "DG_NOT_CONVERGED", 2: "DG_BREAKDOWN", 3: "DG_SINGULAR",
+                 4: "DG_BAD_INPUT", 5: "DG_CUDA_ERROR", 6: "DG_NO_DEVICE", 7: "DG_NOT_READY"}
+
+EXPORTED_SYMBOLS = [
+    "dg_create", "dg_destroy", "dg_last_error", "dg_set_option", "dg_load_ctl",
+    "dg_set_matrix_coo", "dg_set_rhs", "dg_set_partition", "dg_setup", "dg_solve",
+    "dg_solve_device", "dg_write_solution", "dg_get_sizes", "dg_get_aggregates",
+    "dg_get_subdomains", "dg_get_restriction", "dg_get_coarse_matrix",
+]
+
+
+class DougError(RuntimeError):
+    def __init__(self, status: int, message: str):
+        super().__init__(f"{_STATUS_NAMES.get(status, status)}: {message}")
+        self.status = status
+
+
+class _Stats(C.Structure):
+    _fields_ = [("iterations", C.c_int), ("init_norm", C.c_double), ("final_norm", C.c_double),
+                ("true_rel_residual", C.c_double), ("cond_num", C.c_double),
+                ("t_setup_s", C.c_double), ("t_factor_s", C.c_double), ("t_iterate_s", C.c_double),
+                ("t_total_s", C.c_double), ("n", C.c_int), ("nsubdomains", C.c_int),
+                ("ncoarse", C.c_int), ("gpu_launches", C.c_int), ("factor_nnz", C.c_longlong),
+                ("factor_gflop", C.c_double)]
+
+
+@dataclass
+class SolveStats:
+    status: int
+    iterations: int
+    init_norm: float
+    final_norm: float
+    true_rel_residual: float
+    cond_num: float
+    t_setup_s: float
+    t_factor_s: float
+    t_iterate_s: float
+    t_total_s: float
+    n: int
+    nsubdomains: int
+    ncoarse: int
+    gpu_launches: int
+    factor_nnz: int
+    factor_gflop: float
+
+
+_lib = None
+
+
+def load_library(path: str | None = None):
+    """Load libdouggpu.so (built in-tree by ``build_library()``)."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    p = path or _LIB_PATH
+    if not os.path.exists(p):
+        raise DougError(DG_CUDA_ERROR, f"{p} is missing: run doug_gb300.build_library() "
+                                       "(there is no CPU fallback)")
+    L = C.CDLL(p)
+    P = C.POINTER
+    vp = C.c_void_p
+    L.dg_create.argtypes = [P(vp)]
+    L.dg_destroy.argtypes = [vp]
+    L.dg_last_error.argtypes = [vp]
+    L.dg_last_error.restype = C.c_char_p
+    L.dg_set_option.argtypes = [vp, C.c_char_p, C.c_char_p]
+    L.dg_load_ctl.argtypes = [vp, C.c_char_p]
+    L.dg_set_matrix_coo.argtypes = [vp, C.c_int, C.c_int, P(C.c_int), P(C.c_int), P(C.c_double)]
+    L.dg_set_rhs.argtypes = [vp, P(C.c_double)]
+    L.dg_set_partition.argtypes = [vp, P(C.c_int), C.c_int]
+    L.dg_setup.argtypes = [vp]
+    L.dg_solve.argtypes = [vp, P(C.c_double), P(C.c_double), P(_Stats)]
+    L.dg_solve_device.argtypes = [vp, vp, vp, P(_Stats), vp]
+    L.dg_write_solution.argtypes = [vp, P(C.c_double)]
+    L.dg_get_sizes.argtypes = [vp, P(C.c_int), P(C.c_int), P(C.c_int), P(C.c_int), P(C.c_longlong),
+                               P(C.c_int), P(C.c_int)]
+    L.dg_get_aggregates.argtypes = [vp, P(C.c_int), P(C.c_int)]
+    L.dg_get_subdomains.argtypes = [vp, P(C.c_longlong), P(C.c_int)]
+    L.dg_get_restriction.argtypes = [vp, P(C.c_int), P(C.c_int), P(C.c_double)]
+    L.dg_get_coarse_matrix.argtypes = [vp, P(C.c_int), P(C.c_int), P(C.c_double)]
+    for nm in EXPORTED_SYMBOLS:
+        if nm not in ("dg_destroy", "dg_last_error"):
+            getattr(L, nm).restype = C.c_int
+    if path is None:
+        _lib = L
+    return L
+
+
+def _ip(a):
+    return a.ctypes.data_as(C.POINTER(C.c_int))
+
+
+def _dp(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+class DougSolver:
+    """One linear system and its preconditioner on one GPU (a ``dg_handle``)."""
+
+    def __init__(self, options: dict | None = None, ctl: str | None = None):
+        self._L = load_library()
+        self._h = C.c_void_p()
+        self._check(self._L.dg_create(C.byref(self._h)))
+        if ctl is not None:
+            self.load_ctl(ctl)
+        for k, v in (options or {}).items():
+            self.set_option(k, v)
+
+    def __del__(self):
+        try:
+            if self._h:
+                self._L.dg_destroy(self._h)
+                self._h = C.c_void_p()
+        except Exception:
+            pass
+
+    def _check(self, rc, allow=()):
+        if rc != DG_OK and rc not in allow:
+            msg = self._L.dg_last_error(self._h) if self._h else b""
+            raise DougError(rc, (msg or b"").decode(errors="replace"))
+        return rc
+
+    # --- inputs -----------------------------------------------------------
+    def set_option(self, name: str, value) -> None:
+        if isinstance(value, bool):
+            value = "T" if value else "F"
+        self._check(self._L.dg_set_option(self._h, name.encode(), str(value).encode()))
+
+    def load_ctl(self, path: str) -> None:
+        self._check(self._L.dg_load_ctl(self._h, path.encode()))
+
+    def set_matrix_coo(self, n: int, rows1, cols1, vals) -> None:
+        r = np.ascontiguousarray(rows1, dtype=np.int32)
+        c = np.ascontiguousarray(cols1, dtype=np.int32)
+        v = np.ascontiguousarray(vals, dtype=np.float64)
+        self._check(self._L.dg_set_matrix_coo(self._h, int(n), len(v), _ip(r), _ip(c), _dp(v)))
+
+    def set_rhs(self, b) -> None:
+        b = np.ascontiguousarray(b, dtype=np.float64)
+        self._check(self._L.dg_set_rhs(self._h, _dp(b)))
+
+    def set_partition(self, part) -> None:
+        p = np.ascontiguousarray(part, dtype=np.int32)
+        self._check(self._L.dg_set_partition(self._h, _ip(p), int(p.max())))
+
+    # --- setup / solve ----------------------------------------------------
+    def setup(self) -> None:
+        self._check(self._L.dg_setup(self._h))
+
+    def setup_host_only(self) -> int:
+        """Run the host setup; a missing GPU is reported, not raised.  The
+        parity export (aggregates, subdomains, R, AC) is available after it."""
+        return self._check(self._L.dg_setup(self._h), allow=(DG_NO_DEVICE, DG_CUDA_ERROR))
+
+    def solve(self, b=None, allow_not_converged: bool = False):
+        n = self.sizes()["n"]
+        x = np.zeros(n, dtype=np.float64)
+        st = _Stats()
+        bb = None if b is None else np.ascontiguousarray(b, dtype=np.float64)
+        rc = self._L.dg_solve(self._h, _dp(bb) if bb is not None else None, _dp(x), C.byref(st))
+        self._check(rc, allow=(DG_NOT_CONVERGED,) if allow_not_converged else ())
+        return x, self._stats(rc, st)
+
+    def solve_device(self, b_ptr: int, x_ptr: int, stream: int = 0, allow_not_converged=False):
+        """Solve with device pointers (e.g. ``tensor.data_ptr()``) on a CUDA stream."""
+        st = _Stats()
+        rc = self._L.dg_solve_device(self._h, C.c_void_p(b_ptr), C.c_void_p(x_ptr), C.byref(st),
+                                     C.c_void_p(stream))
+        self._check(rc, allow=(DG_NOT_CONVERGED,) if allow_not_converged else ())
+        return self._stats(rc, st)
+
+    def write_solution(self, x) -> None:
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        self._check(self._L.dg_write_solution(self._h, _dp(x)))
+
+    @staticmethod
+    def _stats(rc, st):
+        return SolveStats(rc, st.iterations, st.init_norm, st.final_norm, st.true_rel_residual,
+                          st.cond_num, st.t_setup_s, st.t_factor_s, st.t_iterate_s, st.t_total_s,
+                          st.n, st.nsubdomains, st.ncoarse, st.gpu_launches, st.factor_nnz,
+                          st.factor_gflop)
+
+    # --- parity export ----------------------------------------------------
+    def sizes(self) -> dict:
+        v = [C.c_int() for _ in range(4)]
+        tot = C.c_longlong()
+        rn, an = C.c_int(), C.c_int()
+        self._check(self._L.dg_get_sizes(self._h, C.byref(v[0]), C.byref(v[1]), C.byref(v[2]),
+                                         C.byref(v[3]), C.byref(tot), C.byref(rn), C.byref(an)))
+        return {"n": v[0].value, "nagr_fine": v[1].value, "nagr_coarse": v[2].value,
+                "nsubdomains": v[3].value, "subdomain_total": tot.value, "R_nnz": rn.value,
+                "AC_nnz": an.value}
+
+    def aggregates(self):
+        s = self.sizes()
+        f = np.zeros(s["n"], dtype=np.int32)
+        c = np.zeros(max(s["nagr_fine"], 1), dtype=np.int32)
+        self._check(self._L.dg_get_aggregates(self._h, _ip(f), _ip(c)))
+        return f, c[: s["nagr_fine"]]
+
+    def subdomains(self):
+        s = self.sizes()
+        st = np.zeros(s["nsubdomains"] + 1, dtype=np.int64)
+        nd = np.zeros(max(s["subdomain_total"], 1), dtype=np.int32)
+        self._check(self._L.dg_get_subdomains(self._h, st.ctypes.data_as(C.POINTER(C.c_longlong)),
+                                              _ip(nd)))
+        return [nd[st[i]:st[i + 1]].copy() for i in range(s["nsubdomains"])]
+
+    def restriction(self):
+        s = self.sizes()
+        k = s["R_nnz"]
+        i, j, v = np.zeros(k, np.int32), np.zeros(k, np.int32), np.zeros(k, np.float64)
+        self._check(self._L.dg_get_restriction(self._h, _ip(i), _ip(j), _dp(v)))
+        return i, j, v
+
+    def coarse_matrix(self):
+        s = self.sizes()
+        k = s["AC_nnz"]
+        i, j, v = np.zeros(k, np.int32), np.zeros(k, np.int32), np.zeros(k, np.float64)
+        self._check(self._L.dg_get_coarse_matrix(self._h, _ip(i), _ip(j), _dp(v)))
+        return i, j, v

@@ -1,0 +1,481 @@
+// sm_103a kernels of the GB300 solve path.
+//
+//   * batched multifrontal Cholesky (assembly + extend-add + partial
+//     factorisation), one launch per assembly-tree level for all subdomains;
+//   * multifrontal forward / backward solves, one launch per level;
+//   * Schwarz gather and deterministic "pull" sum of subdomain solutions
+//     (the reference adds subdomain solutions in subdomain order,
+//     src/solvers/subsolvers.F90:68-73, then the coarse correction,
+//     src/solvers/pcg.F90:191-193; the pull kernel adds in that same order);
+//   * restriction / prolongation with R and P = R^T (src/solvers/pcg.F90:149,188);
+//   * CSR SpMV fused with the CG direction update and the p.q partial sums;
+//   * fused PCG vector updates with deterministic two-pass reductions.
+//
+// All waits are __syncthreads barriers; no kernel spins on memory.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace dg {
+
+constexpr int kRedBlocks = 1024;   // partial-sum slots of every reduction
+constexpr int kVecThreads = 256;
+
+// device error word bits
+enum : int { ERR_NOT_SPD = 1, ERR_NAN = 2, ERR_BREAKDOWN = 4 };
+
+struct MfView {  // device pointers of one multifrontal batch
+  const int64_t *f_off;
+  const int *f_m, *f_k;
+  const int64_t *f_rows, *f_xoff;
+  const int *f_p0;
+  const int64_t *f_uoff, *f_woff;
+  const int *f_child_ptr, *f_children;
+  const int64_t *f_relmap, *f_asm;
+  const int *rows, *relmap;
+  const int64_t *asm_tgt, *asm_sp, *asm_src;
+};
+
+// ---------------------------------------------------------------------------
+// reductions
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  return v;
+}
+__device__ __forceinline__ float warp_sumf(float v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// block sum in a fixed order (result valid in thread 0)
+template <int NT>
+__device__ __forceinline__ double block_sum(double v, double *sh) {
+  v = warp_sum(v);
+  int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (lane == 0) sh[wid] = v;
+  __syncthreads();
+  double s = 0.0;
+  if (wid == 0) {
+    s = lane < NT / 32 ? sh[lane] : 0.0;
+    s = warp_sum(s);
+  }
+  __syncthreads();
+  return s;
+}
+
+// sum of the kRedBlocks partials in a fixed order, by one warp; every lane
+// of warp 0 gets the result
+__device__ __forceinline__ double sum_partials(const double *part) {
+  double s = 0.0;
+  int lane = threadIdx.x & 31;
+  for (int q = lane; q < kRedBlocks; q += 32) s += part[q];
+  s = warp_sum(s);
+  return __shfl_sync(0xffffffffu, s, 0);
+}
+
+// ---------------------------------------------------------------------------
+// multifrontal numeric factorisation, one CTA per front of a level
+// ---------------------------------------------------------------------------
+template <typename T>
+__device__ __forceinline__ T tsqrt(T x);
+template <>
+__device__ __forceinline__ double tsqrt<double>(double x) { return sqrt(x); }
+template <>
+__device__ __forceinline__ float tsqrt<float>(float x) { return sqrtf(x); }
+
+constexpr int kMfThreads = 256;
+constexpr int kNB = 32;      // panel width
+constexpr int kTile = 64;    // trailing-update tile (64 x 64 per CTA step, 4x4 per thread)
+
+template <typename T>
+__global__ void __launch_bounds__(kMfThreads)
+mf_factor_level(MfView v, const int *__restrict__ fronts, const double *__restrict__ vals,
+                T *__restrict__ arena, int *__restrict__ status) {
+  __shared__ T As[kNB][kTile];
+  __shared__ T Bs[kNB][kTile];
+  __shared__ T piv;
+  const int f = fronts[blockIdx.x];
+  const int m = v.f_m[f], k = v.f_k[f];
+  T *F = arena + v.f_off[f];
+  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5, nw = kMfThreads / 32;
+  // 1. zero the lower triangle
+  for (int c = wid; c < m; c += nw)
+    for (int i = c + lane; i < m; i += 32) F[(int64_t)c * m + i] = T(0);
+  __syncthreads();
+  // 2. original entries (each target appears once; duplicates summed in order)
+  for (int64_t e = v.f_asm[f] + tid; e < v.f_asm[f + 1]; e += kMfThreads) {
+    double s = 0.0;
+    for (int64_t q = v.asm_sp[e]; q < v.asm_sp[e + 1]; q++) s += vals[v.asm_src[q]];
+    arena[v.asm_tgt[e]] = (T)s;
+  }
+  __syncthreads();
+  // 3. extend-add of the children's update matrices, children in order
+  for (int ci = v.f_child_ptr[f]; ci < v.f_child_ptr[f + 1]; ci++) {
+    const int c = v.f_children[ci];
+    const int mc = v.f_m[c], kc = v.f_k[c], rc = mc - kc;
+    const T *U = arena + v.f_off[c] + (int64_t)kc * mc + kc;
+    const int *rel = v.relmap + v.f_relmap[c];
+    for (int b = wid; b < rc; b += nw) {
+      const int pb = rel[b];
+      for (int a = b + lane; a < rc; a += 32) F[(int64_t)pb * m + rel[a]] += U[(int64_t)b * mc + a];
+    }
+    __syncthreads();
+  }
+  // 4. partial Cholesky of the k pivot columns; the trailing (m-k) block
+  //    becomes the update (Schur complement) matrix
+  for (int j0 = 0; j0 < k; j0 += kNB) {
+    const int jb = min(kNB, k - j0);
+    for (int j = j0; j < j0 + jb; j++) {
+      if (tid == 0) {
+        T d = F[(int64_t)j * m + j];
+        if (!(d > T(0))) { atomicOr(status, ERR_NOT_SPD); d = T(1); }
+        piv = tsqrt<T>(d);
+        F[(int64_t)j * m + j] = piv;
+      }
+      __syncthreads();
+      const T p = piv;
+      for (int i = j + 1 + tid; i < m; i += kMfThreads) F[(int64_t)j * m + i] /= p;
+      __syncthreads();
+      // remaining columns of the panel
+      for (int c = j + 1 + wid; c < j0 + jb; c += nw) {
+        const T lcj = F[(int64_t)j * m + c];
+        for (int i = c + lane; i < m; i += 32) F[(int64_t)c * m + i] -= F[(int64_t)j * m + i] * lcj;
+      }
+      __syncthreads();
+    }
+    // trailing update of columns [j0+jb, m): F -= Lp Lp^T (lower part)
+    const int c0 = j0 + jb;
+    const int nt = (m - c0 + kTile - 1) / kTile;
+    const int tx = tid & 15, ty = tid >> 4;
+    for (int tj = 0; tj < nt; tj++) {
+      for (int ti = tj; ti < nt; ti++) {
+        const int r0 = c0 + ti * kTile, cc0 = c0 + tj * kTile;
+        for (int q = tid; q < kNB * kTile; q += kMfThreads) {
+          int t = q / kTile, r = q % kTile;
+          T a = T(0), b = T(0);
+          if (t < jb) {
+            if (r0 + r < m) a = F[(int64_t)(j0 + t) * m + r0 + r];
+            if (cc0 + r < m) b = F[(int64_t)(j0 + t) * m + cc0 + r];
+          }
+          As[t][r] = a;
+          Bs[t][r] = b;
+        }
+        __syncthreads();
+        T acc[4][4];
+#pragma unroll
+        for (int a = 0; a < 4; a++)
+#pragma unroll
+          for (int b = 0; b < 4; b++) acc[a][b] = T(0);
+        for (int t = 0; t < jb; t++) {
+          T ra[4], rb[4];
+#pragma unroll
+          for (int a = 0; a < 4; a++) ra[a] = As[t][tx + 16 * a];
+#pragma unroll
+          for (int b = 0; b < 4; b++) rb[b] = Bs[t][ty + 16 * b];
+#pragma unroll
+          for (int a = 0; a < 4; a++)
+#pragma unroll
+            for (int b = 0; b < 4; b++) acc[a][b] += ra[a] * rb[b];
+        }
+#pragma unroll
+        for (int b = 0; b < 4; b++) {
+          const int col = cc0 + ty + 16 * b;
+          if (col >= m) continue;
+#pragma unroll
+          for (int a = 0; a < 4; a++) {
+            const int row = r0 + tx + 16 * a;
+            if (row < m && row >= col) F[(int64_t)col * m + row] -= acc[a][b];
+          }
+        }
+        __syncthreads();
+      }
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// multifrontal solves
+// ---------------------------------------------------------------------------
+// forward: gather the right-hand side of the pivots, add the children's update
+// vectors, solve with L11, leave L21-updated tail as this front's update vector
+template <typename T>
+__global__ void __launch_bounds__(kMfThreads)
+mf_fwd_level(MfView v, const int *__restrict__ fronts, const T *__restrict__ arena,
+             T *__restrict__ xl, T *__restrict__ uvec, T *__restrict__ wv) {
+  const int f = fronts[blockIdx.x];
+  const int m = v.f_m[f], k = v.f_k[f];
+  const T *F = arena + v.f_off[f];
+  T *w = wv + v.f_woff[f];
+  T *x = xl + v.f_xoff[f] + v.f_p0[f];
+  const int tid = threadIdx.x;
+  for (int i = tid; i < m; i += kMfThreads) w[i] = i < k ? x[i] : T(0);
+  __syncthreads();
+  for (int ci = v.f_child_ptr[f]; ci < v.f_child_ptr[f + 1]; ci++) {
+    const int c = v.f_children[ci];
+    const int rc = v.f_m[c] - v.f_k[c];
+    const int *rel = v.relmap + v.f_relmap[c];
+    const T *u = uvec + v.f_uoff[c];
+    for (int a = tid; a < rc; a += kMfThreads) w[rel[a]] += u[a];
+    __syncthreads();
+  }
+  for (int j = 0; j < k; j++) {
+    const T yj = w[j] / F[(int64_t)j * m + j];
+    __syncthreads();
+    for (int i = j + 1 + tid; i < m; i += kMfThreads) w[i] -= F[(int64_t)j * m + i] * yj;
+    if (tid == 0) w[j] = yj;
+    __syncthreads();
+  }
+  for (int i = tid; i < k; i += kMfThreads) x[i] = w[i];
+  T *u = uvec + v.f_uoff[f];
+  for (int a = tid; a < m - k; a += kMfThreads) u[a] = w[k + a];
+}
+
+// backward: x_piv = L11^-T (y - L21^T x_rows)
+template <typename T>
+__global__ void __launch_bounds__(kMfThreads)
+mf_bwd_level(MfView v, const int *__restrict__ fronts, const T *__restrict__ arena,
+             T *__restrict__ xl, T *__restrict__ wv) {
+  const int f = fronts[blockIdx.x];
+  const int m = v.f_m[f], k = v.f_k[f];
+  const T *F = arena + v.f_off[f];
+  T *w = wv + v.f_woff[f];
+  T *xb = xl + v.f_xoff[f];
+  const int *rows = v.rows + v.f_rows[f];
+  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5, nw = kMfThreads / 32;
+  for (int i = tid; i < m; i += kMfThreads) w[i] = xb[rows[i]];
+  __syncthreads();
+  // contributions of the already solved update rows
+  for (int j = wid; j < k; j += nw) {
+    double s = 0.0;
+    for (int i = k + lane; i < m; i += 32) s += (double)(F[(int64_t)j * m + i] * w[i]);
+    s = warp_sum(s);
+    if (lane == 0) w[j] -= (T)s;
+  }
+  __syncthreads();
+  if (wid == 0) {
+    for (int j = k - 1; j >= 0; j--) {
+      double s = 0.0;
+      for (int i = j + 1 + lane; i < k; i += 32) s += (double)(F[(int64_t)j * m + i] * w[i]);
+      s = warp_sum(s);
+      if (lane == 0) w[j] = (w[j] - (T)s) / F[(int64_t)j * m + j];
+      __syncwarp();
+    }
+  }
+  __syncthreads();
+  for (int i = tid; i < k; i += kMfThreads) xb[rows[i]] = w[i];
+}
+
+// ---------------------------------------------------------------------------
+// Schwarz gather / pull sum and coarse transfer
+// ---------------------------------------------------------------------------
+template <typename T>
+__global__ void gather_subdomains(const double *__restrict__ r, const int *__restrict__ gidx,
+                                  T *__restrict__ xl, int64_t len) {
+  for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < len;
+       p += (int64_t)gridDim.x * blockDim.x)
+    xl[p] = (T)r[gidx[p]];
+}
+
+// crhs (in the coarse batch's local numbering) = R r
+template <typename TR>
+__global__ void restrict_to_coarse(const int64_t *__restrict__ Rp, const int *__restrict__ Rc,
+                                   const TR *__restrict__ Rv, const double *__restrict__ r,
+                                   const int *__restrict__ cpos, double *__restrict__ xc, int nc) {
+  const int lane = threadIdx.x & 31;
+  const int warps = (gridDim.x * blockDim.x) >> 5;
+  for (int a = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; a < nc; a += warps) {
+    double s = 0.0;
+    for (int64_t e = Rp[a] + lane; e < Rp[a + 1]; e += 32) s += (double)Rv[e] * r[Rc[e]];
+    s = warp_sum(s);
+    if (lane == 0) xc[cpos[a]] = s;
+  }
+}
+
+// z_g = (sum of subdomain solutions at g, in subdomain order) + (P csol)_g ;
+// partial sums of r.z (and of r.z_old for the flexible variant)
+template <typename T, typename TP>
+__global__ void __launch_bounds__(kVecThreads)
+pull_prolong_dot(int n, const int64_t *__restrict__ pull_ptr, const int64_t *__restrict__ pull_idx,
+                 const T *__restrict__ xl, const int64_t *__restrict__ Pp, const int *__restrict__ Pc,
+                 const TP *__restrict__ Pv, const double *__restrict__ xc, const int *__restrict__ cpos,
+                 int mode, const double *__restrict__ r, double *__restrict__ z,
+                 double *__restrict__ zold, double *__restrict__ part_rz, double *__restrict__ part_rzo) {
+  // mode bit 0: fine subdomains on; bit 1: coarse on; bit 2: identity fine (z=r);
+  // bit 3: keep z_old and produce r.z_old
+  __shared__ double sh[32];
+  double srz = 0.0, srzo = 0.0;
+  for (int g = blockIdx.x * kVecThreads + threadIdx.x; g < n; g += gridDim.x * kVecThreads) {
+    double s = 0.0;
+    if (mode & 4) {
+      s = r[g];
+    } else if (mode & 1) {
+      for (int64_t q = pull_ptr[g]; q < pull_ptr[g + 1]; q++) s = s + (double)xl[pull_idx[q]];
+    }
+    if (mode & 2) {
+      TP t = TP(0);
+      for (int64_t e = Pp[g]; e < Pp[g + 1]; e++) t = t + Pv[e] * (TP)xc[cpos[Pc[e]]];
+      s = s + (double)t;
+    }
+    const double rg = r[g];
+    if (mode & 8) {
+      const double zo = zold[g];
+      srzo += rg * zo;
+      zold[g] = s;
+    }
+    z[g] = s;
+    srz += rg * s;
+  }
+  double b = block_sum<kVecThreads>(srz, sh);
+  if (threadIdx.x == 0) part_rz[blockIdx.x] = b;
+  if (mode & 8) {
+    b = block_sum<kVecThreads>(srzo, sh);
+    if (threadIdx.x == 0) part_rzo[blockIdx.x] = b;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// CG steps.  sc[] holds device scalars:
+//   0 rho_prev, 1 rho, 2 alpha, 3 res_norm (r.r), 4 init_norm, 5 beta, 6 p.q
+// ---------------------------------------------------------------------------
+enum { SC_RHO_PREV = 0, SC_RHO = 1, SC_ALPHA = 2, SC_RES = 3, SC_INIT = 4, SC_BETA = 5, SC_PQ = 6 };
+
+// beta of the iteration from the r.z partials: Fletcher-Reeves (DOUG) or
+// flexible Polak-Ribiere
+__device__ __forceinline__ double cg_beta(const double *part_rz, const double *part_rzo,
+                                          const double *sc, int first, int flexible, double *rho_out) {
+  const double rho = sum_partials(part_rz);
+  *rho_out = rho;
+  if (first) return 0.0;
+  if (flexible) {
+    const double rzo = sum_partials(part_rzo);
+    return __ddiv_rn(__dsub_rn(rho, rzo), sc[SC_RHO_PREV]);
+  }
+  return __ddiv_rn(rho, sc[SC_RHO_PREV]);
+}
+
+// q = A (z + beta p) with LANES lanes per row; partial sums of (z+beta p).q
+template <int LANES>
+__global__ void __launch_bounds__(kVecThreads)
+spmv_dir(int n, const int64_t *__restrict__ Ap, const int *__restrict__ Ac, const double *__restrict__ Av,
+         const double *__restrict__ z, const double *__restrict__ p, double *__restrict__ q,
+         const double *__restrict__ part_rz, const double *__restrict__ part_rzo, double *__restrict__ sc,
+         int first, int flexible, double *__restrict__ part_pq) {
+  __shared__ double sh[32];
+  __shared__ double s_beta;
+  if (threadIdx.x < 32) {
+    double rho;
+    double beta = cg_beta(part_rz, part_rzo, sc, first, flexible, &rho);
+    if (threadIdx.x == 0) {
+      s_beta = beta;
+      if (blockIdx.x == 0) { sc[SC_RHO] = rho; sc[SC_BETA] = beta; }
+    }
+  }
+  __syncthreads();
+  const double beta = s_beta;
+  const int sub = threadIdx.x % LANES;
+  const int rows_per_block = kVecThreads / LANES;
+  double spq = 0.0;
+  for (int row0 = blockIdx.x * rows_per_block; row0 < n; row0 += gridDim.x * rows_per_block) {
+    const int i = row0 + threadIdx.x / LANES;
+    double s = 0.0;
+    if (i < n) {
+      for (int64_t e = Ap[i] + sub; e < Ap[i + 1]; e += LANES) {
+        const int j = Ac[e];
+        const double pj = first ? z[j] : __dadd_rn(z[j], __dmul_rn(beta, p[j]));
+        s = __fma_rn(Av[e], pj, s);
+      }
+    }
+#pragma unroll
+    for (int o = LANES / 2; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o, LANES);
+    if (i < n && sub == 0) {
+      q[i] = s;
+      const double pi = first ? z[i] : __dadd_rn(z[i], __dmul_rn(beta, p[i]));
+      spq += pi * s;
+    }
+  }
+  double b = block_sum<kVecThreads>(spq, sh);
+  if (threadIdx.x == 0) part_pq[blockIdx.x] = b;
+}
+
+// p = z + beta p; x += alpha p; r -= alpha q; partial r.r
+__global__ void __launch_bounds__(kVecThreads)
+cg_update(int n, const double *__restrict__ z, double *__restrict__ p, const double *__restrict__ q,
+          double *__restrict__ x, double *__restrict__ r, double *__restrict__ sc,
+          const double *__restrict__ part_pq, int first, double *__restrict__ part_rr) {
+  __shared__ double sh[32];
+  __shared__ double s_alpha;
+  if (threadIdx.x < 32) {
+    const double pq = sum_partials(part_pq);
+    if (threadIdx.x == 0) {
+      const double alpha = __ddiv_rn(sc[SC_RHO], pq);
+      s_alpha = alpha;
+      if (blockIdx.x == 0) { sc[SC_ALPHA] = alpha; sc[SC_PQ] = pq; }
+    }
+  }
+  __syncthreads();
+  const double alpha = s_alpha, beta = sc[SC_BETA];
+  double srr = 0.0;
+  for (int i = blockIdx.x * kVecThreads + threadIdx.x; i < n; i += gridDim.x * kVecThreads) {
+    const double pi = first ? z[i] : __dadd_rn(z[i], __dmul_rn(beta, p[i]));
+    p[i] = pi;
+    x[i] = __dadd_rn(x[i], __dmul_rn(alpha, pi));
+    const double ri = __dsub_rn(r[i], __dmul_rn(alpha, q[i]));
+    r[i] = ri;
+    srr += ri * ri;
+  }
+  double b = block_sum<kVecThreads>(srr, sh);
+  if (threadIdx.x == 0) part_rr[blockIdx.x] = b;
+}
+
+// r = b - A x (FP64 true residual), partial r.r
+template <int LANES>
+__global__ void __launch_bounds__(kVecThreads)
+residual(int n, const int64_t *__restrict__ Ap, const int *__restrict__ Ac, const double *__restrict__ Av,
+         const double *__restrict__ x, const double *__restrict__ b, double *__restrict__ r,
+         double *__restrict__ part_rr) {
+  __shared__ double sh[32];
+  const int sub = threadIdx.x % LANES;
+  const int rows_per_block = kVecThreads / LANES;
+  double srr = 0.0;
+  for (int row0 = blockIdx.x * rows_per_block; row0 < n; row0 += gridDim.x * rows_per_block) {
+    const int i = row0 + threadIdx.x / LANES;
+    double s = 0.0;
+    if (i < n)
+      for (int64_t e = Ap[i] + sub; e < Ap[i + 1]; e += LANES) s = __fma_rn(Av[e], x[Ac[e]], s);
+#pragma unroll
+    for (int o = LANES / 2; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o, LANES);
+    if (i < n && sub == 0) {
+      const double ri = __dsub_rn(b[i], s);
+      r[i] = ri;
+      srr += ri * ri;
+    }
+  }
+  double t = block_sum<kVecThreads>(srr, sh);
+  if (threadIdx.x == 0) part_rr[blockIdx.x] = t;
+}
+
+// finish an iteration: res = sum(part_rr); rho_prev = rho; publish to host
+__global__ void cg_finish(double *__restrict__ sc, const double *__restrict__ part_rr, int init,
+                          volatile double *__restrict__ host_out, const int *__restrict__ status,
+                          volatile int *__restrict__ host_status) {
+  if (threadIdx.x < 32) {
+    const double rr = sum_partials(part_rr);
+    if (threadIdx.x == 0) {
+      // init: 1 = initial residual, 0 = end of an iteration, 2 = report only
+      if (init == 1) sc[SC_INIT] = rr;
+      else if (init == 0) { sc[SC_RES] = rr; sc[SC_RHO_PREV] = sc[SC_RHO]; }
+      host_out[0] = rr;
+      host_out[1] = sc[SC_INIT];
+      host_out[2] = sc[SC_ALPHA];
+      host_out[3] = sc[SC_BETA];
+      host_out[4] = sc[SC_RHO];
+      host_out[5] = sc[SC_PQ];
+      *host_status = *status;
+    }
+  }
+}
+
+}  // namespace dg

@@ -1,0 +1,680 @@
+// GB300 solve path: device data, numeric factorisation and the PCG loop,
+// behind the C ABI of include/doug_gpu.h.
+//
+// Layout in HBM (one handle):
+//   fine matrix A           CSR (int64 row pointers, int32 columns, FP64 values)
+//   PCG vectors             x, r, p, q, z, z_old, b  (FP64, n each)
+//   subdomain batch         front arena (T), local vectors xl (T), update and
+//                           work vectors (T); T = double (plain) or float (mixed)
+//   coarse batch            same structures in FP64 for the coarse matrix
+//   transfer                R (nagr x n) and P = R^T (n x nagr) in CSR
+//   reductions              kRedBlocks partials per dot product + 8 scalars
+// Nothing is allocated after dg_setup; a solve only launches kernels.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "../../include/doug_gpu.h"
+#include "dg_kernels.cuh"
+#include "host/mf_symbolic.hpp"
+#include "host/setup.hpp"
+
+namespace dg {
+
+struct CudaError {
+  cudaError_t e;
+  const char *what;
+};
+#define CK(call)                                                     \
+  do {                                                               \
+    cudaError_t _e = (call);                                         \
+    if (_e != cudaSuccess) throw CudaError{_e, #call};               \
+  } while (0)
+
+template <typename T>
+struct DBuf {
+  T *p = nullptr;
+  size_t n = 0;
+  DBuf() = default;
+  DBuf(const DBuf &) = delete;
+  DBuf &operator=(const DBuf &) = delete;
+  ~DBuf() { if (p) cudaFree(p); }
+  void alloc(size_t count) {
+    if (p) { cudaFree(p); p = nullptr; }
+    n = count;
+    CK(cudaMalloc(&p, std::max<size_t>(count, 1) * sizeof(T)));
+  }
+  void upload(const std::vector<T> &v) {
+    alloc(v.size());
+    if (!v.empty()) CK(cudaMemcpy(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice));
+  }
+};
+
+static double wall() {
+  return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
+// one multifrontal batch on the device, factor precision T
+template <typename T>
+struct MfDevice {
+  DBuf<int64_t> f_off, f_rows, f_xoff, f_uoff, f_woff, f_relmap, f_asm, asm_tgt, asm_sp, asm_src;
+  DBuf<int> f_m, f_k, f_p0, f_child_ptr, f_children, rows, relmap, lvl_fronts, gidx;
+  DBuf<T> arena, xl, u, w;
+  std::vector<int> lvl_ptr;
+  int nlevels = 0, nfronts = 0;
+  int64_t xlen = 0;
+  MfView view{};
+
+  void upload(const MfBatch &B) {
+    f_off.upload(B.f_off); f_rows.upload(B.f_rows); f_xoff.upload(B.f_xoff);
+    f_uoff.upload(B.f_uoff); f_woff.upload(B.f_woff); f_relmap.upload(B.f_relmap);
+    f_asm.upload(B.f_asm); asm_tgt.upload(B.asm_tgt); asm_sp.upload(B.asm_sp);
+    asm_src.upload(B.asm_src);
+    f_m.upload(B.f_m); f_k.upload(B.f_k); f_p0.upload(B.f_p0);
+    f_child_ptr.upload(B.f_child_ptr); f_children.upload(B.f_children);
+    rows.upload(B.rows); relmap.upload(B.relmap); lvl_fronts.upload(B.lvl_fronts);
+    gidx.upload(B.gidx);
+    arena.alloc((size_t)B.arena);
+    xl.alloc((size_t)B.xlen);
+    u.alloc((size_t)std::max<int64_t>(B.ulen, 1));
+    w.alloc((size_t)std::max<int64_t>(B.wlen, 1));
+    lvl_ptr = B.lvl_ptr;
+    nlevels = B.nlevels;
+    nfronts = B.nfronts;
+    xlen = B.xlen;
+    view = MfView{f_off.p, f_m.p, f_k.p, f_rows.p, f_xoff.p, f_p0.p, f_uoff.p, f_woff.p,
+                  f_child_ptr.p, f_children.p, f_relmap.p, f_asm.p, rows.p, relmap.p,
+                  asm_tgt.p, asm_sp.p, asm_src.p};
+  }
+
+  int factor(const double *vals, int *status, cudaStream_t s) {
+    int launches = 0;
+    for (int l = 0; l < nlevels; l++) {
+      int nf = lvl_ptr[(size_t)l + 1] - lvl_ptr[(size_t)l];
+      if (!nf) continue;
+      mf_factor_level<T><<<nf, kMfThreads, 0, s>>>(view, lvl_fronts.p + lvl_ptr[(size_t)l], vals,
+                                                    arena.p, status);
+      launches++;
+    }
+    return launches;
+  }
+
+  int solve(cudaStream_t s) {  // in place on xl
+    int launches = 0;
+    for (int l = 0; l < nlevels; l++) {
+      int nf = lvl_ptr[(size_t)l + 1] - lvl_ptr[(size_t)l];
+      if (!nf) continue;
+      mf_fwd_level<T><<<nf, kMfThreads, 0, s>>>(view, lvl_fronts.p + lvl_ptr[(size_t)l], arena.p,
+                                                 xl.p, u.p, w.p);
+      launches++;
+    }
+    for (int l = nlevels - 1; l >= 0; l--) {
+      int nf = lvl_ptr[(size_t)l + 1] - lvl_ptr[(size_t)l];
+      if (!nf) continue;
+      mf_bwd_level<T><<<nf, kMfThreads, 0, s>>>(view, lvl_fronts.p + lvl_ptr[(size_t)l], arena.p,
+                                                 xl.p, w.p);
+      launches++;
+    }
+    return launches;
+  }
+};
+
+}  // namespace dg
+
+using namespace dg;
+
+struct dg_handle {
+  Controls ctl;
+  std::string ctl_text;           // words given through dg_set_option (applied first)
+  std::string ctl_dir = ".";
+  std::string err;
+  int n = 0;
+  std::vector<int> ii, jj;
+  std::vector<double> vv, rhs;
+  bool have_matrix = false, have_rhs = false, ready = false;
+  std::vector<int> part;
+  int nparts = 0;
+  SetupResult S;
+  MfBatch Bsub, Bco;
+  double t_setup = 0;
+  int precision = 0;
+  int lanes = 8;
+  // device
+  int device = 0;
+  DBuf<int64_t> Ap, Rp, Pp, pull_ptr, pull_idx;
+  DBuf<int> Ac, Rc, Pc, cpos, status;
+  DBuf<double> Av, ACv, Rv, Pv, b, x, r, p, q, z, zold, xc_dummy;
+  DBuf<float> Rvf, Pvf;
+  DBuf<double> part_rz, part_rzo, part_pq, part_rr, sc;
+  std::unique_ptr<MfDevice<double>> sub64, co64;
+  std::unique_ptr<MfDevice<float>> sub32;
+  double *host_out = nullptr;     // mapped pinned
+  int *host_status = nullptr;
+  double *d_host_out = nullptr;
+  int *d_host_status = nullptr;
+  cudaEvent_t ev[4]{};
+  ~dg_handle() {
+    if (host_out) cudaFreeHost(host_out);
+    if (host_status) cudaFreeHost(host_status);
+    for (auto &e : ev) if (e) cudaEventDestroy(e);
+  }
+};
+
+namespace {
+
+dg_status fail(dg_handle *h, dg_status s, const std::string &msg) {
+  h->err = msg;
+  return s;
+}
+
+dg_status cuda_fail(dg_handle *h, const CudaError &e) {
+  h->err = std::string("CUDA error in ") + e.what + ": " + cudaGetErrorString(e.e);
+  return DG_CUDA_ERROR;
+}
+
+// host Lanczos eigenvalue range of the CG tridiagonal (pcg.F90:465-491):
+// bisection with Sturm counts, an independent method from the reference's QL
+double tridiag_cond(const std::vector<double> &alpha, const std::vector<double> &beta) {
+  int it = (int)alpha.size();
+  if (it < 1) return 0.0;
+  std::vector<double> d((size_t)it), e((size_t)it, 0.0);
+  d[0] = 1.0 / alpha[0];
+  for (int i = 1; i < it; i++) {
+    if (alpha[(size_t)i] == 0 || beta[(size_t)i] < 0) return 0.0;
+    d[(size_t)i] = 1.0 / alpha[(size_t)i] + beta[(size_t)i] / alpha[(size_t)i - 1];
+    e[(size_t)i] = -std::sqrt(beta[(size_t)i]) / alpha[(size_t)i - 1];
+  }
+  double lo = 1e300, hi = -1e300;
+  for (int i = 0; i < it; i++) {
+    double rr = (i > 0 ? std::fabs(e[(size_t)i]) : 0) + (i + 1 < it ? std::fabs(e[(size_t)i + 1]) : 0);
+    lo = std::min(lo, d[(size_t)i] - rr);
+    hi = std::max(hi, d[(size_t)i] + rr);
+  }
+  auto count_below = [&](double xv) {  // eigenvalues < xv
+    int c = 0;
+    double q = d[0] - xv;
+    if (q < 0) c++;
+    for (int i = 1; i < it; i++) {
+      if (q == 0) q = 1e-300;
+      q = d[(size_t)i] - xv - e[(size_t)i] * e[(size_t)i] / q;
+      if (q < 0) c++;
+    }
+    return c;
+  };
+  auto kth = [&](int kidx) {  // kidx-th smallest (0-based)
+    double a = lo, b = hi;
+    for (int t = 0; t < 200; t++) {
+      double mid = 0.5 * (a + b);
+      if (count_below(mid) > kidx) b = mid; else a = mid;
+    }
+    return 0.5 * (a + b);
+  };
+  double lmin = kth(0), lmax = kth(it - 1);
+  return lmin != 0 ? lmax / lmin : 0.0;
+}
+
+int lanes_for(const Csr &A) {
+  double avg = A.nrows ? (double)A.nnz() / A.nrows : 1;
+  if (avg <= 3) return 2;
+  if (avg <= 6) return 4;
+  if (avg <= 12) return 8;
+  if (avg <= 24) return 16;
+  return 32;
+}
+
+template <int L>
+void launch_spmv(int grid, cudaStream_t s, dg_handle *h, int first, int flexible) {
+  spmv_dir<L><<<grid, kVecThreads, 0, s>>>(h->n, h->Ap.p, h->Ac.p, h->Av.p, h->z.p, h->p.p, h->q.p,
+                                            h->part_rz.p, h->part_rzo.p, h->sc.p, first, flexible,
+                                            h->part_pq.p);
+}
+template <int L>
+void launch_resid(int grid, cudaStream_t s, dg_handle *h, const double *xx, const double *bb, double *rr) {
+  residual<L><<<grid, kVecThreads, 0, s>>>(h->n, h->Ap.p, h->Ac.p, h->Av.p, xx, bb, rr, h->part_rr.p);
+}
+void spmv_any(int lanes, int grid, cudaStream_t s, dg_handle *h, int first, int flexible) {
+  switch (lanes) {
+    case 2: launch_spmv<2>(grid, s, h, first, flexible); break;
+    case 4: launch_spmv<4>(grid, s, h, first, flexible); break;
+    case 8: launch_spmv<8>(grid, s, h, first, flexible); break;
+    case 16: launch_spmv<16>(grid, s, h, first, flexible); break;
+    default: launch_spmv<32>(grid, s, h, first, flexible); break;
+  }
+}
+void resid_any(int lanes, int grid, cudaStream_t s, dg_handle *h, const double *xx, const double *bb, double *rr) {
+  switch (lanes) {
+    case 2: launch_resid<2>(grid, s, h, xx, bb, rr); break;
+    case 4: launch_resid<4>(grid, s, h, xx, bb, rr); break;
+    case 8: launch_resid<8>(grid, s, h, xx, bb, rr); break;
+    case 16: launch_resid<16>(grid, s, h, xx, bb, rr); break;
+    default: launch_resid<32>(grid, s, h, xx, bb, rr); break;
+  }
+}
+
+dg_status do_setup(dg_handle *h) {
+  if (!h->have_matrix) return fail(h, DG_NOT_READY, "no matrix: call dg_set_matrix_coo or dg_load_ctl first");
+  std::string err;
+  Controls c = h->ctl;
+  ctl_finish(c);
+  double t0 = wall();
+  if (!build_setup(c, h->n, h->ii, h->jj, h->vv, h->part.empty() ? nullptr : &h->part, h->nparts, h->S, err))
+    return fail(h, DG_BAD_INPUT, err);
+  MfOptions mo;
+  try {
+    if (c.fine_method == 1) mf_build_subdomains(h->S.A, h->S.sd_ptr, h->S.sd_nodes, mo, h->Bsub);
+    if (c.levels > 1) mf_build_single(h->S.AC, mo, h->Bco);
+  } catch (const std::exception &ex) {
+    return fail(h, DG_BAD_INPUT, std::string("symbolic analysis failed: ") + ex.what());
+  }
+  h->t_setup = wall() - t0;
+  h->precision = c.precision;
+  // device upload
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)
+    return fail(h, DG_NO_DEVICE, "no CUDA device is visible; the solver has no CPU fallback");
+  try {
+    CK(cudaGetDevice(&h->device));
+    const SetupResult &S = h->S;
+    int n = h->n;
+    h->Ap.upload(S.A.ptr); h->Ac.upload(S.A.col); h->Av.upload(S.A.val);
+    h->lanes = lanes_for(S.A);
+    for (auto *v : {&h->b, &h->x, &h->r, &h->p, &h->q, &h->z, &h->zold}) v->alloc((size_t)n);
+    for (auto *v : {&h->part_rz, &h->part_rzo, &h->part_pq, &h->part_rr}) {
+      v->alloc(kRedBlocks);
+      CK(cudaMemset(v->p, 0, kRedBlocks * sizeof(double)));
+    }
+    h->sc.alloc(8);
+    CK(cudaMemset(h->sc.p, 0, 8 * sizeof(double)));
+    h->status.alloc(1);
+    CK(cudaMemset(h->status.p, 0, sizeof(int)));
+    if (!h->host_out) {
+      CK(cudaHostAlloc(&h->host_out, 16 * sizeof(double), cudaHostAllocMapped));
+      CK(cudaHostAlloc(&h->host_status, sizeof(int), cudaHostAllocMapped));
+      CK(cudaHostGetDevicePointer(&h->d_host_out, h->host_out, 0));
+      CK(cudaHostGetDevicePointer(&h->d_host_status, h->host_status, 0));
+      for (auto &e : h->ev) CK(cudaEventCreate(&e));
+    }
+    // transfer operators
+    h->Rp.upload(S.R.ptr); h->Rc.upload(S.R.col); h->Rv.upload(S.R.val);
+    h->Pp.upload(S.P.ptr); h->Pc.upload(S.P.col); h->Pv.upload(S.P.val);
+    std::vector<float> rf(S.R.val.begin(), S.R.val.end()), pf(S.P.val.begin(), S.P.val.end());
+    h->Rvf.upload(rf); h->Pvf.upload(pf);
+    h->ACv.upload(S.AC.val);
+    // subdomain batch
+    h->sub64.reset(); h->sub32.reset(); h->co64.reset();
+    if (c.fine_method == 1) {
+      if (h->precision == 1) { h->sub32.reset(new MfDevice<float>()); h->sub32->upload(h->Bsub); }
+      else { h->sub64.reset(new MfDevice<double>()); h->sub64->upload(h->Bsub); }
+      // pull lists: subdomain arena positions of every node, subdomain order
+      std::vector<int64_t> pp((size_t)n + 1, 0);
+      for (int g : h->Bsub.gidx) pp[(size_t)g + 1]++;
+      for (int i = 0; i < n; i++) pp[(size_t)i + 1] += pp[(size_t)i];
+      std::vector<int64_t> idx((size_t)pp[(size_t)n]);
+      std::vector<int64_t> fill(pp.begin(), pp.end() - 1);
+      for (int64_t q = 0; q < (int64_t)h->Bsub.gidx.size(); q++)
+        idx[(size_t)fill[(size_t)h->Bsub.gidx[(size_t)q]]++] = q;
+      h->pull_ptr.upload(pp);
+      h->pull_idx.upload(idx);
+    } else {
+      h->pull_ptr.alloc(1); h->pull_idx.alloc(1);
+    }
+    if (c.levels > 1) {
+      h->co64.reset(new MfDevice<double>());
+      h->co64->upload(h->Bco);
+      std::vector<int> cp((size_t)S.AC.nrows, 0);
+      for (int64_t q = 0; q < (int64_t)h->Bco.gidx.size(); q++) cp[(size_t)h->Bco.gidx[(size_t)q]] = (int)q;
+      h->cpos.upload(cp);
+    } else {
+      h->cpos.alloc(1);
+    }
+    CK(cudaDeviceSynchronize());
+  } catch (const CudaError &e) {
+    return cuda_fail(h, e);
+  }
+  h->ready = true;
+  return DG_OK;
+}
+
+// the solve: numeric factorisation + PCG (pcg_weigs, pcg.F90:289-462)
+dg_status do_solve(dg_handle *h, const double *d_b, double *d_x, dg_stats *st, cudaStream_t s) {
+  if (!h->ready) return fail(h, DG_NOT_READY, "dg_setup has not run");
+  Controls c = h->ctl;
+  ctl_finish(c);
+  const int n = h->n;
+  const int grid = kRedBlocks;
+  const bool fine = c.fine_method == 1 && c.method != 0;
+  const bool coarse = c.levels > 1 && c.method != 0;
+  const bool mixed = h->precision == 1;
+  int launches = 0;
+  dg_stats out{};
+  out.n = n;
+  out.nsubdomains = (int)h->S.sd_ptr.size() - 1;
+  out.ncoarse = h->S.AC.nrows;
+  out.factor_nnz = h->Bsub.factor_nnz;
+  out.factor_gflop = h->Bsub.factor_flops * 1e-9;
+  out.t_setup_s = h->t_setup;
+  try {
+    CK(cudaMemsetAsync(h->status.p, 0, sizeof(int), s));
+    CK(cudaEventRecord(h->ev[0], s));
+    // numeric factorisations (the reference factorises lazily in the first
+    // preconditioner call, subsolvers.F90:78-101, pcg.F90:166-178)
+    if (fine) launches += mixed ? h->sub32->factor(h->Av.p, h->status.p, s) : h->sub64->factor(h->Av.p, h->status.p, s);
+    if (coarse) launches += h->co64->factor(h->ACv.p, h->status.p, s);
+    CK(cudaEventRecord(h->ev[1], s));
+    CK(cudaMemcpyAsync(h->b.p, d_b, (size_t)n * sizeof(double), cudaMemcpyDeviceToDevice, s));
+    CK(cudaMemsetAsync(h->x.p, 0, (size_t)n * sizeof(double), s));
+    CK(cudaMemsetAsync(h->p.p, 0, (size_t)n * sizeof(double), s));
+    CK(cudaMemsetAsync(h->zold.p, 0, (size_t)n * sizeof(double), s));
+    // r = b - A x0, init_norm = r.r
+    resid_any(h->lanes, grid, s, h, h->x.p, h->b.p, h->r.p);
+    cg_finish<<<1, 32, 0, s>>>(h->sc.p, h->part_rr.p, 1, h->d_host_out, h->status.p, h->d_host_status);
+    launches += 2;
+    CK(cudaStreamSynchronize(s));
+    if (*h->host_status & ERR_NOT_SPD)
+      return fail(h, DG_SINGULAR, "a subdomain or coarse matrix is not positive definite");
+    double init = h->host_out[0];
+    if (init == 0.0) {
+      init = 1.0;
+      double one = 1.0;
+      CK(cudaMemcpy(h->sc.p + SC_INIT, &one, sizeof(double), cudaMemcpyHostToDevice));
+    }
+    out.init_norm = std::sqrt(init);
+    const double tol = c.solve_tolerance;
+    const int maxit = c.solve_maxiters == -1 ? 100000 : c.solve_maxiters;
+    double ratio = 1.0, res = init;
+    int it = 0;
+    std::vector<double> alphas, betas;
+    dg_status rc = DG_OK;
+    int mode = 0;
+    if (c.method == 0) mode |= 4;
+    else if (c.fine_method == 0) mode |= 4;
+    else mode |= 1;
+    if (coarse && c.method == 1) mode |= 2;
+    if (mixed) mode |= 8;
+    // (the reference adds the coarse correction only for method 1, pcg.F90:191-193)
+    while (ratio > tol * tol && it < maxit) {
+      it++;
+      const int first = it == 1;
+      if (fine) {
+        if (mixed) {
+          gather_subdomains<float><<<grid, kVecThreads, 0, s>>>(h->r.p, h->sub32->gidx.p, h->sub32->xl.p, h->sub32->xlen);
+          launches += 1 + h->sub32->solve(s);
+        } else {
+          gather_subdomains<double><<<grid, kVecThreads, 0, s>>>(h->r.p, h->sub64->gidx.p, h->sub64->xl.p, h->sub64->xlen);
+          launches += 1 + h->sub64->solve(s);
+        }
+      }
+      if (coarse) {
+        if (mixed)
+          restrict_to_coarse<float><<<grid, kVecThreads, 0, s>>>(h->Rp.p, h->Rc.p, h->Rvf.p, h->r.p, h->cpos.p, h->co64->xl.p, h->S.R.nrows);
+        else
+          restrict_to_coarse<double><<<grid, kVecThreads, 0, s>>>(h->Rp.p, h->Rc.p, h->Rv.p, h->r.p, h->cpos.p, h->co64->xl.p, h->S.R.nrows);
+        launches += 1 + h->co64->solve(s);
+      }
+      const double *xc = coarse ? h->co64->xl.p : nullptr;
+      if (mixed)
+        pull_prolong_dot<float, float><<<grid, kVecThreads, 0, s>>>(
+            n, h->pull_ptr.p, h->pull_idx.p, fine ? h->sub32->xl.p : nullptr, h->Pp.p, h->Pc.p, h->Pvf.p, xc,
+            h->cpos.p, mode, h->r.p, h->z.p, h->zold.p, h->part_rz.p, h->part_rzo.p);
+      else
+        pull_prolong_dot<double, double><<<grid, kVecThreads, 0, s>>>(
+            n, h->pull_ptr.p, h->pull_idx.p, fine ? h->sub64->xl.p : nullptr, h->Pp.p, h->Pc.p, h->Pv.p, xc,
+            h->cpos.p, mode, h->r.p, h->z.p, h->zold.p, h->part_rz.p, h->part_rzo.p);
+      spmv_any(h->lanes, grid, s, h, first, mixed ? 1 : 0);
+      cg_update<<<grid, kVecThreads, 0, s>>>(n, h->z.p, h->p.p, h->q.p, h->x.p, h->r.p, h->sc.p, h->part_pq.p, first,
+                                             h->part_rr.p);
+      launches += 3;
+      if (mixed && c.replace_every > 0 && it % c.replace_every == 0) {
+        // FP64 residual replacement: r = b - A x
+        resid_any(h->lanes, grid, s, h, h->x.p, h->b.p, h->r.p);
+        launches++;
+      }
+      cg_finish<<<1, 32, 0, s>>>(h->sc.p, h->part_rr.p, 0, h->d_host_out, h->status.p, h->d_host_status);
+      launches++;
+      CK(cudaStreamSynchronize(s));
+      res = h->host_out[0];
+      double alpha = h->host_out[2], beta = h->host_out[3], pq = h->host_out[5];
+      alphas.push_back(alpha);
+      betas.push_back(beta);
+      if (!(pq > 0.0) || std::isnan(res)) { rc = DG_BREAKDOWN; h->err = "CG breakdown: p.q <= 0 or NaN"; break; }
+      ratio = res / init;
+      if (mixed && !(ratio > tol * tol)) {
+        // confirm with the true FP64 residual before stopping
+        resid_any(h->lanes, grid, s, h, h->x.p, h->b.p, h->r.p);
+        cg_finish<<<1, 32, 0, s>>>(h->sc.p, h->part_rr.p, 0, h->d_host_out, h->status.p, h->d_host_status);
+        launches += 2;
+        CK(cudaStreamSynchronize(s));
+        res = h->host_out[0];
+        ratio = res / init;
+      }
+    }
+    CK(cudaEventRecord(h->ev[2], s));
+    if (rc == DG_OK && ratio > tol * tol && it >= maxit) rc = DG_NOT_CONVERGED;
+    // true residual for the report (into q, which is free now)
+    resid_any(h->lanes, grid, s, h, h->x.p, h->b.p, h->q.p);
+    cg_finish<<<1, 32, 0, s>>>(h->sc.p, h->part_rr.p, 2, h->d_host_out, h->status.p, h->d_host_status);
+    launches += 2;
+    CK(cudaMemcpyAsync(d_x, h->x.p, (size_t)n * sizeof(double), cudaMemcpyDeviceToDevice, s));
+    CK(cudaStreamSynchronize(s));
+    float ms_f = 0, ms_i = 0;
+    CK(cudaEventElapsedTime(&ms_f, h->ev[0], h->ev[1]));
+    CK(cudaEventElapsedTime(&ms_i, h->ev[1], h->ev[2]));
+    out.iterations = it;
+    out.final_norm = std::sqrt(res);
+    out.true_rel_residual = std::sqrt(h->host_out[0] / init);
+    out.cond_num = tridiag_cond(alphas, betas);
+    out.t_factor_s = ms_f * 1e-3;
+    out.t_iterate_s = ms_i * 1e-3;
+    out.t_total_s = out.t_factor_s + out.t_iterate_s;
+    out.gpu_launches = launches;
+    if (st) *st = out;
+    return rc;
+  } catch (const CudaError &e) {
+    return cuda_fail(h, e);
+  }
+}
+
+std::string dirname_of(const std::string &p) {
+  size_t k = p.find_last_of('/');
+  return k == std::string::npos ? "." : p.substr(0, k);
+}
+std::string resolve(const std::string &dir, const std::string &f) {
+  if (f.empty() || f[0] == '/') return f;
+  return dir + "/" + f;
+}
+
+}  // namespace
+
+extern "C" {
+
+dg_status dg_create(dg_handle **h) {
+  if (!h) return DG_BAD_INPUT;
+  *h = new (std::nothrow) dg_handle();
+  return *h ? DG_OK : DG_BAD_INPUT;
+}
+
+void dg_destroy(dg_handle *h) { delete h; }
+
+const char *dg_last_error(const dg_handle *h) { return h ? h->err.c_str() : "null handle"; }
+
+dg_status dg_set_option(dg_handle *h, const char *name, const char *value) {
+  if (!h || !name || !value) return DG_BAD_INPUT;
+  std::string w1(name), w2(value), err;
+  for (auto &ch : w1) ch = (char)tolower((unsigned char)ch);
+  if (w1 == "precision") {
+    int v;
+    if (!parse_i10(w2, v) || v < 0 || v > 1) return fail(h, DG_BAD_INPUT, "precision must be 0 or 1");
+    h->ctl.precision = v;
+    return DG_OK;
+  }
+  if (w1 == "replace_every") {
+    int v;
+    if (!parse_i10(w2, v)) return fail(h, DG_BAD_INPUT, "bad replace_every");
+    h->ctl.replace_every = v;
+    return DG_OK;
+  }
+  if (w1 == "omega") {
+    char *end = nullptr;
+    double v = strtod(w2.c_str(), &end);
+    if (*end || !(v > 0)) return fail(h, DG_BAD_INPUT, "bad omega");
+    h->ctl.omega = v;
+    return DG_OK;
+  }
+  if (!ctl_apply(h->ctl, w1, w2, err)) return fail(h, DG_BAD_INPUT, err);
+  h->ready = false;
+  return DG_OK;
+}
+
+dg_status dg_load_ctl(dg_handle *h, const char *path) {
+  if (!h || !path) return DG_BAD_INPUT;
+  FILE *f = fopen(path, "rb");
+  if (!f) return fail(h, DG_BAD_INPUT, std::string("Unable to open DOUG control file: ") + path);
+  std::string text;
+  char buf[4096];
+  size_t got;
+  while ((got = fread(buf, 1, sizeof buf, f)) > 0) text.append(buf, got);
+  fclose(f);
+  std::string err;
+  if (!ctl_parse_text(h->ctl, text, err)) return fail(h, DG_BAD_INPUT, err);
+  h->ctl_dir = dirname_of(path);
+  Controls &c = h->ctl;
+  if (c.input_type != 2)
+    return fail(h, DG_BAD_INPUT, "input_type " + std::to_string(c.input_type) +
+                                     ": only assembled input (2) is read from control files so far");
+  std::vector<int> ii, jj;
+  std::vector<double> vv;
+  int n = 0;
+  if (!read_assembled(resolve(h->ctl_dir, c.assembled_mtx_file), c.assembled_mtx_format, n, ii, jj, vv, err))
+    return fail(h, DG_BAD_INPUT, err);
+  dg_status s = dg_set_matrix_coo(h, n, (int)vv.size(), ii.data(), jj.data(), vv.data());
+  if (s != DG_OK) return s;
+  if (!c.assembled_rhs_file.empty()) {
+    std::vector<double> b;
+    if (!read_vector(resolve(h->ctl_dir, c.assembled_rhs_file), c.assembled_rhs_format, n, b, err))
+      return fail(h, DG_BAD_INPUT, err);
+    return dg_set_rhs(h, b.data());
+  }
+  return DG_OK;
+}
+
+dg_status dg_set_matrix_coo(dg_handle *h, int n, int nnz, const int *rows, const int *cols, const double *vals) {
+  if (!h || n <= 0 || nnz <= 0 || !rows || !cols || !vals) return DG_BAD_INPUT;
+  h->n = n;
+  h->ii.assign(rows, rows + nnz);
+  h->jj.assign(cols, cols + nnz);
+  h->vv.assign(vals, vals + nnz);
+  h->have_matrix = true;
+  h->ready = false;
+  if (!h->have_rhs || (int)h->rhs.size() != n) { h->rhs.assign((size_t)n, 1.0); h->have_rhs = false; }
+  return DG_OK;
+}
+
+dg_status dg_set_rhs(dg_handle *h, const double *b) {
+  if (!h || !b || h->n <= 0) return DG_BAD_INPUT;
+  h->rhs.assign(b, b + h->n);
+  h->have_rhs = true;
+  return DG_OK;
+}
+
+dg_status dg_set_partition(dg_handle *h, const int *part, int nparts) {
+  if (!h || !part || nparts <= 0 || h->n <= 0) return DG_BAD_INPUT;
+  for (int i = 0; i < h->n; i++)
+    if (part[i] < 1 || part[i] > nparts) return fail(h, DG_BAD_INPUT, "partition id out of range");
+  h->part.assign(part, part + h->n);
+  h->nparts = nparts;
+  h->ready = false;
+  return DG_OK;
+}
+
+dg_status dg_setup(dg_handle *h) {
+  if (!h) return DG_BAD_INPUT;
+  return do_setup(h);
+}
+
+dg_status dg_solve_device(dg_handle *h, const double *d_b, double *d_x, dg_stats *stats, void *stream) {
+  if (!h || !d_b || !d_x) return DG_BAD_INPUT;
+  return do_solve(h, d_b, d_x, stats, (cudaStream_t)stream);
+}
+
+dg_status dg_solve(dg_handle *h, const double *b, double *x, dg_stats *stats) {
+  if (!h || !x) return DG_BAD_INPUT;
+  if (!h->ready) return fail(h, DG_NOT_READY, "dg_setup has not run");
+  const double *src = b ? b : h->rhs.data();
+  double *db = nullptr, *dx = nullptr;
+  size_t bytes = (size_t)h->n * sizeof(double);
+  if (cudaMalloc(&db, bytes) != cudaSuccess || cudaMalloc(&dx, bytes) != cudaSuccess) {
+    if (db) cudaFree(db);
+    return fail(h, DG_CUDA_ERROR, "cudaMalloc failed for the solve vectors");
+  }
+  dg_status s = DG_OK;
+  if (cudaMemcpy(db, src, bytes, cudaMemcpyHostToDevice) != cudaSuccess) s = fail(h, DG_CUDA_ERROR, "H2D copy failed");
+  if (s == DG_OK) {
+    s = do_solve(h, db, dx, stats, 0);
+    if ((s == DG_OK || s == DG_NOT_CONVERGED) && cudaMemcpy(x, dx, bytes, cudaMemcpyDeviceToHost) != cudaSuccess)
+      s = fail(h, DG_CUDA_ERROR, "D2H copy failed");
+  }
+  cudaFree(db);
+  cudaFree(dx);
+  return s;
+}
+
+dg_status dg_write_solution(dg_handle *h, const double *x) {
+  if (!h || !x) return DG_BAD_INPUT;
+  std::string err;
+  if (h->ctl.solution_file.empty()) return fail(h, DG_BAD_INPUT, "no solution_file in the control words");
+  if (!write_solution(resolve(h->ctl_dir, h->ctl.solution_file), h->ctl.solution_format, x, h->n, err))
+    return fail(h, DG_BAD_INPUT, err);
+  return DG_OK;
+}
+
+dg_status dg_get_sizes(const dg_handle *h, int *n, int *nf, int *nc, int *nsd, long long *tot, int *rnnz, int *acnnz) {
+  if (!h) return DG_BAD_INPUT;
+  if (!h->ready && h->S.n == 0) return DG_NOT_READY;
+  if (n) *n = h->n;
+  if (nf) *nf = h->S.fine.nagr;
+  if (nc) *nc = h->S.coarse.nagr;
+  if (nsd) *nsd = (int)h->S.sd_ptr.size() - 1;
+  if (tot) *tot = (long long)h->S.sd_nodes.size();
+  if (rnnz) *rnnz = (int)h->S.R_i.size();
+  if (acnnz) *acnnz = (int)h->S.AC_i.size();
+  return DG_OK;
+}
+
+dg_status dg_get_aggregates(const dg_handle *h, int *fine_num, int *coarse_num) {
+  if (!h || h->S.n == 0) return DG_NOT_READY;
+  if (fine_num) std::copy(h->S.fine.num.begin(), h->S.fine.num.end(), fine_num);
+  if (coarse_num) std::copy(h->S.coarse.num.begin(), h->S.coarse.num.end(), coarse_num);
+  return DG_OK;
+}
+
+dg_status dg_get_subdomains(const dg_handle *h, long long *starts, int *nodes) {
+  if (!h || h->S.n == 0) return DG_NOT_READY;
+  if (starts) for (size_t q = 0; q < h->S.sd_ptr.size(); q++) starts[q] = h->S.sd_ptr[q];
+  if (nodes) std::copy(h->S.sd_nodes.begin(), h->S.sd_nodes.end(), nodes);
+  return DG_OK;
+}
+
+dg_status dg_get_restriction(const dg_handle *h, int *ri, int *rj, double *rv) {
+  if (!h || h->S.n == 0) return DG_NOT_READY;
+  if (ri) std::copy(h->S.R_i.begin(), h->S.R_i.end(), ri);
+  if (rj) std::copy(h->S.R_j.begin(), h->S.R_j.end(), rj);
+  if (rv) std::copy(h->S.R_v.begin(), h->S.R_v.end(), rv);
+  return DG_OK;
+}
+
+dg_status dg_get_coarse_matrix(const dg_handle *h, int *ci, int *cj, double *cv) {
+  if (!h || h->S.n == 0) return DG_NOT_READY;
+  if (ci) std::copy(h->S.AC_i.begin(), h->S.AC_i.end(), ci);
+  if (cj) std::copy(h->S.AC_j.begin(), h->S.AC_j.end(), cj);
+  if (cv) std::copy(h->S.AC_v.begin(), h->S.AC_v.end(), cv);
+  return DG_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,1079 @@
+// Host setup for the GB300 solver: control words, input formats and DOUG's
+// np=1 setup (strength, aggregation, smoothed aggregation, Galerkin product,
+// overlapping subdomains).  Node ids are 0-based inside this file; aggregate
+// numbers stay 1-based (0 = unaggregated) because the reference's repair
+// logic tests them against zero.
+//
+// Build with -ffp-contract=off: the coarse aggregation depends on the exact
+// bits of the Galerkin product, which the reference evaluates in source order.
+#include "setup.hpp"
+
+#include <algorithm>
+#include <cctype>
+#include <climits>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <fstream>
+#include <sstream>
+
+namespace dg {
+
+// ---------------------------------------------------------------------------
+// control words (controls.F90:159-246, DOUG_utils.F90:629-1150)
+// ---------------------------------------------------------------------------
+static std::string first10_noblank(const std::string &s) {
+  std::string b;
+  for (size_t i = 0; i < s.size() && i < 10; i++)
+    if (s[i] != ' ') b.push_back(s[i]);
+  return b;
+}
+
+bool parse_i10(const std::string &s, int &out) {
+  std::string b = first10_noblank(s);
+  if (b.empty()) { out = 0; return true; }
+  char *end = nullptr;
+  long v = strtol(b.c_str(), &end, 10);
+  if (*end) return false;
+  out = (int)v;
+  return true;
+}
+
+bool parse_f10_5(const std::string &s, double &out) {
+  std::string b = first10_noblank(s);
+  if (b.empty()) { out = 0.0; return true; }
+  size_t p = 0;
+  bool neg = false;
+  if (b[p] == '+' || b[p] == '-') { neg = b[p] == '-'; p++; }
+  std::string mant;
+  bool dot = false;
+  int ndig = 0;
+  while (p < b.size() && (isdigit((unsigned char)b[p]) || b[p] == '.')) {
+    if (b[p] == '.') { if (dot) return false; dot = true; } else ndig++;
+    mant.push_back(b[p++]);
+  }
+  if (ndig == 0) return false;
+  int expo = 0;
+  if (p < b.size()) {
+    char e = b[p];
+    if (e == 'e' || e == 'E' || e == 'd' || e == 'D') p++;
+    if (p >= b.size()) return false;
+    char *end = nullptr;
+    long ev = strtol(b.c_str() + p, &end, 10);
+    if (*end || end == b.c_str() + p) return false;
+    expo = (int)ev;
+  }
+  // F10.5 without a decimal point: five implied decimals
+  std::string num = mant + "e" + std::to_string(dot ? expo : expo - 5);
+  double v = strtod(num.c_str(), nullptr);
+  out = neg ? -v : v;
+  return true;
+}
+
+bool parse_l1(const std::string &s, bool &out) {
+  if (s.empty()) return false;
+  char c = s[0];
+  if (c == '.' && s.size() > 1) c = s[1];
+  if (c == 'T' || c == 't') { out = true; return true; }
+  if (c == 'F' || c == 'f') { out = false; return true; }
+  return false;
+}
+
+bool ctl_apply(Controls &c, const std::string &w1, const std::string &w2, std::string &err) {
+  // the first occurrence of a word wins; repeats only warn in the reference
+  auto I = [&](const char *nm, int &f) -> int {
+    if (w1 != nm) return 0;
+    if (f == -1 && !parse_i10(w2, f)) { err = "bad integer for " + w1 + ": '" + w2 + "'"; return -1; }
+    return 1;
+  };
+  auto R = [&](const char *nm, double &f) -> int {
+    if (w1 != nm) return 0;
+    if (f == -1.0 && !parse_f10_5(w2, f)) { err = "bad real for " + w1 + ": '" + w2 + "'"; return -1; }
+    return 1;
+  };
+  auto L = [&](const char *nm, bool &f) -> int {
+    if (w1 != nm) return 0;
+    if (!parse_l1(w2, f)) { err = "bad logical for " + w1 + ": '" + w2 + "'"; return -1; }
+    return 1;
+  };
+  auto S = [&](const char *nm, std::string &f) -> int {
+    if (w1 != nm) return 0;
+    if (f.empty()) f = w2;
+    return 1;
+  };
+  int r = 0;
+#define TRY(x) if ((r = (x)) != 0) return r > 0;
+  TRY(I("solver", c.solver)) TRY(I("method", c.method)) TRY(I("fine_method", c.fine_method))
+  TRY(I("num_iters", c.num_iters)) TRY(I("grid_size", c.grid_size))
+  TRY(I("coarse_method", c.coarse_method)) TRY(I("num_subdomains", c.num_subdomains))
+  TRY(I("levels", c.levels)) TRY(I("overlap", c.overlap)) TRY(I("smoothers", c.smoothers))
+  TRY(I("input_type", c.input_type)) TRY(I("matrix_type", c.matrix_type))
+  TRY(I("initial_guess", c.initial_guess)) TRY(I("number_of_blocks", c.number_of_blocks))
+  TRY(I("radius1", c.radius1)) TRY(I("radius2", c.radius2)) TRY(I("minasize1", c.minasize1))
+  TRY(I("minasize2", c.minasize2)) TRY(I("maxasize1", c.maxasize1)) TRY(I("maxasize2", c.maxasize2))
+  TRY(I("debug", c.debug)) TRY(I("verbose", c.verbose)) TRY(I("plotting", c.plotting))
+  TRY(R("strong1", c.strong1)) TRY(R("strong2", c.strong2)) TRY(R("solve_tolerance", c.solve_tolerance))
+  TRY(I("solve_maxiters", c.solve_maxiters))
+  TRY(L("symmstruct", c.symmstruct)) TRY(L("symmnumeric", c.symmnumeric))
+  TRY(I("interpolation_type", c.interpolation_type))
+  TRY(S("assembled_mtx_file", c.assembled_mtx_file)) TRY(I("assembled_mtx_format", c.assembled_mtx_format))
+  TRY(S("assembled_rhs_file", c.assembled_rhs_file)) TRY(I("assembled_rhs_format", c.assembled_rhs_format))
+  TRY(S("info_file", c.info_file)) TRY(S("elemmat_rhs_file", c.elemmat_rhs_file))
+  TRY(S("freedom_lists_file", c.freedom_lists_file)) TRY(S("coords_file", c.coords_file))
+  TRY(S("freemap_file", c.freemap_file))
+  TRY(S("solution_file", c.solution_file)) TRY(I("solution_format", c.solution_format))
+  TRY(I("start_vec_type", c.start_vec_type))
+#undef TRY
+  return true;  // unknown words are ignored
+}
+
+static std::string getword(const std::string &line, int num) {
+  // words are separated by blanks only (DOUG_utils.F90:1518-1544)
+  int n = (int)line.size();
+  while (n > 0 && (line[n - 1] == ' ' || line[n - 1] == '\r')) n--;
+  int j = 0, k = 0;
+  for (int i = 1; i <= num; i++) {
+    while (j < n && line[j] == ' ') j++;
+    if (j >= n) return "";
+    k = j;
+    while (j < n && line[j] != ' ') j++;
+  }
+  return line.substr(k, j - k);
+}
+
+bool ctl_parse_text(Controls &c, const std::string &text, std::string &err) {
+  std::istringstream is(text);
+  std::string line;
+  while (std::getline(is, line)) {
+    if (line.size() > 300) line.resize(300);
+    while (!line.empty() && (line.back() == ' ' || line.back() == '\r')) line.pop_back();
+    if (line.empty() || line[0] == '#') continue;
+    std::string w1 = getword(line, 1), w2 = getword(line, 2);
+    for (auto &ch : w1)
+      if (ch >= 'A' && ch <= 'Z') ch = (char)(ch + 32);
+    if (!ctl_apply(c, w1, w2, err)) return false;
+  }
+  return true;
+}
+
+void ctl_finish(Controls &c) {
+  if (c.solve_maxiters == -1) c.solve_maxiters = 100;
+}
+
+// ---------------------------------------------------------------------------
+// formats
+// ---------------------------------------------------------------------------
+static bool slurp(const std::string &path, std::vector<unsigned char> &buf) {
+  FILE *f = fopen(path.c_str(), "rb");
+  if (!f) return false;
+  fseek(f, 0, SEEK_END);
+  long L = ftell(f);
+  fseek(f, 0, SEEK_SET);
+  buf.resize((size_t)L + 1);
+  size_t got = L > 0 ? fread(buf.data(), 1, (size_t)L, f) : 0;
+  fclose(f);
+  if ((long)got != L) return false;
+  buf[(size_t)L] = 0;
+  buf.resize((size_t)L);
+  return true;
+}
+static uint32_t rd_be32(const unsigned char *p) {
+  return ((uint32_t)p[0] << 24) | ((uint32_t)p[1] << 16) | ((uint32_t)p[2] << 8) | p[3];
+}
+static uint32_t rd_le32(const unsigned char *p) {
+  return ((uint32_t)p[3] << 24) | ((uint32_t)p[2] << 16) | ((uint32_t)p[1] << 8) | p[0];
+}
+static double rd_bed(const unsigned char *p) {
+  uint64_t u = ((uint64_t)rd_be32(p) << 32) | rd_be32(p + 4);
+  double d;
+  memcpy(&d, &u, 8);
+  return d;
+}
+static double rd_led(const unsigned char *p) {
+  uint64_t u = ((uint64_t)rd_le32(p + 4) << 32) | rd_le32(p);
+  double d;
+  memcpy(&d, &u, 8);
+  return d;
+}
+
+// One Fortran unformatted sequential record (little-endian 4-byte markers;
+// negative markers are gfortran sub-records of a long record).
+static bool fortran_record(const std::vector<unsigned char> &b, size_t &pos,
+                           std::vector<unsigned char> &rec) {
+  rec.clear();
+  for (;;) {
+    if (pos + 4 > b.size()) return false;
+    int32_t m = (int32_t)rd_le32(&b[pos]);
+    size_t len = (size_t)(m < 0 ? -(int64_t)m : m);
+    if (pos + 8 + len > b.size()) return false;
+    rec.insert(rec.end(), b.begin() + (long)pos + 4, b.begin() + (long)(pos + 4 + len));
+    pos += 8 + len;
+    if (m >= 0) return true;
+  }
+}
+
+static void skip_sep(const char *&p) {
+  while (*p == ',' || isspace((unsigned char)*p)) p++;
+}
+static bool next_double(const char *&p, double &v) {
+  skip_sep(p);
+  char tmp[64];
+  int k = 0;
+  while (*p && !isspace((unsigned char)*p) && *p != ',' && k < 63) {
+    char ch = *p++;
+    tmp[k++] = (ch == 'd' || ch == 'D') ? 'e' : ch;
+  }
+  tmp[k] = 0;
+  char *end = nullptr;
+  v = strtod(tmp, &end);
+  return k > 0 && *end == 0;
+}
+static bool next_int(const char *&p, long &v) {
+  skip_sep(p);
+  char *end = nullptr;
+  v = strtol(p, &end, 10);
+  if (end == p) return false;
+  p = end;
+  return true;
+}
+
+bool read_assembled(const std::string &path, int format, int &n, std::vector<int> &ii,
+                    std::vector<int> &jj, std::vector<double> &vv, std::string &err) {
+  std::vector<unsigned char> b;
+  if (!slurp(path, b)) { err = "Unable to open assembled file: " + path; return false; }
+  long N = 0, NNZ = 0;
+  if (format == 0 || format < 0) {
+    b.push_back(0);
+    const char *p = (const char *)b.data();
+    if (!next_int(p, N) || !next_int(p, NNZ)) { err = "File " + path + " too short!"; return false; }
+    long cnt = std::max(N, NNZ);
+    ii.resize(cnt); jj.resize(cnt); vv.resize(cnt);
+    for (long k = 0; k < cnt; k++) {
+      long a, c;
+      double v;
+      if (!next_int(p, a) || !next_int(p, c) || !next_double(p, v)) {
+        err = "[ReadInSparseAssembledBulk_TextBinary] File too short! " + path;
+        return false;
+      }
+      ii[k] = (int)a; jj[k] = (int)c; vv[k] = v;
+    }
+  } else if (format == 1) {
+    size_t pos = 0;
+    std::vector<unsigned char> rec;
+    if (!fortran_record(b, pos, rec) || rec.size() < 8) { err = "File " + path + " too short!"; return false; }
+    N = (int32_t)rd_le32(&rec[0]); NNZ = (int32_t)rd_le32(&rec[4]);
+    long cnt = std::max(N, NNZ);
+    if (!fortran_record(b, pos, rec) || (long)rec.size() < 16 * cnt) { err = "File " + path + " too short!"; return false; }
+    ii.resize(cnt); jj.resize(cnt); vv.resize(cnt);
+    for (long k = 0; k < cnt; k++) {
+      ii[k] = (int32_t)rd_le32(&rec[16 * k]);
+      jj[k] = (int32_t)rd_le32(&rec[16 * k + 4]);
+      vv[k] = rd_led(&rec[16 * k + 8]);
+    }
+  } else if (format == 2) {
+    if (b.size() < 8) { err = "File " + path + " too short!"; return false; }
+    N = (int32_t)rd_be32(&b[0]); NNZ = (int32_t)rd_be32(&b[4]);
+    long cnt = std::max(N, NNZ);
+    if ((long)b.size() < 8 + 16 * cnt) { err = "File " + path + " too short!"; return false; }
+    ii.resize(cnt); jj.resize(cnt); vv.resize(cnt);
+    for (long k = 0; k < cnt; k++) {
+      ii[k] = (int32_t)rd_be32(&b[8 + 16 * k]);
+      jj[k] = (int32_t)rd_be32(&b[8 + 16 * k + 4]);
+      vv[k] = rd_bed(&b[8 + 16 * k + 8]);
+    }
+  } else {
+    err = "[ReadInSparseAssembledHeader] Data format not recognized";
+    return false;
+  }
+  // header swap when n > nnz (SpMtx_class.F90:421-425)
+  n = (int)std::min(N, NNZ);
+  if (N <= NNZ) n = (int)N;
+  return true;
+}
+
+bool read_vector(const std::string &path, int format, int n, std::vector<double> &x,
+                 std::string &err) {
+  std::vector<unsigned char> b;
+  if (!slurp(path, b)) { err = "Unable to open vector file: " + path; return false; }
+  x.assign(n, 0.0);
+  if (format == 0) {
+    b.push_back(0);
+    const char *p = (const char *)b.data();
+    long m;
+    if (!next_int(p, m) || m != n) {
+      err = "[Vect_ReadFromFile_Text] : Number of vector elements in file is not as expected.";
+      return false;
+    }
+    for (int k = 0; k < n; k++)
+      if (!next_double(p, x[k])) { err = "[Vect_ReadFromFile_Text] : End of file reached to early."; return false; }
+  } else if (format == 1 || format < 0) {
+    size_t pos = 0;
+    std::vector<unsigned char> rec;
+    if (!fortran_record(b, pos, rec) || (long)rec.size() < 8L * n) {
+      err = "[Vect_ReadFromFile_Binary] : End of file reached to early.";
+      return false;
+    }
+    for (int k = 0; k < n; k++) x[k] = rd_led(&rec[8 * (size_t)k]);
+  } else if (format == 2) {
+    if (b.size() < 4 || (int)rd_be32(&b[0]) != n || b.size() < 4 + 8 * (size_t)n) {
+      err = "[Vect_ReadFromFile_XDR] : Number of vector elements in file is not as expected.";
+      return false;
+    }
+    for (int k = 0; k < n; k++) x[k] = rd_bed(&b[4 + 8 * (size_t)k]);
+  } else {
+    err = "[Vect_ReadFromFile] Data format not recognized";
+    return false;
+  }
+  return true;
+}
+
+bool write_solution(const std::string &path, int format, const double *x, int n, std::string &err) {
+  FILE *f = fopen(path.c_str(), "wb");
+  if (!f) { err = "cannot open " + path; return false; }
+  if (format == 0) {
+    fprintf(f, "%6d\n", n);
+    for (int k = 0; k < n; k++) fprintf(f, "%21.14E\n", x[k]);
+  } else if (format == 1) {
+    uint32_t m = (uint32_t)(8 * n);
+    fwrite(&m, 4, 1, f);
+    fwrite(x, 8, (size_t)n, f);
+    fwrite(&m, 4, 1, f);
+  } else if (format == 2) {
+    unsigned char hb[4] = {(unsigned char)(n >> 24), (unsigned char)(n >> 16),
+                           (unsigned char)(n >> 8), (unsigned char)n};
+    fwrite(hb, 1, 4, f);
+    for (int k = 0; k < n; k++) {
+      uint64_t u;
+      memcpy(&u, &x[k], 8);
+      unsigned char o[8];
+      for (int q = 0; q < 8; q++) o[q] = (unsigned char)(u >> (56 - 8 * q));
+      fwrite(o, 1, 8, f);
+    }
+  } else {
+    fclose(f);
+    err = "Solution format is not valid";
+    return false;
+  }
+  fclose(f);
+  return true;
+}
+
+// ---------------------------------------------------------------------------
+// sparse helpers with DOUG's ordering semantics
+// ---------------------------------------------------------------------------
+struct Coo {  // triplets in a definite order, 0-based
+  int nrows = 0, ncols = 0;
+  std::vector<int> i, j;
+  std::vector<double> v;
+  size_t size() const { return v.size(); }
+};
+
+// stable bucketing by row (SpMtx_arrange ROWS, sort=.false.)
+static Csr rows_of(const Coo &m) {
+  Csr c;
+  c.nrows = m.nrows; c.ncols = m.ncols;
+  c.ptr.assign((size_t)m.nrows + 1, 0);
+  for (size_t k = 0; k < m.size(); k++) c.ptr[(size_t)m.i[k] + 1]++;
+  for (int r = 0; r < m.nrows; r++) c.ptr[(size_t)r + 1] += c.ptr[(size_t)r];
+  c.col.resize(m.size()); c.val.resize(m.size());
+  std::vector<int64_t> fill(c.ptr.begin(), c.ptr.end() - 1);
+  for (size_t k = 0; k < m.size(); k++) {
+    int64_t d = fill[(size_t)m.i[k]]++;
+    c.col[(size_t)d] = m.j[k]; c.val[(size_t)d] = m.v[k];
+  }
+  return c;
+}
+// stable bucketing by column: a "row view" of the transpose
+static Csr cols_of(const Coo &m) {
+  Coo t;
+  t.nrows = m.ncols; t.ncols = m.nrows;
+  t.i = m.j; t.j = m.i; t.v = m.v;
+  return rows_of(t);
+}
+static Coo coo_of(const Csr &c) {
+  Coo m;
+  m.nrows = c.nrows; m.ncols = c.ncols;
+  m.i.resize(c.col.size()); m.j = c.col; m.v = c.val;
+  for (int r = 0; r < c.nrows; r++)
+    for (int64_t k = c.ptr[(size_t)r]; k < c.ptr[(size_t)r + 1]; k++) m.i[(size_t)k] = r;
+  return m;
+}
+
+// SpMtx_AB (SpMtx_op_AB.f90:39-200): A given as a row view, B as a row view
+// (of B, or of B^T).  Output row i lists its columns in first-touch order;
+// each value is summed in the order A's row entries, then B's row entries,
+// are visited; explicit zeros are kept.
+static Csr spgemm_first_touch(const Csr &A, const Csr &B) {
+  Csr C;
+  C.nrows = A.nrows; C.ncols = B.ncols;
+  C.ptr.assign((size_t)A.nrows + 1, 0);
+  std::vector<int> mark((size_t)B.ncols, -1);
+  std::vector<int64_t> pos((size_t)B.ncols, 0);
+  for (int i = 0; i < A.nrows; i++) {
+    int64_t cnt = 0;
+    for (int64_t k = A.ptr[(size_t)i]; k < A.ptr[(size_t)i + 1]; k++) {
+      int kk = A.col[(size_t)k];
+      for (int64_t j = B.ptr[(size_t)kk]; j < B.ptr[(size_t)kk + 1]; j++) {
+        int jj = B.col[(size_t)j];
+        if (mark[(size_t)jj] != i) { mark[(size_t)jj] = i; cnt++; }
+      }
+    }
+    C.ptr[(size_t)i + 1] = C.ptr[(size_t)i] + cnt;
+  }
+  C.col.resize((size_t)C.ptr.back());
+  C.val.resize((size_t)C.ptr.back());
+  std::fill(mark.begin(), mark.end(), -1);
+  for (int i = 0; i < A.nrows; i++) {
+    int64_t base = C.ptr[(size_t)i], nind = 0;
+    for (int64_t k = A.ptr[(size_t)i]; k < A.ptr[(size_t)i + 1]; k++) {
+      int kk = A.col[(size_t)k];
+      double av = A.val[(size_t)k];
+      for (int64_t j = B.ptr[(size_t)kk]; j < B.ptr[(size_t)kk + 1]; j++) {
+        int jj = B.col[(size_t)j];
+        double prod = av * B.val[(size_t)j];
+        if (mark[(size_t)jj] != i) {
+          mark[(size_t)jj] = i;
+          pos[(size_t)jj] = base + nind;
+          C.col[(size_t)(base + nind)] = jj;
+          C.val[(size_t)(base + nind)] = prod;
+          nind++;
+        } else {
+          C.val[(size_t)pos[(size_t)jj]] = C.val[(size_t)pos[(size_t)jj]] + prod;
+        }
+      }
+    }
+  }
+  return C;
+}
+
+// ---------------------------------------------------------------------------
+// strength of connection and aggregation
+// ---------------------------------------------------------------------------
+struct ScaledMatrix {
+  Csr M;                     // DOUG row order
+  std::vector<double> diag;  // unscaled diagonal (last diagonal entry of each row)
+  bool symmetric = false;    // symmstruct && symmnumeric
+  std::vector<char> strong;  // per entry
+  std::vector<int64_t> sptr; // sorted strong adjacency
+  std::vector<int> scol;
+};
+
+// SpMtx_scale (SpMtx_arrangement.F90:298-346) applied entrywise.
+static void scale_rows(ScaledMatrix &S) {
+  Csr &M = S.M;
+  S.diag.assign((size_t)std::max(M.nrows, M.ncols), 0.0);
+  // diag(indi)=val for every diagonal entry, in entry order
+  for (int r = 0; r < M.nrows; r++)
+    for (int64_t k = M.ptr[(size_t)r]; k < M.ptr[(size_t)r + 1]; k++)
+      if (M.col[(size_t)k] == r) S.diag[(size_t)r] = M.val[(size_t)k];
+  std::vector<double> s(S.diag.size());
+  if (S.symmetric) {
+    for (size_t q = 0; q < s.size(); q++) s[q] = std::sqrt(std::fabs(S.diag[q]));
+    for (int r = 0; r < M.nrows; r++)
+      for (int64_t k = M.ptr[(size_t)r]; k < M.ptr[(size_t)r + 1]; k++) {
+        double v = M.val[(size_t)k] / s[(size_t)r];
+        M.val[(size_t)k] = v / s[(size_t)M.col[(size_t)k]];
+      }
+  } else {
+    for (size_t q = 0; q < s.size(); q++) s[q] = std::fabs(S.diag[q]);
+    for (int r = 0; r < M.nrows; r++)
+      for (int64_t k = M.ptr[(size_t)r]; k < M.ptr[(size_t)r + 1]; k++)
+        M.val[(size_t)k] = M.val[(size_t)k] / s[(size_t)r];
+  }
+}
+
+// SpMtx_unscale (SpMtx_arrangement.F90:350-388).
+static void unscale_rows(ScaledMatrix &S) {
+  Csr &M = S.M;
+  std::vector<double> s(S.diag.size());
+  if (S.symmetric) {
+    for (size_t q = 0; q < s.size(); q++) s[q] = std::sqrt(std::fabs(S.diag[q]));
+    for (int r = 0; r < M.nrows; r++)
+      for (int64_t k = M.ptr[(size_t)r]; k < M.ptr[(size_t)r + 1]; k++) {
+        double v = M.val[(size_t)k] * s[(size_t)r];
+        M.val[(size_t)k] = v * s[(size_t)M.col[(size_t)k]];
+      }
+  } else {
+    for (size_t q = 0; q < s.size(); q++) s[q] = std::fabs(S.diag[q]);
+    for (int r = 0; r < M.nrows; r++)
+      for (int64_t k = M.ptr[(size_t)r]; k < M.ptr[(size_t)r + 1]; k++)
+        M.val[(size_t)k] = M.val[(size_t)k] * s[(size_t)r];
+  }
+}
+
+// SpMtx_find_strong (SpMtx_aggregation.F90:829-900) + sorted strong
+// adjacency SpMtx_build_refs_symm(sortdown) (SpMtx_arrangement.F90:461-568).
+static void find_strong(ScaledMatrix &S, double alpha) {
+  const Csr &M = S.M;
+  S.strong.assign(M.col.size(), 0);
+  for (int r = 0; r < M.nrows; r++) {
+    double mx = (double)(-1.0e15f);
+    for (int64_t k = M.ptr[(size_t)r]; k < M.ptr[(size_t)r + 1]; k++)
+      if (M.col[(size_t)k] != r) mx = std::max(mx, std::fabs(M.val[(size_t)k]));
+    mx = mx * alpha;
+    for (int64_t k = M.ptr[(size_t)r]; k < M.ptr[(size_t)r + 1]; k++) {
+      if (M.col[(size_t)k] != r) S.strong[(size_t)k] = std::fabs(M.val[(size_t)k]) > mx;
+      else S.strong[(size_t)k] = S.diag[(size_t)r] > mx;  // unscaled diagonal
+    }
+  }
+  // strong off-diagonal neighbours of each row, by |value| descending; equal
+  // magnitudes keep their entry order (stable)
+  int n = M.nrows;
+  S.sptr.assign((size_t)n + 1, 0);
+  std::vector<int64_t> tmp;
+  S.scol.clear();
+  for (int r = 0; r < n; r++) {
+    tmp.clear();
+    for (int64_t k = M.ptr[(size_t)r]; k < M.ptr[(size_t)r + 1]; k++)
+      if (S.strong[(size_t)k] && M.col[(size_t)k] != r && M.col[(size_t)k] < n) tmp.push_back(k);
+    std::stable_sort(tmp.begin(), tmp.end(), [&](int64_t a, int64_t b) {
+      return std::fabs(M.val[(size_t)a]) > std::fabs(M.val[(size_t)b]);
+    });
+    for (int64_t k : tmp) S.scol.push_back(M.col[(size_t)k]);
+    S.sptr[(size_t)r + 1] = (int64_t)S.scol.size();
+  }
+}
+
+// Persistent state of the reference's aggregation (SAVE variables):
+// allmind (Aggregate_mod.F90:348) and beta (SpMtx_aggregation.F90:81).
+struct AggState {
+  int allmind = INT_MAX;
+  double beta = 1.0e-5;
+};
+
+static constexpr int kAggregated = INT_MAX;       // D_AGGREGATED
+static constexpr int kPending = INT_MAX / 2;      // D_PENDING
+
+class Colourer {  // lets_colour / can_add_roundlayer (Aggregate_mod.F90:287-497)
+ public:
+  Colourer(const ScaledMatrix &S, int r, int maxasize, std::vector<int> &stat,
+           std::vector<int> &dist, std::vector<int> &nodes, AggState &st)
+      : S_(S), r_(r), maxa_(maxasize), stat_(stat), dist_(dist), nodes_(nodes), st_(st) {}
+
+  // returns ok (0..3); nodes_[0..nneigs) are the found nodes
+  int colour(int seed, int &nneigs) {
+    nneigs = 0;
+    stat_[(size_t)seed] = 1;
+    dist_[(size_t)seed] = 0;
+    inl_.assign(1, seed);
+    return layer(0, nneigs);
+  }
+
+ private:
+  int layer(int lay, int &nneigs) {
+    bool fits = true;
+    std::vector<int> newl;
+    if (lay <= 2 * r_) {
+      for (size_t q = 0; q < inl_.size(); q++) {
+        int ln = inl_[q];
+        for (int64_t k = S_.sptr[(size_t)ln]; k < S_.sptr[(size_t)ln + 1]; k++) {
+          int cn = S_.scol[(size_t)k];
+          if (stat_[(size_t)cn] <= 0) {
+            if (stat_[(size_t)cn] == 0) {
+              newl.push_back(cn);
+              dist_[(size_t)cn] = dist_[(size_t)ln] + 1;
+            }
+            stat_[(size_t)cn] -= 1;  // weight for the rounding step
+          }
+        }
+      }
+    }
+    if (lay <= r_) {  // rounding
+      int nround = 0;
+      std::vector<int> rounders;
+      int mind = INT_MAX, maxd = 0;
+      for (int cn : newl) {
+        int d = -stat_[(size_t)cn];
+        mind = std::min(mind, d);
+        maxd = std::max(maxd, d);
+      }
+      if (mind < st_.allmind) st_.allmind = mind;
+      if (mind < maxd || mind > st_.allmind) {
+        for (size_t q = 0; q < newl.size(); q++) {
+          if (stat_[(size_t)newl[q]] == -maxd) {
+            nround++;
+            if (nneigs + (int)inl_.size() + 1 > maxa_) { fits = false; break; }
+            inl_.push_back(newl[q]);
+            rounders.push_back(newl[q]);
+            newl[q] = -1;
+          }
+        }
+      }
+      if (!fits) rounders.clear();
+      newl.erase(std::remove(newl.begin(), newl.end(), -1), newl.end());
+      for (int rn : rounders)
+        for (int64_t k = S_.sptr[(size_t)rn]; k < S_.sptr[(size_t)rn + 1]; k++) {
+          int cn = S_.scol[(size_t)k];
+          if (stat_[(size_t)cn] == 0) {
+            newl.push_back(cn);
+            dist_[(size_t)cn] = dist_[(size_t)rn] + 1;
+          }
+        }
+      (void)nround;
+    }
+    if (lay <= r_ && nneigs + (int)inl_.size() > maxa_) fits = false;
+    if (fits) {
+      for (int v : inl_) {
+        stat_[(size_t)v] = lay + 1;
+        put(nneigs++, v);
+      }
+      if (lay <= 2 * r_) {
+        for (int v : newl) stat_[(size_t)v] = kPending - 1;
+        inl_ = newl;
+        return layer(lay + 1, nneigs);
+      }
+      return 3;
+    }
+    for (int v : inl_) dist_[(size_t)v] = 0;
+    for (int v : newl) dist_[(size_t)v] = 0;
+    for (int q = 0; q < nneigs; q++) dist_[(size_t)nodes_[(size_t)q]] = 0;
+    for (int v : inl_) put(nneigs++, v);
+    if (nneigs > 0) return lay > r_ ? 2 : 1;
+    return 0;
+  }
+
+  void put(int pos, int v) {
+    if ((size_t)pos >= nodes_.size()) nodes_.resize(2 * nodes_.size() + 64, 0);
+    nodes_[(size_t)pos] = v;
+  }
+
+  const ScaledMatrix &S_;
+  int r_, maxa_;
+  std::vector<int> &stat_, &dist_, &nodes_;
+  AggState &st_;
+  std::vector<int> inl_;
+};
+
+static void form_aggr(Aggregates &ag, int nagr, int n, const std::vector<int> &num) {
+  ag.nagr = nagr;
+  ag.num = num;
+  ag.starts.assign((size_t)nagr + 1, 0);
+  for (int i = 0; i < n; i++)
+    if (num[(size_t)i] > 0) ag.starts[(size_t)num[(size_t)i]]++;
+  for (int a = 0; a < nagr; a++) ag.starts[(size_t)a + 1] += ag.starts[(size_t)a];
+  ag.nodes.assign((size_t)ag.starts[(size_t)nagr], 0);
+  std::vector<int> fill(ag.starts.begin(), ag.starts.end() - 1);
+  for (int i = 0; i < n; i++)
+    if (num[(size_t)i] > 0) ag.nodes[(size_t)fill[(size_t)num[(size_t)i] - 1]++] = i + 1;
+}
+
+// SpMtx_aggregate (SpMtx_aggregation.F90:49-641), one process.
+static bool aggregate(ScaledMatrix &S, int neighood, int minasize, int maxasize, double alpha,
+                      bool coarse, AggState &st, Aggregates &inner, Aggregates &full,
+                      std::string &err) {
+  const Csr &M = S.M;
+  int n = M.nrows;
+  std::vector<int> aggrnum((size_t)n, 0);
+  int nagrs = 0, nisolated = 0;
+  bool toosmall = false;
+  int sn = (int)std::sqrt((float)n);
+  int maxasizelargest;
+  if (alpha >= 0 || sn * sn != n) {
+    // the reference's nodes(n) can receive a node twice (a neighbour of two
+    // rounder nodes is queued by each), so the list may outgrow n on small
+    // graphs; it is sized with room for that
+    std::vector<int> stat((size_t)n, 0), dist((size_t)n, 0), nodes((size_t)4 * n + 64, 0);
+    // nextgoodstart (1-based, length n): good seeds at the head, the outer
+    // layer of the newest aggregate at the tail, exactly as the reference
+    std::vector<int> ngs((size_t)n + 1, 0);
+    int ngood = 0;
+    maxasizelargest = coarse ? 3 * maxasize : maxasize + 4 * (2 * neighood);
+    if (!coarse) st.beta = alpha / 4.0;
+    Colourer col(S, neighood, maxasize, stat, dist, nodes, st);
+    int first = 0;
+    for (;;) {
+      // drop good starts that got aggregated meanwhile
+      if (ngood > 0) {
+        int w = 0;
+        for (int q = 1; q <= ngood; q++)
+          if (stat[(size_t)ngs[(size_t)q]] < kPending) {
+            w++;
+            if (w < q) ngs[(size_t)w] = ngs[(size_t)q];
+          }
+        ngood = w;
+      }
+      int start;
+      if (ngood == 0) {
+        while (first < n && stat[(size_t)first] >= kPending) first++;
+        if (first >= n) break;
+        start = first;
+      } else {
+        start = -1;
+        for (int a = 2; a <= ngood && start < 0; a++)
+          for (int b = 1; b < a; b++)
+            if (ngs[(size_t)a] == ngs[(size_t)b]) { start = ngs[(size_t)a]; break; }
+        if (start < 0) start = ngs[1];
+      }
+      int nneigs = 0;
+      int ok = col.colour(start, nneigs);
+      if (ok <= 0) { err = "aggregation found nothing"; return false; }
+      nagrs++;
+      int next_layer;
+      if (ok == 3) {
+        std::vector<int> layerlen((size_t)2 * neighood + 3, 0);
+        int maxlayer = 0;
+        if (!toosmall && nneigs < minasize) toosmall = true;
+        for (int q = nneigs - 1; q >= 0; q--) {
+          int k = stat[(size_t)nodes[(size_t)q]];
+          if (k > maxlayer) maxlayer = k;
+          if (k <= neighood + 1) break;
+          if (k > 2 * neighood + 2) { err = "aggregation layer out of range"; return false; }
+          layerlen[(size_t)k]++;
+        }
+        next_layer = neighood + 2;
+        int best = layerlen[(size_t)neighood + 2];
+        for (int q = neighood + 3; q <= maxlayer; q++)
+          if (best < layerlen[(size_t)q]) { best = layerlen[(size_t)q]; next_layer = q; }
+      } else if (ok == 2) {
+        next_layer = neighood + 2;
+        if (!toosmall && nneigs < minasize) toosmall = true;
+      } else {
+        next_layer = 0;
+      }
+      int mindistance = INT_MAX, nouters = 0;
+      for (int q = 0; q < nneigs; q++) {
+        int node = nodes[(size_t)q];
+        if (stat[(size_t)node] <= neighood + 1 && q + 1 <= maxasize) {
+          stat[(size_t)node] = kAggregated;
+          aggrnum[(size_t)node] = nagrs;
+        } else if (next_layer > neighood + 1) {
+          if (stat[(size_t)node] == next_layer) {
+            mindistance = std::min(mindistance, dist[(size_t)node]);
+            nouters++;
+            ngs[(size_t)(n - nouters + 1)] = node;
+          }
+        }
+      }
+      for (int q = 1; q <= nouters; q++)
+        if (dist[(size_t)ngs[(size_t)(n - q + 1)]] == mindistance) {
+          ngood++;
+          ngs[(size_t)ngood] = ngs[(size_t)(n - q + 1)];
+        }
+      for (int q = 0; q < nneigs; q++) {
+        int node = nodes[(size_t)q];
+        if (stat[(size_t)node] != kAggregated) { dist[(size_t)node] = 0; stat[(size_t)node] = 0; }
+      }
+    }
+  } else {
+    // Cartesian aggregates (:332-346)
+    int nsa = (sn + neighood - 1) / neighood, k = 0;
+    for (int i = 1; i <= sn; i++)
+      for (int j = 1; j <= sn; j++)
+        aggrnum[(size_t)k++] = ((i + neighood - 1) / neighood - 1) * nsa + (j + neighood - 1) / neighood;
+    nagrs = *std::max_element(aggrnum.begin(), aggrnum.end());
+    maxasizelargest = maxasize + 4 * (2 * neighood);
+  }
+  std::vector<int> fullnum;
+  int full_nagrs;
+  if (!toosmall) {
+    fullnum = aggrnum;
+    full_nagrs = std::max(0, n > 0 ? *std::max_element(fullnum.begin(), fullnum.end()) : 0);
+    form_aggr(inner, nagrs, n, aggrnum);
+  } else {
+    // repair of too small aggregates (:369-591)
+    std::vector<std::vector<int>> members((size_t)nagrs + 1);
+    for (int i = 0; i < n; i++) members[(size_t)aggrnum[(size_t)i]].push_back(i);
+    int nagrs_new = nagrs;
+    for (int a = 1; a <= nagrs; a++) {
+      int asz = (int)members[(size_t)a].size();
+      if (asz >= minasize) continue;
+      std::vector<int> cols;
+      std::vector<double> wsum;
+      for (int node : members[(size_t)a]) {
+        for (int64_t k = M.ptr[(size_t)node]; k < M.ptr[(size_t)node + 1]; k++) {
+          int cn = M.col[(size_t)k];
+          if (cn >= n) continue;
+          int colr = aggrnum[(size_t)cn];
+          if (colr > 0 && colr != a) {
+            size_t q = 0;
+            for (; q < cols.size(); q++)
+              if (cols[q] == colr) { wsum[q] = wsum[q] + std::fabs(M.val[(size_t)k]); break; }
+            if (q == cols.size()) {
+              if ((int)cols.size() >= 4 * maxasize) { err = "mnstructneigs too small"; return false; }
+              cols.push_back(colr);
+              wsum.push_back(std::fabs(M.val[(size_t)k]));
+            }
+          }
+        }
+      }
+      double best = 0.0;
+      int eater = 0;
+      for (size_t q = 0; q < cols.size(); q++)
+        if (best < wsum[q] && (int)members[(size_t)cols[q]].size() + asz <= maxasize) {
+          best = wsum[q];
+          eater = cols[q];
+        }
+      if (best >= alpha || (coarse && best >= st.beta)) {
+        if (eater == 0) { err = "aggregate repair without an eater"; return false; }
+        for (int node : members[(size_t)a]) {
+          members[(size_t)eater].push_back(node);
+          aggrnum[(size_t)node] = eater;
+        }
+        members[(size_t)a].clear();
+        nagrs_new--;
+      } else {
+        // give the nodes away one by one, scanning from the last member
+        std::vector<int> &mem = members[(size_t)a];
+        int nleft = asz;
+        bool reduced = true;
+        while (nleft > 0 && reduced) {
+          reduced = false;
+          for (int q = (int)mem.size() - 1; q >= 0; q--) {
+            int node = mem[(size_t)q];
+            if (node < 0) continue;
+            for (int64_t k = M.ptr[(size_t)node]; k < M.ptr[(size_t)node + 1]; k++) {
+              int cn = M.col[(size_t)k];
+              if (cn >= n) continue;
+              int colr = aggrnum[(size_t)cn];
+              if (colr != a) {
+                if (colr < 1) { err = "repair found an unaggregated neighbour"; return false; }
+                if ((int)members[(size_t)colr].size() < maxasizelargest &&
+                    std::fabs(M.val[(size_t)k]) >= st.beta) {
+                  members[(size_t)colr].push_back(node);
+                  aggrnum[(size_t)node] = colr;
+                  mem[(size_t)q] = -1;
+                  nleft--;
+                  reduced = true;
+                  break;
+                }
+              }
+            }
+          }
+        }
+        if (nleft > 0 && nleft < asz) {
+          std::vector<int> keep;
+          for (int v : mem) if (v >= 0) keep.push_back(v);
+          mem = keep;
+        } else if (nleft == 0) {
+          mem.clear();
+          nagrs_new--;
+        }
+        // nleft == asz: the aggregate stays as it was
+      }
+    }
+    int naggregated = 0;
+    for (int a = 1; a <= nagrs; a++) naggregated += (int)members[(size_t)a].size();
+    full_nagrs = nagrs_new;
+    int cnt = *std::max_element(aggrnum.begin(), aggrnum.end());
+    if (cnt > nagrs_new) {  // renumber in first-touch order (:539-559)
+      std::vector<int> map((size_t)cnt + 1, 0);
+      int colc = 0;
+      for (int i = 0; i < n; i++) {
+        int a = aggrnum[(size_t)i];
+        if (a > 0) {
+          if (map[(size_t)a] == 0) map[(size_t)a] = ++colc;
+          aggrnum[(size_t)i] = map[(size_t)a];
+        }
+      }
+    }
+    fullnum.assign((size_t)n, 0);
+    if (n == naggregated) {
+      fullnum = aggrnum;
+      full_nagrs = *std::max_element(fullnum.begin(), fullnum.end());
+    } else {
+      for (int i = 0; i < n; i++) {
+        if (aggrnum[(size_t)i] > 0) fullnum[(size_t)i] = aggrnum[(size_t)i];
+        else fullnum[(size_t)i] = ++full_nagrs;
+      }
+    }
+    form_aggr(inner, nagrs_new, n, aggrnum);
+    nisolated = n - naggregated;
+  }
+  (void)nisolated;
+  form_aggr(full, full_nagrs, n, fullnum);
+  return true;
+}
+
+// ---------------------------------------------------------------------------
+// smoothed aggregation (CoarseMtx.F90:50-516)
+// ---------------------------------------------------------------------------
+static Coo smoother(const Csr &A, const std::vector<char> &strong, double omega, bool assign_diag) {
+  int N = std::max(A.nrows, A.ncols);
+  std::vector<double> d((size_t)N, 0.0);
+  for (int r = 0; r < A.nrows; r++)
+    for (int64_t k = A.ptr[(size_t)r]; k < A.ptr[(size_t)r + 1]; k++) {
+      if (A.col[(size_t)k] == r) d[(size_t)r] = assign_diag ? A.val[(size_t)k] : d[(size_t)r] + A.val[(size_t)k];
+      else if (!strong[(size_t)k]) d[(size_t)r] = d[(size_t)r] + A.val[(size_t)k];
+    }
+  Coo S;
+  S.nrows = A.nrows; S.ncols = A.nrows;
+  for (int r = 0; r < A.nrows; r++)
+    for (int64_t k = A.ptr[(size_t)r]; k < A.ptr[(size_t)r + 1]; k++) {
+      int c = A.col[(size_t)k];
+      double v;
+      if (c == r) v = 1.0 - omega;
+      else if (strong[(size_t)k]) v = -(omega / d[(size_t)r] * A.val[(size_t)k]);
+      else v = 0.0;  // weak connections stay as explicit zeros
+      S.i.push_back(r); S.j.push_back(c); S.v.push_back(v);
+    }
+  return S;
+}
+
+bool build_setup(const Controls &c_in, int n, const std::vector<int> &ii, const std::vector<int> &jj,
+                 const std::vector<double> &vv, const std::vector<int> *part, int nparts,
+                 SetupResult &out, std::string &err) {
+  Controls c = c_in;
+  out = SetupResult();
+  out.n = n;
+  if (c.fine_method < 0 || c.fine_method > 1) {
+    err = "Wrong fine method " + std::to_string(c.fine_method);
+    return false;
+  }
+  if (c.coarse_method > 1) {
+    err = "coarse_method " + std::to_string(c.coarse_method) + " is not the smoothed-aggregation path";
+    return false;
+  }
+  size_t nnz = vv.size();
+  int shift = (nnz > 0 && ii[0] == 0) ? 1 : 0;  // 0-based files (SpMtx_class.F90:441-444)
+  Coo A0;
+  A0.nrows = n; A0.ncols = n;
+  A0.i.resize(nnz); A0.j.resize(nnz); A0.v = vv;
+  for (size_t k = 0; k < nnz; k++) {
+    int a = ii[k] + shift - 1, b = jj[k] + shift - 1;
+    if (a < 0 || a >= n || b < 0 || b >= n) {
+      err = "matrix entry " + std::to_string(k + 1) + " out of range";
+      return false;
+    }
+    A0.i[k] = a; A0.j[k] = b;
+  }
+  // Partitionings_aggr_InitFine (Partitioning_aggr.F90:33-117)
+  out.strong1 = (c.strong1 != 0.0) ? c.strong1 : 0.67;
+  out.r1 = c.radius1 > 0 ? c.radius1 : 2;
+  out.min1 = c.minasize1 > 0 ? c.minasize1 : (int)(0.5 * (double)((2 * out.r1 + 1) * (2 * out.r1 + 1)));
+  out.max1 = c.maxasize1 > 0 ? c.maxasize1 : (2 * out.r1 + 1) * (2 * out.r1 + 1);
+  AggState st;
+  ScaledMatrix SA;
+  SA.M = rows_of(A0);
+  SA.symmetric = c.symmstruct && c.symmnumeric;
+  scale_rows(SA);
+  find_strong(SA, out.strong1);
+  if (!aggregate(SA, out.r1, out.min1, out.max1, out.strong1, false, st, out.fine, out.fine_full, err))
+    return false;
+  unscale_rows(SA);
+  const Csr &A = SA.M;
+  // IntRestBuild (CoarseMtx.F90:50-474); smoothers are capped at radius1
+  if (c.smoothers > c.radius1) c.smoothers = c.radius1;
+  int sm = c.smoothers;
+  if (sm < 0) { err = "smoothers must be >= 0 for the smoothed-aggregation coarse space"; return false; }
+  Coo T;  // tentative prolongator as restriction rows
+  T.nrows = out.fine.nagr; T.ncols = n;
+  for (int a = 0; a < out.fine.nagr; a++)
+    for (int q = out.fine.starts[(size_t)a]; q < out.fine.starts[(size_t)a + 1]; q++) {
+      T.i.push_back(a); T.j.push_back(out.fine.nodes[(size_t)q] - 1); T.v.push_back(1.0);
+    }
+  Csr Trows = rows_of(T);
+  Csr R;  // reference's Restrict, arranged by rows after SpMtx_AB
+  Coo Rcoo;
+  if (sm == 0) {
+    Rcoo = T;
+  } else {
+    Coo S = smoother(A, SA.strong, c.omega, false);
+    if (sm == 1) {
+      R = spgemm_first_touch(Trows, cols_of(S));
+    } else {
+      Coo S2 = smoother(A, SA.strong, c.omega, true);
+      Csr SS = spgemm_first_touch(rows_of(S2), rows_of(S));
+      auto mul = [&](const Csr &X, const Csr &Y) { return spgemm_first_touch(X, Y); };
+      Csr S2r = rows_of(S2);
+      if (sm == 3) R = mul(Trows, mul(SS, S2r));
+      else if (sm == 4) R = mul(Trows, mul(SS, SS));
+      else if (sm == 5) R = mul(Trows, mul(mul(SS, SS), S2r));
+      else if (sm == 6) R = mul(Trows, mul(mul(SS, SS), SS));
+      else if (sm == 7) R = mul(Trows, mul(mul(mul(SS, SS), SS), S2r));
+      else if (sm == 8) { Csr S4 = mul(SS, SS); R = mul(Trows, mul(S4, S4)); }
+      else R = mul(Trows, cols_of(coo_of(SS)));  // 2 (and >8, performed as 2)
+    }
+    Rcoo = coo_of(R);
+  }
+  // CoarseMtxBuild (CoarseMtx.F90:476-516): T = A R^T (R arranged by columns),
+  // AC = R T with R's rows re-bucketed from that column order.
+  Csr Rcols = cols_of(Rcoo);                 // column view: for each fine node, aggregates ascending
+  Csr Tm = spgemm_first_touch(A, Rcols);     // n x nagr
+  Coo RcolOrder;                             // R's COO after arrangement by columns
+  RcolOrder.nrows = Rcoo.nrows; RcolOrder.ncols = Rcoo.ncols;
+  for (int col = 0; col < Rcols.nrows; col++)
+    for (int64_t k = Rcols.ptr[(size_t)col]; k < Rcols.ptr[(size_t)col + 1]; k++) {
+      RcolOrder.i.push_back(Rcols.col[(size_t)k]);
+      RcolOrder.j.push_back(col);
+      RcolOrder.v.push_back(Rcols.val[(size_t)k]);
+    }
+  out.R = rows_of(RcolOrder);                // rows = aggregates, columns ascending
+  out.P = Rcols;                             // rows = fine nodes, aggregates ascending
+  out.P.nrows = n; out.P.ncols = Rcoo.nrows;
+  Csr AC = spgemm_first_touch(out.R, Tm);
+  for (size_t k = 0; k < RcolOrder.size(); k++) {
+    out.R_i.push_back(RcolOrder.i[k] + 1); out.R_j.push_back(RcolOrder.j[k] + 1);
+    out.R_v.push_back(RcolOrder.v[k]);
+  }
+  // Partitionings_aggr_InitCoarse (Partitioning_aggr.F90:120-193)
+  out.strong2 = c.strong2 > 0 ? c.strong2 : out.strong1 / 2.0;
+  ScaledMatrix SC;
+  SC.M = AC;
+  SC.symmetric = false;
+  scale_rows(SC);
+  find_strong(SC, out.strong2);
+  if (c.radius2 > 0) out.r2 = c.radius2;
+  else {
+    int nn = (int)std::sqrt(1.0 * (double)n);
+    out.r2 = (int)std::lround(3.0 * std::sqrt((double)nn) / (double)(2 * out.r1 + 1) - 1.0);
+  }
+  if (c.minasize2 > 0) out.min2 = c.minasize2;
+  else if (c.radius2 > 0) out.min2 = 2 * c.radius2 + 1;
+  else out.min2 = (int)(0.5 * (double)((2 * out.r2 + 1) * (2 * out.r2 + 1)));
+  out.max2 = c.maxasize2 > 0 ? c.maxasize2 : (2 * out.r2 + 1) * (2 * out.r2 + 1);
+  if (!aggregate(SC, out.r2, out.min2, out.max2, out.strong2, true, st, out.coarse,
+                 out.coarse_full, err))
+    return false;
+  unscale_rows(SC);
+  out.AC = SC.M;
+  for (int r = 0; r < out.AC.nrows; r++)
+    for (int64_t k = out.AC.ptr[(size_t)r]; k < out.AC.ptr[(size_t)r + 1]; k++) {
+      out.AC_i.push_back(r + 1); out.AC_j.push_back(out.AC.col[(size_t)k] + 1);
+      out.AC_v.push_back(out.AC.val[(size_t)k]);
+    }
+  // subdomains (Preconditioner_base.F90:96-123, Decomposition.f90:56-99)
+  out.overlap = c.overlap < 0 ? std::max(c.smoothers, 0) : c.overlap;
+  out.smoothers = c.smoothers;
+  out.levels = c.levels;
+  int np = part ? nparts : out.coarse_full.nagr;
+  out.sd_ptr.assign(1, 0);
+  std::vector<int> onfront((size_t)n, 0), nodes;
+  std::vector<int> loc((size_t)n, 0);
+  for (int p = 1; p <= np; p++) {
+    nodes.clear();
+    if (part) {
+      for (int i = 0; i < n; i++) if ((*part)[(size_t)i] == p) nodes.push_back(i);
+    } else {  // Get_aggregate_nodes (Aggregate_mod.F90:162-190)
+      const Aggregates &ca = out.coarse_full, &fa = out.fine_full;
+      for (int q = ca.starts[(size_t)p - 1]; q < ca.starts[(size_t)p]; q++) {
+        int f = ca.nodes[(size_t)q];
+        for (int t = fa.starts[(size_t)f - 1]; t < fa.starts[(size_t)f]; t++) {
+          int node = fa.nodes[(size_t)t] - 1;
+          if (!loc[(size_t)node]) { loc[(size_t)node] = 1; nodes.push_back(node); }
+        }
+      }
+      for (int v : nodes) loc[(size_t)v] = 0;
+    }
+    for (int v : nodes) onfront[(size_t)v] = -1;
+    size_t lo = 0, hi = nodes.size();
+    for (int layer = 1; layer <= out.overlap; layer++) {
+      // the reference restarts each layer one entry early; that entry's
+      // neighbours are already marked, so the visited order is unchanged
+      for (size_t q = lo; q < hi; q++) {
+        int v = nodes[q];
+        for (int64_t k = A.ptr[(size_t)v]; k < A.ptr[(size_t)v + 1]; k++) {
+          int w = A.col[(size_t)k];
+          if (onfront[(size_t)w] == 0) { onfront[(size_t)w] = layer; nodes.push_back(w); }
+        }
+      }
+      lo = hi;
+      hi = nodes.size();
+    }
+    for (int v : nodes) { onfront[(size_t)v] = 0; out.sd_nodes.push_back(v + 1); }
+    out.sd_ptr.push_back((int64_t)out.sd_nodes.size());
+  }
+  out.A = A;
+  return true;
+}
+
+}  // namespace dg

@@ -1,0 +1,95 @@
+// Host-side setup of DOUG's two-level additive Schwarz preconditioner:
+// control words, assembled input, strength of connection, aggregation,
+// smoothed-aggregation restriction, Galerkin coarse matrix and overlapping
+// subdomains.  This is the reference's np=1 semantics of doug_aggr
+// (src/main/aggr.F90:124-215), restated on a CSR layout.  Everything here is
+// integer / ordering work that the reference does sequentially on one rank;
+// it runs once per matrix, before the GPU solve.
+#pragma once
+#include <cstdint>
+#include <string>
+#include <vector>
+
+namespace dg {
+
+// Shared + master control data (src/utils/globals.F90:85-154); -1 = unset.
+struct Controls {
+  int solver = -1, method = -1, fine_method = -1, num_iters = -1, coarse_method = -1;
+  int num_subdomains = -1, levels = -1, overlap = -1, smoothers = -1, input_type = -1;
+  int grid_size = -1, matrix_type = -1, initial_guess = -1, number_of_blocks = -1;
+  int radius1 = -1, radius2 = -1, minasize1 = -1, minasize2 = -1, maxasize1 = -1, maxasize2 = -1;
+  int debug = -1, verbose = -1, plotting = -1;
+  double strong1 = -1.0, strong2 = -1.0, solve_tolerance = -1.0;
+  int solve_maxiters = -1;
+  bool symmstruct = false, symmnumeric = false;
+  int interpolation_type = -1;
+  std::string assembled_mtx_file, assembled_rhs_file, solution_file;
+  std::string info_file, elemmat_rhs_file, freedom_lists_file, coords_file, freemap_file;
+  int assembled_mtx_format = -1, assembled_rhs_format = -1, solution_format = -1;
+  int start_vec_type = -1;
+  // extensions of this library (not reference control words)
+  double omega = 0.33333333333333;  // prolongator smoother weight (CoarseMtx.F90:64)
+  int precision = 0;                // 0 = FP64 path, 1 = mixed (FP32 factors)
+  int replace_every = 50;           // residual replacement period (mixed path)
+};
+
+// Parse one "name value" line the way util_actionOnCtrlArg does
+// (DOUG_utils.F90:703-1150).  Returns false and fills err on a malformed value.
+bool ctl_apply(Controls &c, const std::string &name, const std::string &value, std::string &err);
+bool ctl_parse_text(Controls &c, const std::string &text, std::string &err);
+void ctl_finish(Controls &c);  // solve_maxiters default (DOUG_utils.F90:676-678)
+bool parse_i10(const std::string &s, int &out);
+bool parse_f10_5(const std::string &s, double &out);
+bool parse_l1(const std::string &s, bool &out);
+
+// Assembled input / vector / solution formats (SpMtx_class.F90:410-617,
+// Vect.F90:840-947, DOUG_utils.F90:1598-1700).
+bool read_assembled(const std::string &path, int format, int &n, std::vector<int> &ii,
+                    std::vector<int> &jj, std::vector<double> &vv, std::string &err);
+bool read_vector(const std::string &path, int format, int n, std::vector<double> &x,
+                 std::string &err);
+bool write_solution(const std::string &path, int format, const double *x, int n,
+                    std::string &err);
+
+// CSR with DOUG's stable row arrangement (entries of a row keep their input order).
+struct Csr {
+  int nrows = 0, ncols = 0;
+  std::vector<int64_t> ptr;
+  std::vector<int> col;
+  std::vector<double> val;
+  int64_t nnz() const { return (int64_t)col.size(); }
+};
+
+struct Aggregates {
+  int nagr = 0;
+  std::vector<int> num;                 // 1-based aggregate per node, 0 = none
+  std::vector<int> starts, nodes;       // 0-based CSR of nodes per aggregate (1-based ids)
+};
+
+struct SetupResult {
+  int n = 0;
+  Csr A;                                // fine matrix after the scale/unscale round trip
+  std::vector<double> rhs;
+  Aggregates fine, fine_full, coarse, coarse_full;
+  Csr R;                                // restriction nagr x n, columns ascending per row
+  Csr P;                                // prolongation n x nagr (= R^T), aggregates ascending
+  Csr AC;                               // coarse matrix after its scale/unscale round trip
+  std::vector<int64_t> sd_ptr;          // subdomain node lists (0-based offsets)
+  std::vector<int> sd_nodes;            // 1-based node ids in DOUG order
+  int overlap = 0, smoothers = 0, levels = 1;
+  double strong1 = 0, strong2 = 0;
+  int r1 = 0, r2 = 0, min1 = 0, max1 = 0, min2 = 0, max2 = 0;
+  // R and AC in the reference's final COO order (for pattern export)
+  std::vector<int> R_i, R_j, AC_i, AC_j;
+  std::vector<double> R_v, AC_v;
+};
+
+// Build everything from 1-based COO triplets (assembled semantics: header
+// swap and 0-based shift already applied by the caller).  part: optional
+// 1-based partition vector (length n) that replaces the coarse-aggregate
+// subdomains.  Returns false with err on a DOUG abort condition.
+bool build_setup(const Controls &c_in, int n, const std::vector<int> &ii,
+                 const std::vector<int> &jj, const std::vector<double> &vv,
+                 const std::vector<int> *part, int nparts, SetupResult &out, std::string &err);
+
+}  // namespace dg

@@ -1,0 +1,160 @@
+"""Seeded synthetic problems in the reference's assembled format.
+
+No public benchmark suite exists for this path, so every workload is
+generated here from a seed:
+
+* ``poisson2d_p1`` -- -Laplace(u) = f on the unit square with P1 triangles on a
+  jittered node grid, each cell split along a random diagonal, homogeneous
+  Dirichlet boundary (boundary nodes removed), f ~ U[-1, 1] per node with a
+  mass-lumped load.  129 x 129 nodes give 16,129 unknowns.
+* ``diffusion3d_fv`` -- -div(kappa grad u) = f on a cell-centred N^3 grid, 7-point
+  finite volumes with harmonic-mean face coefficients, Dirichlet boundary,
+  kappa = exp(g) with g a Gaussian field (std sigma, correlation length `corr`
+  cells, FFT-filtered white noise), f ~ U[-1, 1].  N = 128 gives 2,097,152
+  unknowns and 14,581,760 nonzeros.
+* ``block_partition`` -- the stand-in for a METIS partition of a structured
+  grid: equal boxes of cells, numbered 1..nparts.
+
+Matrices are returned as 1-based COO triplets sorted by row then column, as
+an assembled text file would list them.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+
+def _csr_to_coo1(A):
+    A = A.tocsr()
+    A.sort_indices()
+    rows = np.repeat(np.arange(A.shape[0], dtype=np.int64), np.diff(A.indptr))
+    return (rows + 1).astype(np.int32), (A.indices + 1).astype(np.int32), A.data.astype(np.float64)
+
+
+def poisson2d_p1(nodes: int = 129, jitter: float = 0.2, seed: int = 0):
+    """Returns (n, rows1, cols1, vals, rhs, coords) for the 2-D P1 problem."""
+    import scipy.sparse as sp
+
+    rng = np.random.default_rng(seed)
+    h = 1.0 / (nodes - 1)
+    ii, jj = np.meshgrid(np.arange(nodes), np.arange(nodes), indexing="ij")
+    x = ii * h
+    y = jj * h
+    interior = (ii > 0) & (ii < nodes - 1) & (jj > 0) & (jj < nodes - 1)
+    dx = rng.uniform(-jitter * h, jitter * h, size=x.shape)
+    dy = rng.uniform(-jitter * h, jitter * h, size=y.shape)
+    x = np.where(interior, x + dx, x)
+    y = np.where(interior, y + dy, y)
+    gid = ii * nodes + jj
+    X = x.ravel()
+    Y = y.ravel()
+    c0 = gid[:-1, :-1].ravel()
+    c1 = gid[1:, :-1].ravel()
+    c2 = gid[1:, 1:].ravel()
+    c3 = gid[:-1, 1:].ravel()
+    diag = rng.integers(0, 2, size=c0.shape)  # which diagonal splits the cell
+    t1 = np.where(diag[:, None] == 0, np.stack([c0, c1, c2], 1), np.stack([c0, c1, c3], 1))
+    t2 = np.where(diag[:, None] == 0, np.stack([c0, c2, c3], 1), np.stack([c1, c2, c3], 1))
+    tri = np.concatenate([t1, t2], 0)
+    px = X[tri]
+    py = Y[tri]
+    b = np.stack([py[:, 1] - py[:, 2], py[:, 2] - py[:, 0], py[:, 0] - py[:, 1]], 1)
+    c = np.stack([px[:, 2] - px[:, 1], px[:, 0] - px[:, 2], px[:, 1] - px[:, 0]], 1)
+    area = 0.5 * (px[:, 1] * py[:, 2] - px[:, 2] * py[:, 1] - px[:, 0] * py[:, 2]
+                  + px[:, 2] * py[:, 0] + px[:, 0] * py[:, 1] - px[:, 1] * py[:, 0])
+    area = np.abs(area)
+    K = (b[:, :, None] * b[:, None, :] + c[:, :, None] * c[:, None, :]) / (4.0 * area[:, None, None])
+    R = np.repeat(tri, 3, axis=1).ravel()
+    Cc = np.tile(tri, (1, 3)).ravel()
+    A = sp.coo_matrix((K.ravel(), (R, Cc)), shape=(nodes * nodes,) * 2).tocsr()
+    f = rng.uniform(-1.0, 1.0, size=nodes * nodes)
+    lump = np.zeros(nodes * nodes)
+    np.add.at(lump, tri.ravel(), np.repeat(area / 3.0, 3))
+    load = f * lump
+    keep = np.flatnonzero(interior.ravel())
+    A = A[keep][:, keep]
+    rows1, cols1, vals = _csr_to_coo1(A)
+    coords = np.stack([X[keep], Y[keep]], 1)
+    return len(keep), rows1, cols1, vals, load[keep].copy(), coords
+
+
+def gaussian_field_3d(N: int, sigma: float = 1.0, corr: float = 8.0, seed: int = 0):
+    """Stationary Gaussian field: FFT-filtered white noise with a Gaussian
+    covariance of correlation length `corr` cells, scaled to std `sigma`."""
+    rng = np.random.default_rng(seed)
+    w = rng.standard_normal((N, N, N))
+    k = np.fft.fftfreq(N) * 2.0 * np.pi
+    kx, ky, kz = np.meshgrid(k, k, k, indexing="ij")
+    filt = np.exp(-0.25 * (corr ** 2) * (kx ** 2 + ky ** 2 + kz ** 2))
+    g = np.real(np.fft.ifftn(np.fft.fftn(w) * filt))
+    g -= g.mean()
+    g *= sigma / g.std()
+    return g
+
+
+def diffusion3d_fv(N: int = 128, sigma: float = 1.0, corr: float = 8.0, seed: int = 0):
+    """Returns (n, rows1, cols1, vals, rhs) of the cell-centred 7-point problem."""
+    g = gaussian_field_3d(N, sigma, corr, seed)
+    kap = np.exp(g)
+    rng = np.random.default_rng(seed + 1)
+    f = rng.uniform(-1.0, 1.0, size=N ** 3)
+    idx = np.arange(N ** 3, dtype=np.int64).reshape(N, N, N)
+    diag = np.zeros((N, N, N))
+    rows, cols, vals = [], [], []
+    for ax in range(3):
+        a = [slice(None)] * 3
+        b = [slice(None)] * 3
+        a[ax] = slice(0, N - 1)
+        b[ax] = slice(1, N)
+        ka = kap[tuple(a)]
+        kb = kap[tuple(b)]
+        t = 2.0 * ka * kb / (ka + kb)           # harmonic mean face coefficient
+        diag[tuple(a)] += t
+        diag[tuple(b)] += t
+        ia = idx[tuple(a)].ravel()
+        ib = idx[tuple(b)].ravel()
+        rows += [ia, ib]
+        cols += [ib, ia]
+        vals += [-t.ravel(), -t.ravel()]
+        # Dirichlet faces: half-cell distance gives 2 kappa
+        lo = [slice(None)] * 3
+        hi = [slice(None)] * 3
+        lo[ax] = 0
+        hi[ax] = N - 1
+        diag[tuple(lo)] += 2.0 * kap[tuple(lo)]
+        diag[tuple(hi)] += 2.0 * kap[tuple(hi)]
+    rows.append(idx.ravel())
+    cols.append(idx.ravel())
+    vals.append(diag.ravel())
+    r = np.concatenate(rows)
+    c = np.concatenate(cols)
+    v = np.concatenate(vals)
+    order = np.lexsort((c, r))
+    r, c, v = r[order], c[order], v[order]
+    return N ** 3, (r + 1).astype(np.int32), (c + 1).astype(np.int32), v, f
+
+
+def block_partition(N: int, parts_per_dim: int, dim: int = 3):
+    """1-based ids of equal boxes of an N^dim grid (row-major cell order)."""
+    b = np.arange(N) * parts_per_dim // N
+    if dim == 2:
+        I, J = np.meshgrid(b, b, indexing="ij")
+        p = I * parts_per_dim + J
+    else:
+        I, J, K = np.meshgrid(b, b, b, indexing="ij")
+        p = (I * parts_per_dim + J) * parts_per_dim + K
+    return (p.ravel() + 1).astype(np.int32)
+
+
+def laplace2d(m: int):
+    """5-point Laplacian on an m x m grid (the reference's LapNxN fixtures)."""
+    n = m * m
+    r, c, v = [], [], []
+    for i in range(m):
+        for j in range(m):
+            k = i * m + j
+            r.append(k); c.append(k); v.append(4.0)
+            for di, dj in ((-1, 0), (1, 0), (0, -1), (0, 1)):
+                a, b = i + di, j + dj
+                if 0 <= a < m and 0 <= b < m:
+                    r.append(k); c.append(a * m + b); v.append(-1.0)
+    return n, np.array(r, np.int32) + 1, np.array(c, np.int32) + 1, np.array(v), np.ones(n)

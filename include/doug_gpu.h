@@ -1,0 +1,125 @@
+/*
+ * doug_gpu.h -- C ABI of the GB300 solve path for DOUG
+ * (Domain decomposition On Unstructured Grids).
+ *
+ * One handle = one linear system A x = b and its two-level additive Schwarz
+ * preconditioner (overlapping subdomain solves + smoothed-aggregation coarse
+ * grid), solved by preconditioned conjugate gradients on one GPU.  All
+ * pointers are plain host pointers unless the name says "device"; sizes are
+ * ints; no call aborts the process: every call returns a dg_status and
+ * dg_last_error() gives the message.  Handles are independent (no global
+ * state), one handle per host thread.
+ *
+ * The entry points replace the following pieces of the reference (paths
+ * relative to the DOUG source tree):
+ *   dg_load_ctl / dg_set_option  -> CtrlData_initFromFile, util_actionOnCtrlArg
+ *                                   (src/utils/DOUG_utils.F90:629-1150)
+ *   dg_set_matrix_coo / dg_set_rhs -> ReadInSparseAssembled, Vect_ReadFromFile,
+ *                                   parallelDistributeAssembledInput
+ *                                   (src/datatypes/SpMtx/SpMtx_class.F90:410-453,
+ *                                    src/datatypes/Vect.F90:840-947,
+ *                                    src/components/Distribution_assm.F90:49-102)
+ *   dg_set_partition             -> the partition import of the debug 4321
+ *                                   path (src/components/Distribution_assm.F90:202-215)
+ *   dg_setup                     -> Partitionings_aggr_InitFine/InitCoarse,
+ *                                   CoarsePreconditioner_smooth_Init,
+ *                                   FinePreconditioner_Init
+ *                                   (src/main/aggr.F90:131-226)
+ *   dg_solve / dg_solve_device   -> pcg_weigs (src/solvers/pcg.F90:289-462), including
+ *                                   the lazy factorisations (src/solvers/subsolvers.F90:78-163)
+ *   dg_write_solution            -> WriteSolutionToFile (src/utils/DOUG_utils.F90:1598-1700)
+ *   dg_get_*                     -> parity export of aggregates, subdomains, R, AC
+ *   the handle as a whole        -> the stale C extension API src/ext/C/doug_ext.h:4-13
+ *                                   (opaque handles, caller-owned buffers), with size
+ *                                   queries so callers never hard-code sizes.
+ */
+#ifndef DOUG_GPU_H
+#define DOUG_GPU_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct dg_handle dg_handle;
+
+typedef enum {
+  DG_OK = 0,
+  DG_NOT_CONVERGED = 1,   /* maxit reached before the tolerance */
+  DG_BREAKDOWN = 2,       /* p.q <= 0 or a NaN in the CG recurrences */
+  DG_SINGULAR = 3,        /* a subdomain or coarse matrix is not positive definite */
+  DG_BAD_INPUT = 4,       /* malformed control word, file or argument */
+  DG_CUDA_ERROR = 5,      /* a CUDA call failed */
+  DG_NO_DEVICE = 6,       /* no CUDA device */
+  DG_NOT_READY = 7        /* call order: e.g. dg_solve before dg_setup */
+} dg_status;
+
+typedef struct {
+  int iterations;             /* PCG iterations */
+  double init_norm;           /* ||b - A x0||_2 */
+  double final_norm;          /* ||r_k||_2 of the recurrence */
+  double true_rel_residual;   /* ||b - A x||_2 / ||b - A x0||_2 (FP64 recomputed) */
+  double cond_num;            /* Lanczos estimate lambda_max / lambda_min */
+  double t_setup_s;           /* host setup: aggregation, R, AC, symbolic analysis */
+  double t_factor_s;          /* GPU numeric factorisations (subdomains + coarse) */
+  double t_iterate_s;         /* GPU PCG iterations */
+  double t_total_s;           /* factor + iterate (time to tolerance) */
+  int n;                      /* unknowns */
+  int nsubdomains;
+  int ncoarse;                /* coarse unknowns (fine aggregates) */
+  int gpu_launches;           /* kernels launched by the last solve */
+  long long factor_nnz;       /* stored factor entries (subdomains) */
+  double factor_gflop;        /* partial-Cholesky flops of the subdomain factors */
+} dg_stats;
+
+dg_status dg_create(dg_handle **h);
+void dg_destroy(dg_handle *h);
+const char *dg_last_error(const dg_handle *h);
+
+/* Control words, same names and parsing as a DOUG control file ("name value";
+ * the first value given for a name wins, as in the reference).  Extension
+ * words of this library: precision (0 = FP64, 1 = mixed FP32 subdomain
+ * factors with flexible CG and FP64 residual replacement), replace_every,
+ * omega (prolongator smoother weight; the reference hard-codes 1/3). */
+dg_status dg_set_option(dg_handle *h, const char *name, const char *value);
+/* Parse a control file and read the input files it names (assembled
+ * matrix + optional RHS; relative names resolve against the file's folder). */
+dg_status dg_load_ctl(dg_handle *h, const char *path);
+
+/* Assembled matrix as 1-based COO triplets in any order (0-based accepted,
+ * as in the reference's reader); duplicates are summed. */
+dg_status dg_set_matrix_coo(dg_handle *h, int n, int nnz, const int *rows, const int *cols,
+                            const double *vals);
+/* Right-hand side (n values); without one, b = 1 as in the reference. */
+dg_status dg_set_rhs(dg_handle *h, const double *b);
+/* Optional subdomain partition: part[i] in 1..nparts for every unknown.
+ * Replaces the coarse-aggregate subdomains of the one-process path. */
+dg_status dg_set_partition(dg_handle *h, const int *part, int nparts);
+
+/* Aggregation, restriction, coarse matrix, subdomains, symbolic analysis and
+ * device upload.  Must follow the matrix. */
+dg_status dg_setup(dg_handle *h);
+
+/* Solve with host buffers (b may be NULL: the stored RHS is used).  x must
+ * hold n doubles.  stats may be NULL. */
+dg_status dg_solve(dg_handle *h, const double *b, double *x, dg_stats *stats);
+/* Same with device pointers on the given CUDA stream (NULL: default stream). */
+dg_status dg_solve_device(dg_handle *h, const double *d_b, double *d_x, dg_stats *stats,
+                          void *cuda_stream);
+/* Write x with the control file's solution_file / solution_format. */
+dg_status dg_write_solution(dg_handle *h, const double *x);
+
+/* Size queries and parity export (1-based ids as in the reference). */
+dg_status dg_get_sizes(const dg_handle *h, int *n, int *nagr_fine, int *nagr_coarse,
+                       int *nsubdomains, long long *subdomain_total, int *R_nnz, int *AC_nnz);
+dg_status dg_get_aggregates(const dg_handle *h, int *fine_num /* n */,
+                            int *coarse_num /* nagr_fine */);
+dg_status dg_get_subdomains(const dg_handle *h, long long *starts /* nsubd+1 */,
+                            int *nodes /* subdomain_total */);
+/* R and AC in the reference's final entry order (COO, 1-based). */
+dg_status dg_get_restriction(const dg_handle *h, int *ri, int *rj, double *rv);
+dg_status dg_get_coarse_matrix(const dg_handle *h, int *ci, int *cj, double *cv);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -673,7 +673,12 @@ static void spm_aggregate(spm *A, aggrs *inner, aggrs *full, int neighood,
   maxasize = maxaggrsize;
   if (alpha >= 0 || sn * sn != n) {
     if (!A->srow) spm_build_refs_symm(A);
-    int *stat = NEWI(n), *nodes = NEWI(n), *distance = NEWI(n);
+    /* nodes(n) in the reference; a node next to two rounder nodes is queued
+     * twice (the rounder-neighbour scan does not mark it), so on small graphs
+     * the list can outgrow n and the Fortran writes past the array end.  A
+     * longer array gives that write somewhere to land. */
+    int nodes_cap = 4 * n + 64;
+    int *stat = NEWI(n), *nodes = NEWI(nodes_cap), *distance = NEWI(n);
     if (!coarse) maxasizelargest = maxasize + 4 * (2 * neighood);
     else maxasizelargest = 3 * maxasize;
     if (!coarse) g_beta = alpha / 4.0;
@@ -684,7 +689,7 @@ static void spm_aggregate(spm *A, aggrs *inner, aggrs *full, int neighood,
     memset(&c, 0, sizeof c);
     c.neighood = neighood; c.minasize = minasize; c.maxasize = maxasize;
     c.stat = stat; c.distance = distance; c.rowstart = A->srow;
-    c.colnrs = A->scol; c.nodes = nodes; c.nodes_cap = n;
+    c.colnrs = A->scol; c.nodes = nodes; c.nodes_cap = nodes_cap;
     while (firstwocol <= n) {
       int startnode, nneigs, ok, mindistance, nouters, next_start_layer;
       if (ngoodstarts > 0) {

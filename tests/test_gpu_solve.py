@@ -1,0 +1,137 @@
+"""GPU parity of the solve path against the oracle and the reference's fixtures.
+
+Bars (FP64 path): solution within relative 1e-10 of the oracle's, iteration
+count within +-1, and the reference harness rule ||x - x_ref||_2 <= 1e-6 on
+its fixtures.  Mixed path: error against the FP64 direct solve <= 1e-7
+relative at tolerance 1e-10.
+"""
+import os
+
+import numpy as np
+import pytest
+
+import oracle as O
+import doug_gb300 as D
+from doug_gb300 import problems as P
+
+from conftest import GOLDEN
+
+pytestmark = pytest.mark.gpu
+
+
+def _ctl_text(d):
+    return "".join(f"{k} {v}\n" for k, v in d.items())
+
+
+def _solve(n, r, c, v, b, opts, part=None, precision=0):
+    s = D.DougSolver(opts)
+    if precision:
+        s.set_option("precision", precision)
+    s.set_matrix_coo(n, r, c, v)
+    s.set_rhs(b)
+    if part is not None:
+        s.set_partition(part)
+    s.setup()
+    return s.solve(allow_not_converged=False)
+
+
+@pytest.mark.parametrize("levels,smoothers,overlap",
+                         [(2, s, o) for s in (0, 1, 2) for o in (-1, 0)] + [(1, 0, o) for o in (-1, 0, 1, 2)])
+def test_lap16x16_fixture(levels, smoothers, overlap):
+    opts = dict(solver=2, method=1, fine_method=1, levels=levels, smoothers=smoothers, overlap=overlap)
+    s = D.DougSolver(opts)
+    s.load_ctl(os.path.join(GOLDEN, "lap16x16", "DOUG.ctl"))
+    s.setup()
+    x, st = s.solve()
+    ref = O.read_vector(os.path.join(GOLDEN, "lap16x16", "csolution.xdr"), 2, 225)
+    assert np.linalg.norm(x - ref) <= 1e-6
+    assert np.linalg.norm(x - ref) <= 1e-9
+    ro = O.run_ctl(os.path.join(GOLDEN, "lap16x16", "DOUG.ctl"), _ctl_text(opts))
+    assert abs(st.iterations - ro["iterations"]) <= 1
+    assert np.linalg.norm(x - ro["x"]) <= 1e-10 * np.linalg.norm(ro["x"])
+    assert st.gpu_launches > 0
+
+
+def test_lap4x4_fixture():
+    opts = dict(solver=2, method=1, fine_method=1, levels=2, smoothers=0, overlap=-1)
+    s = D.DougSolver(opts)
+    s.load_ctl(os.path.join(GOLDEN, "lap4x4", "DOUG.ctl"))
+    s.setup()
+    x, st = s.solve()
+    ref = O.read_vector(os.path.join(GOLDEN, "lap4x4", "solution_correct.dat"), 1, 9)
+    assert np.linalg.norm(x - ref) <= 1e-12
+
+
+CFG0 = dict(solver=2, method=1, fine_method=1, levels=2, overlap=1, smoothers=1, strong1="0.08",
+            radius1=2, solve_tolerance="1.0e-8", solve_maxiters=1000)
+
+
+@pytest.mark.parametrize("seed", [0, 1])
+def test_poisson2d_fp64_matches_oracle(seed):
+    n, r, c, v, b, _ = P.poisson2d_p1(129 if seed == 0 else 65, seed=seed)
+    x, st = _solve(n, r, c, v, b, CFG0)
+    ro = O.run_coo(n, r, c, v, rhs=b, ctl=_ctl_text(CFG0))
+    assert ro["status"] == 0
+    assert abs(st.iterations - ro["iterations"]) <= 1
+    assert np.linalg.norm(x - ro["x"]) <= 1e-10 * np.linalg.norm(ro["x"]) * max(1, ro["iterations"] / 10)
+    assert st.true_rel_residual <= 1.01e-8
+
+
+def test_diffusion3d_partition_fp64_matches_oracle():
+    N = 20
+    n, r, c, v, b = P.diffusion3d_fv(N, seed=2)
+    part = P.block_partition(N, 2)
+    opts = dict(solver=2, method=1, fine_method=1, levels=2, overlap=2, smoothers=1, strong1="0.08",
+                radius1=2, solve_tolerance="1.0e-8", solve_maxiters=1000)
+    x, st = _solve(n, r, c, v, b, opts, part=part)
+    ro = O.run_coo(n, r, c, v, rhs=b, ctl=_ctl_text(opts), part=part)
+    assert ro["status"] == 0
+    assert abs(st.iterations - ro["iterations"]) <= 1
+    assert np.linalg.norm(x - ro["x"]) <= 1e-9 * np.linalg.norm(ro["x"])
+
+
+def test_mixed_precision_error_vs_direct_solve():
+    n, r, c, v, b, _ = P.poisson2d_p1(97, seed=4)
+    opts = dict(CFG0, solve_tolerance="1.0e-10")
+    x, st = _solve(n, r, c, v, b, opts, precision=1)
+    xd = O.spd_solve(n, r - 1, c - 1, v, b)
+    assert st.true_rel_residual <= 1.0e-10 * 1.01
+    assert np.linalg.norm(x - xd) <= 1e-7 * np.linalg.norm(xd)
+
+
+def test_not_spd_reports_singular():
+    n, r, c, v, b = P.laplace2d(10)
+    v = v.copy()
+    v[(r == c) & (r == 37)] = -4.0   # indefinite diagonal entry
+    s = D.DougSolver(dict(solver=2, method=1, fine_method=1, levels=2, overlap=1, smoothers=1,
+                          strong1="0.08", radius1=2, solve_tolerance="1.0e-8"))
+    s.set_matrix_coo(n, r, c, v)
+    s.setup()
+    with pytest.raises(D.DougError) as e:
+        s.solve()
+    assert e.value.status in (D.DG_SINGULAR, D.DG_BREAKDOWN)
+
+
+def test_maxit_reports_not_converged():
+    n, r, c, v, b, _ = P.poisson2d_p1(65, seed=0)
+    opts = dict(CFG0, solve_maxiters=2, solve_tolerance="1.0e-12")
+    s = D.DougSolver(opts)
+    s.set_matrix_coo(n, r, c, v)
+    s.setup()
+    x, st = s.solve(allow_not_converged=True)
+    assert st.status == D.DG_NOT_CONVERGED and st.iterations == 2
+
+
+def test_device_pointer_entry_matches_host_entry():
+    torch = pytest.importorskip("torch")
+    n, r, c, v, b, _ = P.poisson2d_p1(65, seed=3)
+    s = D.DougSolver(CFG0)
+    s.set_matrix_coo(n, r, c, v)
+    s.setup()
+    xh, _ = s.solve(b)
+    bd = torch.tensor(b, dtype=torch.float64, device="cuda")
+    xd = torch.empty_like(bd)
+    st = s.solve_device(bd.data_ptr(), xd.data_ptr(), torch.cuda.current_stream().cuda_stream)
+    torch.cuda.synchronize()
+    assert np.array_equal(xd.cpu().numpy(), xh)
+    assert st.iterations > 0
