@@ -1,0 +1,372 @@
+#!/usr/bin/env python
+"""Benchmark of the GB300 DOUG solve path.
+
+Metric: time to relative residual 1e-8 (seconds per solve) on the 128^3
+log-normal diffusion problem (2,097,152 unknowns, 14,581,760 nonzeros;
+kappa = exp(g), g Gaussian with std 1 and correlation length 8 cells),
+two-level additive Schwarz with 64 subdomains (4x4x4 boxes of the grid, the
+stand-in for a METIS partition), overlap 2 and a smoothed-aggregation coarse
+grid, solved by PCG on one GB300.
+
+A step is one complete solve from a right-hand side already in HBM: the
+numeric factorisations of the 64 subdomain matrices and of the coarse matrix,
+then PCG to ||r||/||r0|| <= 1e-8.  The headline `value` is the mixed-precision
+solve (FP32 subdomain factors and solves, flexible CG with FP64 recurrences,
+FP64 residual replacement, FP64 coarse Cholesky); the plain FP64 solve of the
+same system is timed beside it (`fp64_s`, `mixed_vs_fp64`).
+
+Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+Under torchrun each rank solves its own replica (the path does not shard
+across GPUs here: replicas only); rank 0 prints one JSON line.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+N = 128
+PARTS_PER_DIM = 4
+SEED = 0
+TOL = "1.0e-8"
+CTL = dict(solver=2, method=1, fine_method=1, levels=2, overlap=2, smoothers=1,
+           strong1="0.08", radius1=3, maxasize1=125, solve_tolerance=TOL, solve_maxiters=2000)
+METRIC = "time to rel. residual 1e-8 (s), mixed+batched vs plain FP64 PCG, 1 GB300"
+WORKLOAD = ("128^3 log-normal diffusion (sigma 1, corr. length 8), 7-point FV, 2,097,152 unknowns; "
+            "PCG + 2-level additive Schwarz: 64 subdomains (4x4x4 boxes), overlap 2, "
+            "smoothed-aggregation coarse grid")
+
+
+def _peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle sampling during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def _problem():
+    from doug_gb300 import problems as P
+    n, r, c, v, b = P.diffusion3d_fv(N, sigma=1.0, corr=8.0, seed=SEED)
+    part = P.block_partition(N, PARTS_PER_DIM)
+    return n, r, c, v, b, part
+
+
+def _solver(n, r, c, v, b, part, precision):
+    import doug_gb300 as D
+    s = D.DougSolver(CTL)
+    s.set_option("precision", precision)
+    s.set_matrix_coo(n, r, c, v)
+    s.set_rhs(b)
+    s.set_partition(part)
+    s.setup()
+    return s
+
+
+def _subdomain_sample(n, r, c, v, part, box=(1, 1, 1)):
+    """Index set of one interior subdomain (its box plus two overlap layers)
+    and its principal submatrix, 0-based COO."""
+    import scipy.sparse as sp
+    A = sp.csr_matrix((v, (r - 1, c - 1)), shape=(n, n))
+    pid = (box[0] * PARTS_PER_DIM + box[1]) * PARTS_PER_DIM + box[2] + 1
+    inds = np.flatnonzero(part == pid)
+    mask = np.zeros(n, bool)
+    mask[inds] = True
+    pat = A.copy()
+    pat.data[:] = 1.0
+    for _ in range(int(CTL["overlap"])):  # overlap layers over the matrix graph (Add_layers)
+        mask = mask | ((pat @ mask.astype(np.float64)) != 0)
+    idx = np.flatnonzero(mask)
+    S = A[idx][:, idx].tocoo()
+    return len(idx), S.row, S.col, S.data
+
+
+def _oracle_sample_worker(args):
+    m, rows, cols, vals, nsolves = args
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    rng = np.random.default_rng(0)
+    b = rng.uniform(-1, 1, m)
+    t0 = time.perf_counter()
+    f = O.SpdFactor(m, rows, cols, vals)
+    t1 = time.perf_counter()
+    for _ in range(nsolves):
+        f.solve(b)
+    t2 = time.perf_counter()
+    return t1 - t0, t2 - t1
+
+
+def cpu_sample(n, r, c, v, part, iterations, workers=1):
+    """Time the oracle's exact subdomain factor + `iterations` subdomain solves
+    for `workers` subdomains in parallel processes, and scale to the 64
+    subdomains of the workload."""
+    import multiprocessing as mp
+    m, sr, sc, sv = _subdomain_sample(n, r, c, v, part)
+    nsd = PARTS_PER_DIM ** 3
+    t0 = time.perf_counter()
+    if workers <= 1:
+        tf, ts = _oracle_sample_worker((m, sr, sc, sv, iterations))
+        wall = tf + ts
+    else:
+        ctx = mp.get_context("spawn")
+        with ctx.Pool(workers) as pool:
+            res = pool.map(_oracle_sample_worker, [(m, sr, sc, sv, iterations)] * workers)
+        wall = time.perf_counter() - t0
+        tf = max(x[0] for x in res)
+        ts = max(x[1] for x in res)
+    est = wall * (-(-nsd // workers))
+    sample = (f"interior subdomain (box + 2 overlap layers, {m} unknowns) of the 64: oracle "
+              f"exact factorisation + {iterations} subdomain solves on {workers} core(s) "
+              f"{'in parallel' if workers > 1 else ''}, x{-(-nsd // workers)} for 64 subdomains; "
+              f"coarse solve, SpMV and vector work omitted (a lower bound of the CPU solve)")
+    return est, {"factor_s": tf, "solves_s": ts, "wall_s": wall}, sample
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return 0
+    n, r, c, v, b, part = _problem()
+    iterations = int(os.environ.get("DG_REF_ITERS", "60"))
+    workers = max(1, min(os.cpu_count() or 1, 16))
+    # warm-up: a small sample (loads and builds the oracle)
+    for _ in range(max(1, min(args.warmup, 1))):
+        cpu_sample_small = _oracle_sample_worker((8, np.arange(8), np.arange(8), np.ones(8), 1))
+        del cpu_sample_small
+    vals = []
+    info = None
+    for _ in range(args.steps):
+        est, info, sample = cpu_sample(n, r, c, v, part, iterations, workers)
+        vals.append(est)
+    value = float(np.mean(vals))
+    line = {"metric": METRIC, "value": value, "unit": "s", "impl": "reference", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": value * 1e3,
+            "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded)", "config": {"workload": WORKLOAD, "sample": "see cpu_baseline"},
+            "cpu_baseline": {"value": value, "unit": "s", "cores": workers, "kind": "port",
+                             "sample": sample, "detail": info},
+            "e2e": {"value": value, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_gpu(args, rank, world):
+    import torch
+    import doug_gb300 as D
+
+    D.build_library()
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(dev)
+    n, r, c, v, b, part = _problem()
+    stream = torch.cuda.current_stream()
+    sptr = stream.cuda_stream
+
+    # ---- mixed precision (headline) ----
+    t0 = time.perf_counter()
+    sm = _solver(n, r, c, v, b, part, precision=1)
+    setup_s = time.perf_counter() - t0
+    bd = torch.tensor(b, dtype=torch.float64, device="cuda")
+    xd = torch.empty_like(bd)
+    for _ in range(args.warmup):
+        st = sm.solve_device(bd.data_ptr(), xd.data_ptr(), sptr)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    launches = 0
+    its = []
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(dev) as clk:
+        e0.record(stream)
+        for _ in range(args.steps):
+            st = sm.solve_device(bd.data_ptr(), xd.data_ptr(), sptr)
+            launches += st.gpu_launches
+            its.append(st.iterations)
+        e1.record(stream)
+        torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    t_mixed = e0.elapsed_time(e1) * 1e-3 / args.steps
+    if world > 1:
+        tt = torch.tensor([t_mixed], device="cuda", dtype=torch.float64)
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        t_mixed = float(tt.item())
+    last = st
+    # accuracy of the mixed solve against the FP64 path (below)
+    x_mixed = xd.cpu().numpy()
+
+    # ---- end to end through the host-buffer API (pinned host memory) ----
+    bh = torch.tensor(b, dtype=torch.float64).pin_memory()
+    xh = torch.empty(n, dtype=torch.float64).pin_memory()
+    import ctypes
+    L = D.load_library()
+    stats = D._Stats()
+    e2e = []
+    for _ in range(args.steps):
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        rc = L.dg_solve(sm._h, ctypes.cast(bh.data_ptr(), ctypes.POINTER(ctypes.c_double)),
+                        ctypes.cast(xh.data_ptr(), ctypes.POINTER(ctypes.c_double)), ctypes.byref(stats))
+        e2e.append(time.perf_counter() - t)
+        assert rc == D.DG_OK, L.dg_last_error(sm._h)
+    t_e2e = float(np.mean(e2e))
+
+    # ---- phase profile of one extra solve (not timed) ----
+    sm.set_option("profile", 1)
+    prof = sm.solve_device(bd.data_ptr(), xd.data_ptr(), sptr)
+    sm.set_option("profile", 0)
+    del sm
+    torch.cuda.empty_cache()
+
+    # ---- plain FP64 path ----
+    sf = _solver(n, r, c, v, b, part, precision=0)
+    for _ in range(1):
+        sf.solve_device(bd.data_ptr(), xd.data_ptr(), sptr)
+    f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    f0.record(stream)
+    for _ in range(args.fp64_steps):
+        stf = sf.solve_device(bd.data_ptr(), xd.data_ptr(), sptr)
+    f1.record(stream)
+    torch.cuda.synchronize()
+    t_fp64 = f0.elapsed_time(f1) * 1e-3 / args.fp64_steps
+    x64 = xd.cpu().numpy()
+    err_mixed_vs_fp64 = float(np.linalg.norm(x_mixed - x64) / np.linalg.norm(x64))
+    del sf
+
+    if rank != 0:
+        return 0
+    hbm, peak_kind = _peaks()
+    # roofline of the dominant kernel group: the subdomain triangular solves
+    # (multifrontal forward + backward over all levels), HBM-bound
+    per_solve_s = prof.t_subsolve_s / max(prof.iterations, 1)
+    achieved = prof.subsolve_bytes / per_solve_s / 1e9 if per_solve_s > 0 else None
+    roofline = {"kernel": "mf_fwd_level+mf_bwd_level (FP32 subdomain solves, all levels)",
+                "bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                "frac": (achieved / hbm) if achieved else None, "traffic": None,
+                "peak_source": f"{peak_kind} hbm_gbs",
+                "bytes_per_launch_group": prof.subsolve_bytes, "launch_group_s": per_solve_s}
+    phases = {"factor_s": prof.t_factor_s, "iterate_s": prof.t_iterate_s,
+              "subsolve_s": prof.t_subsolve_s, "coarse_s": prof.t_coarse_s, "spmv_s": prof.t_spmv_s,
+              "spmv_GBps": (prof.spmv_bytes * prof.iterations / prof.t_spmv_s / 1e9) if prof.t_spmv_s else None}
+    cpu = None
+    if not args.no_cpu_baseline:
+        est, info, sample = cpu_sample(n, r, c, v, part, last.iterations, workers=1)
+        cpu = {"value": est, "unit": "s", "cores": 1, "kind": "port", "sample": sample, "detail": info}
+    clocks = clk.summary()
+    line = {
+        "metric": METRIC, "value": t_mixed, "unit": "s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": t_mixed * 1e3, "higher_is_better": False,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64 outer / f32 subdomain factors",
+        "data": "synthetic (seeded generator, doug_gb300/problems.py)",
+        "config": {"workload": WORKLOAD, "n": n, "nnz": int(len(v)), "subdomains": last.nsubdomains,
+                   "coarse_unknowns": last.ncoarse, "controls": CTL,
+                   "l2": "working set (factors ~2 GB) far larger than the 129 MB L2; no flush needed",
+                   "parallelism": "replicas" if world > 1 else "1 GPU"},
+        "iterations": last.iterations, "true_rel_residual": last.true_rel_residual,
+        "fp64_s": t_fp64, "fp64_iterations": stf.iterations, "mixed_vs_fp64": t_mixed / t_fp64,
+        "mixed_rel_err_vs_fp64_solution": err_mixed_vs_fp64,
+        "setup_host_s": setup_s, "phases_mixed": phases,
+        "e2e": {"value": t_e2e, "unit": "s", "h2d_bytes_per_step": 8 * n, "d2h_bytes_per_step": 8 * n,
+                "api": "dg_solve (host buffers, pinned)"},
+        "roofline": roofline, "cpu_baseline": cpu, "clocks": clocks,
+        "gpu_launches": int(launches),
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--fp64-steps", type=int, default=1)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        backend = "nccl" if args.impl == "gb300" else "gloo"
+        if args.impl == "gb300":
+            torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+        dist.init_process_group(backend)
+    if args.impl == "reference":
+        rc = run_reference(args, rank, world)
+    else:
+        rc = run_gpu(args, rank, world)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+    return rc
+
+
+if __name__ == "__main__":
+    sys.exit(main())

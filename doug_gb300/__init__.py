@@ -53,7 +53,9 @@ class _Stats(C.Structure):
                 ("t_setup_s", C.c_double), ("t_factor_s", C.c_double), ("t_iterate_s", C.c_double),
                 ("t_total_s", C.c_double), ("n", C.c_int), ("nsubdomains", C.c_int),
                 ("ncoarse", C.c_int), ("gpu_launches", C.c_int), ("factor_nnz", C.c_longlong),
-                ("factor_gflop", C.c_double)]
+                ("factor_gflop", C.c_double), ("t_subsolve_s", C.c_double),
+                ("subsolve_bytes", C.c_double), ("t_coarse_s", C.c_double),
+                ("coarse_bytes", C.c_double), ("t_spmv_s", C.c_double), ("spmv_bytes", C.c_double)]
 
 
 @dataclass
@@ -74,6 +76,12 @@ class SolveStats:
     gpu_launches: int
     factor_nnz: int
     factor_gflop: float
+    t_subsolve_s: float = 0.0
+    subsolve_bytes: float = 0.0
+    t_coarse_s: float = 0.0
+    coarse_bytes: float = 0.0
+    t_spmv_s: float = 0.0
+    spmv_bytes: float = 0.0
 
 
 _lib = None
@@ -210,7 +218,8 @@ class DougSolver:
         return SolveStats(rc, st.iterations, st.init_norm, st.final_norm, st.true_rel_residual,
                           st.cond_num, st.t_setup_s, st.t_factor_s, st.t_iterate_s, st.t_total_s,
                           st.n, st.nsubdomains, st.ncoarse, st.gpu_launches, st.factor_nnz,
-                          st.factor_gflop)
+                          st.factor_gflop, st.t_subsolve_s, st.subsolve_bytes, st.t_coarse_s,
+                          st.coarse_bytes, st.t_spmv_s, st.spmv_bytes)
 
     # --- parity export ----------------------------------------------------
     def sizes(self) -> dict:

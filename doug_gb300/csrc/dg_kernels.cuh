@@ -196,21 +196,279 @@ mf_factor_level(MfView v, const int *__restrict__ fronts, const double *__restri
   }
 }
 
+// Small fronts: the whole m x m front lives in shared memory while it is
+// assembled and factored, then its lower part is written back.
+constexpr int kSmallThreads = 128;
+
+template <typename T>
+__global__ void __launch_bounds__(kSmallThreads)
+mf_factor_small(MfView v, const int *__restrict__ fronts, const double *__restrict__ vals,
+                T *__restrict__ arena, int *__restrict__ status) {
+  extern __shared__ unsigned char smem_raw[];
+  T *S = reinterpret_cast<T *>(smem_raw);
+  const int f = fronts[blockIdx.x];
+  const int m = v.f_m[f], k = v.f_k[f];
+  const int64_t off = v.f_off[f];
+  const int tid = threadIdx.x, nt = kSmallThreads;
+  for (int q = tid; q < m * m; q += nt) S[q] = T(0);
+  __syncthreads();
+  for (int64_t e = v.f_asm[f] + tid; e < v.f_asm[f + 1]; e += nt) {
+    double sv = 0.0;
+    for (int64_t q = v.asm_sp[e]; q < v.asm_sp[e + 1]; q++) sv += vals[v.asm_src[q]];
+    S[v.asm_tgt[e] - off] = (T)sv;
+  }
+  __syncthreads();
+  for (int ci = v.f_child_ptr[f]; ci < v.f_child_ptr[f + 1]; ci++) {
+    const int c = v.f_children[ci];
+    const int mc = v.f_m[c], kc = v.f_k[c], rc = mc - kc;
+    const T *U = arena + v.f_off[c] + (int64_t)kc * mc + kc;
+    const int *rel = v.relmap + v.f_relmap[c];
+    for (int q = tid; q < rc * rc; q += nt) {
+      const int b = q / rc, a = q % rc;
+      if (a >= b) S[rel[b] * m + rel[a]] += U[(int64_t)b * mc + a];
+    }
+    __syncthreads();
+  }
+  for (int j = 0; j < k; j++) {
+    if (tid == 0) {
+      T d = S[j * m + j];
+      if (!(d > T(0))) { atomicOr(status, ERR_NOT_SPD); d = T(1); }
+      S[j * m + j] = tsqrt<T>(d);
+    }
+    __syncthreads();
+    const T p = S[j * m + j];
+    for (int i = j + 1 + tid; i < m; i += nt) S[j * m + i] /= p;
+    __syncthreads();
+    const int r = m - j - 1;
+    for (int q = tid; q < r * r; q += nt) {
+      const int c = j + 1 + q / r, i = j + 1 + q % r;
+      if (i >= c) S[c * m + i] -= S[j * m + i] * S[j * m + c];
+    }
+    __syncthreads();
+  }
+  T *F = arena + off;
+  for (int q = tid; q < m * m; q += nt) {
+    const int c = q / m, i = q % m;
+    if (i >= c) F[q] = S[q];
+  }
+}
+
+// ---------------------------------------------------------------------------
+// large fronts: assembly by column chunks, then for every panel step one
+// launch that factors the panels and one that applies the trailing update
+// tile by tile, so that one front occupies many SMs.
+// ---------------------------------------------------------------------------
+constexpr int kAsmCols = 64;
+
+__device__ __forceinline__ int64_t lower_bound64(const int64_t *a, int64_t lo, int64_t hi, int64_t key) {
+  while (lo < hi) {
+    int64_t mid = (lo + hi) >> 1;
+    if (a[mid] < key) lo = mid + 1; else hi = mid;
+  }
+  return lo;
+}
+__device__ __forceinline__ int lower_bound32(const int *a, int lo, int hi, int key) {
+  while (lo < hi) {
+    int mid = (lo + hi) >> 1;
+    if (a[mid] < key) lo = mid + 1; else hi = mid;
+  }
+  return lo;
+}
+
+// task = {front, first column of the chunk}
+template <typename T>
+__global__ void __launch_bounds__(kMfThreads)
+mf_assemble_large(MfView v, const int2 *__restrict__ tasks, const double *__restrict__ vals,
+                  T *__restrict__ arena) {
+  const int f = tasks[blockIdx.x].x, c0 = tasks[blockIdx.x].y;
+  const int m = v.f_m[f];
+  const int c1 = min(c0 + kAsmCols, m);
+  const int64_t off = v.f_off[f];
+  T *F = arena + off;
+  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5, nw = kMfThreads / 32;
+  for (int c = c0 + wid; c < c1; c += nw)
+    for (int i = c + lane; i < m; i += 32) F[(int64_t)c * m + i] = T(0);
+  __syncthreads();
+  const int64_t lo = lower_bound64(v.asm_tgt, v.f_asm[f], v.f_asm[f + 1], off + (int64_t)c0 * m);
+  const int64_t hi = lower_bound64(v.asm_tgt, lo, v.f_asm[f + 1], off + (int64_t)c1 * m);
+  for (int64_t e = lo + tid; e < hi; e += kMfThreads) {
+    double s = 0.0;
+    for (int64_t q = v.asm_sp[e]; q < v.asm_sp[e + 1]; q++) s += vals[v.asm_src[q]];
+    arena[v.asm_tgt[e]] = (T)s;
+  }
+  __syncthreads();
+  for (int ci = v.f_child_ptr[f]; ci < v.f_child_ptr[f + 1]; ci++) {
+    const int c = v.f_children[ci];
+    const int mc = v.f_m[c], kc = v.f_k[c], rc = mc - kc;
+    const T *U = arena + v.f_off[c] + (int64_t)kc * mc + kc;
+    const int *rel = v.relmap + v.f_relmap[c];
+    const int blo = lower_bound32(rel, 0, rc, c0), bhi = lower_bound32(rel, blo, rc, c1);
+    for (int b = blo + wid; b < bhi; b += nw) {
+      const int pb = rel[b];
+      for (int a = b + lane; a < rc; a += 32) F[(int64_t)pb * m + rel[a]] += U[(int64_t)b * mc + a];
+    }
+    __syncthreads();
+  }
+}
+
+// Panel at column j0 of a large front in two launches: mf_diag factors the
+// jb x jb diagonal block of every listed front (one CTA each, in shared
+// memory); mf_panel then solves L21 = A21 L11^-T for row chunks of kPanelRows
+// rows (task = {front, first row of the chunk}), many CTAs per front.
+constexpr int kPanelRows = 256;
+
+template <typename T>
+__device__ __forceinline__ void chol_small_smem(T (*D)[kNB + 1], int jb, int *status) {
+  // right-looking Cholesky of D[0..jb)[0..jb) (lower, D[row][col]) by one CTA
+  const int tid = threadIdx.x;
+  for (int j = 0; j < jb; j++) {
+    if (tid == 0) {
+      T d = D[j][j];
+      if (!(d > T(0))) { atomicOr(status, ERR_NOT_SPD); d = T(1); }
+      D[j][j] = tsqrt<T>(d);
+    }
+    __syncthreads();
+    const T p = D[j][j];
+    for (int i = j + 1 + tid; i < jb; i += blockDim.x) D[i][j] /= p;
+    __syncthreads();
+    for (int q = tid; q < (jb - j - 1) * (jb - j - 1); q += blockDim.x) {
+      int i = j + 1 + q / (jb - j - 1), c = j + 1 + q % (jb - j - 1);
+      if (i >= c) D[i][c] -= D[i][j] * D[c][j];
+    }
+    __syncthreads();
+  }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kMfThreads)
+mf_diag(MfView v, const int *__restrict__ fronts, int j0, T *__restrict__ arena, int *__restrict__ status) {
+  __shared__ T D[kNB][kNB + 1];
+  const int f = fronts[blockIdx.x];
+  const int m = v.f_m[f], k = v.f_k[f];
+  const int jb = min(kNB, k - j0);
+  T *F = arena + v.f_off[f];
+  const int tid = threadIdx.x;
+  for (int q = tid; q < jb * jb; q += kMfThreads) {
+    int c = q / jb, i = q % jb;  // column-major walk: coalesced over i
+    D[i][c] = i >= c ? F[(int64_t)(j0 + c) * m + j0 + i] : T(0);
+  }
+  __syncthreads();
+  chol_small_smem<T>(D, jb, status);
+  for (int q = tid; q < jb * jb; q += kMfThreads) {
+    int c = q / jb, i = q % jb;
+    if (i >= c) F[(int64_t)(j0 + c) * m + j0 + i] = D[i][c];
+  }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kMfThreads)
+mf_panel(MfView v, const int2 *__restrict__ tasks, int j0, T *__restrict__ arena) {
+  __shared__ T D[kNB][kNB + 1];
+  const int f = tasks[blockIdx.x].x, r0 = tasks[blockIdx.x].y;
+  const int m = v.f_m[f], k = v.f_k[f];
+  const int jb = min(kNB, k - j0);
+  T *F = arena + v.f_off[f];
+  const int tid = threadIdx.x;
+  for (int q = tid; q < jb * jb; q += kMfThreads) {  // the factored diagonal block
+    int c = q / jb, i = q % jb;
+    D[i][c] = i >= c ? F[(int64_t)(j0 + c) * m + j0 + i] : T(0);
+  }
+  __syncthreads();
+  const int rb = max(r0, j0 + jb), re = min(r0 + kPanelRows, m);
+  for (int i = rb + tid; i < re; i += kMfThreads) {
+    T x[kNB];
+#pragma unroll
+    for (int t = 0; t < kNB; t++) x[t] = t < jb ? F[(int64_t)(j0 + t) * m + i] : T(0);
+#pragma unroll
+    for (int t = 0; t < kNB; t++) {
+      if (t < jb) {
+        T s = x[t];
+#pragma unroll
+        for (int q = 0; q < t; q++) s -= x[q] * D[t][q];
+        x[t] = s / D[t][t];
+      }
+    }
+#pragma unroll
+    for (int t = 0; t < kNB; t++)
+      if (t < jb) F[(int64_t)(j0 + t) * m + i] = x[t];
+  }
+}
+
+// one 64x64 tile of the trailing update after the panel at j0;
+// task = {front, (ti << 16) | tj}, tiles relative to column j0 + jb
+template <typename T>
+__global__ void __launch_bounds__(kMfThreads)
+mf_update(MfView v, const int2 *__restrict__ tasks, int j0, T *__restrict__ arena) {
+  __shared__ T As[kNB][kTile];
+  __shared__ T Bs[kNB][kTile];
+  const int f = tasks[blockIdx.x].x;
+  const int ti = tasks[blockIdx.x].y >> 16, tj = tasks[blockIdx.x].y & 0xffff;
+  const int m = v.f_m[f], k = v.f_k[f];
+  const int jb = min(kNB, k - j0);
+  T *F = arena + v.f_off[f];
+  const int c0 = j0 + jb;
+  const int r0 = c0 + ti * kTile, cc0 = c0 + tj * kTile;
+  const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
+  for (int q = tid; q < kNB * kTile; q += kMfThreads) {
+    int t = q / kTile, r = q % kTile;
+    T a = T(0), b = T(0);
+    if (t < jb) {
+      if (r0 + r < m) a = F[(int64_t)(j0 + t) * m + r0 + r];
+      if (cc0 + r < m) b = F[(int64_t)(j0 + t) * m + cc0 + r];
+    }
+    As[t][r] = a;
+    Bs[t][r] = b;
+  }
+  __syncthreads();
+  T acc[4][4];
+#pragma unroll
+  for (int a = 0; a < 4; a++)
+#pragma unroll
+    for (int b = 0; b < 4; b++) acc[a][b] = T(0);
+  for (int t = 0; t < jb; t++) {
+    T ra[4], rb[4];
+#pragma unroll
+    for (int a = 0; a < 4; a++) ra[a] = As[t][tx + 16 * a];
+#pragma unroll
+    for (int b = 0; b < 4; b++) rb[b] = Bs[t][ty + 16 * b];
+#pragma unroll
+    for (int a = 0; a < 4; a++)
+#pragma unroll
+      for (int b = 0; b < 4; b++) acc[a][b] += ra[a] * rb[b];
+  }
+#pragma unroll
+  for (int b = 0; b < 4; b++) {
+    const int col = cc0 + ty + 16 * b;
+    if (col >= m) continue;
+#pragma unroll
+    for (int a = 0; a < 4; a++) {
+      const int row = r0 + tx + 16 * a;
+      if (row < m && row >= col) F[(int64_t)col * m + row] -= acc[a][b];
+    }
+  }
+}
+
 // ---------------------------------------------------------------------------
 // multifrontal solves
 // ---------------------------------------------------------------------------
-// forward: gather the right-hand side of the pivots, add the children's update
-// vectors, solve with L11, leave L21-updated tail as this front's update vector
+// Solves keep the front's work vector w (length m) in shared memory when it
+// fits (`wglob` otherwise) and walk the pivots in blocks of 32 columns: one
+// warp solves the 32x32 triangle, all warps apply the block to the rest.
+constexpr int kSB = 32;
+
+// forward: w = [b_piv ; 0] + children's update vectors; y = L11^-1 w1;
+// this front's update vector = w2 - L21 y
 template <typename T>
 __global__ void __launch_bounds__(kMfThreads)
 mf_fwd_level(MfView v, const int *__restrict__ fronts, const T *__restrict__ arena,
-             T *__restrict__ xl, T *__restrict__ uvec, T *__restrict__ wv) {
+             T *__restrict__ xl, T *__restrict__ uvec, T *__restrict__ wglob, int use_smem) {
+  extern __shared__ unsigned char smem_raw[];
   const int f = fronts[blockIdx.x];
   const int m = v.f_m[f], k = v.f_k[f];
   const T *F = arena + v.f_off[f];
-  T *w = wv + v.f_woff[f];
+  T *w = use_smem ? reinterpret_cast<T *>(smem_raw) : wglob + v.f_woff[f];
   T *x = xl + v.f_xoff[f] + v.f_p0[f];
-  const int tid = threadIdx.x;
+  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
   for (int i = tid; i < m; i += kMfThreads) w[i] = i < k ? x[i] : T(0);
   __syncthreads();
   for (int ci = v.f_child_ptr[f]; ci < v.f_child_ptr[f + 1]; ci++) {
@@ -221,11 +479,30 @@ mf_fwd_level(MfView v, const int *__restrict__ fronts, const T *__restrict__ are
     for (int a = tid; a < rc; a += kMfThreads) w[rel[a]] += u[a];
     __syncthreads();
   }
-  for (int j = 0; j < k; j++) {
-    const T yj = w[j] / F[(int64_t)j * m + j];
+  __shared__ T Dg[kSB][kSB + 1];
+  for (int J0 = 0; J0 < k; J0 += kSB) {
+    const int jb = min(kSB, k - J0);
+    for (int q = tid; q < jb * jb; q += kMfThreads) {
+      int c = q / jb, i = q % jb;
+      Dg[i][c] = F[(int64_t)(J0 + c) * m + J0 + i];
+    }
     __syncthreads();
-    for (int i = j + 1 + tid; i < m; i += kMfThreads) w[i] -= F[(int64_t)j * m + i] * yj;
-    if (tid == 0) w[j] = yj;
+    if (wid == 0) {
+      T wl = lane < jb ? w[J0 + lane] : T(0);
+      for (int j = 0; j < jb; j++) {
+        const T yj = __shfl_sync(0xffffffffu, wl, j) / Dg[j][j];
+        if (lane == j) wl = yj;
+        if (lane > j && lane < jb) wl -= Dg[lane][j] * yj;
+      }
+      if (lane < jb) w[J0 + lane] = wl;
+    }
+    __syncthreads();
+    for (int i = J0 + jb + tid; i < m; i += kMfThreads) {
+      T s = T(0);
+#pragma unroll 8
+      for (int j = 0; j < jb; j++) s += F[(int64_t)(J0 + j) * m + i] * w[J0 + j];
+      w[i] -= s;
+    }
     __syncthreads();
   }
   for (int i = tid; i < k; i += kMfThreads) x[i] = w[i];
@@ -237,11 +514,12 @@ mf_fwd_level(MfView v, const int *__restrict__ fronts, const T *__restrict__ are
 template <typename T>
 __global__ void __launch_bounds__(kMfThreads)
 mf_bwd_level(MfView v, const int *__restrict__ fronts, const T *__restrict__ arena,
-             T *__restrict__ xl, T *__restrict__ wv) {
+             T *__restrict__ xl, T *__restrict__ wglob, int use_smem) {
+  extern __shared__ unsigned char smem_raw[];
   const int f = fronts[blockIdx.x];
   const int m = v.f_m[f], k = v.f_k[f];
   const T *F = arena + v.f_off[f];
-  T *w = wv + v.f_woff[f];
+  T *w = use_smem ? reinterpret_cast<T *>(smem_raw) : wglob + v.f_woff[f];
   T *xb = xl + v.f_xoff[f];
   const int *rows = v.rows + v.f_rows[f];
   const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5, nw = kMfThreads / 32;
@@ -249,22 +527,44 @@ mf_bwd_level(MfView v, const int *__restrict__ fronts, const T *__restrict__ are
   __syncthreads();
   // contributions of the already solved update rows
   for (int j = wid; j < k; j += nw) {
-    double s = 0.0;
-    for (int i = k + lane; i < m; i += 32) s += (double)(F[(int64_t)j * m + i] * w[i]);
-    s = warp_sum(s);
-    if (lane == 0) w[j] -= (T)s;
+    T s = T(0);
+    for (int i = k + lane; i < m; i += 32) s += F[(int64_t)j * m + i] * w[i];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+    if (lane == 0) w[j] -= s;
   }
   __syncthreads();
-  if (wid == 0) {
-    for (int j = k - 1; j >= 0; j--) {
-      double s = 0.0;
-      for (int i = j + 1 + lane; i < k; i += 32) s += (double)(F[(int64_t)j * m + i] * w[i]);
-      s = warp_sum(s);
-      if (lane == 0) w[j] = (w[j] - (T)s) / F[(int64_t)j * m + j];
-      __syncwarp();
+  __shared__ T Dg[kSB][kSB + 1];
+  for (int J1 = k; J1 > 0; J1 -= kSB) {
+    const int J0 = max(0, J1 - kSB), jb = J1 - J0;
+    for (int q = tid; q < jb * jb; q += kMfThreads) {
+      int c = q / jb, i = q % jb;
+      Dg[i][c] = F[(int64_t)(J0 + c) * m + J0 + i];
     }
+    __syncthreads();
+    if (wid == 0) {
+      T wl = lane < jb ? w[J0 + lane] : T(0);
+      for (int j = jb - 1; j >= 0; j--) {
+        // x_j = (w_j - sum_{i>j in block} L(i,j) x_i) / L(j,j); the sum is
+        // accumulated into wl of lane j by the lanes of the solved rows
+        T contrib = (lane > j && lane < jb) ? Dg[lane][j] * wl : T(0);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) contrib += __shfl_down_sync(0xffffffffu, contrib, o);
+        contrib = __shfl_sync(0xffffffffu, contrib, 0);
+        if (lane == j) wl = (wl - contrib) / Dg[j][j];
+      }
+      if (lane < jb) w[J0 + lane] = wl;
+    }
+    __syncthreads();
+    // columns left of the block: w_j -= sum_{i in block} L(i,j) x_i
+    for (int j = wid; j < J0; j += nw) {
+      T s = lane < jb ? F[(int64_t)j * m + J0 + lane] * w[J0 + lane] : T(0);
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+      if (lane == 0) w[j] -= s;
+    }
+    __syncthreads();
   }
-  __syncthreads();
   for (int i = tid; i < k; i += kMfThreads) xb[rows[i]] = w[i];
 }
 

@@ -62,12 +62,21 @@ static double wall() {
 }
 
 // one multifrontal batch on the device, factor precision T
+constexpr int kLargeFront = 256;      // fronts above this size use the multi-CTA pipeline
+constexpr int kMaxSolveSmem = 200 * 1024;
+
 template <typename T>
 struct MfDevice {
   DBuf<int64_t> f_off, f_rows, f_xoff, f_uoff, f_woff, f_relmap, f_asm, asm_tgt, asm_sp, asm_src;
   DBuf<int> f_m, f_k, f_p0, f_child_ptr, f_children, rows, relmap, lvl_fronts, gidx;
+  DBuf<int> small_fronts, tiny_fronts, diag_fronts;
+  DBuf<int2> asm_tasks, upd_tasks, panel_tasks;
   DBuf<T> arena, xl, u, w;
-  std::vector<int> lvl_ptr;
+  std::vector<int> lvl_ptr, lvl_max_m;
+  // per level: small-front range, assembly-task range, steps
+  struct Step { int j0, diag_off, diag_cnt, panel_off, panel_cnt; int64_t upd_off, upd_cnt; };
+  struct Level { int tiny_off, tiny_cnt, tiny_maxm, small_off, small_cnt, asm_off, asm_cnt; std::vector<Step> steps; };
+  std::vector<Level> levels;
   int nlevels = 0, nfronts = 0;
   int64_t xlen = 0;
   MfView view{};
@@ -86,22 +95,103 @@ struct MfDevice {
     u.alloc((size_t)std::max<int64_t>(B.ulen, 1));
     w.alloc((size_t)std::max<int64_t>(B.wlen, 1));
     lvl_ptr = B.lvl_ptr;
+    lvl_max_m = B.lvl_max_m;
     nlevels = B.nlevels;
     nfronts = B.nfronts;
     xlen = B.xlen;
     view = MfView{f_off.p, f_m.p, f_k.p, f_rows.p, f_xoff.p, f_p0.p, f_uoff.p, f_woff.p,
                   f_child_ptr.p, f_children.p, f_relmap.p, f_asm.p, rows.p, relmap.p,
                   asm_tgt.p, asm_sp.p, asm_src.p};
+    // work lists of the factorisation
+    std::vector<int> sm, ty, df;
+    std::vector<int2> at, ut, pf;
+    const int tiny_max = sizeof(T) == 8 ? 112 : 160;  // front fits in ~100 KB of shared memory
+    levels.assign((size_t)nlevels, Level());
+    for (int l = 0; l < nlevels; l++) {
+      Level &L = levels[(size_t)l];
+      L.small_off = (int)sm.size();
+      L.tiny_off = (int)ty.size();
+      L.tiny_maxm = 0;
+      L.asm_off = (int)at.size();
+      std::vector<int> large;
+      for (int q = B.lvl_ptr[(size_t)l]; q < B.lvl_ptr[(size_t)l + 1]; q++) {
+        int f = B.lvl_fronts[(size_t)q];
+        int m = B.f_m[(size_t)f];
+        if (m > kLargeFront) large.push_back(f);
+        else if (m <= tiny_max) { ty.push_back(f); L.tiny_maxm = std::max(L.tiny_maxm, m); }
+        else sm.push_back(f);
+      }
+      L.small_cnt = (int)sm.size() - L.small_off;
+      L.tiny_cnt = (int)ty.size() - L.tiny_off;
+      int kmax = 0;
+      for (int f : large) {
+        int m = B.f_m[(size_t)f];
+        for (int c0 = 0; c0 < m; c0 += kAsmCols) at.push_back(make_int2(f, c0));
+        kmax = std::max(kmax, B.f_k[(size_t)f]);
+      }
+      L.asm_cnt = (int)at.size() - L.asm_off;
+      for (int j0 = 0; j0 < kmax; j0 += kNB) {
+        Step st{j0, (int)df.size(), 0, (int)pf.size(), 0, (int64_t)ut.size(), 0};
+        for (int f : large) {
+          int m = B.f_m[(size_t)f], k = B.f_k[(size_t)f];
+          if (j0 >= k) continue;
+          df.push_back(f);
+          for (int r0 = j0 + std::min(kNB, k - j0); r0 < m; r0 += kPanelRows) pf.push_back(make_int2(f, r0));
+          int c0 = j0 + std::min(kNB, k - j0);
+          int nt = (m - c0 + kTile - 1) / kTile;
+          for (int tj = 0; tj < nt; tj++)
+            for (int ti = tj; ti < nt; ti++) ut.push_back(make_int2(f, (ti << 16) | tj));
+        }
+        st.diag_cnt = (int)df.size() - st.diag_off;
+        st.panel_cnt = (int)pf.size() - st.panel_off;
+        st.upd_cnt = (int64_t)ut.size() - st.upd_off;
+        L.steps.push_back(st);
+      }
+    }
+    small_fronts.upload(sm);
+    tiny_fronts.upload(ty);
+    CK(cudaFuncSetAttribute(mf_factor_small<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 110 * 1024));
+    panel_tasks.upload(pf);
+    diag_fronts.upload(df);
+    asm_tasks.upload(at);
+    upd_tasks.upload(ut);
+    CK(cudaFuncSetAttribute(mf_fwd_level<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxSolveSmem));
+    CK(cudaFuncSetAttribute(mf_bwd_level<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxSolveSmem));
   }
 
   int factor(const double *vals, int *status, cudaStream_t s) {
     int launches = 0;
     for (int l = 0; l < nlevels; l++) {
-      int nf = lvl_ptr[(size_t)l + 1] - lvl_ptr[(size_t)l];
-      if (!nf) continue;
-      mf_factor_level<T><<<nf, kMfThreads, 0, s>>>(view, lvl_fronts.p + lvl_ptr[(size_t)l], vals,
-                                                    arena.p, status);
-      launches++;
+      const Level &L = levels[(size_t)l];
+      if (L.tiny_cnt) {
+        size_t smem = (size_t)L.tiny_maxm * L.tiny_maxm * sizeof(T);
+        mf_factor_small<T><<<L.tiny_cnt, kSmallThreads, smem, s>>>(view, tiny_fronts.p + L.tiny_off, vals,
+                                                                  arena.p, status);
+        launches++;
+      }
+      if (L.small_cnt) {
+        mf_factor_level<T><<<L.small_cnt, kMfThreads, 0, s>>>(view, small_fronts.p + L.small_off, vals,
+                                                              arena.p, status);
+        launches++;
+      }
+      if (L.asm_cnt) {
+        mf_assemble_large<T><<<L.asm_cnt, kMfThreads, 0, s>>>(view, asm_tasks.p + L.asm_off, vals, arena.p);
+        launches++;
+      }
+      for (const Step &st : L.steps) {
+        mf_diag<T><<<st.diag_cnt, kMfThreads, 0, s>>>(view, diag_fronts.p + st.diag_off, st.j0, arena.p, status);
+        launches++;
+        if (st.panel_cnt) {
+          mf_panel<T><<<st.panel_cnt, kMfThreads, 0, s>>>(view, panel_tasks.p + st.panel_off, st.j0, arena.p);
+          launches++;
+        }
+        for (int64_t o = 0; o < st.upd_cnt; o += 1 << 30) {
+          int cnt = (int)std::min<int64_t>(st.upd_cnt - o, 1 << 30);
+          if (!cnt) continue;
+          mf_update<T><<<cnt, kMfThreads, 0, s>>>(view, upd_tasks.p + st.upd_off + o, st.j0, arena.p);
+          launches++;
+        }
+      }
     }
     return launches;
   }
@@ -111,15 +201,19 @@ struct MfDevice {
     for (int l = 0; l < nlevels; l++) {
       int nf = lvl_ptr[(size_t)l + 1] - lvl_ptr[(size_t)l];
       if (!nf) continue;
-      mf_fwd_level<T><<<nf, kMfThreads, 0, s>>>(view, lvl_fronts.p + lvl_ptr[(size_t)l], arena.p,
-                                                 xl.p, u.p, w.p);
+      size_t sm = (size_t)lvl_max_m[(size_t)l] * sizeof(T);
+      int use = sm <= (size_t)kMaxSolveSmem;
+      mf_fwd_level<T><<<nf, kMfThreads, use ? sm : 0, s>>>(view, lvl_fronts.p + lvl_ptr[(size_t)l], arena.p,
+                                                            xl.p, u.p, w.p, use);
       launches++;
     }
     for (int l = nlevels - 1; l >= 0; l--) {
       int nf = lvl_ptr[(size_t)l + 1] - lvl_ptr[(size_t)l];
       if (!nf) continue;
-      mf_bwd_level<T><<<nf, kMfThreads, 0, s>>>(view, lvl_fronts.p + lvl_ptr[(size_t)l], arena.p,
-                                                 xl.p, w.p);
+      size_t sm = (size_t)lvl_max_m[(size_t)l] * sizeof(T);
+      int use = sm <= (size_t)kMaxSolveSmem;
+      mf_bwd_level<T><<<nf, kMfThreads, use ? sm : 0, s>>>(view, lvl_fronts.p + lvl_ptr[(size_t)l], arena.p,
+                                                            xl.p, w.p, use);
       launches++;
     }
     return launches;
@@ -150,7 +244,7 @@ struct dg_handle {
   int device = 0;
   DBuf<int64_t> Ap, Rp, Pp, pull_ptr, pull_idx;
   DBuf<int> Ac, Rc, Pc, cpos, status;
-  DBuf<double> Av, ACv, Rv, Pv, b, x, r, p, q, z, zold, xc_dummy;
+  DBuf<double> Av, ACv, Rv, Pv, b, x, r, p, q, z, zold, hb, hx;
   DBuf<float> Rvf, Pvf;
   DBuf<double> part_rz, part_rzo, part_pq, part_rr, sc;
   std::unique_ptr<MfDevice<double>> sub64, co64;
@@ -159,7 +253,7 @@ struct dg_handle {
   int *host_status = nullptr;
   double *d_host_out = nullptr;
   int *d_host_status = nullptr;
-  cudaEvent_t ev[4]{};
+  cudaEvent_t ev[10]{};
   ~dg_handle() {
     if (host_out) cudaFreeHost(host_out);
     if (host_status) cudaFreeHost(host_status);
@@ -267,6 +361,7 @@ dg_status do_setup(dg_handle *h) {
   if (!build_setup(c, h->n, h->ii, h->jj, h->vv, h->part.empty() ? nullptr : &h->part, h->nparts, h->S, err))
     return fail(h, DG_BAD_INPUT, err);
   MfOptions mo;
+  mo.leaf = c.nd_leaf;
   try {
     if (c.fine_method == 1) mf_build_subdomains(h->S.A, h->S.sd_ptr, h->S.sd_nodes, mo, h->Bsub);
     if (c.levels > 1) mf_build_single(h->S.AC, mo, h->Bco);
@@ -285,7 +380,7 @@ dg_status do_setup(dg_handle *h) {
     int n = h->n;
     h->Ap.upload(S.A.ptr); h->Ac.upload(S.A.col); h->Av.upload(S.A.val);
     h->lanes = lanes_for(S.A);
-    for (auto *v : {&h->b, &h->x, &h->r, &h->p, &h->q, &h->z, &h->zold}) v->alloc((size_t)n);
+    for (auto *v : {&h->b, &h->x, &h->r, &h->p, &h->q, &h->z, &h->zold, &h->hb, &h->hx}) v->alloc((size_t)n);
     for (auto *v : {&h->part_rz, &h->part_rzo, &h->part_pq, &h->part_rr}) {
       v->alloc(kRedBlocks);
       CK(cudaMemset(v->p, 0, kRedBlocks * sizeof(double)));
@@ -399,9 +494,17 @@ dg_status do_solve(dg_handle *h, const double *d_b, double *d_x, dg_stats *st, c
     if (coarse && c.method == 1) mode |= 2;
     if (mixed) mode |= 8;
     // (the reference adds the coarse correction only for method 1, pcg.F90:191-193)
+    const bool prof = c.profile != 0;
+    double t_sub = 0, t_co = 0, t_sp = 0;
+    auto lap = [&](int a, int b) -> double {
+      float ms = 0;
+      CK(cudaEventElapsedTime(&ms, h->ev[a], h->ev[b]));
+      return ms * 1e-3;
+    };
     while (ratio > tol * tol && it < maxit) {
       it++;
       const int first = it == 1;
+      if (prof) CK(cudaEventRecord(h->ev[3], s));
       if (fine) {
         if (mixed) {
           gather_subdomains<float><<<grid, kVecThreads, 0, s>>>(h->r.p, h->sub32->gidx.p, h->sub32->xl.p, h->sub32->xlen);
@@ -411,6 +514,7 @@ dg_status do_solve(dg_handle *h, const double *d_b, double *d_x, dg_stats *st, c
           launches += 1 + h->sub64->solve(s);
         }
       }
+      if (prof) CK(cudaEventRecord(h->ev[4], s));
       if (coarse) {
         if (mixed)
           restrict_to_coarse<float><<<grid, kVecThreads, 0, s>>>(h->Rp.p, h->Rc.p, h->Rvf.p, h->r.p, h->cpos.p, h->co64->xl.p, h->S.R.nrows);
@@ -418,6 +522,7 @@ dg_status do_solve(dg_handle *h, const double *d_b, double *d_x, dg_stats *st, c
           restrict_to_coarse<double><<<grid, kVecThreads, 0, s>>>(h->Rp.p, h->Rc.p, h->Rv.p, h->r.p, h->cpos.p, h->co64->xl.p, h->S.R.nrows);
         launches += 1 + h->co64->solve(s);
       }
+      if (prof) CK(cudaEventRecord(h->ev[5], s));
       const double *xc = coarse ? h->co64->xl.p : nullptr;
       if (mixed)
         pull_prolong_dot<float, float><<<grid, kVecThreads, 0, s>>>(
@@ -427,7 +532,9 @@ dg_status do_solve(dg_handle *h, const double *d_b, double *d_x, dg_stats *st, c
         pull_prolong_dot<double, double><<<grid, kVecThreads, 0, s>>>(
             n, h->pull_ptr.p, h->pull_idx.p, fine ? h->sub64->xl.p : nullptr, h->Pp.p, h->Pc.p, h->Pv.p, xc,
             h->cpos.p, mode, h->r.p, h->z.p, h->zold.p, h->part_rz.p, h->part_rzo.p);
+      if (prof) CK(cudaEventRecord(h->ev[6], s));
       spmv_any(h->lanes, grid, s, h, first, mixed ? 1 : 0);
+      if (prof) CK(cudaEventRecord(h->ev[7], s));
       cg_update<<<grid, kVecThreads, 0, s>>>(n, h->z.p, h->p.p, h->q.p, h->x.p, h->r.p, h->sc.p, h->part_pq.p, first,
                                              h->part_rr.p);
       launches += 3;
@@ -439,6 +546,7 @@ dg_status do_solve(dg_handle *h, const double *d_b, double *d_x, dg_stats *st, c
       cg_finish<<<1, 32, 0, s>>>(h->sc.p, h->part_rr.p, 0, h->d_host_out, h->status.p, h->d_host_status);
       launches++;
       CK(cudaStreamSynchronize(s));
+      if (prof) { t_sub += lap(3, 4); t_co += lap(4, 5); t_sp += lap(6, 7); }
       res = h->host_out[0];
       double alpha = h->host_out[2], beta = h->host_out[3], pq = h->host_out[5];
       alphas.push_back(alpha);
@@ -474,6 +582,16 @@ dg_status do_solve(dg_handle *h, const double *d_b, double *d_x, dg_stats *st, c
     out.t_iterate_s = ms_i * 1e-3;
     out.t_total_s = out.t_factor_s + out.t_iterate_s;
     out.gpu_launches = launches;
+    {
+      const double tsz = mixed ? 4.0 : 8.0;
+      out.subsolve_bytes = 2.0 * (double)h->Bsub.factor_nnz * tsz;
+      out.coarse_bytes = 2.0 * (double)h->Bco.factor_nnz * 8.0;
+      const double nnz = (double)h->S.A.nnz();
+      out.spmv_bytes = 12.0 * nnz + 8.0 * (n + 1) + 8.0 * n * 3.0;  // A, z and p read, q written
+      out.t_subsolve_s = t_sub;
+      out.t_coarse_s = t_co;
+      out.t_spmv_s = t_sp;
+    }
     if (st) *st = out;
     return rc;
   } catch (const CudaError &e) {
@@ -512,12 +630,26 @@ dg_status dg_set_option(dg_handle *h, const char *name, const char *value) {
     int v;
     if (!parse_i10(w2, v) || v < 0 || v > 1) return fail(h, DG_BAD_INPUT, "precision must be 0 or 1");
     h->ctl.precision = v;
+    h->ready = false;  // the subdomain factors change precision: set up again
     return DG_OK;
   }
   if (w1 == "replace_every") {
     int v;
     if (!parse_i10(w2, v)) return fail(h, DG_BAD_INPUT, "bad replace_every");
     h->ctl.replace_every = v;
+    return DG_OK;
+  }
+  if (w1 == "profile") {
+    int v;
+    if (!parse_i10(w2, v)) return fail(h, DG_BAD_INPUT, "bad profile");
+    h->ctl.profile = v;
+    return DG_OK;
+  }
+  if (w1 == "nd_leaf") {
+    int v;
+    if (!parse_i10(w2, v) || v < 2) return fail(h, DG_BAD_INPUT, "nd_leaf must be >= 2");
+    h->ctl.nd_leaf = v;
+    h->ready = false;
     return DG_OK;
   }
   if (w1 == "omega") {
@@ -607,21 +739,13 @@ dg_status dg_solve(dg_handle *h, const double *b, double *x, dg_stats *stats) {
   if (!h || !x) return DG_BAD_INPUT;
   if (!h->ready) return fail(h, DG_NOT_READY, "dg_setup has not run");
   const double *src = b ? b : h->rhs.data();
-  double *db = nullptr, *dx = nullptr;
   size_t bytes = (size_t)h->n * sizeof(double);
-  if (cudaMalloc(&db, bytes) != cudaSuccess || cudaMalloc(&dx, bytes) != cudaSuccess) {
-    if (db) cudaFree(db);
-    return fail(h, DG_CUDA_ERROR, "cudaMalloc failed for the solve vectors");
-  }
-  dg_status s = DG_OK;
-  if (cudaMemcpy(db, src, bytes, cudaMemcpyHostToDevice) != cudaSuccess) s = fail(h, DG_CUDA_ERROR, "H2D copy failed");
-  if (s == DG_OK) {
-    s = do_solve(h, db, dx, stats, 0);
-    if ((s == DG_OK || s == DG_NOT_CONVERGED) && cudaMemcpy(x, dx, bytes, cudaMemcpyDeviceToHost) != cudaSuccess)
-      s = fail(h, DG_CUDA_ERROR, "D2H copy failed");
-  }
-  cudaFree(db);
-  cudaFree(dx);
+  // the handle's own device vectors (allocated by dg_setup) carry b and x
+  if (cudaMemcpy(h->hb.p, src, bytes, cudaMemcpyHostToDevice) != cudaSuccess)
+    return fail(h, DG_CUDA_ERROR, "H2D copy failed");
+  dg_status s = do_solve(h, h->hb.p, h->hx.p, stats, 0);
+  if ((s == DG_OK || s == DG_NOT_CONVERGED) && cudaMemcpy(x, h->hx.p, bytes, cudaMemcpyDeviceToHost) != cudaSuccess)
+    s = fail(h, DG_CUDA_ERROR, "D2H copy failed");
   return s;
 }
 

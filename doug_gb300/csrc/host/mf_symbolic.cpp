@@ -431,7 +431,25 @@ void mf_build_subdomains(const Csr &A, const std::vector<int64_t> &sd_ptr,
     }
     analyse((int)m, lr, lc, src, opt.leaf, locs[(size_t)s]);
   });
-  for (int s = 0; s < nsd; s++) append(locs[(size_t)s], gids[(size_t)s], out);
+  // reserve the batch arrays once (they are large for big subdomains)
+  {
+    size_t nf = 0, nr = 0, ne = 0;
+    for (const Local &L : locs) {
+      nf += L.p0.size();
+      for (const auto &r : L.rows) nr += r.size();
+      ne += L.er.size();
+    }
+    out.f_off.reserve(nf); out.f_m.reserve(nf); out.f_k.reserve(nf); out.f_rows.reserve(nf);
+    out.f_xoff.reserve(nf); out.f_p0.reserve(nf); out.f_uoff.reserve(nf); out.f_woff.reserve(nf);
+    out.f_parent.reserve(nf); out.f_level.reserve(nf); out.f_relmap.reserve(nf); out.f_asm.reserve(nf + 1);
+    out.f_child_ptr.reserve(nf + 1); out.f_children.reserve(nf);
+    out.rows.reserve(nr); out.relmap.reserve(nr);
+    out.asm_tgt.reserve(ne); out.asm_sp.reserve(ne + 1); out.asm_src.reserve(ne);
+  }
+  for (int s = 0; s < nsd; s++) {
+    append(locs[(size_t)s], gids[(size_t)s], out);
+    Local().rows.swap(locs[(size_t)s].rows);  // release as we go
+  }
   finalize(out);
 }
 

@@ -15,9 +15,22 @@
 #include <cstdio>
 #include <cstring>
 #include <fstream>
+#include <chrono>
+#include <cstdlib>
 #include <sstream>
 
 namespace dg {
+
+// Phase timing on stderr when DG_SETUP_TIMING is set in the environment.
+struct PhaseTimer {
+  bool on = std::getenv("DG_SETUP_TIMING") != nullptr;
+  std::chrono::steady_clock::time_point t = std::chrono::steady_clock::now();
+  void lap(const char *what) {
+    auto now = std::chrono::steady_clock::now();
+    if (on) fprintf(stderr, "[setup] %-28s %8.3f s\n", what, std::chrono::duration<double>(now - t).count());
+    t = now;
+  }
+};
 
 // ---------------------------------------------------------------------------
 // control words (controls.F90:159-246, DOUG_utils.F90:629-1150)
@@ -677,6 +690,8 @@ static bool aggregate(ScaledMatrix &S, int neighood, int minasize, int maxasize,
     // layer of the newest aggregate at the tail, exactly as the reference
     std::vector<int> ngs((size_t)n + 1, 0);
     int ngood = 0;
+    std::vector<int> seen((size_t)n, 0);
+    int seen_stamp = 0;
     maxasizelargest = coarse ? 3 * maxasize : maxasize + 4 * (2 * neighood);
     if (!coarse) st.beta = alpha / 4.0;
     Colourer col(S, neighood, maxasize, stat, dist, nodes, st);
@@ -698,10 +713,16 @@ static bool aggregate(ScaledMatrix &S, int neighood, int minasize, int maxasize,
         if (first >= n) break;
         start = first;
       } else {
+        // the first entry that repeats an earlier one (the reference scans all
+        // pairs, SpMtx_aggregation.F90:210-217; a stamp per pass gives the
+        // same answer in one sweep)
         start = -1;
-        for (int a = 2; a <= ngood && start < 0; a++)
-          for (int b = 1; b < a; b++)
-            if (ngs[(size_t)a] == ngs[(size_t)b]) { start = ngs[(size_t)a]; break; }
+        seen_stamp++;
+        for (int a = 1; a <= ngood; a++) {
+          int v = ngs[(size_t)a];
+          if (seen[(size_t)v] == seen_stamp) { start = v; break; }
+          seen[(size_t)v] = seen_stamp;
+        }
         if (start < 0) start = ngs[1];
       }
       int nneigs = 0;
@@ -897,6 +918,7 @@ static Coo smoother(const Csr &A, const std::vector<char> &strong, double omega,
     }
   Coo S;
   S.nrows = A.nrows; S.ncols = A.nrows;
+  S.i.reserve(A.col.size()); S.j.reserve(A.col.size()); S.v.reserve(A.col.size());
   for (int r = 0; r < A.nrows; r++)
     for (int64_t k = A.ptr[(size_t)r]; k < A.ptr[(size_t)r + 1]; k++) {
       int c = A.col[(size_t)k];
@@ -915,6 +937,7 @@ bool build_setup(const Controls &c_in, int n, const std::vector<int> &ii, const 
   Controls c = c_in;
   out = SetupResult();
   out.n = n;
+  PhaseTimer tm;
   if (c.fine_method < 0 || c.fine_method > 1) {
     err = "Wrong fine method " + std::to_string(c.fine_method);
     return false;
@@ -947,9 +970,11 @@ bool build_setup(const Controls &c_in, int n, const std::vector<int> &ii, const 
   SA.symmetric = c.symmstruct && c.symmnumeric;
   scale_rows(SA);
   find_strong(SA, out.strong1);
+  tm.lap("fine strength");
   if (!aggregate(SA, out.r1, out.min1, out.max1, out.strong1, false, st, out.fine, out.fine_full, err))
     return false;
   unscale_rows(SA);
+  tm.lap("fine aggregation");
   const Csr &A = SA.M;
   // IntRestBuild (CoarseMtx.F90:50-474); smoothers are capped at radius1
   if (c.smoothers > c.radius1) c.smoothers = c.radius1;
@@ -957,6 +982,7 @@ bool build_setup(const Controls &c_in, int n, const std::vector<int> &ii, const 
   if (sm < 0) { err = "smoothers must be >= 0 for the smoothed-aggregation coarse space"; return false; }
   Coo T;  // tentative prolongator as restriction rows
   T.nrows = out.fine.nagr; T.ncols = n;
+  T.i.reserve((size_t)n); T.j.reserve((size_t)n); T.v.reserve((size_t)n);
   for (int a = 0; a < out.fine.nagr; a++)
     for (int q = out.fine.starts[(size_t)a]; q < out.fine.starts[(size_t)a + 1]; q++) {
       T.i.push_back(a); T.j.push_back(out.fine.nodes[(size_t)q] - 1); T.v.push_back(1.0);
@@ -991,6 +1017,7 @@ bool build_setup(const Controls &c_in, int n, const std::vector<int> &ii, const 
   Csr Tm = spgemm_first_touch(A, Rcols);     // n x nagr
   Coo RcolOrder;                             // R's COO after arrangement by columns
   RcolOrder.nrows = Rcoo.nrows; RcolOrder.ncols = Rcoo.ncols;
+  RcolOrder.i.reserve(Rcoo.size()); RcolOrder.j.reserve(Rcoo.size()); RcolOrder.v.reserve(Rcoo.size());
   for (int col = 0; col < Rcols.nrows; col++)
     for (int64_t k = Rcols.ptr[(size_t)col]; k < Rcols.ptr[(size_t)col + 1]; k++) {
       RcolOrder.i.push_back(Rcols.col[(size_t)k]);
@@ -1001,6 +1028,8 @@ bool build_setup(const Controls &c_in, int n, const std::vector<int> &ii, const 
   out.P = Rcols;                             // rows = fine nodes, aggregates ascending
   out.P.nrows = n; out.P.ncols = Rcoo.nrows;
   Csr AC = spgemm_first_touch(out.R, Tm);
+  tm.lap("restriction + Galerkin");
+  out.R_i.reserve(RcolOrder.size()); out.R_j.reserve(RcolOrder.size()); out.R_v.reserve(RcolOrder.size());
   for (size_t k = 0; k < RcolOrder.size(); k++) {
     out.R_i.push_back(RcolOrder.i[k] + 1); out.R_j.push_back(RcolOrder.j[k] + 1);
     out.R_v.push_back(RcolOrder.v[k]);
@@ -1025,7 +1054,9 @@ bool build_setup(const Controls &c_in, int n, const std::vector<int> &ii, const 
                  out.coarse_full, err))
     return false;
   unscale_rows(SC);
+  tm.lap("coarse aggregation");
   out.AC = SC.M;
+  out.AC_i.reserve(out.AC.col.size()); out.AC_j.reserve(out.AC.col.size()); out.AC_v.reserve(out.AC.col.size());
   for (int r = 0; r < out.AC.nrows; r++)
     for (int64_t k = out.AC.ptr[(size_t)r]; k < out.AC.ptr[(size_t)r + 1]; k++) {
       out.AC_i.push_back(r + 1); out.AC_j.push_back(out.AC.col[(size_t)k] + 1);
@@ -1037,12 +1068,17 @@ bool build_setup(const Controls &c_in, int n, const std::vector<int> &ii, const 
   out.levels = c.levels;
   int np = part ? nparts : out.coarse_full.nagr;
   out.sd_ptr.assign(1, 0);
+  std::vector<std::vector<int>> part_nodes;
+  if (part) {  // Get_nodes (Decomposition.f90:35-53) for every part in one sweep
+    part_nodes.resize((size_t)np);
+    for (int i = 0; i < n; i++) part_nodes[(size_t)(*part)[(size_t)i] - 1].push_back(i);
+  }
   std::vector<int> onfront((size_t)n, 0), nodes;
   std::vector<int> loc((size_t)n, 0);
   for (int p = 1; p <= np; p++) {
     nodes.clear();
     if (part) {
-      for (int i = 0; i < n; i++) if ((*part)[(size_t)i] == p) nodes.push_back(i);
+      nodes = part_nodes[(size_t)p - 1];
     } else {  // Get_aggregate_nodes (Aggregate_mod.F90:162-190)
       const Aggregates &ca = out.coarse_full, &fa = out.fine_full;
       for (int q = ca.starts[(size_t)p - 1]; q < ca.starts[(size_t)p]; q++) {
@@ -1072,6 +1108,7 @@ bool build_setup(const Controls &c_in, int n, const std::vector<int> &ii, const 
     for (int v : nodes) { onfront[(size_t)v] = 0; out.sd_nodes.push_back(v + 1); }
     out.sd_ptr.push_back((int64_t)out.sd_nodes.size());
   }
+  tm.lap("subdomains + overlap");
   out.A = A;
   return true;
 }

@@ -69,6 +69,14 @@ typedef struct {
   int gpu_launches;           /* kernels launched by the last solve */
   long long factor_nnz;       /* stored factor entries (subdomains) */
   double factor_gflop;        /* partial-Cholesky flops of the subdomain factors */
+  /* phase timings, filled when the control word "profile 1" is set (CUDA
+   * events around each phase; adds a little overhead, so off by default) */
+  double t_subsolve_s;        /* subdomain forward+backward solves, all iterations */
+  double subsolve_bytes;      /* algorithmic bytes of one subdomain solve (factor read twice) */
+  double t_coarse_s;          /* restriction + coarse solves, all iterations */
+  double coarse_bytes;        /* algorithmic bytes of one coarse solve */
+  double t_spmv_s;            /* fused direction update + SpMV, all iterations */
+  double spmv_bytes;          /* algorithmic bytes of one SpMV */
 } dg_stats;
 
 dg_status dg_create(dg_handle **h);

@@ -93,6 +93,11 @@ int orc_write_solution(const char *path, int format, int n, const double *x);
 int orc_spd_solve(int n, int nnz, const int *ii, const int *jj, const double *vv,
                   const double *b, double *x);
 
+/* The same solver with the factorisation kept (NULL on failure). */
+void *orc_spd_factor(int n, int nnz, const int *ii, const int *jj, const double *vv);
+int orc_spd_solve_factored(void *fact, const double *b, double *x);
+void orc_spd_free(void *fact);
+
 /* Parse one control-file value the way DOUG does: i10 / f10.5 / l1. */
 int orc_parse_i10(const char *s, int *out);
 int orc_parse_f10_5(const char *s, double *out);

@@ -72,6 +72,10 @@ def lib():
             L.orc_write_solution.argtypes = [C.c_char_p, C.c_int, C.c_int, P(C.c_double)]
             L.orc_spd_solve.argtypes = [C.c_int, C.c_int, P(C.c_int), P(C.c_int), P(C.c_double),
                                         P(C.c_double), P(C.c_double)]
+            L.orc_spd_factor.argtypes = [C.c_int, C.c_int, P(C.c_int), P(C.c_int), P(C.c_double)]
+            L.orc_spd_factor.restype = C.c_void_p
+            L.orc_spd_solve_factored.argtypes = [C.c_void_p, P(C.c_double), P(C.c_double)]
+            L.orc_spd_free.argtypes = [C.c_void_p]
             for nm in ("orc_parse_i10", "orc_parse_l1"):
                 getattr(L, nm).argtypes = [C.c_char_p, P(C.c_int)]
             L.orc_parse_f10_5.argtypes = [C.c_char_p, P(C.c_double)]
@@ -227,3 +231,32 @@ def parse_value(kind, text):
     if rc:
         raise ValueError(text)
     return v.value
+
+
+class SpdFactor:
+    """Exact SPD factorisation of the oracle (profile Cholesky after RCM)."""
+
+    def __init__(self, n, rows0, cols0, vals):
+        L = lib()
+        ii = np.ascontiguousarray(rows0, dtype=np.int32)
+        jj = np.ascontiguousarray(cols0, dtype=np.int32)
+        vv = np.ascontiguousarray(vals, dtype=np.float64)
+        self.n = n
+        self._L = L
+        self._f = L.orc_spd_factor(n, len(vv), _ip(ii), _ip(jj), _dp(vv))
+        if not self._f:
+            raise RuntimeError("oracle factorisation failed")
+
+    def solve(self, b):
+        b = np.ascontiguousarray(b, dtype=np.float64)
+        x = np.zeros(self.n, dtype=np.float64)
+        self._L.orc_spd_solve_factored(self._f, _dp(b), _dp(x))
+        return x
+
+    def __del__(self):
+        try:
+            if self._f:
+                self._L.orc_spd_free(self._f)
+                self._f = None
+        except Exception:
+            pass

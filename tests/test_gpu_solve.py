@@ -135,3 +135,20 @@ def test_device_pointer_entry_matches_host_entry():
     torch.cuda.synchronize()
     assert np.array_equal(xd.cpu().numpy(), xh)
     assert st.iterations > 0
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_large_fronts_multi_cta_path(precision):
+    # one subdomain over a 24^3 grid: separator fronts of several hundred
+    # rows go through the multi-CTA panel / TRSM / tiled-update pipeline
+    N = 24
+    n, r, c, v, b = P.diffusion3d_fv(N, seed=5)
+    part = np.ones(n, dtype=np.int32)
+    opts = dict(solver=2, method=1, fine_method=1, levels=2, overlap=0, smoothers=1, strong1="0.08",
+                radius1=2, solve_tolerance="1.0e-10", solve_maxiters=200)
+    x, st = _solve(n, r, c, v, b, opts, part=part, precision=precision)
+    xd = O.spd_solve(n, r - 1, c - 1, v, b)
+    # one exact subdomain solve of the whole matrix (plus the additive coarse
+    # term): a few steps; FP32 factors gain ~7 digits per step
+    assert st.iterations <= (3 if precision == 0 else 8)
+    assert np.linalg.norm(x - xd) <= (1e-9 if precision == 0 else 1e-7) * np.linalg.norm(xd)
