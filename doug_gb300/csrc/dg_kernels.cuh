@@ -569,6 +569,472 @@ mf_bwd_level(MfView v, const int *__restrict__ fronts, const T *__restrict__ are
 }
 
 // ---------------------------------------------------------------------------
+// Tiled solve layout of large fronts.  After the factorisation every 32-column
+// block J of a large front (columns 32J .. 32J+jb) is stored as a contiguous
+// run of 32x32 tiles:
+//   Dinv_J          inverse of the jb x jb diagonal block, row-major
+//   tile(R, J)      rows 32R..32R+31 of the block for row blocks R >= J,
+//                   row-major; entries of the diagonal block (and of rows past
+//                   m) are zero, so tile(J, J) only carries update rows
+// The solves of one front are split over a thread-block cluster of C CTAs:
+// CTA q owns the row blocks R with R % C == q, keeps their part of the work
+// vector in its shared memory, streams its own tiles with cp.async, and the
+// CTAs exchange the 32-value block solutions through distributed shared
+// memory with one cluster barrier per column block.  C = 1 is the plain
+// one-CTA solve.
+// ---------------------------------------------------------------------------
+constexpr int kTileThreads = 256;
+constexpr int kTileStages = 8;
+
+struct PackView {
+  const int *blk_front;        // block -> front
+  const int *blk_j;            // block -> J
+  const int *f_blk;            // front -> first block (large fronts), -1 otherwise
+  const int64_t *blk_off;      // block -> element offset in the packed buffer
+};
+
+// one CTA per column block: invert the diagonal block, copy the tiles
+template <typename T>
+__global__ void __launch_bounds__(256)
+mf_pack(MfView v, PackView pk, const T *__restrict__ arena, T *__restrict__ packed) {
+  __shared__ T L[32][33];
+  __shared__ T X[32][33];
+  const int b = blockIdx.x;
+  const int f = pk.blk_front[b], J = pk.blk_j[b];
+  const int m = v.f_m[f], k = v.f_k[f];
+  const int J0 = 32 * J, jb = min(32, k - J0);
+  const T *F = arena + v.f_off[f];
+  T *dst = packed + pk.blk_off[b];
+  const int tid = threadIdx.x;
+  for (int q = tid; q < 32 * 32; q += 256) {
+    int c = q / 32, i = q % 32;
+    L[i][c] = (i < jb && c < jb && i >= c) ? F[(int64_t)(J0 + c) * m + J0 + i] : T(0);
+    X[i][c] = T(0);
+  }
+  __syncthreads();
+  if (tid < jb) {  // column tid of the inverse of a lower triangular block
+    const int c = tid;
+    X[c][c] = T(1) / L[c][c];
+    for (int i = c + 1; i < jb; i++) {
+      T sum = T(0);
+      for (int t = c; t < i; t++) sum += L[i][t] * X[t][c];
+      X[i][c] = -sum / L[i][i];
+    }
+  }
+  __syncthreads();
+  for (int q = tid; q < 32 * 32; q += 256) dst[q] = X[q / 32][q % 32];
+  const int nR = (m + 31) / 32;
+  for (int R = J; R < nR; R++) {
+    T *td = dst + 1024 * (int64_t)(1 + R - J);
+    for (int q = tid; q < 32 * 32; q += 256) {
+      const int rr = q / 32, c = q % 32;  // row-major tile
+      const int row = 32 * R + rr;
+      td[q] = (c < jb && row >= J0 + jb && row < m) ? F[(int64_t)(J0 + c) * m + row] : T(0);
+    }
+  }
+}
+
+__device__ __forceinline__ void cp_async16(void *smem, const void *gmem) {
+  unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(gmem));
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N)); }
+
+template <typename T>
+__device__ __forceinline__ void issue_tile(T *slot, const T *src) {
+  constexpr int n16 = 1024 * (int)sizeof(T) / 16;
+  for (int q = threadIdx.x; q < n16; q += blockDim.x)
+    cp_async16(reinterpret_cast<char *>(slot) + 16 * q, reinterpret_cast<const char *>(src) + 16 * q);
+}
+
+// distributed shared memory helpers (cluster rank of this CTA; remote address)
+__device__ __forceinline__ unsigned cluster_rank() {
+  unsigned r;
+  asm volatile("mov.u32 %0, %%cluster_ctarank;\n" : "=r"(r));
+  return r;
+}
+__device__ __forceinline__ void cluster_sync() {
+  asm volatile("barrier.cluster.arrive.release.aligned;\nbarrier.cluster.wait.acquire.aligned;\n" ::: "memory");
+}
+template <typename T>
+__device__ __forceinline__ T ld_dsmem(const T *local_addr, unsigned rank);
+template <>
+__device__ __forceinline__ double ld_dsmem<double>(const double *p, unsigned rank) {
+  unsigned sa = (unsigned)__cvta_generic_to_shared(p), ra;
+  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;\n" : "=r"(ra) : "r"(sa), "r"(rank));
+  double v;
+  asm volatile("ld.shared::cluster.f64 %0, [%1];\n" : "=d"(v) : "r"(ra) : "memory");
+  return v;
+}
+template <>
+__device__ __forceinline__ float ld_dsmem<float>(const float *p, unsigned rank) {
+  unsigned sa = (unsigned)__cvta_generic_to_shared(p), ra;
+  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;\n" : "=r"(ra) : "r"(sa), "r"(rank));
+  float v;
+  asm volatile("ld.shared::cluster.f32 %0, [%1];\n" : "=f"(v) : "r"(ra) : "memory");
+  return v;
+}
+
+// The tiles one CTA consumes, in order: for each column block J, Dinv_J (if
+// the CTA owns row block J) then tile(R, J) for its row blocks R >= J.
+struct TileCursor {
+  int J, R, nb, nR, C, q;
+  bool dinv;  // the next chunk of block J is its Dinv
+  __device__ void start(int nb_, int nR_, int C_, int q_, bool forward) {
+    nb = nb_; nR = nR_; C = C_; q = q_;
+    J = forward ? 0 : nb - 1;
+    begin_block(forward);
+  }
+  __device__ int first_owned(int from) const {  // smallest R >= from with R % C == q
+    int r = from + ((q - from % C) + C) % C;
+    return r;
+  }
+  __device__ void begin_block(bool forward) {
+    if (forward) {
+      dinv = (J % C) == q;
+      R = first_owned(J);
+    } else {  // backward: tiles first (descending R), Dinv last
+      dinv = false;
+      int last = nR - 1;
+      R = last - ((last % C) - q + C) % C;  // largest R <= nR-1 owned
+      if (R < J) R = -1;
+    }
+  }
+  __device__ bool valid() const { return J >= 0 && J < nb; }
+  // true for a Dinv chunk, false for a tile chunk (R set)
+  __device__ bool current_is_dinv(bool forward) const {
+    if (forward) return dinv;
+    return R < 0 && (J % C) == q;
+  }
+  __device__ void advance(bool forward) {
+    if (forward) {
+      if (dinv) { dinv = false; }
+      else R += C;
+      if (!dinv && R >= nR) { J++; if (J < nb) begin_block(true); }
+    } else {
+      if (R >= 0) {
+        R -= C;
+        if (R < J) R = -1;
+        if (R < 0 && (J % C) != q) { J--; if (J >= 0) begin_block(false); }
+      } else {  // Dinv consumed
+        J--;
+        if (J >= 0) begin_block(false);
+      }
+    }
+  }
+  // skip positions that hold no chunk (backward block without owned tiles and not owner)
+  __device__ void settle(bool forward) {
+    if (forward) {
+      while (valid() && !dinv && R >= nR) { J++; if (J < nb) begin_block(true); }
+    } else {
+      while (valid() && R < 0 && (J % C) != q) { J--; if (J >= 0) begin_block(false); }
+    }
+  }
+};
+
+template <typename T>
+__device__ __forceinline__ const T *chunk_ptr(const T *base, int J, int R, bool dinv) {
+  // base = start of block J
+  return dinv ? base : base + 1024 * (int64_t)(1 + R - J);
+}
+
+// forward solve, grid = nfronts * C, cluster (C,1,1)
+template <typename T, int C>
+__global__ void __launch_bounds__(kTileThreads)
+mf_fwd_tiles(MfView v, PackView pk, const int *__restrict__ fronts, const T *__restrict__ packed,
+             T *__restrict__ xl, T *__restrict__ uvec) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T *ring = reinterpret_cast<T *>(smem_raw);            // kTileStages x 1024
+  T *wloc = ring + kTileStages * 1024;                  // owned row blocks x 32
+  __shared__ T ybuf[2][32];
+  const unsigned q = C > 1 ? cluster_rank() : 0;
+  const int f = fronts[blockIdx.x / C];
+  const int m = v.f_m[f], k = v.f_k[f];
+  const int fb = pk.f_blk[f], nb = (k + 31) / 32, nR = (m + 31) / 32;
+  const int tid = threadIdx.x;
+  T *x = xl + v.f_xoff[f] + v.f_p0[f];
+  auto loc = [&](int row) -> T & { return wloc[(row / 32) / C * 32 + row % 32]; };
+  auto owned = [&](int row) { return (row / 32) % C == (int)q; };
+  // stream the first chunks
+  TileCursor cur;
+  cur.start(nb, nR, C, q, true);
+  cur.settle(true);
+  for (int st = 0; st < kTileStages; st++) {
+    if (cur.valid()) {
+      issue_tile<T>(ring + st * 1024, chunk_ptr(packed + pk.blk_off[fb + cur.J], cur.J, cur.R, cur.dinv));
+      cur.advance(true);
+      cur.settle(true);
+    }
+    cp_async_commit();
+  }
+  // right-hand side of the owned rows: pivots from xl, then children
+  const int nown = (nR - (int)q + C - 1) / C;
+  for (int i = tid; i < nown * 32; i += kTileThreads) {
+    const int row = ((i / 32) * C + (int)q) * 32 + i % 32;
+    wloc[i] = row < k ? x[row] : T(0);
+  }
+  __syncthreads();
+  for (int ci = v.f_child_ptr[f]; ci < v.f_child_ptr[f + 1]; ci++) {
+    const int c = v.f_children[ci];
+    const int rc = v.f_m[c] - v.f_k[c];
+    const int *rel = v.relmap + v.f_relmap[c];
+    const T *u = uvec + v.f_uoff[c];
+    for (int a = tid; a < rc; a += kTileThreads) {
+      const int row = rel[a];
+      if (owned(row)) loc(row) += u[a];
+    }
+    __syncthreads();
+  }
+  int slot = 0;
+  for (int J = 0; J < nb; J++) {
+    const int J0 = 32 * J, jb = min(32, k - J0);
+    if (J % C == (int)q) {  // owner: y_J = Dinv_J w_J (its Dinv is the next chunk)
+      cp_async_wait<kTileStages - 1>();
+      __syncthreads();
+      const T *S = ring + slot * 1024;
+      if (tid < 32) {
+        T sum = T(0);
+        if (tid < jb)
+          for (int sidx = 0; sidx <= tid; sidx++) sum += S[tid * 32 + sidx] * loc(J0 + sidx);
+        ybuf[J & 1][tid] = sum;
+      }
+      __syncthreads();
+      if (tid < jb) loc(J0 + tid) = ybuf[J & 1][tid];
+      __syncthreads();
+      // refill the consumed slot
+      if (cur.valid()) {
+        issue_tile<T>(ring + slot * 1024, chunk_ptr(packed + pk.blk_off[fb + cur.J], cur.J, cur.R, cur.dinv));
+        cur.advance(true); cur.settle(true);
+      }
+      cp_async_commit();
+      slot = (slot + 1) % kTileStages;
+    }
+    if (C > 1) cluster_sync();
+    __shared__ T yJ[32];
+    if (tid < 32) yJ[tid] = C > 1 ? ld_dsmem<T>(&ybuf[J & 1][tid], (unsigned)(J % C)) : ybuf[J & 1][tid];
+    __syncthreads();
+    // owned tiles of block J
+    for (int R = cur.first_owned(J); R < nR; R += C) {
+      cp_async_wait<kTileStages - 1>();
+      __syncthreads();
+      const T *S = ring + slot * 1024;
+      // 32 rows x 32 columns: 8 threads per row, 4 columns each
+      const int rr = tid >> 3, c4 = (tid & 7) * 4;
+      T part = S[rr * 32 + c4] * yJ[c4] + S[rr * 32 + c4 + 1] * yJ[c4 + 1] +
+               S[rr * 32 + c4 + 2] * yJ[c4 + 2] + S[rr * 32 + c4 + 3] * yJ[c4 + 3];
+      part += __shfl_down_sync(0xffffffffu, part, 4, 8);
+      part += __shfl_down_sync(0xffffffffu, part, 2, 8);
+      part += __shfl_down_sync(0xffffffffu, part, 1, 8);
+      const int row = 32 * R + rr;
+      if ((tid & 7) == 0 && row < m) loc(row) -= part;
+      __syncthreads();
+      if (cur.valid()) {
+        issue_tile<T>(ring + slot * 1024, chunk_ptr(packed + pk.blk_off[fb + cur.J], cur.J, cur.R, cur.dinv));
+        cur.advance(true); cur.settle(true);
+      }
+      cp_async_commit();
+      slot = (slot + 1) % kTileStages;
+    }
+  }
+  cp_async_wait<0>();
+  __syncthreads();
+  for (int i = tid; i < nown * 32; i += kTileThreads) {
+    const int row = ((i / 32) * C + (int)q) * 32 + i % 32;
+    if (row < k) x[row] = wloc[i];
+    else if (row < m) uvec[v.f_uoff[f] + row - k] = wloc[i];
+  }
+  if (C > 1) cluster_sync();  // no CTA leaves while its shared memory may still be read
+}
+
+// backward solve, grid = nfronts * C, cluster (C,1,1)
+template <typename T, int C>
+__global__ void __launch_bounds__(kTileThreads)
+mf_bwd_tiles(MfView v, PackView pk, const int *__restrict__ fronts, const T *__restrict__ packed,
+             T *__restrict__ xl) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T *ring = reinterpret_cast<T *>(smem_raw);
+  T *wloc = ring + kTileStages * 1024;
+  __shared__ T part[2][32];
+  __shared__ T red[8][32];
+  const unsigned q = C > 1 ? cluster_rank() : 0;
+  const int f = fronts[blockIdx.x / C];
+  const int m = v.f_m[f], k = v.f_k[f];
+  const int fb = pk.f_blk[f], nb = (k + 31) / 32, nR = (m + 31) / 32;
+  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+  T *xb = xl + v.f_xoff[f];
+  const int *rows = v.rows + v.f_rows[f];
+  auto loc = [&](int row) -> T & { return wloc[(row / 32) / C * 32 + row % 32]; };
+  TileCursor cur;
+  cur.start(nb, nR, C, q, false);
+  cur.settle(false);
+  for (int st = 0; st < kTileStages; st++) {
+    if (cur.valid()) {
+      issue_tile<T>(ring + st * 1024, chunk_ptr(packed + pk.blk_off[fb + cur.J], cur.J, cur.R, cur.R < 0));
+      cur.advance(false);
+      cur.settle(false);
+    }
+    cp_async_commit();
+  }
+  const int nown = (nR - (int)q + C - 1) / C;
+  for (int i = tid; i < nown * 32; i += kTileThreads) {
+    const int row = ((i / 32) * C + (int)q) * 32 + i % 32;
+    wloc[i] = row < m ? xb[rows[row]] : T(0);
+  }
+  __syncthreads();
+  int slot = 0;
+  for (int J = nb - 1; J >= 0; J--) {
+    const int J0 = 32 * J, jb = min(32, k - J0);
+    // partial t_J = sum over owned R >= J of tile(R,J)^T x_R
+    T acc = T(0);  // thread (wid, lane): column lane, rows wid*4 .. wid*4+3 of each tile
+    const int last = nR - 1;
+    int Rstart = last - ((last % C) - (int)q + C) % C;
+    for (int R = Rstart; R >= J; R -= C) {
+      cp_async_wait<kTileStages - 1>();
+      __syncthreads();
+      const T *S = ring + slot * 1024;
+#pragma unroll
+      for (int t = 0; t < 4; t++) {
+        const int rr = wid * 4 + t;
+        const int row = 32 * R + rr;
+        if (row < m) acc += S[rr * 32 + lane] * loc(row);
+      }
+      __syncthreads();
+      if (cur.valid()) {
+        issue_tile<T>(ring + slot * 1024, chunk_ptr(packed + pk.blk_off[fb + cur.J], cur.J, cur.R, cur.R < 0));
+        cur.advance(false); cur.settle(false);
+      }
+      cp_async_commit();
+      slot = (slot + 1) % kTileStages;
+    }
+    red[wid][lane] = acc;
+    __syncthreads();
+    if (tid < 32) {
+      T s = T(0);
+#pragma unroll
+      for (int w = 0; w < 8; w++) s += red[w][tid];
+      part[J & 1][tid] = s;
+    }
+    __syncthreads();
+    if (C > 1) cluster_sync();
+    if (J % C == (int)q) {  // owner: t_J = y_J - sum of partials; x_J = Dinv_J^T t_J
+      __shared__ T tJ[32];
+      if (tid < 32) {
+        T s = T(0);
+        for (int r = 0; r < C; r++) s += C > 1 ? ld_dsmem<T>(&part[J & 1][tid], (unsigned)r) : part[J & 1][tid];
+        tJ[tid] = tid < jb ? loc(J0 + tid) - s : T(0);
+      }
+      cp_async_wait<kTileStages - 1>();
+      __syncthreads();
+      const T *S = ring + slot * 1024;
+      if (tid < jb) {
+        T sum = T(0);
+        for (int sidx = tid; sidx < jb; sidx++) sum += S[sidx * 32 + tid] * tJ[sidx];
+        loc(J0 + tid) = sum;
+      }
+      __syncthreads();
+      if (cur.valid()) {
+        issue_tile<T>(ring + slot * 1024, chunk_ptr(packed + pk.blk_off[fb + cur.J], cur.J, cur.R, cur.R < 0));
+        cur.advance(false); cur.settle(false);
+      }
+      cp_async_commit();
+      slot = (slot + 1) % kTileStages;
+    }
+  }
+  cp_async_wait<0>();
+  __syncthreads();
+  for (int i = tid; i < nown * 32; i += kTileThreads) {
+    const int row = ((i / 32) * C + (int)q) * 32 + i % 32;
+    if (row < k) xb[rows[row]] = wloc[i];
+  }
+  if (C > 1) cluster_sync();
+}
+
+// ---------------------------------------------------------------------------
+// Small fronts (m <= 128): one warp per front.  The front's factor columns
+// (m x k, contiguous in the arena) are staged in shared memory with cp.async,
+// then the pivots are eliminated from shared memory.
+// ---------------------------------------------------------------------------
+__host__ __device__ __forceinline__ int round4(int x) { return (x + 3) & ~3; }
+
+template <typename T>
+__device__ __forceinline__ void stage_factor_warp(T *Ls, const T *src, int elems) {
+  const int lane = threadIdx.x & 31;
+  const int n16 = (elems * (int)sizeof(T) + 15) / 16;
+  for (int q = lane; q < n16; q += 32)
+    cp_async16(reinterpret_cast<char *>(Ls) + 16 * q, reinterpret_cast<const char *>(src) + 16 * q);
+  cp_async_commit();
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256)
+mf_fwd_warp(MfView v, const int *__restrict__ fronts, int nf, const T *__restrict__ arena,
+            T *__restrict__ xl, T *__restrict__ uvec, int per_warp) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  const int gw = blockIdx.x * nw + wid;
+  if (gw >= nf) return;  // warp-level kernel: no block barriers below
+  T *Ls = reinterpret_cast<T *>(smem_raw) + (size_t)wid * per_warp;
+  const int f = fronts[gw];
+  const int m = v.f_m[f], k = v.f_k[f];
+  T *w = Ls + round4(m * k);
+  stage_factor_warp<T>(Ls, arena + v.f_off[f], m * k);
+  T *x = xl + v.f_xoff[f] + v.f_p0[f];
+  for (int i = lane; i < m; i += 32) w[i] = i < k ? x[i] : T(0);
+  __syncwarp();
+  for (int ci = v.f_child_ptr[f]; ci < v.f_child_ptr[f + 1]; ci++) {
+    const int c = v.f_children[ci];
+    const int rc = v.f_m[c] - v.f_k[c];
+    const int *rel = v.relmap + v.f_relmap[c];
+    const T *u = uvec + v.f_uoff[c];
+    for (int a = lane; a < rc; a += 32) w[rel[a]] += u[a];
+    __syncwarp();
+  }
+  cp_async_wait<0>();
+  __syncwarp();
+  for (int j = 0; j < k; j++) {
+    const T yj = w[j] / Ls[j * m + j];
+    __syncwarp();
+    for (int i = j + 1 + lane; i < m; i += 32) w[i] -= Ls[j * m + i] * yj;
+    if (lane == 0) w[j] = yj;
+    __syncwarp();
+  }
+  for (int i = lane; i < k; i += 32) x[i] = w[i];
+  T *u = uvec + v.f_uoff[f];
+  for (int a = lane; a < m - k; a += 32) u[a] = w[k + a];
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256)
+mf_bwd_warp(MfView v, const int *__restrict__ fronts, int nf, const T *__restrict__ arena,
+            T *__restrict__ xl, int per_warp) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  const int gw = blockIdx.x * nw + wid;
+  if (gw >= nf) return;
+  T *Ls = reinterpret_cast<T *>(smem_raw) + (size_t)wid * per_warp;
+  const int f = fronts[gw];
+  const int m = v.f_m[f], k = v.f_k[f];
+  T *w = Ls + round4(m * k);
+  stage_factor_warp<T>(Ls, arena + v.f_off[f], m * k);
+  T *xb = xl + v.f_xoff[f];
+  const int *rows = v.rows + v.f_rows[f];
+  for (int i = lane; i < m; i += 32) w[i] = xb[rows[i]];
+  cp_async_wait<0>();
+  __syncwarp();
+  for (int j = k - 1; j >= 0; j--) {
+    T sum = T(0);
+    for (int i = j + 1 + lane; i < m; i += 32) sum += Ls[j * m + i] * w[i];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) sum += __shfl_down_sync(0xffffffffu, sum, o);
+    if (lane == 0) w[j] = (w[j] - sum) / Ls[j * m + j];
+    __syncwarp();
+  }
+  for (int i = lane; i < k; i += 32) xb[rows[i]] = w[i];
+}
+
+// ---------------------------------------------------------------------------
 // Schwarz gather / pull sum and coarse transfer
 // ---------------------------------------------------------------------------
 template <typename T>

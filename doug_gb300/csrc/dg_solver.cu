@@ -64,6 +64,7 @@ static double wall() {
 // one multifrontal batch on the device, factor precision T
 constexpr int kLargeFront = 256;      // fronts above this size use the multi-CTA pipeline
 constexpr int kMaxSolveSmem = 200 * 1024;
+constexpr int kSolveLarge = 128;      // fronts above this size use the packed, pipelined solves
 
 template <typename T>
 struct MfDevice {
@@ -71,7 +72,17 @@ struct MfDevice {
   DBuf<int> f_m, f_k, f_p0, f_child_ptr, f_children, rows, relmap, lvl_fronts, gidx;
   DBuf<int> small_fronts, tiny_fronts, diag_fronts;
   DBuf<int2> asm_tasks, upd_tasks, panel_tasks;
-  DBuf<T> arena, xl, u, w;
+  DBuf<T> arena, xl, u, w, packed;
+  DBuf<int> blk_front, blk_j, f_blk, solve_small, solve_large;
+  DBuf<int64_t> blk_off;
+  int nblk = 0;
+  struct SolveLevel {
+    int small_off, small_cnt, large_off, large_cnt;
+    int per_warp, warps, C;
+    size_t warp_smem, tile_smem;
+  };
+  std::vector<SolveLevel> slevels;
+  PackView pview{};
   std::vector<int> lvl_ptr, lvl_max_m;
   // per level: small-front range, assembly-task range, steps
   struct Step { int j0, diag_off, diag_cnt, panel_off, panel_cnt; int64_t upd_off, upd_cnt; };
@@ -157,6 +168,104 @@ struct MfDevice {
     upd_tasks.upload(ut);
     CK(cudaFuncSetAttribute(mf_fwd_level<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxSolveSmem));
     CK(cudaFuncSetAttribute(mf_bwd_level<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxSolveSmem));
+    // tiled solve layout for the fronts above kSolveLarge rows
+    {
+      std::vector<int> bf, bj, fblk((size_t)nfronts, -1), ss, sl;
+      std::vector<int64_t> bo;
+      int64_t len = 0;
+      for (int f = 0; f < nfronts; f++) {
+        int m = B.f_m[(size_t)f], k = B.f_k[(size_t)f];
+        if (m <= kSolveLarge) continue;
+        fblk[(size_t)f] = (int)bf.size();
+        const int nR = (m + 31) / 32;
+        for (int J = 0; 32 * J < k; J++) {
+          bf.push_back(f);
+          bj.push_back(J);
+          bo.push_back(len);
+          len += 1024 * (int64_t)(1 + nR - J);
+        }
+      }
+      nblk = (int)bf.size();
+      blk_front.upload(bf); blk_j.upload(bj); f_blk.upload(fblk); blk_off.upload(bo);
+      packed.alloc((size_t)std::max<int64_t>(len, 1));
+      pview = PackView{blk_front.p, blk_j.p, f_blk.p, blk_off.p};
+      int dev = 0, optin = 0, nsm = 0;
+      CK(cudaGetDevice(&dev));
+      CK(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+      CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+      slevels.assign((size_t)nlevels, SolveLevel());
+      for (int l = 0; l < nlevels; l++) {
+        SolveLevel &L = slevels[(size_t)l];
+        L.small_off = (int)ss.size();
+        L.large_off = (int)sl.size();
+        int per_warp = 0, maxnR = 0;
+        for (int q = B.lvl_ptr[(size_t)l]; q < B.lvl_ptr[(size_t)l + 1]; q++) {
+          int f = B.lvl_fronts[(size_t)q];
+          int m = B.f_m[(size_t)f], k = B.f_k[(size_t)f];
+          if (m > kSolveLarge) { sl.push_back(f); maxnR = std::max(maxnR, (m + 31) / 32); }
+          else { ss.push_back(f); per_warp = std::max(per_warp, round4(m * k) + round4(m)); }
+        }
+        L.small_cnt = (int)ss.size() - L.small_off;
+        L.large_cnt = (int)sl.size() - L.large_off;
+        L.per_warp = per_warp;
+        L.warps = std::max(1, std::min(8, (int)((96 * 1024) / std::max<size_t>(1, (size_t)per_warp * sizeof(T)))));
+        L.warp_smem = (size_t)L.warps * per_warp * sizeof(T);
+        if (L.small_cnt && L.warp_smem > (size_t)optin)
+          throw CudaError{cudaErrorInvalidValue, "small front too large for the warp solve"};
+        // cluster size: enough CTAs for the machine, at most 8, at most the row blocks
+        int C = 1;
+        while (C < 8 && L.large_cnt * C < 2 * nsm && C * 2 <= maxnR) C *= 2;
+        L.C = C;
+        L.tile_smem = (size_t)kTileStages * 1024 * sizeof(T) + (size_t)((maxnR + C - 1) / C) * 32 * sizeof(T);
+        if (L.large_cnt && L.tile_smem > (size_t)optin - 1024)
+          throw CudaError{cudaErrorInvalidValue, "front too large for the shared-memory solve"};
+      }
+      solve_small.upload(ss);
+      solve_large.upload(sl);
+      CK(cudaFuncSetAttribute(mf_fwd_warp<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
+      CK(cudaFuncSetAttribute(mf_bwd_warp<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
+      set_tile_attrs<1>(optin);
+      set_tile_attrs<2>(optin);
+      set_tile_attrs<4>(optin);
+      set_tile_attrs<8>(optin);
+    }
+  }
+
+  template <int C>
+  void set_tile_attrs(int optin) {
+    cudaFuncAttributes fa{}, fb{};
+    CK(cudaFuncGetAttributes(&fa, mf_fwd_tiles<T, C>));
+    CK(cudaFuncGetAttributes(&fb, mf_bwd_tiles<T, C>));
+    const int dyn = optin - (int)std::max(fa.sharedSizeBytes, fb.sharedSizeBytes);
+    CK(cudaFuncSetAttribute(mf_fwd_tiles<T, C>, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn));
+    CK(cudaFuncSetAttribute(mf_bwd_tiles<T, C>, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn));
+  }
+
+  template <int C>
+  void launch_tiles(bool fwd, int nfr, const int *fr, size_t smem, cudaStream_t s) {
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = dim3((unsigned)(nfr * C));
+    cfg.blockDim = dim3(kTileThreads);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = C;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    if (fwd) CK(cudaLaunchKernelEx(&cfg, mf_fwd_tiles<T, C>, view, pview, fr, (const T *)packed.p, xl.p, u.p));
+    else CK(cudaLaunchKernelEx(&cfg, mf_bwd_tiles<T, C>, view, pview, fr, (const T *)packed.p, xl.p));
+  }
+
+  void tiles_any(int C, bool fwd, int nfr, const int *fr, size_t smem, cudaStream_t s) {
+    switch (C) {
+      case 1: launch_tiles<1>(fwd, nfr, fr, smem, s); break;
+      case 2: launch_tiles<2>(fwd, nfr, fr, smem, s); break;
+      case 4: launch_tiles<4>(fwd, nfr, fr, smem, s); break;
+      default: launch_tiles<8>(fwd, nfr, fr, smem, s); break;
+    }
   }
 
   int factor(const double *vals, int *status, cudaStream_t s) {
@@ -193,28 +302,40 @@ struct MfDevice {
         }
       }
     }
+    if (nblk) {  // packed solve layout of the large fronts
+      mf_pack<T><<<nblk, 256, 0, s>>>(view, pview, arena.p, packed.p);
+      launches++;
+    }
     return launches;
   }
 
   int solve(cudaStream_t s) {  // in place on xl
     int launches = 0;
     for (int l = 0; l < nlevels; l++) {
-      int nf = lvl_ptr[(size_t)l + 1] - lvl_ptr[(size_t)l];
-      if (!nf) continue;
-      size_t sm = (size_t)lvl_max_m[(size_t)l] * sizeof(T);
-      int use = sm <= (size_t)kMaxSolveSmem;
-      mf_fwd_level<T><<<nf, kMfThreads, use ? sm : 0, s>>>(view, lvl_fronts.p + lvl_ptr[(size_t)l], arena.p,
-                                                            xl.p, u.p, w.p, use);
-      launches++;
+      const SolveLevel &L = slevels[(size_t)l];
+      if (L.small_cnt) {
+        int blocks = (L.small_cnt + L.warps - 1) / L.warps;
+        mf_fwd_warp<T><<<blocks, 32 * L.warps, L.warp_smem, s>>>(view, solve_small.p + L.small_off, L.small_cnt,
+                                                                  arena.p, xl.p, u.p, L.per_warp);
+        launches++;
+      }
+      if (L.large_cnt) {
+        tiles_any(L.C, true, L.large_cnt, solve_large.p + L.large_off, L.tile_smem, s);
+        launches++;
+      }
     }
     for (int l = nlevels - 1; l >= 0; l--) {
-      int nf = lvl_ptr[(size_t)l + 1] - lvl_ptr[(size_t)l];
-      if (!nf) continue;
-      size_t sm = (size_t)lvl_max_m[(size_t)l] * sizeof(T);
-      int use = sm <= (size_t)kMaxSolveSmem;
-      mf_bwd_level<T><<<nf, kMfThreads, use ? sm : 0, s>>>(view, lvl_fronts.p + lvl_ptr[(size_t)l], arena.p,
-                                                            xl.p, w.p, use);
-      launches++;
+      const SolveLevel &L = slevels[(size_t)l];
+      if (L.large_cnt) {
+        tiles_any(L.C, false, L.large_cnt, solve_large.p + L.large_off, L.tile_smem, s);
+        launches++;
+      }
+      if (L.small_cnt) {
+        int blocks = (L.small_cnt + L.warps - 1) / L.warps;
+        mf_bwd_warp<T><<<blocks, 32 * L.warps, L.warp_smem, s>>>(view, solve_small.p + L.small_off, L.small_cnt,
+                                                                  arena.p, xl.p, L.per_warp);
+        launches++;
+      }
     }
     return launches;
   }
@@ -254,7 +375,12 @@ struct dg_handle {
   double *d_host_out = nullptr;
   int *d_host_status = nullptr;
   cudaEvent_t ev[10]{};
+  cudaStream_t s2 = nullptr;        // coarse-level stream (runs beside the subdomain solves)
+  cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
   ~dg_handle() {
+    if (s2) cudaStreamDestroy(s2);
+    if (fork_ev) cudaEventDestroy(fork_ev);
+    if (join_ev) cudaEventDestroy(join_ev);
     if (host_out) cudaFreeHost(host_out);
     if (host_status) cudaFreeHost(host_status);
     for (auto &e : ev) if (e) cudaEventDestroy(e);
@@ -395,6 +521,9 @@ dg_status do_setup(dg_handle *h) {
       CK(cudaHostGetDevicePointer(&h->d_host_out, h->host_out, 0));
       CK(cudaHostGetDevicePointer(&h->d_host_status, h->host_status, 0));
       for (auto &e : h->ev) CK(cudaEventCreate(&e));
+      CK(cudaStreamCreateWithFlags(&h->s2, cudaStreamNonBlocking));
+      CK(cudaEventCreateWithFlags(&h->fork_ev, cudaEventDisableTiming));
+      CK(cudaEventCreateWithFlags(&h->join_ev, cudaEventDisableTiming));
     }
     // transfer operators
     h->Rp.upload(S.R.ptr); h->Rc.upload(S.R.col); h->Rv.upload(S.R.val);
@@ -460,8 +589,14 @@ dg_status do_solve(dg_handle *h, const double *d_b, double *d_x, dg_stats *st, c
     CK(cudaEventRecord(h->ev[0], s));
     // numeric factorisations (the reference factorises lazily in the first
     // preconditioner call, subsolvers.F90:78-101, pcg.F90:166-178)
+    if (coarse) {  // the coarse factorisation runs beside the subdomain factorisations
+      CK(cudaEventRecord(h->fork_ev, s));
+      CK(cudaStreamWaitEvent(h->s2, h->fork_ev, 0));
+      launches += h->co64->factor(h->ACv.p, h->status.p, h->s2);
+      CK(cudaEventRecord(h->join_ev, h->s2));
+    }
     if (fine) launches += mixed ? h->sub32->factor(h->Av.p, h->status.p, s) : h->sub64->factor(h->Av.p, h->status.p, s);
-    if (coarse) launches += h->co64->factor(h->ACv.p, h->status.p, s);
+    if (coarse) CK(cudaStreamWaitEvent(s, h->join_ev, 0));
     CK(cudaEventRecord(h->ev[1], s));
     CK(cudaMemcpyAsync(h->b.p, d_b, (size_t)n * sizeof(double), cudaMemcpyDeviceToDevice, s));
     CK(cudaMemsetAsync(h->x.p, 0, (size_t)n * sizeof(double), s));
@@ -471,6 +606,7 @@ dg_status do_solve(dg_handle *h, const double *d_b, double *d_x, dg_stats *st, c
     resid_any(h->lanes, grid, s, h, h->x.p, h->b.p, h->r.p);
     cg_finish<<<1, 32, 0, s>>>(h->sc.p, h->part_rr.p, 1, h->d_host_out, h->status.p, h->d_host_status);
     launches += 2;
+    CK(cudaGetLastError());
     CK(cudaStreamSynchronize(s));
     if (*h->host_status & ERR_NOT_SPD)
       return fail(h, DG_SINGULAR, "a subdomain or coarse matrix is not positive definite");
@@ -504,6 +640,18 @@ dg_status do_solve(dg_handle *h, const double *d_b, double *d_x, dg_stats *st, c
     while (ratio > tol * tol && it < maxit) {
       it++;
       const int first = it == 1;
+      if (coarse) {  // restriction + coarse solve on the second stream
+        CK(cudaEventRecord(h->fork_ev, s));
+        CK(cudaStreamWaitEvent(h->s2, h->fork_ev, 0));
+        if (prof) CK(cudaEventRecord(h->ev[4], h->s2));
+        if (mixed)
+          restrict_to_coarse<float><<<grid, kVecThreads, 0, h->s2>>>(h->Rp.p, h->Rc.p, h->Rvf.p, h->r.p, h->cpos.p, h->co64->xl.p, h->S.R.nrows);
+        else
+          restrict_to_coarse<double><<<grid, kVecThreads, 0, h->s2>>>(h->Rp.p, h->Rc.p, h->Rv.p, h->r.p, h->cpos.p, h->co64->xl.p, h->S.R.nrows);
+        launches += 1 + h->co64->solve(h->s2);
+        if (prof) CK(cudaEventRecord(h->ev[5], h->s2));
+        CK(cudaEventRecord(h->join_ev, h->s2));
+      }
       if (prof) CK(cudaEventRecord(h->ev[3], s));
       if (fine) {
         if (mixed) {
@@ -514,15 +662,8 @@ dg_status do_solve(dg_handle *h, const double *d_b, double *d_x, dg_stats *st, c
           launches += 1 + h->sub64->solve(s);
         }
       }
-      if (prof) CK(cudaEventRecord(h->ev[4], s));
-      if (coarse) {
-        if (mixed)
-          restrict_to_coarse<float><<<grid, kVecThreads, 0, s>>>(h->Rp.p, h->Rc.p, h->Rvf.p, h->r.p, h->cpos.p, h->co64->xl.p, h->S.R.nrows);
-        else
-          restrict_to_coarse<double><<<grid, kVecThreads, 0, s>>>(h->Rp.p, h->Rc.p, h->Rv.p, h->r.p, h->cpos.p, h->co64->xl.p, h->S.R.nrows);
-        launches += 1 + h->co64->solve(s);
-      }
-      if (prof) CK(cudaEventRecord(h->ev[5], s));
+      if (prof) CK(cudaEventRecord(h->ev[8], s));
+      if (coarse) CK(cudaStreamWaitEvent(s, h->join_ev, 0));
       const double *xc = coarse ? h->co64->xl.p : nullptr;
       if (mixed)
         pull_prolong_dot<float, float><<<grid, kVecThreads, 0, s>>>(
@@ -545,8 +686,13 @@ dg_status do_solve(dg_handle *h, const double *d_b, double *d_x, dg_stats *st, c
       }
       cg_finish<<<1, 32, 0, s>>>(h->sc.p, h->part_rr.p, 0, h->d_host_out, h->status.p, h->d_host_status);
       launches++;
+      CK(cudaGetLastError());  // a failed launch must not pass as a converged step
       CK(cudaStreamSynchronize(s));
-      if (prof) { t_sub += lap(3, 4); t_co += lap(4, 5); t_sp += lap(6, 7); }
+      if (prof) {
+        t_sub += lap(3, 8);
+        if (coarse) t_co += lap(4, 5);
+        t_sp += lap(6, 7);
+      }
       res = h->host_out[0];
       double alpha = h->host_out[2], beta = h->host_out[3], pq = h->host_out[5];
       alphas.push_back(alpha);

@@ -275,7 +275,7 @@ void append(const Local &L, const std::vector<int> &gid_of_local, MfBatch &B) {
     int m = (int)L.rows[(size_t)f].size(), k = L.k[(size_t)f];
     foff[(size_t)f] = B.arena;
     B.f_off.push_back(B.arena);
-    B.arena += (int64_t)m * m;
+    B.arena += ((int64_t)m * m + 3) & ~(int64_t)3;  // 16-byte aligned fronts (cp.async staging)
     B.f_m.push_back(m);
     B.f_k.push_back(k);
     B.f_rows.push_back((int64_t)B.rows.size());
@@ -354,6 +354,7 @@ void append(const Local &L, const std::vector<int> &gid_of_local, MfBatch &B) {
 
 void finalize(MfBatch &B) {
   B.xoff.push_back(B.xlen);
+  B.arena += 16;  // slack: staging copies round the last front up to 16 bytes
   B.f_child_ptr.push_back((int)B.f_children.size());
   B.f_asm.push_back((int64_t)B.asm_tgt.size());
   B.asm_sp.push_back((int64_t)B.asm_src.size());
