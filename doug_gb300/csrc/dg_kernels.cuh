@@ -584,7 +584,11 @@ mf_bwd_level(MfView v, const int *__restrict__ fronts, const T *__restrict__ are
 // one-CTA solve.
 // ---------------------------------------------------------------------------
 constexpr int kTileThreads = 256;
-constexpr int kTileStages = 8;
+// cp.async stages per CTA: enough 32x32 tiles in flight to cover the memory
+// latency (16 x 4 KB for FP32, 8 x 8 KB for FP64)
+template <typename T> struct TileStages;
+template <> struct TileStages<float> { static constexpr int S = 16; };
+template <> struct TileStages<double> { static constexpr int S = 8; };
 
 struct PackView {
   const int *blk_front;        // block -> front
@@ -745,6 +749,7 @@ template <typename T, int C>
 __global__ void __launch_bounds__(kTileThreads)
 mf_fwd_tiles(MfView v, PackView pk, const int *__restrict__ fronts, const T *__restrict__ packed,
              T *__restrict__ xl, T *__restrict__ uvec) {
+  constexpr int kTileStages = TileStages<T>::S;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T *ring = reinterpret_cast<T *>(smem_raw);            // kTileStages x 1024
   T *wloc = ring + kTileStages * 1024;                  // owned row blocks x 32
@@ -853,6 +858,7 @@ template <typename T, int C>
 __global__ void __launch_bounds__(kTileThreads)
 mf_bwd_tiles(MfView v, PackView pk, const int *__restrict__ fronts, const T *__restrict__ packed,
              T *__restrict__ xl) {
+  constexpr int kTileStages = TileStages<T>::S;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T *ring = reinterpret_cast<T *>(smem_raw);
   T *wloc = ring + kTileStages * 1024;

@@ -216,7 +216,7 @@ struct MfDevice {
         int C = 1;
         while (C < 8 && L.large_cnt * C < 2 * nsm && C * 2 <= maxnR) C *= 2;
         L.C = C;
-        L.tile_smem = (size_t)kTileStages * 1024 * sizeof(T) + (size_t)((maxnR + C - 1) / C) * 32 * sizeof(T);
+        L.tile_smem = (size_t)TileStages<T>::S * 1024 * sizeof(T) + (size_t)((maxnR + C - 1) / C) * 32 * sizeof(T);
         if (L.large_cnt && L.tile_smem > (size_t)optin - 1024)
           throw CudaError{cudaErrorInvalidValue, "front too large for the shared-memory solve"};
       }
