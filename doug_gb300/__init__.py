@@ -24,7 +24,7 @@ import numpy as np
 
 from .build import LIB as _LIB_PATH, build as build_library
 
-__all__ = ["DougSolver", "DougError", "SolveStats", "load_library", "build_library",
+__all__ = ["DougSolver", "DougError", "SolveStats", "load_library", "build_library", "residual_csr",
            "DG_OK", "DG_NOT_CONVERGED", "DG_BREAKDOWN", "DG_SINGULAR", "DG_BAD_INPUT",
            "DG_CUDA_ERROR", "DG_NO_DEVICE", "DG_NOT_READY", "EXPORTED_SYMBOLS"]
 
@@ -37,7 +37,7 @@ EXPORTED_SYMBOLS = [
     "dg_create", "dg_destroy", "dg_last_error", "dg_set_option", "dg_load_ctl",
     "dg_set_matrix_coo", "dg_set_rhs", "dg_set_partition", "dg_setup", "dg_solve",
     "dg_solve_device", "dg_write_solution", "dg_get_sizes", "dg_get_aggregates",
-    "dg_get_subdomains", "dg_get_restriction", "dg_get_coarse_matrix",
+    "dg_get_subdomains", "dg_get_restriction", "dg_get_coarse_matrix", "dg_residual_csr",
 ]
 
 
@@ -118,6 +118,7 @@ def load_library(path: str | None = None):
     L.dg_get_subdomains.argtypes = [vp, P(C.c_longlong), P(C.c_int)]
     L.dg_get_restriction.argtypes = [vp, P(C.c_int), P(C.c_int), P(C.c_double)]
     L.dg_get_coarse_matrix.argtypes = [vp, P(C.c_int), P(C.c_int), P(C.c_double)]
+    L.dg_residual_csr.argtypes = [C.c_int, vp, vp, vp, vp, vp, vp, vp, vp]
     for nm in EXPORTED_SYMBOLS:
         if nm not in ("dg_destroy", "dg_last_error"):
             getattr(L, nm).restype = C.c_int
@@ -132,6 +133,21 @@ def _ip(a):
 
 def _dp(a):
     return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def residual_csr(rowptr, col, val, x, b, stream: int = 0):
+    """r = b - A x and ||r||^2 on the GPU for torch CUDA tensors (CSR with
+    int64 row pointers, int32 columns, float64 values).  Returns (r, norm2)."""
+    import torch
+    L = load_library()
+    n = x.numel()
+    r = torch.empty_like(x)
+    nrm = torch.empty(1, dtype=torch.float64, device=x.device)
+    rc = L.dg_residual_csr(n, rowptr.data_ptr(), col.data_ptr(), val.data_ptr(), x.data_ptr(),
+                           b.data_ptr(), r.data_ptr(), nrm.data_ptr(), stream)
+    if rc != DG_OK:
+        raise DougError(rc, "dg_residual_csr failed")
+    return r, nrm
 
 
 class DougSolver:

@@ -18,7 +18,7 @@ LIB = os.path.join(OUT, "libdouggpu.so")
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 
 HOST_SRC = ["host/setup.cpp", "host/mf_symbolic.cpp"]
-CUDA_SRC = ["dg_solver.cu"]
+CUDA_SRC = ["dg_solver.cu", "dg_residual.cu"]
 
 
 def _nvcc() -> str:

@@ -1,0 +1,92 @@
+// FP64 true residual r = b - A x and ||r||_2^2 for a CSR matrix on the GPU.
+//
+// The reference computes this residual before the PCG loop
+// (src/solvers/pcg.F90:364-367) and, in doug_geom, after it
+// (src/main/geom.F90:135-142).  The solver uses the same arithmetic
+// internally; this file exposes it to callers that hold their own device
+// CSR matrix (for example to check a solution written by dg_solve_device).
+//
+// The norm is reduced deterministically: each block of kResidRowsPerBlock
+// rows writes one partial sum, and one block adds the partials in order.
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "../../include/doug_gpu.h"
+
+namespace dg {
+namespace resid {
+
+constexpr int kThreads = 256;
+constexpr int kLanes = 8;                         // lanes per row
+constexpr int kRowsPerBlock = 1024;               // rows per partial sum
+
+// r = b - A x for rows [blk*1024, (blk+1)*1024); partial[blk] = sum r_i^2
+__global__ void __launch_bounds__(kThreads)
+residual_partials(int n, const long long *__restrict__ rp, const int *__restrict__ col,
+                  const double *__restrict__ val, const double *__restrict__ x,
+                  const double *__restrict__ b, double *__restrict__ r, double *__restrict__ partial) {
+  __shared__ double sh[kThreads / 32];
+  const int sub = threadIdx.x % kLanes;
+  const int row_in_pass = threadIdx.x / kLanes;   // 32 rows per pass
+  const int r0 = blockIdx.x * kRowsPerBlock;
+  double acc = 0.0;
+  for (int pass = 0; pass < kRowsPerBlock / (kThreads / kLanes); pass++) {
+    const int i = r0 + pass * (kThreads / kLanes) + row_in_pass;
+    double s = 0.0;
+    if (i < n)
+      for (long long e = rp[i] + sub; e < rp[i + 1]; e += kLanes) s = __fma_rn(val[e], x[col[e]], s);
+#pragma unroll
+    for (int o = kLanes / 2; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o, kLanes);
+    if (i < n && sub == 0) {
+      const double ri = __dsub_rn(b[i], s);
+      r[i] = ri;
+      acc += ri * ri;
+    }
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int w = 0; w < kThreads / 32; w++) t += sh[w];
+    partial[blockIdx.x] = t;
+  }
+}
+
+// out = sum of partial[0..np) in a fixed order (one block)
+__global__ void __launch_bounds__(kThreads)
+sum_partials_ordered(int np, const double *__restrict__ partial, double *__restrict__ out) {
+  __shared__ double sh[kThreads];
+  double s = 0.0;
+  for (int q = threadIdx.x; q < np; q += kThreads) s += partial[q];
+  sh[threadIdx.x] = s;
+  __syncthreads();
+  for (int w = kThreads / 2; w > 0; w >>= 1) {
+    if (threadIdx.x < w) sh[threadIdx.x] += sh[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *out = sh[0];
+}
+
+int blocks_for(int n) { return (n + kRowsPerBlock - 1) / kRowsPerBlock; }
+
+}  // namespace resid
+}  // namespace dg
+
+extern "C" dg_status dg_residual_csr(int n, const long long *d_rowptr, const int *d_col,
+                                     const double *d_val, const double *d_x, const double *d_b,
+                                     double *d_r, double *d_norm2, void *cuda_stream) {
+  using namespace dg::resid;
+  if (n <= 0 || !d_rowptr || !d_col || !d_val || !d_x || !d_b || !d_r || !d_norm2) return DG_BAD_INPUT;
+  cudaStream_t s = (cudaStream_t)cuda_stream;
+  const int nb = blocks_for(n);
+  double *partial = nullptr;
+  if (cudaMallocAsync(&partial, (size_t)nb * sizeof(double), s) != cudaSuccess) return DG_CUDA_ERROR;
+  residual_partials<<<nb, kThreads, 0, s>>>(n, d_rowptr, d_col, d_val, d_x, d_b, d_r, partial);
+  sum_partials_ordered<<<1, kThreads, 0, s>>>(nb, partial, d_norm2);
+  cudaError_t e = cudaGetLastError();
+  cudaFreeAsync(partial, s);
+  return e == cudaSuccess ? DG_OK : DG_CUDA_ERROR;
+}

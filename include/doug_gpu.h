@@ -116,6 +116,16 @@ dg_status dg_solve_device(dg_handle *h, const double *d_b, double *d_x, dg_stats
 /* Write x with the control file's solution_file / solution_format. */
 dg_status dg_write_solution(dg_handle *h, const double *x);
 
+/* FP64 true residual of a caller-held CSR matrix on the device:
+ * r = b - A x and *d_norm2 = ||r||_2^2 (all device pointers, 0-based CSR with
+ * 64-bit row pointers), on the given CUDA stream.  The same arithmetic as the
+ * reference's initial residual (src/solvers/pcg.F90:364-367) and doug_geom's
+ * final residual check (src/main/geom.F90:135-142).  Uses stream-ordered
+ * scratch (cudaMallocAsync) for the partial sums. */
+dg_status dg_residual_csr(int n, const long long *d_rowptr, const int *d_col, const double *d_val,
+                          const double *d_x, const double *d_b, double *d_r, double *d_norm2,
+                          void *cuda_stream);
+
 /* Size queries and parity export (1-based ids as in the reference). */
 dg_status dg_get_sizes(const dg_handle *h, int *n, int *nagr_fine, int *nagr_coarse,
                        int *nsubdomains, long long *subdomain_total, int *R_nnz, int *AC_nnz);

@@ -152,3 +152,26 @@ def test_large_fronts_multi_cta_path(precision):
     # term): a few steps; FP32 factors gain ~7 digits per step
     assert st.iterations <= (3 if precision == 0 else 8)
     assert np.linalg.norm(x - xd) <= (1e-9 if precision == 0 else 1e-7) * np.linalg.norm(xd)
+
+
+def _csr_tensors(n, r, c, v):
+    import scipy.sparse as sp
+    torch = pytest.importorskip("torch")
+    A = sp.csr_matrix((v, (r - 1, c - 1)), shape=(n, n))
+    return (A, torch.tensor(A.indptr, dtype=torch.int64, device="cuda"),
+            torch.tensor(A.indices, dtype=torch.int32, device="cuda"),
+            torch.tensor(A.data, dtype=torch.float64, device="cuda"))
+
+
+def test_true_residual_entry_matches_numpy():
+    torch = pytest.importorskip("torch")
+    n, r, c, v, b = P.diffusion3d_fv(24, seed=7)
+    A, rp, ci, vv = _csr_tensors(n, r, c, v)
+    x = np.random.default_rng(0).uniform(-1, 1, n)
+    xt = torch.tensor(x, device="cuda")
+    bt = torch.tensor(b, device="cuda")
+    res, nrm = D.residual_csr(rp, ci, vv, xt, bt)
+    torch.cuda.synchronize()
+    ref = b - A @ x
+    assert np.allclose(res.cpu().numpy(), ref, rtol=0, atol=1e-12 * np.abs(ref).max())
+    assert abs(nrm.item() - ref @ ref) <= 1e-12 * (ref @ ref)
