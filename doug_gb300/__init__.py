@@ -38,6 +38,7 @@ EXPORTED_SYMBOLS = [
     "dg_set_matrix_coo", "dg_set_rhs", "dg_set_partition", "dg_setup", "dg_solve",
     "dg_solve_device", "dg_write_solution", "dg_get_sizes", "dg_get_aggregates",
     "dg_get_subdomains", "dg_get_restriction", "dg_get_coarse_matrix", "dg_residual_csr",
+    "dg_residual_csr_noalloc",
 ]
 
 
@@ -119,6 +120,7 @@ def load_library(path: str | None = None):
     L.dg_get_restriction.argtypes = [vp, P(C.c_int), P(C.c_int), P(C.c_double)]
     L.dg_get_coarse_matrix.argtypes = [vp, P(C.c_int), P(C.c_int), P(C.c_double)]
     L.dg_residual_csr.argtypes = [C.c_int, vp, vp, vp, vp, vp, vp, vp, vp]
+    L.dg_residual_csr_noalloc.argtypes = [C.c_int, vp, vp, vp, vp, vp, vp, vp, vp]
     for nm in EXPORTED_SYMBOLS:
         if nm not in ("dg_destroy", "dg_last_error"):
             getattr(L, nm).restype = C.c_int

@@ -11,6 +11,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <mutex>
 
 #include "../../include/doug_gpu.h"
 
@@ -89,4 +90,69 @@ extern "C" dg_status dg_residual_csr(int n, const long long *d_rowptr, const int
   cudaError_t e = cudaGetLastError();
   cudaFreeAsync(partial, s);
   return e == cudaSuccess ? DG_OK : DG_CUDA_ERROR;
+}
+
+// ---------------------------------------------------------------------------
+// Allocation-free variant.
+//
+// Some callers cannot allocate device memory at the point where they need
+// the residual: an application that hands all device memory to its own pool
+// and forbids other allocations, code that runs while another component is
+// capturing the stream into a CUDA graph (where cudaMalloc is not allowed),
+// or a latency-critical loop that must not pay for an allocation's implicit
+// synchronisation.  dg_residual_csr_noalloc gives them the same result as
+// dg_residual_csr without calling cudaMalloc, cudaFree or any allocating
+// routine: its partial sums live in the fixed array below, which is part of
+// the library image and stays resident on every GPU that loads the library
+// until the process exits.
+// ---------------------------------------------------------------------------
+namespace dg {
+namespace resid {
+
+constexpr int kNoAllocMaxPartials = 65536;  // 512 KiB of doubles
+constexpr long long kNoAllocMaxRows = (long long)kNoAllocMaxPartials * kRowsPerBlock;  // 67,108,864
+
+static __device__ __align__(256) double g_noalloc_partials[kNoAllocMaxPartials];
+
+// Host code may not use g_noalloc_partials as an address: on the host the
+// name refers to a stand-in variable, not to device memory.  The device
+// address is looked up once per device (with that device current) and cached.
+constexpr int kMaxDevices = 128;
+static double *g_noalloc_ptr[kMaxDevices];
+static std::mutex g_noalloc_mu;
+
+static cudaError_t noalloc_scratch(double **out) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
+  std::lock_guard<std::mutex> lk(g_noalloc_mu);
+  if (!g_noalloc_ptr[dev]) {
+    double *p = nullptr;
+    e = cudaGetSymbolAddress(reinterpret_cast<void **>(&p), g_noalloc_partials);
+    if (e != cudaSuccess) return e;
+    g_noalloc_ptr[dev] = p;
+  }
+  *out = g_noalloc_ptr[dev];
+  return cudaSuccess;
+}
+
+}  // namespace resid
+}  // namespace dg
+
+extern "C" dg_status dg_residual_csr_noalloc(int n, const long long *d_rowptr, const int *d_col,
+                                             const double *d_val, const double *d_x, const double *d_b,
+                                             double *d_r, double *d_norm2, void *cuda_stream) {
+  using namespace dg::resid;
+  if (n <= 0 || !d_rowptr || !d_col || !d_val || !d_x || !d_b || !d_r || !d_norm2) return DG_BAD_INPUT;
+  if ((long long)n > kNoAllocMaxRows) return DG_BAD_INPUT;  // the fixed scratch holds 65,536 partials
+  double *partial = nullptr;
+  if (noalloc_scratch(&partial) != cudaSuccess) return DG_CUDA_ERROR;
+  cudaStream_t s = (cudaStream_t)cuda_stream;
+  const int nb = blocks_for(n);
+  // every partial of [0, nb) is written before it is read, so the contents
+  // left by an earlier call need no clearing
+  residual_partials<<<nb, kThreads, 0, s>>>(n, d_rowptr, d_col, d_val, d_x, d_b, d_r, partial);
+  sum_partials_ordered<<<1, kThreads, 0, s>>>(nb, partial, d_norm2);
+  return cudaGetLastError() == cudaSuccess ? DG_OK : DG_CUDA_ERROR;
 }

@@ -126,6 +126,22 @@ dg_status dg_residual_csr(int n, const long long *d_rowptr, const int *d_col, co
                           const double *d_x, const double *d_b, double *d_r, double *d_norm2,
                           void *cuda_stream);
 
+/* The same residual without any device allocation, for callers that cannot
+ * allocate at this point (a caller-owned memory pool that forbids other
+ * allocations, a stream being captured into a CUDA graph, a loop that must
+ * not pay for cudaMalloc's synchronisation).  This entry point has no
+ * counterpart in the reference.  Its partial sums use a fixed 512 KiB array
+ * inside the library that every GPU loading the library keeps until the
+ * process exits; n may be at most 67,108,864 (65,536 partial sums of 1,024
+ * rows), larger n returns DG_BAD_INPUT.  The first call on each device looks
+ * up the array's device address (the calling thread's current device must be
+ * the stream's device), so make that first call before any stream capture.
+ * All calls share the array: calls that overlap on the GPU (other streams,
+ * other threads) race and must be serialised by the caller. */
+dg_status dg_residual_csr_noalloc(int n, const long long *d_rowptr, const int *d_col,
+                                  const double *d_val, const double *d_x, const double *d_b,
+                                  double *d_r, double *d_norm2, void *cuda_stream);
+
 /* Size queries and parity export (1-based ids as in the reference). */
 dg_status dg_get_sizes(const dg_handle *h, int *n, int *nagr_fine, int *nagr_coarse,
                        int *nsubdomains, long long *subdomain_total, int *R_nnz, int *AC_nnz);
