@@ -571,31 +571,39 @@ mf_bwd_level(MfView v, const int *__restrict__ fronts, const T *__restrict__ are
 // ---------------------------------------------------------------------------
 // Tiled solve layout of large fronts.  After the factorisation every 32-column
 // block J of a large front (columns 32J .. 32J+jb) is stored as a contiguous
-// run of 32x32 tiles:
-//   Dinv_J          inverse of the jb x jb diagonal block, row-major
-//   tile(R, J)      rows 32R..32R+31 of the block for row blocks R >= J,
-//                   row-major; entries of the diagonal block (and of rows past
-//                   m) are zero, so tile(J, J) only carries update rows
+// run:
+//   Dinv_J                        inverse of the jb x jb diagonal block (32 x 32)
+//   run of rank 0, rank 1, ...    32x32 tiles tile(R, J), row-major, for the
+//                                 row blocks R >= J owned by that cluster rank
+//                                 (R % C == rank), ascending R
+// Entries of the diagonal block (and rows past m) are zero in tile(J, J).
 // The solves of one front are split over a thread-block cluster of C CTAs:
 // CTA q owns the row blocks R with R % C == q, keeps their part of the work
-// vector in its shared memory, streams its own tiles with cp.async, and the
-// CTAs exchange the 32-value block solutions through distributed shared
-// memory with one cluster barrier per column block.  C = 1 is the plain
-// one-CTA solve.
+// vector in shared memory and streams its own tile run with cp.async, G tiles
+// per stage; the CTAs exchange the 32-value block solutions through
+// distributed shared memory with one cluster barrier per column block.
+// C = 1 is the plain one-CTA solve.
 // ---------------------------------------------------------------------------
 constexpr int kTileThreads = 256;
-// cp.async stages per CTA: enough 32x32 tiles in flight to cover the memory
-// latency (16 x 4 KB for FP32, 8 x 8 KB for FP64)
-template <typename T> struct TileStages;
-template <> struct TileStages<float> { static constexpr int S = 16; };
-template <> struct TileStages<double> { static constexpr int S = 8; };
+template <typename T> struct TilePipe;
+template <> struct TilePipe<float> { static constexpr int G = 4, S = 4; };   // 16 KB stages, 64 KB ring
+template <> struct TilePipe<double> { static constexpr int G = 2, S = 4; };  // 16 KB stages, 64 KB ring
 
 struct PackView {
   const int *blk_front;        // block -> front
   const int *blk_j;            // block -> J
   const int *f_blk;            // front -> first block (large fronts), -1 otherwise
   const int64_t *blk_off;      // block -> element offset in the packed buffer
+  const int *f_C;              // front -> cluster size of its solves
 };
+
+__host__ __device__ __forceinline__ int first_owned(int J, int C, int q) {  // smallest R >= J, R % C == q
+  return J + ((q - J % C) % C + C) % C;
+}
+__host__ __device__ __forceinline__ int owned_count(int J, int nR, int C, int q) {
+  const int f0 = first_owned(J, C, q);
+  return f0 < nR ? (nR - f0 + C - 1) / C : 0;
+}
 
 // one CTA per column block: invert the diagonal block, copy the tiles
 template <typename T>
@@ -605,7 +613,7 @@ mf_pack(MfView v, PackView pk, const T *__restrict__ arena, T *__restrict__ pack
   __shared__ T X[32][33];
   const int b = blockIdx.x;
   const int f = pk.blk_front[b], J = pk.blk_j[b];
-  const int m = v.f_m[f], k = v.f_k[f];
+  const int m = v.f_m[f], k = v.f_k[f], C = pk.f_C[f];
   const int J0 = 32 * J, jb = min(32, k - J0);
   const T *F = arena + v.f_off[f];
   T *dst = packed + pk.blk_off[b];
@@ -629,7 +637,11 @@ mf_pack(MfView v, PackView pk, const T *__restrict__ arena, T *__restrict__ pack
   for (int q = tid; q < 32 * 32; q += 256) dst[q] = X[q / 32][q % 32];
   const int nR = (m + 31) / 32;
   for (int R = J; R < nR; R++) {
-    T *td = dst + 1024 * (int64_t)(1 + R - J);
+    const int rank = R % C;
+    int pos = 0;
+    for (int r = 0; r < rank; r++) pos += owned_count(J, nR, C, r);
+    pos += (R - first_owned(J, C, rank)) / C;
+    T *td = dst + 1024 * (int64_t)(1 + pos);
     for (int q = tid; q < 32 * 32; q += 256) {
       const int rr = q / 32, c = q % 32;  // row-major tile
       const int row = 32 * R + rr;
@@ -647,13 +659,13 @@ template <int N>
 __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N)); }
 
 template <typename T>
-__device__ __forceinline__ void issue_tile(T *slot, const T *src) {
-  constexpr int n16 = 1024 * (int)sizeof(T) / 16;
+__device__ __forceinline__ void issue_chunk(T *slot, const T *src, int elems) {
+  const int n16 = elems * (int)sizeof(T) / 16;
   for (int q = threadIdx.x; q < n16; q += blockDim.x)
     cp_async16(reinterpret_cast<char *>(slot) + 16 * q, reinterpret_cast<const char *>(src) + 16 * q);
 }
 
-// distributed shared memory helpers (cluster rank of this CTA; remote address)
+// distributed shared memory helpers (cluster rank of this CTA; remote loads)
 __device__ __forceinline__ unsigned cluster_rank() {
   unsigned r;
   asm volatile("mov.u32 %0, %%cluster_ctarank;\n" : "=r"(r));
@@ -681,79 +693,77 @@ __device__ __forceinline__ float ld_dsmem<float>(const float *p, unsigned rank) 
   return v;
 }
 
-// The tiles one CTA consumes, in order: for each column block J, Dinv_J (if
-// the CTA owns row block J) then tile(R, J) for its row blocks R >= J.
-struct TileCursor {
-  int J, R, nb, nR, C, q;
-  bool dinv;  // the next chunk of block J is its Dinv
-  __device__ void start(int nb_, int nR_, int C_, int q_, bool forward) {
-    nb = nb_; nR = nR_; C = C_; q = q_;
-    J = forward ? 0 : nb - 1;
-    begin_block(forward);
+// The chunks one CTA consumes, in order.  Forward: for J ascending, Dinv_J
+// (if the CTA owns row block J) then its tile run of block J in pieces of G
+// tiles.  Backward: for J descending, the tile run, then Dinv_J if owned.
+template <typename T>
+struct ChunkCursor {
+  const int64_t *blk_off;
+  int fb, nb, nR, C, q;
+  bool fwd;
+  int J, t0, cnt;   // current block, first tile of the piece, tiles owned in block J
+  bool dinv;        // current chunk is Dinv_J
+  __device__ void setup_block() {
+    cnt = owned_count(J, nR, C, q);
+    t0 = 0;
+    dinv = fwd ? (J % C == q) : false;
+    if (!fwd && cnt == 0) dinv = (J % C == q);
   }
-  __device__ int first_owned(int from) const {  // smallest R >= from with R % C == q
-    int r = from + ((q - from % C) + C) % C;
-    return r;
-  }
-  __device__ void begin_block(bool forward) {
-    if (forward) {
-      dinv = (J % C) == q;
-      R = first_owned(J);
-    } else {  // backward: tiles first (descending R), Dinv last
-      dinv = false;
-      int last = nR - 1;
-      R = last - ((last % C) - q + C) % C;  // largest R <= nR-1 owned
-      if (R < J) R = -1;
-    }
+  __device__ void start(const int64_t *bo, int fb_, int nb_, int nR_, int C_, int q_, bool fwd_) {
+    blk_off = bo; fb = fb_; nb = nb_; nR = nR_; C = C_; q = q_; fwd = fwd_;
+    J = fwd ? 0 : nb - 1;
+    setup_block();
+    settle();
   }
   __device__ bool valid() const { return J >= 0 && J < nb; }
-  // true for a Dinv chunk, false for a tile chunk (R set)
-  __device__ bool current_is_dinv(bool forward) const {
-    if (forward) return dinv;
-    return R < 0 && (J % C) == q;
+  __device__ bool has_chunk() const { return dinv || t0 < cnt; }
+  __device__ void settle() {  // skip blocks without a chunk for this CTA
+    while (valid() && !has_chunk()) {
+      J += fwd ? 1 : -1;
+      if (valid()) setup_block();
+    }
   }
-  __device__ void advance(bool forward) {
-    if (forward) {
-      if (dinv) { dinv = false; }
-      else R += C;
-      if (!dinv && R >= nR) { J++; if (J < nb) begin_block(true); }
+  __device__ void advance() {
+    constexpr int G = TilePipe<T>::G;
+    if (fwd) {
+      if (dinv) dinv = false;
+      else t0 += G;
     } else {
-      if (R >= 0) {
-        R -= C;
-        if (R < J) R = -1;
-        if (R < 0 && (J % C) != q) { J--; if (J >= 0) begin_block(false); }
-      } else {  // Dinv consumed
-        J--;
-        if (J >= 0) begin_block(false);
+      if (t0 < cnt) {
+        t0 += G;
+        if (t0 >= cnt) dinv = (J % C == q);
+      } else {
+        dinv = false;
       }
     }
-  }
-  // skip positions that hold no chunk (backward block without owned tiles and not owner)
-  __device__ void settle(bool forward) {
-    if (forward) {
-      while (valid() && !dinv && R >= nR) { J++; if (J < nb) begin_block(true); }
-    } else {
-      while (valid() && R < 0 && (J % C) != q) { J--; if (J >= 0) begin_block(false); }
+    if (!has_chunk()) {
+      J += fwd ? 1 : -1;
+      if (valid()) setup_block();
     }
+    settle();
+  }
+  __device__ int ntiles() const { return min(TilePipe<T>::G, cnt - t0); }
+  __device__ const T *src(const T *packed, int &elems) const {
+    const T *base = packed + blk_off[fb + J];
+    if (dinv) { elems = 1024; return base; }
+    int pre = 0;
+    for (int r = 0; r < q; r++) pre += owned_count(J, nR, C, r);
+    elems = 1024 * ntiles();
+    return base + 1024 * (int64_t)(1 + pre + t0);
   }
 };
-
-template <typename T>
-__device__ __forceinline__ const T *chunk_ptr(const T *base, int J, int R, bool dinv) {
-  // base = start of block J
-  return dinv ? base : base + 1024 * (int64_t)(1 + R - J);
-}
 
 // forward solve, grid = nfronts * C, cluster (C,1,1)
 template <typename T, int C>
 __global__ void __launch_bounds__(kTileThreads)
 mf_fwd_tiles(MfView v, PackView pk, const int *__restrict__ fronts, const T *__restrict__ packed,
              T *__restrict__ xl, T *__restrict__ uvec) {
-  constexpr int kTileStages = TileStages<T>::S;
+  constexpr int G = TilePipe<T>::G, S = TilePipe<T>::S, SLOT = G * 1024;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  T *ring = reinterpret_cast<T *>(smem_raw);            // kTileStages x 1024
-  T *wloc = ring + kTileStages * 1024;                  // owned row blocks x 32
+  T *ring = reinterpret_cast<T *>(smem_raw);            // S slots of G tiles
+  T *wloc = ring + S * SLOT;                            // owned row blocks x 32
   __shared__ T ybuf[2][32];
+  __shared__ T yJ[32];
   const unsigned q = C > 1 ? cluster_rank() : 0;
   const int f = fronts[blockIdx.x / C];
   const int m = v.f_m[f], k = v.f_k[f];
@@ -762,19 +772,17 @@ mf_fwd_tiles(MfView v, PackView pk, const int *__restrict__ fronts, const T *__r
   T *x = xl + v.f_xoff[f] + v.f_p0[f];
   auto loc = [&](int row) -> T & { return wloc[(row / 32) / C * 32 + row % 32]; };
   auto owned = [&](int row) { return (row / 32) % C == (int)q; };
-  // stream the first chunks
-  TileCursor cur;
-  cur.start(nb, nR, C, q, true);
-  cur.settle(true);
-  for (int st = 0; st < kTileStages; st++) {
+  ChunkCursor<T> cur;
+  cur.start(pk.blk_off, fb, nb, nR, C, (int)q, true);
+  for (int st = 0; st < S; st++) {
     if (cur.valid()) {
-      issue_tile<T>(ring + st * 1024, chunk_ptr(packed + pk.blk_off[fb + cur.J], cur.J, cur.R, cur.dinv));
-      cur.advance(true);
-      cur.settle(true);
+      int el;
+      const T *sp = cur.src(packed, el);
+      issue_chunk<T>(ring + st * SLOT, sp, el);
+      cur.advance();
     }
     cp_async_commit();
   }
-  // right-hand side of the owned rows: pivots from xl, then children
   const int nown = (nR - (int)q + C - 1) / C;
   for (int i = tid; i < nown * 32; i += kTileThreads) {
     const int row = ((i / 32) * C + (int)q) * 32 + i % 32;
@@ -793,54 +801,56 @@ mf_fwd_tiles(MfView v, PackView pk, const int *__restrict__ fronts, const T *__r
     __syncthreads();
   }
   int slot = 0;
+  auto refill = [&]() {
+    if (cur.valid()) {
+      int el;
+      const T *sp = cur.src(packed, el);
+      issue_chunk<T>(ring + slot * SLOT, sp, el);
+      cur.advance();
+    }
+    cp_async_commit();
+    slot = (slot + 1) % S;
+  };
   for (int J = 0; J < nb; J++) {
     const int J0 = 32 * J, jb = min(32, k - J0);
     if (J % C == (int)q) {  // owner: y_J = Dinv_J w_J (its Dinv is the next chunk)
-      cp_async_wait<kTileStages - 1>();
+      cp_async_wait<S - 1>();
       __syncthreads();
-      const T *S = ring + slot * 1024;
+      const T *Sm = ring + slot * SLOT;
       if (tid < 32) {
         T sum = T(0);
         if (tid < jb)
-          for (int sidx = 0; sidx <= tid; sidx++) sum += S[tid * 32 + sidx] * loc(J0 + sidx);
-        ybuf[J & 1][tid] = sum;
+          for (int sidx = 0; sidx <= tid; sidx++) sum += Sm[tid * 32 + sidx] * loc(J0 + sidx);
+        ybuf[J & 1][tid] = sum;  // zero past jb: the padded tile columns multiply it
       }
       __syncthreads();
       if (tid < jb) loc(J0 + tid) = ybuf[J & 1][tid];
       __syncthreads();
-      // refill the consumed slot
-      if (cur.valid()) {
-        issue_tile<T>(ring + slot * 1024, chunk_ptr(packed + pk.blk_off[fb + cur.J], cur.J, cur.R, cur.dinv));
-        cur.advance(true); cur.settle(true);
-      }
-      cp_async_commit();
-      slot = (slot + 1) % kTileStages;
+      refill();
     }
     if (C > 1) cluster_sync();
-    __shared__ T yJ[32];
     if (tid < 32) yJ[tid] = C > 1 ? ld_dsmem<T>(&ybuf[J & 1][tid], (unsigned)(J % C)) : ybuf[J & 1][tid];
     __syncthreads();
-    // owned tiles of block J
-    for (int R = cur.first_owned(J); R < nR; R += C) {
-      cp_async_wait<kTileStages - 1>();
+    const int cnt = owned_count(J, nR, C, (int)q);
+    const int f0 = first_owned(J, C, (int)q);
+    for (int t0 = 0; t0 < cnt; t0 += G) {
+      cp_async_wait<S - 1>();
       __syncthreads();
-      const T *S = ring + slot * 1024;
-      // 32 rows x 32 columns: 8 threads per row, 4 columns each
-      const int rr = tid >> 3, c4 = (tid & 7) * 4;
-      T part = S[rr * 32 + c4] * yJ[c4] + S[rr * 32 + c4 + 1] * yJ[c4 + 1] +
-               S[rr * 32 + c4 + 2] * yJ[c4 + 2] + S[rr * 32 + c4 + 3] * yJ[c4 + 3];
-      part += __shfl_down_sync(0xffffffffu, part, 4, 8);
-      part += __shfl_down_sync(0xffffffffu, part, 2, 8);
-      part += __shfl_down_sync(0xffffffffu, part, 1, 8);
-      const int row = 32 * R + rr;
-      if ((tid & 7) == 0 && row < m) loc(row) -= part;
-      __syncthreads();
-      if (cur.valid()) {
-        issue_tile<T>(ring + slot * 1024, chunk_ptr(packed + pk.blk_off[fb + cur.J], cur.J, cur.R, cur.dinv));
-        cur.advance(true); cur.settle(true);
+      const T *Sm = ring + slot * SLOT;
+      const int nt = min(G, cnt - t0);
+      const int rr = tid >> 3, c4 = (tid & 7) * 4;  // 8 threads per tile row
+      for (int t = 0; t < nt; t++) {
+        const T *tl = Sm + t * 1024;
+        T part = tl[rr * 32 + c4] * yJ[c4] + tl[rr * 32 + c4 + 1] * yJ[c4 + 1] +
+                 tl[rr * 32 + c4 + 2] * yJ[c4 + 2] + tl[rr * 32 + c4 + 3] * yJ[c4 + 3];
+        part += __shfl_down_sync(0xffffffffu, part, 4, 8);
+        part += __shfl_down_sync(0xffffffffu, part, 2, 8);
+        part += __shfl_down_sync(0xffffffffu, part, 1, 8);
+        const int row = 32 * (f0 + (t0 + t) * C) + rr;
+        if ((tid & 7) == 0 && row < m) loc(row) -= part;
       }
-      cp_async_commit();
-      slot = (slot + 1) % kTileStages;
+      __syncthreads();
+      refill();
     }
   }
   cp_async_wait<0>();
@@ -858,12 +868,13 @@ template <typename T, int C>
 __global__ void __launch_bounds__(kTileThreads)
 mf_bwd_tiles(MfView v, PackView pk, const int *__restrict__ fronts, const T *__restrict__ packed,
              T *__restrict__ xl) {
-  constexpr int kTileStages = TileStages<T>::S;
+  constexpr int G = TilePipe<T>::G, S = TilePipe<T>::S, SLOT = G * 1024;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T *ring = reinterpret_cast<T *>(smem_raw);
-  T *wloc = ring + kTileStages * 1024;
+  T *wloc = ring + S * SLOT;
   __shared__ T part[2][32];
   __shared__ T red[8][32];
+  __shared__ T tJ[32];
   const unsigned q = C > 1 ? cluster_rank() : 0;
   const int f = fronts[blockIdx.x / C];
   const int m = v.f_m[f], k = v.f_k[f];
@@ -872,14 +883,14 @@ mf_bwd_tiles(MfView v, PackView pk, const int *__restrict__ fronts, const T *__r
   T *xb = xl + v.f_xoff[f];
   const int *rows = v.rows + v.f_rows[f];
   auto loc = [&](int row) -> T & { return wloc[(row / 32) / C * 32 + row % 32]; };
-  TileCursor cur;
-  cur.start(nb, nR, C, q, false);
-  cur.settle(false);
-  for (int st = 0; st < kTileStages; st++) {
+  ChunkCursor<T> cur;
+  cur.start(pk.blk_off, fb, nb, nR, C, (int)q, false);
+  for (int st = 0; st < S; st++) {
     if (cur.valid()) {
-      issue_tile<T>(ring + st * 1024, chunk_ptr(packed + pk.blk_off[fb + cur.J], cur.J, cur.R, cur.R < 0));
-      cur.advance(false);
-      cur.settle(false);
+      int el;
+      const T *sp = cur.src(packed, el);
+      issue_chunk<T>(ring + st * SLOT, sp, el);
+      cur.advance();
     }
     cp_async_commit();
   }
@@ -890,29 +901,39 @@ mf_bwd_tiles(MfView v, PackView pk, const int *__restrict__ fronts, const T *__r
   }
   __syncthreads();
   int slot = 0;
+  auto refill = [&]() {
+    if (cur.valid()) {
+      int el;
+      const T *sp = cur.src(packed, el);
+      issue_chunk<T>(ring + slot * SLOT, sp, el);
+      cur.advance();
+    }
+    cp_async_commit();
+    slot = (slot + 1) % S;
+  };
   for (int J = nb - 1; J >= 0; J--) {
     const int J0 = 32 * J, jb = min(32, k - J0);
     // partial t_J = sum over owned R >= J of tile(R,J)^T x_R
     T acc = T(0);  // thread (wid, lane): column lane, rows wid*4 .. wid*4+3 of each tile
-    const int last = nR - 1;
-    int Rstart = last - ((last % C) - (int)q + C) % C;
-    for (int R = Rstart; R >= J; R -= C) {
-      cp_async_wait<kTileStages - 1>();
+    const int cnt = owned_count(J, nR, C, (int)q);
+    const int f0 = first_owned(J, C, (int)q);
+    for (int t0 = 0; t0 < cnt; t0 += G) {
+      cp_async_wait<S - 1>();
       __syncthreads();
-      const T *S = ring + slot * 1024;
+      const T *Sm = ring + slot * SLOT;
+      const int nt = min(G, cnt - t0);
+      for (int t = 0; t < nt; t++) {
+        const T *tl = Sm + t * 1024;
+        const int R = f0 + (t0 + t) * C;
 #pragma unroll
-      for (int t = 0; t < 4; t++) {
-        const int rr = wid * 4 + t;
-        const int row = 32 * R + rr;
-        if (row < m) acc += S[rr * 32 + lane] * loc(row);
+        for (int u = 0; u < 4; u++) {
+          const int rr = wid * 4 + u;
+          const int row = 32 * R + rr;
+          if (row < m) acc += tl[rr * 32 + lane] * loc(row);
+        }
       }
       __syncthreads();
-      if (cur.valid()) {
-        issue_tile<T>(ring + slot * 1024, chunk_ptr(packed + pk.blk_off[fb + cur.J], cur.J, cur.R, cur.R < 0));
-        cur.advance(false); cur.settle(false);
-      }
-      cp_async_commit();
-      slot = (slot + 1) % kTileStages;
+      refill();
     }
     red[wid][lane] = acc;
     __syncthreads();
@@ -925,27 +946,21 @@ mf_bwd_tiles(MfView v, PackView pk, const int *__restrict__ fronts, const T *__r
     __syncthreads();
     if (C > 1) cluster_sync();
     if (J % C == (int)q) {  // owner: t_J = y_J - sum of partials; x_J = Dinv_J^T t_J
-      __shared__ T tJ[32];
       if (tid < 32) {
         T s = T(0);
         for (int r = 0; r < C; r++) s += C > 1 ? ld_dsmem<T>(&part[J & 1][tid], (unsigned)r) : part[J & 1][tid];
         tJ[tid] = tid < jb ? loc(J0 + tid) - s : T(0);
       }
-      cp_async_wait<kTileStages - 1>();
+      cp_async_wait<S - 1>();
       __syncthreads();
-      const T *S = ring + slot * 1024;
+      const T *Sm = ring + slot * SLOT;
       if (tid < jb) {
         T sum = T(0);
-        for (int sidx = tid; sidx < jb; sidx++) sum += S[sidx * 32 + tid] * tJ[sidx];
+        for (int sidx = tid; sidx < jb; sidx++) sum += Sm[sidx * 32 + tid] * tJ[sidx];
         loc(J0 + tid) = sum;
       }
       __syncthreads();
-      if (cur.valid()) {
-        issue_tile<T>(ring + slot * 1024, chunk_ptr(packed + pk.blk_off[fb + cur.J], cur.J, cur.R, cur.R < 0));
-        cur.advance(false); cur.settle(false);
-      }
-      cp_async_commit();
-      slot = (slot + 1) % kTileStages;
+      refill();
     }
   }
   cp_async_wait<0>();
@@ -1066,13 +1081,14 @@ __global__ void restrict_to_coarse(const int64_t *__restrict__ Rp, const int *__
   }
 }
 
-// z_g = (sum of subdomain solutions at g, in subdomain order) + (P csol)_g ;
-// partial sums of r.z (and of r.z_old for the flexible variant)
+// z_g = (sum of subdomain solutions at g, in subdomain order) + (P x_c)_g ;
+// partial sums of r.z (and of r.z_old for the flexible variant).  One thread
+// per node; Pcp holds coarse-vector positions (composed at setup).
 template <typename T, typename TP>
 __global__ void __launch_bounds__(kVecThreads)
 pull_prolong_dot(int n, const int64_t *__restrict__ pull_ptr, const int64_t *__restrict__ pull_idx,
-                 const T *__restrict__ xl, const int64_t *__restrict__ Pp, const int *__restrict__ Pc,
-                 const TP *__restrict__ Pv, const double *__restrict__ xc, const int *__restrict__ cpos,
+                 const T *__restrict__ xl, const int64_t *__restrict__ Pp, const int *__restrict__ Pcp,
+                 const TP *__restrict__ Pv, const double *__restrict__ xc,
                  int mode, const double *__restrict__ r, double *__restrict__ z,
                  double *__restrict__ zold, double *__restrict__ part_rz, double *__restrict__ part_rzo) {
   // mode bit 0: fine subdomains on; bit 1: coarse on; bit 2: identity fine (z=r);
@@ -1080,25 +1096,36 @@ pull_prolong_dot(int n, const int64_t *__restrict__ pull_ptr, const int64_t *__r
   __shared__ double sh[32];
   double srz = 0.0, srzo = 0.0;
   for (int g = blockIdx.x * kVecThreads + threadIdx.x; g < n; g += gridDim.x * kVecThreads) {
-    double s = 0.0;
+    double sv = 0.0;
     if (mode & 4) {
-      s = r[g];
+      sv = r[g];
     } else if (mode & 1) {
-      for (int64_t q = pull_ptr[g]; q < pull_ptr[g + 1]; q++) s = s + (double)xl[pull_idx[q]];
+      const int64_t q0 = pull_ptr[g], q1 = pull_ptr[g + 1];
+      for (int64_t q = q0; q < q1; q++) sv = sv + (double)xl[pull_idx[q]];
     }
     if (mode & 2) {
+      const int64_t e0 = Pp[g], e1 = Pp[g + 1];
       TP t = TP(0);
-      for (int64_t e = Pp[g]; e < Pp[g + 1]; e++) t = t + Pv[e] * (TP)xc[cpos[Pc[e]]];
-      s = s + (double)t;
+      int64_t e = e0;
+      for (; e + 4 <= e1; e += 4) {  // independent loads in flight
+        const int c0 = Pcp[e], c1 = Pcp[e + 1], c2 = Pcp[e + 2], c3 = Pcp[e + 3];
+        const TP v0 = Pv[e], v1 = Pv[e + 1], v2 = Pv[e + 2], v3 = Pv[e + 3];
+        const TP x0 = (TP)xc[c0], x1 = (TP)xc[c1], x2 = (TP)xc[c2], x3 = (TP)xc[c3];
+        t += v0 * x0;
+        t += v1 * x1;
+        t += v2 * x2;
+        t += v3 * x3;
+      }
+      for (; e < e1; e++) t += Pv[e] * (TP)xc[Pcp[e]];
+      sv = sv + (double)t;
     }
     const double rg = r[g];
     if (mode & 8) {
-      const double zo = zold[g];
-      srzo += rg * zo;
-      zold[g] = s;
+      srzo += rg * zold[g];
+      zold[g] = sv;
     }
-    z[g] = s;
-    srz += rg * s;
+    z[g] = sv;
+    srz += rg * sv;
   }
   double b = block_sum<kVecThreads>(srz, sh);
   if (threadIdx.x == 0) part_rz[blockIdx.x] = b;
@@ -1128,14 +1155,11 @@ __device__ __forceinline__ double cg_beta(const double *part_rz, const double *p
   return __ddiv_rn(rho, sc[SC_RHO_PREV]);
 }
 
-// q = A (z + beta p) with LANES lanes per row; partial sums of (z+beta p).q
-template <int LANES>
+// p = z + beta p (p = z on the first step); beta from the r.z partials
 __global__ void __launch_bounds__(kVecThreads)
-spmv_dir(int n, const int64_t *__restrict__ Ap, const int *__restrict__ Ac, const double *__restrict__ Av,
-         const double *__restrict__ z, const double *__restrict__ p, double *__restrict__ q,
-         const double *__restrict__ part_rz, const double *__restrict__ part_rzo, double *__restrict__ sc,
-         int first, int flexible, double *__restrict__ part_pq) {
-  __shared__ double sh[32];
+cg_direction(int n, const double *__restrict__ z, double *__restrict__ p,
+             const double *__restrict__ part_rz, const double *__restrict__ part_rzo,
+             double *__restrict__ sc, int first, int flexible) {
   __shared__ double s_beta;
   if (threadIdx.x < 32) {
     double rho;
@@ -1147,6 +1171,16 @@ spmv_dir(int n, const int64_t *__restrict__ Ap, const int *__restrict__ Ac, cons
   }
   __syncthreads();
   const double beta = s_beta;
+  for (int i = blockIdx.x * kVecThreads + threadIdx.x; i < n; i += gridDim.x * kVecThreads)
+    p[i] = first ? z[i] : __dadd_rn(z[i], __dmul_rn(beta, p[i]));
+}
+
+// q = A p with LANES lanes per row; partial sums of p.q
+template <int LANES>
+__global__ void __launch_bounds__(kVecThreads)
+spmv_pq(int n, const int64_t *__restrict__ Ap, const int *__restrict__ Ac, const double *__restrict__ Av,
+        const double *__restrict__ p, double *__restrict__ q, double *__restrict__ part_pq) {
+  __shared__ double sh[32];
   const int sub = threadIdx.x % LANES;
   const int rows_per_block = kVecThreads / LANES;
   double spq = 0.0;
@@ -1154,29 +1188,37 @@ spmv_dir(int n, const int64_t *__restrict__ Ap, const int *__restrict__ Ac, cons
     const int i = row0 + threadIdx.x / LANES;
     double s = 0.0;
     if (i < n) {
-      for (int64_t e = Ap[i] + sub; e < Ap[i + 1]; e += LANES) {
-        const int j = Ac[e];
-        const double pj = first ? z[j] : __dadd_rn(z[j], __dmul_rn(beta, p[j]));
-        s = __fma_rn(Av[e], pj, s);
+      int64_t e = Ap[i] + sub;
+      const int64_t e1 = Ap[i + 1];
+      if (LANES == 1) {  // short rows: all loads of a row issued before the sums
+        for (; e + 4 <= e1; e += 4) {
+          const int c0 = Ac[e], c1 = Ac[e + 1], c2 = Ac[e + 2], c3 = Ac[e + 3];
+          const double a0 = Av[e], a1 = Av[e + 1], a2 = Av[e + 2], a3 = Av[e + 3];
+          const double p0 = p[c0], p1 = p[c1], p2 = p[c2], p3 = p[c3];
+          s = __fma_rn(a0, p0, s);
+          s = __fma_rn(a1, p1, s);
+          s = __fma_rn(a2, p2, s);
+          s = __fma_rn(a3, p3, s);
+        }
       }
+      for (; e < e1; e += LANES) s = __fma_rn(Av[e], p[Ac[e]], s);
     }
 #pragma unroll
     for (int o = LANES / 2; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o, LANES);
     if (i < n && sub == 0) {
       q[i] = s;
-      const double pi = first ? z[i] : __dadd_rn(z[i], __dmul_rn(beta, p[i]));
-      spq += pi * s;
+      spq += p[i] * s;
     }
   }
   double b = block_sum<kVecThreads>(spq, sh);
   if (threadIdx.x == 0) part_pq[blockIdx.x] = b;
 }
 
-// p = z + beta p; x += alpha p; r -= alpha q; partial r.r
+// x += alpha p; r -= alpha q; partial r.r  (alpha = rho / p.q)
 __global__ void __launch_bounds__(kVecThreads)
-cg_update(int n, const double *__restrict__ z, double *__restrict__ p, const double *__restrict__ q,
+cg_update(int n, const double *__restrict__ p, const double *__restrict__ q,
           double *__restrict__ x, double *__restrict__ r, double *__restrict__ sc,
-          const double *__restrict__ part_pq, int first, double *__restrict__ part_rr) {
+          const double *__restrict__ part_pq, double *__restrict__ part_rr) {
   __shared__ double sh[32];
   __shared__ double s_alpha;
   if (threadIdx.x < 32) {
@@ -1188,12 +1230,10 @@ cg_update(int n, const double *__restrict__ z, double *__restrict__ p, const dou
     }
   }
   __syncthreads();
-  const double alpha = s_alpha, beta = sc[SC_BETA];
+  const double alpha = s_alpha;
   double srr = 0.0;
   for (int i = blockIdx.x * kVecThreads + threadIdx.x; i < n; i += gridDim.x * kVecThreads) {
-    const double pi = first ? z[i] : __dadd_rn(z[i], __dmul_rn(beta, p[i]));
-    p[i] = pi;
-    x[i] = __dadd_rn(x[i], __dmul_rn(alpha, pi));
+    x[i] = __dadd_rn(x[i], __dmul_rn(alpha, p[i]));
     const double ri = __dsub_rn(r[i], __dmul_rn(alpha, q[i]));
     r[i] = ri;
     srr += ri * ri;

@@ -73,7 +73,7 @@ struct MfDevice {
   DBuf<int> small_fronts, tiny_fronts, diag_fronts;
   DBuf<int2> asm_tasks, upd_tasks, panel_tasks;
   DBuf<T> arena, xl, u, w, packed;
-  DBuf<int> blk_front, blk_j, f_blk, solve_small, solve_large;
+  DBuf<int> blk_front, blk_j, f_blk, f_C, solve_small, solve_large;
   DBuf<int64_t> blk_off;
   int nblk = 0;
   struct SolveLevel {
@@ -188,11 +188,34 @@ struct MfDevice {
       nblk = (int)bf.size();
       blk_front.upload(bf); blk_j.upload(bj); f_blk.upload(fblk); blk_off.upload(bo);
       packed.alloc((size_t)std::max<int64_t>(len, 1));
-      pview = PackView{blk_front.p, blk_j.p, f_blk.p, blk_off.p};
+      std::vector<int> fc((size_t)nfronts, 1);  // cluster size per front, set per level below
       int dev = 0, optin = 0, nsm = 0;
       CK(cudaGetDevice(&dev));
       CK(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
       CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+      max_cluster_ = 8;
+      if (sizeof(T) == 8) {  // can 16-CTA clusters of the FP64 tile kernels be scheduled?
+        cudaError_t e1 = cudaFuncSetAttribute(mf_fwd_tiles<T, 16>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+        cudaError_t e2 = cudaFuncSetAttribute(mf_bwd_tiles<T, 16>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+        if (e1 == cudaSuccess && e2 == cudaSuccess) {
+          cudaLaunchConfig_t cfg{};
+          cfg.gridDim = dim3(16);
+          cfg.blockDim = dim3(kTileThreads);
+          cfg.dynamicSmemBytes = (size_t)TilePipe<T>::S * TilePipe<T>::G * 1024 * sizeof(T) + 8 * 1024;
+          cudaLaunchAttribute attr[1];
+          attr[0].id = cudaLaunchAttributeClusterDimension;
+          attr[0].val.clusterDim.x = 16;
+          attr[0].val.clusterDim.y = 1;
+          attr[0].val.clusterDim.z = 1;
+          cfg.attrs = attr;
+          cfg.numAttrs = 1;
+          int nclusters = 0;
+          set_tile_attrs<16>(optin);
+          if (cudaOccupancyMaxActiveClusters(&nclusters, mf_fwd_tiles<T, 16>, &cfg) == cudaSuccess && nclusters > 0)
+            max_cluster_ = 16;
+        }
+        cudaGetLastError();  // a refused attribute only means: stay at 8
+      }
       slevels.assign((size_t)nlevels, SolveLevel());
       for (int l = 0; l < nlevels; l++) {
         SolveLevel &L = slevels[(size_t)l];
@@ -212,24 +235,33 @@ struct MfDevice {
         L.warp_smem = (size_t)L.warps * per_warp * sizeof(T);
         if (L.small_cnt && L.warp_smem > (size_t)optin)
           throw CudaError{cudaErrorInvalidValue, "small front too large for the warp solve"};
-        // cluster size: enough CTAs for the machine, at most 8, at most the row blocks
+        // cluster size: enough CTAs for the machine, at most the row blocks;
+        // FP64 fronts (FP64 pipe bound) may use 16-CTA clusters where the
+        // device can schedule them
         int C = 1;
-        while (C < 8 && L.large_cnt * C < 2 * nsm && C * 2 <= maxnR) C *= 2;
+        const int cmax = sizeof(T) == 8 ? max_cluster_ : 8;
+        while (C < cmax && L.large_cnt * C < 2 * nsm && C * 2 <= maxnR) C *= 2;
         L.C = C;
-        L.tile_smem = (size_t)TileStages<T>::S * 1024 * sizeof(T) + (size_t)((maxnR + C - 1) / C) * 32 * sizeof(T);
+        for (int qq = L.large_off; qq < (int)sl.size(); qq++) fc[(size_t)sl[(size_t)qq]] = C;
+        L.tile_smem = (size_t)TilePipe<T>::S * TilePipe<T>::G * 1024 * sizeof(T) +
+                      (size_t)((maxnR + C - 1) / C) * 32 * sizeof(T);
         if (L.large_cnt && L.tile_smem > (size_t)optin - 1024)
           throw CudaError{cudaErrorInvalidValue, "front too large for the shared-memory solve"};
       }
       solve_small.upload(ss);
       solve_large.upload(sl);
+      f_C.upload(fc);
+      pview = PackView{blk_front.p, blk_j.p, f_blk.p, blk_off.p, f_C.p};
       CK(cudaFuncSetAttribute(mf_fwd_warp<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
       CK(cudaFuncSetAttribute(mf_bwd_warp<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
       set_tile_attrs<1>(optin);
       set_tile_attrs<2>(optin);
       set_tile_attrs<4>(optin);
       set_tile_attrs<8>(optin);
+      set_tile_attrs<16>(optin);
     }
   }
+  int max_cluster_ = 8;
 
   template <int C>
   void set_tile_attrs(int optin) {
@@ -264,7 +296,8 @@ struct MfDevice {
       case 1: launch_tiles<1>(fwd, nfr, fr, smem, s); break;
       case 2: launch_tiles<2>(fwd, nfr, fr, smem, s); break;
       case 4: launch_tiles<4>(fwd, nfr, fr, smem, s); break;
-      default: launch_tiles<8>(fwd, nfr, fr, smem, s); break;
+      case 8: launch_tiles<8>(fwd, nfr, fr, smem, s); break;
+      default: launch_tiles<16>(fwd, nfr, fr, smem, s); break;
     }
   }
 
@@ -376,9 +409,14 @@ struct dg_handle {
   int *d_host_status = nullptr;
   cudaEvent_t ev[10]{};
   cudaStream_t s2 = nullptr;        // coarse-level stream (runs beside the subdomain solves)
+  cudaStream_t s3 = nullptr;        // capture stream of the iteration graph
+  cudaGraphExec_t iter_exec = nullptr;
+  int iter_nodes = 0;
   cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
   ~dg_handle() {
+    if (iter_exec) cudaGraphExecDestroy(iter_exec);
     if (s2) cudaStreamDestroy(s2);
+    if (s3) cudaStreamDestroy(s3);
     if (fork_ev) cudaEventDestroy(fork_ev);
     if (join_ev) cudaEventDestroy(join_ev);
     if (host_out) cudaFreeHost(host_out);
@@ -442,6 +480,7 @@ double tridiag_cond(const std::vector<double> &alpha, const std::vector<double> 
 
 int lanes_for(const Csr &A) {
   double avg = A.nrows ? (double)A.nnz() / A.nrows : 1;
+  if (avg <= 9) return 1;  // thread per row, loads unrolled
   if (avg <= 3) return 2;
   if (avg <= 6) return 4;
   if (avg <= 12) return 8;
@@ -451,9 +490,9 @@ int lanes_for(const Csr &A) {
 
 template <int L>
 void launch_spmv(int grid, cudaStream_t s, dg_handle *h, int first, int flexible) {
-  spmv_dir<L><<<grid, kVecThreads, 0, s>>>(h->n, h->Ap.p, h->Ac.p, h->Av.p, h->z.p, h->p.p, h->q.p,
-                                            h->part_rz.p, h->part_rzo.p, h->sc.p, first, flexible,
-                                            h->part_pq.p);
+  cg_direction<<<grid, kVecThreads, 0, s>>>(h->n, h->z.p, h->p.p, h->part_rz.p, h->part_rzo.p, h->sc.p, first,
+                                            flexible);
+  spmv_pq<L><<<grid, kVecThreads, 0, s>>>(h->n, h->Ap.p, h->Ac.p, h->Av.p, h->p.p, h->q.p, h->part_pq.p);
 }
 template <int L>
 void launch_resid(int grid, cudaStream_t s, dg_handle *h, const double *xx, const double *bb, double *rr) {
@@ -461,6 +500,7 @@ void launch_resid(int grid, cudaStream_t s, dg_handle *h, const double *xx, cons
 }
 void spmv_any(int lanes, int grid, cudaStream_t s, dg_handle *h, int first, int flexible) {
   switch (lanes) {
+    case 1: launch_spmv<1>(grid, s, h, first, flexible); break;
     case 2: launch_spmv<2>(grid, s, h, first, flexible); break;
     case 4: launch_spmv<4>(grid, s, h, first, flexible); break;
     case 8: launch_spmv<8>(grid, s, h, first, flexible); break;
@@ -470,6 +510,7 @@ void spmv_any(int lanes, int grid, cudaStream_t s, dg_handle *h, int first, int 
 }
 void resid_any(int lanes, int grid, cudaStream_t s, dg_handle *h, const double *xx, const double *bb, double *rr) {
   switch (lanes) {
+    case 1: launch_resid<1>(grid, s, h, xx, bb, rr); break;
     case 2: launch_resid<2>(grid, s, h, xx, bb, rr); break;
     case 4: launch_resid<4>(grid, s, h, xx, bb, rr); break;
     case 8: launch_resid<8>(grid, s, h, xx, bb, rr); break;
@@ -522,12 +563,14 @@ dg_status do_setup(dg_handle *h) {
       CK(cudaHostGetDevicePointer(&h->d_host_status, h->host_status, 0));
       for (auto &e : h->ev) CK(cudaEventCreate(&e));
       CK(cudaStreamCreateWithFlags(&h->s2, cudaStreamNonBlocking));
+      CK(cudaStreamCreateWithFlags(&h->s3, cudaStreamNonBlocking));
       CK(cudaEventCreateWithFlags(&h->fork_ev, cudaEventDisableTiming));
       CK(cudaEventCreateWithFlags(&h->join_ev, cudaEventDisableTiming));
     }
+    if (h->iter_exec) { cudaGraphExecDestroy(h->iter_exec); h->iter_exec = nullptr; }
     // transfer operators
     h->Rp.upload(S.R.ptr); h->Rc.upload(S.R.col); h->Rv.upload(S.R.val);
-    h->Pp.upload(S.P.ptr); h->Pc.upload(S.P.col); h->Pv.upload(S.P.val);
+    h->Pp.upload(S.P.ptr); h->Pv.upload(S.P.val);
     std::vector<float> rf(S.R.val.begin(), S.R.val.end()), pf(S.P.val.begin(), S.P.val.end());
     h->Rvf.upload(rf); h->Pvf.upload(pf);
     h->ACv.upload(S.AC.val);
@@ -555,8 +598,13 @@ dg_status do_setup(dg_handle *h) {
       std::vector<int> cp((size_t)S.AC.nrows, 0);
       for (int64_t q = 0; q < (int64_t)h->Bco.gidx.size(); q++) cp[(size_t)h->Bco.gidx[(size_t)q]] = (int)q;
       h->cpos.upload(cp);
+      // prolongation columns as positions in the coarse solver's vector
+      std::vector<int> pcp(S.P.col.size());
+      for (size_t e = 0; e < pcp.size(); e++) pcp[e] = cp[(size_t)S.P.col[e]];
+      h->Pc.upload(pcp);
     } else {
       h->cpos.alloc(1);
+      h->Pc.alloc(1);
     }
     CK(cudaDeviceSynchronize());
   } catch (const CudaError &e) {
@@ -637,55 +685,76 @@ dg_status do_solve(dg_handle *h, const double *d_b, double *d_x, dg_stats *st, c
       CK(cudaEventElapsedTime(&ms, h->ev[a], h->ev[b]));
       return ms * 1e-3;
     };
-    while (ratio > tol * tol && it < maxit) {
-      it++;
-      const int first = it == 1;
+    // one PCG iteration's launches on stream st (coarse branch forked to s2);
+    // returns the number of kernels
+    auto iteration = [&](cudaStream_t st, int first, bool replace, bool profile) -> int {
+      int nl = 0;
       if (coarse) {  // restriction + coarse solve on the second stream
-        CK(cudaEventRecord(h->fork_ev, s));
+        CK(cudaEventRecord(h->fork_ev, st));
         CK(cudaStreamWaitEvent(h->s2, h->fork_ev, 0));
-        if (prof) CK(cudaEventRecord(h->ev[4], h->s2));
+        if (profile) CK(cudaEventRecord(h->ev[4], h->s2));
         if (mixed)
           restrict_to_coarse<float><<<grid, kVecThreads, 0, h->s2>>>(h->Rp.p, h->Rc.p, h->Rvf.p, h->r.p, h->cpos.p, h->co64->xl.p, h->S.R.nrows);
         else
           restrict_to_coarse<double><<<grid, kVecThreads, 0, h->s2>>>(h->Rp.p, h->Rc.p, h->Rv.p, h->r.p, h->cpos.p, h->co64->xl.p, h->S.R.nrows);
-        launches += 1 + h->co64->solve(h->s2);
-        if (prof) CK(cudaEventRecord(h->ev[5], h->s2));
+        nl += 1 + h->co64->solve(h->s2);
+        if (profile) CK(cudaEventRecord(h->ev[5], h->s2));
         CK(cudaEventRecord(h->join_ev, h->s2));
       }
-      if (prof) CK(cudaEventRecord(h->ev[3], s));
+      if (profile) CK(cudaEventRecord(h->ev[3], st));
       if (fine) {
         if (mixed) {
-          gather_subdomains<float><<<grid, kVecThreads, 0, s>>>(h->r.p, h->sub32->gidx.p, h->sub32->xl.p, h->sub32->xlen);
-          launches += 1 + h->sub32->solve(s);
+          gather_subdomains<float><<<grid, kVecThreads, 0, st>>>(h->r.p, h->sub32->gidx.p, h->sub32->xl.p, h->sub32->xlen);
+          nl += 1 + h->sub32->solve(st);
         } else {
-          gather_subdomains<double><<<grid, kVecThreads, 0, s>>>(h->r.p, h->sub64->gidx.p, h->sub64->xl.p, h->sub64->xlen);
-          launches += 1 + h->sub64->solve(s);
+          gather_subdomains<double><<<grid, kVecThreads, 0, st>>>(h->r.p, h->sub64->gidx.p, h->sub64->xl.p, h->sub64->xlen);
+          nl += 1 + h->sub64->solve(st);
         }
       }
-      if (prof) CK(cudaEventRecord(h->ev[8], s));
-      if (coarse) CK(cudaStreamWaitEvent(s, h->join_ev, 0));
+      if (profile) CK(cudaEventRecord(h->ev[8], st));
+      if (coarse) CK(cudaStreamWaitEvent(st, h->join_ev, 0));
       const double *xc = coarse ? h->co64->xl.p : nullptr;
       if (mixed)
-        pull_prolong_dot<float, float><<<grid, kVecThreads, 0, s>>>(
+        pull_prolong_dot<float, float><<<grid, kVecThreads, 0, st>>>(
             n, h->pull_ptr.p, h->pull_idx.p, fine ? h->sub32->xl.p : nullptr, h->Pp.p, h->Pc.p, h->Pvf.p, xc,
-            h->cpos.p, mode, h->r.p, h->z.p, h->zold.p, h->part_rz.p, h->part_rzo.p);
+            mode, h->r.p, h->z.p, h->zold.p, h->part_rz.p, h->part_rzo.p);
       else
-        pull_prolong_dot<double, double><<<grid, kVecThreads, 0, s>>>(
+        pull_prolong_dot<double, double><<<grid, kVecThreads, 0, st>>>(
             n, h->pull_ptr.p, h->pull_idx.p, fine ? h->sub64->xl.p : nullptr, h->Pp.p, h->Pc.p, h->Pv.p, xc,
-            h->cpos.p, mode, h->r.p, h->z.p, h->zold.p, h->part_rz.p, h->part_rzo.p);
-      if (prof) CK(cudaEventRecord(h->ev[6], s));
-      spmv_any(h->lanes, grid, s, h, first, mixed ? 1 : 0);
-      if (prof) CK(cudaEventRecord(h->ev[7], s));
-      cg_update<<<grid, kVecThreads, 0, s>>>(n, h->z.p, h->p.p, h->q.p, h->x.p, h->r.p, h->sc.p, h->part_pq.p, first,
-                                             h->part_rr.p);
-      launches += 3;
-      if (mixed && c.replace_every > 0 && it % c.replace_every == 0) {
-        // FP64 residual replacement: r = b - A x
-        resid_any(h->lanes, grid, s, h, h->x.p, h->b.p, h->r.p);
-        launches++;
+            mode, h->r.p, h->z.p, h->zold.p, h->part_rz.p, h->part_rzo.p);
+      if (profile) CK(cudaEventRecord(h->ev[6], st));
+      spmv_any(h->lanes, grid, st, h, first, mixed ? 1 : 0);
+      if (profile) CK(cudaEventRecord(h->ev[7], st));
+      cg_update<<<grid, kVecThreads, 0, st>>>(n, h->p.p, h->q.p, h->x.p, h->r.p, h->sc.p, h->part_pq.p,
+                                              h->part_rr.p);
+      nl += 4;
+      if (replace) {  // FP64 residual replacement: r = b - A x
+        resid_any(h->lanes, grid, st, h, h->x.p, h->b.p, h->r.p);
+        nl++;
       }
-      cg_finish<<<1, 32, 0, s>>>(h->sc.p, h->part_rr.p, 0, h->d_host_out, h->status.p, h->d_host_status);
-      launches++;
+      cg_finish<<<1, 32, 0, st>>>(h->sc.p, h->part_rr.p, 0, h->d_host_out, h->status.p, h->d_host_status);
+      nl++;
+      return nl;
+    };
+    // the steady-state iteration is captured once into a CUDA graph
+    if (!h->iter_exec && c.profile == 0) {
+      cudaGraph_t g = nullptr;
+      CK(cudaStreamBeginCapture(h->s3, cudaStreamCaptureModeThreadLocal));
+      h->iter_nodes = iteration(h->s3, 0, false, false);
+      CK(cudaStreamEndCapture(h->s3, &g));
+      CK(cudaGraphInstantiate(&h->iter_exec, g, 0));
+      CK(cudaGraphDestroy(g));
+    }
+    while (ratio > tol * tol && it < maxit) {
+      it++;
+      const int first = it == 1;
+      const bool replace = mixed && c.replace_every > 0 && it % c.replace_every == 0;
+      if (!first && !replace && !prof && h->iter_exec) {
+        CK(cudaGraphLaunch(h->iter_exec, s));
+        launches += h->iter_nodes;
+      } else {
+        launches += iteration(s, first, replace, prof);
+      }
       CK(cudaGetLastError());  // a failed launch must not pass as a converged step
       CK(cudaStreamSynchronize(s));
       if (prof) {
@@ -733,7 +802,8 @@ dg_status do_solve(dg_handle *h, const double *d_b, double *d_x, dg_stats *st, c
       out.subsolve_bytes = 2.0 * (double)h->Bsub.factor_nnz * tsz;
       out.coarse_bytes = 2.0 * (double)h->Bco.factor_nnz * 8.0;
       const double nnz = (double)h->S.A.nnz();
-      out.spmv_bytes = 12.0 * nnz + 8.0 * (n + 1) + 8.0 * n * 3.0;  // A, z and p read, q written
+      // direction update (z, p read, p written) + SpMV (A, p read, q written)
+      out.spmv_bytes = 12.0 * nnz + 8.0 * (n + 1) + 8.0 * n * 5.0;
       out.t_subsolve_s = t_sub;
       out.t_coarse_s = t_co;
       out.t_spmv_s = t_sp;

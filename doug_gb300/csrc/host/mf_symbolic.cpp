@@ -101,11 +101,25 @@ class Dissector {
       }
     }
     if (comps.size() > 1) {
+      // components larger than a leaf are dissected on their own; the small
+      // ones are packed together into leaf fronts (one dense front may hold
+      // several disconnected pieces), which keeps tiny fronts with large
+      // boundaries out of the tree
+      std::vector<int> pack;
+      auto flush = [&]() {
+        if (!pack.empty()) { roots.push_back(new_front(pack)); pack.clear(); }
+      };
       for (auto &c : comps) {
-        std::vector<int> r;
-        dissect(c, r);
-        roots.insert(roots.end(), r.begin(), r.end());
+        if ((int)c.size() > leaf_) {
+          std::vector<int> r;
+          dissect(c, r);
+          roots.insert(roots.end(), r.begin(), r.end());
+        } else {
+          if ((int)(pack.size() + c.size()) > leaf_) flush();
+          pack.insert(pack.end(), c.begin(), c.end());
+        }
       }
+      flush();
       return;
     }
     std::vector<int> &S = comps[0];
