@@ -111,10 +111,11 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def _problem():
+def _problem(grid=None):
     from doug_gb300 import problems as P
-    n, r, c, v, b = P.diffusion3d_fv(N, sigma=1.0, corr=8.0, seed=SEED)
-    part = P.block_partition(N, PARTS_PER_DIM)
+    g = grid or N
+    n, r, c, v, b = P.diffusion3d_fv(g, sigma=1.0, corr=8.0, seed=SEED)
+    part = P.block_partition(g, PARTS_PER_DIM)
     return n, r, c, v, b, part
 
 
@@ -305,7 +306,7 @@ def run_gpu(args, rank, world):
     # (multifrontal forward + backward over all levels), HBM-bound
     per_solve_s = prof.t_subsolve_s / max(prof.iterations, 1)
     achieved = prof.subsolve_bytes / per_solve_s / 1e9 if per_solve_s > 0 else None
-    roofline = {"kernel": "mf_fwd_level+mf_bwd_level (FP32 subdomain solves, all levels)",
+    roofline = {"kernel": "mf_fwd_tiles+mf_bwd_tiles+mf_fwd_warp+mf_bwd_warp (FP32 subdomain solves, all levels)",
                 "bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                 "frac": (achieved / hbm) if achieved else None, "traffic": None,
                 "peak_source": f"{peak_kind} hbm_gbs",
@@ -340,6 +341,32 @@ def run_gpu(args, rank, world):
     return 0
 
 
+def run_profile_solve(args):
+    """One solve of the workload (grid args.grid^3) inside a
+    cudaProfilerStart/Stop range, after one warm-up solve: the command the
+    kernel summaries are captured from (`ncu --profile-from-start off`)."""
+    import torch
+    import doug_gb300 as D
+
+    D.build_library()
+    torch.cuda.set_device(0)
+    n, r, c, v, b, part = _problem(args.grid)
+    s = _solver(n, r, c, v, b, part, precision=args.precision)
+    stream = torch.cuda.current_stream()
+    bd = torch.tensor(b, dtype=torch.float64, device="cuda")
+    xd = torch.empty_like(bd)
+    s.solve_device(bd.data_ptr(), xd.data_ptr(), stream.cuda_stream)
+    torch.cuda.synchronize()
+    torch.cuda.profiler.start()
+    st = s.solve_device(bd.data_ptr(), xd.data_ptr(), stream.cuda_stream)
+    torch.cuda.synchronize()
+    torch.cuda.profiler.stop()
+    print(json.dumps({"grid": args.grid, "n": n, "precision": args.precision, "iterations": st.iterations,
+                      "true_rel_residual": st.true_rel_residual, "gpu_launches": st.gpu_launches,
+                      "t_factor_s": st.t_factor_s, "t_iterate_s": st.t_iterate_s}), flush=True)
+    return 0 if st.true_rel_residual < 1e-7 else 1
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -348,7 +375,13 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--fp64-steps", type=int, default=1)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--profile-solve", action="store_true",
+                    help="one solve inside a profiler range (for ncu), no timing line")
+    ap.add_argument("--grid", type=int, default=N, help="grid size of --profile-solve")
+    ap.add_argument("--precision", type=int, default=1, help="precision of --profile-solve")
     args = ap.parse_args()
+    if args.profile_solve:
+        return run_profile_solve(args)
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     if world > 1:

@@ -34,7 +34,10 @@ struct MfView {  // device pointers of one multifrontal batch
   const int64_t *f_relmap, *f_asm;
   const int *rows, *relmap;
   const int64_t *asm_tgt, *asm_sp, *asm_src;
+  const int64_t *e_off;        // offset of the front's elimination matrix E (m x k, ld round4(m))
 };
+
+__host__ __device__ __forceinline__ int round4(int x) { return (x + 3) & ~3; }
 
 // ---------------------------------------------------------------------------
 // reductions
@@ -90,20 +93,36 @@ constexpr int kMfThreads = 256;
 constexpr int kNB = 32;      // panel width
 constexpr int kTile = 64;    // trailing-update tile (64 x 64 per CTA step, 4x4 per thread)
 
+// Every factorisation kernel also produces the front's elimination matrix
+//     E = [ L11^-1 ; -L21 L11^-1 ]     (m x k, column-major, ld = round4(m)),
+// the partial forward elimination applied to the identity columns [I ; 0]:
+// pivot j scales row j of E by 1/L(j,j) and subtracts L(i,j) times it from
+// the rows i > j.  A forward solve of the front is then the product
+// [y ; u] = E b1 + [0 ; b2] and a backward solve x1 = E^T [y ; x2]; neither
+// has a dependency chain inside the front.  E needs L only while the panel
+// that produced it is current, so the factor columns of the arena are dead
+// once E is formed; the update (Schur complement) block stays in the arena
+// for the parent's extend-add.
+
+// one CTA per front of a level (fronts of up to a few hundred rows)
 template <typename T>
 __global__ void __launch_bounds__(kMfThreads)
 mf_factor_level(MfView v, const int *__restrict__ fronts, const double *__restrict__ vals,
-                T *__restrict__ arena, int *__restrict__ status) {
+                T *__restrict__ arena, T *__restrict__ E, int *__restrict__ status) {
   __shared__ T As[kNB][kTile];
-  __shared__ T Bs[kNB][kTile];
+  __shared__ T Bs[kNB][kTile + 1];
   __shared__ T piv;
   const int f = fronts[blockIdx.x];
-  const int m = v.f_m[f], k = v.f_k[f];
+  const int m = v.f_m[f], k = v.f_k[f], ld = round4(m);
   T *F = arena + v.f_off[f];
+  T *Eg = E + v.e_off[f];
   const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5, nw = kMfThreads / 32;
-  // 1. zero the lower triangle
+  const int tx = tid & 15, ty = tid >> 4;
+  // 1. zero the lower triangle; E = [I ; 0]
   for (int c = wid; c < m; c += nw)
     for (int i = c + lane; i < m; i += 32) F[(int64_t)c * m + i] = T(0);
+  for (int c = wid; c < k; c += nw)
+    for (int i = lane; i < ld; i += 32) Eg[(int64_t)c * ld + i] = i == c ? T(1) : T(0);
   __syncthreads();
   // 2. original entries (each target appears once; duplicates summed in order)
   for (int64_t e = v.f_asm[f] + tid; e < v.f_asm[f + 1]; e += kMfThreads) {
@@ -146,10 +165,73 @@ mf_factor_level(MfView v, const int *__restrict__ fronts, const double *__restri
       }
       __syncthreads();
     }
-    // trailing update of columns [j0+jb, m): F -= Lp Lp^T (lower part)
     const int c0 = j0 + jb;
+    // E rows of the panel: E_J <- L_JJ^-1 E_J on columns [0, c0), one thread per column
+    for (int c = tid; c < c0; c += kMfThreads) {
+      T e[kNB];
+#pragma unroll
+      for (int t = 0; t < kNB; t++) e[t] = t < jb ? Eg[(int64_t)c * ld + j0 + t] : T(0);
+#pragma unroll
+      for (int t = 0; t < kNB; t++) {
+        if (t < jb) {
+          T s = e[t];
+#pragma unroll
+          for (int q = 0; q < t; q++) s -= F[(int64_t)(j0 + q) * m + j0 + t] * e[q];
+          e[t] = s / F[(int64_t)(j0 + t) * m + j0 + t];
+        }
+      }
+#pragma unroll
+      for (int t = 0; t < kNB; t++)
+        if (t < jb) Eg[(int64_t)c * ld + j0 + t] = e[t];
+    }
+    __syncthreads();
+    // E rows below the panel: E[c0:m, 0:c0] -= L[c0:m, J] E_J
+    {
+      const int ntr = (m - c0 + kTile - 1) / kTile, ntc = (c0 + kTile - 1) / kTile;
+      for (int tr = 0; tr < ntr; tr++) {
+        for (int tc = 0; tc < ntc; tc++) {
+          const int r0 = c0 + tr * kTile, e0 = tc * kTile;
+          for (int q = tid; q < kNB * kTile; q += kMfThreads) {
+            const int t = q / kTile, r = q % kTile;
+            As[t][r] = (t < jb && r0 + r < m) ? F[(int64_t)(j0 + t) * m + r0 + r] : T(0);
+          }
+          for (int q = tid; q < kNB * kTile; q += kMfThreads) {
+            const int r = q / kNB, t = q % kNB;
+            Bs[t][r] = (t < jb && e0 + r < c0) ? Eg[(int64_t)(e0 + r) * ld + j0 + t] : T(0);
+          }
+          __syncthreads();
+          T acc[4][4];
+#pragma unroll
+          for (int a = 0; a < 4; a++)
+#pragma unroll
+            for (int b = 0; b < 4; b++) acc[a][b] = T(0);
+          for (int t = 0; t < jb; t++) {
+            T ra[4], rb[4];
+#pragma unroll
+            for (int a = 0; a < 4; a++) ra[a] = As[t][tx + 16 * a];
+#pragma unroll
+            for (int b = 0; b < 4; b++) rb[b] = Bs[t][ty + 16 * b];
+#pragma unroll
+            for (int a = 0; a < 4; a++)
+#pragma unroll
+              for (int b = 0; b < 4; b++) acc[a][b] += ra[a] * rb[b];
+          }
+#pragma unroll
+          for (int b = 0; b < 4; b++) {
+            const int col = e0 + ty + 16 * b;
+            if (col >= c0) continue;
+#pragma unroll
+            for (int a = 0; a < 4; a++) {
+              const int row = r0 + tx + 16 * a;
+              if (row < m) Eg[(int64_t)col * ld + row] -= acc[a][b];
+            }
+          }
+          __syncthreads();
+        }
+      }
+    }
+    // trailing update of columns [j0+jb, m): F -= Lp Lp^T (lower part)
     const int nt = (m - c0 + kTile - 1) / kTile;
-    const int tx = tid & 15, ty = tid >> 4;
     for (int tj = 0; tj < nt; tj++) {
       for (int ti = tj; ti < nt; ti++) {
         const int r0 = c0 + ti * kTile, cc0 = c0 + tj * kTile;
@@ -196,21 +278,24 @@ mf_factor_level(MfView v, const int *__restrict__ fronts, const double *__restri
   }
 }
 
-// Small fronts: the whole m x m front lives in shared memory while it is
-// assembled and factored, then its lower part is written back.
+// Small fronts: the whole m x m front and its m x k elimination matrix live
+// in shared memory while the front is assembled and factored; then E and the
+// update block are written back.
 constexpr int kSmallThreads = 128;
 
 template <typename T>
 __global__ void __launch_bounds__(kSmallThreads)
 mf_factor_small(MfView v, const int *__restrict__ fronts, const double *__restrict__ vals,
-                T *__restrict__ arena, int *__restrict__ status) {
+                T *__restrict__ arena, T *__restrict__ E, int *__restrict__ status) {
   extern __shared__ unsigned char smem_raw[];
   T *S = reinterpret_cast<T *>(smem_raw);
   const int f = fronts[blockIdx.x];
   const int m = v.f_m[f], k = v.f_k[f];
+  T *Es = S + m * m;  // m x k, column-major, ld m
   const int64_t off = v.f_off[f];
   const int tid = threadIdx.x, nt = kSmallThreads;
   for (int q = tid; q < m * m; q += nt) S[q] = T(0);
+  for (int q = tid; q < m * k; q += nt) Es[q] = q / m == q % m ? T(1) : T(0);
   __syncthreads();
   for (int64_t e = v.f_asm[f] + tid; e < v.f_asm[f + 1]; e += nt) {
     double sv = 0.0;
@@ -238,18 +323,26 @@ mf_factor_small(MfView v, const int *__restrict__ fronts, const double *__restri
     __syncthreads();
     const T p = S[j * m + j];
     for (int i = j + 1 + tid; i < m; i += nt) S[j * m + i] /= p;
+    for (int c = tid; c <= j; c += nt) Es[c * m + j] /= p;
     __syncthreads();
     const int r = m - j - 1;
     for (int q = tid; q < r * r; q += nt) {
       const int c = j + 1 + q / r, i = j + 1 + q % r;
       if (i >= c) S[c * m + i] -= S[j * m + i] * S[j * m + c];
     }
+    for (int q = tid; q < r * (j + 1); q += nt) {
+      const int c = q / r, i = j + 1 + q % r;
+      Es[c * m + i] -= S[j * m + i] * Es[c * m + j];
+    }
     __syncthreads();
   }
+  const int ld = round4(m);
+  T *Eg = E + v.e_off[f];
+  for (int q = tid; q < m * k; q += nt) Eg[(int64_t)(q / m) * ld + q % m] = Es[q];
   T *F = arena + off;
-  for (int q = tid; q < m * m; q += nt) {
-    const int c = q / m, i = q % m;
-    if (i >= c) F[q] = S[q];
+  for (int q = tid; q < (m - k) * m; q += nt) {
+    const int c = k + q / m, i = q % m;
+    if (i >= c) F[(int64_t)c * m + i] = S[c * m + i];
   }
 }
 
@@ -360,11 +453,19 @@ mf_diag(MfView v, const int *__restrict__ fronts, int j0, T *__restrict__ arena,
   }
 }
 
+// E rows of the panel (escale task = {front, first column}): E_J <- L_JJ^-1 E_J
+// on kEscCols columns of [0, j0 + jb); the columns of block J start as the
+// identity, so block J of E becomes L_JJ^-1
+template <typename T> struct EscCols { static constexpr int N = 1024 / sizeof(T); };
+
 template <typename T>
 __global__ void __launch_bounds__(kMfThreads)
-mf_panel(MfView v, const int2 *__restrict__ tasks, int j0, T *__restrict__ arena) {
+mf_panel(MfView v, const int2 *__restrict__ tasks, int npanel, const int2 *__restrict__ esc, int j0,
+         T *__restrict__ arena, T *__restrict__ E) {
   __shared__ T D[kNB][kNB + 1];
-  const int f = tasks[blockIdx.x].x, r0 = tasks[blockIdx.x].y;
+  const bool escale = (int)blockIdx.x >= npanel;
+  const int2 task = escale ? esc[blockIdx.x - npanel] : tasks[blockIdx.x];
+  const int f = task.x;
   const int m = v.f_m[f], k = v.f_k[f];
   const int jb = min(kNB, k - j0);
   T *F = arena + v.f_off[f];
@@ -373,7 +474,35 @@ mf_panel(MfView v, const int2 *__restrict__ tasks, int j0, T *__restrict__ arena
     int c = q / jb, i = q % jb;
     D[i][c] = i >= c ? F[(int64_t)(j0 + c) * m + j0 + i] : T(0);
   }
+  if (escale) {
+    constexpr int NC = EscCols<T>::N;
+    __shared__ T Eb[NC][kNB + 1];
+    const int ld = round4(m);
+    T *Eg = E + v.e_off[f];
+    const int c0 = task.y, nc = min(NC, j0 + jb - c0);
+    for (int q = tid; q < nc * kNB; q += kMfThreads) {
+      const int cc = q / kNB, t = q % kNB, c = c0 + cc;
+      T e = T(0);
+      if (t < jb) e = c < j0 ? Eg[(int64_t)c * ld + j0 + t] : (c - j0 == t ? T(1) : T(0));
+      Eb[cc][t] = e;
+    }
+    __syncthreads();
+    for (int cc = tid; cc < nc; cc += kMfThreads) {
+      for (int t = 0; t < jb; t++) {
+        T s = Eb[cc][t];
+        for (int q = 0; q < t; q++) s -= D[t][q] * Eb[cc][q];
+        Eb[cc][t] = s / D[t][t];
+      }
+    }
+    __syncthreads();
+    for (int q = tid; q < nc * kNB; q += kMfThreads) {
+      const int cc = q / kNB, t = q % kNB;
+      if (t < jb) Eg[(int64_t)(c0 + cc) * ld + j0 + t] = Eb[cc][t];
+    }
+    return;
+  }
   __syncthreads();
+  const int r0 = task.y;
   const int rb = max(r0, j0 + jb), re = min(r0 + kPanelRows, m);
   for (int i = rb + tid; i < re; i += kMfThreads) {
     T x[kNB];
@@ -394,30 +523,44 @@ mf_panel(MfView v, const int2 *__restrict__ tasks, int j0, T *__restrict__ arena
   }
 }
 
-// one 64x64 tile of the trailing update after the panel at j0;
-// task = {front, (ti << 16) | tj}, tiles relative to column j0 + jb
+// one 64x64 tile after the panel at j0: either a tile of the trailing update
+// (task = {front, (ti << 16) | tj}, tiles relative to column j0 + jb) or, for
+// blockIdx.x >= nupd, a tile of the E update E[c0:m, 0:c0] -= L[c0:m, J] E_J
+// (task = {front, (ti << 16) | tc}, rows relative to c0 = j0 + jb, columns
+// from 0); the columns of block J are assigned, the earlier ones accumulated
 template <typename T>
 __global__ void __launch_bounds__(kMfThreads)
-mf_update(MfView v, const int2 *__restrict__ tasks, int j0, T *__restrict__ arena) {
+mf_update(MfView v, const int2 *__restrict__ tasks, int nupd, const int2 *__restrict__ etasks, int j0,
+          T *__restrict__ arena, T *__restrict__ E) {
   __shared__ T As[kNB][kTile];
-  __shared__ T Bs[kNB][kTile];
-  const int f = tasks[blockIdx.x].x;
-  const int ti = tasks[blockIdx.x].y >> 16, tj = tasks[blockIdx.x].y & 0xffff;
+  __shared__ T Bs[kNB][kTile + 1];
+  const bool etile = (int)blockIdx.x >= nupd;
+  const int2 task = etile ? etasks[blockIdx.x - nupd] : tasks[blockIdx.x];
+  const int f = task.x;
+  const int ti = task.y >> 16, tj = task.y & 0xffff;
   const int m = v.f_m[f], k = v.f_k[f];
   const int jb = min(kNB, k - j0);
   T *F = arena + v.f_off[f];
   const int c0 = j0 + jb;
-  const int r0 = c0 + ti * kTile, cc0 = c0 + tj * kTile;
+  const int r0 = c0 + ti * kTile;
+  const int cc0 = etile ? tj * kTile : c0 + tj * kTile;
   const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
+  const int ld = round4(m);
+  T *Eg = E + v.e_off[f];
   for (int q = tid; q < kNB * kTile; q += kMfThreads) {
     int t = q / kTile, r = q % kTile;
-    T a = T(0), b = T(0);
-    if (t < jb) {
-      if (r0 + r < m) a = F[(int64_t)(j0 + t) * m + r0 + r];
-      if (cc0 + r < m) b = F[(int64_t)(j0 + t) * m + cc0 + r];
+    As[t][r] = (t < jb && r0 + r < m) ? F[(int64_t)(j0 + t) * m + r0 + r] : T(0);
+  }
+  if (etile) {
+    for (int q = tid; q < kNB * kTile; q += kMfThreads) {
+      const int r = q / kNB, t = q % kNB;
+      Bs[t][r] = (t < jb && cc0 + r < c0) ? Eg[(int64_t)(cc0 + r) * ld + j0 + t] : T(0);
     }
-    As[t][r] = a;
-    Bs[t][r] = b;
+  } else {
+    for (int q = tid; q < kNB * kTile; q += kMfThreads) {
+      int t = q / kTile, r = q % kTile;
+      Bs[t][r] = (t < jb && cc0 + r < m) ? F[(int64_t)(j0 + t) * m + cc0 + r] : T(0);
+    }
   }
   __syncthreads();
   T acc[4][4];
@@ -436,6 +579,21 @@ mf_update(MfView v, const int2 *__restrict__ tasks, int j0, T *__restrict__ aren
 #pragma unroll
       for (int b = 0; b < 4; b++) acc[a][b] += ra[a] * rb[b];
   }
+  if (etile) {
+#pragma unroll
+    for (int b = 0; b < 4; b++) {
+      const int col = cc0 + ty + 16 * b;
+      if (col >= c0) continue;
+#pragma unroll
+      for (int a = 0; a < 4; a++) {
+        const int row = r0 + tx + 16 * a;
+        if (row >= m) continue;
+        T *dst = Eg + (int64_t)col * ld + row;
+        *dst = col >= j0 ? -acc[a][b] : *dst - acc[a][b];
+      }
+    }
+    return;
+  }
 #pragma unroll
   for (int b = 0; b < 4; b++) {
     const int col = cc0 + ty + 16 * b;
@@ -449,560 +607,53 @@ mf_update(MfView v, const int2 *__restrict__ tasks, int j0, T *__restrict__ aren
 }
 
 // ---------------------------------------------------------------------------
-// multifrontal solves
+// multifrontal solves with the elimination matrices E
+//
+// Forward, one level:  the front's right-hand side is b = [xl(pivots) ; 0]
+// plus the children's update vectors (extend-add, children in order); then
+//     y = E[0:k, :] b1   -> yl (pivots)      u = b2 + E[k:m, :] b1 -> uvec.
+// Backward, one level: v = [yl(pivots) ; xl(ancestor rows)], x1 = E^T v -> xl.
+// The forward writes y to a second local vector so that the CTAs of one front
+// never overwrite the right-hand side another CTA still reads.
+//
+// E is read with 16-byte vector loads: ld = round4(m) and every E block starts
+// on a multiple of 4 elements, and the padding rows m..ld-1 are zero.
 // ---------------------------------------------------------------------------
-// Solves keep the front's work vector w (length m) in shared memory when it
-// fits (`wglob` otherwise) and walk the pivots in blocks of 32 columns: one
-// warp solves the 32x32 triangle, all warps apply the block to the rest.
-constexpr int kSB = 32;
-
-// forward: w = [b_piv ; 0] + children's update vectors; y = L11^-1 w1;
-// this front's update vector = w2 - L21 y
-template <typename T>
-__global__ void __launch_bounds__(kMfThreads)
-mf_fwd_level(MfView v, const int *__restrict__ fronts, const T *__restrict__ arena,
-             T *__restrict__ xl, T *__restrict__ uvec, T *__restrict__ wglob, int use_smem) {
-  extern __shared__ unsigned char smem_raw[];
-  const int f = fronts[blockIdx.x];
-  const int m = v.f_m[f], k = v.f_k[f];
-  const T *F = arena + v.f_off[f];
-  T *w = use_smem ? reinterpret_cast<T *>(smem_raw) : wglob + v.f_woff[f];
-  T *x = xl + v.f_xoff[f] + v.f_p0[f];
-  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
-  for (int i = tid; i < m; i += kMfThreads) w[i] = i < k ? x[i] : T(0);
-  __syncthreads();
-  for (int ci = v.f_child_ptr[f]; ci < v.f_child_ptr[f + 1]; ci++) {
-    const int c = v.f_children[ci];
-    const int rc = v.f_m[c] - v.f_k[c];
-    const int *rel = v.relmap + v.f_relmap[c];
-    const T *u = uvec + v.f_uoff[c];
-    for (int a = tid; a < rc; a += kMfThreads) w[rel[a]] += u[a];
-    __syncthreads();
+template <typename T> struct Vec16;
+template <> struct Vec16<float> {
+  static constexpr int N = 4;
+  __device__ static __forceinline__ void load(const float *p, float *o) {
+    const float4 t = __ldg(reinterpret_cast<const float4 *>(p));
+    o[0] = t.x; o[1] = t.y; o[2] = t.z; o[3] = t.w;
   }
-  __shared__ T Dg[kSB][kSB + 1];
-  for (int J0 = 0; J0 < k; J0 += kSB) {
-    const int jb = min(kSB, k - J0);
-    for (int q = tid; q < jb * jb; q += kMfThreads) {
-      int c = q / jb, i = q % jb;
-      Dg[i][c] = F[(int64_t)(J0 + c) * m + J0 + i];
-    }
-    __syncthreads();
-    if (wid == 0) {
-      T wl = lane < jb ? w[J0 + lane] : T(0);
-      for (int j = 0; j < jb; j++) {
-        const T yj = __shfl_sync(0xffffffffu, wl, j) / Dg[j][j];
-        if (lane == j) wl = yj;
-        if (lane > j && lane < jb) wl -= Dg[lane][j] * yj;
-      }
-      if (lane < jb) w[J0 + lane] = wl;
-    }
-    __syncthreads();
-    for (int i = J0 + jb + tid; i < m; i += kMfThreads) {
-      T s = T(0);
-#pragma unroll 8
-      for (int j = 0; j < jb; j++) s += F[(int64_t)(J0 + j) * m + i] * w[J0 + j];
-      w[i] -= s;
-    }
-    __syncthreads();
-  }
-  for (int i = tid; i < k; i += kMfThreads) x[i] = w[i];
-  T *u = uvec + v.f_uoff[f];
-  for (int a = tid; a < m - k; a += kMfThreads) u[a] = w[k + a];
-}
-
-// backward: x_piv = L11^-T (y - L21^T x_rows)
-template <typename T>
-__global__ void __launch_bounds__(kMfThreads)
-mf_bwd_level(MfView v, const int *__restrict__ fronts, const T *__restrict__ arena,
-             T *__restrict__ xl, T *__restrict__ wglob, int use_smem) {
-  extern __shared__ unsigned char smem_raw[];
-  const int f = fronts[blockIdx.x];
-  const int m = v.f_m[f], k = v.f_k[f];
-  const T *F = arena + v.f_off[f];
-  T *w = use_smem ? reinterpret_cast<T *>(smem_raw) : wglob + v.f_woff[f];
-  T *xb = xl + v.f_xoff[f];
-  const int *rows = v.rows + v.f_rows[f];
-  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5, nw = kMfThreads / 32;
-  for (int i = tid; i < m; i += kMfThreads) w[i] = xb[rows[i]];
-  __syncthreads();
-  // contributions of the already solved update rows
-  for (int j = wid; j < k; j += nw) {
-    T s = T(0);
-    for (int i = k + lane; i < m; i += 32) s += F[(int64_t)j * m + i] * w[i];
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
-    if (lane == 0) w[j] -= s;
-  }
-  __syncthreads();
-  __shared__ T Dg[kSB][kSB + 1];
-  for (int J1 = k; J1 > 0; J1 -= kSB) {
-    const int J0 = max(0, J1 - kSB), jb = J1 - J0;
-    for (int q = tid; q < jb * jb; q += kMfThreads) {
-      int c = q / jb, i = q % jb;
-      Dg[i][c] = F[(int64_t)(J0 + c) * m + J0 + i];
-    }
-    __syncthreads();
-    if (wid == 0) {
-      T wl = lane < jb ? w[J0 + lane] : T(0);
-      for (int j = jb - 1; j >= 0; j--) {
-        // x_j = (w_j - sum_{i>j in block} L(i,j) x_i) / L(j,j); the sum is
-        // accumulated into wl of lane j by the lanes of the solved rows
-        T contrib = (lane > j && lane < jb) ? Dg[lane][j] * wl : T(0);
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) contrib += __shfl_down_sync(0xffffffffu, contrib, o);
-        contrib = __shfl_sync(0xffffffffu, contrib, 0);
-        if (lane == j) wl = (wl - contrib) / Dg[j][j];
-      }
-      if (lane < jb) w[J0 + lane] = wl;
-    }
-    __syncthreads();
-    // columns left of the block: w_j -= sum_{i in block} L(i,j) x_i
-    for (int j = wid; j < J0; j += nw) {
-      T s = lane < jb ? F[(int64_t)j * m + J0 + lane] * w[J0 + lane] : T(0);
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
-      if (lane == 0) w[j] -= s;
-    }
-    __syncthreads();
-  }
-  for (int i = tid; i < k; i += kMfThreads) xb[rows[i]] = w[i];
-}
-
-// ---------------------------------------------------------------------------
-// Tiled solve layout of large fronts.  After the factorisation every 32-column
-// block J of a large front (columns 32J .. 32J+jb) is stored as a contiguous
-// run:
-//   Dinv_J                        inverse of the jb x jb diagonal block (32 x 32)
-//   run of rank 0, rank 1, ...    32x32 tiles tile(R, J), row-major, for the
-//                                 row blocks R >= J owned by that cluster rank
-//                                 (R % C == rank), ascending R
-// Entries of the diagonal block (and rows past m) are zero in tile(J, J).
-// The solves of one front are split over a thread-block cluster of C CTAs:
-// CTA q owns the row blocks R with R % C == q, keeps their part of the work
-// vector in shared memory and streams its own tile run with cp.async, G tiles
-// per stage; the CTAs exchange the 32-value block solutions through
-// distributed shared memory with one cluster barrier per column block.
-// C = 1 is the plain one-CTA solve.
-// ---------------------------------------------------------------------------
-constexpr int kTileThreads = 256;
-template <typename T> struct TilePipe;
-template <> struct TilePipe<float> { static constexpr int G = 4, S = 4; };   // 16 KB stages, 64 KB ring
-template <> struct TilePipe<double> { static constexpr int G = 2, S = 4; };  // 16 KB stages, 64 KB ring
-
-struct PackView {
-  const int *blk_front;        // block -> front
-  const int *blk_j;            // block -> J
-  const int *f_blk;            // front -> first block (large fronts), -1 otherwise
-  const int64_t *blk_off;      // block -> element offset in the packed buffer
-  const int *f_C;              // front -> cluster size of its solves
 };
-
-__host__ __device__ __forceinline__ int first_owned(int J, int C, int q) {  // smallest R >= J, R % C == q
-  return J + ((q - J % C) % C + C) % C;
-}
-__host__ __device__ __forceinline__ int owned_count(int J, int nR, int C, int q) {
-  const int f0 = first_owned(J, C, q);
-  return f0 < nR ? (nR - f0 + C - 1) / C : 0;
-}
-
-// one CTA per column block: invert the diagonal block, copy the tiles
-template <typename T>
-__global__ void __launch_bounds__(256)
-mf_pack(MfView v, PackView pk, const T *__restrict__ arena, T *__restrict__ packed) {
-  __shared__ T L[32][33];
-  __shared__ T X[32][33];
-  const int b = blockIdx.x;
-  const int f = pk.blk_front[b], J = pk.blk_j[b];
-  const int m = v.f_m[f], k = v.f_k[f], C = pk.f_C[f];
-  const int J0 = 32 * J, jb = min(32, k - J0);
-  const T *F = arena + v.f_off[f];
-  T *dst = packed + pk.blk_off[b];
-  const int tid = threadIdx.x;
-  for (int q = tid; q < 32 * 32; q += 256) {
-    int c = q / 32, i = q % 32;
-    L[i][c] = (i < jb && c < jb && i >= c) ? F[(int64_t)(J0 + c) * m + J0 + i] : T(0);
-    X[i][c] = T(0);
-  }
-  __syncthreads();
-  if (tid < jb) {  // column tid of the inverse of a lower triangular block
-    const int c = tid;
-    X[c][c] = T(1) / L[c][c];
-    for (int i = c + 1; i < jb; i++) {
-      T sum = T(0);
-      for (int t = c; t < i; t++) sum += L[i][t] * X[t][c];
-      X[i][c] = -sum / L[i][i];
-    }
-  }
-  __syncthreads();
-  for (int q = tid; q < 32 * 32; q += 256) dst[q] = X[q / 32][q % 32];
-  const int nR = (m + 31) / 32;
-  for (int R = J; R < nR; R++) {
-    const int rank = R % C;
-    int pos = 0;
-    for (int r = 0; r < rank; r++) pos += owned_count(J, nR, C, r);
-    pos += (R - first_owned(J, C, rank)) / C;
-    T *td = dst + 1024 * (int64_t)(1 + pos);
-    for (int q = tid; q < 32 * 32; q += 256) {
-      const int rr = q / 32, c = q % 32;  // row-major tile
-      const int row = 32 * R + rr;
-      td[q] = (c < jb && row >= J0 + jb && row < m) ? F[(int64_t)(J0 + c) * m + row] : T(0);
-    }
-  }
-}
-
-__device__ __forceinline__ void cp_async16(void *smem, const void *gmem) {
-  unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
-  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(gmem));
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::); }
-template <int N>
-__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N)); }
-
-template <typename T>
-__device__ __forceinline__ void issue_chunk(T *slot, const T *src, int elems) {
-  const int n16 = elems * (int)sizeof(T) / 16;
-  for (int q = threadIdx.x; q < n16; q += blockDim.x)
-    cp_async16(reinterpret_cast<char *>(slot) + 16 * q, reinterpret_cast<const char *>(src) + 16 * q);
-}
-
-// distributed shared memory helpers (cluster rank of this CTA; remote loads)
-__device__ __forceinline__ unsigned cluster_rank() {
-  unsigned r;
-  asm volatile("mov.u32 %0, %%cluster_ctarank;\n" : "=r"(r));
-  return r;
-}
-__device__ __forceinline__ void cluster_sync() {
-  asm volatile("barrier.cluster.arrive.release.aligned;\nbarrier.cluster.wait.acquire.aligned;\n" ::: "memory");
-}
-template <typename T>
-__device__ __forceinline__ T ld_dsmem(const T *local_addr, unsigned rank);
-template <>
-__device__ __forceinline__ double ld_dsmem<double>(const double *p, unsigned rank) {
-  unsigned sa = (unsigned)__cvta_generic_to_shared(p), ra;
-  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;\n" : "=r"(ra) : "r"(sa), "r"(rank));
-  double v;
-  asm volatile("ld.shared::cluster.f64 %0, [%1];\n" : "=d"(v) : "r"(ra) : "memory");
-  return v;
-}
-template <>
-__device__ __forceinline__ float ld_dsmem<float>(const float *p, unsigned rank) {
-  unsigned sa = (unsigned)__cvta_generic_to_shared(p), ra;
-  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;\n" : "=r"(ra) : "r"(sa), "r"(rank));
-  float v;
-  asm volatile("ld.shared::cluster.f32 %0, [%1];\n" : "=f"(v) : "r"(ra) : "memory");
-  return v;
-}
-
-// The chunks one CTA consumes, in order.  Forward: for J ascending, Dinv_J
-// (if the CTA owns row block J) then its tile run of block J in pieces of G
-// tiles.  Backward: for J descending, the tile run, then Dinv_J if owned.
-template <typename T>
-struct ChunkCursor {
-  const int64_t *blk_off;
-  int fb, nb, nR, C, q;
-  bool fwd;
-  int J, t0, cnt;   // current block, first tile of the piece, tiles owned in block J
-  bool dinv;        // current chunk is Dinv_J
-  __device__ void setup_block() {
-    cnt = owned_count(J, nR, C, q);
-    t0 = 0;
-    dinv = fwd ? (J % C == q) : false;
-    if (!fwd && cnt == 0) dinv = (J % C == q);
-  }
-  __device__ void start(const int64_t *bo, int fb_, int nb_, int nR_, int C_, int q_, bool fwd_) {
-    blk_off = bo; fb = fb_; nb = nb_; nR = nR_; C = C_; q = q_; fwd = fwd_;
-    J = fwd ? 0 : nb - 1;
-    setup_block();
-    settle();
-  }
-  __device__ bool valid() const { return J >= 0 && J < nb; }
-  __device__ bool has_chunk() const { return dinv || t0 < cnt; }
-  __device__ void settle() {  // skip blocks without a chunk for this CTA
-    while (valid() && !has_chunk()) {
-      J += fwd ? 1 : -1;
-      if (valid()) setup_block();
-    }
-  }
-  __device__ void advance() {
-    constexpr int G = TilePipe<T>::G;
-    if (fwd) {
-      if (dinv) dinv = false;
-      else t0 += G;
-    } else {
-      if (t0 < cnt) {
-        t0 += G;
-        if (t0 >= cnt) dinv = (J % C == q);
-      } else {
-        dinv = false;
-      }
-    }
-    if (!has_chunk()) {
-      J += fwd ? 1 : -1;
-      if (valid()) setup_block();
-    }
-    settle();
-  }
-  __device__ int ntiles() const { return min(TilePipe<T>::G, cnt - t0); }
-  __device__ const T *src(const T *packed, int &elems) const {
-    const T *base = packed + blk_off[fb + J];
-    if (dinv) { elems = 1024; return base; }
-    int pre = 0;
-    for (int r = 0; r < q; r++) pre += owned_count(J, nR, C, r);
-    elems = 1024 * ntiles();
-    return base + 1024 * (int64_t)(1 + pre + t0);
+template <> struct Vec16<double> {
+  static constexpr int N = 2;
+  __device__ static __forceinline__ void load(const double *p, double *o) {
+    const double2 t = __ldg(reinterpret_cast<const double2 *>(p));
+    o[0] = t.x; o[1] = t.y;
   }
 };
 
-// forward solve, grid = nfronts * C, cluster (C,1,1)
-template <typename T, int C>
-__global__ void __launch_bounds__(kTileThreads)
-mf_fwd_tiles(MfView v, PackView pk, const int *__restrict__ fronts, const T *__restrict__ packed,
-             T *__restrict__ xl, T *__restrict__ uvec) {
-  constexpr int G = TilePipe<T>::G, S = TilePipe<T>::S, SLOT = G * 1024;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  T *ring = reinterpret_cast<T *>(smem_raw);            // S slots of G tiles
-  T *wloc = ring + S * SLOT;                            // owned row blocks x 32
-  __shared__ T ybuf[2][32];
-  __shared__ T yJ[32];
-  const unsigned q = C > 1 ? cluster_rank() : 0;
-  const int f = fronts[blockIdx.x / C];
-  const int m = v.f_m[f], k = v.f_k[f];
-  const int fb = pk.f_blk[f], nb = (k + 31) / 32, nR = (m + 31) / 32;
-  const int tid = threadIdx.x;
-  T *x = xl + v.f_xoff[f] + v.f_p0[f];
-  auto loc = [&](int row) -> T & { return wloc[(row / 32) / C * 32 + row % 32]; };
-  auto owned = [&](int row) { return (row / 32) % C == (int)q; };
-  ChunkCursor<T> cur;
-  cur.start(pk.blk_off, fb, nb, nR, C, (int)q, true);
-  for (int st = 0; st < S; st++) {
-    if (cur.valid()) {
-      int el;
-      const T *sp = cur.src(packed, el);
-      issue_chunk<T>(ring + st * SLOT, sp, el);
-      cur.advance();
-    }
-    cp_async_commit();
-  }
-  const int nown = (nR - (int)q + C - 1) / C;
-  for (int i = tid; i < nown * 32; i += kTileThreads) {
-    const int row = ((i / 32) * C + (int)q) * 32 + i % 32;
-    wloc[i] = row < k ? x[row] : T(0);
-  }
-  __syncthreads();
-  for (int ci = v.f_child_ptr[f]; ci < v.f_child_ptr[f + 1]; ci++) {
-    const int c = v.f_children[ci];
-    const int rc = v.f_m[c] - v.f_k[c];
-    const int *rel = v.relmap + v.f_relmap[c];
-    const T *u = uvec + v.f_uoff[c];
-    for (int a = tid; a < rc; a += kTileThreads) {
-      const int row = rel[a];
-      if (owned(row)) loc(row) += u[a];
-    }
-    __syncthreads();
-  }
-  int slot = 0;
-  auto refill = [&]() {
-    if (cur.valid()) {
-      int el;
-      const T *sp = cur.src(packed, el);
-      issue_chunk<T>(ring + slot * SLOT, sp, el);
-      cur.advance();
-    }
-    cp_async_commit();
-    slot = (slot + 1) % S;
-  };
-  for (int J = 0; J < nb; J++) {
-    const int J0 = 32 * J, jb = min(32, k - J0);
-    if (J % C == (int)q) {  // owner: y_J = Dinv_J w_J (its Dinv is the next chunk)
-      cp_async_wait<S - 1>();
-      __syncthreads();
-      const T *Sm = ring + slot * SLOT;
-      if (tid < 32) {
-        T sum = T(0);
-        if (tid < jb)
-          for (int sidx = 0; sidx <= tid; sidx++) sum += Sm[tid * 32 + sidx] * loc(J0 + sidx);
-        ybuf[J & 1][tid] = sum;  // zero past jb: the padded tile columns multiply it
-      }
-      __syncthreads();
-      if (tid < jb) loc(J0 + tid) = ybuf[J & 1][tid];
-      __syncthreads();
-      refill();
-    }
-    if (C > 1) cluster_sync();
-    if (tid < 32) yJ[tid] = C > 1 ? ld_dsmem<T>(&ybuf[J & 1][tid], (unsigned)(J % C)) : ybuf[J & 1][tid];
-    __syncthreads();
-    const int cnt = owned_count(J, nR, C, (int)q);
-    const int f0 = first_owned(J, C, (int)q);
-    for (int t0 = 0; t0 < cnt; t0 += G) {
-      cp_async_wait<S - 1>();
-      __syncthreads();
-      const T *Sm = ring + slot * SLOT;
-      const int nt = min(G, cnt - t0);
-      const int rr = tid >> 3, c4 = (tid & 7) * 4;  // 8 threads per tile row
-      for (int t = 0; t < nt; t++) {
-        const T *tl = Sm + t * 1024;
-        T part = tl[rr * 32 + c4] * yJ[c4] + tl[rr * 32 + c4 + 1] * yJ[c4 + 1] +
-                 tl[rr * 32 + c4 + 2] * yJ[c4 + 2] + tl[rr * 32 + c4 + 3] * yJ[c4 + 3];
-        part += __shfl_down_sync(0xffffffffu, part, 4, 8);
-        part += __shfl_down_sync(0xffffffffu, part, 2, 8);
-        part += __shfl_down_sync(0xffffffffu, part, 1, 8);
-        const int row = 32 * (f0 + (t0 + t) * C) + rr;
-        if ((tid & 7) == 0 && row < m) loc(row) -= part;
-      }
-      __syncthreads();
-      refill();
-    }
-  }
-  cp_async_wait<0>();
-  __syncthreads();
-  for (int i = tid; i < nown * 32; i += kTileThreads) {
-    const int row = ((i / 32) * C + (int)q) * 32 + i % 32;
-    if (row < k) x[row] = wloc[i];
-    else if (row < m) uvec[v.f_uoff[f] + row - k] = wloc[i];
-  }
-  if (C > 1) cluster_sync();  // no CTA leaves while its shared memory may still be read
-}
+constexpr int kSolveSmall = 128;   // fronts of at most this many rows: one warp each
+constexpr int kEThreads = 256;
+constexpr int kEUnroll = 8;        // independent E loads in flight per thread
 
-// backward solve, grid = nfronts * C, cluster (C,1,1)
-template <typename T, int C>
-__global__ void __launch_bounds__(kTileThreads)
-mf_bwd_tiles(MfView v, PackView pk, const int *__restrict__ fronts, const T *__restrict__ packed,
-             T *__restrict__ xl) {
-  constexpr int G = TilePipe<T>::G, S = TilePipe<T>::S, SLOT = G * 1024;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  T *ring = reinterpret_cast<T *>(smem_raw);
-  T *wloc = ring + S * SLOT;
-  __shared__ T part[2][32];
-  __shared__ T red[8][32];
-  __shared__ T tJ[32];
-  const unsigned q = C > 1 ? cluster_rank() : 0;
-  const int f = fronts[blockIdx.x / C];
-  const int m = v.f_m[f], k = v.f_k[f];
-  const int fb = pk.f_blk[f], nb = (k + 31) / 32, nR = (m + 31) / 32;
-  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
-  T *xb = xl + v.f_xoff[f];
-  const int *rows = v.rows + v.f_rows[f];
-  auto loc = [&](int row) -> T & { return wloc[(row / 32) / C * 32 + row % 32]; };
-  ChunkCursor<T> cur;
-  cur.start(pk.blk_off, fb, nb, nR, C, (int)q, false);
-  for (int st = 0; st < S; st++) {
-    if (cur.valid()) {
-      int el;
-      const T *sp = cur.src(packed, el);
-      issue_chunk<T>(ring + st * SLOT, sp, el);
-      cur.advance();
-    }
-    cp_async_commit();
-  }
-  const int nown = (nR - (int)q + C - 1) / C;
-  for (int i = tid; i < nown * 32; i += kTileThreads) {
-    const int row = ((i / 32) * C + (int)q) * 32 + i % 32;
-    wloc[i] = row < m ? xb[rows[row]] : T(0);
-  }
-  __syncthreads();
-  int slot = 0;
-  auto refill = [&]() {
-    if (cur.valid()) {
-      int el;
-      const T *sp = cur.src(packed, el);
-      issue_chunk<T>(ring + slot * SLOT, sp, el);
-      cur.advance();
-    }
-    cp_async_commit();
-    slot = (slot + 1) % S;
-  };
-  for (int J = nb - 1; J >= 0; J--) {
-    const int J0 = 32 * J, jb = min(32, k - J0);
-    // partial t_J = sum over owned R >= J of tile(R,J)^T x_R
-    T acc = T(0);  // thread (wid, lane): column lane, rows wid*4 .. wid*4+3 of each tile
-    const int cnt = owned_count(J, nR, C, (int)q);
-    const int f0 = first_owned(J, C, (int)q);
-    for (int t0 = 0; t0 < cnt; t0 += G) {
-      cp_async_wait<S - 1>();
-      __syncthreads();
-      const T *Sm = ring + slot * SLOT;
-      const int nt = min(G, cnt - t0);
-      for (int t = 0; t < nt; t++) {
-        const T *tl = Sm + t * 1024;
-        const int R = f0 + (t0 + t) * C;
-#pragma unroll
-        for (int u = 0; u < 4; u++) {
-          const int rr = wid * 4 + u;
-          const int row = 32 * R + rr;
-          if (row < m) acc += tl[rr * 32 + lane] * loc(row);
-        }
-      }
-      __syncthreads();
-      refill();
-    }
-    red[wid][lane] = acc;
-    __syncthreads();
-    if (tid < 32) {
-      T s = T(0);
-#pragma unroll
-      for (int w = 0; w < 8; w++) s += red[w][tid];
-      part[J & 1][tid] = s;
-    }
-    __syncthreads();
-    if (C > 1) cluster_sync();
-    if (J % C == (int)q) {  // owner: t_J = y_J - sum of partials; x_J = Dinv_J^T t_J
-      if (tid < 32) {
-        T s = T(0);
-        for (int r = 0; r < C; r++) s += C > 1 ? ld_dsmem<T>(&part[J & 1][tid], (unsigned)r) : part[J & 1][tid];
-        tJ[tid] = tid < jb ? loc(J0 + tid) - s : T(0);
-      }
-      cp_async_wait<S - 1>();
-      __syncthreads();
-      const T *Sm = ring + slot * SLOT;
-      if (tid < jb) {
-        T sum = T(0);
-        for (int sidx = tid; sidx < jb; sidx++) sum += Sm[sidx * 32 + tid] * tJ[sidx];
-        loc(J0 + tid) = sum;
-      }
-      __syncthreads();
-      refill();
-    }
-  }
-  cp_async_wait<0>();
-  __syncthreads();
-  for (int i = tid; i < nown * 32; i += kTileThreads) {
-    const int row = ((i / 32) * C + (int)q) * 32 + i % 32;
-    if (row < k) xb[rows[row]] = wloc[i];
-  }
-  if (C > 1) cluster_sync();
-}
-
-// ---------------------------------------------------------------------------
-// Small fronts (m <= 128): one warp per front.  The front's factor columns
-// (m x k, contiguous in the arena) are staged in shared memory with cp.async,
-// then the pivots are eliminated from shared memory.
-// ---------------------------------------------------------------------------
-__host__ __device__ __forceinline__ int round4(int x) { return (x + 3) & ~3; }
-
+// small fronts, forward: one warp per front; lane l holds rows VN*l + 32*VN*p
 template <typename T>
-__device__ __forceinline__ void stage_factor_warp(T *Ls, const T *src, int elems) {
-  const int lane = threadIdx.x & 31;
-  const int n16 = (elems * (int)sizeof(T) + 15) / 16;
-  for (int q = lane; q < n16; q += 32)
-    cp_async16(reinterpret_cast<char *>(Ls) + 16 * q, reinterpret_cast<const char *>(src) + 16 * q);
-  cp_async_commit();
-}
-
-template <typename T>
-__global__ void __launch_bounds__(256)
-mf_fwd_warp(MfView v, const int *__restrict__ fronts, int nf, const T *__restrict__ arena,
-            T *__restrict__ xl, T *__restrict__ uvec, int per_warp) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
+__global__ void __launch_bounds__(256, 4)
+mf_fwd_small(MfView v, const int *__restrict__ fronts, int nf, const T *__restrict__ E,
+             const T *__restrict__ xl, T *__restrict__ yl, T *__restrict__ uvec) {
+  constexpr int VN = Vec16<T>::N, PASS = kSolveSmall / (32 * VN);
+  __shared__ __align__(16) T wsh[8][kSolveSmall];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
   const int gw = blockIdx.x * nw + wid;
   if (gw >= nf) return;  // warp-level kernel: no block barriers below
-  T *Ls = reinterpret_cast<T *>(smem_raw) + (size_t)wid * per_warp;
+  T *w = wsh[wid];
   const int f = fronts[gw];
-  const int m = v.f_m[f], k = v.f_k[f];
-  T *w = Ls + round4(m * k);
-  stage_factor_warp<T>(Ls, arena + v.f_off[f], m * k);
-  T *x = xl + v.f_xoff[f] + v.f_p0[f];
-  for (int i = lane; i < m; i += 32) w[i] = i < k ? x[i] : T(0);
+  const int m = v.f_m[f], k = v.f_k[f], ld = round4(m);
+  const int64_t xo = v.f_xoff[f] + v.f_p0[f];
+  for (int i = lane; i < m; i += 32) w[i] = i < k ? xl[xo + i] : T(0);
   __syncwarp();
   for (int ci = v.f_child_ptr[f]; ci < v.f_child_ptr[f + 1]; ci++) {
     const int c = v.f_children[ci];
@@ -1012,47 +663,252 @@ mf_fwd_warp(MfView v, const int *__restrict__ fronts, int nf, const T *__restric
     for (int a = lane; a < rc; a += 32) w[rel[a]] += u[a];
     __syncwarp();
   }
-  cp_async_wait<0>();
-  __syncwarp();
-  for (int j = 0; j < k; j++) {
-    const T yj = w[j] / Ls[j * m + j];
-    __syncwarp();
-    for (int i = j + 1 + lane; i < m; i += 32) w[i] -= Ls[j * m + i] * yj;
-    if (lane == 0) w[j] = yj;
-    __syncwarp();
+  const T *Ef = E + v.e_off[f];
+  T acc[PASS][VN];
+#pragma unroll
+  for (int p = 0; p < PASS; p++)
+#pragma unroll
+    for (int q = 0; q < VN; q++) acc[p][q] = T(0);
+#pragma unroll
+  for (int p = 0; p < PASS; p++) {
+    const int r = VN * lane + 32 * VN * p;
+    if (r >= m) continue;
+    // columns in batches of kEUnroll independent loads; a vector of rows wholly
+    // above the diagonal (r + VN <= j) is zero and not loaded
+    for (int j0 = 0; j0 < k; j0 += kEUnroll) {
+      T e[kEUnroll][VN];
+#pragma unroll
+      for (int u = 0; u < kEUnroll; u++) {
+        const int j = j0 + u;
+        if (j < k && r + VN > j) Vec16<T>::load(Ef + (int64_t)j * ld + r, e[u]);
+        else {
+#pragma unroll
+          for (int q = 0; q < VN; q++) e[u][q] = T(0);
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < kEUnroll; u++) {
+        const T bj = j0 + u < k ? w[j0 + u] : T(0);
+#pragma unroll
+        for (int q = 0; q < VN; q++) acc[p][q] += e[u][q] * bj;
+      }
+    }
   }
-  for (int i = lane; i < k; i += 32) x[i] = w[i];
-  T *u = uvec + v.f_uoff[f];
-  for (int a = lane; a < m - k; a += 32) u[a] = w[k + a];
+  T *uf = uvec + v.f_uoff[f];
+#pragma unroll
+  for (int p = 0; p < PASS; p++)
+#pragma unroll
+    for (int q = 0; q < VN; q++) {
+      const int row = VN * lane + 32 * VN * p + q;
+      if (row < k) yl[xo + row] = acc[p][q];
+      else if (row < m) uf[row - k] = w[row] + acc[p][q];
+    }
 }
 
+// small fronts, backward: one warp per front
 template <typename T>
-__global__ void __launch_bounds__(256)
-mf_bwd_warp(MfView v, const int *__restrict__ fronts, int nf, const T *__restrict__ arena,
-            T *__restrict__ xl, int per_warp) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
+__global__ void __launch_bounds__(256, 4)
+mf_bwd_small(MfView v, const int *__restrict__ fronts, int nf, const T *__restrict__ E,
+             const T *__restrict__ yl, T *__restrict__ xl) {
+  constexpr int VN = Vec16<T>::N, PASS = kSolveSmall / (32 * VN);
+  __shared__ __align__(16) T wsh[8][kSolveSmall];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
   const int gw = blockIdx.x * nw + wid;
   if (gw >= nf) return;
-  T *Ls = reinterpret_cast<T *>(smem_raw) + (size_t)wid * per_warp;
+  T *w = wsh[wid];
   const int f = fronts[gw];
-  const int m = v.f_m[f], k = v.f_k[f];
-  T *w = Ls + round4(m * k);
-  stage_factor_warp<T>(Ls, arena + v.f_off[f], m * k);
-  T *xb = xl + v.f_xoff[f];
+  const int m = v.f_m[f], k = v.f_k[f], ld = round4(m);
+  const int64_t xo = v.f_xoff[f] + v.f_p0[f];
+  const T *xb = xl + v.f_xoff[f];
   const int *rows = v.rows + v.f_rows[f];
-  for (int i = lane; i < m; i += 32) w[i] = xb[rows[i]];
-  cp_async_wait<0>();
+  for (int i = lane; i < ld; i += 32) w[i] = i < k ? yl[xo + i] : (i < m ? xb[rows[i]] : T(0));
   __syncwarp();
-  for (int j = k - 1; j >= 0; j--) {
-    T sum = T(0);
-    for (int i = j + 1 + lane; i < m; i += 32) sum += Ls[j * m + i] * w[i];
+  T wr[PASS][VN];
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) sum += __shfl_down_sync(0xffffffffu, sum, o);
-    if (lane == 0) w[j] = (w[j] - sum) / Ls[j * m + j];
-    __syncwarp();
+  for (int p = 0; p < PASS; p++)
+#pragma unroll
+    for (int q = 0; q < VN; q++) {
+      const int r = VN * lane + 32 * VN * p + q;
+      wr[p][q] = r < ld ? w[r] : T(0);
+    }
+  const T *Ef = E + v.e_off[f];
+  // columns in batches of kEUnroll: the loads of a batch are issued together,
+  // then each column sum is reduced over the warp
+  for (int c0 = 0; c0 < k; c0 += kEUnroll) {
+    T s[kEUnroll];
+#pragma unroll
+    for (int u = 0; u < kEUnroll; u++) s[u] = T(0);
+#pragma unroll
+    for (int p = 0; p < PASS; p++) {
+      const int r = VN * lane + 32 * VN * p;
+      if (r >= m) continue;
+      T e[kEUnroll][VN];
+#pragma unroll
+      for (int u = 0; u < kEUnroll; u++) {
+        const int c = c0 + u;
+        if (c < k && r + VN > c) Vec16<T>::load(Ef + (int64_t)c * ld + r, e[u]);
+        else {
+#pragma unroll
+          for (int q = 0; q < VN; q++) e[u][q] = T(0);
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < kEUnroll; u++)
+#pragma unroll
+        for (int q = 0; q < VN; q++) s[u] += e[u][q] * wr[p][q];
+    }
+#pragma unroll
+    for (int u = 0; u < kEUnroll; u++) {
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) s[u] += __shfl_xor_sync(0xffffffffu, s[u], o);
+    }
+    if (lane < kEUnroll && c0 + lane < k) {
+      T out = s[0];
+#pragma unroll
+      for (int u = 1; u < kEUnroll; u++) if (lane == u) out = s[u];
+      xl[xo + c0 + lane] = out;
+    }
   }
-  for (int i = lane; i < k; i += 32) xb[rows[i]] = w[i];
+}
+
+// large fronts, forward: task = {front, (first chunk << 16) | chunk count};
+// a chunk is FwdRows<T>::N rows.  The CTA assembles the front's whole
+// right-hand side b (m entries) once, then per chunk each warp takes every
+// 8th column of E and each lane VN rows (one coalesced 512-byte row segment
+// per warp and column); the 8 warp sums are added in a fixed order.
+// Pivot-row chunks need the columns j < min(k, r0 + N) only, and a vector
+// of rows wholly above the diagonal of E is zero and not loaded.
+template <typename T> struct FwdRows { static constexpr int N = 32 * Vec16<T>::N; };
+
+template <typename T>
+__global__ void __launch_bounds__(kEThreads, 2)
+mf_fwd_big(MfView v, const int2 *__restrict__ tasks, const T *__restrict__ E, const T *__restrict__ xl,
+           T *__restrict__ yl, T *__restrict__ uvec) {
+  constexpr int VN = Vec16<T>::N, RC = FwdRows<T>::N, NW = kEThreads / 32;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T *b = reinterpret_cast<T *>(smem_raw);  // b[0, m)
+  __shared__ T red[NW][RC];
+  const int f = tasks[blockIdx.x].x;
+  const int ch0 = tasks[blockIdx.x].y >> 16, nch = tasks[blockIdx.x].y & 0xffff;
+  const int m = v.f_m[f], k = v.f_k[f], ld = round4(m);
+  const int64_t xo = v.f_xoff[f] + v.f_p0[f];
+  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+  for (int i = tid; i < m; i += kEThreads) b[i] = i < k ? xl[xo + i] : T(0);
+  __syncthreads();
+  for (int ci = v.f_child_ptr[f]; ci < v.f_child_ptr[f + 1]; ci++) {
+    const int c = v.f_children[ci];
+    const int rc = v.f_m[c] - v.f_k[c];
+    const int *rel = v.relmap + v.f_relmap[c];
+    const T *u = uvec + v.f_uoff[c];
+    for (int a = tid; a < rc; a += kEThreads) b[rel[a]] += u[a];
+    __syncthreads();
+  }
+  const T *Ef = E + v.e_off[f];
+  T *uf = uvec + v.f_uoff[f];
+  for (int ch = ch0; ch < ch0 + nch; ch++) {
+    const int r0 = ch * RC;
+    const int K = r0 < k ? min(k, r0 + RC) : k;
+    const int rb = r0 + lane * VN;
+    T acc[VN];
+#pragma unroll
+    for (int q = 0; q < VN; q++) acc[q] = T(0);
+    if (rb < m) {
+      const T *Er = Ef + rb;
+      int j = wid;
+      for (; j + (kEUnroll - 1) * NW < K; j += kEUnroll * NW) {
+        T e[kEUnroll][VN];
+#pragma unroll
+        for (int u = 0; u < kEUnroll; u++) {
+          if (rb + VN > j + u * NW) Vec16<T>::load(Er + (int64_t)(j + u * NW) * ld, e[u]);
+          else {
+#pragma unroll
+            for (int q = 0; q < VN; q++) e[u][q] = T(0);
+          }
+        }
+#pragma unroll
+        for (int u = 0; u < kEUnroll; u++) {
+          const T bj = b[j + u * NW];
+#pragma unroll
+          for (int q = 0; q < VN; q++) acc[q] += e[u][q] * bj;
+        }
+      }
+      for (; j < K; j += NW) {
+        if (rb + VN > j) {
+          T e[VN];
+          Vec16<T>::load(Er + (int64_t)j * ld, e);
+          const T bj = b[j];
+#pragma unroll
+          for (int q = 0; q < VN; q++) acc[q] += e[q] * bj;
+        }
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < VN; q++) red[wid][lane * VN + q] = acc[q];
+    __syncthreads();
+    for (int t = tid; t < RC; t += kEThreads) {
+      T s = T(0);
+#pragma unroll
+      for (int w = 0; w < NW; w++) s += red[w][t];
+      const int row = r0 + t;
+      if (row < k) yl[xo + row] = s;
+      else if (row < m) uf[row - k] = b[row] + s;
+    }
+    __syncthreads();
+  }
+}
+
+// large fronts, backward: task = {front, column block J}; x[32J .. 32J+31] from
+// rows [32J, m) of E
+template <typename T>
+__global__ void __launch_bounds__(kEThreads, 2)
+mf_bwd_big(MfView v, const int2 *__restrict__ tasks, const T *__restrict__ E, const T *__restrict__ yl,
+           T *__restrict__ xl) {
+  constexpr int VN = Vec16<T>::N, LPC = 32 / VN, NCS = kEThreads / LPC;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T *w = reinterpret_cast<T *>(smem_raw);  // v[32J, ld)
+  const int f = tasks[blockIdx.x].x, J = tasks[blockIdx.x].y;
+  const int m = v.f_m[f], k = v.f_k[f], ld = round4(m);
+  const int c0 = 32 * J, jb = min(32, k - c0);
+  const int64_t xo = v.f_xoff[f] + v.f_p0[f];
+  const T *xb = xl + v.f_xoff[f];
+  const int *rows = v.rows + v.f_rows[f];
+  const int tid = threadIdx.x;
+  for (int i = c0 + tid; i < ld; i += kEThreads) w[i - c0] = i < k ? yl[xo + i] : (i < m ? xb[rows[i]] : T(0));
+  __syncthreads();
+  const int rq = tid % LPC, cs = tid / LPC;
+  for (int cc = cs; cc < 32; cc += NCS) {  // uniform trip count: the shuffles below need whole groups
+    const int c = c0 + cc;
+    T s = T(0);
+    if (cc < jb) {
+      const T *Ec = E + v.e_off[f] + (int64_t)c * ld;
+      int i = c0 + rq * VN;
+      for (; i + (kEUnroll - 1) * 32 < m; i += kEUnroll * 32) {
+        T e[kEUnroll][VN];
+#pragma unroll
+        for (int u = 0; u < kEUnroll; u++) {
+          if (i + u * 32 + VN > c) Vec16<T>::load(Ec + i + u * 32, e[u]);
+          else {
+#pragma unroll
+            for (int q = 0; q < VN; q++) e[u][q] = T(0);
+          }
+        }
+#pragma unroll
+        for (int u = 0; u < kEUnroll; u++)
+#pragma unroll
+          for (int q = 0; q < VN; q++) s += e[u][q] * w[i + u * 32 + q - c0];
+      }
+      for (; i < m; i += 32) {
+        if (i + VN <= c) continue;
+        T e[VN];
+        Vec16<T>::load(Ec + i, e);
+#pragma unroll
+        for (int q = 0; q < VN; q++) s += e[q] * w[i + q - c0];
+      }
+    }
+#pragma unroll
+    for (int o = LPC / 2; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (rq == 0 && cc < jb) xl[xo + c] = s;
+  }
 }
 
 // ---------------------------------------------------------------------------

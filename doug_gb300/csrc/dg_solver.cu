@@ -63,31 +63,33 @@ static double wall() {
 
 // one multifrontal batch on the device, factor precision T
 constexpr int kLargeFront = 256;      // fronts above this size use the multi-CTA pipeline
-constexpr int kMaxSolveSmem = 200 * 1024;
-constexpr int kSolveLarge = 128;      // fronts above this size use the packed, pipelined solves
+constexpr int64_t kFwdTaskBytes = 96 * 1024;  // E bytes per forward task of a large front
 
 template <typename T>
 struct MfDevice {
-  DBuf<int64_t> f_off, f_rows, f_xoff, f_uoff, f_woff, f_relmap, f_asm, asm_tgt, asm_sp, asm_src;
+  DBuf<int64_t> f_off, f_rows, f_xoff, f_uoff, f_woff, f_relmap, f_asm, asm_tgt, asm_sp, asm_src, e_off;
   DBuf<int> f_m, f_k, f_p0, f_child_ptr, f_children, rows, relmap, lvl_fronts, gidx;
-  DBuf<int> small_fronts, tiny_fronts, diag_fronts;
-  DBuf<int2> asm_tasks, upd_tasks, panel_tasks;
-  DBuf<T> arena, xl, u, w, packed;
-  DBuf<int> blk_front, blk_j, f_blk, f_C, solve_small, solve_large;
-  DBuf<int64_t> blk_off;
-  int nblk = 0;
+  DBuf<int> small_fronts, tiny_fronts, diag_fronts, solve_small;
+  DBuf<int2> asm_tasks, upd_tasks, panel_tasks, esc_tasks, etile_tasks, fwd_tasks, bwd_tasks;
+  DBuf<T> arena, E, xl, yl, u;
+  int64_t e_len = 0;
+  // per level: small-front range, assembly-task range, steps
+  struct Step {
+    int j0, diag_off, diag_cnt, panel_off, panel_cnt, esc_off, esc_cnt;
+    int upd_off, upd_cnt, etile_off, etile_cnt;
+  };
+  struct Level {
+    int tiny_off, tiny_cnt, small_off, small_cnt, asm_off, asm_cnt;
+    size_t tiny_smem;
+    std::vector<Step> steps;
+  };
+  std::vector<Level> levels;
+  // per level: solve work lists
   struct SolveLevel {
-    int small_off, small_cnt, large_off, large_cnt;
-    int per_warp, warps, C;
-    size_t warp_smem, tile_smem;
+    int small_off, small_cnt, fwd_off, fwd_cnt, bwd_off, bwd_cnt;
+    size_t fwd_smem, bwd_smem;
   };
   std::vector<SolveLevel> slevels;
-  PackView pview{};
-  std::vector<int> lvl_ptr, lvl_max_m;
-  // per level: small-front range, assembly-task range, steps
-  struct Step { int j0, diag_off, diag_cnt, panel_off, panel_cnt; int64_t upd_off, upd_cnt; };
-  struct Level { int tiny_off, tiny_cnt, tiny_maxm, small_off, small_cnt, asm_off, asm_cnt; std::vector<Step> steps; };
-  std::vector<Level> levels;
   int nlevels = 0, nfronts = 0;
   int64_t xlen = 0;
   MfView view{};
@@ -101,37 +103,53 @@ struct MfDevice {
     f_child_ptr.upload(B.f_child_ptr); f_children.upload(B.f_children);
     rows.upload(B.rows); relmap.upload(B.relmap); lvl_fronts.upload(B.lvl_fronts);
     gidx.upload(B.gidx);
-    arena.alloc((size_t)B.arena);
-    xl.alloc((size_t)B.xlen);
-    u.alloc((size_t)std::max<int64_t>(B.ulen, 1));
-    w.alloc((size_t)std::max<int64_t>(B.wlen, 1));
-    lvl_ptr = B.lvl_ptr;
-    lvl_max_m = B.lvl_max_m;
     nlevels = B.nlevels;
     nfronts = B.nfronts;
     xlen = B.xlen;
+    // elimination matrices: m x k per front, ld = round4(m); the padding rows
+    // are zero once and never written again
+    std::vector<int64_t> eo((size_t)nfronts);
+    e_len = 0;
+    for (int f = 0; f < nfronts; f++) {
+      eo[(size_t)f] = e_len;
+      e_len += (int64_t)round4(B.f_m[(size_t)f]) * B.f_k[(size_t)f];
+    }
+    e_off.upload(eo);
+    E.alloc((size_t)std::max<int64_t>(e_len, 4));
+    CK(cudaMemset(E.p, 0, (size_t)std::max<int64_t>(e_len, 4) * sizeof(T)));
+    arena.alloc((size_t)B.arena);
+    xl.alloc((size_t)B.xlen);
+    yl.alloc((size_t)B.xlen);
+    u.alloc((size_t)std::max<int64_t>(B.ulen, 1));
     view = MfView{f_off.p, f_m.p, f_k.p, f_rows.p, f_xoff.p, f_p0.p, f_uoff.p, f_woff.p,
                   f_child_ptr.p, f_children.p, f_relmap.p, f_asm.p, rows.p, relmap.p,
-                  asm_tgt.p, asm_sp.p, asm_src.p};
+                  asm_tgt.p, asm_sp.p, asm_src.p, e_off.p};
+    int dev = 0, optin = 0;
+    CK(cudaGetDevice(&dev));
+    CK(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
     // work lists of the factorisation
     std::vector<int> sm, ty, df;
-    std::vector<int2> at, ut, pf;
-    const int tiny_max = sizeof(T) == 8 ? 112 : 160;  // front fits in ~100 KB of shared memory
+    std::vector<int2> at, ut, pf, es, et;
+    const int tiny_max = sizeof(T) == 8 ? 112 : 160;  // front + E fit in shared memory
+    size_t tiny_smem_max = 0;
     levels.assign((size_t)nlevels, Level());
     for (int l = 0; l < nlevels; l++) {
       Level &L = levels[(size_t)l];
       L.small_off = (int)sm.size();
       L.tiny_off = (int)ty.size();
-      L.tiny_maxm = 0;
+      L.tiny_smem = 0;
       L.asm_off = (int)at.size();
       std::vector<int> large;
       for (int q = B.lvl_ptr[(size_t)l]; q < B.lvl_ptr[(size_t)l + 1]; q++) {
         int f = B.lvl_fronts[(size_t)q];
-        int m = B.f_m[(size_t)f];
+        int m = B.f_m[(size_t)f], k = B.f_k[(size_t)f];
         if (m > kLargeFront) large.push_back(f);
-        else if (m <= tiny_max) { ty.push_back(f); L.tiny_maxm = std::max(L.tiny_maxm, m); }
-        else sm.push_back(f);
+        else if (m <= tiny_max) {
+          ty.push_back(f);
+          L.tiny_smem = std::max(L.tiny_smem, (size_t)(m * m + m * k) * sizeof(T));
+        } else sm.push_back(f);
       }
+      tiny_smem_max = std::max(tiny_smem_max, L.tiny_smem);
       L.small_cnt = (int)sm.size() - L.small_off;
       L.tiny_cnt = (int)ty.size() - L.tiny_off;
       int kmax = 0;
@@ -142,162 +160,100 @@ struct MfDevice {
       }
       L.asm_cnt = (int)at.size() - L.asm_off;
       for (int j0 = 0; j0 < kmax; j0 += kNB) {
-        Step st{j0, (int)df.size(), 0, (int)pf.size(), 0, (int64_t)ut.size(), 0};
+        Step st{j0, (int)df.size(), 0, (int)pf.size(), 0, (int)es.size(), 0,
+                (int)ut.size(), 0, (int)et.size(), 0};
         for (int f : large) {
           int m = B.f_m[(size_t)f], k = B.f_k[(size_t)f];
           if (j0 >= k) continue;
           df.push_back(f);
-          for (int r0 = j0 + std::min(kNB, k - j0); r0 < m; r0 += kPanelRows) pf.push_back(make_int2(f, r0));
-          int c0 = j0 + std::min(kNB, k - j0);
+          const int c0 = j0 + std::min(kNB, k - j0);
+          for (int r0 = c0; r0 < m; r0 += kPanelRows) pf.push_back(make_int2(f, r0));
+          for (int e0 = 0; e0 < c0; e0 += EscCols<T>::N) es.push_back(make_int2(f, e0));
           int nt = (m - c0 + kTile - 1) / kTile;
           for (int tj = 0; tj < nt; tj++)
             for (int ti = tj; ti < nt; ti++) ut.push_back(make_int2(f, (ti << 16) | tj));
+          int ntc = (c0 + kTile - 1) / kTile;
+          for (int ti = 0; ti < nt; ti++)
+            for (int tc = 0; tc < ntc; tc++) et.push_back(make_int2(f, (ti << 16) | tc));
         }
         st.diag_cnt = (int)df.size() - st.diag_off;
         st.panel_cnt = (int)pf.size() - st.panel_off;
-        st.upd_cnt = (int64_t)ut.size() - st.upd_off;
+        st.esc_cnt = (int)es.size() - st.esc_off;
+        st.upd_cnt = (int)ut.size() - st.upd_off;
+        st.etile_cnt = (int)et.size() - st.etile_off;
         L.steps.push_back(st);
       }
     }
     small_fronts.upload(sm);
     tiny_fronts.upload(ty);
-    CK(cudaFuncSetAttribute(mf_factor_small<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 110 * 1024));
+    // kernel attributes are per function, shared by every batch of this
+    // precision: always the device maximum, never a batch's own size
+    if (tiny_smem_max > (size_t)optin) throw CudaError{cudaErrorInvalidValue, "front too large for shared memory"};
+    CK(cudaFuncSetAttribute(mf_factor_small<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
     panel_tasks.upload(pf);
+    esc_tasks.upload(es);
     diag_fronts.upload(df);
     asm_tasks.upload(at);
     upd_tasks.upload(ut);
-    CK(cudaFuncSetAttribute(mf_fwd_level<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxSolveSmem));
-    CK(cudaFuncSetAttribute(mf_bwd_level<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxSolveSmem));
-    // tiled solve layout for the fronts above kSolveLarge rows
-    {
-      std::vector<int> bf, bj, fblk((size_t)nfronts, -1), ss, sl;
-      std::vector<int64_t> bo;
-      int64_t len = 0;
-      for (int f = 0; f < nfronts; f++) {
+    etile_tasks.upload(et);
+    // solve work lists: warp kernels for the small fronts; one task per 32-row
+    // block (forward) and per 32-column block (backward) of the others, the
+    // longest first
+    std::vector<int> ss;
+    std::vector<int2> fw, bw;
+    size_t fwd_smem_max = 0, bwd_smem_max = 0;
+    slevels.assign((size_t)nlevels, SolveLevel());
+    for (int l = 0; l < nlevels; l++) {
+      SolveLevel &L = slevels[(size_t)l];
+      L.small_off = (int)ss.size();
+      L.fwd_off = (int)fw.size();
+      L.bwd_off = (int)bw.size();
+      L.fwd_smem = L.bwd_smem = 0;
+      std::vector<std::pair<int, int2>> fl, bl;
+      for (int q = B.lvl_ptr[(size_t)l]; q < B.lvl_ptr[(size_t)l + 1]; q++) {
+        int f = B.lvl_fronts[(size_t)q];
         int m = B.f_m[(size_t)f], k = B.f_k[(size_t)f];
-        if (m <= kSolveLarge) continue;
-        fblk[(size_t)f] = (int)bf.size();
-        const int nR = (m + 31) / 32;
-        for (int J = 0; 32 * J < k; J++) {
-          bf.push_back(f);
-          bj.push_back(J);
-          bo.push_back(len);
-          len += 1024 * (int64_t)(1 + nR - J);
+        if (m <= kSolveSmall) { ss.push_back(f); continue; }
+        // forward tasks: runs of row chunks of at least kFwdTaskBytes of E each
+        const int RC = FwdRows<T>::N, nch = (m + RC - 1) / RC;
+        for (int c = 0; c < nch;) {
+          int c1 = c;
+          int64_t bytes = 0;
+          do {
+            const int r0 = c1 * RC, K = r0 < k ? std::min(k, r0 + RC) : k;
+            bytes += (int64_t)RC * K * (int64_t)sizeof(T);
+            c1++;
+          } while (c1 < nch && bytes < kFwdTaskBytes);
+          fl.push_back({(int)std::min<int64_t>(bytes, 1 << 30), make_int2(f, (c << 16) | (c1 - c))});
+          c = c1;
         }
+        for (int J = 0; 32 * J < k; J++) bl.push_back({m - 32 * J, make_int2(f, J)});
+        L.fwd_smem = std::max(L.fwd_smem, (size_t)round4(m) * sizeof(T));
+        L.bwd_smem = std::max(L.bwd_smem, (size_t)round4(m) * sizeof(T));
       }
-      nblk = (int)bf.size();
-      blk_front.upload(bf); blk_j.upload(bj); f_blk.upload(fblk); blk_off.upload(bo);
-      packed.alloc((size_t)std::max<int64_t>(len, 1));
-      std::vector<int> fc((size_t)nfronts, 1);  // cluster size per front, set per level below
-      int dev = 0, optin = 0, nsm = 0;
-      CK(cudaGetDevice(&dev));
-      CK(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
-      CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
-      max_cluster_ = 8;
-      if (sizeof(T) == 8) {  // can 16-CTA clusters of the FP64 tile kernels be scheduled?
-        cudaError_t e1 = cudaFuncSetAttribute(mf_fwd_tiles<T, 16>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
-        cudaError_t e2 = cudaFuncSetAttribute(mf_bwd_tiles<T, 16>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
-        if (e1 == cudaSuccess && e2 == cudaSuccess) {
-          cudaLaunchConfig_t cfg{};
-          cfg.gridDim = dim3(16);
-          cfg.blockDim = dim3(kTileThreads);
-          cfg.dynamicSmemBytes = (size_t)TilePipe<T>::S * TilePipe<T>::G * 1024 * sizeof(T) + 8 * 1024;
-          cudaLaunchAttribute attr[1];
-          attr[0].id = cudaLaunchAttributeClusterDimension;
-          attr[0].val.clusterDim.x = 16;
-          attr[0].val.clusterDim.y = 1;
-          attr[0].val.clusterDim.z = 1;
-          cfg.attrs = attr;
-          cfg.numAttrs = 1;
-          int nclusters = 0;
-          set_tile_attrs<16>(optin);
-          if (cudaOccupancyMaxActiveClusters(&nclusters, mf_fwd_tiles<T, 16>, &cfg) == cudaSuccess && nclusters > 0)
-            max_cluster_ = 16;
-        }
-        cudaGetLastError();  // a refused attribute only means: stay at 8
-      }
-      slevels.assign((size_t)nlevels, SolveLevel());
-      for (int l = 0; l < nlevels; l++) {
-        SolveLevel &L = slevels[(size_t)l];
-        L.small_off = (int)ss.size();
-        L.large_off = (int)sl.size();
-        int per_warp = 0, maxnR = 0;
-        for (int q = B.lvl_ptr[(size_t)l]; q < B.lvl_ptr[(size_t)l + 1]; q++) {
-          int f = B.lvl_fronts[(size_t)q];
-          int m = B.f_m[(size_t)f], k = B.f_k[(size_t)f];
-          if (m > kSolveLarge) { sl.push_back(f); maxnR = std::max(maxnR, (m + 31) / 32); }
-          else { ss.push_back(f); per_warp = std::max(per_warp, round4(m * k) + round4(m)); }
-        }
-        L.small_cnt = (int)ss.size() - L.small_off;
-        L.large_cnt = (int)sl.size() - L.large_off;
-        L.per_warp = per_warp;
-        L.warps = std::max(1, std::min(8, (int)((96 * 1024) / std::max<size_t>(1, (size_t)per_warp * sizeof(T)))));
-        L.warp_smem = (size_t)L.warps * per_warp * sizeof(T);
-        if (L.small_cnt && L.warp_smem > (size_t)optin)
-          throw CudaError{cudaErrorInvalidValue, "small front too large for the warp solve"};
-        // cluster size: enough CTAs for the machine, at most the row blocks;
-        // FP64 fronts (FP64 pipe bound) may use 16-CTA clusters where the
-        // device can schedule them
-        int C = 1;
-        const int cmax = sizeof(T) == 8 ? max_cluster_ : 8;
-        while (C < cmax && L.large_cnt * C < 2 * nsm && C * 2 <= maxnR) C *= 2;
-        L.C = C;
-        for (int qq = L.large_off; qq < (int)sl.size(); qq++) fc[(size_t)sl[(size_t)qq]] = C;
-        L.tile_smem = (size_t)TilePipe<T>::S * TilePipe<T>::G * 1024 * sizeof(T) +
-                      (size_t)((maxnR + C - 1) / C) * 32 * sizeof(T);
-        if (L.large_cnt && L.tile_smem > (size_t)optin - 1024)
-          throw CudaError{cudaErrorInvalidValue, "front too large for the shared-memory solve"};
-      }
-      solve_small.upload(ss);
-      solve_large.upload(sl);
-      f_C.upload(fc);
-      pview = PackView{blk_front.p, blk_j.p, f_blk.p, blk_off.p, f_C.p};
-      CK(cudaFuncSetAttribute(mf_fwd_warp<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
-      CK(cudaFuncSetAttribute(mf_bwd_warp<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
-      set_tile_attrs<1>(optin);
-      set_tile_attrs<2>(optin);
-      set_tile_attrs<4>(optin);
-      set_tile_attrs<8>(optin);
-      set_tile_attrs<16>(optin);
+      std::stable_sort(fl.begin(), fl.end(), [](const std::pair<int, int2> &a, const std::pair<int, int2> &b) { return a.first > b.first; });
+      std::stable_sort(bl.begin(), bl.end(), [](const std::pair<int, int2> &a, const std::pair<int, int2> &b) { return a.first > b.first; });
+      for (auto &e : fl) fw.push_back(e.second);
+      for (auto &e : bl) bw.push_back(e.second);
+      L.small_cnt = (int)ss.size() - L.small_off;
+      L.fwd_cnt = (int)fw.size() - L.fwd_off;
+      L.bwd_cnt = (int)bw.size() - L.bwd_off;
+      fwd_smem_max = std::max(fwd_smem_max, L.fwd_smem);
+      bwd_smem_max = std::max(bwd_smem_max, L.bwd_smem);
     }
-  }
-  int max_cluster_ = 8;
-
-  template <int C>
-  void set_tile_attrs(int optin) {
-    cudaFuncAttributes fa{}, fb{};
-    CK(cudaFuncGetAttributes(&fa, mf_fwd_tiles<T, C>));
-    CK(cudaFuncGetAttributes(&fb, mf_bwd_tiles<T, C>));
-    const int dyn = optin - (int)std::max(fa.sharedSizeBytes, fb.sharedSizeBytes);
-    CK(cudaFuncSetAttribute(mf_fwd_tiles<T, C>, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn));
-    CK(cudaFuncSetAttribute(mf_bwd_tiles<T, C>, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn));
-  }
-
-  template <int C>
-  void launch_tiles(bool fwd, int nfr, const int *fr, size_t smem, cudaStream_t s) {
-    cudaLaunchConfig_t cfg{};
-    cfg.gridDim = dim3((unsigned)(nfr * C));
-    cfg.blockDim = dim3(kTileThreads);
-    cfg.dynamicSmemBytes = smem;
-    cfg.stream = s;
-    cudaLaunchAttribute attr[1];
-    attr[0].id = cudaLaunchAttributeClusterDimension;
-    attr[0].val.clusterDim.x = C;
-    attr[0].val.clusterDim.y = 1;
-    attr[0].val.clusterDim.z = 1;
-    cfg.attrs = attr;
-    cfg.numAttrs = 1;
-    if (fwd) CK(cudaLaunchKernelEx(&cfg, mf_fwd_tiles<T, C>, view, pview, fr, (const T *)packed.p, xl.p, u.p));
-    else CK(cudaLaunchKernelEx(&cfg, mf_bwd_tiles<T, C>, view, pview, fr, (const T *)packed.p, xl.p));
-  }
-
-  void tiles_any(int C, bool fwd, int nfr, const int *fr, size_t smem, cudaStream_t s) {
-    switch (C) {
-      case 1: launch_tiles<1>(fwd, nfr, fr, smem, s); break;
-      case 2: launch_tiles<2>(fwd, nfr, fr, smem, s); break;
-      case 4: launch_tiles<4>(fwd, nfr, fr, smem, s); break;
-      case 8: launch_tiles<8>(fwd, nfr, fr, smem, s); break;
-      default: launch_tiles<16>(fwd, nfr, fr, smem, s); break;
+    solve_small.upload(ss);
+    fwd_tasks.upload(fw);
+    bwd_tasks.upload(bw);
+    {
+      cudaFuncAttributes fa{}, fb{};
+      CK(cudaFuncGetAttributes(&fa, mf_fwd_big<T>));
+      CK(cudaFuncGetAttributes(&fb, mf_bwd_big<T>));
+      if (fwd_smem_max + fa.sharedSizeBytes > (size_t)optin || bwd_smem_max + fb.sharedSizeBytes > (size_t)optin)
+        throw CudaError{cudaErrorInvalidValue, "front too large for the shared-memory solve"};
+      CK(cudaFuncSetAttribute(mf_fwd_big<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              optin - (int)fa.sharedSizeBytes));
+      CK(cudaFuncSetAttribute(mf_bwd_big<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              optin - (int)fb.sharedSizeBytes));
     }
   }
 
@@ -306,14 +262,13 @@ struct MfDevice {
     for (int l = 0; l < nlevels; l++) {
       const Level &L = levels[(size_t)l];
       if (L.tiny_cnt) {
-        size_t smem = (size_t)L.tiny_maxm * L.tiny_maxm * sizeof(T);
-        mf_factor_small<T><<<L.tiny_cnt, kSmallThreads, smem, s>>>(view, tiny_fronts.p + L.tiny_off, vals,
-                                                                  arena.p, status);
+        mf_factor_small<T><<<L.tiny_cnt, kSmallThreads, L.tiny_smem, s>>>(view, tiny_fronts.p + L.tiny_off, vals,
+                                                                         arena.p, E.p, status);
         launches++;
       }
       if (L.small_cnt) {
         mf_factor_level<T><<<L.small_cnt, kMfThreads, 0, s>>>(view, small_fronts.p + L.small_off, vals,
-                                                              arena.p, status);
+                                                              arena.p, E.p, status);
         launches++;
       }
       if (L.asm_cnt) {
@@ -323,50 +278,45 @@ struct MfDevice {
       for (const Step &st : L.steps) {
         mf_diag<T><<<st.diag_cnt, kMfThreads, 0, s>>>(view, diag_fronts.p + st.diag_off, st.j0, arena.p, status);
         launches++;
-        if (st.panel_cnt) {
-          mf_panel<T><<<st.panel_cnt, kMfThreads, 0, s>>>(view, panel_tasks.p + st.panel_off, st.j0, arena.p);
+        if (st.panel_cnt + st.esc_cnt) {
+          mf_panel<T><<<st.panel_cnt + st.esc_cnt, kMfThreads, 0, s>>>(
+              view, panel_tasks.p + st.panel_off, st.panel_cnt, esc_tasks.p + st.esc_off, st.j0, arena.p, E.p);
           launches++;
         }
-        for (int64_t o = 0; o < st.upd_cnt; o += 1 << 30) {
-          int cnt = (int)std::min<int64_t>(st.upd_cnt - o, 1 << 30);
-          if (!cnt) continue;
-          mf_update<T><<<cnt, kMfThreads, 0, s>>>(view, upd_tasks.p + st.upd_off + o, st.j0, arena.p);
+        if (st.upd_cnt + st.etile_cnt) {
+          mf_update<T><<<st.upd_cnt + st.etile_cnt, kMfThreads, 0, s>>>(
+              view, upd_tasks.p + st.upd_off, st.upd_cnt, etile_tasks.p + st.etile_off, st.j0, arena.p, E.p);
           launches++;
         }
       }
-    }
-    if (nblk) {  // packed solve layout of the large fronts
-      mf_pack<T><<<nblk, 256, 0, s>>>(view, pview, arena.p, packed.p);
-      launches++;
     }
     return launches;
   }
 
-  int solve(cudaStream_t s) {  // in place on xl
+  // forward + backward solve: right-hand side in xl, solution back in xl
+  int solve(cudaStream_t s) {
     int launches = 0;
     for (int l = 0; l < nlevels; l++) {
       const SolveLevel &L = slevels[(size_t)l];
       if (L.small_cnt) {
-        int blocks = (L.small_cnt + L.warps - 1) / L.warps;
-        mf_fwd_warp<T><<<blocks, 32 * L.warps, L.warp_smem, s>>>(view, solve_small.p + L.small_off, L.small_cnt,
-                                                                  arena.p, xl.p, u.p, L.per_warp);
+        mf_fwd_small<T><<<(L.small_cnt + 7) / 8, 256, 0, s>>>(view, solve_small.p + L.small_off, L.small_cnt,
+                                                              E.p, xl.p, yl.p, u.p);
         launches++;
       }
-      if (L.large_cnt) {
-        tiles_any(L.C, true, L.large_cnt, solve_large.p + L.large_off, L.tile_smem, s);
+      if (L.fwd_cnt) {
+        mf_fwd_big<T><<<L.fwd_cnt, kEThreads, L.fwd_smem, s>>>(view, fwd_tasks.p + L.fwd_off, E.p, xl.p, yl.p, u.p);
         launches++;
       }
     }
     for (int l = nlevels - 1; l >= 0; l--) {
       const SolveLevel &L = slevels[(size_t)l];
-      if (L.large_cnt) {
-        tiles_any(L.C, false, L.large_cnt, solve_large.p + L.large_off, L.tile_smem, s);
+      if (L.bwd_cnt) {
+        mf_bwd_big<T><<<L.bwd_cnt, kEThreads, L.bwd_smem, s>>>(view, bwd_tasks.p + L.bwd_off, E.p, yl.p, xl.p);
         launches++;
       }
       if (L.small_cnt) {
-        int blocks = (L.small_cnt + L.warps - 1) / L.warps;
-        mf_bwd_warp<T><<<blocks, 32 * L.warps, L.warp_smem, s>>>(view, solve_small.p + L.small_off, L.small_cnt,
-                                                                  arena.p, xl.p, L.per_warp);
+        mf_bwd_small<T><<<(L.small_cnt + 7) / 8, 256, 0, s>>>(view, solve_small.p + L.small_off, L.small_cnt,
+                                                              E.p, yl.p, xl.p);
         launches++;
       }
     }
