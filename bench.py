@@ -40,7 +40,7 @@ PARTS_PER_DIM = 4
 SEED = 0
 TOL = "1.0e-8"
 CTL = dict(solver=2, method=1, fine_method=1, levels=2, overlap=2, smoothers=1,
-           strong1="0.08", radius1=3, maxasize1=125, solve_tolerance=TOL, solve_maxiters=2000)
+           strong1="0.08", radius1=4, maxasize1=200, solve_tolerance=TOL, solve_maxiters=2000)
 METRIC = "time to rel. residual 1e-8 (s), mixed+batched vs plain FP64 PCG, 1 GB300"
 WORKLOAD = ("128^3 log-normal diffusion (sigma 1, corr. length 8), 7-point FV, 2,097,152 unknowns; "
             "PCG + 2-level additive Schwarz: 64 subdomains (4x4x4 boxes), overlap 2, "
@@ -306,7 +306,7 @@ def run_gpu(args, rank, world):
     # (multifrontal forward + backward over all levels), HBM-bound
     per_solve_s = prof.t_subsolve_s / max(prof.iterations, 1)
     achieved = prof.subsolve_bytes / per_solve_s / 1e9 if per_solve_s > 0 else None
-    roofline = {"kernel": "mf_fwd_tiles+mf_bwd_tiles+mf_fwd_warp+mf_bwd_warp (FP32 subdomain solves, all levels)",
+    roofline = {"kernel": "mf_fwd_small+mf_fwd_big+mf_bwd_big+mf_bwd_small (FP32 subdomain solves, all levels)",
                 "bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                 "frac": (achieved / hbm) if achieved else None, "traffic": None,
                 "peak_source": f"{peak_kind} hbm_gbs",

@@ -104,31 +104,43 @@ constexpr int kTile = 64;    // trailing-update tile (64 x 64 per CTA step, 4x4 
 // once E is formed; the update (Schur complement) block stays in the arena
 // for the parent's extend-add.
 
-// one CTA per front of a level (fronts of up to a few hundred rows)
+// Fronts whose pivot panel (m x k) and E (m x k) fit in shared memory: one
+// CTA per front.  The pivot columns are assembled straight into shared
+// memory, the update block in the arena; the panel is factored and E formed
+// in shared memory, E is written out, and the update block receives
+// -L21 L21^T in 4x4 register blocks.
+constexpr int kPanThreads = 128;
+
 template <typename T>
-__global__ void __launch_bounds__(kMfThreads)
-mf_factor_level(MfView v, const int *__restrict__ fronts, const double *__restrict__ vals,
+__global__ void __launch_bounds__(kPanThreads)
+mf_factor_panel(MfView v, const int *__restrict__ fronts, const double *__restrict__ vals,
                 T *__restrict__ arena, T *__restrict__ E, int *__restrict__ status) {
-  __shared__ T As[kNB][kTile];
-  __shared__ T Bs[kNB][kTile + 1];
+  extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ T piv;
   const int f = fronts[blockIdx.x];
-  const int m = v.f_m[f], k = v.f_k[f], ld = round4(m);
-  T *F = arena + v.f_off[f];
-  T *Eg = E + v.e_off[f];
-  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5, nw = kMfThreads / 32;
-  const int tx = tid & 15, ty = tid >> 4;
-  // 1. zero the lower triangle; E = [I ; 0]
-  for (int c = wid; c < m; c += nw)
-    for (int i = c + lane; i < m; i += 32) F[(int64_t)c * m + i] = T(0);
-  for (int c = wid; c < k; c += nw)
-    for (int i = lane; i < ld; i += 32) Eg[(int64_t)c * ld + i] = i == c ? T(1) : T(0);
+  const int m = v.f_m[f], k = v.f_k[f], r = m - k;
+  T *P = reinterpret_cast<T *>(smem_raw);  // m x k pivot columns, ld m
+  T *Es = P + m * k;                         // m x k elimination matrix, ld m
+  const int64_t off = v.f_off[f];
+  T *F = arena + off;
+  const int tid = threadIdx.x, nt = kPanThreads;
+  // 1. zero: panel and E = [I ; 0] in shared memory, update block in the arena
+  for (int q = tid; q < m * k; q += nt) {
+    P[q] = T(0);
+    Es[q] = q / m == q % m ? T(1) : T(0);
+  }
+  for (int q = tid; q < r * r; q += nt) {
+    const int c = q / r, i = q % r;
+    if (i >= c) F[(int64_t)(k + c) * m + k + i] = T(0);
+  }
   __syncthreads();
-  // 2. original entries (each target appears once; duplicates summed in order)
-  for (int64_t e = v.f_asm[f] + tid; e < v.f_asm[f + 1]; e += kMfThreads) {
-    double s = 0.0;
-    for (int64_t q = v.asm_sp[e]; q < v.asm_sp[e + 1]; q++) s += vals[v.asm_src[q]];
-    arena[v.asm_tgt[e]] = (T)s;
+  // 2. original entries (each target once, duplicates summed in order)
+  for (int64_t e = v.f_asm[f] + tid; e < v.f_asm[f + 1]; e += nt) {
+    double sv = 0.0;
+    for (int64_t q = v.asm_sp[e]; q < v.asm_sp[e + 1]; q++) sv += vals[v.asm_src[q]];
+    const int64_t t = v.asm_tgt[e] - off;
+    if (t < (int64_t)m * k) P[t] = (T)sv;
+    else F[t] = (T)sv;
   }
   __syncthreads();
   // 3. extend-add of the children's update matrices, children in order
@@ -137,212 +149,79 @@ mf_factor_level(MfView v, const int *__restrict__ fronts, const double *__restri
     const int mc = v.f_m[c], kc = v.f_k[c], rc = mc - kc;
     const T *U = arena + v.f_off[c] + (int64_t)kc * mc + kc;
     const int *rel = v.relmap + v.f_relmap[c];
-    for (int b = wid; b < rc; b += nw) {
-      const int pb = rel[b];
-      for (int a = b + lane; a < rc; a += 32) F[(int64_t)pb * m + rel[a]] += U[(int64_t)b * mc + a];
-    }
-    __syncthreads();
-  }
-  // 4. partial Cholesky of the k pivot columns; the trailing (m-k) block
-  //    becomes the update (Schur complement) matrix
-  for (int j0 = 0; j0 < k; j0 += kNB) {
-    const int jb = min(kNB, k - j0);
-    for (int j = j0; j < j0 + jb; j++) {
-      if (tid == 0) {
-        T d = F[(int64_t)j * m + j];
-        if (!(d > T(0))) { atomicOr(status, ERR_NOT_SPD); d = T(1); }
-        piv = tsqrt<T>(d);
-        F[(int64_t)j * m + j] = piv;
-      }
-      __syncthreads();
-      const T p = piv;
-      for (int i = j + 1 + tid; i < m; i += kMfThreads) F[(int64_t)j * m + i] /= p;
-      __syncthreads();
-      // remaining columns of the panel
-      for (int c = j + 1 + wid; c < j0 + jb; c += nw) {
-        const T lcj = F[(int64_t)j * m + c];
-        for (int i = c + lane; i < m; i += 32) F[(int64_t)c * m + i] -= F[(int64_t)j * m + i] * lcj;
-      }
-      __syncthreads();
-    }
-    const int c0 = j0 + jb;
-    // E rows of the panel: E_J <- L_JJ^-1 E_J on columns [0, c0), one thread per column
-    for (int c = tid; c < c0; c += kMfThreads) {
-      T e[kNB];
-#pragma unroll
-      for (int t = 0; t < kNB; t++) e[t] = t < jb ? Eg[(int64_t)c * ld + j0 + t] : T(0);
-#pragma unroll
-      for (int t = 0; t < kNB; t++) {
-        if (t < jb) {
-          T s = e[t];
-#pragma unroll
-          for (int q = 0; q < t; q++) s -= F[(int64_t)(j0 + q) * m + j0 + t] * e[q];
-          e[t] = s / F[(int64_t)(j0 + t) * m + j0 + t];
-        }
-      }
-#pragma unroll
-      for (int t = 0; t < kNB; t++)
-        if (t < jb) Eg[(int64_t)c * ld + j0 + t] = e[t];
-    }
-    __syncthreads();
-    // E rows below the panel: E[c0:m, 0:c0] -= L[c0:m, J] E_J
-    {
-      const int ntr = (m - c0 + kTile - 1) / kTile, ntc = (c0 + kTile - 1) / kTile;
-      for (int tr = 0; tr < ntr; tr++) {
-        for (int tc = 0; tc < ntc; tc++) {
-          const int r0 = c0 + tr * kTile, e0 = tc * kTile;
-          for (int q = tid; q < kNB * kTile; q += kMfThreads) {
-            const int t = q / kTile, r = q % kTile;
-            As[t][r] = (t < jb && r0 + r < m) ? F[(int64_t)(j0 + t) * m + r0 + r] : T(0);
-          }
-          for (int q = tid; q < kNB * kTile; q += kMfThreads) {
-            const int r = q / kNB, t = q % kNB;
-            Bs[t][r] = (t < jb && e0 + r < c0) ? Eg[(int64_t)(e0 + r) * ld + j0 + t] : T(0);
-          }
-          __syncthreads();
-          T acc[4][4];
-#pragma unroll
-          for (int a = 0; a < 4; a++)
-#pragma unroll
-            for (int b = 0; b < 4; b++) acc[a][b] = T(0);
-          for (int t = 0; t < jb; t++) {
-            T ra[4], rb[4];
-#pragma unroll
-            for (int a = 0; a < 4; a++) ra[a] = As[t][tx + 16 * a];
-#pragma unroll
-            for (int b = 0; b < 4; b++) rb[b] = Bs[t][ty + 16 * b];
-#pragma unroll
-            for (int a = 0; a < 4; a++)
-#pragma unroll
-              for (int b = 0; b < 4; b++) acc[a][b] += ra[a] * rb[b];
-          }
-#pragma unroll
-          for (int b = 0; b < 4; b++) {
-            const int col = e0 + ty + 16 * b;
-            if (col >= c0) continue;
-#pragma unroll
-            for (int a = 0; a < 4; a++) {
-              const int row = r0 + tx + 16 * a;
-              if (row < m) Eg[(int64_t)col * ld + row] -= acc[a][b];
-            }
-          }
-          __syncthreads();
-        }
-      }
-    }
-    // trailing update of columns [j0+jb, m): F -= Lp Lp^T (lower part)
-    const int nt = (m - c0 + kTile - 1) / kTile;
-    for (int tj = 0; tj < nt; tj++) {
-      for (int ti = tj; ti < nt; ti++) {
-        const int r0 = c0 + ti * kTile, cc0 = c0 + tj * kTile;
-        for (int q = tid; q < kNB * kTile; q += kMfThreads) {
-          int t = q / kTile, r = q % kTile;
-          T a = T(0), b = T(0);
-          if (t < jb) {
-            if (r0 + r < m) a = F[(int64_t)(j0 + t) * m + r0 + r];
-            if (cc0 + r < m) b = F[(int64_t)(j0 + t) * m + cc0 + r];
-          }
-          As[t][r] = a;
-          Bs[t][r] = b;
-        }
-        __syncthreads();
-        T acc[4][4];
-#pragma unroll
-        for (int a = 0; a < 4; a++)
-#pragma unroll
-          for (int b = 0; b < 4; b++) acc[a][b] = T(0);
-        for (int t = 0; t < jb; t++) {
-          T ra[4], rb[4];
-#pragma unroll
-          for (int a = 0; a < 4; a++) ra[a] = As[t][tx + 16 * a];
-#pragma unroll
-          for (int b = 0; b < 4; b++) rb[b] = Bs[t][ty + 16 * b];
-#pragma unroll
-          for (int a = 0; a < 4; a++)
-#pragma unroll
-            for (int b = 0; b < 4; b++) acc[a][b] += ra[a] * rb[b];
-        }
-#pragma unroll
-        for (int b = 0; b < 4; b++) {
-          const int col = cc0 + ty + 16 * b;
-          if (col >= m) continue;
-#pragma unroll
-          for (int a = 0; a < 4; a++) {
-            const int row = r0 + tx + 16 * a;
-            if (row < m && row >= col) F[(int64_t)col * m + row] -= acc[a][b];
-          }
-        }
-        __syncthreads();
-      }
-    }
-  }
-}
-
-// Small fronts: the whole m x m front and its m x k elimination matrix live
-// in shared memory while the front is assembled and factored; then E and the
-// update block are written back.
-constexpr int kSmallThreads = 128;
-
-template <typename T>
-__global__ void __launch_bounds__(kSmallThreads)
-mf_factor_small(MfView v, const int *__restrict__ fronts, const double *__restrict__ vals,
-                T *__restrict__ arena, T *__restrict__ E, int *__restrict__ status) {
-  extern __shared__ unsigned char smem_raw[];
-  T *S = reinterpret_cast<T *>(smem_raw);
-  const int f = fronts[blockIdx.x];
-  const int m = v.f_m[f], k = v.f_k[f];
-  T *Es = S + m * m;  // m x k, column-major, ld m
-  const int64_t off = v.f_off[f];
-  const int tid = threadIdx.x, nt = kSmallThreads;
-  for (int q = tid; q < m * m; q += nt) S[q] = T(0);
-  for (int q = tid; q < m * k; q += nt) Es[q] = q / m == q % m ? T(1) : T(0);
-  __syncthreads();
-  for (int64_t e = v.f_asm[f] + tid; e < v.f_asm[f + 1]; e += nt) {
-    double sv = 0.0;
-    for (int64_t q = v.asm_sp[e]; q < v.asm_sp[e + 1]; q++) sv += vals[v.asm_src[q]];
-    S[v.asm_tgt[e] - off] = (T)sv;
-  }
-  __syncthreads();
-  for (int ci = v.f_child_ptr[f]; ci < v.f_child_ptr[f + 1]; ci++) {
-    const int c = v.f_children[ci];
-    const int mc = v.f_m[c], kc = v.f_k[c], rc = mc - kc;
-    const T *U = arena + v.f_off[c] + (int64_t)kc * mc + kc;
-    const int *rel = v.relmap + v.f_relmap[c];
     for (int q = tid; q < rc * rc; q += nt) {
       const int b = q / rc, a = q % rc;
-      if (a >= b) S[rel[b] * m + rel[a]] += U[(int64_t)b * mc + a];
+      if (a < b) continue;
+      const int col = rel[b], row = rel[a];
+      const T val = U[(int64_t)b * mc + a];
+      if (col < k) P[col * m + row] += val;
+      else F[(int64_t)col * m + row] += val;
     }
     __syncthreads();
   }
+  // 4. factor the panel and eliminate E
   for (int j = 0; j < k; j++) {
     if (tid == 0) {
-      T d = S[j * m + j];
+      T d = P[j * m + j];
       if (!(d > T(0))) { atomicOr(status, ERR_NOT_SPD); d = T(1); }
-      S[j * m + j] = tsqrt<T>(d);
+      piv = tsqrt<T>(d);
+      P[j * m + j] = piv;
     }
     __syncthreads();
-    const T p = S[j * m + j];
-    for (int i = j + 1 + tid; i < m; i += nt) S[j * m + i] /= p;
+    const T p = piv;
+    for (int i = j + 1 + tid; i < m; i += nt) P[j * m + i] /= p;
     for (int c = tid; c <= j; c += nt) Es[c * m + j] /= p;
     __syncthreads();
-    const int r = m - j - 1;
-    for (int q = tid; q < r * r; q += nt) {
-      const int c = j + 1 + q / r, i = j + 1 + q % r;
-      if (i >= c) S[c * m + i] -= S[j * m + i] * S[j * m + c];
+    const int rj = m - j - 1;
+    for (int q = tid; q < rj * (k - j - 1); q += nt) {  // panel columns c in (j, k), rows i >= c
+      const int c = j + 1 + q / rj, i = j + 1 + q % rj;
+      if (i >= c) P[c * m + i] -= P[j * m + i] * P[j * m + c];
     }
-    for (int q = tid; q < r * (j + 1); q += nt) {
-      const int c = q / r, i = j + 1 + q % r;
-      Es[c * m + i] -= S[j * m + i] * Es[c * m + j];
+    for (int q = tid; q < rj * (j + 1); q += nt) {  // E rows i > j, columns c <= j
+      const int c = q / rj, i = j + 1 + q % rj;
+      Es[c * m + i] -= P[j * m + i] * Es[c * m + j];
     }
     __syncthreads();
   }
-  const int ld = round4(m);
-  T *Eg = E + v.e_off[f];
-  for (int q = tid; q < m * k; q += nt) Eg[(int64_t)(q / m) * ld + q % m] = Es[q];
-  T *F = arena + off;
-  for (int q = tid; q < (m - k) * m; q += nt) {
-    const int c = k + q / m, i = q % m;
-    if (i >= c) F[(int64_t)c * m + i] = S[c * m + i];
+  // 5. E -> global (ld round4(m)); the padding rows stay zero
+  {
+    const int ld = round4(m);
+    T *Eg = E + v.e_off[f];
+    for (int q = tid; q < m * k; q += nt) Eg[(int64_t)(q / m) * ld + q % m] = Es[q];
+  }
+  // 6. update block: F[k:m, k:m] -= L21 L21^T (lower), 4x4 blocks per thread
+  const int nb4 = (r + 3) / 4;
+  for (int q = tid; q < nb4 * nb4; q += nt) {
+    const int bi = q % nb4, bc = q / nb4;
+    if (bi < bc) continue;
+    const int i0 = k + 4 * bi, c0 = k + 4 * bc;
+    T acc[4][4];
+#pragma unroll
+    for (int a = 0; a < 4; a++)
+#pragma unroll
+      for (int b = 0; b < 4; b++) acc[a][b] = T(0);
+    for (int j = 0; j < k; j++) {
+      T li[4], lc[4];
+#pragma unroll
+      for (int a = 0; a < 4; a++) {
+        li[a] = i0 + a < m ? P[j * m + i0 + a] : T(0);
+        lc[a] = c0 + a < m ? P[j * m + c0 + a] : T(0);
+      }
+#pragma unroll
+      for (int a = 0; a < 4; a++)
+#pragma unroll
+        for (int b = 0; b < 4; b++) acc[a][b] += li[a] * lc[b];
+    }
+#pragma unroll
+    for (int b = 0; b < 4; b++) {
+      const int col = c0 + b;
+      if (col >= m) continue;
+#pragma unroll
+      for (int a = 0; a < 4; a++) {
+        const int row = i0 + a;
+        if (row < m && row >= col) F[(int64_t)col * m + row] -= acc[a][b];
+      }
+    }
   }
 }
 
@@ -637,11 +516,34 @@ template <> struct Vec16<double> {
 
 constexpr int kSolveSmall = 128;   // fronts of at most this many rows: one warp each
 constexpr int kEThreads = 256;
+constexpr int kELeanThreads = 128;
 constexpr int kEUnroll = 8;        // independent E loads in flight per thread
 
-// small fronts, forward: one warp per front; lane l holds rows VN*l + 32*VN*p
+// E loads of one batch of kEUnroll columns [j0, j0 + kEUnroll) for the rows
+// of one lane; vectors wholly above the diagonal (r + VN <= j) are zero
+template <typename T, int PASS>
+__device__ __forceinline__ void load_e_batch(const T *Ef, int ld, int m, int k, int lane, int j0,
+                                             T (&e)[PASS][kEUnroll][Vec16<T>::N]) {
+  constexpr int VN = Vec16<T>::N;
+#pragma unroll
+  for (int p = 0; p < PASS; p++) {
+    const int r = VN * lane + 32 * VN * p;
+#pragma unroll
+    for (int u = 0; u < kEUnroll; u++) {
+      const int j = j0 + u;
+      if (r < m && j < k && r + VN > j) Vec16<T>::load(Ef + (int64_t)j * ld + r, e[p][u]);
+      else {
+#pragma unroll
+        for (int q = 0; q < VN; q++) e[p][u][q] = T(0);
+      }
+    }
+  }
+}
+
+// small fronts, forward: one warp per front; lane l holds rows VN*l + 32*VN*p.
+// The first batch of E is loaded before the right-hand side is assembled.
 template <typename T>
-__global__ void __launch_bounds__(256, 4)
+__global__ void __launch_bounds__(256, sizeof(T) == 8 ? 2 : 4)
 mf_fwd_small(MfView v, const int *__restrict__ fronts, int nf, const T *__restrict__ E,
              const T *__restrict__ xl, T *__restrict__ yl, T *__restrict__ uvec) {
   constexpr int VN = Vec16<T>::N, PASS = kSolveSmall / (32 * VN);
@@ -653,6 +555,9 @@ mf_fwd_small(MfView v, const int *__restrict__ fronts, int nf, const T *__restri
   const int f = fronts[gw];
   const int m = v.f_m[f], k = v.f_k[f], ld = round4(m);
   const int64_t xo = v.f_xoff[f] + v.f_p0[f];
+  const T *Ef = E + v.e_off[f];
+  T e[PASS][kEUnroll][VN];
+  load_e_batch<T, PASS>(Ef, ld, m, k, lane, 0, e);
   for (int i = lane; i < m; i += 32) w[i] = i < k ? xl[xo + i] : T(0);
   __syncwarp();
   for (int ci = v.f_child_ptr[f]; ci < v.f_child_ptr[f + 1]; ci++) {
@@ -663,35 +568,20 @@ mf_fwd_small(MfView v, const int *__restrict__ fronts, int nf, const T *__restri
     for (int a = lane; a < rc; a += 32) w[rel[a]] += u[a];
     __syncwarp();
   }
-  const T *Ef = E + v.e_off[f];
   T acc[PASS][VN];
 #pragma unroll
   for (int p = 0; p < PASS; p++)
 #pragma unroll
     for (int q = 0; q < VN; q++) acc[p][q] = T(0);
+  for (int j0 = 0; j0 < k; j0 += kEUnroll) {
+    if (j0 > 0) load_e_batch<T, PASS>(Ef, ld, m, k, lane, j0, e);
 #pragma unroll
-  for (int p = 0; p < PASS; p++) {
-    const int r = VN * lane + 32 * VN * p;
-    if (r >= m) continue;
-    // columns in batches of kEUnroll independent loads; a vector of rows wholly
-    // above the diagonal (r + VN <= j) is zero and not loaded
-    for (int j0 = 0; j0 < k; j0 += kEUnroll) {
-      T e[kEUnroll][VN];
+    for (int u = 0; u < kEUnroll; u++) {
+      const T bj = j0 + u < k ? w[j0 + u] : T(0);
 #pragma unroll
-      for (int u = 0; u < kEUnroll; u++) {
-        const int j = j0 + u;
-        if (j < k && r + VN > j) Vec16<T>::load(Ef + (int64_t)j * ld + r, e[u]);
-        else {
+      for (int p = 0; p < PASS; p++)
 #pragma unroll
-          for (int q = 0; q < VN; q++) e[u][q] = T(0);
-        }
-      }
-#pragma unroll
-      for (int u = 0; u < kEUnroll; u++) {
-        const T bj = j0 + u < k ? w[j0 + u] : T(0);
-#pragma unroll
-        for (int q = 0; q < VN; q++) acc[p][q] += e[u][q] * bj;
-      }
+        for (int q = 0; q < VN; q++) acc[p][q] += e[p][u][q] * bj;
     }
   }
   T *uf = uvec + v.f_uoff[f];
@@ -705,9 +595,10 @@ mf_fwd_small(MfView v, const int *__restrict__ fronts, int nf, const T *__restri
     }
 }
 
-// small fronts, backward: one warp per front
+// small fronts, backward: one warp per front; the first batch of E is loaded
+// before v is gathered
 template <typename T>
-__global__ void __launch_bounds__(256, 4)
+__global__ void __launch_bounds__(256, sizeof(T) == 8 ? 2 : 4)
 mf_bwd_small(MfView v, const int *__restrict__ fronts, int nf, const T *__restrict__ E,
              const T *__restrict__ yl, T *__restrict__ xl) {
   constexpr int VN = Vec16<T>::N, PASS = kSolveSmall / (32 * VN);
@@ -719,6 +610,9 @@ mf_bwd_small(MfView v, const int *__restrict__ fronts, int nf, const T *__restri
   const int f = fronts[gw];
   const int m = v.f_m[f], k = v.f_k[f], ld = round4(m);
   const int64_t xo = v.f_xoff[f] + v.f_p0[f];
+  const T *Ef = E + v.e_off[f];
+  T e[PASS][kEUnroll][VN];
+  load_e_batch<T, PASS>(Ef, ld, m, k, lane, 0, e);
   const T *xb = xl + v.f_xoff[f];
   const int *rows = v.rows + v.f_rows[f];
   for (int i = lane; i < ld; i += 32) w[i] = i < k ? yl[xo + i] : (i < m ? xb[rows[i]] : T(0));
@@ -731,34 +625,17 @@ mf_bwd_small(MfView v, const int *__restrict__ fronts, int nf, const T *__restri
       const int r = VN * lane + 32 * VN * p + q;
       wr[p][q] = r < ld ? w[r] : T(0);
     }
-  const T *Ef = E + v.e_off[f];
-  // columns in batches of kEUnroll: the loads of a batch are issued together,
-  // then each column sum is reduced over the warp
+  // each column sum is reduced over the warp; lane u of the batch keeps column u
   for (int c0 = 0; c0 < k; c0 += kEUnroll) {
+    if (c0 > 0) load_e_batch<T, PASS>(Ef, ld, m, k, lane, c0, e);
     T s[kEUnroll];
 #pragma unroll
-    for (int u = 0; u < kEUnroll; u++) s[u] = T(0);
-#pragma unroll
-    for (int p = 0; p < PASS; p++) {
-      const int r = VN * lane + 32 * VN * p;
-      if (r >= m) continue;
-      T e[kEUnroll][VN];
-#pragma unroll
-      for (int u = 0; u < kEUnroll; u++) {
-        const int c = c0 + u;
-        if (c < k && r + VN > c) Vec16<T>::load(Ef + (int64_t)c * ld + r, e[u]);
-        else {
-#pragma unroll
-          for (int q = 0; q < VN; q++) e[u][q] = T(0);
-        }
-      }
-#pragma unroll
-      for (int u = 0; u < kEUnroll; u++)
-#pragma unroll
-        for (int q = 0; q < VN; q++) s[u] += e[u][q] * wr[p][q];
-    }
-#pragma unroll
     for (int u = 0; u < kEUnroll; u++) {
+      s[u] = T(0);
+#pragma unroll
+      for (int p = 0; p < PASS; p++)
+#pragma unroll
+        for (int q = 0; q < VN; q++) s[u] += e[p][u][q] * wr[p][q];
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) s[u] += __shfl_xor_sync(0xffffffffu, s[u], o);
     }
@@ -780,11 +657,11 @@ mf_bwd_small(MfView v, const int *__restrict__ fronts, int nf, const T *__restri
 // of rows wholly above the diagonal of E is zero and not loaded.
 template <typename T> struct FwdRows { static constexpr int N = 32 * Vec16<T>::N; };
 
-template <typename T>
-__global__ void __launch_bounds__(kEThreads, 2)
+template <typename T, int NT>
+__global__ void __launch_bounds__(NT, NT == kELeanThreads ? 8 : 2)
 mf_fwd_big(MfView v, const int2 *__restrict__ tasks, const T *__restrict__ E, const T *__restrict__ xl,
            T *__restrict__ yl, T *__restrict__ uvec) {
-  constexpr int VN = Vec16<T>::N, RC = FwdRows<T>::N, NW = kEThreads / 32;
+  constexpr int VN = Vec16<T>::N, RC = FwdRows<T>::N, NW = NT / 32, UN = NT == kELeanThreads ? 4 : kEUnroll;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T *b = reinterpret_cast<T *>(smem_raw);  // b[0, m)
   __shared__ T red[NW][RC];
@@ -793,14 +670,14 @@ mf_fwd_big(MfView v, const int2 *__restrict__ tasks, const T *__restrict__ E, co
   const int m = v.f_m[f], k = v.f_k[f], ld = round4(m);
   const int64_t xo = v.f_xoff[f] + v.f_p0[f];
   const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
-  for (int i = tid; i < m; i += kEThreads) b[i] = i < k ? xl[xo + i] : T(0);
+  for (int i = tid; i < m; i += NT) b[i] = i < k ? xl[xo + i] : T(0);
   __syncthreads();
   for (int ci = v.f_child_ptr[f]; ci < v.f_child_ptr[f + 1]; ci++) {
     const int c = v.f_children[ci];
     const int rc = v.f_m[c] - v.f_k[c];
     const int *rel = v.relmap + v.f_relmap[c];
     const T *u = uvec + v.f_uoff[c];
-    for (int a = tid; a < rc; a += kEThreads) b[rel[a]] += u[a];
+    for (int a = tid; a < rc; a += NT) b[rel[a]] += u[a];
     __syncthreads();
   }
   const T *Ef = E + v.e_off[f];
@@ -815,10 +692,10 @@ mf_fwd_big(MfView v, const int2 *__restrict__ tasks, const T *__restrict__ E, co
     if (rb < m) {
       const T *Er = Ef + rb;
       int j = wid;
-      for (; j + (kEUnroll - 1) * NW < K; j += kEUnroll * NW) {
-        T e[kEUnroll][VN];
+      for (; j + (UN - 1) * NW < K; j += UN * NW) {
+        T e[UN][VN];
 #pragma unroll
-        for (int u = 0; u < kEUnroll; u++) {
+        for (int u = 0; u < UN; u++) {
           if (rb + VN > j + u * NW) Vec16<T>::load(Er + (int64_t)(j + u * NW) * ld, e[u]);
           else {
 #pragma unroll
@@ -826,7 +703,7 @@ mf_fwd_big(MfView v, const int2 *__restrict__ tasks, const T *__restrict__ E, co
           }
         }
 #pragma unroll
-        for (int u = 0; u < kEUnroll; u++) {
+        for (int u = 0; u < UN; u++) {
           const T bj = b[j + u * NW];
 #pragma unroll
           for (int q = 0; q < VN; q++) acc[q] += e[u][q] * bj;
@@ -845,7 +722,7 @@ mf_fwd_big(MfView v, const int2 *__restrict__ tasks, const T *__restrict__ E, co
 #pragma unroll
     for (int q = 0; q < VN; q++) red[wid][lane * VN + q] = acc[q];
     __syncthreads();
-    for (int t = tid; t < RC; t += kEThreads) {
+    for (int t = tid; t < RC; t += NT) {
       T s = T(0);
 #pragma unroll
       for (int w = 0; w < NW; w++) s += red[w][t];
@@ -859,11 +736,11 @@ mf_fwd_big(MfView v, const int2 *__restrict__ tasks, const T *__restrict__ E, co
 
 // large fronts, backward: task = {front, column block J}; x[32J .. 32J+31] from
 // rows [32J, m) of E
-template <typename T>
-__global__ void __launch_bounds__(kEThreads, 2)
+template <typename T, int NT>
+__global__ void __launch_bounds__(NT, NT == kELeanThreads ? 8 : 2)
 mf_bwd_big(MfView v, const int2 *__restrict__ tasks, const T *__restrict__ E, const T *__restrict__ yl,
            T *__restrict__ xl) {
-  constexpr int VN = Vec16<T>::N, LPC = 32 / VN, NCS = kEThreads / LPC;
+  constexpr int VN = Vec16<T>::N, LPC = 32 / VN, NCS = NT / LPC, UN = NT == kELeanThreads ? 4 : kEUnroll;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T *w = reinterpret_cast<T *>(smem_raw);  // v[32J, ld)
   const int f = tasks[blockIdx.x].x, J = tasks[blockIdx.x].y;
@@ -873,7 +750,7 @@ mf_bwd_big(MfView v, const int2 *__restrict__ tasks, const T *__restrict__ E, co
   const T *xb = xl + v.f_xoff[f];
   const int *rows = v.rows + v.f_rows[f];
   const int tid = threadIdx.x;
-  for (int i = c0 + tid; i < ld; i += kEThreads) w[i - c0] = i < k ? yl[xo + i] : (i < m ? xb[rows[i]] : T(0));
+  for (int i = c0 + tid; i < ld; i += NT) w[i - c0] = i < k ? yl[xo + i] : (i < m ? xb[rows[i]] : T(0));
   __syncthreads();
   const int rq = tid % LPC, cs = tid / LPC;
   for (int cc = cs; cc < 32; cc += NCS) {  // uniform trip count: the shuffles below need whole groups
@@ -882,10 +759,10 @@ mf_bwd_big(MfView v, const int2 *__restrict__ tasks, const T *__restrict__ E, co
     if (cc < jb) {
       const T *Ec = E + v.e_off[f] + (int64_t)c * ld;
       int i = c0 + rq * VN;
-      for (; i + (kEUnroll - 1) * 32 < m; i += kEUnroll * 32) {
-        T e[kEUnroll][VN];
+      for (; i + (UN - 1) * 32 < m; i += UN * 32) {
+        T e[UN][VN];
 #pragma unroll
-        for (int u = 0; u < kEUnroll; u++) {
+        for (int u = 0; u < UN; u++) {
           if (i + u * 32 + VN > c) Vec16<T>::load(Ec + i + u * 32, e[u]);
           else {
 #pragma unroll
@@ -893,7 +770,7 @@ mf_bwd_big(MfView v, const int2 *__restrict__ tasks, const T *__restrict__ E, co
           }
         }
 #pragma unroll
-        for (int u = 0; u < kEUnroll; u++)
+        for (int u = 0; u < UN; u++)
 #pragma unroll
           for (int q = 0; q < VN; q++) s += e[u][q] * w[i + u * 32 + q - c0];
       }

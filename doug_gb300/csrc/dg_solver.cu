@@ -62,14 +62,18 @@ static double wall() {
 }
 
 // one multifrontal batch on the device, factor precision T
-constexpr int kLargeFront = 256;      // fronts above this size use the multi-CTA pipeline
+// fronts of at most kPanelFrontRows rows whose panel and E fit in kPanelSmem
+// bytes are factored by one CTA each; the others by the multi-CTA pipeline
+constexpr int kPanelFrontRows = 512;
+constexpr size_t kPanelSmem = 96 * 1024;
 constexpr int64_t kFwdTaskBytes = 96 * 1024;  // E bytes per forward task of a large front
+constexpr int64_t kLeanTaskBytes = 80 * 1024; // levels with smaller average tasks use 128-thread CTAs
 
 template <typename T>
 struct MfDevice {
   DBuf<int64_t> f_off, f_rows, f_xoff, f_uoff, f_woff, f_relmap, f_asm, asm_tgt, asm_sp, asm_src, e_off;
   DBuf<int> f_m, f_k, f_p0, f_child_ptr, f_children, rows, relmap, lvl_fronts, gidx;
-  DBuf<int> small_fronts, tiny_fronts, diag_fronts, solve_small;
+  DBuf<int> pan_fronts, diag_fronts, solve_small;
   DBuf<int2> asm_tasks, upd_tasks, panel_tasks, esc_tasks, etile_tasks, fwd_tasks, bwd_tasks;
   DBuf<T> arena, E, xl, yl, u;
   int64_t e_len = 0;
@@ -79,8 +83,8 @@ struct MfDevice {
     int upd_off, upd_cnt, etile_off, etile_cnt;
   };
   struct Level {
-    int tiny_off, tiny_cnt, small_off, small_cnt, asm_off, asm_cnt;
-    size_t tiny_smem;
+    int pan_off, pan_cnt, asm_off, asm_cnt;
+    size_t pan_smem;
     std::vector<Step> steps;
   };
   std::vector<Level> levels;
@@ -88,6 +92,7 @@ struct MfDevice {
   struct SolveLevel {
     int small_off, small_cnt, fwd_off, fwd_cnt, bwd_off, bwd_cnt;
     size_t fwd_smem, bwd_smem;
+    bool fwd_lean, bwd_lean;      // 128-thread CTAs for levels of small tasks
   };
   std::vector<SolveLevel> slevels;
   int nlevels = 0, nfronts = 0;
@@ -128,30 +133,27 @@ struct MfDevice {
     CK(cudaGetDevice(&dev));
     CK(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
     // work lists of the factorisation
-    std::vector<int> sm, ty, df;
+    std::vector<int> pn, df;
     std::vector<int2> at, ut, pf, es, et;
-    const int tiny_max = sizeof(T) == 8 ? 112 : 160;  // front + E fit in shared memory
-    size_t tiny_smem_max = 0;
     levels.assign((size_t)nlevels, Level());
     for (int l = 0; l < nlevels; l++) {
       Level &L = levels[(size_t)l];
-      L.small_off = (int)sm.size();
-      L.tiny_off = (int)ty.size();
-      L.tiny_smem = 0;
+      L.pan_off = (int)pn.size();
+      L.pan_smem = 0;
       L.asm_off = (int)at.size();
       std::vector<int> large;
       for (int q = B.lvl_ptr[(size_t)l]; q < B.lvl_ptr[(size_t)l + 1]; q++) {
         int f = B.lvl_fronts[(size_t)q];
         int m = B.f_m[(size_t)f], k = B.f_k[(size_t)f];
-        if (m > kLargeFront) large.push_back(f);
-        else if (m <= tiny_max) {
-          ty.push_back(f);
-          L.tiny_smem = std::max(L.tiny_smem, (size_t)(m * m + m * k) * sizeof(T));
-        } else sm.push_back(f);
+        const size_t smem = (size_t)2 * m * k * sizeof(T);
+        if (m <= kPanelFrontRows && smem <= kPanelSmem) {
+          pn.push_back(f);
+          L.pan_smem = std::max(L.pan_smem, smem);
+        } else {
+          large.push_back(f);
+        }
       }
-      tiny_smem_max = std::max(tiny_smem_max, L.tiny_smem);
-      L.small_cnt = (int)sm.size() - L.small_off;
-      L.tiny_cnt = (int)ty.size() - L.tiny_off;
+      L.pan_cnt = (int)pn.size() - L.pan_off;
       int kmax = 0;
       for (int f : large) {
         int m = B.f_m[(size_t)f];
@@ -184,12 +186,10 @@ struct MfDevice {
         L.steps.push_back(st);
       }
     }
-    small_fronts.upload(sm);
-    tiny_fronts.upload(ty);
+    pan_fronts.upload(pn);
     // kernel attributes are per function, shared by every batch of this
     // precision: always the device maximum, never a batch's own size
-    if (tiny_smem_max > (size_t)optin) throw CudaError{cudaErrorInvalidValue, "front too large for shared memory"};
-    CK(cudaFuncSetAttribute(mf_factor_small<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
+    CK(cudaFuncSetAttribute(mf_factor_panel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin - 1024));
     panel_tasks.upload(pf);
     esc_tasks.upload(es);
     diag_fronts.upload(df);
@@ -210,6 +210,7 @@ struct MfDevice {
       L.bwd_off = (int)bw.size();
       L.fwd_smem = L.bwd_smem = 0;
       std::vector<std::pair<int, int2>> fl, bl;
+      int64_t fwd_bytes = 0, bwd_bytes = 0;
       for (int q = B.lvl_ptr[(size_t)l]; q < B.lvl_ptr[(size_t)l + 1]; q++) {
         int f = B.lvl_fronts[(size_t)q];
         int m = B.f_m[(size_t)f], k = B.f_k[(size_t)f];
@@ -225,9 +226,13 @@ struct MfDevice {
             c1++;
           } while (c1 < nch && bytes < kFwdTaskBytes);
           fl.push_back({(int)std::min<int64_t>(bytes, 1 << 30), make_int2(f, (c << 16) | (c1 - c))});
+          fwd_bytes += bytes;
           c = c1;
         }
-        for (int J = 0; 32 * J < k; J++) bl.push_back({m - 32 * J, make_int2(f, J)});
+        for (int J = 0; 32 * J < k; J++) {
+          bl.push_back({m - 32 * J, make_int2(f, J)});
+          bwd_bytes += (int64_t)32 * (m - 32 * J) * (int64_t)sizeof(T);
+        }
         L.fwd_smem = std::max(L.fwd_smem, (size_t)round4(m) * sizeof(T));
         L.bwd_smem = std::max(L.bwd_smem, (size_t)round4(m) * sizeof(T));
       }
@@ -238,37 +243,38 @@ struct MfDevice {
       L.small_cnt = (int)ss.size() - L.small_off;
       L.fwd_cnt = (int)fw.size() - L.fwd_off;
       L.bwd_cnt = (int)bw.size() - L.bwd_off;
+      L.fwd_lean = L.fwd_cnt && fwd_bytes / L.fwd_cnt < kLeanTaskBytes;
+      L.bwd_lean = L.bwd_cnt && bwd_bytes / L.bwd_cnt < kLeanTaskBytes;
       fwd_smem_max = std::max(fwd_smem_max, L.fwd_smem);
       bwd_smem_max = std::max(bwd_smem_max, L.bwd_smem);
     }
     solve_small.upload(ss);
     fwd_tasks.upload(fw);
     bwd_tasks.upload(bw);
-    {
-      cudaFuncAttributes fa{}, fb{};
-      CK(cudaFuncGetAttributes(&fa, mf_fwd_big<T>));
-      CK(cudaFuncGetAttributes(&fb, mf_bwd_big<T>));
-      if (fwd_smem_max + fa.sharedSizeBytes > (size_t)optin || bwd_smem_max + fb.sharedSizeBytes > (size_t)optin)
-        throw CudaError{cudaErrorInvalidValue, "front too large for the shared-memory solve"};
-      CK(cudaFuncSetAttribute(mf_fwd_big<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              optin - (int)fa.sharedSizeBytes));
-      CK(cudaFuncSetAttribute(mf_bwd_big<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              optin - (int)fb.sharedSizeBytes));
-    }
+    set_solve_attrs<kEThreads>(optin, fwd_smem_max, bwd_smem_max);
+    set_solve_attrs<kELeanThreads>(optin, fwd_smem_max, bwd_smem_max);
+  }
+
+  template <int NT>
+  void set_solve_attrs(int optin, size_t fwd_smem_max, size_t bwd_smem_max) {
+    cudaFuncAttributes fa{}, fb{};
+    CK(cudaFuncGetAttributes(&fa, mf_fwd_big<T, NT>));
+    CK(cudaFuncGetAttributes(&fb, mf_bwd_big<T, NT>));
+    if (fwd_smem_max + fa.sharedSizeBytes > (size_t)optin || bwd_smem_max + fb.sharedSizeBytes > (size_t)optin)
+      throw CudaError{cudaErrorInvalidValue, "front too large for the shared-memory solve"};
+    CK(cudaFuncSetAttribute(mf_fwd_big<T, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                            optin - (int)fa.sharedSizeBytes));
+    CK(cudaFuncSetAttribute(mf_bwd_big<T, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                            optin - (int)fb.sharedSizeBytes));
   }
 
   int factor(const double *vals, int *status, cudaStream_t s) {
     int launches = 0;
     for (int l = 0; l < nlevels; l++) {
       const Level &L = levels[(size_t)l];
-      if (L.tiny_cnt) {
-        mf_factor_small<T><<<L.tiny_cnt, kSmallThreads, L.tiny_smem, s>>>(view, tiny_fronts.p + L.tiny_off, vals,
-                                                                         arena.p, E.p, status);
-        launches++;
-      }
-      if (L.small_cnt) {
-        mf_factor_level<T><<<L.small_cnt, kMfThreads, 0, s>>>(view, small_fronts.p + L.small_off, vals,
-                                                              arena.p, E.p, status);
+      if (L.pan_cnt) {
+        mf_factor_panel<T><<<L.pan_cnt, kPanThreads, L.pan_smem, s>>>(view, pan_fronts.p + L.pan_off, vals,
+                                                                      arena.p, E.p, status);
         launches++;
       }
       if (L.asm_cnt) {
@@ -304,14 +310,24 @@ struct MfDevice {
         launches++;
       }
       if (L.fwd_cnt) {
-        mf_fwd_big<T><<<L.fwd_cnt, kEThreads, L.fwd_smem, s>>>(view, fwd_tasks.p + L.fwd_off, E.p, xl.p, yl.p, u.p);
+        if (L.fwd_lean)
+          mf_fwd_big<T, kELeanThreads><<<L.fwd_cnt, kELeanThreads, L.fwd_smem, s>>>(view, fwd_tasks.p + L.fwd_off,
+                                                                                  E.p, xl.p, yl.p, u.p);
+        else
+          mf_fwd_big<T, kEThreads><<<L.fwd_cnt, kEThreads, L.fwd_smem, s>>>(view, fwd_tasks.p + L.fwd_off, E.p,
+                                                                          xl.p, yl.p, u.p);
         launches++;
       }
     }
     for (int l = nlevels - 1; l >= 0; l--) {
       const SolveLevel &L = slevels[(size_t)l];
       if (L.bwd_cnt) {
-        mf_bwd_big<T><<<L.bwd_cnt, kEThreads, L.bwd_smem, s>>>(view, bwd_tasks.p + L.bwd_off, E.p, yl.p, xl.p);
+        if (L.bwd_lean)
+          mf_bwd_big<T, kELeanThreads><<<L.bwd_cnt, kELeanThreads, L.bwd_smem, s>>>(view, bwd_tasks.p + L.bwd_off,
+                                                                                  E.p, yl.p, xl.p);
+        else
+          mf_bwd_big<T, kEThreads><<<L.bwd_cnt, kEThreads, L.bwd_smem, s>>>(view, bwd_tasks.p + L.bwd_off, E.p,
+                                                                          yl.p, xl.p);
         launches++;
       }
       if (L.small_cnt) {

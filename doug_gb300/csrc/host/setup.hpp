@@ -31,7 +31,7 @@ struct Controls {
   double omega = 0.33333333333333;  // prolongator smoother weight (CoarseMtx.F90:64)
   int precision = 0;                // 0 = FP64 path, 1 = mixed (FP32 factors)
   int replace_every = 50;           // residual replacement period (mixed path)
-  int nd_leaf = 16;                 // nested-dissection leaf size of the subdomain factors
+  int nd_leaf = 24;                 // nested-dissection leaf size of the subdomain factors
   int profile = 0;                  // 1: CUDA-event timing of the solve phases
 };
 
