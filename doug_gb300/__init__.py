@@ -38,6 +38,7 @@ EXPORTED_SYMBOLS = [
     "dg_set_matrix_coo", "dg_set_rhs", "dg_set_partition", "dg_setup", "dg_solve",
     "dg_solve_device", "dg_write_solution", "dg_get_sizes", "dg_get_aggregates",
     "dg_get_subdomains", "dg_get_restriction", "dg_get_coarse_matrix", "dg_residual_csr",
+    "dg_set_elements", "dg_get_input",
     "dg_residual_csr_noalloc",
 ]
 
@@ -108,6 +109,9 @@ def load_library(path: str | None = None):
     L.dg_load_ctl.argtypes = [vp, C.c_char_p]
     L.dg_set_matrix_coo.argtypes = [vp, C.c_int, C.c_int, P(C.c_int), P(C.c_int), P(C.c_double)]
     L.dg_set_rhs.argtypes = [vp, P(C.c_double)]
+    L.dg_set_elements.argtypes = [vp, C.c_int, C.c_int, P(C.c_int), P(C.c_int), P(C.c_double), P(C.c_double)]
+    L.dg_get_input.argtypes = [vp, P(C.c_int), P(C.c_int), P(C.c_int), P(C.c_int), P(C.c_double),
+                               P(C.c_double)]
     L.dg_set_partition.argtypes = [vp, P(C.c_int), C.c_int]
     L.dg_setup.argtypes = [vp]
     L.dg_solve.argtypes = [vp, P(C.c_double), P(C.c_double), P(_Stats)]
@@ -192,6 +196,27 @@ class DougSolver:
         c = np.ascontiguousarray(cols1, dtype=np.int32)
         v = np.ascontiguousarray(vals, dtype=np.float64)
         self._check(self._L.dg_set_matrix_coo(self._h, int(n), len(v), _ip(r), _ip(c), _dp(v)))
+
+    def set_elements(self, ngf: int, eptr, efree, emat, erhs) -> None:
+        """Elemental input (the in-memory form of DOUG's input_type 1 files):
+        element e has the 1-based freedoms efree[eptr[e]:eptr[e+1]], its
+        matrix column by column in emat and its right-hand side in erhs."""
+        ep = np.ascontiguousarray(eptr, dtype=np.int32)
+        ef = np.ascontiguousarray(efree, dtype=np.int32)
+        em = np.ascontiguousarray(emat, dtype=np.float64)
+        er = np.ascontiguousarray(erhs, dtype=np.float64)
+        self._check(self._L.dg_set_elements(self._h, len(ep) - 1, int(ngf), _ip(ep), _ip(ef), _dp(em), _dp(er)))
+
+    def input_matrix(self):
+        """(n, rows1, cols1, vals, rhs) the handle holds, in entry order."""
+        n, nnz = C.c_int(), C.c_int()
+        self._check(self._L.dg_get_input(self._h, C.byref(n), C.byref(nnz), None, None, None, None))
+        r = np.zeros(nnz.value, np.int32)
+        c = np.zeros(nnz.value, np.int32)
+        v = np.zeros(nnz.value, np.float64)
+        b = np.zeros(n.value, np.float64)
+        self._check(self._L.dg_get_input(self._h, None, None, _ip(r), _ip(c), _dp(v), _dp(b)))
+        return n.value, r, c, v, b
 
     def set_rhs(self, b) -> None:
         b = np.ascontiguousarray(b, dtype=np.float64)

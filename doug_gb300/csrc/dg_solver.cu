@@ -846,6 +846,19 @@ dg_status dg_set_option(dg_handle *h, const char *name, const char *value) {
   return DG_OK;
 }
 
+// elemental input: assemble on the host (one process) and keep the result as
+// the matrix and right-hand side of the handle
+static dg_status set_elements(dg_handle *h, const ElementMesh &M) {
+  int n = 0;
+  std::vector<int> ii, jj, lg;
+  std::vector<double> vv, b;
+  assemble_elements(M, n, ii, jj, vv, b, lg);
+  if (n <= 0 || vv.empty()) return fail(h, DG_BAD_INPUT, "elements: the assembled matrix is empty");
+  dg_status s = dg_set_matrix_coo(h, n, (int)vv.size(), ii.data(), jj.data(), vv.data());
+  if (s != DG_OK) return s;
+  return dg_set_rhs(h, b.data());
+}
+
 dg_status dg_load_ctl(dg_handle *h, const char *path) {
   if (!h || !path) return DG_BAD_INPUT;
   FILE *f = fopen(path, "rb");
@@ -859,9 +872,16 @@ dg_status dg_load_ctl(dg_handle *h, const char *path) {
   if (!ctl_parse_text(h->ctl, text, err)) return fail(h, DG_BAD_INPUT, err);
   h->ctl_dir = dirname_of(path);
   Controls &c = h->ctl;
+  if (c.input_type == 1) {  // elemental input (Distribution.F90:62-64)
+    ElementMesh M;
+    if (!read_elemental(resolve(h->ctl_dir, c.info_file), resolve(h->ctl_dir, c.freedom_lists_file),
+                        resolve(h->ctl_dir, c.elemmat_rhs_file), c.number_of_blocks, M, err))
+      return fail(h, DG_BAD_INPUT, err);
+    return set_elements(h, M);
+  }
   if (c.input_type != 2)
     return fail(h, DG_BAD_INPUT, "input_type " + std::to_string(c.input_type) +
-                                     ": only assembled input (2) is read from control files so far");
+                                     ": elemental (1) and assembled (2) input are read from control files");
   std::vector<int> ii, jj;
   std::vector<double> vv;
   int n = 0;
@@ -888,6 +908,31 @@ dg_status dg_set_matrix_coo(dg_handle *h, int n, int nnz, const int *rows, const
   h->ready = false;
   if (!h->have_rhs || (int)h->rhs.size() != n) { h->rhs.assign((size_t)n, 1.0); h->have_rhs = false; }
   return DG_OK;
+}
+
+dg_status dg_set_elements(dg_handle *h, int nell, int ngf, const int *eptr, const int *efree,
+                          const double *emat, const double *erhs) {
+  if (!h || nell <= 0 || ngf <= 0 || !eptr || !efree || !emat || !erhs) return DG_BAD_INPUT;
+  ElementMesh M;
+  M.nell = nell;
+  M.ngf = ngf;
+  M.eptr.assign(eptr, eptr + nell + 1);
+  if (M.eptr[0] != 0) return fail(h, DG_BAD_INPUT, "elements: eptr[0] must be 0");
+  for (int e = 0; e < nell; e++)
+    if (M.eptr[(size_t)e + 1] < M.eptr[(size_t)e]) return fail(h, DG_BAD_INPUT, "elements: freedom list offsets decrease");
+  const int64_t nfree = M.eptr.back();
+  M.efree.assign(efree, efree + nfree);
+  M.erhs.assign(erhs, erhs + nfree);
+  M.emat_off.assign(1, 0);
+  for (int e = 0; e < nell; e++) {
+    const int64_t nf = M.eptr[(size_t)e + 1] - M.eptr[(size_t)e];
+    M.emat_off.push_back(M.emat_off.back() + nf * nf);
+    M.mfrelt = std::max<int>(M.mfrelt, (int)nf);
+  }
+  M.emat.assign(emat, emat + M.emat_off.back());
+  std::string err;
+  if (!check_elements(M, err)) return fail(h, DG_BAD_INPUT, err);
+  return set_elements(h, M);
 }
 
 dg_status dg_set_rhs(dg_handle *h, const double *b) {
@@ -980,6 +1025,18 @@ dg_status dg_get_coarse_matrix(const dg_handle *h, int *ci, int *cj, double *cv)
   if (ci) std::copy(h->S.AC_i.begin(), h->S.AC_i.end(), ci);
   if (cj) std::copy(h->S.AC_j.begin(), h->S.AC_j.end(), cj);
   if (cv) std::copy(h->S.AC_v.begin(), h->S.AC_v.end(), cv);
+  return DG_OK;
+}
+
+dg_status dg_get_input(const dg_handle *h, int *n, int *nnz, int *rows, int *cols, double *vals, double *rhs) {
+  if (!h) return DG_BAD_INPUT;
+  if (!h->have_matrix) return DG_NOT_READY;
+  if (n) *n = h->n;
+  if (nnz) *nnz = (int)h->vv.size();
+  if (rows) std::copy(h->ii.begin(), h->ii.end(), rows);
+  if (cols) std::copy(h->jj.begin(), h->jj.end(), cols);
+  if (vals) std::copy(h->vv.begin(), h->vv.end(), vals);
+  if (rhs) std::copy(h->rhs.begin(), h->rhs.end(), rhs);
   return DG_OK;
 }
 

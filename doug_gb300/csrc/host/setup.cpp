@@ -340,6 +340,143 @@ bool read_vector(const std::string &path, int format, int n, std::vector<double>
   return true;
 }
 
+bool read_elemental(const std::string &info, const std::string &freelists, const std::string &elemmat,
+                    int number_of_blocks, ElementMesh &M, std::string &err) {
+  std::vector<unsigned char> b, rec;
+  size_t pos = 0;
+  // info_file: one record nell, ngf, nsd, mfrelt, nnode (Mesh.F90:305-307)
+  if (!slurp(info, b)) { err = "Unable to open info file: " + info; return false; }
+  if (!fortran_record(b, pos, rec) || rec.size() < 20) { err = "info file too short: " + info; return false; }
+  M.nell = (int32_t)rd_le32(&rec[0]);
+  M.ngf = (int32_t)rd_le32(&rec[4]);
+  M.nsd = (int32_t)rd_le32(&rec[8]);
+  M.mfrelt = (int32_t)rd_le32(&rec[12]);
+  M.nnode = (int32_t)rd_le32(&rec[16]);
+  if (M.nell <= 0 || M.ngf <= 0 || M.mfrelt <= 0) { err = "info file: bad mesh sizes in " + info; return false; }
+  // freedom lists: per element one record nfrelt, mhead(1:nfrelt) (Mesh.F90:452-460)
+  if (!slurp(freelists, b)) { err = "Unable to open freedom lists file: " + freelists; return false; }
+  pos = 0;
+  M.eptr.assign(1, 0);
+  M.efree.clear();
+  for (int e = 0; e < M.nell; e++) {
+    if (!fortran_record(b, pos, rec) || rec.size() < 4) { err = "freedom lists file too short: " + freelists; return false; }
+    const int nf = (int32_t)rd_le32(&rec[0]);
+    if (nf < 0 || nf > M.mfrelt || rec.size() < 4 + 4 * (size_t)nf) {
+      err = "freedom lists file: bad element record in " + freelists;
+      return false;
+    }
+    for (int i = 0; i < nf; i++) M.efree.push_back((int32_t)rd_le32(&rec[4 + 4 * (size_t)i]));
+    M.eptr.push_back((int)M.efree.size());
+  }
+  if (number_of_blocks > 1) M.ngf = *std::max_element(M.efree.begin(), M.efree.end());  // Mesh.F90:313-319
+  // element matrices and right-hand sides: per element nfrelt records (one per
+  // column) and one record of the right-hand side (ElemMtxs_distribute.F90:572-575)
+  if (!slurp(elemmat, b)) { err = "Unable to open element matrix file: " + elemmat; return false; }
+  pos = 0;
+  M.emat_off.assign(1, 0);
+  M.emat.clear();
+  M.erhs.clear();
+  for (int e = 0; e < M.nell; e++) {
+    const int nf = M.eptr[(size_t)e + 1] - M.eptr[(size_t)e];
+    for (int j = 0; j < nf; j++) {
+      if (!fortran_record(b, pos, rec) || rec.size() < 8 * (size_t)nf) {
+        err = "element matrix file too short: " + elemmat;
+        return false;
+      }
+      for (int k = 0; k < nf; k++) M.emat.push_back(rd_led(&rec[8 * (size_t)k]));
+    }
+    if (!fortran_record(b, pos, rec) || rec.size() < 8 * (size_t)nf) {
+      err = "element matrix file too short: " + elemmat;
+      return false;
+    }
+    for (int k = 0; k < nf; k++) M.erhs.push_back(rd_led(&rec[8 * (size_t)k]));
+    M.emat_off.push_back((int64_t)M.emat.size());
+  }
+  return check_elements(M, err);
+}
+
+bool check_elements(const ElementMesh &M, std::string &err) {
+  if (M.nell <= 0 || M.ngf <= 0 || (int)M.eptr.size() != M.nell + 1 || M.eptr[0] != 0) {
+    err = "elements: bad element count or freedom list offsets";
+    return false;
+  }
+  for (int e = 0; e < M.nell; e++)
+    if (M.eptr[(size_t)e + 1] < M.eptr[(size_t)e]) { err = "elements: freedom list offsets decrease"; return false; }
+  if ((int64_t)M.efree.size() != M.eptr.back() || (int64_t)M.erhs.size() != M.eptr.back() ||
+      (int)M.emat_off.size() != M.nell + 1 || (int64_t)M.emat.size() != M.emat_off.back()) {
+    err = "elements: array sizes do not match the freedom lists";
+    return false;
+  }
+  for (int e = 0; e < M.nell; e++) {
+    const int64_t nf = M.eptr[(size_t)e + 1] - M.eptr[(size_t)e];
+    if (M.emat_off[(size_t)e + 1] - M.emat_off[(size_t)e] != nf * nf) {
+      err = "elements: element matrix size does not match its freedom count";
+      return false;
+    }
+  }
+  for (int g : M.efree)
+    if (g < 1 || g > M.ngf) { err = "[Mesh_readFileFreelists] - freedom index out of range"; return false; }
+  return true;
+}
+
+void assemble_elements(const ElementMesh &M, int &n, std::vector<int> &ii, std::vector<int> &jj,
+                       std::vector<double> &vv, std::vector<double> &b, std::vector<int> &lg_fmap) {
+  // local freedoms: used freedoms in increasing global order (Mesh.F90:1131-1191, one partition)
+  std::vector<int> gl((size_t)M.ngf + 1, 0);
+  for (int g : M.efree) gl[(size_t)g] = 1;
+  lg_fmap.clear();
+  for (int g = 1; g <= M.ngf; g++)
+    if (gl[(size_t)g]) { lg_fmap.push_back(g); gl[(size_t)g] = (int)lg_fmap.size(); }
+  n = (int)lg_fmap.size();
+  // pattern: per local row, the sorted distinct local columns with a non-zero
+  // element value somewhere
+  std::vector<int64_t> rp((size_t)n + 1, 0);
+  std::vector<std::pair<int, int>> pairs;
+  for (int e = 0; e < M.nell; e++) {
+    const int e0 = M.eptr[(size_t)e], nf = M.eptr[(size_t)e + 1] - e0;
+    const double *Ae = &M.emat[(size_t)M.emat_off[(size_t)e]];
+    for (int i = 0; i < nf; i++)
+      for (int j = 0; j < nf; j++)
+        if (Ae[(size_t)j * nf + i] != 0.0)
+          pairs.push_back({gl[(size_t)M.efree[(size_t)(e0 + i)]] - 1, gl[(size_t)M.efree[(size_t)(e0 + j)]] - 1});
+  }
+  std::sort(pairs.begin(), pairs.end());
+  pairs.erase(std::unique(pairs.begin(), pairs.end()), pairs.end());
+  std::vector<int> col(pairs.size());
+  for (size_t q = 0; q < pairs.size(); q++) {
+    rp[(size_t)pairs[q].first + 1]++;
+    col[q] = pairs[q].second;
+  }
+  for (int r = 0; r < n; r++) rp[(size_t)r + 1] += rp[(size_t)r];
+  // values: element order, then row i, column j within the element
+  std::vector<double> val(col.size(), 0.0);
+  b.assign((size_t)n, 0.0);
+  for (int e = 0; e < M.nell; e++) {
+    const int e0 = M.eptr[(size_t)e], nf = M.eptr[(size_t)e + 1] - e0;
+    const double *Ae = &M.emat[(size_t)M.emat_off[(size_t)e]];
+    for (int i = 0; i < nf; i++) {
+      const int li = gl[(size_t)M.efree[(size_t)(e0 + i)]] - 1;
+      for (int j = 0; j < nf; j++) {
+        const double a = Ae[(size_t)j * nf + i];
+        if (a == 0.0) continue;
+        const int lj = gl[(size_t)M.efree[(size_t)(e0 + j)]] - 1;
+        const int *c0 = &col[(size_t)rp[(size_t)li]], *c1 = &col[(size_t)rp[(size_t)li + 1] - 1] + 1;
+        val[(size_t)(std::lower_bound(c0, c1, lj) - &col[0])] += a;
+      }
+      b[(size_t)li] += M.erhs[(size_t)(e0 + i)];
+    }
+  }
+  // COO in row order with the reference's flipped indices (ElemMtxs_assemble.F90:262-266)
+  ii.resize(col.size());
+  jj.resize(col.size());
+  vv = val;
+  for (int r = 0; r < n; r++)
+    for (int64_t q = rp[(size_t)r]; q < rp[(size_t)r + 1]; q++) {
+      ii[(size_t)q] = col[(size_t)q] + 1;
+      jj[(size_t)q] = r + 1;
+    }
+}
+
 bool write_solution(const std::string &path, int format, const double *x, int n, std::string &err) {
   FILE *f = fopen(path.c_str(), "wb");
   if (!f) { err = "cannot open " + path; return false; }
@@ -776,7 +913,15 @@ static bool aggregate(ScaledMatrix &S, int neighood, int minasize, int maxasize,
       }
     }
   } else {
-    // Cartesian aggregates (:332-346)
+    // Cartesian aggregates (:332-346); the reference divides by the radius,
+    // so a radius below 1 (the coarse default nint(3 n^(1/4) / (2 r1 + 1) - 1)
+    // on a tiny coarse matrix) stops it with an integer division fault: here
+    // it is an input error
+    if (neighood < 1) {
+      err = "Cartesian aggregation needs an aggregation radius >= 1 (radius " + std::to_string(neighood) +
+            "); set radius1 / radius2";
+      return false;
+    }
     int nsa = (sn + neighood - 1) / neighood, k = 0;
     for (int i = 1; i <= sn; i++)
       for (int j = 1; j <= sn; j++)

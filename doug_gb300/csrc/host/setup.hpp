@@ -53,6 +53,34 @@ bool read_vector(const std::string &path, int format, int n, std::vector<double>
 bool write_solution(const std::string &path, int format, const double *x, int n,
                     std::string &err);
 
+// Elemental input (input_type 1): element freedom lists and element matrices
+// with right-hand sides.  Element e has the global freedoms (1-based)
+// efree[eptr[e] .. eptr[e+1]) and the nfrelt x nfrelt matrix
+// emat[emat_off[e] ..] stored column by column (the file's record j is
+// column j), and the right-hand side erhs[eptr[e] ..].
+struct ElementMesh {
+  int nell = 0, ngf = 0, nsd = 0, mfrelt = 0, nnode = 0;
+  std::vector<int> eptr, efree;
+  std::vector<int64_t> emat_off;
+  std::vector<double> emat, erhs;
+};
+// Reads info_file, freedom_lists_file and elemmat_rhs_file
+// (Mesh.F90:293-460, ElemMtxs_distribute.F90:548-575): Fortran unformatted
+// sequential records, little-endian.  number_of_blocks > 1 takes ngf from the
+// largest freedom number, as the reference does.
+bool read_elemental(const std::string &info, const std::string &freelists, const std::string &elemmat,
+                    int number_of_blocks, ElementMesh &M, std::string &err);
+bool check_elements(const ElementMesh &M, std::string &err);
+// Assembles A and b the way one process does (ElemMtxs_assemble.F90:82-289):
+// local freedoms are the freedoms used by some element in increasing global
+// order; an entry exists where some element has a non-zero (i,j) and sums the
+// elements' values in element order; b sums every element's right-hand side.
+// The COO output walks the rows in order and each row's columns ascending,
+// with the reference's flipped indices (row index = column freedom).  Indices
+// are 1-based; lg_fmap[l] is the global freedom of local freedom l.
+void assemble_elements(const ElementMesh &M, int &n, std::vector<int> &ii, std::vector<int> &jj,
+                       std::vector<double> &vv, std::vector<double> &b, std::vector<int> &lg_fmap);
+
 // CSR with DOUG's stable row arrangement (entries of a row keep their input order).
 struct Csr {
   int nrows = 0, ncols = 0;

@@ -14,6 +14,9 @@ generated here from a seed:
   unknowns and 14,581,760 nonzeros.
 * ``block_partition`` -- the stand-in for a METIS partition of a structured
   grid: equal boxes of cells, numbered 1..nparts.
+* ``poisson2d_p1_elements`` -- the same 2-D P1 problem as element matrices
+  (DOUG's elemental input, input_type 1), optionally with one conductivity
+  per element; ``write_elemental_files`` writes them in DOUG's files.
 
 Matrices are returned as 1-based COO triplets sorted by row then column, as
 an assembled text file would list them.
@@ -75,6 +78,93 @@ def poisson2d_p1(nodes: int = 129, jitter: float = 0.2, seed: int = 0):
     rows1, cols1, vals = _csr_to_coo1(A)
     coords = np.stack([X[keep], Y[keep]], 1)
     return len(keep), rows1, cols1, vals, load[keep].copy(), coords
+
+
+def poisson2d_p1_elements(nodes: int = 17, jitter: float = 0.2, seed: int = 0, kappa=None):
+    """The P1 problem of ``poisson2d_p1`` as element matrices.
+
+    Freedoms are the interior nodes (numbered 1..ngf in node order; boundary
+    nodes carry no freedom, as in DOUG's freemap); element e lists its interior
+    vertices.  kappa (one value per triangle, default 1) scales the element
+    stiffness.  Returns (ngf, eptr, efree, emat, erhs, info) with emat the
+    element matrices column by column and info a dict of the mesh sizes.
+    """
+    rng = np.random.default_rng(seed)
+    h = 1.0 / (nodes - 1)
+    ii, jj = np.meshgrid(np.arange(nodes), np.arange(nodes), indexing="ij")
+    x = ii * h
+    y = jj * h
+    interior = (ii > 0) & (ii < nodes - 1) & (jj > 0) & (jj < nodes - 1)
+    dx = rng.uniform(-jitter * h, jitter * h, size=x.shape)
+    dy = rng.uniform(-jitter * h, jitter * h, size=y.shape)
+    x = np.where(interior, x + dx, x)
+    y = np.where(interior, y + dy, y)
+    gid = ii * nodes + jj
+    X = x.ravel()
+    Y = y.ravel()
+    c0 = gid[:-1, :-1].ravel()
+    c1 = gid[1:, :-1].ravel()
+    c2 = gid[1:, 1:].ravel()
+    c3 = gid[:-1, 1:].ravel()
+    diag = rng.integers(0, 2, size=c0.shape)
+    t1 = np.where(diag[:, None] == 0, np.stack([c0, c1, c2], 1), np.stack([c0, c1, c3], 1))
+    t2 = np.where(diag[:, None] == 0, np.stack([c0, c2, c3], 1), np.stack([c1, c2, c3], 1))
+    tri = np.concatenate([t1, t2], 0)
+    px = X[tri]
+    py = Y[tri]
+    b = np.stack([py[:, 1] - py[:, 2], py[:, 2] - py[:, 0], py[:, 0] - py[:, 1]], 1)
+    c = np.stack([px[:, 2] - px[:, 1], px[:, 0] - px[:, 2], px[:, 1] - px[:, 0]], 1)
+    area = np.abs(0.5 * (px[:, 1] * py[:, 2] - px[:, 2] * py[:, 1] - px[:, 0] * py[:, 2]
+                         + px[:, 2] * py[:, 0] + px[:, 0] * py[:, 1] - px[:, 1] * py[:, 0]))
+    K = (b[:, :, None] * b[:, None, :] + c[:, :, None] * c[:, None, :]) / (4.0 * area[:, None, None])
+    if kappa is not None:
+        K = K * np.asarray(kappa, dtype=np.float64)[:, None, None]
+    f = rng.uniform(-1.0, 1.0, size=nodes * nodes)
+    free = np.zeros(nodes * nodes, dtype=np.int64)
+    free[interior.ravel()] = np.arange(1, int(interior.sum()) + 1)
+    eptr = [0]
+    efree, emat, erhs = [], [], []
+    for e in range(len(tri)):
+        loc = [a for a in range(3) if free[tri[e, a]] > 0]
+        efree.extend(int(free[tri[e, a]]) for a in loc)
+        Ke = K[e][np.ix_(loc, loc)]
+        emat.extend(Ke.T.ravel())          # column by column
+        erhs.extend(f[tri[e, a]] * area[e] / 3.0 for a in loc)
+        eptr.append(len(efree))
+    info = {"nell": len(tri), "ngf": int(interior.sum()), "nsd": 2, "mfrelt": 3, "nnode": nodes * nodes}
+    return (info["ngf"], np.array(eptr, np.int32), np.array(efree, np.int32), np.array(emat, np.float64),
+            np.array(erhs, np.float64), info)
+
+
+def _fortran_record(fh, payload: bytes) -> None:
+    n = np.array([len(payload)], dtype="<i4").tobytes()
+    fh.write(n + payload + n)
+
+
+def write_elemental_files(folder: str, ngf, eptr, efree, emat, erhs, info) -> dict:
+    """Writes DOUG's elemental input files (Fortran unformatted sequential,
+    little-endian): info, freedom lists and element matrices + RHS.  Returns
+    the control-file words that name them."""
+    import os
+    eptr = np.asarray(eptr)
+    files = {"info_file": "doug_info.dat", "freedom_lists_file": "doug_element.dat",
+             "elemmat_rhs_file": "doug_system.dat"}
+    with open(os.path.join(folder, files["info_file"]), "wb") as fh:
+        _fortran_record(fh, np.array([info["nell"], ngf, info["nsd"], info["mfrelt"], info["nnode"]],
+                                     dtype="<i4").tobytes())
+    with open(os.path.join(folder, files["freedom_lists_file"]), "wb") as fh:
+        for e in range(len(eptr) - 1):
+            fr = np.asarray(efree[eptr[e]:eptr[e + 1]], dtype="<i4")
+            _fortran_record(fh, np.array([len(fr)], dtype="<i4").tobytes() + fr.tobytes())
+    with open(os.path.join(folder, files["elemmat_rhs_file"]), "wb") as fh:
+        off = 0
+        for e in range(len(eptr) - 1):
+            nf = int(eptr[e + 1] - eptr[e])
+            for j in range(nf):
+                _fortran_record(fh, np.asarray(emat[off + j * nf: off + (j + 1) * nf], dtype="<f8").tobytes())
+            off += nf * nf
+            _fortran_record(fh, np.asarray(erhs[eptr[e]:eptr[e + 1]], dtype="<f8").tobytes())
+    return files
 
 
 def gaussian_field_3d(N: int, sigma: float = 1.0, corr: float = 8.0, seed: int = 0):

@@ -19,6 +19,12 @@
  *                                   (src/datatypes/SpMtx/SpMtx_class.F90:410-453,
  *                                    src/datatypes/Vect.F90:840-947,
  *                                    src/components/Distribution_assm.F90:49-102)
+ *   dg_set_elements, and dg_load_ctl with input_type 1
+ *                                -> Mesh_initFromFile, Mesh_readFileFreelists,
+ *                                   ElemMtxs_readAndDistribute and the one-process
+ *                                   element assembly (src/datatypes/Mesh.F90:293-460,
+ *                                   src/datatypes/ElemMtxs/ElemMtxs_distribute.F90:509-631,
+ *                                   src/datatypes/ElemMtxs/ElemMtxs_assemble.F90:82-289)
  *   dg_set_partition             -> the partition import of the debug 4321
  *                                   path (src/components/Distribution_assm.F90:202-215)
  *   dg_setup                     -> Partitionings_aggr_InitFine/InitCoarse,
@@ -89,14 +95,26 @@ const char *dg_last_error(const dg_handle *h);
  * factors with flexible CG and FP64 residual replacement), replace_every,
  * omega (prolongator smoother weight; the reference hard-codes 1/3). */
 dg_status dg_set_option(dg_handle *h, const char *name, const char *value);
-/* Parse a control file and read the input files it names (assembled
- * matrix + optional RHS; relative names resolve against the file's folder). */
+/* Parse a control file and read the input files it names: input_type 2,
+ * the assembled matrix + optional RHS; input_type 1, the info, freedom-list
+ * and element-matrix files (assembled as one DOUG process assembles them).
+ * Relative names resolve against the control file's folder. */
 dg_status dg_load_ctl(dg_handle *h, const char *path);
 
 /* Assembled matrix as 1-based COO triplets in any order (0-based accepted,
  * as in the reference's reader); duplicates are summed. */
 dg_status dg_set_matrix_coo(dg_handle *h, int n, int nnz, const int *rows, const int *cols,
                             const double *vals);
+/* Elemental input held in memory: nell elements over ngf global freedoms;
+ * element e has the 1-based freedoms efree[eptr[e] .. eptr[e+1]), its
+ * nf x nf matrix (nf = eptr[e+1] - eptr[e]) column by column in emat (the
+ * elements one after another) and its right-hand side in erhs (laid out
+ * like efree).  Assembled exactly like the elemental input files: the
+ * unknowns are the used freedoms in increasing order (an element may have
+ * no freedoms), entries sum the
+ * elements' non-zero values in element order, b sums the elements' RHS. */
+dg_status dg_set_elements(dg_handle *h, int nell, int ngf, const int *eptr, const int *efree,
+                          const double *emat, const double *erhs);
 /* Right-hand side (n values); without one, b = 1 as in the reference. */
 dg_status dg_set_rhs(dg_handle *h, const double *b);
 /* Optional subdomain partition: part[i] in 1..nparts for every unknown.
@@ -152,6 +170,11 @@ dg_status dg_get_subdomains(const dg_handle *h, long long *starts /* nsubd+1 */,
 /* R and AC in the reference's final entry order (COO, 1-based). */
 dg_status dg_get_restriction(const dg_handle *h, int *ri, int *rj, double *rv);
 dg_status dg_get_coarse_matrix(const dg_handle *h, int *ci, int *cj, double *cv);
+/* The matrix and right-hand side the handle holds (after dg_set_matrix_coo,
+ * dg_set_elements or dg_load_ctl), as given or as assembled from elements:
+ * 1-based COO in entry order.  NULL arrays are skipped (ask for n, nnz first). */
+dg_status dg_get_input(const dg_handle *h, int *n, int *nnz, int *rows, int *cols, double *vals,
+                       double *rhs);
 
 #ifdef __cplusplus
 }

@@ -85,6 +85,7 @@ typedef struct {
   char solution_file[300];
   int solution_format;
   int start_vec_type;
+  char info_file[300], freedom_lists_file[300], elemmat_rhs_file[300];
 } ctl_t;
 
 static void ctl_defaults(ctl_t *c) {
@@ -209,6 +210,7 @@ static void ctl_action(ctl_t *c, const char *w1, const char *w2) {
   SETS(assembled_mtx_file) SETI(assembled_mtx_format)
   SETS(assembled_rhs_file) SETI(assembled_rhs_format)
   SETS(solution_file) SETI(solution_format) SETI(start_vec_type)
+  SETS(info_file) SETS(freedom_lists_file) SETS(elemmat_rhs_file)
 }
 
 /* CtrlData_initFromFile (DOUG_utils.F90:629-696), on text. */
@@ -768,7 +770,9 @@ static void spm_aggregate(spm *A, aggrs *inner, aggrs *full, int neighood,
     }
     free(nextgoodstart); free(distance); free(nodes); free(stat);
   } else {
-    /* Cartesian aggregates (:332-346) */
+    /* Cartesian aggregates (:332-346); a radius below 1 is an integer
+     * division fault in the reference */
+    if (neighood < 1) orc_abort("Cartesian aggregation needs an aggregation radius >= 1 (radius %d)", neighood);
     int nsa = (sn + neighood - 1) / neighood;
     k = 0;
     for (i = 1; i <= sn; i++)
@@ -2042,6 +2046,170 @@ int orc_write_solution(const char *path, int format, int n, const double *x) {
   return 0;
 }
 
+/* ------------------------------------------------------------------ */
+/* Elemental input, one process.  Restates Mesh_initFromFile and
+ * Mesh_readFileFreelists (src/datatypes/Mesh.F90:293-460), the element loop of
+ * ElemMtxs_readAndDistribute (src/datatypes/ElemMtxs/ElemMtxs_distribute.F90:548-575),
+ * the one-partition local numbering of Mesh_MapsAndNghbrs (Mesh.F90:1131-1193)
+ * and ElemMtxsAssembleContext_addChunk / _extractSpMtx / _extractVect
+ * (src/datatypes/ElemMtxs/ElemMtxs_assemble.F90:158-289), with the sorted
+ * per-row index map of src/datatypes/IdxMap.f90:108-182. */
+typedef struct { int size, cap; int *key, *val; } idxmap_t;
+
+static int idxmap_pos(const idxmap_t *m, int k) { /* first position with key >= k */
+  int lo = 0, hi = m->size;
+  while (lo < hi) { int mid = (lo + hi) / 2; if (m->key[mid] < k) lo = mid + 1; else hi = mid; }
+  return lo;
+}
+static int idxmap_lookup(const idxmap_t *m, int k) {
+  int p = idxmap_pos(m, k);
+  return (p < m->size && m->key[p] == k) ? m->val[p] : -1;
+}
+static void idxmap_insert(idxmap_t *m, int k, int x) {
+  int p = idxmap_pos(m, k);
+  if (p < m->size && m->key[p] == k) return;
+  if (m->size + 1 > m->cap) {
+    m->cap = m->size * 4 / 3 + 4;
+    m->key = (int *)realloc(m->key, sizeof(int) * (size_t)m->cap);
+    m->val = (int *)realloc(m->val, sizeof(int) * (size_t)m->cap);
+  }
+  memmove(m->key + p + 1, m->key + p, sizeof(int) * (size_t)(m->size - p));
+  memmove(m->val + p + 1, m->val + p, sizeof(int) * (size_t)(m->size - p));
+  m->key[p] = k;
+  m->val[p] = x;
+  m->size++;
+}
+
+/* out: n local freedoms, 1-based COO (indi = column freedom, indj = row,
+ * the reference's flip), rhs.  Returns 0 or a negative error code. */
+int orc_read_elemental(const char *info, const char *freel, const char *elemmat, int nblocks,
+                       int *n_out, int *nnz_out, int **ii_out, int **jj_out, double **vv_out,
+                       double **rhs_out) {
+  long len, pos, rl;
+  unsigned char *own;
+  const unsigned char *r;
+  unsigned char *buf = slurp(info, &len);
+  if (!buf) return -1;
+  pos = 0;
+  r = fort_record(buf, len, &pos, &rl, &own);
+  if (!r || rl < 20) { free(buf); free(own); return -2; }
+  int nell = (int32_t)le32(r), ngf = (int32_t)le32(r + 4), mfrelt = (int32_t)le32(r + 12);
+  free(own); free(buf);
+  if (nell <= 0 || ngf <= 0 || mfrelt <= 0) return -2;
+  /* freedom lists: record = nfrelt, mhead(1:nfrelt) */
+  int *nfrelt = (int *)calloc((size_t)nell, sizeof(int));
+  int *mhead = (int *)calloc((size_t)nell * (size_t)mfrelt, sizeof(int)); /* mhead(i,e) = [e*mfrelt+i-1] */
+  buf = slurp(freel, &len);
+  if (!buf) { free(nfrelt); free(mhead); return -3; }
+  pos = 0;
+  for (int e = 0; e < nell; e++) {
+    r = fort_record(buf, len, &pos, &rl, &own);
+    if (!r || rl < 4) { free(own); free(buf); free(nfrelt); free(mhead); return -3; }
+    int nf = (int32_t)le32(r);
+    if (nf < 0 || nf > mfrelt || rl < 4 + 4L * nf) { free(own); free(buf); free(nfrelt); free(mhead); return -3; }
+    nfrelt[e] = nf;
+    for (int i = 0; i < nf; i++) mhead[(size_t)e * mfrelt + i] = (int32_t)le32(r + 4 + 4 * i);
+    free(own);
+  }
+  free(buf);
+  if (nblocks > 1) { /* Mesh.F90:313-319: ngf = maxval(mhead) */
+    int mx = 0;
+    for (int e = 0; e < nell; e++)
+      for (int i = 0; i < nfrelt[e]; i++) if (mhead[(size_t)e * mfrelt + i] > mx) mx = mhead[(size_t)e * mfrelt + i];
+    ngf = mx;
+  }
+  for (int e = 0; e < nell; e++)
+    for (int i = 0; i < nfrelt[e]; i++) {
+      int g = mhead[(size_t)e * mfrelt + i];
+      if (g < 1 || g > ngf) { free(nfrelt); free(mhead); return -4; }
+    }
+  /* one partition: a freedom is local iff some element has it; local
+   * numbers in increasing global order, all inner (inv_perm_map = identity) */
+  int *gl = (int *)calloc((size_t)ngf + 1, sizeof(int));
+  for (int e = 0; e < nell; e++)
+    for (int i = 0; i < nfrelt[e]; i++) gl[mhead[(size_t)e * mfrelt + i]] = 1;
+  int nlf = 0;
+  for (int g = 1; g <= ngf; g++) if (gl[g]) gl[g] = ++nlf;
+  idxmap_t *maps = (idxmap_t *)calloc((size_t)nlf + 1, sizeof(idxmap_t)); /* 1-based rows */
+  double *val = NULL, *rhs = (double *)calloc((size_t)nlf + 1, sizeof(double));
+  long nval = 0, cap = 0;
+  buf = slurp(elemmat, &len);
+  if (!buf) { free(gl); free(maps); free(rhs); free(nfrelt); free(mhead); return -5; }
+  pos = 0;
+  double *elem = (double *)malloc(sizeof(double) * (size_t)mfrelt * (size_t)mfrelt);
+  double *erhs = (double *)malloc(sizeof(double) * (size_t)mfrelt);
+  int bad = 0;
+  for (int e = 0; e < nell && !bad; e++) {
+    int nf = nfrelt[e];
+    for (int j = 1; j <= nf && !bad; j++) { /* record j: elem(1:nf, j) */
+      r = fort_record(buf, len, &pos, &rl, &own);
+      if (!r || rl < 8L * nf) bad = 1;
+      else for (int k = 1; k <= nf; k++) elem[(size_t)(j - 1) * nf + (k - 1)] = led(r + 8 * (k - 1));
+      free(own);
+    }
+    if (bad) break;
+    r = fort_record(buf, len, &pos, &rl, &own);
+    if (!r || rl < 8L * nf) { free(own); bad = 1; break; }
+    for (int k = 1; k <= nf; k++) erhs[k - 1] = led(r + 8 * (k - 1));
+    free(own);
+    /* ElemMtxsAssembleContext_addChunk, one element */
+    for (int i = 1; i <= nf; i++) {
+      int lf = gl[mhead[(size_t)e * mfrelt + i - 1]];
+      for (int j = 1; j <= nf; j++) {
+        double a = elem[(size_t)(j - 1) * nf + (i - 1)];
+        if (a == 0.0) continue;
+        int collf = gl[mhead[(size_t)e * mfrelt + j - 1]];
+        int idx = idxmap_lookup(&maps[lf], collf);
+        if (idx == -1) {
+          nval++;
+          idx = (int)nval;
+          if (cap < nval) {
+            long nc = nval * 4 / 3 + 16;
+            val = (double *)realloc(val, sizeof(double) * (size_t)(nc + 1));
+            for (long q = cap + 1; q <= nc; q++) val[q] = 0.0;
+            cap = nc;
+          }
+          idxmap_insert(&maps[lf], collf, idx);
+        }
+        val[idx] = val[idx] + a;
+      }
+      rhs[lf] = rhs[lf] + erhs[i - 1];
+    }
+  }
+  free(buf); free(elem); free(erhs);
+  if (bad) {
+    for (int i = 1; i <= nlf; i++) { free(maps[i].key); free(maps[i].val); }
+    free(maps); free(val); free(rhs); free(gl); free(nfrelt); free(mhead);
+    return -5;
+  }
+  /* _extractSpMtx: rows in order, keys ascending, indi = key, indj = row */
+  int *ii = (int *)malloc(sizeof(int) * (size_t)(nval + 1));
+  int *jj = (int *)malloc(sizeof(int) * (size_t)(nval + 1));
+  double *vv = (double *)malloc(sizeof(double) * (size_t)(nval + 1));
+  long bbe = 0;
+  for (int i = 1; i <= nlf; i++)
+    for (int k = 0; k < maps[i].size; k++) {
+      int jkey = maps[i].key[k];
+      vv[bbe] = val[idxmap_lookup(&maps[i], jkey)];
+      ii[bbe] = jkey;
+      jj[bbe] = i;
+      bbe++;
+    }
+  double *b = (double *)malloc(sizeof(double) * (size_t)(nlf + 1));
+  for (int i = 0; i < nlf; i++) b[i] = rhs[i + 1];
+  for (int i = 1; i <= nlf; i++) { free(maps[i].key); free(maps[i].val); }
+  free(maps); free(val); free(rhs); free(gl); free(nfrelt); free(mhead);
+  *n_out = nlf;
+  *nnz_out = (int)nval;
+  *ii_out = ii;
+  *jj_out = jj;
+  *vv_out = vv;
+  *rhs_out = b;
+  return 0;
+}
+
+void orc_free_buffers(void *a, void *b, void *c, void *d) { free(a); free(b); free(c); free(d); }
+
 int orc_run_ctl(const char *ctl_path, const char *overrides, orc_result **out) {
   *out = NULL;
   long len = 0;
@@ -2078,6 +2246,21 @@ int orc_run_ctl(const char *ctl_path, const char *overrides, orc_result **out) {
   }
   ctl_defaults(&c);
   ctl_parse_text(&c, all);
+  if (c.input_type == 1) { /* elemental input (Distribution.F90:62-64) */
+    char ip[1400], fp[1400], ep[1400];
+#define ORC_PATH(dst, name) \
+    if (name[0] == '/') snprintf(dst, sizeof dst, "%s", name); else snprintf(dst, sizeof dst, "%s/%s", dir, name);
+    ORC_PATH(ip, c.info_file) ORC_PATH(fp, c.freedom_lists_file) ORC_PATH(ep, c.elemmat_rhs_file)
+#undef ORC_PATH
+    int n, nnz, *ii, *jj;
+    double *vv, *rhs;
+    rc = orc_read_elemental(ip, fp, ep, c.number_of_blocks, &n, &nnz, &ii, &jj, &vv, &rhs);
+    if (rc) orc_abort("Unable to read elemental input (%d)", rc);
+    rc = orc_run_coo(n, nnz, ii, jj, vv, rhs, all, NULL, 0, &r);
+    free(ii); free(jj); free(vv); free(rhs); free(all);
+    *out = r;
+    return rc;
+  }
   if (c.input_type != 2) orc_abort("input_type %d not supported by the oracle", c.input_type);
   char mpath[1400], rpath[1400];
   if (c.assembled_mtx_file[0] == '/') snprintf(mpath, sizeof mpath, "%s", c.assembled_mtx_file);

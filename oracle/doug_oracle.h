@@ -66,6 +66,12 @@ typedef struct orc_result {
  * repeated word, so overrides win).  `workdir` resolves relative file names
  * (NULL: directory of the control file). */
 int orc_run_ctl(const char *ctl_path, const char *overrides, orc_result **out);
+/* Elemental input files (input_type 1) assembled as one DOUG process does;
+ * 1-based COO with the reference's flipped indices, malloc'ed (free with
+ * orc_free_buffers). */
+int orc_read_elemental(const char *info, const char *freel, const char *elemmat, int nblocks,
+                       int *n, int *nnz, int **ii, int **jj, double **vv, double **rhs);
+void orc_free_buffers(void *a, void *b, void *c, void *d);
 
 /* Run the full path on an in-memory matrix given as COO triplets (1-based,
  * any order, as in the assembled text format), rhs (NULL -> b = 1),

@@ -69,6 +69,10 @@ def lib():
             L.orc_read_assembled.argtypes = [C.c_char_p, C.c_int, P(C.c_int), P(C.c_int),
                                              P(P(C.c_int)), P(P(C.c_int)), P(P(C.c_double))]
             L.orc_read_vector.argtypes = [C.c_char_p, C.c_int, C.c_int, P(C.c_double)]
+            L.orc_read_elemental.argtypes = [C.c_char_p, C.c_char_p, C.c_char_p, C.c_int, P(C.c_int),
+                                             P(C.c_int), P(P(C.c_int)), P(P(C.c_int)),
+                                             P(P(C.c_double)), P(P(C.c_double))]
+            L.orc_free_buffers.argtypes = [C.c_void_p] * 4
             L.orc_write_solution.argtypes = [C.c_char_p, C.c_int, C.c_int, P(C.c_double)]
             L.orc_spd_solve.argtypes = [C.c_int, C.c_int, P(C.c_int), P(C.c_int), P(C.c_double),
                                         P(C.c_double), P(C.c_double)]
@@ -185,6 +189,25 @@ def read_assembled(path, fmt=0):
         raise IOError(f"oracle could not read {path}: {rc}")
     m = max(n.value, nnz.value)
     return (n.value, nnz.value, _arr(ii, m, np.int32), _arr(jj, m, np.int32), _arr(vv, m, np.float64))
+
+
+def read_elemental(info, freelists, elemmat, number_of_blocks=1):
+    """Elemental input files assembled as one DOUG process assembles them:
+    (n, rows1, cols1, vals, rhs), the COO in the reference's entry order."""
+    L = lib()
+    n, nnz = C.c_int(), C.c_int()
+    ii, jj = C.POINTER(C.c_int)(), C.POINTER(C.c_int)()
+    vv, bb = C.POINTER(C.c_double)(), C.POINTER(C.c_double)()
+    rc = L.orc_read_elemental(info.encode(), freelists.encode(), elemmat.encode(), int(number_of_blocks),
+                              C.byref(n), C.byref(nnz), C.byref(ii), C.byref(jj), C.byref(vv), C.byref(bb))
+    if rc:
+        raise RuntimeError(f"orc_read_elemental failed ({rc})")
+    out = (n.value, np.ctypeslib.as_array(ii, (nnz.value,)).copy(),
+           np.ctypeslib.as_array(jj, (nnz.value,)).copy(), np.ctypeslib.as_array(vv, (nnz.value,)).copy(),
+           np.ctypeslib.as_array(bb, (n.value,)).copy())
+    L.orc_free_buffers(C.cast(ii, C.c_void_p), C.cast(jj, C.c_void_p), C.cast(vv, C.c_void_p),
+                       C.cast(bb, C.c_void_p))
+    return out
 
 
 def read_vector(path, fmt, n):

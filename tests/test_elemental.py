@@ -1,0 +1,155 @@
+"""Elemental input (input_type 1): DOUG's mesh / element-matrix files and the
+in-memory element API, assembled the way one DOUG process assembles them.
+
+The reference fixture tests/elemental/e4x4 (copied byte for byte into
+tests/golden/e4x4) pins the final solution; the assembled matrix (entries,
+their order, the row/column flip of ElemMtxs_assemble.F90:262-266) is pinned
+by the product's host assembly and the oracle's restatement agreeing bit for
+bit.  The GPU cases solve through the C ABI and compare with the fixture and
+with the oracle.
+"""
+import os
+
+import numpy as np
+import pytest
+
+import oracle as O
+import doug_gb300 as D
+from doug_gb300 import problems as P
+
+from conftest import GOLDEN
+
+E4 = os.path.join(GOLDEN, "e4x4")
+# the fixture's control file leaves strong1 and radius1/2 unset: the fine
+# level then takes the Cartesian branch (9 = 3^2) and the coarse default
+# radius rounds to 0 on 4 coarse nodes; radius2 1 (or a strength threshold)
+# gives a defined aggregation, as the reference harness's aggregation runs set
+E4_EXTRA = dict(radius1=2, radius2=1)
+
+
+def _ctl_text(d):
+    return "".join(f"{k} {v}\n" for k, v in d.items())
+
+
+def _oracle_e4():
+    return O.read_elemental(os.path.join(E4, "doug_info.dat"), os.path.join(E4, "doug_element.dat"),
+                            os.path.join(E4, "doug_system.dat"))
+
+
+def test_e4x4_assembly_product_equals_oracle():
+    n, ii, jj, vv, b = _oracle_e4()
+    assert n == 9 and len(vv) == 49
+    s = D.DougSolver({})
+    s.load_ctl(os.path.join(E4, "DOUG.ctl"))
+    n2, r2, c2, v2, b2 = s.input_matrix()
+    assert n2 == n
+    assert np.array_equal(r2, ii) and np.array_equal(c2, jj)
+    assert np.array_equal(v2.view(np.int64), vv.view(np.int64))  # bit for bit
+    assert np.array_equal(b2.view(np.int64), b.view(np.int64))
+    # the reference's flip: entries come row by row with the row in indj
+    assert np.all(np.diff(jj) >= 0)
+
+
+@pytest.mark.parametrize("levels,smoothers,overlap",
+                         [(1, 0, o) for o in (-1, 0, 1, 2)] + [(2, s, o) for s in (0, 1, 2) for o in (-1, 0)])
+def test_e4x4_oracle_matches_fixture(levels, smoothers, overlap):
+    ref = O.read_vector(os.path.join(E4, "csolution.xdr"), 2, 9)
+    opts = dict(fine_method=1, levels=levels, smoothers=smoothers, overlap=overlap, **E4_EXTRA)
+    r = O.run_ctl(os.path.join(E4, "DOUG.ctl"), _ctl_text(opts))
+    assert r.get("status", 0) == 0, r
+    assert np.linalg.norm(r["x"] - ref) <= 1e-6          # the harness rule
+    assert np.linalg.norm(r["x"] - ref) <= 1e-12 * np.linalg.norm(ref) + 1e-14
+
+
+def test_cartesian_radius_zero_is_an_input_error():
+    # the reference divides by the radius (SpMtx_aggregation.F90:334-338)
+    opts = dict(fine_method=1, levels=2, smoothers=0, overlap=-1, radius1=2)
+    r = O.run_ctl(os.path.join(E4, "DOUG.ctl"), _ctl_text(opts))
+    assert r["status"] != 0 and "radius" in r["errmsg"]
+    s = D.DougSolver(opts)
+    s.load_ctl(os.path.join(E4, "DOUG.ctl"))
+    with pytest.raises(D.DougError) as ei:
+        s.setup_host_only()
+    assert ei.value.status == D.DG_BAD_INPUT and "radius" in str(ei.value)
+
+
+def _p1_elements(nodes=17, seed=3, kappa=False):
+    rng = np.random.default_rng(seed + 100)
+    ntri = 2 * (nodes - 1) ** 2
+    k = np.exp(0.5 * rng.standard_normal(ntri)) if kappa else None
+    return P.poisson2d_p1_elements(nodes=nodes, seed=seed, kappa=k)
+
+
+@pytest.mark.parametrize("kappa", [False, True])
+def test_elements_files_memory_and_oracle_agree(tmp_path, kappa):
+    ngf, eptr, efree, emat, erhs, info = _p1_elements(kappa=kappa)
+    assert np.any(np.diff(eptr) == 0)  # corner triangles carry no freedom
+    files = P.write_elemental_files(str(tmp_path), ngf, eptr, efree, emat, erhs, info)
+    n, ii, jj, vv, b = O.read_elemental(*(str(tmp_path / files[k]) for k in
+                                          ("info_file", "freedom_lists_file", "elemmat_rhs_file")))
+    assert n == ngf
+    ctl = tmp_path / "DOUG.ctl"
+    ctl.write_text("input_type 1\n" + _ctl_text(files))
+    s = D.DougSolver({})
+    s.load_ctl(str(ctl))
+    got_f = s.input_matrix()
+    s2 = D.DougSolver({})
+    s2.set_elements(ngf, eptr, efree, emat, erhs)
+    got_m = s2.input_matrix()
+    for got in (got_f, got_m):
+        assert got[0] == n
+        assert np.array_equal(got[1], ii) and np.array_equal(got[2], jj)
+        assert np.array_equal(got[3].view(np.int64), vv.view(np.int64))
+        assert np.array_equal(got[4].view(np.int64), b.view(np.int64))
+    # the element sums equal the assembled operator up to rounding
+    na, ra, ca, va, ba, _ = P.poisson2d_p1(nodes=17, seed=3) if not kappa else (None,) * 6
+    if not kappa:
+        import scipy.sparse as sp
+        A1 = sp.csr_matrix((va, (ra - 1, ca - 1)), shape=(na, na)).toarray()
+        A2 = sp.csr_matrix((vv, (ii - 1, jj - 1)), shape=(n, n)).toarray()
+        assert np.abs(A1 - A2).max() <= 1e-12 * np.abs(A1).max()
+
+
+def test_elements_bad_input():
+    s = D.DougSolver({})
+    with pytest.raises(D.DougError):
+        s.set_elements(3, [0, 2, 1], [1, 2, 3], np.ones(5), np.ones(3))  # offsets decrease
+    with pytest.raises(D.DougError):
+        s.set_elements(2, [0, 2], [1, 3], np.ones(4), np.ones(2))        # freedom 3 > ngf
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("levels,smoothers,overlap", [(1, 0, -1), (1, 0, 2), (2, 0, -1), (2, 1, 0), (2, 2, -1)])
+def test_e4x4_gpu_matches_fixture_and_oracle(levels, smoothers, overlap):
+    ref = O.read_vector(os.path.join(E4, "csolution.xdr"), 2, 9)
+    opts = dict(solver=2, method=1, fine_method=1, levels=levels, smoothers=smoothers, overlap=overlap,
+                **E4_EXTRA)
+    s = D.DougSolver(opts)
+    s.load_ctl(os.path.join(E4, "DOUG.ctl"))
+    s.setup()
+    x, st = s.solve()
+    assert np.linalg.norm(x - ref) <= 1e-9
+    ro = O.run_ctl(os.path.join(E4, "DOUG.ctl"), _ctl_text(opts))
+    assert abs(st.iterations - ro["iterations"]) <= 1
+    assert np.linalg.norm(x - ro["x"]) <= 1e-10 * np.linalg.norm(ro["x"])
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision", [0, 1])
+def test_elements_p1_gpu_vs_oracle(precision):
+    ngf, eptr, efree, emat, erhs, info = _p1_elements(nodes=49, seed=5, kappa=True)
+    opts = dict(solver=2, method=1, fine_method=1, levels=2, smoothers=1, overlap=1, strong1="0.08",
+                radius1=2, solve_tolerance="1.0e-10", solve_maxiters=500)
+    s = D.DougSolver(opts)
+    if precision:
+        s.set_option("precision", precision)
+    s.set_elements(ngf, eptr, efree, emat, erhs)
+    n, r, c, v, b = s.input_matrix()
+    s.setup()
+    x, st = s.solve()
+    ro = O.run_coo(n, r, c, v, rhs=b, ctl=_ctl_text(opts))
+    if precision == 0:
+        assert abs(st.iterations - ro["iterations"]) <= 1
+        assert np.linalg.norm(x - ro["x"]) <= 1e-10 * np.linalg.norm(ro["x"])
+    else:
+        assert np.linalg.norm(x - ro["x"]) <= 1e-7 * np.linalg.norm(ro["x"])
