@@ -670,6 +670,24 @@ mf_fwd_big(MfView v, const int2 *__restrict__ tasks, const T *__restrict__ E, co
   const int m = v.f_m[f], k = v.f_k[f], ld = round4(m);
   const int64_t xo = v.f_xoff[f] + v.f_p0[f];
   const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+  const T *Ef = E + v.e_off[f];
+  // one batch: columns j + u*NW (u < UN) of the chunk's rows of this lane;
+  // a vector wholly above E's diagonal (rb + VN <= column) is zero
+  T e[UN][VN];
+  auto load_batch = [&](int r0, int K, int j) {
+    const int rb = r0 + lane * VN;
+#pragma unroll
+    for (int u = 0; u < UN; u++) {
+      const int jj = j + u * NW;
+      if (rb < m && jj < K && rb + VN > jj) Vec16<T>::load(Ef + (int64_t)jj * ld + rb, e[u]);
+      else {
+#pragma unroll
+        for (int q = 0; q < VN; q++) e[u][q] = T(0);
+      }
+    }
+  };
+  auto chunk_cols = [&](int r0) { return r0 < k ? min(k, r0 + RC) : k; };
+  load_batch(ch0 * RC, chunk_cols(ch0 * RC), wid);  // in flight while b is assembled
   for (int i = tid; i < m; i += NT) b[i] = i < k ? xl[xo + i] : T(0);
   __syncthreads();
   for (int ci = v.f_child_ptr[f]; ci < v.f_child_ptr[f + 1]; ci++) {
@@ -680,43 +698,21 @@ mf_fwd_big(MfView v, const int2 *__restrict__ tasks, const T *__restrict__ E, co
     for (int a = tid; a < rc; a += NT) b[rel[a]] += u[a];
     __syncthreads();
   }
-  const T *Ef = E + v.e_off[f];
   T *uf = uvec + v.f_uoff[f];
   for (int ch = ch0; ch < ch0 + nch; ch++) {
     const int r0 = ch * RC;
-    const int K = r0 < k ? min(k, r0 + RC) : k;
-    const int rb = r0 + lane * VN;
+    const int K = chunk_cols(r0);
     T acc[VN];
 #pragma unroll
     for (int q = 0; q < VN; q++) acc[q] = T(0);
-    if (rb < m) {
-      const T *Er = Ef + rb;
-      int j = wid;
-      for (; j + (UN - 1) * NW < K; j += UN * NW) {
-        T e[UN][VN];
+    for (int j = wid; j < K; j += UN * NW) {
+      if (ch != ch0 || j != wid) load_batch(r0, K, j);
 #pragma unroll
-        for (int u = 0; u < UN; u++) {
-          if (rb + VN > j + u * NW) Vec16<T>::load(Er + (int64_t)(j + u * NW) * ld, e[u]);
-          else {
+      for (int u = 0; u < UN; u++) {
+        const int jj = j + u * NW;
+        const T bj = jj < K ? b[jj] : T(0);  // b holds rows [0, m): columns past K are not read
 #pragma unroll
-            for (int q = 0; q < VN; q++) e[u][q] = T(0);
-          }
-        }
-#pragma unroll
-        for (int u = 0; u < UN; u++) {
-          const T bj = b[j + u * NW];
-#pragma unroll
-          for (int q = 0; q < VN; q++) acc[q] += e[u][q] * bj;
-        }
-      }
-      for (; j < K; j += NW) {
-        if (rb + VN > j) {
-          T e[VN];
-          Vec16<T>::load(Er + (int64_t)j * ld, e);
-          const T bj = b[j];
-#pragma unroll
-          for (int q = 0; q < VN; q++) acc[q] += e[q] * bj;
-        }
+        for (int q = 0; q < VN; q++) acc[q] += e[u][q] * bj;
       }
     }
 #pragma unroll
@@ -750,36 +746,39 @@ mf_bwd_big(MfView v, const int2 *__restrict__ tasks, const T *__restrict__ E, co
   const T *xb = xl + v.f_xoff[f];
   const int *rows = v.rows + v.f_rows[f];
   const int tid = threadIdx.x;
+  const int rq = tid % LPC, cs = tid / LPC;
+  // one batch: rows i + 32u (u < UN) of column c for this lane; a vector
+  // wholly above E's diagonal (i + VN <= c) is zero
+  T e[UN][VN];
+  auto load_batch = [&](int c, int i) {
+    const T *Ec = E + v.e_off[f] + (int64_t)c * ld;
+#pragma unroll
+    for (int u = 0; u < UN; u++) {
+      const int ii = i + u * 32;
+      if (c - c0 < jb && ii < m && ii + VN > c) Vec16<T>::load(Ec + ii, e[u]);
+      else {
+#pragma unroll
+        for (int q = 0; q < VN; q++) e[u][q] = T(0);
+      }
+    }
+  };
+  load_batch(c0 + cs, c0 + rq * VN);  // in flight while v is gathered
   for (int i = c0 + tid; i < ld; i += NT) w[i - c0] = i < k ? yl[xo + i] : (i < m ? xb[rows[i]] : T(0));
   __syncthreads();
-  const int rq = tid % LPC, cs = tid / LPC;
   for (int cc = cs; cc < 32; cc += NCS) {  // uniform trip count: the shuffles below need whole groups
     const int c = c0 + cc;
     T s = T(0);
     if (cc < jb) {
-      const T *Ec = E + v.e_off[f] + (int64_t)c * ld;
-      int i = c0 + rq * VN;
-      for (; i + (UN - 1) * 32 < m; i += UN * 32) {
-        T e[UN][VN];
+      for (int i = c0 + rq * VN; i < m; i += UN * 32) {
+        if (cc != cs || i != c0 + rq * VN) load_batch(c, i);
 #pragma unroll
         for (int u = 0; u < UN; u++) {
-          if (i + u * 32 + VN > c) Vec16<T>::load(Ec + i + u * 32, e[u]);
-          else {
+          const int ii = i + u * 32;  // w holds rows [c0, ld): rows past m are not read
+          if (ii < m) {
 #pragma unroll
-            for (int q = 0; q < VN; q++) e[u][q] = T(0);
+            for (int q = 0; q < VN; q++) s += e[u][q] * w[ii + q - c0];
           }
         }
-#pragma unroll
-        for (int u = 0; u < UN; u++)
-#pragma unroll
-          for (int q = 0; q < VN; q++) s += e[u][q] * w[i + u * 32 + q - c0];
-      }
-      for (; i < m; i += 32) {
-        if (i + VN <= c) continue;
-        T e[VN];
-        Vec16<T>::load(Ec + i, e);
-#pragma unroll
-        for (int q = 0; q < VN; q++) s += e[q] * w[i + q - c0];
       }
     }
 #pragma unroll
