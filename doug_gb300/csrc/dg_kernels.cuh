@@ -402,15 +402,19 @@ mf_panel(MfView v, const int2 *__restrict__ tasks, int npanel, const int2 *__res
   }
 }
 
-// one 64x64 tile after the panel at j0: either a tile of the trailing update
-// (task = {front, (ti << 16) | tj}, tiles relative to column j0 + jb) or, for
-// blockIdx.x >= nupd, a tile of the E update E[c0:m, 0:c0] -= L[c0:m, J] E_J
-// (task = {front, (ti << 16) | tc}, rows relative to c0 = j0 + jb, columns
-// from 0); the columns of block J are assigned, the earlier ones accumulated
+// One 64x64 tile of an update with the L columns [jl, jl + K), K = min(kw, k - jl).
+// Trailing-update tiles (task = {front, (ti << 16) | tj}, ti >= tj) cover rows
+// and columns from c0 = jl + K: C -= L[rows, J] L[cols, J]^T (lower part),
+// only columns below cend = min(cend_base, k) when cend_base > 0 (the update
+// inside a 128-column super-panel), all columns otherwise (the trailing update
+// of the whole super-panel, K up to 128, staged 32 columns at a time).  For
+// blockIdx.x >= nupd (single-panel steps only) the tile belongs to the E update
+// E[c0:m, 0:c0] -= L[c0:m, J] E_J (task = {front, (ti << 16) | tc}, columns
+// from 0); the columns of block J are assigned, the earlier ones accumulated.
 template <typename T>
 __global__ void __launch_bounds__(kMfThreads)
-mf_update(MfView v, const int2 *__restrict__ tasks, int nupd, const int2 *__restrict__ etasks, int j0,
-          T *__restrict__ arena, T *__restrict__ E) {
+mf_update(MfView v, const int2 *__restrict__ tasks, int nupd, const int2 *__restrict__ etasks, int jl, int kw,
+          int cend_base, T *__restrict__ arena, T *__restrict__ E) {
   __shared__ T As[kNB][kTile];
   __shared__ T Bs[kNB][kTile + 1];
   const bool etile = (int)blockIdx.x >= nupd;
@@ -418,46 +422,52 @@ mf_update(MfView v, const int2 *__restrict__ tasks, int nupd, const int2 *__rest
   const int f = task.x;
   const int ti = task.y >> 16, tj = task.y & 0xffff;
   const int m = v.f_m[f], k = v.f_k[f];
-  const int jb = min(kNB, k - j0);
+  const int K = min(kw, k - jl);
   T *F = arena + v.f_off[f];
-  const int c0 = j0 + jb;
+  const int c0 = jl + K;
   const int r0 = c0 + ti * kTile;
   const int cc0 = etile ? tj * kTile : c0 + tj * kTile;
+  const int cend = cend_base > 0 ? min(cend_base, k) : m;
   const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
   const int ld = round4(m);
   T *Eg = E + v.e_off[f];
-  for (int q = tid; q < kNB * kTile; q += kMfThreads) {
-    int t = q / kTile, r = q % kTile;
-    As[t][r] = (t < jb && r0 + r < m) ? F[(int64_t)(j0 + t) * m + r0 + r] : T(0);
-  }
-  if (etile) {
-    for (int q = tid; q < kNB * kTile; q += kMfThreads) {
-      const int r = q / kNB, t = q % kNB;
-      Bs[t][r] = (t < jb && cc0 + r < c0) ? Eg[(int64_t)(cc0 + r) * ld + j0 + t] : T(0);
-    }
-  } else {
-    for (int q = tid; q < kNB * kTile; q += kMfThreads) {
-      int t = q / kTile, r = q % kTile;
-      Bs[t][r] = (t < jb && cc0 + r < m) ? F[(int64_t)(j0 + t) * m + cc0 + r] : T(0);
-    }
-  }
-  __syncthreads();
   T acc[4][4];
 #pragma unroll
   for (int a = 0; a < 4; a++)
 #pragma unroll
     for (int b = 0; b < 4; b++) acc[a][b] = T(0);
-  for (int t = 0; t < jb; t++) {
-    T ra[4], rb[4];
+  for (int t0 = 0; t0 < K; t0 += kNB) {
+    const int tb = min(kNB, K - t0);
+    if (t0 > 0) __syncthreads();  // the previous chunk is consumed
+    for (int q = tid; q < kNB * kTile; q += kMfThreads) {
+      int t = q / kTile, r = q % kTile;
+      As[t][r] = (t < tb && r0 + r < m) ? F[(int64_t)(jl + t0 + t) * m + r0 + r] : T(0);
+    }
+    if (etile) {
+      for (int q = tid; q < kNB * kTile; q += kMfThreads) {
+        const int r = q / kNB, t = q % kNB;
+        Bs[t][r] = (t < tb && cc0 + r < c0) ? Eg[(int64_t)(cc0 + r) * ld + jl + t0 + t] : T(0);
+      }
+    } else {
+      for (int q = tid; q < kNB * kTile; q += kMfThreads) {
+        int t = q / kTile, r = q % kTile;
+        Bs[t][r] = (t < tb && cc0 + r < cend) ? F[(int64_t)(jl + t0 + t) * m + cc0 + r] : T(0);
+      }
+    }
+    __syncthreads();
+    for (int t = 0; t < tb; t++) {
+      T ra[4], rb[4];
 #pragma unroll
-    for (int a = 0; a < 4; a++) ra[a] = As[t][tx + 16 * a];
+      for (int a = 0; a < 4; a++) ra[a] = As[t][tx + 16 * a];
 #pragma unroll
-    for (int b = 0; b < 4; b++) rb[b] = Bs[t][ty + 16 * b];
+      for (int b = 0; b < 4; b++) rb[b] = Bs[t][ty + 16 * b];
 #pragma unroll
-    for (int a = 0; a < 4; a++)
+      for (int a = 0; a < 4; a++)
 #pragma unroll
-      for (int b = 0; b < 4; b++) acc[a][b] += ra[a] * rb[b];
+        for (int b = 0; b < 4; b++) acc[a][b] += ra[a] * rb[b];
+    }
   }
+  const int j0 = jl;
   if (etile) {
 #pragma unroll
     for (int b = 0; b < 4; b++) {
@@ -476,7 +486,7 @@ mf_update(MfView v, const int2 *__restrict__ tasks, int nupd, const int2 *__rest
 #pragma unroll
   for (int b = 0; b < 4; b++) {
     const int col = cc0 + ty + 16 * b;
-    if (col >= m) continue;
+    if (col >= cend) continue;
 #pragma unroll
     for (int a = 0; a < 4; a++) {
       const int row = r0 + tx + 16 * a;

@@ -66,6 +66,7 @@ static double wall() {
 // bytes are factored by one CTA each; the others by the multi-CTA pipeline
 constexpr int kPanelFrontRows = 512;
 constexpr size_t kPanelSmem = 96 * 1024;
+constexpr int kSuperPanel = 128;      // columns of L per trailing update of a large front
 constexpr int64_t kFwdTaskBytes = 96 * 1024;  // E bytes per forward task of a large front
 constexpr int64_t kLeanTaskBytes = 80 * 1024; // levels with smaller average tasks use 128-thread CTAs
 
@@ -78,9 +79,13 @@ struct MfDevice {
   DBuf<T> arena, E, xl, yl, u;
   int64_t e_len = 0;
   // per level: small-front range, assembly-task range, steps
+  // a panel step (diag, panel + E rows, update inside the super-panel + E
+  // update; kw = kNB) or a super-panel's trailing update (kw = kSuperPanel,
+  // no diag / panel); cend_base > 0 limits the update to columns < cend_base
   struct Step {
     int j0, diag_off, diag_cnt, panel_off, panel_cnt, esc_off, esc_cnt;
     int upd_off, upd_cnt, etile_off, etile_cnt;
+    int kw, cend_base;
   };
   struct Level {
     int pan_off, pan_cnt, asm_off, asm_cnt;
@@ -161,29 +166,48 @@ struct MfDevice {
         kmax = std::max(kmax, B.f_k[(size_t)f]);
       }
       L.asm_cnt = (int)at.size() - L.asm_off;
-      for (int j0 = 0; j0 < kmax; j0 += kNB) {
-        Step st{j0, (int)df.size(), 0, (int)pf.size(), 0, (int)es.size(), 0,
-                (int)ut.size(), 0, (int)et.size(), 0};
+      // right-looking by super-panels of kSuperPanel columns: each 32-column
+      // panel updates only the rest of its super-panel; the trailing matrix
+      // receives one update with up to kSuperPanel columns of L per super-panel
+      for (int S0 = 0; S0 < kmax; S0 += kSuperPanel) {
+        for (int j0 = S0; j0 < std::min(S0 + kSuperPanel, kmax); j0 += kNB) {
+          Step st{j0, (int)df.size(), 0, (int)pf.size(), 0, (int)es.size(), 0,
+                  (int)ut.size(), 0, (int)et.size(), 0, kNB, S0 + kSuperPanel};
+          for (int f : large) {
+            int m = B.f_m[(size_t)f], k = B.f_k[(size_t)f];
+            if (j0 >= k) continue;
+            df.push_back(f);
+            const int c0 = j0 + std::min(kNB, k - j0);
+            for (int r0 = c0; r0 < m; r0 += kPanelRows) pf.push_back(make_int2(f, r0));
+            for (int e0 = 0; e0 < c0; e0 += EscCols<T>::N) es.push_back(make_int2(f, e0));
+            const int nt = (m - c0 + kTile - 1) / kTile;
+            const int cend = std::min(S0 + kSuperPanel, k);
+            const int ntc = cend > c0 ? (cend - c0 + kTile - 1) / kTile : 0;
+            for (int tj = 0; tj < ntc; tj++)
+              for (int ti = tj; ti < nt; ti++) ut.push_back(make_int2(f, (ti << 16) | tj));
+            const int nte = (c0 + kTile - 1) / kTile;
+            for (int ti = 0; ti < nt; ti++)
+              for (int tc = 0; tc < nte; tc++) et.push_back(make_int2(f, (ti << 16) | tc));
+          }
+          st.diag_cnt = (int)df.size() - st.diag_off;
+          st.panel_cnt = (int)pf.size() - st.panel_off;
+          st.esc_cnt = (int)es.size() - st.esc_off;
+          st.upd_cnt = (int)ut.size() - st.upd_off;
+          st.etile_cnt = (int)et.size() - st.etile_off;
+          L.steps.push_back(st);
+        }
+        Step st{S0, (int)df.size(), 0, (int)pf.size(), 0, (int)es.size(), 0,
+                (int)ut.size(), 0, (int)et.size(), 0, kSuperPanel, 0};
         for (int f : large) {
           int m = B.f_m[(size_t)f], k = B.f_k[(size_t)f];
-          if (j0 >= k) continue;
-          df.push_back(f);
-          const int c0 = j0 + std::min(kNB, k - j0);
-          for (int r0 = c0; r0 < m; r0 += kPanelRows) pf.push_back(make_int2(f, r0));
-          for (int e0 = 0; e0 < c0; e0 += EscCols<T>::N) es.push_back(make_int2(f, e0));
-          int nt = (m - c0 + kTile - 1) / kTile;
+          if (S0 >= k) continue;
+          const int c1 = S0 + std::min(kSuperPanel, k - S0);
+          const int nt = (m - c1 + kTile - 1) / kTile;
           for (int tj = 0; tj < nt; tj++)
             for (int ti = tj; ti < nt; ti++) ut.push_back(make_int2(f, (ti << 16) | tj));
-          int ntc = (c0 + kTile - 1) / kTile;
-          for (int ti = 0; ti < nt; ti++)
-            for (int tc = 0; tc < ntc; tc++) et.push_back(make_int2(f, (ti << 16) | tc));
         }
-        st.diag_cnt = (int)df.size() - st.diag_off;
-        st.panel_cnt = (int)pf.size() - st.panel_off;
-        st.esc_cnt = (int)es.size() - st.esc_off;
         st.upd_cnt = (int)ut.size() - st.upd_off;
-        st.etile_cnt = (int)et.size() - st.etile_off;
-        L.steps.push_back(st);
+        if (st.upd_cnt) L.steps.push_back(st);
       }
     }
     pan_fronts.upload(pn);
@@ -282,8 +306,10 @@ struct MfDevice {
         launches++;
       }
       for (const Step &st : L.steps) {
-        mf_diag<T><<<st.diag_cnt, kMfThreads, 0, s>>>(view, diag_fronts.p + st.diag_off, st.j0, arena.p, status);
-        launches++;
+        if (st.diag_cnt) {
+          mf_diag<T><<<st.diag_cnt, kMfThreads, 0, s>>>(view, diag_fronts.p + st.diag_off, st.j0, arena.p, status);
+          launches++;
+        }
         if (st.panel_cnt + st.esc_cnt) {
           mf_panel<T><<<st.panel_cnt + st.esc_cnt, kMfThreads, 0, s>>>(
               view, panel_tasks.p + st.panel_off, st.panel_cnt, esc_tasks.p + st.esc_off, st.j0, arena.p, E.p);
@@ -291,7 +317,8 @@ struct MfDevice {
         }
         if (st.upd_cnt + st.etile_cnt) {
           mf_update<T><<<st.upd_cnt + st.etile_cnt, kMfThreads, 0, s>>>(
-              view, upd_tasks.p + st.upd_off, st.upd_cnt, etile_tasks.p + st.etile_off, st.j0, arena.p, E.p);
+              view, upd_tasks.p + st.upd_off, st.upd_cnt, etile_tasks.p + st.etile_off, st.j0, st.kw,
+              st.cend_base, arena.p, E.p);
           launches++;
         }
       }
