@@ -906,9 +906,18 @@ dg_status dg_load_ctl(dg_handle *h, const char *path) {
       return fail(h, DG_BAD_INPUT, err);
     return set_elements(h, M);
   }
+  if (c.input_type == 3) {  // generated structured problem (Distribution.F90:67-70)
+    int n = 0;
+    std::vector<int> ii, jj;
+    std::vector<double> vv, b;
+    structured_laplace(c.grid_size, n, ii, jj, vv, b);
+    dg_status st = dg_set_matrix_coo(h, n, (int)vv.size(), ii.data(), jj.data(), vv.data());
+    if (st != DG_OK) return st;
+    return dg_set_rhs(h, b.data());
+  }
   if (c.input_type != 2)
     return fail(h, DG_BAD_INPUT, "input_type " + std::to_string(c.input_type) +
-                                     ": elemental (1) and assembled (2) input are read from control files");
+                                     ": elemental (1), assembled (2) and structured (3) input are supported");
   std::vector<int> ii, jj;
   std::vector<double> vv;
   int n = 0;

@@ -340,6 +340,24 @@ bool read_vector(const std::string &path, int format, int n, std::vector<double>
   return true;
 }
 
+void structured_laplace(int n, int &nrows, std::vector<int> &ii, std::vector<int> &jj, std::vector<double> &vv,
+                        std::vector<double> &b) {
+  if (n < 1) n = 100;
+  nrows = n * n;
+  ii.clear(); jj.clear(); vv.clear();
+  auto put = [&](int r, int c, double v) { ii.push_back(r); jj.push_back(c); vv.push_back(v); };
+  for (int ri = 1; ri <= n; ri++)
+    for (int ci = 1; ci <= n; ci++) {
+      const int mri = (ri - 1) * n + ci;
+      put(mri, mri, 4.0);
+      if (ci > 1) put(mri, mri - 1, -1.0);
+      if (ci < n) put(mri, mri + 1, -1.0);
+      if (ri > 1) put(mri, mri - n, -1.0);
+      if (ri < n) put(mri, mri + n, -1.0);
+    }
+  b.assign((size_t)nrows, -1.0);
+}
+
 bool read_elemental(const std::string &info, const std::string &freelists, const std::string &elemmat,
                     int number_of_blocks, ElementMesh &M, std::string &err) {
   std::vector<unsigned char> b, rec;

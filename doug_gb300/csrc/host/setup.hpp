@@ -53,6 +53,15 @@ bool read_vector(const std::string &path, int format, int n, std::vector<double>
 bool write_solution(const std::string &path, int format, const double *x, int n,
                     std::string &err);
 
+// Structured input (input_type 3): the reference's generated test problem on
+// one process (Distribution_struct.F90:36-147): the 5-point Laplacian
+// (4 on the diagonal, -1 to the left, right, upper and lower neighbour that
+// exist) on an n x n node grid, rows numbered row-major, entries of a row in
+// the order diagonal, left, right, up, down; b = -1.  n < 1 means 100
+// (Distribution.F90:69).
+void structured_laplace(int n, int &nrows, std::vector<int> &ii, std::vector<int> &jj, std::vector<double> &vv,
+                        std::vector<double> &b);
+
 // Elemental input (input_type 1): element freedom lists and element matrices
 // with right-hand sides.  Element e has the global freedoms (1-based)
 // efree[eptr[e] .. eptr[e+1]) and the nfrelt x nfrelt matrix

@@ -2261,6 +2261,26 @@ int orc_run_ctl(const char *ctl_path, const char *overrides, orc_result **out) {
     *out = r;
     return rc;
   }
+  if (c.input_type == 3) { /* Distribution_struct_NewInit (Distribution_struct.F90:36-147), one process */
+    int g = c.grid_size < 1 ? 100 : c.grid_size; /* Distribution.F90:69 */
+    int n = g * g, cap = 5 * n, nnz = 0;
+    int *ii = (int *)malloc(sizeof(int) * (size_t)cap), *jj = (int *)malloc(sizeof(int) * (size_t)cap);
+    double *vv = (double *)malloc(sizeof(double) * (size_t)cap), *rhs = (double *)malloc(sizeof(double) * (size_t)n);
+    for (int ri = 1; ri <= g; ri++)
+      for (int ci = 1; ci <= g; ci++) {
+        int mri = (ri - 1) * g + ci;
+        ii[nnz] = mri; jj[nnz] = mri; vv[nnz++] = 4;             /* diagonal */
+        if (ci > 1) { ii[nnz] = mri; jj[nnz] = mri - 1; vv[nnz++] = -1; } /* left */
+        if (ci < g) { ii[nnz] = mri; jj[nnz] = mri + 1; vv[nnz++] = -1; } /* right */
+        if (ri > 1) { ii[nnz] = mri; jj[nnz] = mri - g; vv[nnz++] = -1; } /* up */
+        if (ri < g) { ii[nnz] = mri; jj[nnz] = mri + g; vv[nnz++] = -1; } /* down */
+      }
+    for (int i = 0; i < n; i++) rhs[i] = -1;
+    rc = orc_run_coo(n, nnz, ii, jj, vv, rhs, all, NULL, 0, &r);
+    free(ii); free(jj); free(vv); free(rhs); free(all);
+    *out = r;
+    return rc;
+  }
   if (c.input_type != 2) orc_abort("input_type %d not supported by the oracle", c.input_type);
   char mpath[1400], rpath[1400];
   if (c.assembled_mtx_file[0] == '/') snprintf(mpath, sizeof mpath, "%s", c.assembled_mtx_file);
