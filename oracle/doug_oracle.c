@@ -1603,8 +1603,13 @@ static void run_pcg(state *s, orc_result *res) {
   int n = s->n, i, sd;
   int levels = c->levels;
   int method = c->method;
-  if (c->fine_method != 1 && c->fine_method != 0)
+  if (c->fine_method != 1 && c->fine_method != 0 && c->fine_method != 2)
     orc_abort("Wrong fine method %d", c->fine_method); /* aggr.F90:216-226 */
+  if (method == 2 || method == 3)
+    orc_abort("method %d restricts a residual the one-process reference never sets (pcg.F90:146-149)", method);
+  int sgs_iters = c->num_iters <= 0 ? 3 : c->num_iters; /* aggr.F90:221 */
+  unsigned char *sgs_in = (unsigned char *)xcalloc((size_t)n + 1, 1);
+  double *sgs_diag = NEWD(n), *sgs_x = NEWD(n);
   double t0 = now_s();
   /* Factorise_subdomains (subsolvers.F90:78-163) */
   profchol *fact = NULL;
@@ -1674,6 +1679,38 @@ static void run_pcg(state *s, orc_result *res) {
       for (i = 1; i <= n; i++) z[i] = 0.0;
       if (c->fine_method == 0) { /* FinePreconditioner_Apply, type NONE (Preconditioner.F90:38-39) */
         for (i = 1; i <= n; i++) z[i] = r[i];
+      } else if (c->fine_method == 2) {
+        /* FinePreconditioner_sgs_Apply (FinePreconditioner_sgs.F90:69-86): per
+         * subdomain, SymGaussSeidel (stationary.F90:33-88) on the entries of A
+         * with row and column in the subdomain, rows in global order, x0 = 0;
+         * the subdomain results are added in subdomain order */
+        for (sd = 0; sd < s->nsubd; sd++) {
+          int b0 = s->sd_start[sd], m = s->sd_start[sd + 1] - b0, k, it2, jj;
+          for (k = 0; k < m; k++) sgs_in[s->sd_nodes[b0 + k]] = 1;
+          for (i = 1; i <= n; i++) { sgs_diag[i] = 0.0; sgs_x[i] = 0.0; }
+          for (i = 1; i <= n; i++)
+            if (sgs_in[i])
+              for (jj = s->A.mbound[i]; jj <= s->A.mbound[i + 1] - 1; jj++)
+                if (s->A.indj[jj] == i) sgs_diag[i] = s->A.val[jj];
+          for (it2 = 1; it2 <= sgs_iters; it2++) {
+            int dir;
+            for (dir = 0; dir < 2; dir++) {
+              int i0 = dir == 0 ? 1 : n, i1 = dir == 0 ? n + 1 : 0, di = dir == 0 ? 1 : -1;
+              for (i = i0; i != i1; i += di) {
+                if (sgs_diag[i] == 0) continue;
+                sgs_x[i] = r[i];
+                for (jj = s->A.mbound[i]; jj <= s->A.mbound[i + 1] - 1; jj++) {
+                  int j = s->A.indj[jj];
+                  if (!sgs_in[j] || j == i) continue;
+                  sgs_x[i] = sgs_x[i] - s->A.val[jj] * sgs_x[j];
+                }
+                sgs_x[i] = sgs_x[i] / sgs_diag[i];
+              }
+            }
+          }
+          for (k = 0; k < m; k++) z[s->sd_nodes[b0 + k]] = z[s->sd_nodes[b0 + k]] + sgs_x[s->sd_nodes[b0 + k]];
+          for (k = 0; k < m; k++) sgs_in[s->sd_nodes[b0 + k]] = 0;
+        }
       } else { /* Solve_subdomains (subsolvers.F90:54-76) */
         for (sd = 0; sd < s->nsubd; sd++) {
           int b0 = s->sd_start[sd], m = s->sd_start[sd + 1] - b0, k;
@@ -1686,7 +1723,7 @@ static void run_pcg(state *s, orc_result *res) {
         spmv_R(&s->R, r, crhs, 0, nc);
         pc_solve(&cfact, crhs + 1, csol + 1, cw);
         spmv_R(&s->R, csol, tmpsol, 1, n);
-        if (method == 1)
+        if (method == 1 || method == 5) /* pcg.F90:191-193, 205-208 */
           for (i = 1; i <= n; i++) z[i] = z[i] + tmpsol[i];
       }
     }
@@ -1718,6 +1755,7 @@ static void run_pcg(state *s, orc_result *res) {
   pc_free(&cfact);
   free(x); free(r); free(p); free(q); free(z); free(subrhs); free(subsol); free(work);
   free(crhs); free(csol); free(cw); free(tmpsol); free(alpha); free(beta);
+  free(sgs_in); free(sgs_diag); free(sgs_x);
 }
 
 static int *dup0(const int *a1, int n) { /* 1-based -> 0-based copy */

@@ -96,3 +96,25 @@ def test_setup_structure_lap16x16():
     P = np.zeros((n, nR))
     P[Rj - 1, Ri - 1] += Rv
     assert np.isfinite(P).all()
+
+
+@pytest.mark.parametrize("levels,smoothers,overlap,iters", [(2, 1, 1, -1), (2, 0, -1, 2), (1, 0, 0, 4)])
+def test_oracle_sgs_fine_preconditioner_matches_fixture(levels, smoothers, overlap, iters):
+    # fine_method 2: symmetric Gauss-Seidel on every subdomain (FinePreconditioner_sgs.F90)
+    ref = O.read_vector(os.path.join(GOLDEN, "lap16x16", "csolution.xdr"), 2, 225)
+    ov = (f"solver 2\nmethod 1\nfine_method 2\nlevels {levels}\nsmoothers {smoothers}\n"
+          f"overlap {overlap}\nnum_iters {iters}\n")
+    r = O.run_ctl(os.path.join(GOLDEN, "lap16x16", "DOUG.ctl"), ov)
+    assert r.get("status", 0) == 0, r
+    assert np.linalg.norm(r["x"] - ref) <= 1e-9
+
+
+def test_oracle_method5_is_additive_and_2_3_are_rejected():
+    path = os.path.join(GOLDEN, "lap16x16", "DOUG.ctl")
+    base = "solver 2\nfine_method 1\nlevels 2\nsmoothers 1\noverlap 1\n"
+    r1 = O.run_ctl(path, "method 1\n" + base)
+    r5 = O.run_ctl(path, "method 5\n" + base)
+    assert r1["iterations"] == r5["iterations"] and np.array_equal(r1["x"], r5["x"])
+    for m in (2, 3):
+        r = O.run_ctl(path, f"method {m}\n" + base)
+        assert r["status"] != 0 and "residual" in r["errmsg"]
