@@ -798,6 +798,60 @@ mf_bwd_big(MfView v, const int2 *__restrict__ tasks, const T *__restrict__ E, co
 }
 
 // ---------------------------------------------------------------------------
+// Symmetric Gauss-Seidel subdomain preconditioner (fine_method 2).  The
+// reference runs, per subdomain, forward and backward Gauss-Seidel sweeps in
+// global row order on the entries of A inside the subdomain, from x = 0
+// (FinePreconditioner_sgs.F90:69-86, stationary.F90:33-88).  Here one CTA owns
+// one subdomain; its rows are grouped into dependency levels of the
+// (symmetrised) subdomain graph, so every row of a level depends only on rows
+// of earlier levels in the sweep direction, and the result equals the
+// sequential sweep (same entry order, separate multiply and subtract,
+// division by the diagonal).  Levels are separated by __syncthreads.
+// ---------------------------------------------------------------------------
+struct SgsView {
+  const int64_t *rp;        // local CSR over arena positions (entries inside the subdomain)
+  const int *ci;            // column as arena position
+  const double *va, *dg;    // values; diagonal (0 = row skipped, as in the reference)
+  const int *gidx;          // global row of every arena position
+  const int *sd_lev_f, *sd_lev_b;    // per subdomain: its range of levels
+  const int *lev_f, *lev_b;          // per level: its range of rows
+  const int *rows_f, *rows_b;        // rows (arena positions) grouped by level
+};
+
+constexpr int kSgsThreads = 256;
+
+__device__ __forceinline__ void sgs_sweep(const SgsView &g, const int *sd_lev, const int *lev, const int *rows,
+                                          int sd, const double *__restrict__ r, double *__restrict__ x) {
+  for (int L = sd_lev[sd]; L < sd_lev[sd + 1]; L++) {
+    for (int t = lev[L] + threadIdx.x; t < lev[L + 1]; t += kSgsThreads) {
+      const int q = rows[t];
+      const double d = g.dg[q];
+      if (d == 0.0) continue;
+      double xi = r[g.gidx[q]];
+      for (int64_t e = g.rp[q]; e < g.rp[q + 1]; e++) {
+        const int c = g.ci[e];
+        if (c != q) xi = __dsub_rn(xi, __dmul_rn(g.va[e], x[c]));
+      }
+      x[q] = __ddiv_rn(xi, d);
+    }
+    __syncthreads();
+  }
+}
+
+// one CTA per subdomain: x (arena, subdomain block) = SGS(iters) applied to r
+__global__ void __launch_bounds__(kSgsThreads)
+sgs_subdomains(SgsView g, const int64_t *__restrict__ sd_ptr, int iters, const double *__restrict__ r,
+               double *__restrict__ x) {
+  const int sd = blockIdx.x;
+  for (int64_t q = sd_ptr[sd] + threadIdx.x; q < sd_ptr[sd + 1]; q += kSgsThreads) x[q] = 0.0;
+  __syncthreads();
+  for (int it = 0; it < iters; it++) {
+    sgs_sweep(g, g.sd_lev_f, g.lev_f, g.rows_f, sd, r, x);
+    sgs_sweep(g, g.sd_lev_b, g.lev_b, g.rows_b, sd, r, x);
+  }
+}
+
+// ---------------------------------------------------------------------------
 // Schwarz gather / pull sum and coarse transfer
 // ---------------------------------------------------------------------------
 template <typename T>

@@ -371,6 +371,97 @@ struct MfDevice {
 
 using namespace dg;
 
+// symmetric Gauss-Seidel subdomain data (fine_method 2): the arena holds
+// every subdomain's rows in increasing global order; rows of a subdomain are
+// grouped into dependency levels for the forward and the backward sweep
+struct SgsDevice {
+  DBuf<int64_t> rp, sd_ptr;
+  DBuf<int> ci, gidx, sd_lev_f, sd_lev_b, lev_f, lev_b, rows_f, rows_b;
+  DBuf<double> va, dg, x;
+  int nsd = 0;
+  std::vector<int> gidx_h;
+  SgsView view{};
+
+  // levels of one sweep over the rows [q0, q1) of a subdomain (local CSR),
+  // in increasing (fwd) or decreasing order: a row comes after every row it
+  // shares an entry with (either direction) that precedes it in the sweep
+  static void levels(const std::vector<int64_t> &rp, const std::vector<int> &ci, int q0, int q1, bool fwd,
+                     std::vector<int> &lev, std::vector<int> &minlev) {
+    for (int q = q0; q < q1; q++) minlev[(size_t)q] = 0;
+    for (int t = 0; t < q1 - q0; t++) {
+      const int q = fwd ? q0 + t : q1 - 1 - t;
+      int L = minlev[(size_t)q];
+      for (int64_t e = rp[(size_t)q]; e < rp[(size_t)q + 1]; e++) {
+        const int c = ci[(size_t)e];
+        if (c != q && (fwd ? c < q : c > q)) L = std::max(L, lev[(size_t)c] + 1);
+      }
+      lev[(size_t)q] = L;
+      for (int64_t e = rp[(size_t)q]; e < rp[(size_t)q + 1]; e++) {
+        const int c = ci[(size_t)e];
+        if (c != q && (fwd ? c > q : c < q)) minlev[(size_t)c] = std::max(minlev[(size_t)c], L + 1);
+      }
+    }
+  }
+
+  void build(const Csr &A, const std::vector<int64_t> &sdp, const std::vector<int> &sd_nodes) {
+    nsd = (int)sdp.size() - 1;
+    const int64_t len = sdp.back();
+    gidx_h.assign((size_t)len, 0);
+    for (int s = 0; s < nsd; s++) {
+      std::vector<int> nodes(sd_nodes.begin() + sdp[(size_t)s], sd_nodes.begin() + sdp[(size_t)s + 1]);
+      std::sort(nodes.begin(), nodes.end());
+      for (size_t t = 0; t < nodes.size(); t++) gidx_h[(size_t)sdp[(size_t)s] + t] = nodes[t] - 1;
+    }
+    std::vector<int> loc((size_t)A.nrows, -1);
+    std::vector<int64_t> rph((size_t)len + 1, 0);
+    std::vector<int> cih;
+    std::vector<double> vah, dgh((size_t)len, 0.0);
+    for (int s = 0; s < nsd; s++) {
+      for (int64_t q = sdp[(size_t)s]; q < sdp[(size_t)s + 1]; q++) loc[(size_t)gidx_h[(size_t)q]] = (int)q;
+      for (int64_t q = sdp[(size_t)s]; q < sdp[(size_t)s + 1]; q++) {
+        const int g = gidx_h[(size_t)q];
+        for (int64_t e = A.ptr[(size_t)g]; e < A.ptr[(size_t)g + 1]; e++) {
+          const int c = A.col[(size_t)e];
+          if (loc[(size_t)c] < 0) continue;
+          cih.push_back(loc[(size_t)c]);
+          vah.push_back(A.val[(size_t)e]);
+          if (c == g) dgh[(size_t)q] = A.val[(size_t)e];
+        }
+        rph[(size_t)q + 1] = (int64_t)cih.size();
+      }
+      for (int64_t q = sdp[(size_t)s]; q < sdp[(size_t)s + 1]; q++) loc[(size_t)gidx_h[(size_t)q]] = -1;
+    }
+    std::vector<int> lf((size_t)len), lb((size_t)len), ml((size_t)len);
+    std::vector<int> sdlf(1, 0), sdlb(1, 0), levf(1, 0), levb(1, 0), rowf, rowb;
+    for (int s = 0; s < nsd; s++) {
+      const int q0 = (int)sdp[(size_t)s], q1 = (int)sdp[(size_t)s + 1];
+      levels(rph, cih, q0, q1, true, lf, ml);
+      levels(rph, cih, q0, q1, false, lb, ml);
+      for (int dir = 0; dir < 2; dir++) {
+        const std::vector<int> &lv = dir == 0 ? lf : lb;
+        std::vector<int> &rows = dir == 0 ? rowf : rowb;
+        std::vector<int> &lev = dir == 0 ? levf : levb;
+        std::vector<int> &sdl = dir == 0 ? sdlf : sdlb;
+        int nl = 0;
+        for (int q = q0; q < q1; q++) nl = std::max(nl, lv[(size_t)q] + 1);
+        std::vector<std::vector<int>> byl((size_t)nl);
+        for (int q = q0; q < q1; q++) byl[(size_t)lv[(size_t)q]].push_back(q);
+        for (auto &b : byl) {
+          rows.insert(rows.end(), b.begin(), b.end());
+          lev.push_back((int)rows.size());
+        }
+        sdl.push_back((int)lev.size() - 1);
+      }
+    }
+    rp.upload(rph); ci.upload(cih); va.upload(vah); dg.upload(dgh); gidx.upload(gidx_h);
+    sd_ptr.upload(sdp);
+    sd_lev_f.upload(sdlf); sd_lev_b.upload(sdlb); lev_f.upload(levf); lev_b.upload(levb);
+    rows_f.upload(rowf); rows_b.upload(rowb);
+    x.alloc((size_t)std::max<int64_t>(len, 1));
+    view = SgsView{rp.p, ci.p, va.p, dg.p, gidx.p, sd_lev_f.p, sd_lev_b.p, lev_f.p, lev_b.p, rows_f.p, rows_b.p};
+  }
+};
+
 struct dg_handle {
   Controls ctl;
   std::string ctl_text;           // words given through dg_set_option (applied first)
@@ -396,6 +487,7 @@ struct dg_handle {
   DBuf<double> part_rz, part_rzo, part_pq, part_rr, sc;
   std::unique_ptr<MfDevice<double>> sub64, co64;
   std::unique_ptr<MfDevice<float>> sub32;
+  std::unique_ptr<SgsDevice> sgs;
   double *host_out = nullptr;     // mapped pinned
   int *host_status = nullptr;
   double *d_host_out = nullptr;
@@ -568,18 +660,26 @@ dg_status do_setup(dg_handle *h) {
     h->Rvf.upload(rf); h->Pvf.upload(pf);
     h->ACv.upload(S.AC.val);
     // subdomain batch
-    h->sub64.reset(); h->sub32.reset(); h->co64.reset();
-    if (c.fine_method == 1) {
-      if (h->precision == 1) { h->sub32.reset(new MfDevice<float>()); h->sub32->upload(h->Bsub); }
-      else { h->sub64.reset(new MfDevice<double>()); h->sub64->upload(h->Bsub); }
+    h->sub64.reset(); h->sub32.reset(); h->co64.reset(); h->sgs.reset();
+    if (c.fine_method == 1 || c.fine_method == 2) {
+      const std::vector<int> *arena_rows = &h->Bsub.gidx;
+      if (c.fine_method == 2) {
+        h->sgs.reset(new SgsDevice());
+        h->sgs->build(S.A, S.sd_ptr, S.sd_nodes);
+        arena_rows = &h->sgs->gidx_h;
+      } else if (h->precision == 1) {
+        h->sub32.reset(new MfDevice<float>()); h->sub32->upload(h->Bsub);
+      } else {
+        h->sub64.reset(new MfDevice<double>()); h->sub64->upload(h->Bsub);
+      }
       // pull lists: subdomain arena positions of every node, subdomain order
       std::vector<int64_t> pp((size_t)n + 1, 0);
-      for (int g : h->Bsub.gidx) pp[(size_t)g + 1]++;
+      for (int g : *arena_rows) pp[(size_t)g + 1]++;
       for (int i = 0; i < n; i++) pp[(size_t)i + 1] += pp[(size_t)i];
       std::vector<int64_t> idx((size_t)pp[(size_t)n]);
       std::vector<int64_t> fill(pp.begin(), pp.end() - 1);
-      for (int64_t q = 0; q < (int64_t)h->Bsub.gidx.size(); q++)
-        idx[(size_t)fill[(size_t)h->Bsub.gidx[(size_t)q]]++] = q;
+      for (int64_t q = 0; q < (int64_t)arena_rows->size(); q++)
+        idx[(size_t)fill[(size_t)(*arena_rows)[(size_t)q]]++] = q;
       h->pull_ptr.upload(pp);
       h->pull_idx.upload(idx);
     } else {
@@ -614,7 +714,9 @@ dg_status do_solve(dg_handle *h, const double *d_b, double *d_x, dg_stats *st, c
   ctl_finish(c);
   const int n = h->n;
   const int grid = kRedBlocks;
-  const bool fine = c.fine_method == 1 && c.method != 0;
+  const bool fine = (c.fine_method == 1 || c.fine_method == 2) && c.method != 0;
+  const bool sgs = c.fine_method == 2;
+  const int sgs_iters = c.num_iters <= 0 ? 3 : c.num_iters;  // aggr.F90:221
   const bool coarse = c.levels > 1 && c.method != 0;
   const bool mixed = h->precision == 1;
   int launches = 0;
@@ -636,7 +738,8 @@ dg_status do_solve(dg_handle *h, const double *d_b, double *d_x, dg_stats *st, c
       launches += h->co64->factor(h->ACv.p, h->status.p, h->s2);
       CK(cudaEventRecord(h->join_ev, h->s2));
     }
-    if (fine) launches += mixed ? h->sub32->factor(h->Av.p, h->status.p, s) : h->sub64->factor(h->Av.p, h->status.p, s);
+    if (fine && !sgs)
+      launches += mixed ? h->sub32->factor(h->Av.p, h->status.p, s) : h->sub64->factor(h->Av.p, h->status.p, s);
     if (coarse) CK(cudaStreamWaitEvent(s, h->join_ev, 0));
     CK(cudaEventRecord(h->ev[1], s));
     CK(cudaMemcpyAsync(h->b.p, d_b, (size_t)n * sizeof(double), cudaMemcpyDeviceToDevice, s));
@@ -668,7 +771,7 @@ dg_status do_solve(dg_handle *h, const double *d_b, double *d_x, dg_stats *st, c
     if (c.method == 0) mode |= 4;
     else if (c.fine_method == 0) mode |= 4;
     else mode |= 1;
-    if (coarse && c.method == 1) mode |= 2;
+    if (coarse && (c.method == 1 || c.method == 5)) mode |= 2;  // method 5: pcg.F90:205-208
     if (mixed) mode |= 8;
     // (the reference adds the coarse correction only for method 1, pcg.F90:191-193)
     const bool prof = c.profile != 0;
@@ -695,7 +798,11 @@ dg_status do_solve(dg_handle *h, const double *d_b, double *d_x, dg_stats *st, c
         CK(cudaEventRecord(h->join_ev, h->s2));
       }
       if (profile) CK(cudaEventRecord(h->ev[3], st));
-      if (fine) {
+      if (fine && sgs) {
+        sgs_subdomains<<<h->sgs->nsd, kSgsThreads, 0, st>>>(h->sgs->view, h->sgs->sd_ptr.p, sgs_iters, h->r.p,
+                                                             h->sgs->x.p);
+        nl++;
+      } else if (fine) {
         if (mixed) {
           gather_subdomains<float><<<grid, kVecThreads, 0, st>>>(h->r.p, h->sub32->gidx.p, h->sub32->xl.p, h->sub32->xlen);
           nl += 1 + h->sub32->solve(st);
@@ -707,7 +814,15 @@ dg_status do_solve(dg_handle *h, const double *d_b, double *d_x, dg_stats *st, c
       if (profile) CK(cudaEventRecord(h->ev[8], st));
       if (coarse) CK(cudaStreamWaitEvent(st, h->join_ev, 0));
       const double *xc = coarse ? h->co64->xl.p : nullptr;
-      if (mixed)
+      if (sgs && mixed)
+        pull_prolong_dot<double, float><<<grid, kVecThreads, 0, st>>>(
+            n, h->pull_ptr.p, h->pull_idx.p, fine ? h->sgs->x.p : nullptr, h->Pp.p, h->Pc.p, h->Pvf.p, xc,
+            mode, h->r.p, h->z.p, h->zold.p, h->part_rz.p, h->part_rzo.p);
+      else if (sgs)
+        pull_prolong_dot<double, double><<<grid, kVecThreads, 0, st>>>(
+            n, h->pull_ptr.p, h->pull_idx.p, fine ? h->sgs->x.p : nullptr, h->Pp.p, h->Pc.p, h->Pv.p, xc,
+            mode, h->r.p, h->z.p, h->zold.p, h->part_rz.p, h->part_rzo.p);
+      else if (mixed)
         pull_prolong_dot<float, float><<<grid, kVecThreads, 0, st>>>(
             n, h->pull_ptr.p, h->pull_idx.p, fine ? h->sub32->xl.p : nullptr, h->Pp.p, h->Pc.p, h->Pvf.p, xc,
             mode, h->r.p, h->z.p, h->zold.p, h->part_rz.p, h->part_rzo.p);

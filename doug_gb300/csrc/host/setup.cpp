@@ -1101,8 +1101,15 @@ bool build_setup(const Controls &c_in, int n, const std::vector<int> &ii, const 
   out = SetupResult();
   out.n = n;
   PhaseTimer tm;
-  if (c.fine_method < 0 || c.fine_method > 1) {
+  if (c.fine_method < 0 || c.fine_method > 2) {
     err = "Wrong fine method " + std::to_string(c.fine_method);
+    return false;
+  }
+  if (c.method == 2 || c.method == 3) {
+    // the one-process reference restricts a residual vector it allocates but
+    // never sets for these multiplicative variants (pcg.F90:146-149, 264-266)
+    err = "method " + std::to_string(c.method) +
+          " restricts a residual the one-process reference never sets (pcg.F90:146-149)";
     return false;
   }
   if (c.coarse_method > 1) {
