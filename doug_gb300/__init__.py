@@ -38,7 +38,7 @@ EXPORTED_SYMBOLS = [
     "dg_set_matrix_coo", "dg_set_rhs", "dg_set_partition", "dg_setup", "dg_solve",
     "dg_solve_device", "dg_write_solution", "dg_get_sizes", "dg_get_aggregates",
     "dg_get_subdomains", "dg_get_restriction", "dg_get_coarse_matrix", "dg_residual_csr",
-    "dg_set_elements", "dg_get_input",
+    "dg_set_elements", "dg_get_input", "dg_grad_matrix", "dg_grad_elements",
     "dg_residual_csr_noalloc",
 ]
 
@@ -109,6 +109,8 @@ def load_library(path: str | None = None):
     L.dg_load_ctl.argtypes = [vp, C.c_char_p]
     L.dg_set_matrix_coo.argtypes = [vp, C.c_int, C.c_int, P(C.c_int), P(C.c_int), P(C.c_double)]
     L.dg_set_rhs.argtypes = [vp, P(C.c_double)]
+    L.dg_grad_matrix.argtypes = [vp, vp, vp, vp, vp]
+    L.dg_grad_elements.argtypes = [vp, vp, vp, vp, vp]
     L.dg_set_elements.argtypes = [vp, C.c_int, C.c_int, P(C.c_int), P(C.c_int), P(C.c_double), P(C.c_double)]
     L.dg_get_input.argtypes = [vp, P(C.c_int), P(C.c_int), P(C.c_int), P(C.c_int), P(C.c_double),
                                P(C.c_double)]
@@ -206,6 +208,16 @@ class DougSolver:
         em = np.ascontiguousarray(emat, dtype=np.float64)
         er = np.ascontiguousarray(erhs, dtype=np.float64)
         self._check(self._L.dg_set_elements(self._h, len(ep) - 1, int(ngf), _ip(ep), _ip(ef), _dp(em), _dp(er)))
+
+    def grad_matrix(self, d_lambda: int, d_x: int, d_grad: int, stream: int = 0) -> None:
+        """d_grad[k] = -lambda[row_k] x[col_k] per input triplet (device pointers)."""
+        self._check(self._L.dg_grad_matrix(self._h, C.c_void_p(d_lambda), C.c_void_p(d_x), C.c_void_p(d_grad),
+                                           C.c_void_p(stream)))
+
+    def grad_elements(self, d_lambda: int, d_x: int, d_grad: int, stream: int = 0) -> None:
+        """d_grad[e] = dL/ds_e for a factor scaling element e's matrix (device pointers)."""
+        self._check(self._L.dg_grad_elements(self._h, C.c_void_p(d_lambda), C.c_void_p(d_x),
+                                             C.c_void_p(d_grad), C.c_void_p(stream)))
 
     def input_matrix(self):
         """(n, rows1, cols1, vals, rhs) the handle holds, in entry order."""

@@ -852,6 +852,38 @@ sgs_subdomains(SgsView g, const int64_t *__restrict__ sd_ptr, int iters, const d
 }
 
 // ---------------------------------------------------------------------------
+// Gradients of a loss L(x) through x = A^-1 b, given the adjoint solution
+// lambda = A^-1 dL/dx (A symmetric): dL/db = lambda, dL/dA_ij = -lambda_i x_j.
+// ---------------------------------------------------------------------------
+// one value per input triplet (row gi, column gj, 0-based)
+__global__ void grad_coo(int64_t nnz, const int *__restrict__ gi, const int *__restrict__ gj,
+                         const double *__restrict__ lam, const double *__restrict__ x, double *__restrict__ g) {
+  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < nnz; k += (int64_t)gridDim.x * blockDim.x)
+    g[k] = -(lam[gi[k]] * x[gj[k]]);
+}
+
+// one value per element: the derivative with respect to a factor s_e that
+// scales the element's matrix, -sum_ij lambda[f_j] A_e(i,j) x[f_i] (the
+// element assembly stores A_e(i,j) at row f_j, column f_i); one warp per
+// element, the element's terms summed in a fixed order
+__global__ void grad_elements(int nell, const int *__restrict__ eptr, const int *__restrict__ efl,
+                              const int64_t *__restrict__ eoff, const double *__restrict__ emat,
+                              const double *__restrict__ lam, const double *__restrict__ x, double *__restrict__ g) {
+  const int lane = threadIdx.x & 31;
+  const int e = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (e >= nell) return;
+  const int f0 = eptr[e], nf = eptr[e + 1] - f0;
+  const double *Ae = emat + eoff[e];
+  double s = 0.0;
+  for (int q = lane; q < nf * nf; q += 32) {
+    const int j = q / nf, i = q % nf;  // column j, row i of the element matrix
+    s += lam[efl[f0 + j]] * Ae[q] * x[efl[f0 + i]];
+  }
+  s = warp_sum(s);
+  if (lane == 0) g[e] = -s;
+}
+
+// ---------------------------------------------------------------------------
 // Schwarz gather / pull sum and coarse transfer
 // ---------------------------------------------------------------------------
 template <typename T>

@@ -472,6 +472,16 @@ struct dg_handle {
   std::vector<double> vv, rhs;
   bool have_matrix = false, have_rhs = false, ready = false;
   std::vector<int> part;
+  // elemental input kept for the element gradients: local (0-based) unknown of
+  // every element freedom, element offsets, matrices
+  bool have_elements = false;
+  std::vector<int> el_eptr, el_local;
+  std::vector<int64_t> el_off;
+  std::vector<double> el_mat;
+  DBuf<int> d_el_eptr, d_el_local, d_gi, d_gj;
+  DBuf<int64_t> d_el_off;
+  DBuf<double> d_el_mat;
+  bool factored = false;          // the device holds factors of the current setup
   int nparts = 0;
   SetupResult S;
   MfBatch Bsub, Bco;
@@ -630,6 +640,18 @@ dg_status do_setup(dg_handle *h) {
     CK(cudaGetDevice(&h->device));
     const SetupResult &S = h->S;
     int n = h->n;
+    h->factored = false;
+    {  // input triplets (0-based) for the matrix gradient; element data for the element gradient
+      const int shift = (!h->ii.empty() && h->ii[0] == 0) ? 0 : 1;  // 0-based input is accepted
+      std::vector<int> gi(h->ii.size()), gj(h->jj.size());
+      for (size_t k = 0; k < gi.size(); k++) { gi[k] = h->ii[k] - shift; gj[k] = h->jj[k] - shift; }
+      h->d_gi.upload(gi);
+      h->d_gj.upload(gj);
+      if (h->have_elements) {
+        h->d_el_eptr.upload(h->el_eptr); h->d_el_local.upload(h->el_local);
+        h->d_el_off.upload(h->el_off); h->d_el_mat.upload(h->el_mat);
+      }
+    }
     h->Ap.upload(S.A.ptr); h->Ac.upload(S.A.col); h->Av.upload(S.A.val);
     h->lanes = lanes_for(S.A);
     for (auto *v : {&h->b, &h->x, &h->r, &h->p, &h->q, &h->z, &h->zold, &h->hb, &h->hx}) v->alloc((size_t)n);
@@ -703,6 +725,7 @@ dg_status do_setup(dg_handle *h) {
   } catch (const CudaError &e) {
     return cuda_fail(h, e);
   }
+  h->factored = false;
   h->ready = true;
   return DG_OK;
 }
@@ -732,15 +755,16 @@ dg_status do_solve(dg_handle *h, const double *d_b, double *d_x, dg_stats *st, c
     CK(cudaEventRecord(h->ev[0], s));
     // numeric factorisations (the reference factorises lazily in the first
     // preconditioner call, subsolvers.F90:78-101, pcg.F90:166-178)
-    if (coarse) {  // the coarse factorisation runs beside the subdomain factorisations
+    const bool refactor = !(c.reuse_factors && h->factored);
+    if (coarse && refactor) {  // the coarse factorisation runs beside the subdomain factorisations
       CK(cudaEventRecord(h->fork_ev, s));
       CK(cudaStreamWaitEvent(h->s2, h->fork_ev, 0));
       launches += h->co64->factor(h->ACv.p, h->status.p, h->s2);
       CK(cudaEventRecord(h->join_ev, h->s2));
     }
-    if (fine && !sgs)
+    if (fine && !sgs && refactor)
       launches += mixed ? h->sub32->factor(h->Av.p, h->status.p, s) : h->sub64->factor(h->Av.p, h->status.p, s);
-    if (coarse) CK(cudaStreamWaitEvent(s, h->join_ev, 0));
+    if (coarse && refactor) CK(cudaStreamWaitEvent(s, h->join_ev, 0));
     CK(cudaEventRecord(h->ev[1], s));
     CK(cudaMemcpyAsync(h->b.p, d_b, (size_t)n * sizeof(double), cudaMemcpyDeviceToDevice, s));
     CK(cudaMemsetAsync(h->x.p, 0, (size_t)n * sizeof(double), s));
@@ -752,8 +776,11 @@ dg_status do_solve(dg_handle *h, const double *d_b, double *d_x, dg_stats *st, c
     launches += 2;
     CK(cudaGetLastError());
     CK(cudaStreamSynchronize(s));
-    if (*h->host_status & ERR_NOT_SPD)
+    if (*h->host_status & ERR_NOT_SPD) {
+      h->factored = false;
       return fail(h, DG_SINGULAR, "a subdomain or coarse matrix is not positive definite");
+    }
+    h->factored = true;
     double init = h->host_out[0];
     if (init == 0.0) {
       init = 1.0;
@@ -963,6 +990,12 @@ dg_status dg_set_option(dg_handle *h, const char *name, const char *value) {
     h->ctl.replace_every = v;
     return DG_OK;
   }
+  if (w1 == "reuse_factors") {
+    int v;
+    if (!parse_i10(w2, v)) return fail(h, DG_BAD_INPUT, "bad reuse_factors");
+    h->ctl.reuse_factors = v;
+    return DG_OK;
+  }
   if (w1 == "profile") {
     int v;
     if (!parse_i10(w2, v)) return fail(h, DG_BAD_INPUT, "bad profile");
@@ -998,7 +1031,17 @@ static dg_status set_elements(dg_handle *h, const ElementMesh &M) {
   if (n <= 0 || vv.empty()) return fail(h, DG_BAD_INPUT, "elements: the assembled matrix is empty");
   dg_status s = dg_set_matrix_coo(h, n, (int)vv.size(), ii.data(), jj.data(), vv.data());
   if (s != DG_OK) return s;
-  return dg_set_rhs(h, b.data());
+  s = dg_set_rhs(h, b.data());
+  if (s != DG_OK) return s;
+  std::vector<int> gl((size_t)M.ngf + 1, -1);
+  for (size_t l = 0; l < lg.size(); l++) gl[(size_t)lg[l]] = (int)l;
+  h->el_eptr = M.eptr;
+  h->el_local.resize(M.efree.size());
+  for (size_t q = 0; q < M.efree.size(); q++) h->el_local[q] = gl[(size_t)M.efree[q]];
+  h->el_off = M.emat_off;
+  h->el_mat = M.emat;
+  h->have_elements = true;
+  return DG_OK;
 }
 
 dg_status dg_load_ctl(dg_handle *h, const char *path) {
@@ -1051,6 +1094,7 @@ dg_status dg_load_ctl(dg_handle *h, const char *path) {
 
 dg_status dg_set_matrix_coo(dg_handle *h, int n, int nnz, const int *rows, const int *cols, const double *vals) {
   if (!h || n <= 0 || nnz <= 0 || !rows || !cols || !vals) return DG_BAD_INPUT;
+  h->have_elements = false;  // set_elements sets it again after this call
   h->n = n;
   h->ii.assign(rows, rows + nnz);
   h->jj.assign(cols, cols + nnz);
@@ -1176,6 +1220,33 @@ dg_status dg_get_coarse_matrix(const dg_handle *h, int *ci, int *cj, double *cv)
   if (ci) std::copy(h->S.AC_i.begin(), h->S.AC_i.end(), ci);
   if (cj) std::copy(h->S.AC_j.begin(), h->S.AC_j.end(), cj);
   if (cv) std::copy(h->S.AC_v.begin(), h->S.AC_v.end(), cv);
+  return DG_OK;
+}
+
+dg_status dg_grad_matrix(dg_handle *h, const double *d_lambda, const double *d_x, double *d_grad,
+                         void *cuda_stream) {
+  if (!h || !d_lambda || !d_x || !d_grad) return DG_BAD_INPUT;
+  if (!h->ready) return fail(h, DG_NOT_READY, "dg_setup has not run");
+  const int64_t nnz = (int64_t)h->d_gi.n;
+  cudaStream_t s = (cudaStream_t)cuda_stream;
+  grad_coo<<<(unsigned)std::min<int64_t>((nnz + 255) / 256, 65535), 256, 0, s>>>(nnz, h->d_gi.p, h->d_gj.p,
+                                                                             d_lambda, d_x, d_grad);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return fail(h, DG_CUDA_ERROR, std::string("grad_coo: ") + cudaGetErrorString(e));
+  return DG_OK;
+}
+
+dg_status dg_grad_elements(dg_handle *h, const double *d_lambda, const double *d_x, double *d_grad,
+                           void *cuda_stream) {
+  if (!h || !d_lambda || !d_x || !d_grad) return DG_BAD_INPUT;
+  if (!h->ready) return fail(h, DG_NOT_READY, "dg_setup has not run");
+  if (!h->have_elements) return fail(h, DG_BAD_INPUT, "the matrix was not given as elements");
+  const int nell = (int)h->el_eptr.size() - 1;
+  cudaStream_t s = (cudaStream_t)cuda_stream;
+  grad_elements<<<(nell + 7) / 8, 256, 0, s>>>(nell, h->d_el_eptr.p, h->d_el_local.p, h->d_el_off.p,
+                                               h->d_el_mat.p, d_lambda, d_x, d_grad);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return fail(h, DG_CUDA_ERROR, std::string("grad_elements: ") + cudaGetErrorString(e));
   return DG_OK;
 }
 

@@ -33,6 +33,7 @@ struct Controls {
   int replace_every = 50;           // residual replacement period (mixed path)
   int nd_leaf = 24;                 // nested-dissection leaf size of the subdomain factors
   int profile = 0;                  // 1: CUDA-event timing of the solve phases
+  int reuse_factors = 0;            // 1: a solve after the first keeps the numeric factors
 };
 
 // Parse one "name value" line the way util_actionOnCtrlArg does

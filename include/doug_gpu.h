@@ -93,7 +93,9 @@ const char *dg_last_error(const dg_handle *h);
  * the first value given for a name wins, as in the reference).  Extension
  * words of this library: precision (0 = FP64, 1 = mixed FP32 subdomain
  * factors with flexible CG and FP64 residual replacement), replace_every,
- * omega (prolongator smoother weight; the reference hard-codes 1/3). */
+ * omega (prolongator smoother weight; the reference hard-codes 1/3),
+ * reuse_factors (1: solves after the first keep the numeric factors, for
+ * adjoint solves and further right-hand sides of the same matrix). */
 dg_status dg_set_option(dg_handle *h, const char *name, const char *value);
 /* Parse a control file and read the input files it names: input_type 2,
  * the assembled matrix + optional RHS; input_type 1, the info, freedom-list
@@ -159,6 +161,22 @@ dg_status dg_residual_csr(int n, const long long *d_rowptr, const int *d_col, co
 dg_status dg_residual_csr_noalloc(int n, const long long *d_rowptr, const int *d_col,
                                   const double *d_val, const double *d_x, const double *d_b,
                                   double *d_r, double *d_norm2, void *cuda_stream);
+
+/* Gradients through x = A^-1 b (the reference has no gradients).  Given the
+ * adjoint solution d_lambda = A^-1 dL/dx (a second solve with the same
+ * handle; with the option reuse_factors 1 it keeps the factors of the first)
+ * and the solution d_x, both device vectors of n values:
+ *   dg_grad_matrix   -> d_grad[k] = -lambda[row_k] x[col_k] for every input
+ *                       triplet k of dg_set_matrix_coo / the control file
+ *                       (dL/dA_ij; dL/db is lambda itself);
+ *   dg_grad_elements -> d_grad[e] = dL/ds_e for a factor s_e scaling element
+ *                       e's matrix (elemental input only): with A_e =
+ *                       kappa_e K_e, dL/dkappa_e = d_grad[e] / kappa_e.
+ * Both run on the given stream and return without waiting. */
+dg_status dg_grad_matrix(dg_handle *h, const double *d_lambda, const double *d_x, double *d_grad,
+                         void *cuda_stream);
+dg_status dg_grad_elements(dg_handle *h, const double *d_lambda, const double *d_x, double *d_grad,
+                           void *cuda_stream);
 
 /* Size queries and parity export (1-based ids as in the reference). */
 dg_status dg_get_sizes(const dg_handle *h, int *n, int *nagr_fine, int *nagr_coarse,
