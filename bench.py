@@ -42,6 +42,7 @@ TOL = "1.0e-8"
 CTL = dict(solver=2, method=1, fine_method=1, levels=2, overlap=2, smoothers=1,
            strong1="0.08", radius1=4, maxasize1=200, solve_tolerance=TOL, solve_maxiters=2000)
 METRIC = "time to rel. residual 1e-8 (s), mixed+batched vs plain FP64 PCG, 1 GB300"
+SUBSOLVE_TRAFFIC_BYTES = 4.5975e9  # ncu, one PCG iteration of the 128^3 mixed solve
 WORKLOAD = ("128^3 log-normal diffusion (sigma 1, corr. length 8), 7-point FV, 2,097,152 unknowns; "
             "PCG + 2-level additive Schwarz: 64 subdomains (4x4x4 boxes), overlap 2, "
             "smoothed-aggregation coarse grid")
@@ -308,7 +309,11 @@ def run_gpu(args, rank, world):
     achieved = prof.subsolve_bytes / per_solve_s / 1e9 if per_solve_s > 0 else None
     roofline = {"kernel": "mf_fwd_small+mf_fwd_big+mf_bwd_big+mf_bwd_small (FP32 subdomain solves, all levels)",
                 "bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
-                "frac": (achieved / hbm) if achieved else None, "traffic": None,
+                "frac": (achieved / hbm) if achieved else None,
+                # DRAM bytes (read + write) of the group per application, from one
+                # ncu capture of this workload (dram__bytes_read.sum + dram__bytes_write.sum
+                # summed over one iteration's subdomain-solve launches)
+                "traffic": SUBSOLVE_TRAFFIC_BYTES,
                 "peak_source": f"{peak_kind} hbm_gbs",
                 "bytes_per_launch_group": prof.subsolve_bytes, "launch_group_s": per_solve_s}
     phases = {"factor_s": prof.t_factor_s, "iterate_s": prof.t_iterate_s,
