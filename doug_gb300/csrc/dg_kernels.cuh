@@ -884,6 +884,61 @@ __global__ void grad_elements(int nell, const int *__restrict__ eptr, const int 
 }
 
 // ---------------------------------------------------------------------------
+// Matrix-free product with stored element matrices (elemental input, option
+// elemental_matvec 1): q = A p with A = sum_e of element e's matrix placed at
+// its freedoms (A_e(i,j) at row f_j, column f_i, as the element assembly puts
+// it).  Pass 1 stages a run of element matrices in shared memory with
+// coalesced loads and forms every element's column products
+// c[e, j] = sum_i A_e(i,j) p[f_i]; pass 2 sums, for every row, its element
+// contributions in element order (no atomics: the result is deterministic)
+// and the p.q partial sums.
+// ---------------------------------------------------------------------------
+constexpr int kElemChunk = 4096;  // doubles of element matrices per CTA stage (32 KB)
+
+// task t = elements [erun[t], erun[t+1]) whose matrices total <= kElemChunk values
+__global__ void __launch_bounds__(256)
+elem_contrib(const int *__restrict__ erun, const int *__restrict__ eptr, const int *__restrict__ efl,
+             const int64_t *__restrict__ eoff, const double *__restrict__ emat, const double *__restrict__ p,
+             double *__restrict__ c) {
+  __shared__ double Ms[kElemChunk];
+  const int e0 = erun[blockIdx.x], e1 = erun[blockIdx.x + 1];
+  const int64_t m0 = eoff[e0];
+  const int len = (int)(eoff[e1] - m0);
+  for (int q = threadIdx.x; q < len; q += blockDim.x) Ms[q] = emat[m0 + q];
+  __syncthreads();
+  // one thread per (element, column)
+  const int f0 = eptr[e0], nitems = eptr[e1] - f0;
+  for (int t = threadIdx.x; t < nitems; t += blockDim.x) {
+    int lo = e0, hi = e1 - 1;  // element of item t: the last e with eptr[e] <= f0 + t
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (eptr[mid] <= f0 + t) lo = mid; else hi = mid - 1;
+    }
+    const int e = lo, fe = eptr[e], nf = eptr[e + 1] - fe, j = f0 + t - fe;
+    const double *Aj = Ms + (eoff[e] - m0) + (int64_t)j * nf;  // column j
+    double s = 0.0;
+    for (int i = 0; i < nf; i++) s = __dadd_rn(s, __dmul_rn(Aj[i], p[efl[fe + i]]));
+    c[f0 + t] = s;
+  }
+}
+
+// q[r] = sum of r's element contributions (element order); partial p.q
+__global__ void __launch_bounds__(kVecThreads)
+elem_pull_pq(int n, const int64_t *__restrict__ rptr, const int *__restrict__ ridx, const double *__restrict__ c,
+             const double *__restrict__ p, double *__restrict__ q, double *__restrict__ part_pq) {
+  __shared__ double sh[32];
+  double spq = 0.0;
+  for (int r = blockIdx.x * kVecThreads + threadIdx.x; r < n; r += gridDim.x * kVecThreads) {
+    double s = 0.0;
+    for (int64_t t = rptr[r]; t < rptr[r + 1]; t++) s = __dadd_rn(s, c[ridx[t]]);
+    q[r] = s;
+    spq += p[r] * s;
+  }
+  double b = block_sum<kVecThreads>(spq, sh);
+  if (threadIdx.x == 0) part_pq[blockIdx.x] = b;
+}
+
+// ---------------------------------------------------------------------------
 // Schwarz gather / pull sum and coarse transfer
 // ---------------------------------------------------------------------------
 template <typename T>

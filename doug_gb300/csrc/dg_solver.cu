@@ -478,7 +478,11 @@ struct dg_handle {
   std::vector<int> el_eptr, el_local;
   std::vector<int64_t> el_off;
   std::vector<double> el_mat;
-  DBuf<int> d_el_eptr, d_el_local, d_gi, d_gj;
+  DBuf<int> d_el_eptr, d_el_local, d_gi, d_gj, d_el_run, d_el_ridx;
+  DBuf<int64_t> d_el_rptr;
+  DBuf<double> d_el_c;
+  int el_nrun = 0;
+  bool elem_mv = false;           // PCG products with the element matrices
   DBuf<int64_t> d_el_off;
   DBuf<double> d_el_mat;
   bool factored = false;          // the device holds factors of the current setup
@@ -594,6 +598,15 @@ void launch_resid(int grid, cudaStream_t s, dg_handle *h, const double *xx, cons
   residual<L><<<grid, kVecThreads, 0, s>>>(h->n, h->Ap.p, h->Ac.p, h->Av.p, xx, bb, rr, h->part_rr.p);
 }
 void spmv_any(int lanes, int grid, cudaStream_t s, dg_handle *h, int first, int flexible) {
+  if (h->elem_mv) {  // matrix-free product with the element matrices
+    cg_direction<<<grid, kVecThreads, 0, s>>>(h->n, h->z.p, h->p.p, h->part_rz.p, h->part_rzo.p, h->sc.p, first,
+                                              flexible);
+    elem_contrib<<<h->el_nrun, 256, 0, s>>>(h->d_el_run.p, h->d_el_eptr.p, h->d_el_local.p, h->d_el_off.p,
+                                            h->d_el_mat.p, h->p.p, h->d_el_c.p);
+    elem_pull_pq<<<grid, kVecThreads, 0, s>>>(h->n, h->d_el_rptr.p, h->d_el_ridx.p, h->d_el_c.p, h->p.p, h->q.p,
+                                              h->part_pq.p);
+    return;
+  }
   switch (lanes) {
     case 1: launch_spmv<1>(grid, s, h, first, flexible); break;
     case 2: launch_spmv<2>(grid, s, h, first, flexible); break;
@@ -647,9 +660,34 @@ dg_status do_setup(dg_handle *h) {
       for (size_t k = 0; k < gi.size(); k++) { gi[k] = h->ii[k] - shift; gj[k] = h->jj[k] - shift; }
       h->d_gi.upload(gi);
       h->d_gj.upload(gj);
+      h->elem_mv = false;
       if (h->have_elements) {
         h->d_el_eptr.upload(h->el_eptr); h->d_el_local.upload(h->el_local);
         h->d_el_off.upload(h->el_off); h->d_el_mat.upload(h->el_mat);
+        if (c.elemental_matvec == 1) {
+          // element runs of at most kElemChunk matrix values; per row, its
+          // contribution slots in element order
+          const int nell = (int)h->el_eptr.size() - 1;
+          std::vector<int> run(1, 0);
+          for (int e = 0; e < nell; e++) {
+            const int64_t sz = h->el_off[(size_t)e + 1] - h->el_off[(size_t)e];
+            if (sz > kElemChunk) throw CudaError{cudaErrorInvalidValue, "element matrix larger than the matvec stage"};
+            if (h->el_off[(size_t)e + 1] - h->el_off[(size_t)run.back()] > kElemChunk) run.push_back(e);
+          }
+          run.push_back(nell);
+          std::vector<int64_t> rptr((size_t)n + 1, 0);
+          for (int l : h->el_local) rptr[(size_t)l + 1]++;
+          for (int i = 0; i < n; i++) rptr[(size_t)i + 1] += rptr[(size_t)i];
+          std::vector<int> ridx(h->el_local.size());
+          std::vector<int64_t> fillp(rptr.begin(), rptr.end() - 1);
+          for (size_t t = 0; t < h->el_local.size(); t++) ridx[(size_t)fillp[(size_t)h->el_local[t]]++] = (int)t;
+          h->d_el_run.upload(run);
+          h->el_nrun = (int)run.size() - 1;
+          h->d_el_rptr.upload(rptr);
+          h->d_el_ridx.upload(ridx);
+          h->d_el_c.alloc(std::max<size_t>(h->el_local.size(), 1));
+          h->elem_mv = true;
+        }
       }
     }
     h->Ap.upload(S.A.ptr); h->Ac.upload(S.A.col); h->Av.upload(S.A.val);
@@ -988,6 +1026,13 @@ dg_status dg_set_option(dg_handle *h, const char *name, const char *value) {
     int v;
     if (!parse_i10(w2, v)) return fail(h, DG_BAD_INPUT, "bad replace_every");
     h->ctl.replace_every = v;
+    return DG_OK;
+  }
+  if (w1 == "elemental_matvec") {
+    int v;
+    if (!parse_i10(w2, v)) return fail(h, DG_BAD_INPUT, "bad elemental_matvec");
+    h->ctl.elemental_matvec = v;
+    h->ready = false;
     return DG_OK;
   }
   if (w1 == "reuse_factors") {

@@ -34,6 +34,7 @@ struct Controls {
   int nd_leaf = 24;                 // nested-dissection leaf size of the subdomain factors
   int profile = 0;                  // 1: CUDA-event timing of the solve phases
   int reuse_factors = 0;            // 1: a solve after the first keeps the numeric factors
+  int elemental_matvec = 0;         // 1: PCG products with the stored element matrices
 };
 
 // Parse one "name value" line the way util_actionOnCtrlArg does

@@ -153,3 +153,25 @@ def test_elements_p1_gpu_vs_oracle(precision):
         assert np.linalg.norm(x - ro["x"]) <= 1e-10 * np.linalg.norm(ro["x"])
     else:
         assert np.linalg.norm(x - ro["x"]) <= 1e-7 * np.linalg.norm(ro["x"])
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision", [0, 1])
+def test_elemental_matvec_gpu(precision):
+    # PCG products with the stored element matrices (elemental_matvec 1) give the
+    # same solve as the assembled CSR products
+    ngf, eptr, efree, emat, erhs, info = _p1_elements(nodes=65, seed=9, kappa=True)
+    opts = dict(solver=2, method=1, fine_method=1, levels=2, smoothers=1, overlap=1, strong1="0.08",
+                radius1=2, solve_tolerance="1.0e-10", solve_maxiters=500)
+    xs = []
+    for emv in (0, 1):
+        s = D.DougSolver(opts)
+        s.set_option("precision", precision)
+        s.set_option("elemental_matvec", emv)
+        s.set_elements(ngf, eptr, efree, emat, erhs)
+        s.setup()
+        xs.append(s.solve())
+    (x0, s0), (x1, s1) = xs
+    assert abs(s0.iterations - s1.iterations) <= 1
+    assert s1.true_rel_residual <= 1.01e-10
+    assert np.linalg.norm(x1 - x0) <= (1e-10 if precision == 0 else 1e-7) * np.linalg.norm(x0)
