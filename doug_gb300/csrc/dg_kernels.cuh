@@ -104,6 +104,34 @@ constexpr int kTile = 64;    // trailing-update tile (64 x 64 per CTA step, 4x4 
 // once E is formed; the update (Schur complement) block stays in the arena
 // for the parent's extend-add.
 
+// Extend-add of column b of a child's update block into column pb of the
+// parent (Dst = the parent's column base): rows a >= b, by the lanes of one
+// warp.  kEaBatch rows per lane are loaded (child values, target rows, old
+// target values) before any is stored, so a warp keeps many independent
+// loads in flight; the targets of one child column are distinct.
+constexpr int kEaBatch = 4;
+
+template <typename T>
+__device__ __forceinline__ void extend_add_column(T *__restrict__ Dst, const int *__restrict__ rel,
+                                                  const T *__restrict__ Ucol, int b, int rc, int lane) {
+  for (int a0 = b + lane; a0 < rc; a0 += 32 * kEaBatch) {
+    int row[kEaBatch];
+    T val[kEaBatch], old[kEaBatch];
+#pragma unroll
+    for (int u = 0; u < kEaBatch; u++) {
+      const int a = a0 + 32 * u;
+      row[u] = a < rc ? rel[a] : 0;
+      val[u] = a < rc ? Ucol[a] : T(0);
+    }
+#pragma unroll
+    for (int u = 0; u < kEaBatch; u++)
+      if (a0 + 32 * u < rc) old[u] = Dst[row[u]];
+#pragma unroll
+    for (int u = 0; u < kEaBatch; u++)
+      if (a0 + 32 * u < rc) Dst[row[u]] = old[u] + val[u];
+  }
+}
+
 // Fronts whose pivot panel (m x k) and E (m x k) fit in shared memory: one
 // CTA per front.  The pivot columns are assembled straight into shared
 // memory, the update block in the arena; the panel is factored and E formed
@@ -149,13 +177,11 @@ mf_factor_panel(MfView v, const int *__restrict__ fronts, const double *__restri
     const int mc = v.f_m[c], kc = v.f_k[c], rc = mc - kc;
     const T *U = arena + v.f_off[c] + (int64_t)kc * mc + kc;
     const int *rel = v.relmap + v.f_relmap[c];
-    for (int q = tid; q < rc * rc; q += nt) {
-      const int b = q / rc, a = q % rc;
-      if (a < b) continue;
-      const int col = rel[b], row = rel[a];
-      const T val = U[(int64_t)b * mc + a];
-      if (col < k) P[col * m + row] += val;
-      else F[(int64_t)col * m + row] += val;
+    const int lane = tid & 31, wid = tid >> 5, nw = nt / 32;
+    for (int b = wid; b < rc; b += nw) {
+      const int col = rel[b];
+      T *Dst = col < k ? P + col * m : F + (int64_t)col * m;
+      extend_add_column<T>(Dst, rel, U + (int64_t)b * mc, b, rc, lane);
     }
     __syncthreads();
   }
@@ -275,10 +301,8 @@ mf_assemble_large(MfView v, const int2 *__restrict__ tasks, const double *__rest
     const T *U = arena + v.f_off[c] + (int64_t)kc * mc + kc;
     const int *rel = v.relmap + v.f_relmap[c];
     const int blo = lower_bound32(rel, 0, rc, c0), bhi = lower_bound32(rel, blo, rc, c1);
-    for (int b = blo + wid; b < bhi; b += nw) {
-      const int pb = rel[b];
-      for (int a = b + lane; a < rc; a += 32) F[(int64_t)pb * m + rel[a]] += U[(int64_t)b * mc + a];
-    }
+    for (int b = blo + wid; b < bhi; b += nw)
+      extend_add_column<T>(F + (int64_t)rel[b] * m, rel, U + (int64_t)b * mc, b, rc, lane);
     __syncthreads();
   }
 }
