@@ -86,6 +86,7 @@ struct MfDevice {
     int j0, diag_off, diag_cnt, panel_off, panel_cnt, esc_off, esc_cnt;
     int upd_off, upd_cnt, etile_off, etile_cnt;
     int kw, cend_base;
+    bool big;                     // trailing update in 128 x 128 tiles (FP32)
   };
   struct Level {
     int pan_off, pan_cnt, asm_off, asm_cnt;
@@ -172,7 +173,7 @@ struct MfDevice {
       for (int S0 = 0; S0 < kmax; S0 += kSuperPanel) {
         for (int j0 = S0; j0 < std::min(S0 + kSuperPanel, kmax); j0 += kNB) {
           Step st{j0, (int)df.size(), 0, (int)pf.size(), 0, (int)es.size(), 0,
-                  (int)ut.size(), 0, (int)et.size(), 0, kNB, S0 + kSuperPanel};
+                  (int)ut.size(), 0, (int)et.size(), 0, kNB, S0 + kSuperPanel, false};
           for (int f : large) {
             int m = B.f_m[(size_t)f], k = B.f_k[(size_t)f];
             if (j0 >= k) continue;
@@ -196,13 +197,15 @@ struct MfDevice {
           st.etile_cnt = (int)et.size() - st.etile_off;
           L.steps.push_back(st);
         }
+        const bool bigt = sizeof(T) == 4;  // FP32: 128 x 128 tiles; FP64 keeps 64 x 64 (FP64-pipe bound)
+        const int tile = bigt ? kBT : kTile;
         Step st{S0, (int)df.size(), 0, (int)pf.size(), 0, (int)es.size(), 0,
-                (int)ut.size(), 0, (int)et.size(), 0, kSuperPanel, 0};
+                (int)ut.size(), 0, (int)et.size(), 0, kSuperPanel, 0, bigt};
         for (int f : large) {
           int m = B.f_m[(size_t)f], k = B.f_k[(size_t)f];
           if (S0 >= k) continue;
           const int c1 = S0 + std::min(kSuperPanel, k - S0);
-          const int nt = (m - c1 + kTile - 1) / kTile;
+          const int nt = (m - c1 + tile - 1) / tile;
           for (int tj = 0; tj < nt; tj++)
             for (int ti = tj; ti < nt; ti++) ut.push_back(make_int2(f, (ti << 16) | tj));
         }
@@ -315,7 +318,12 @@ struct MfDevice {
               view, panel_tasks.p + st.panel_off, st.panel_cnt, esc_tasks.p + st.esc_off, st.j0, arena.p, E.p);
           launches++;
         }
-        if (st.upd_cnt + st.etile_cnt) {
+        if (st.big) {
+          if constexpr (sizeof(T) == 4) {  // planned for FP32 batches only
+            mf_update_big<T><<<st.upd_cnt, 256, 0, s>>>(view, upd_tasks.p + st.upd_off, st.j0, st.kw, arena.p);
+            launches++;
+          }
+        } else if (st.upd_cnt + st.etile_cnt) {
           mf_update<T><<<st.upd_cnt + st.etile_cnt, kMfThreads, 0, s>>>(
               view, upd_tasks.p + st.upd_off, st.upd_cnt, etile_tasks.p + st.etile_off, st.j0, st.kw,
               st.cend_base, arena.p, E.p);
@@ -508,6 +516,8 @@ struct dg_handle {
   int *d_host_status = nullptr;
   cudaEvent_t ev[10]{};
   cudaStream_t s2 = nullptr;        // coarse-level stream (runs beside the subdomain solves)
+  cudaStream_t sf = nullptr;        // high-priority stream of the subdomain factorisation
+  cudaEvent_t fine_ev = nullptr;
   cudaStream_t s3 = nullptr;        // capture stream of the iteration graph
   cudaGraphExec_t iter_exec = nullptr;
   int iter_nodes = 0;
@@ -515,6 +525,8 @@ struct dg_handle {
   ~dg_handle() {
     if (iter_exec) cudaGraphExecDestroy(iter_exec);
     if (s2) cudaStreamDestroy(s2);
+    if (sf) cudaStreamDestroy(sf);
+    if (fine_ev) cudaEventDestroy(fine_ev);
     if (s3) cudaStreamDestroy(s3);
     if (fork_ev) cudaEventDestroy(fork_ev);
     if (join_ev) cudaEventDestroy(join_ev);
@@ -707,7 +719,13 @@ dg_status do_setup(dg_handle *h) {
       CK(cudaHostGetDevicePointer(&h->d_host_out, h->host_out, 0));
       CK(cudaHostGetDevicePointer(&h->d_host_status, h->host_status, 0));
       for (auto &e : h->ev) CK(cudaEventCreate(&e));
-      CK(cudaStreamCreateWithFlags(&h->s2, cudaStreamNonBlocking));
+      // the subdomain factorisation is the longer of the two factorisation
+      // chains: its stream gets the highest priority, the coarse stream the lowest
+      int prio_lo = 0, prio_hi = 0;
+      CK(cudaDeviceGetStreamPriorityRange(&prio_lo, &prio_hi));
+      CK(cudaStreamCreateWithPriority(&h->s2, cudaStreamNonBlocking, prio_lo));
+      CK(cudaStreamCreateWithPriority(&h->sf, cudaStreamNonBlocking, prio_hi));
+      CK(cudaEventCreateWithFlags(&h->fine_ev, cudaEventDisableTiming));
       CK(cudaStreamCreateWithFlags(&h->s3, cudaStreamNonBlocking));
       CK(cudaEventCreateWithFlags(&h->fork_ev, cudaEventDisableTiming));
       CK(cudaEventCreateWithFlags(&h->join_ev, cudaEventDisableTiming));
@@ -800,8 +818,14 @@ dg_status do_solve(dg_handle *h, const double *d_b, double *d_x, dg_stats *st, c
       launches += h->co64->factor(h->ACv.p, h->status.p, h->s2);
       CK(cudaEventRecord(h->join_ev, h->s2));
     }
-    if (fine && !sgs && refactor)
-      launches += mixed ? h->sub32->factor(h->Av.p, h->status.p, s) : h->sub64->factor(h->Av.p, h->status.p, s);
+    if (fine && !sgs && refactor) {
+      CK(cudaEventRecord(h->fork_ev, s));
+      CK(cudaStreamWaitEvent(h->sf, h->fork_ev, 0));
+      launches += mixed ? h->sub32->factor(h->Av.p, h->status.p, h->sf)
+                        : h->sub64->factor(h->Av.p, h->status.p, h->sf);
+      CK(cudaEventRecord(h->fine_ev, h->sf));
+      CK(cudaStreamWaitEvent(s, h->fine_ev, 0));
+    }
     if (coarse && refactor) CK(cudaStreamWaitEvent(s, h->join_ev, 0));
     CK(cudaEventRecord(h->ev[1], s));
     CK(cudaMemcpyAsync(h->b.p, d_b, (size_t)n * sizeof(double), cudaMemcpyDeviceToDevice, s));
