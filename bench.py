@@ -40,7 +40,7 @@ PARTS_PER_DIM = 4
 SEED = 0
 TOL = "1.0e-8"
 CTL = dict(solver=2, method=1, fine_method=1, levels=2, overlap=2, smoothers=1,
-           strong1="0.08", radius1=4, maxasize1=200, solve_tolerance=TOL, solve_maxiters=2000)
+           strong1="0.08", radius1=5, maxasize1=400, solve_tolerance=TOL, solve_maxiters=2000)
 METRIC = "time to rel. residual 1e-8 (s), mixed+batched vs plain FP64 PCG, 1 GB300"
 SUBSOLVE_TRAFFIC_BYTES = 4.5975e9  # ncu, one PCG iteration of the 128^3 mixed solve
 WORKLOAD = ("128^3 log-normal diffusion (sigma 1, corr. length 8), 7-point FV, 2,097,152 unknowns; "

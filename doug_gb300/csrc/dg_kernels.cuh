@@ -137,10 +137,12 @@ __device__ __forceinline__ void extend_add_column(T *__restrict__ Dst, const int
 // memory, the update block in the arena; the panel is factored and E formed
 // in shared memory, E is written out, and the update block receives
 // -L21 L21^T in 4x4 register blocks.
-constexpr int kPanThreads = 128;
+constexpr int kPanThreads = 128;       // fronts of up to kPanWideRows rows
+constexpr int kPanThreadsWide = 256;   // larger fronts
+constexpr int kPanWideRows = 160;
 
 template <typename T>
-__global__ void __launch_bounds__(kPanThreads)
+__global__ void __launch_bounds__(kPanThreadsWide)
 mf_factor_panel(MfView v, const int *__restrict__ fronts, const double *__restrict__ vals,
                 T *__restrict__ arena, T *__restrict__ E, int *__restrict__ status) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -151,7 +153,7 @@ mf_factor_panel(MfView v, const int *__restrict__ fronts, const double *__restri
   T *Es = P + m * k;                         // m x k elimination matrix, ld m
   const int64_t off = v.f_off[f];
   T *F = arena + off;
-  const int tid = threadIdx.x, nt = kPanThreads;
+  const int tid = threadIdx.x, nt = blockDim.x;
   // 1. zero: panel and E = [I ; 0] in shared memory, update block in the arena
   for (int q = tid; q < m * k; q += nt) {
     P[q] = T(0);

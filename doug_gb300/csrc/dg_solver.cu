@@ -89,7 +89,7 @@ struct MfDevice {
     bool big;                     // trailing update in 128 x 128 tiles (FP32)
   };
   struct Level {
-    int pan_off, pan_cnt, asm_off, asm_cnt;
+    int pan_off, pan_cnt, asm_off, asm_cnt, pan_maxm;
     size_t pan_smem;
     std::vector<Step> steps;
   };
@@ -146,6 +146,7 @@ struct MfDevice {
       Level &L = levels[(size_t)l];
       L.pan_off = (int)pn.size();
       L.pan_smem = 0;
+      L.pan_maxm = 0;
       L.asm_off = (int)at.size();
       std::vector<int> large;
       for (int q = B.lvl_ptr[(size_t)l]; q < B.lvl_ptr[(size_t)l + 1]; q++) {
@@ -155,6 +156,7 @@ struct MfDevice {
         if (m <= kPanelFrontRows && smem <= kPanelSmem) {
           pn.push_back(f);
           L.pan_smem = std::max(L.pan_smem, smem);
+          L.pan_maxm = std::max(L.pan_maxm, m);
         } else {
           large.push_back(f);
         }
@@ -300,7 +302,7 @@ struct MfDevice {
     for (int l = 0; l < nlevels; l++) {
       const Level &L = levels[(size_t)l];
       if (L.pan_cnt) {
-        mf_factor_panel<T><<<L.pan_cnt, kPanThreads, L.pan_smem, s>>>(view, pan_fronts.p + L.pan_off, vals,
+        mf_factor_panel<T><<<L.pan_cnt, L.pan_maxm > kPanWideRows ? kPanThreadsWide : kPanThreads, L.pan_smem, s>>>(view, pan_fronts.p + L.pan_off, vals,
                                                                       arena.p, E.p, status);
         launches++;
       }
