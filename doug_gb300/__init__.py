@@ -39,7 +39,7 @@ EXPORTED_SYMBOLS = [
     "dg_solve_device", "dg_write_solution", "dg_get_sizes", "dg_get_aggregates",
     "dg_get_subdomains", "dg_get_restriction", "dg_get_coarse_matrix", "dg_residual_csr",
     "dg_set_elements", "dg_get_input", "dg_grad_matrix", "dg_grad_elements",
-    "dg_residual_csr_noalloc",
+    "dg_residual_csr_noalloc", "dg_autotune",
 ]
 
 
@@ -111,6 +111,7 @@ def load_library(path: str | None = None):
     L.dg_set_rhs.argtypes = [vp, P(C.c_double)]
     L.dg_grad_matrix.argtypes = [vp, vp, vp, vp, vp]
     L.dg_grad_elements.argtypes = [vp, vp, vp, vp, vp]
+    L.dg_autotune.argtypes = [vp, P(C.c_double), P(C.c_int)]
     L.dg_set_elements.argtypes = [vp, C.c_int, C.c_int, P(C.c_int), P(C.c_int), P(C.c_double), P(C.c_double)]
     L.dg_get_input.argtypes = [vp, P(C.c_int), P(C.c_int), P(C.c_int), P(C.c_int), P(C.c_double),
                                P(C.c_double)]
@@ -241,6 +242,17 @@ class DougSolver:
     # --- setup / solve ----------------------------------------------------
     def setup(self) -> None:
         self._check(self._L.dg_setup(self._h))
+
+    def autotune(self) -> tuple[dict, float]:
+        """Time full solves of the stored right-hand side over a grid of the
+        batch parameters (nd_leaf, panel_rows, fwd_task_kb, lean_task_kb),
+        keep the fastest and leave the solver set up with it.  Returns the
+        chosen words and the fastest factor + iterate time in seconds."""
+        t = C.c_double(0.0)
+        ch = (C.c_int * 4)()
+        self._check(self._L.dg_autotune(self._h, C.byref(t), ch))
+        keys = ("nd_leaf", "panel_rows", "fwd_task_kb", "lean_task_kb")
+        return {k: int(ch[i]) for i, k in enumerate(keys)}, t.value
 
     def setup_host_only(self) -> int:
         """Run the host setup; a missing GPU is reported, not raised.  The

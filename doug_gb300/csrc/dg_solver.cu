@@ -62,13 +62,16 @@ static double wall() {
 }
 
 // one multifrontal batch on the device, factor precision T
-// fronts of at most kPanelFrontRows rows whose panel and E fit in kPanelSmem
+// fronts of at most panel_rows rows whose panel and E fit in kPanelSmem
 // bytes are factored by one CTA each; the others by the multi-CTA pipeline
-constexpr int kPanelFrontRows = 512;
 constexpr size_t kPanelSmem = 96 * 1024;
 constexpr int kSuperPanel = 128;      // columns of L per trailing update of a large front
-constexpr int64_t kFwdTaskBytes = 96 * 1024;  // E bytes per forward task of a large front
-constexpr int64_t kLeanTaskBytes = 80 * 1024; // levels with smaller average tasks use 128-thread CTAs
+// tunable batch parameters (control words panel_rows, fwd_task_kb, lean_task_kb)
+struct MfTune {
+  int panel_rows = 512;                  // fronts of at most this many rows may use mf_factor_panel
+  int64_t fwd_task_bytes = 96 * 1024;    // E bytes per forward task of a large front
+  int64_t lean_task_bytes = 80 * 1024;   // levels with smaller average tasks use 128-thread CTAs
+};
 
 template <typename T>
 struct MfDevice {
@@ -105,7 +108,7 @@ struct MfDevice {
   int64_t xlen = 0;
   MfView view{};
 
-  void upload(const MfBatch &B) {
+  void upload(const MfBatch &B, const MfTune &tune) {
     f_off.upload(B.f_off); f_rows.upload(B.f_rows); f_xoff.upload(B.f_xoff);
     f_uoff.upload(B.f_uoff); f_woff.upload(B.f_woff); f_relmap.upload(B.f_relmap);
     f_asm.upload(B.f_asm); asm_tgt.upload(B.asm_tgt); asm_sp.upload(B.asm_sp);
@@ -153,7 +156,7 @@ struct MfDevice {
         int f = B.lvl_fronts[(size_t)q];
         int m = B.f_m[(size_t)f], k = B.f_k[(size_t)f];
         const size_t smem = (size_t)2 * m * k * sizeof(T);
-        if (m <= kPanelFrontRows && smem <= kPanelSmem) {
+        if (m <= tune.panel_rows && smem <= kPanelSmem) {
           pn.push_back(f);
           L.pan_smem = std::max(L.pan_smem, smem);
           L.pan_maxm = std::max(L.pan_maxm, m);
@@ -244,7 +247,7 @@ struct MfDevice {
         int f = B.lvl_fronts[(size_t)q];
         int m = B.f_m[(size_t)f], k = B.f_k[(size_t)f];
         if (m <= kSolveSmall) { ss.push_back(f); continue; }
-        // forward tasks: runs of row chunks of at least kFwdTaskBytes of E each
+        // forward tasks: runs of row chunks of at least tune.fwd_task_bytes of E each
         const int RC = FwdRows<T>::N, nch = (m + RC - 1) / RC;
         for (int c = 0; c < nch;) {
           int c1 = c;
@@ -253,7 +256,7 @@ struct MfDevice {
             const int r0 = c1 * RC, K = r0 < k ? std::min(k, r0 + RC) : k;
             bytes += (int64_t)RC * K * (int64_t)sizeof(T);
             c1++;
-          } while (c1 < nch && bytes < kFwdTaskBytes);
+          } while (c1 < nch && bytes < tune.fwd_task_bytes);
           fl.push_back({(int)std::min<int64_t>(bytes, 1 << 30), make_int2(f, (c << 16) | (c1 - c))});
           fwd_bytes += bytes;
           c = c1;
@@ -272,8 +275,8 @@ struct MfDevice {
       L.small_cnt = (int)ss.size() - L.small_off;
       L.fwd_cnt = (int)fw.size() - L.fwd_off;
       L.bwd_cnt = (int)bw.size() - L.bwd_off;
-      L.fwd_lean = L.fwd_cnt && fwd_bytes / L.fwd_cnt < kLeanTaskBytes;
-      L.bwd_lean = L.bwd_cnt && bwd_bytes / L.bwd_cnt < kLeanTaskBytes;
+      L.fwd_lean = L.fwd_cnt && fwd_bytes / L.fwd_cnt < tune.lean_task_bytes;
+      L.bwd_lean = L.bwd_cnt && bwd_bytes / L.bwd_cnt < tune.lean_task_bytes;
       fwd_smem_max = std::max(fwd_smem_max, L.fwd_smem);
       bwd_smem_max = std::max(bwd_smem_max, L.bwd_smem);
     }
@@ -641,14 +644,22 @@ void resid_any(int lanes, int grid, cudaStream_t s, dg_handle *h, const double *
   }
 }
 
-dg_status do_setup(dg_handle *h) {
+// host setup (aggregation, R, AC, subdomains; skipped with reuse_host when
+// it is current), symbolic analysis and device upload
+dg_status do_setup(dg_handle *h, bool reuse_host = false) {
   if (!h->have_matrix) return fail(h, DG_NOT_READY, "no matrix: call dg_set_matrix_coo or dg_load_ctl first");
   std::string err;
   Controls c = h->ctl;
   ctl_finish(c);
   double t0 = wall();
-  if (!build_setup(c, h->n, h->ii, h->jj, h->vv, h->part.empty() ? nullptr : &h->part, h->nparts, h->S, err))
-    return fail(h, DG_BAD_INPUT, err);
+  if (!(reuse_host && h->S.n == h->n && h->S.n > 0)) {
+    if (!build_setup(c, h->n, h->ii, h->jj, h->vv, h->part.empty() ? nullptr : &h->part, h->nparts, h->S, err))
+      return fail(h, DG_BAD_INPUT, err);
+  }
+  MfTune tune;
+  tune.panel_rows = c.panel_rows;
+  tune.fwd_task_bytes = (int64_t)c.fwd_task_kb * 1024;
+  tune.lean_task_bytes = (int64_t)c.lean_task_kb * 1024;
   MfOptions mo;
   mo.leaf = c.nd_leaf;
   try {
@@ -748,9 +759,9 @@ dg_status do_setup(dg_handle *h) {
         h->sgs->build(S.A, S.sd_ptr, S.sd_nodes);
         arena_rows = &h->sgs->gidx_h;
       } else if (h->precision == 1) {
-        h->sub32.reset(new MfDevice<float>()); h->sub32->upload(h->Bsub);
+        h->sub32.reset(new MfDevice<float>()); h->sub32->upload(h->Bsub, tune);
       } else {
-        h->sub64.reset(new MfDevice<double>()); h->sub64->upload(h->Bsub);
+        h->sub64.reset(new MfDevice<double>()); h->sub64->upload(h->Bsub, tune);
       }
       // pull lists: subdomain arena positions of every node, subdomain order
       std::vector<int64_t> pp((size_t)n + 1, 0);
@@ -767,7 +778,7 @@ dg_status do_setup(dg_handle *h) {
     }
     if (c.levels > 1) {
       h->co64.reset(new MfDevice<double>());
-      h->co64->upload(h->Bco);
+      h->co64->upload(h->Bco, tune);
       std::vector<int> cp((size_t)S.AC.nrows, 0);
       for (int64_t q = 0; q < (int64_t)h->Bco.gidx.size(); q++) cp[(size_t)h->Bco.gidx[(size_t)q]] = (int)q;
       h->cpos.upload(cp);
@@ -1054,6 +1065,13 @@ dg_status dg_set_option(dg_handle *h, const char *name, const char *value) {
     h->ctl.replace_every = v;
     return DG_OK;
   }
+  if (w1 == "panel_rows" || w1 == "fwd_task_kb" || w1 == "lean_task_kb") {
+    int v;
+    if (!parse_i10(w2, v) || v < 1) return fail(h, DG_BAD_INPUT, "bad " + w1);
+    (w1 == "panel_rows" ? h->ctl.panel_rows : w1 == "fwd_task_kb" ? h->ctl.fwd_task_kb : h->ctl.lean_task_kb) = v;
+    h->ready = false;
+    return DG_OK;
+  }
   if (w1 == "elemental_matvec") {
     int v;
     if (!parse_i10(w2, v)) return fail(h, DG_BAD_INPUT, "bad elemental_matvec");
@@ -1221,6 +1239,56 @@ dg_status dg_set_partition(dg_handle *h, const int *part, int nparts) {
 dg_status dg_setup(dg_handle *h) {
   if (!h) return DG_BAD_INPUT;
   return do_setup(h);
+}
+
+dg_status dg_autotune(dg_handle *h, double *best_seconds, int *chosen) {
+  if (!h) return DG_BAD_INPUT;
+  if (!h->have_matrix) return fail(h, DG_NOT_READY, "no matrix: call dg_set_matrix_coo or dg_load_ctl first");
+  // candidates: nested-dissection leaf x panel cutover x forward task size;
+  // each is timed by a full solve (factorisations + PCG) of the stored rhs,
+  // the host aggregation / restriction / coarse matrix are built once
+  struct Cand { int leaf, panel_rows, fwd_kb, lean_kb; };
+  const Cand cands[] = {{24, 512, 96, 80}, {16, 512, 96, 80}, {32, 512, 96, 80}, {24, 256, 96, 80},
+                        {24, 512, 64, 48}, {24, 512, 160, 96}};
+  const Controls keep = h->ctl;
+  double best = 1e300;
+  Cand pick = cands[0];
+  bool host_ready = false;
+  for (const Cand &cd : cands) {
+    h->ctl = keep;
+    h->ctl.nd_leaf = cd.leaf;
+    h->ctl.panel_rows = cd.panel_rows;
+    h->ctl.fwd_task_kb = cd.fwd_kb;
+    h->ctl.lean_task_kb = cd.lean_kb;
+    h->ready = false;
+    dg_status st = do_setup(h, host_ready);
+    if (st != DG_OK) { h->ctl = keep; return st; }
+    host_ready = true;
+    const size_t bytes = (size_t)h->n * sizeof(double);
+    if (cudaMemcpy(h->hb.p, h->rhs.data(), bytes, cudaMemcpyHostToDevice) != cudaSuccess)
+      return fail(h, DG_CUDA_ERROR, "H2D copy failed");
+    dg_stats ss{};
+    double t = 0;
+    for (int rep = 0; rep < 2; rep++) {  // the first solve also captures the iteration graph
+      st = do_solve(h, h->hb.p, h->hx.p, &ss, 0);
+      if (st != DG_OK && st != DG_NOT_CONVERGED) { h->ctl = keep; return st; }
+      t = ss.t_total_s;
+    }
+    if (t < best) { best = t; pick = cd; }
+  }
+  h->ctl = keep;
+  h->ctl.nd_leaf = pick.leaf;
+  h->ctl.panel_rows = pick.panel_rows;
+  h->ctl.fwd_task_kb = pick.fwd_kb;
+  h->ctl.lean_task_kb = pick.lean_kb;
+  h->ready = false;
+  dg_status st = do_setup(h, true);
+  if (best_seconds) *best_seconds = best;
+  if (chosen) {
+    chosen[0] = pick.leaf; chosen[1] = pick.panel_rows;
+    chosen[2] = pick.fwd_kb; chosen[3] = pick.lean_kb;
+  }
+  return st;
 }
 
 dg_status dg_solve_device(dg_handle *h, const double *d_b, double *d_x, dg_stats *stats, void *stream) {

@@ -35,6 +35,10 @@ struct Controls {
   int profile = 0;                  // 1: CUDA-event timing of the solve phases
   int reuse_factors = 0;            // 1: a solve after the first keeps the numeric factors
   int elemental_matvec = 0;         // 1: PCG products with the stored element matrices
+  // tuning of the multifrontal batches (dg_autotune chooses them)
+  int panel_rows = 512;             // fronts up to this size (and panel + E <= 96 KB): one CTA each
+  int fwd_task_kb = 96;             // KB of E per forward task of a large front
+  int lean_task_kb = 80;            // levels with smaller average tasks use 128-thread CTAs
 };
 
 // Parse one "name value" line the way util_actionOnCtrlArg does

@@ -127,6 +127,16 @@ dg_status dg_set_partition(dg_handle *h, const int *part, int nparts);
  * device upload.  Must follow the matrix. */
 dg_status dg_setup(dg_handle *h);
 
+/* Autotuner (no reference counterpart: the reference's factorisation has no
+ * batch parameters).  Times full solves (factorisations + PCG) of the stored
+ * RHS over a small grid of the control words nd_leaf, panel_rows, fwd_task_kb
+ * and lean_task_kb, keeps the fastest and leaves the handle set up with it.
+ * The host aggregation, restriction and coarse matrix are built once.
+ * best_seconds (may be NULL) receives the fastest factor + iterate time and
+ * chosen (may be NULL) the four words nd_leaf, panel_rows, fwd_task_kb,
+ * lean_task_kb in that order. */
+dg_status dg_autotune(dg_handle *h, double *best_seconds, int *chosen);
+
 /* Solve with host buffers (b may be NULL: the stored RHS is used).  x must
  * hold n doubles.  stats may be NULL. */
 dg_status dg_solve(dg_handle *h, const double *b, double *x, dg_stats *stats);

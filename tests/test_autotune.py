@@ -1,0 +1,77 @@
+"""Batch parameters of the multifrontal factorisation and the autotuner.
+
+The control words panel_rows, fwd_task_kb, lean_task_kb and nd_leaf change
+only how fronts are batched into kernels (and, for nd_leaf, the elimination
+order inside a subdomain): every setting must give the oracle's solution to
+the FP64 bar.  dg_autotune times full solves over a grid of them and must
+leave the handle set up with one of the grid's points.
+"""
+import numpy as np
+import pytest
+
+import oracle as O
+import doug_gb300 as D
+from doug_gb300 import problems as P
+
+OPTS = dict(solver=2, method=1, fine_method=1, levels=2, overlap=2, smoothers=1, strong1="0.08",
+            radius1=2, solve_tolerance="1.0e-10", solve_maxiters=1000)
+GRID = {(24, 512, 96, 80), (16, 512, 96, 80), (32, 512, 96, 80), (24, 256, 96, 80),
+        (24, 512, 64, 48), (24, 512, 160, 96)}
+
+
+def _ctl_text(d):
+    return "".join(f"{k} {v}\n" for k, v in d.items())
+
+
+@pytest.mark.parametrize("word", ["panel_rows", "fwd_task_kb", "lean_task_kb"])
+def test_tuning_words_reject_bad_values(word):
+    s = D.DougSolver({})
+    s.set_option(word, 64)
+    for bad in (0, -3, "x"):
+        with pytest.raises(D.DougError):
+            s.set_option(word, bad)
+
+
+@pytest.fixture(scope="module")
+def diffusion24():
+    n, r, c, v, b = P.diffusion3d_fv(24, seed=13)
+    ro = O.run_coo(n, r, c, v, rhs=b, ctl=_ctl_text(OPTS))
+    assert ro["status"] == 0
+    return n, r, c, v, b, ro
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("words", [dict(panel_rows=16), dict(panel_rows=48, fwd_task_kb=4, lean_task_kb=1),
+                                   dict(fwd_task_kb=1024, lean_task_kb=4096), dict(nd_leaf=8)])
+@pytest.mark.parametrize("precision", [0, 1])
+def test_batch_parameters_keep_the_solution(diffusion24, words, precision):
+    n, r, c, v, b, ro = diffusion24
+    s = D.DougSolver(OPTS)
+    s.set_option("precision", precision)
+    for k, val in words.items():
+        s.set_option(k, val)
+    s.set_matrix_coo(n, r, c, v)
+    s.set_rhs(b)
+    s.setup()
+    x, st = s.solve()
+    if precision == 0:
+        assert abs(st.iterations - ro["iterations"]) <= 1
+        assert np.linalg.norm(x - ro["x"]) <= 1e-10 * np.linalg.norm(ro["x"])
+    else:
+        assert st.true_rel_residual <= 1.01e-10
+        assert np.linalg.norm(x - ro["x"]) <= 1e-7 * np.linalg.norm(ro["x"])
+
+
+@pytest.mark.gpu
+def test_autotune_picks_a_grid_point_and_solves(diffusion24):
+    n, r, c, v, b, ro = diffusion24
+    s = D.DougSolver(OPTS)
+    s.set_option("precision", 1)
+    s.set_matrix_coo(n, r, c, v)
+    s.set_rhs(b)
+    words, best = s.autotune()
+    assert (words["nd_leaf"], words["panel_rows"], words["fwd_task_kb"], words["lean_task_kb"]) in GRID
+    assert 0 < best < 60
+    x, st = s.solve()
+    assert st.true_rel_residual <= 1.01e-10
+    assert np.linalg.norm(x - ro["x"]) <= 1e-7 * np.linalg.norm(ro["x"])
