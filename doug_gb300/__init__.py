@@ -39,7 +39,7 @@ EXPORTED_SYMBOLS = [
     "dg_solve_device", "dg_write_solution", "dg_get_sizes", "dg_get_aggregates",
     "dg_get_subdomains", "dg_get_restriction", "dg_get_coarse_matrix", "dg_residual_csr",
     "dg_set_elements", "dg_get_input", "dg_grad_matrix", "dg_grad_elements",
-    "dg_residual_csr_noalloc", "dg_autotune",
+    "dg_residual_csr_noalloc", "dg_autotune", "dg_set_systems", "dg_get_system_stats",
 ]
 
 
@@ -112,6 +112,9 @@ def load_library(path: str | None = None):
     L.dg_grad_matrix.argtypes = [vp, vp, vp, vp, vp]
     L.dg_grad_elements.argtypes = [vp, vp, vp, vp, vp]
     L.dg_autotune.argtypes = [vp, P(C.c_double), P(C.c_int)]
+    L.dg_set_systems.argtypes = [vp, C.c_int, P(C.c_int), P(C.c_longlong), P(C.c_int), P(C.c_int),
+                                 P(C.c_double), P(C.c_double)]
+    L.dg_get_system_stats.argtypes = [vp, P(C.c_int), P(C.c_int), P(C.c_double), P(C.c_double)]
     L.dg_set_elements.argtypes = [vp, C.c_int, C.c_int, P(C.c_int), P(C.c_int), P(C.c_double), P(C.c_double)]
     L.dg_get_input.argtypes = [vp, P(C.c_int), P(C.c_int), P(C.c_int), P(C.c_int), P(C.c_double),
                                P(C.c_double)]
@@ -242,6 +245,40 @@ class DougSolver:
     # --- setup / solve ----------------------------------------------------
     def setup(self) -> None:
         self._check(self._L.dg_setup(self._h))
+
+    def set_systems(self, systems, rhs=None) -> None:
+        """Batched independent systems: ``systems`` is a sequence of
+        (n, rows1, cols1, vals) with 1-based indices per system; ``rhs`` an
+        optional sequence of right-hand sides (default b = 1).  dg_solve then
+        takes and returns the concatenated vectors; system_stats() gives the
+        per-system iterations, status, residuals and times."""
+        ns = np.array([int(t[0]) for t in systems], np.int32)
+        nz = np.array([len(t[3]) for t in systems], np.int64)
+        r = np.ascontiguousarray(np.concatenate([np.asarray(t[1], np.int32) for t in systems]))
+        c = np.ascontiguousarray(np.concatenate([np.asarray(t[2], np.int32) for t in systems]))
+        v = np.ascontiguousarray(np.concatenate([np.asarray(t[3], np.float64) for t in systems]))
+        b = None
+        if rhs is not None:
+            b = np.ascontiguousarray(np.concatenate([np.asarray(x, np.float64) for x in rhs]))
+            if b.shape[0] != int(ns.sum()):
+                raise ValueError("right-hand sides do not match the systems' sizes")
+        self._check(self._L.dg_set_systems(self._h, len(systems), _ip(ns), nz.ctypes.data_as(C.POINTER(C.c_longlong)),
+                                           _ip(r), _ip(c), _dp(v), _dp(b) if b is not None else None))
+        self._sys_n = ns
+
+    def system_stats(self) -> dict:
+        """Per-system results of the last batched solve (numpy arrays)."""
+        k = len(self._sys_n)
+        it = np.zeros(k, np.int32)
+        stt = np.zeros(k, np.int32)
+        rel = np.zeros(k)
+        sec = np.zeros(k)
+        self._check(self._L.dg_get_system_stats(self._h, _ip(it), _ip(stt), _dp(rel), _dp(sec)))
+        return {"iterations": it, "status": stt, "rel_residual": rel, "seconds": sec}
+
+    def split(self, x):
+        """Splits a concatenated batched vector into the systems' vectors."""
+        return np.split(np.asarray(x), np.cumsum(self._sys_n)[:-1])
 
     def autotune(self) -> tuple[dict, float]:
         """Time full solves of the stored right-hand side over a grid of the

@@ -1081,12 +1081,17 @@ pull_prolong_dot(int n, const int64_t *__restrict__ pull_ptr, const int64_t *__r
                  const T *__restrict__ xl, const int64_t *__restrict__ Pp, const int *__restrict__ Pcp,
                  const TP *__restrict__ Pv, const double *__restrict__ xc,
                  int mode, const double *__restrict__ r, double *__restrict__ z,
-                 double *__restrict__ zold, double *__restrict__ part_rz, double *__restrict__ part_rzo) {
+                 double *__restrict__ zold, double *__restrict__ part_rz, double *__restrict__ part_rzo,
+                 const int *__restrict__ cb = nullptr) {
   // mode bit 0: fine subdomains on; bit 1: coarse on; bit 2: identity fine (z=r);
-  // bit 3: keep z_old and produce r.z_old
+  // bit 3: keep z_old and produce r.z_old.  cb (batched systems): CTA b owns
+  // the rows [cb[b], cb[b+1]) and its partial sums are that chunk's.
   __shared__ double sh[32];
   double srz = 0.0, srzo = 0.0;
-  for (int g = blockIdx.x * kVecThreads + threadIdx.x; g < n; g += gridDim.x * kVecThreads) {
+  const int g0 = cb ? cb[blockIdx.x] + threadIdx.x : blockIdx.x * kVecThreads + threadIdx.x;
+  const int gend = cb ? cb[blockIdx.x + 1] : n;
+  const int gstep = cb ? kVecThreads : gridDim.x * kVecThreads;
+  for (int g = g0; g < gend; g += gstep) {
     double sv = 0.0;
     if (mode & 4) {
       sv = r[g];
@@ -1278,6 +1283,220 @@ __global__ void cg_finish(double *__restrict__ sc, const double *__restrict__ pa
       host_out[5] = sc[SC_PQ];
       *host_status = *status;
     }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Batched independent systems (dg_set_systems).  The systems are the diagonal
+// blocks of one matrix; every CTA of these vector kernels owns one chunk
+// [cb[c], cb[c+1]) of the rows of system csys[c], so partial sums are per
+// chunk and the CG scalars per system (bsc[k * BS_N + ...]).  A system leaves
+// the iteration when its own residual test passes: its x, r and p are then
+// frozen while the others go on, which makes each system's iterates those of
+// its own PCG.
+// ---------------------------------------------------------------------------
+constexpr int kBatchChunk = 2048;  // rows per CTA of the batched vector kernels
+enum { BS_RHO_PREV = 0, BS_RHO = 1, BS_ALPHA = 2, BS_RES = 3, BS_INIT = 4, BS_BETA = 5, BS_PQ = 6,
+       BS_TRUE = 7, BS_N = 8 };
+// per-system state
+enum { BT_DONE = 0, BT_ACTIVE = 1, BT_CHECK = 2, BT_BREAKDOWN = 3 };
+// bt_scalars steps
+enum { BT_RHO = 0, BT_ALPHA = 1, BT_INIT = 2, BT_FINISH = 3, BT_CONFIRM = 4, BT_REPORT = 5 };
+
+__global__ void __launch_bounds__(kVecThreads)
+bt_direction(const int *__restrict__ cb, const int *__restrict__ csys, const int *__restrict__ state,
+             const double *__restrict__ bsc, const double *__restrict__ z, double *__restrict__ p, int first) {
+  const int k = csys[blockIdx.x];
+  if (state[k] != BT_ACTIVE) return;
+  const double beta = bsc[k * BS_N + BS_BETA];
+  const int i1 = cb[blockIdx.x + 1];
+  for (int i = cb[blockIdx.x] + threadIdx.x; i < i1; i += kVecThreads)
+    p[i] = first ? z[i] : __dadd_rn(z[i], __dmul_rn(beta, p[i]));
+}
+
+// q = A p on the chunk's rows (LANES lanes per row), partial p.q
+template <int LANES>
+__global__ void __launch_bounds__(kVecThreads)
+bt_spmv_pq(const int *__restrict__ cb, const int *__restrict__ csys, const int *__restrict__ state,
+           const int64_t *__restrict__ Ap, const int *__restrict__ Ac, const double *__restrict__ Av,
+           const double *__restrict__ p, double *__restrict__ q, double *__restrict__ part_pq) {
+  __shared__ double sh[32];
+  if (state[csys[blockIdx.x]] != BT_ACTIVE) {
+    if (threadIdx.x == 0) part_pq[blockIdx.x] = 0.0;
+    return;
+  }
+  const int sub = threadIdx.x % LANES;
+  const int rows_per_block = kVecThreads / LANES;
+  const int i1 = cb[blockIdx.x + 1];
+  double spq = 0.0;
+  for (int row0 = cb[blockIdx.x]; row0 < i1; row0 += rows_per_block) {
+    const int i = row0 + threadIdx.x / LANES;
+    double s = 0.0;
+    if (i < i1) {
+      int64_t e = Ap[i] + sub;
+      const int64_t e1 = Ap[i + 1];
+      if (LANES == 1) {
+        for (; e + 4 <= e1; e += 4) {
+          const int c0 = Ac[e], c1 = Ac[e + 1], c2 = Ac[e + 2], c3 = Ac[e + 3];
+          const double a0 = Av[e], a1 = Av[e + 1], a2 = Av[e + 2], a3 = Av[e + 3];
+          const double p0 = p[c0], p1 = p[c1], p2 = p[c2], p3 = p[c3];
+          s = __fma_rn(a0, p0, s);
+          s = __fma_rn(a1, p1, s);
+          s = __fma_rn(a2, p2, s);
+          s = __fma_rn(a3, p3, s);
+        }
+      }
+      for (; e < e1; e += LANES) s = __fma_rn(Av[e], p[Ac[e]], s);
+    }
+#pragma unroll
+    for (int o = LANES / 2; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o, LANES);
+    if (i < i1 && sub == 0) {
+      q[i] = s;
+      spq += p[i] * s;
+    }
+  }
+  double b = block_sum<kVecThreads>(spq, sh);
+  if (threadIdx.x == 0) part_pq[blockIdx.x] = b;
+}
+
+// x += alpha_k p; r -= alpha_k q; partial r.r
+__global__ void __launch_bounds__(kVecThreads)
+bt_update(const int *__restrict__ cb, const int *__restrict__ csys, const int *__restrict__ state,
+          const double *__restrict__ bsc, const double *__restrict__ p, const double *__restrict__ q,
+          double *__restrict__ x, double *__restrict__ r, double *__restrict__ part_rr) {
+  __shared__ double sh[32];
+  const int k = csys[blockIdx.x];
+  if (state[k] != BT_ACTIVE) {
+    if (threadIdx.x == 0) part_rr[blockIdx.x] = 0.0;
+    return;
+  }
+  const double alpha = bsc[k * BS_N + BS_ALPHA];
+  const int i1 = cb[blockIdx.x + 1];
+  double srr = 0.0;
+  for (int i = cb[blockIdx.x] + threadIdx.x; i < i1; i += kVecThreads) {
+    x[i] = __dadd_rn(x[i], __dmul_rn(alpha, p[i]));
+    const double ri = __dsub_rn(r[i], __dmul_rn(alpha, q[i]));
+    r[i] = ri;
+    srr += ri * ri;
+  }
+  double b = block_sum<kVecThreads>(srr, sh);
+  if (threadIdx.x == 0) part_rr[blockIdx.x] = b;
+}
+
+// r = b - A x on the chunks of the systems in state `want` (all when want < 0)
+template <int LANES>
+__global__ void __launch_bounds__(kVecThreads)
+bt_residual(const int *__restrict__ cb, const int *__restrict__ csys, const int *__restrict__ state, int want,
+            const int64_t *__restrict__ Ap, const int *__restrict__ Ac, const double *__restrict__ Av,
+            const double *__restrict__ x, const double *__restrict__ b, double *__restrict__ r,
+            double *__restrict__ part_rr) {
+  __shared__ double sh[32];
+  if (want >= 0 && state[csys[blockIdx.x]] != want) {
+    if (threadIdx.x == 0) part_rr[blockIdx.x] = 0.0;
+    return;
+  }
+  const int sub = threadIdx.x % LANES;
+  const int rows_per_block = kVecThreads / LANES;
+  const int i1 = cb[blockIdx.x + 1];
+  double srr = 0.0;
+  for (int row0 = cb[blockIdx.x]; row0 < i1; row0 += rows_per_block) {
+    const int i = row0 + threadIdx.x / LANES;
+    double s = 0.0;
+    if (i < i1)
+      for (int64_t e = Ap[i] + sub; e < Ap[i + 1]; e += LANES) s = __fma_rn(Av[e], x[Ac[e]], s);
+#pragma unroll
+    for (int o = LANES / 2; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o, LANES);
+    if (i < i1 && sub == 0) {
+      const double ri = __dsub_rn(b[i], s);
+      r[i] = ri;
+      srr += ri * ri;
+    }
+  }
+  double t = block_sum<kVecThreads>(srr, sh);
+  if (threadIdx.x == 0) part_rr[blockIdx.x] = t;
+}
+
+// Per-system CG scalars from the chunk partials (one warp per system, chunks
+// summed in a fixed order), the state machine and the counts the host reads.
+// One CTA of 1024 threads.  dit: the device iteration counter (incremented by
+// BT_FINISH), so that a captured graph needs no per-iteration argument.
+__global__ void __launch_bounds__(1024)
+bt_scalars(int nsys, const int *__restrict__ sys_cptr, int step, int first, int flexible, int mixed, double tol2,
+           const double *__restrict__ part_a, const double *__restrict__ part_b, double *__restrict__ bsc,
+           int *__restrict__ state, int *__restrict__ iters, int *__restrict__ dit,
+           volatile int *__restrict__ host_counts) {
+  __shared__ int cnt[3];
+  if (threadIdx.x < 3) cnt[threadIdx.x] = 0;
+  __syncthreads();
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  const int it = *dit + (step == BT_FINISH ? 1 : 0);
+  for (int k = wid; k < nsys; k += nw) {
+    double *sc = bsc + (size_t)k * BS_N;
+    const int c0 = sys_cptr[k], c1 = sys_cptr[k + 1];
+    double a = 0.0, b = 0.0;
+    for (int c = c0 + lane; c < c1; c += 32) a += part_a[c];
+    a = __shfl_sync(0xffffffffu, warp_sum(a), 0);
+    if (step == BT_RHO && flexible && !first) {
+      for (int c = c0 + lane; c < c1; c += 32) b += part_b[c];
+      b = __shfl_sync(0xffffffffu, warp_sum(b), 0);
+    }
+    int stt = state[k];
+    if (lane == 0) {
+      switch (step) {
+        case BT_RHO:
+          if (stt == BT_ACTIVE) {
+            sc[BS_RHO] = a;
+            sc[BS_BETA] = first ? 0.0 : flexible ? __ddiv_rn(__dsub_rn(a, b), sc[BS_RHO_PREV])
+                                                 : __ddiv_rn(a, sc[BS_RHO_PREV]);
+          }
+          break;
+        case BT_ALPHA:
+          if (stt == BT_ACTIVE) {
+            sc[BS_PQ] = a;
+            sc[BS_ALPHA] = __ddiv_rn(sc[BS_RHO], a);
+            if (!(a > 0.0)) { stt = BT_BREAKDOWN; iters[k] = *dit + 1; }
+          }
+          break;
+        case BT_INIT:
+          sc[BS_RES] = a;
+          sc[BS_INIT] = a == 0.0 ? 1.0 : a;
+          sc[BS_TRUE] = a;
+          sc[BS_RHO_PREV] = 0.0;
+          stt = BT_ACTIVE;
+          iters[k] = 0;
+          break;
+        case BT_FINISH:
+          if (stt == BT_ACTIVE) {
+            sc[BS_RES] = a;
+            sc[BS_RHO_PREV] = sc[BS_RHO];
+            iters[k] = it;
+            if (a != a) stt = BT_BREAKDOWN;
+            else if (!(a / sc[BS_INIT] > tol2)) stt = mixed ? BT_CHECK : BT_DONE;
+          }
+          break;
+        case BT_CONFIRM:  // the FP64 true residual decides; r now holds it
+          if (stt == BT_CHECK) {
+            sc[BS_RES] = a;
+            stt = a / sc[BS_INIT] > tol2 ? BT_ACTIVE : BT_DONE;
+          }
+          break;
+        default:  // BT_REPORT
+          sc[BS_TRUE] = a;
+          break;
+      }
+      state[k] = stt;
+      if (stt == BT_ACTIVE) atomicAdd(&cnt[0], 1);
+      else if (stt == BT_CHECK) atomicAdd(&cnt[1], 1);
+      else if (stt == BT_BREAKDOWN) atomicAdd(&cnt[2], 1);
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    if (step == BT_FINISH) *dit = it;
+    if (step == BT_INIT) *dit = 0;
+    host_counts[0] = cnt[0];
+    host_counts[1] = cnt[1];
+    host_counts[2] = cnt[2];
   }
 }
 

@@ -14,6 +14,7 @@
 
 #include <algorithm>
 #include <chrono>
+#include <climits>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -500,6 +501,16 @@ struct dg_handle {
   DBuf<double> d_el_mat;
   bool factored = false;          // the device holds factors of the current setup
   int nparts = 0;
+  // batched independent systems (dg_set_systems): system k owns the rows
+  // [sys_row[k], sys_row[k+1]) and the triplets [sys_tri[k], sys_tri[k+1])
+  int nsys = 0;
+  std::vector<int64_t> sys_row, sys_tri;
+  int nchunks = 0;                // row chunks of the batched vector kernels
+  DBuf<int> d_cb, d_csys, d_sys_cptr, d_state, d_iters, d_dit;
+  DBuf<double> bsc;               // per-system CG scalars
+  int *host_counts = nullptr, *d_host_counts = nullptr;  // mapped pinned
+  std::vector<int> sys_iters, sys_state;
+  std::vector<double> sys_relres, sys_seconds;
   SetupResult S;
   MfBatch Bsub, Bco;
   double t_setup = 0;
@@ -537,6 +548,7 @@ struct dg_handle {
     if (join_ev) cudaEventDestroy(join_ev);
     if (host_out) cudaFreeHost(host_out);
     if (host_status) cudaFreeHost(host_status);
+    if (host_counts) cudaFreeHost(host_counts);
     for (auto &e : ev) if (e) cudaEventDestroy(e);
   }
 };
@@ -644,6 +656,32 @@ void resid_any(int lanes, int grid, cudaStream_t s, dg_handle *h, const double *
   }
 }
 
+// batched systems: the chunked product and residual
+template <int L>
+void launch_bt(cudaStream_t s, dg_handle *h, int resid, int want, double *rr) {
+  if (resid)
+    bt_residual<L><<<h->nchunks, kVecThreads, 0, s>>>(h->d_cb.p, h->d_csys.p, h->d_state.p, want, h->Ap.p, h->Ac.p,
+                                                      h->Av.p, h->x.p, h->b.p, rr, h->part_rr.p);
+  else
+    bt_spmv_pq<L><<<h->nchunks, kVecThreads, 0, s>>>(h->d_cb.p, h->d_csys.p, h->d_state.p, h->Ap.p, h->Ac.p, h->Av.p,
+                                                     h->p.p, h->q.p, h->part_pq.p);
+}
+void bt_any(cudaStream_t s, dg_handle *h, int resid, int want = -1, double *rr = nullptr) {
+  switch (h->lanes) {
+    case 1: launch_bt<1>(s, h, resid, want, rr); break;
+    case 2: launch_bt<2>(s, h, resid, want, rr); break;
+    case 4: launch_bt<4>(s, h, resid, want, rr); break;
+    case 8: launch_bt<8>(s, h, resid, want, rr); break;
+    case 16: launch_bt<16>(s, h, resid, want, rr); break;
+    default: launch_bt<32>(s, h, resid, want, rr); break;
+  }
+}
+void bt_step(dg_handle *h, cudaStream_t s, int step, int first, int mixed, double tol2, const double *pa,
+             const double *pb) {
+  bt_scalars<<<1, 1024, 0, s>>>(h->nsys, h->d_sys_cptr.p, step, first, mixed, mixed, tol2, pa, pb, h->bsc.p,
+                                h->d_state.p, h->d_iters.p, h->d_dit.p, h->d_host_counts);
+}
+
 // host setup (aggregation, R, AC, subdomains; skipped with reuse_host when
 // it is current), symbolic analysis and device upload
 dg_status do_setup(dg_handle *h, bool reuse_host = false) {
@@ -653,8 +691,14 @@ dg_status do_setup(dg_handle *h, bool reuse_host = false) {
   ctl_finish(c);
   double t0 = wall();
   if (!(reuse_host && h->S.n == h->n && h->S.n > 0)) {
-    if (!build_setup(c, h->n, h->ii, h->jj, h->vv, h->part.empty() ? nullptr : &h->part, h->nparts, h->S, err))
+    if (h->nsys > 0) {
+      if (!h->part.empty()) return fail(h, DG_BAD_INPUT, "a partition vector cannot be combined with batched systems");
+      if (!build_setup_systems(c, h->sys_row, h->sys_tri, h->ii, h->jj, h->vv, h->S, err))
+        return fail(h, DG_BAD_INPUT, err);
+    } else if (!build_setup(c, h->n, h->ii, h->jj, h->vv, h->part.empty() ? nullptr : &h->part, h->nparts, h->S,
+                            err)) {
       return fail(h, DG_BAD_INPUT, err);
+    }
   }
   MfTune tune;
   tune.panel_rows = c.panel_rows;
@@ -718,9 +762,31 @@ dg_status do_setup(dg_handle *h, bool reuse_host = false) {
     h->Ap.upload(S.A.ptr); h->Ac.upload(S.A.col); h->Av.upload(S.A.val);
     h->lanes = lanes_for(S.A);
     for (auto *v : {&h->b, &h->x, &h->r, &h->p, &h->q, &h->z, &h->zold, &h->hb, &h->hx}) v->alloc((size_t)n);
+    h->nchunks = 0;
+    if (h->nsys > 0) {  // chunks of at most kBatchChunk rows, none across two systems
+      std::vector<int> cb(1, 0), csys, cptr(1, 0);
+      for (int k = 0; k < h->nsys; k++) {
+        for (int64_t r = h->sys_row[(size_t)k]; r < h->sys_row[(size_t)k + 1]; r += kBatchChunk) {
+          cb.push_back((int)std::min<int64_t>(r + kBatchChunk, h->sys_row[(size_t)k + 1]));
+          csys.push_back(k);
+        }
+        cptr.push_back((int)csys.size());
+      }
+      h->nchunks = (int)csys.size();
+      h->d_cb.upload(cb); h->d_csys.upload(csys); h->d_sys_cptr.upload(cptr);
+      h->d_state.alloc((size_t)h->nsys); h->d_iters.alloc((size_t)h->nsys); h->d_dit.alloc(1);
+      h->bsc.alloc((size_t)h->nsys * BS_N);
+      CK(cudaMemset(h->d_state.p, 0, (size_t)h->nsys * sizeof(int)));
+      CK(cudaMemset(h->bsc.p, 0, (size_t)h->nsys * BS_N * sizeof(double)));
+      if (!h->host_counts) {
+        CK(cudaHostAlloc(&h->host_counts, 4 * sizeof(int), cudaHostAllocMapped));
+        CK(cudaHostGetDevicePointer(&h->d_host_counts, h->host_counts, 0));
+      }
+    }
+    const size_t nparts_sum = std::max<size_t>(kRedBlocks, (size_t)h->nchunks);
     for (auto *v : {&h->part_rz, &h->part_rzo, &h->part_pq, &h->part_rr}) {
-      v->alloc(kRedBlocks);
-      CK(cudaMemset(v->p, 0, kRedBlocks * sizeof(double)));
+      v->alloc(nparts_sum);
+      CK(cudaMemset(v->p, 0, nparts_sum * sizeof(double)));
     }
     h->sc.alloc(8);
     CK(cudaMemset(h->sc.p, 0, 8 * sizeof(double)));
@@ -799,18 +865,267 @@ dg_status do_setup(dg_handle *h, bool reuse_host = false) {
   return DG_OK;
 }
 
+// what one solve applies, from the control words
+struct SolvePlan {
+  bool fine = false, sgs = false, coarse = false, mixed = false;
+  int sgs_iters = 3, mode = 0;
+};
+
+SolvePlan plan_of(const dg_handle *h, const Controls &c) {
+  SolvePlan pl;
+  pl.fine = (c.fine_method == 1 || c.fine_method == 2) && c.method != 0;
+  pl.sgs = c.fine_method == 2;
+  pl.sgs_iters = c.num_iters <= 0 ? 3 : c.num_iters;  // aggr.F90:221
+  pl.coarse = c.levels > 1 && c.method != 0;
+  pl.mixed = h->precision == 1;
+  if (c.method == 0) pl.mode |= 4;
+  else if (c.fine_method == 0) pl.mode |= 4;
+  else pl.mode |= 1;
+  // (the reference adds the coarse correction only for method 1, pcg.F90:191-193)
+  if (pl.coarse && (c.method == 1 || c.method == 5)) pl.mode |= 2;  // method 5: pcg.F90:205-208
+  if (pl.mixed) pl.mode |= 8;
+  return pl;
+}
+
+// numeric factorisations (the reference factorises lazily in the first
+// preconditioner call, subsolvers.F90:78-101, pcg.F90:166-178): the coarse
+// factorisation on the low-priority stream beside the subdomain
+// factorisations on the high-priority one.  Returns the number of kernels.
+int factor_all(dg_handle *h, const SolvePlan &pl, cudaStream_t s) {
+  int launches = 0;
+  if (pl.coarse) {
+    CK(cudaEventRecord(h->fork_ev, s));
+    CK(cudaStreamWaitEvent(h->s2, h->fork_ev, 0));
+    launches += h->co64->factor(h->ACv.p, h->status.p, h->s2);
+    CK(cudaEventRecord(h->join_ev, h->s2));
+  }
+  if (pl.fine && !pl.sgs) {
+    CK(cudaEventRecord(h->fork_ev, s));
+    CK(cudaStreamWaitEvent(h->sf, h->fork_ev, 0));
+    launches += pl.mixed ? h->sub32->factor(h->Av.p, h->status.p, h->sf)
+                         : h->sub64->factor(h->Av.p, h->status.p, h->sf);
+    CK(cudaEventRecord(h->fine_ev, h->sf));
+    CK(cudaStreamWaitEvent(s, h->fine_ev, 0));
+  }
+  if (pl.coarse) CK(cudaStreamWaitEvent(s, h->join_ev, 0));
+  return launches;
+}
+
+// z = M r and the r.z partials: restriction + coarse solve on the second
+// stream beside the subdomain solves, then the pull sum with the
+// prolongation.  pg: grid of the pull kernel; cb: the chunk table of batched
+// systems (one chunk per CTA) or null.  Returns the number of kernels.
+int precondition(dg_handle *h, const SolvePlan &pl, cudaStream_t st, bool profile, int pg, const int *cb) {
+  const int grid = kRedBlocks;
+  const int n = h->n;
+  int nl = 0;
+  if (pl.coarse) {  // restriction + coarse solve on the second stream
+    CK(cudaEventRecord(h->fork_ev, st));
+    CK(cudaStreamWaitEvent(h->s2, h->fork_ev, 0));
+    if (profile) CK(cudaEventRecord(h->ev[4], h->s2));
+    if (pl.mixed)
+      restrict_to_coarse<float><<<grid, kVecThreads, 0, h->s2>>>(h->Rp.p, h->Rc.p, h->Rvf.p, h->r.p, h->cpos.p, h->co64->xl.p, h->S.R.nrows);
+    else
+      restrict_to_coarse<double><<<grid, kVecThreads, 0, h->s2>>>(h->Rp.p, h->Rc.p, h->Rv.p, h->r.p, h->cpos.p, h->co64->xl.p, h->S.R.nrows);
+    nl += 1 + h->co64->solve(h->s2);
+    if (profile) CK(cudaEventRecord(h->ev[5], h->s2));
+    CK(cudaEventRecord(h->join_ev, h->s2));
+  }
+  if (profile) CK(cudaEventRecord(h->ev[3], st));
+  if (pl.fine && pl.sgs) {
+    sgs_subdomains<<<h->sgs->nsd, kSgsThreads, 0, st>>>(h->sgs->view, h->sgs->sd_ptr.p, pl.sgs_iters, h->r.p,
+                                                         h->sgs->x.p);
+    nl++;
+  } else if (pl.fine) {
+    if (pl.mixed) {
+      gather_subdomains<float><<<grid, kVecThreads, 0, st>>>(h->r.p, h->sub32->gidx.p, h->sub32->xl.p, h->sub32->xlen);
+      nl += 1 + h->sub32->solve(st);
+    } else {
+      gather_subdomains<double><<<grid, kVecThreads, 0, st>>>(h->r.p, h->sub64->gidx.p, h->sub64->xl.p, h->sub64->xlen);
+      nl += 1 + h->sub64->solve(st);
+    }
+  }
+  if (profile) CK(cudaEventRecord(h->ev[8], st));
+  if (pl.coarse) CK(cudaStreamWaitEvent(st, h->join_ev, 0));
+  const double *xc = pl.coarse ? h->co64->xl.p : nullptr;
+  if (pl.sgs && pl.mixed)
+    pull_prolong_dot<double, float><<<pg, kVecThreads, 0, st>>>(
+        n, h->pull_ptr.p, h->pull_idx.p, pl.fine ? h->sgs->x.p : nullptr, h->Pp.p, h->Pc.p, h->Pvf.p, xc,
+        pl.mode, h->r.p, h->z.p, h->zold.p, h->part_rz.p, h->part_rzo.p, cb);
+  else if (pl.sgs)
+    pull_prolong_dot<double, double><<<pg, kVecThreads, 0, st>>>(
+        n, h->pull_ptr.p, h->pull_idx.p, pl.fine ? h->sgs->x.p : nullptr, h->Pp.p, h->Pc.p, h->Pv.p, xc,
+        pl.mode, h->r.p, h->z.p, h->zold.p, h->part_rz.p, h->part_rzo.p, cb);
+  else if (pl.mixed)
+    pull_prolong_dot<float, float><<<pg, kVecThreads, 0, st>>>(
+        n, h->pull_ptr.p, h->pull_idx.p, pl.fine ? h->sub32->xl.p : nullptr, h->Pp.p, h->Pc.p, h->Pvf.p, xc,
+        pl.mode, h->r.p, h->z.p, h->zold.p, h->part_rz.p, h->part_rzo.p, cb);
+  else
+    pull_prolong_dot<double, double><<<pg, kVecThreads, 0, st>>>(
+        n, h->pull_ptr.p, h->pull_idx.p, pl.fine ? h->sub64->xl.p : nullptr, h->Pp.p, h->Pc.p, h->Pv.p, xc,
+        pl.mode, h->r.p, h->z.p, h->zold.p, h->part_rz.p, h->part_rzo.p, cb);
+  return nl + 1;
+}
+
+// Batched independent systems: every system runs its own pcg_weigs
+// (pcg.F90:289-462) with its own scalars and stopping test; the
+// factorisations, preconditioner applications and products of all systems
+// share the launches.  A system that stops is frozen (its rows are skipped by
+// the direction, product and update kernels).
+dg_status do_solve_batch(dg_handle *h, const double *d_b, double *d_x, dg_stats *st, cudaStream_t s) {
+  Controls c = h->ctl;
+  ctl_finish(c);
+  const int n = h->n, K = h->nsys, nch = h->nchunks;
+  const SolvePlan pl = plan_of(h, c);
+  const int mixed = pl.mixed ? 1 : 0;
+  const double tol = c.solve_tolerance, tol2 = tol * tol;
+  const int maxit = c.solve_maxiters == -1 ? 100000 : c.solve_maxiters;
+  int launches = 0;
+  dg_stats out{};
+  out.n = n;
+  out.nsubdomains = (int)h->S.sd_ptr.size() - 1;
+  out.ncoarse = h->S.AC.nrows;
+  out.factor_nnz = h->Bsub.factor_nnz;
+  out.factor_gflop = h->Bsub.factor_flops * 1e-9;
+  out.t_setup_s = h->t_setup;
+  try {
+    const double t0 = wall();
+    CK(cudaMemsetAsync(h->status.p, 0, sizeof(int), s));
+    CK(cudaEventRecord(h->ev[0], s));
+    if (!(c.reuse_factors && h->factored)) {
+      SolvePlan fp = pl;
+      fp.fine = pl.fine && !pl.sgs;
+      launches += factor_all(h, fp, s);
+    }
+    CK(cudaEventRecord(h->ev[1], s));
+    CK(cudaMemcpyAsync(h->b.p, d_b, (size_t)n * sizeof(double), cudaMemcpyDeviceToDevice, s));
+    CK(cudaMemsetAsync(h->x.p, 0, (size_t)n * sizeof(double), s));
+    CK(cudaMemsetAsync(h->p.p, 0, (size_t)n * sizeof(double), s));
+    CK(cudaMemsetAsync(h->zold.p, 0, (size_t)n * sizeof(double), s));
+    bt_any(s, h, 1, -1, h->r.p);  // r = b - A x0 for every system
+    bt_step(h, s, BT_INIT, 0, mixed, tol2, h->part_rr.p, nullptr);
+    launches += 2;
+    CK(cudaGetLastError());
+    int stv = 0;
+    CK(cudaMemcpyAsync(&stv, h->status.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    if (stv & ERR_NOT_SPD) {
+      h->factored = false;
+      return fail(h, DG_SINGULAR, "a subdomain or coarse matrix is not positive definite");
+    }
+    h->factored = true;
+    auto iteration = [&](cudaStream_t q, int first, bool replace) -> int {
+      int nl = precondition(h, pl, q, false, nch, h->d_cb.p);
+      bt_step(h, q, BT_RHO, first, mixed, tol2, h->part_rz.p, h->part_rzo.p);
+      bt_direction<<<nch, kVecThreads, 0, q>>>(h->d_cb.p, h->d_csys.p, h->d_state.p, h->bsc.p, h->z.p, h->p.p,
+                                               first);
+      bt_any(q, h, 0);
+      bt_step(h, q, BT_ALPHA, first, mixed, tol2, h->part_pq.p, nullptr);
+      bt_update<<<nch, kVecThreads, 0, q>>>(h->d_cb.p, h->d_csys.p, h->d_state.p, h->bsc.p, h->p.p, h->q.p, h->x.p,
+                                            h->r.p, h->part_rr.p);
+      nl += 5;
+      if (replace) {  // FP64 residual replacement, r = b - A x, of the iterating systems
+        bt_any(q, h, 1, BT_ACTIVE, h->r.p);
+        nl++;
+      }
+      bt_step(h, q, BT_FINISH, first, mixed, tol2, h->part_rr.p, nullptr);
+      return nl + 1;
+    };
+    if (!h->iter_exec) {
+      cudaGraph_t g = nullptr;
+      CK(cudaStreamBeginCapture(h->s3, cudaStreamCaptureModeThreadLocal));
+      h->iter_nodes = iteration(h->s3, 0, false);
+      CK(cudaStreamEndCapture(h->s3, &g));
+      CK(cudaGraphInstantiate(&h->iter_exec, g, 0));
+      CK(cudaGraphDestroy(g));
+    }
+    std::vector<double> t_end(1, wall() - t0);
+    int it = 0, active = K;
+    while (active > 0 && it < maxit) {
+      it++;
+      const int first = it == 1;
+      const bool replace = pl.mixed && c.replace_every > 0 && it % c.replace_every == 0;
+      if (!first && !replace) {
+        CK(cudaGraphLaunch(h->iter_exec, s));
+        launches += h->iter_nodes;
+      } else {
+        launches += iteration(s, first, replace);
+      }
+      CK(cudaGetLastError());
+      CK(cudaStreamSynchronize(s));
+      if (h->host_counts[1] > 0) {  // the FP64 true residual confirms the systems the recurrence stopped
+        bt_any(s, h, 1, BT_CHECK, h->r.p);
+        bt_step(h, s, BT_CONFIRM, 0, mixed, tol2, h->part_rr.p, nullptr);
+        launches += 2;
+        CK(cudaGetLastError());
+        CK(cudaStreamSynchronize(s));
+      }
+      t_end.push_back(wall() - t0);
+      active = h->host_counts[0];
+    }
+    CK(cudaEventRecord(h->ev[2], s));
+    // true residuals for the report (into q, which is free now)
+    bt_any(s, h, 1, -1, h->q.p);
+    bt_step(h, s, BT_REPORT, 0, mixed, tol2, h->part_rr.p, nullptr);
+    launches += 2;
+    CK(cudaMemcpyAsync(d_x, h->x.p, (size_t)n * sizeof(double), cudaMemcpyDeviceToDevice, s));
+    std::vector<double> bs((size_t)K * BS_N);
+    h->sys_iters.assign((size_t)K, 0);
+    h->sys_state.assign((size_t)K, 0);
+    CK(cudaMemcpyAsync(bs.data(), h->bsc.p, bs.size() * sizeof(double), cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(h->sys_iters.data(), h->d_iters.p, (size_t)K * sizeof(int), cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(h->sys_state.data(), h->d_state.p, (size_t)K * sizeof(int), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    float ms_f = 0, ms_i = 0;
+    CK(cudaEventElapsedTime(&ms_f, h->ev[0], h->ev[1]));
+    CK(cudaEventElapsedTime(&ms_i, h->ev[1], h->ev[2]));
+    h->sys_relres.assign((size_t)K, 0.0);
+    h->sys_seconds.assign((size_t)K, 0.0);
+    dg_status rc = DG_OK;
+    double init_sum = 0, res_sum = 0, worst = 0;
+    for (int k = 0; k < K; k++) {
+      const double *sc = &bs[(size_t)k * BS_N];
+      const double rel = std::sqrt(sc[BS_TRUE] / sc[BS_INIT]);
+      h->sys_relres[(size_t)k] = rel;
+      worst = std::max(worst, rel);
+      init_sum += sc[BS_INIT];
+      res_sum += sc[BS_RES];
+      const int ik = std::min<int>(std::max(h->sys_iters[(size_t)k], 0), it);
+      h->sys_seconds[(size_t)k] = t_end[(size_t)ik];
+      const int stt = h->sys_state[(size_t)k];
+      if (stt == BT_BREAKDOWN) {
+        rc = DG_BREAKDOWN;
+        h->err = "CG breakdown in system " + std::to_string(k + 1) + ": p.q <= 0 or NaN";
+      } else if (stt != BT_DONE && rc == DG_OK) {
+        rc = DG_NOT_CONVERGED;
+      }
+    }
+    out.iterations = it;
+    out.init_norm = std::sqrt(init_sum);
+    out.final_norm = std::sqrt(res_sum);
+    out.true_rel_residual = worst;
+    out.cond_num = 0.0;
+    out.t_factor_s = ms_f * 1e-3;
+    out.t_iterate_s = ms_i * 1e-3;
+    out.t_total_s = out.t_factor_s + out.t_iterate_s;
+    out.gpu_launches = launches;
+    if (st) *st = out;
+    return rc;
+  } catch (const CudaError &e) {
+    return cuda_fail(h, e);
+  }
+}
+
 // the solve: numeric factorisation + PCG (pcg_weigs, pcg.F90:289-462)
 dg_status do_solve(dg_handle *h, const double *d_b, double *d_x, dg_stats *st, cudaStream_t s) {
   if (!h->ready) return fail(h, DG_NOT_READY, "dg_setup has not run");
+  if (h->nsys > 0) return do_solve_batch(h, d_b, d_x, st, s);
   Controls c = h->ctl;
   ctl_finish(c);
   const int n = h->n;
   const int grid = kRedBlocks;
-  const bool fine = (c.fine_method == 1 || c.fine_method == 2) && c.method != 0;
-  const bool sgs = c.fine_method == 2;
-  const int sgs_iters = c.num_iters <= 0 ? 3 : c.num_iters;  // aggr.F90:221
-  const bool coarse = c.levels > 1 && c.method != 0;
-  const bool mixed = h->precision == 1;
+  const SolvePlan pl = plan_of(h, c);
+  const bool fine = pl.fine, sgs = pl.sgs, coarse = pl.coarse, mixed = pl.mixed;
   int launches = 0;
   dg_stats out{};
   out.n = n;
@@ -822,24 +1137,12 @@ dg_status do_solve(dg_handle *h, const double *d_b, double *d_x, dg_stats *st, c
   try {
     CK(cudaMemsetAsync(h->status.p, 0, sizeof(int), s));
     CK(cudaEventRecord(h->ev[0], s));
-    // numeric factorisations (the reference factorises lazily in the first
-    // preconditioner call, subsolvers.F90:78-101, pcg.F90:166-178)
     const bool refactor = !(c.reuse_factors && h->factored);
-    if (coarse && refactor) {  // the coarse factorisation runs beside the subdomain factorisations
-      CK(cudaEventRecord(h->fork_ev, s));
-      CK(cudaStreamWaitEvent(h->s2, h->fork_ev, 0));
-      launches += h->co64->factor(h->ACv.p, h->status.p, h->s2);
-      CK(cudaEventRecord(h->join_ev, h->s2));
+    if (refactor) {
+      SolvePlan fp = pl;
+      fp.fine = pl.fine && !pl.sgs;
+      launches += factor_all(h, fp, s);
     }
-    if (fine && !sgs && refactor) {
-      CK(cudaEventRecord(h->fork_ev, s));
-      CK(cudaStreamWaitEvent(h->sf, h->fork_ev, 0));
-      launches += mixed ? h->sub32->factor(h->Av.p, h->status.p, h->sf)
-                        : h->sub64->factor(h->Av.p, h->status.p, h->sf);
-      CK(cudaEventRecord(h->fine_ev, h->sf));
-      CK(cudaStreamWaitEvent(s, h->fine_ev, 0));
-    }
-    if (coarse && refactor) CK(cudaStreamWaitEvent(s, h->join_ev, 0));
     CK(cudaEventRecord(h->ev[1], s));
     CK(cudaMemcpyAsync(h->b.p, d_b, (size_t)n * sizeof(double), cudaMemcpyDeviceToDevice, s));
     CK(cudaMemsetAsync(h->x.p, 0, (size_t)n * sizeof(double), s));
@@ -869,13 +1172,6 @@ dg_status do_solve(dg_handle *h, const double *d_b, double *d_x, dg_stats *st, c
     int it = 0;
     std::vector<double> alphas, betas;
     dg_status rc = DG_OK;
-    int mode = 0;
-    if (c.method == 0) mode |= 4;
-    else if (c.fine_method == 0) mode |= 4;
-    else mode |= 1;
-    if (coarse && (c.method == 1 || c.method == 5)) mode |= 2;  // method 5: pcg.F90:205-208
-    if (mixed) mode |= 8;
-    // (the reference adds the coarse correction only for method 1, pcg.F90:191-193)
     const bool prof = c.profile != 0;
     double t_sub = 0, t_co = 0, t_sp = 0;
     auto lap = [&](int a, int b) -> double {
@@ -886,52 +1182,7 @@ dg_status do_solve(dg_handle *h, const double *d_b, double *d_x, dg_stats *st, c
     // one PCG iteration's launches on stream st (coarse branch forked to s2);
     // returns the number of kernels
     auto iteration = [&](cudaStream_t st, int first, bool replace, bool profile) -> int {
-      int nl = 0;
-      if (coarse) {  // restriction + coarse solve on the second stream
-        CK(cudaEventRecord(h->fork_ev, st));
-        CK(cudaStreamWaitEvent(h->s2, h->fork_ev, 0));
-        if (profile) CK(cudaEventRecord(h->ev[4], h->s2));
-        if (mixed)
-          restrict_to_coarse<float><<<grid, kVecThreads, 0, h->s2>>>(h->Rp.p, h->Rc.p, h->Rvf.p, h->r.p, h->cpos.p, h->co64->xl.p, h->S.R.nrows);
-        else
-          restrict_to_coarse<double><<<grid, kVecThreads, 0, h->s2>>>(h->Rp.p, h->Rc.p, h->Rv.p, h->r.p, h->cpos.p, h->co64->xl.p, h->S.R.nrows);
-        nl += 1 + h->co64->solve(h->s2);
-        if (profile) CK(cudaEventRecord(h->ev[5], h->s2));
-        CK(cudaEventRecord(h->join_ev, h->s2));
-      }
-      if (profile) CK(cudaEventRecord(h->ev[3], st));
-      if (fine && sgs) {
-        sgs_subdomains<<<h->sgs->nsd, kSgsThreads, 0, st>>>(h->sgs->view, h->sgs->sd_ptr.p, sgs_iters, h->r.p,
-                                                             h->sgs->x.p);
-        nl++;
-      } else if (fine) {
-        if (mixed) {
-          gather_subdomains<float><<<grid, kVecThreads, 0, st>>>(h->r.p, h->sub32->gidx.p, h->sub32->xl.p, h->sub32->xlen);
-          nl += 1 + h->sub32->solve(st);
-        } else {
-          gather_subdomains<double><<<grid, kVecThreads, 0, st>>>(h->r.p, h->sub64->gidx.p, h->sub64->xl.p, h->sub64->xlen);
-          nl += 1 + h->sub64->solve(st);
-        }
-      }
-      if (profile) CK(cudaEventRecord(h->ev[8], st));
-      if (coarse) CK(cudaStreamWaitEvent(st, h->join_ev, 0));
-      const double *xc = coarse ? h->co64->xl.p : nullptr;
-      if (sgs && mixed)
-        pull_prolong_dot<double, float><<<grid, kVecThreads, 0, st>>>(
-            n, h->pull_ptr.p, h->pull_idx.p, fine ? h->sgs->x.p : nullptr, h->Pp.p, h->Pc.p, h->Pvf.p, xc,
-            mode, h->r.p, h->z.p, h->zold.p, h->part_rz.p, h->part_rzo.p);
-      else if (sgs)
-        pull_prolong_dot<double, double><<<grid, kVecThreads, 0, st>>>(
-            n, h->pull_ptr.p, h->pull_idx.p, fine ? h->sgs->x.p : nullptr, h->Pp.p, h->Pc.p, h->Pv.p, xc,
-            mode, h->r.p, h->z.p, h->zold.p, h->part_rz.p, h->part_rzo.p);
-      else if (mixed)
-        pull_prolong_dot<float, float><<<grid, kVecThreads, 0, st>>>(
-            n, h->pull_ptr.p, h->pull_idx.p, fine ? h->sub32->xl.p : nullptr, h->Pp.p, h->Pc.p, h->Pvf.p, xc,
-            mode, h->r.p, h->z.p, h->zold.p, h->part_rz.p, h->part_rzo.p);
-      else
-        pull_prolong_dot<double, double><<<grid, kVecThreads, 0, st>>>(
-            n, h->pull_ptr.p, h->pull_idx.p, fine ? h->sub64->xl.p : nullptr, h->Pp.p, h->Pc.p, h->Pv.p, xc,
-            mode, h->r.p, h->z.p, h->zold.p, h->part_rz.p, h->part_rzo.p);
+      int nl = precondition(h, pl, st, profile, grid, nullptr);
       if (profile) CK(cudaEventRecord(h->ev[6], st));
       spmv_any(h->lanes, grid, st, h, first, mixed ? 1 : 0);
       if (profile) CK(cudaEventRecord(h->ev[7], st));
@@ -1184,6 +1435,8 @@ dg_status dg_load_ctl(dg_handle *h, const char *path) {
 dg_status dg_set_matrix_coo(dg_handle *h, int n, int nnz, const int *rows, const int *cols, const double *vals) {
   if (!h || n <= 0 || nnz <= 0 || !rows || !cols || !vals) return DG_BAD_INPUT;
   h->have_elements = false;  // set_elements sets it again after this call
+  h->nsys = 0;
+  h->S.n = 0;
   h->n = n;
   h->ii.assign(rows, rows + nnz);
   h->jj.assign(cols, cols + nnz);
@@ -1191,6 +1444,59 @@ dg_status dg_set_matrix_coo(dg_handle *h, int n, int nnz, const int *rows, const
   h->have_matrix = true;
   h->ready = false;
   if (!h->have_rhs || (int)h->rhs.size() != n) { h->rhs.assign((size_t)n, 1.0); h->have_rhs = false; }
+  return DG_OK;
+}
+
+dg_status dg_set_systems(dg_handle *h, int nsys, const int *n_sys, const long long *nnz_sys, const int *rows,
+                         const int *cols, const double *vals, const double *b) {
+  if (!h || nsys <= 0 || !n_sys || !nnz_sys || !rows || !cols || !vals) return DG_BAD_INPUT;
+  std::vector<int64_t> sr(1, 0), stri(1, 0);
+  for (int k = 0; k < nsys; k++) {
+    if (n_sys[k] <= 0 || nnz_sys[k] <= 0)
+      return fail(h, DG_BAD_INPUT, "system " + std::to_string(k + 1) + ": no unknowns or no entries");
+    sr.push_back(sr.back() + n_sys[k]);
+    stri.push_back(stri.back() + nnz_sys[k]);
+  }
+  if (sr.back() > INT_MAX / 2) return fail(h, DG_BAD_INPUT, "batched systems: too many unknowns in total");
+  const size_t ntri = (size_t)stri.back();
+  std::vector<int> ii(ntri), jj(ntri);
+  for (int k = 0; k < nsys; k++)
+    for (int64_t q = stri[(size_t)k]; q < stri[(size_t)k + 1]; q++) {
+      const int a = rows[q], c = cols[q];
+      if (a < 1 || a > n_sys[k] || c < 1 || c > n_sys[k])
+        return fail(h, DG_BAD_INPUT, "system " + std::to_string(k + 1) + ": entry " +
+                                         std::to_string(q - stri[(size_t)k] + 1) +
+                                         " out of range (indices are 1-based within each system)");
+      ii[(size_t)q] = a + (int)sr[(size_t)k];
+      jj[(size_t)q] = c + (int)sr[(size_t)k];
+    }
+  h->have_elements = false;
+  h->n = (int)sr.back();
+  h->ii.swap(ii);
+  h->jj.swap(jj);
+  h->vv.assign(vals, vals + ntri);
+  h->nsys = nsys;
+  h->sys_row = sr;
+  h->sys_tri = stri;
+  h->S.n = 0;
+  h->have_matrix = true;
+  h->ready = false;
+  if (b) { h->rhs.assign(b, b + h->n); h->have_rhs = true; }
+  else { h->rhs.assign((size_t)h->n, 1.0); h->have_rhs = false; }
+  return DG_OK;
+}
+
+dg_status dg_get_system_stats(const dg_handle *h, int *iterations, int *status, double *rel_residual,
+                              double *seconds) {
+  if (!h) return DG_BAD_INPUT;
+  if (h->nsys <= 0 || (int)h->sys_iters.size() != h->nsys) return DG_NOT_READY;
+  for (int k = 0; k < h->nsys; k++) {
+    const int stt = h->sys_state[(size_t)k];
+    if (iterations) iterations[k] = h->sys_iters[(size_t)k];
+    if (status) status[k] = stt == BT_DONE ? DG_OK : stt == BT_BREAKDOWN ? DG_BREAKDOWN : DG_NOT_CONVERGED;
+    if (rel_residual) rel_residual[k] = h->sys_relres[(size_t)k];
+    if (seconds) seconds[k] = h->sys_seconds[(size_t)k];
+  }
   return DG_OK;
 }
 

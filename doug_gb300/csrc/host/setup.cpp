@@ -18,6 +18,8 @@
 #include <chrono>
 #include <cstdlib>
 #include <sstream>
+#include <atomic>
+#include <thread>
 
 namespace dg {
 
@@ -1280,6 +1282,97 @@ bool build_setup(const Controls &c_in, int n, const std::vector<int> &ii, const 
   }
   tm.lap("subdomains + overlap");
   out.A = A;
+  return true;
+}
+
+namespace {
+
+void append_aggregates(Aggregates &dst, const Aggregates &src, int member_off) {
+  if (dst.starts.empty()) dst.starts.push_back(0);
+  for (int v : src.num) dst.num.push_back(v ? v + dst.nagr : 0);
+  const int base = dst.starts.back();
+  for (size_t a = 1; a < src.starts.size(); a++) dst.starts.push_back(base + src.starts[a]);
+  for (int v : src.nodes) dst.nodes.push_back(v + member_off);
+  dst.nagr += src.nagr;
+}
+
+// dst = diag(dst, src): src's rows after dst's rows, its columns after dst's columns
+void append_block(Csr &dst, const Csr &src) {
+  if (dst.ptr.empty()) dst.ptr.push_back(0);
+  const int64_t base = dst.ptr.back();
+  for (int r = 0; r < src.nrows; r++) dst.ptr.push_back(base + src.ptr[(size_t)r + 1]);
+  for (int c : src.col) dst.col.push_back(c + dst.ncols);
+  dst.val.insert(dst.val.end(), src.val.begin(), src.val.end());
+  dst.nrows += src.nrows;
+  dst.ncols += src.ncols;
+}
+
+}  // namespace
+
+bool build_setup_systems(const Controls &c, const std::vector<int64_t> &sys_row,
+                         const std::vector<int64_t> &sys_tri, const std::vector<int> &ii,
+                         const std::vector<int> &jj, const std::vector<double> &vv, SetupResult &out,
+                         std::string &err) {
+  const int K = (int)sys_row.size() - 1;
+  std::vector<SetupResult> S((size_t)K);
+  std::vector<std::string> errs((size_t)K);
+  std::vector<char> ok((size_t)K, 0);
+  std::atomic<int> next{0};
+  auto work = [&]() {
+    for (int k; (k = next.fetch_add(1)) < K;) {
+      const int64_t t0 = sys_tri[(size_t)k], t1 = sys_tri[(size_t)k + 1];
+      const int r0 = (int)sys_row[(size_t)k];
+      std::vector<int> li((size_t)(t1 - t0)), lj((size_t)(t1 - t0));
+      std::vector<double> lv(vv.begin() + t0, vv.begin() + t1);
+      for (int64_t q = t0; q < t1; q++) {
+        li[(size_t)(q - t0)] = ii[(size_t)q] - r0;
+        lj[(size_t)(q - t0)] = jj[(size_t)q] - r0;
+      }
+      ok[(size_t)k] = build_setup(c, (int)(sys_row[(size_t)k + 1] - r0), li, lj, lv, nullptr, 0, S[(size_t)k],
+                                  errs[(size_t)k]);
+    }
+  };
+  const int nth = std::max(1, std::min(K, (int)std::thread::hardware_concurrency()));
+  std::vector<std::thread> pool;
+  for (int t = 1; t < nth; t++) pool.emplace_back(work);
+  work();
+  for (auto &t : pool) t.join();
+  for (int k = 0; k < K; k++)
+    if (!ok[(size_t)k]) {
+      err = "system " + std::to_string(k + 1) + ": " + errs[(size_t)k];
+      return false;
+    }
+  out = SetupResult();
+  out.n = (int)sys_row[(size_t)K];
+  const SetupResult &S0 = S[0];
+  out.overlap = S0.overlap; out.smoothers = S0.smoothers; out.levels = S0.levels;
+  out.strong1 = S0.strong1; out.strong2 = S0.strong2;
+  out.r1 = S0.r1; out.r2 = S0.r2; out.min1 = S0.min1; out.max1 = S0.max1; out.min2 = S0.min2; out.max2 = S0.max2;
+  out.sd_ptr.assign(1, 0);
+  for (int k = 0; k < K; k++) {
+    const SetupResult &Sk = S[(size_t)k];
+    const int row_off = (int)sys_row[(size_t)k];
+    const int agg_off = out.fine.nagr, cagg_off = out.AC.nrows;
+    append_aggregates(out.fine, Sk.fine, row_off);
+    append_aggregates(out.fine_full, Sk.fine_full, row_off);
+    append_aggregates(out.coarse, Sk.coarse, agg_off);
+    append_aggregates(out.coarse_full, Sk.coarse_full, agg_off);
+    for (size_t q = 0; q < Sk.R_i.size(); q++) {
+      out.R_i.push_back(Sk.R_i[q] + agg_off); out.R_j.push_back(Sk.R_j[q] + row_off);
+      out.R_v.push_back(Sk.R_v[q]);
+    }
+    for (size_t q = 0; q < Sk.AC_i.size(); q++) {
+      out.AC_i.push_back(Sk.AC_i[q] + cagg_off); out.AC_j.push_back(Sk.AC_j[q] + cagg_off);
+      out.AC_v.push_back(Sk.AC_v[q]);
+    }
+    append_block(out.A, Sk.A);
+    append_block(out.R, Sk.R);
+    append_block(out.P, Sk.P);
+    append_block(out.AC, Sk.AC);
+    const int64_t sbase = out.sd_ptr.back();
+    for (size_t q = 1; q < Sk.sd_ptr.size(); q++) out.sd_ptr.push_back(sbase + Sk.sd_ptr[q]);
+    for (int v : Sk.sd_nodes) out.sd_nodes.push_back(v + row_off);
+  }
   return true;
 }
 

@@ -137,4 +137,16 @@ bool build_setup(const Controls &c_in, int n, const std::vector<int> &ii,
                  const std::vector<int> &jj, const std::vector<double> &vv,
                  const std::vector<int> *part, int nparts, SetupResult &out, std::string &err);
 
+// Batched independent systems: system k owns the rows [sys_row[k],
+// sys_row[k+1]) and the triplets [sys_tri[k], sys_tri[k+1]) of (ii, jj, vv),
+// whose indices are 1-based in the combined numbering.  Every system gets the
+// setup of its own one-process run (build_setup on its own triplets; the
+// systems run on parallel host threads); the result joins them as diagonal
+// blocks: A, R, P and AC block-diagonal, aggregates and subdomains numbered
+// after those of the systems before.
+bool build_setup_systems(const Controls &c, const std::vector<int64_t> &sys_row,
+                         const std::vector<int64_t> &sys_tri, const std::vector<int> &ii,
+                         const std::vector<int> &jj, const std::vector<double> &vv, SetupResult &out,
+                         std::string &err);
+
 }  // namespace dg

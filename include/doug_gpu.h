@@ -119,6 +119,25 @@ dg_status dg_set_elements(dg_handle *h, int nell, int ngf, const int *eptr, cons
                           const double *emat, const double *erhs);
 /* Right-hand side (n values); without one, b = 1 as in the reference. */
 dg_status dg_set_rhs(dg_handle *h, const double *b);
+/* Batched independent systems (no reference counterpart: one reference run
+ * solves one system).  nsys systems, system k with n_sys[k] unknowns and
+ * nnz_sys[k] triplets; rows/cols/vals hold the triplets of all systems one
+ * after the other, indices 1-based within each system; b (may be NULL: b = 1)
+ * the right-hand sides one after the other.  Every system gets the setup of
+ * its own one-process run (aggregation, R, AC, subdomains) and its own PCG
+ * (scalars, stopping test, iteration count); the factorisations, the
+ * preconditioner applications and the products of all systems share the
+ * kernel launches.  dg_solve then takes and returns the concatenated vectors.
+ * A partition vector cannot be combined with it. */
+dg_status dg_set_systems(dg_handle *h, int nsys, const int *n_sys, const long long *nnz_sys, const int *rows,
+                         const int *cols, const double *vals, const double *b);
+/* Per-system results of the last batched solve (each pointer may be NULL;
+ * nsys entries each): iterations, status (DG_OK, DG_NOT_CONVERGED,
+ * DG_BREAKDOWN), true relative residual ||b - A x|| / ||b|| and the wall time
+ * from the start of the solve to the end of the system's last iteration. */
+dg_status dg_get_system_stats(const dg_handle *h, int *iterations, int *status, double *rel_residual,
+                              double *seconds);
+
 /* Optional subdomain partition: part[i] in 1..nparts for every unknown.
  * Replaces the coarse-aggregate subdomains of the one-process path. */
 dg_status dg_set_partition(dg_handle *h, const int *part, int nparts);
