@@ -299,6 +299,13 @@ def run_gpu(args, rank, world):
     x64 = xd.cpu().numpy()
     err_mixed_vs_fp64 = float(np.linalg.norm(x_mixed - x64) / np.linalg.norm(x64))
     del sf
+    torch.cuda.empty_cache()
+    batched = None
+    if not args.no_batched:
+        try:
+            batched = run_batched(args, args.steps, args.warmup)
+        except Exception as ex:  # reported in the line; the headline stands on its own
+            batched = {"error": repr(ex)}
 
     if rank != 0:
         return 0
@@ -341,9 +348,106 @@ def run_gpu(args, rank, world):
                 "api": "dg_solve (host buffers, pinned)"},
         "roofline": roofline, "cpu_baseline": cpu, "clocks": clocks,
         "gpu_launches": int(launches),
+        "batched": batched,
     }
     print(json.dumps(line), flush=True)
     return 0
+
+
+BATCH_SYSTEMS = 256
+BATCH_CTL = dict(solver=2, method=1, fine_method=1, levels=2, overlap=1, smoothers=1,
+                 strong1="0.08", radius1=2, solve_tolerance=TOL, solve_maxiters=2000)
+BATCH_WORKLOAD = ("256 independent jittered 2-D P1 Poisson systems, unknowns log-uniform in [2k, 200k] "
+                  "(seeded), each with its own two-level additive Schwarz (its own aggregation, "
+                  "coarse-aggregate subdomains with overlap 1, smoothed-aggregation coarse grid), all "
+                  "solved in one batch")
+
+
+def run_batched(args, steps, warmup):
+    """The batched uneven-systems workload: every step solves all systems
+    (factorisations + per-system PCG to 1e-8) from right-hand sides in HBM."""
+    import torch
+    import doug_gb300 as D
+    from doug_gb300 import problems as P
+
+    D.build_library()
+    systems = P.batched_poisson2d_p1(BATCH_SYSTEMS, seed=SEED)
+    ns = np.array([t[0] for t in systems])
+    b = np.concatenate([t[4] for t in systems])
+    n = int(ns.sum())
+    stream = torch.cuda.current_stream()
+    sptr = stream.cuda_stream
+    bd = torch.tensor(b, dtype=torch.float64, device="cuda")
+    xd = torch.empty_like(bd)
+    out = {}
+    for prec in (1, 0):
+        s = D.DougSolver(BATCH_CTL)
+        s.set_option("precision", prec)
+        s.set_systems([t[:4] for t in systems], [t[4] for t in systems])
+        t0 = time.perf_counter()
+        s.setup()
+        setup_s = time.perf_counter() - t0
+        for _ in range(warmup if prec == 1 else 1):
+            s.solve_device(bd.data_ptr(), xd.data_ptr(), sptr)
+        k = steps if prec == 1 else 1
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        launches = 0
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(k):
+            st = s.solve_device(bd.data_ptr(), xd.data_ptr(), sptr)
+            launches += st.gpu_launches
+        e1.record(stream)
+        torch.cuda.synchronize()
+        t = e0.elapsed_time(e1) * 1e-3 / k
+        ss = s.system_stats()
+        sec = ss["seconds"].copy()
+        s.set_option("profile", 1)  # phase split of one extra solve (not timed)
+        pr = s.solve_device(bd.data_ptr(), xd.data_ptr(), sptr)
+        s.set_option("profile", 0)
+        res = {"batch_s": t, "solves_per_s": BATCH_SYSTEMS / t, "setup_host_s": setup_s,
+               "p50_system_s": float(np.percentile(sec, 50)), "p99_system_s": float(np.percentile(sec, 99)),
+               "iterations_max": int(ss["iterations"].max()),
+               "iterations_p50": float(np.median(ss["iterations"])),
+               "worst_true_rel_residual": float(ss["rel_residual"].max()),
+               "all_converged": bool(np.all(ss["status"] == D.DG_OK)), "gpu_launches": int(launches // k),
+               "phases": {"factor_s": pr.t_factor_s, "iterate_s": pr.t_iterate_s, "subsolve_s": pr.t_subsolve_s,
+                          "coarse_s": pr.t_coarse_s, "spmv_s": pr.t_spmv_s,
+                          "subsolve_GBps": pr.subsolve_bytes * pr.iterations / pr.t_subsolve_s / 1e9
+                          if pr.t_subsolve_s else None}}
+        if prec == 1:
+            x_mixed = xd.cpu().numpy()
+            # end to end through dg_solve (pinned host buffers)
+            bh = torch.tensor(b, dtype=torch.float64).pin_memory()
+            xh = torch.empty(n, dtype=torch.float64).pin_memory()
+            import ctypes
+            L = D.load_library()
+            stats = D._Stats()
+            e2e = []
+            for _ in range(k):
+                torch.cuda.synchronize()
+                t1 = time.perf_counter()
+                rc = L.dg_solve(s._h, ctypes.cast(bh.data_ptr(), ctypes.POINTER(ctypes.c_double)),
+                                ctypes.cast(xh.data_ptr(), ctypes.POINTER(ctypes.c_double)), ctypes.byref(stats))
+                e2e.append(time.perf_counter() - t1)
+                assert rc == D.DG_OK, L.dg_last_error(s._h)
+            res["e2e"] = {"value": BATCH_SYSTEMS / float(np.mean(e2e)), "unit": "solves/s",
+                          "h2d_bytes_per_step": 8 * n, "d2h_bytes_per_step": 8 * n}
+            sz = s.sizes()
+            out["config"] = {"workload": BATCH_WORKLOAD, "systems": BATCH_SYSTEMS, "n_total": n,
+                             "n_min": int(ns.min()), "n_median": float(np.median(ns)), "n_max": int(ns.max()),
+                             "subdomains": sz["nsubdomains"], "coarse_unknowns": sz["nagr_fine"],
+                             "controls": BATCH_CTL}
+            out["mixed"] = res
+        else:
+            x64 = xd.cpu().numpy()
+            out["fp64"] = res
+            err = [np.linalg.norm(a - c) / np.linalg.norm(c) for a, c in zip(s.split(x_mixed), s.split(x64))]
+            out["mixed_rel_err_vs_fp64_solution_max"] = float(max(err))
+        del s
+        torch.cuda.empty_cache()
+    out["mixed_vs_fp64"] = out["mixed"]["batch_s"] / out["fp64"]["batch_s"]
+    return out
 
 
 def run_profile_solve(args):
@@ -380,6 +484,9 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--fp64-steps", type=int, default=1)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-batched", action="store_true", help="skip the batched uneven-systems workload")
+    ap.add_argument("--workload", default="diffusion128", choices=["diffusion128", "batched"],
+                    help="batched: print only the batched uneven-systems line")
     ap.add_argument("--profile-solve", action="store_true",
                     help="one solve inside a profiler range (for ncu), no timing line")
     ap.add_argument("--grid", type=int, default=N, help="grid size of --profile-solve")
@@ -387,6 +494,20 @@ def main():
     args = ap.parse_args()
     if args.profile_solve:
         return run_profile_solve(args)
+    if args.workload == "batched" and args.impl == "gb300":
+        import torch
+        torch.cuda.set_device(0)
+        with ClockSampler(0) as clk:
+            bt = run_batched(args, args.steps, args.warmup)
+        m = bt["mixed"]
+        print(json.dumps({"metric": "aggregate solves/s, 256 uneven systems to rel. residual 1e-8, 1 GB300",
+                          "value": m["solves_per_s"], "unit": "solves/s", "n_gpus": 1, "steps": args.steps,
+                          "warmup": args.warmup, "ms_per_step": m["batch_s"] * 1e3, "higher_is_better": True,
+                          "scaling": "weak", "vs_baseline": None, "dtype": "f64 outer / f32 subdomain factors",
+                          "data": "synthetic (seeded generator, doug_gb300/problems.py)",
+                          "config": bt["config"], "batched": bt, "e2e": m["e2e"], "clocks": clk.summary(),
+                          "gpu_launches": m["gpu_launches"] * args.steps}), flush=True)
+        return 0
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     if world > 1:

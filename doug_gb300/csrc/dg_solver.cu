@@ -15,6 +15,7 @@
 #include <algorithm>
 #include <chrono>
 #include <climits>
+#include <cstdlib>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -706,9 +707,15 @@ dg_status do_setup(dg_handle *h, bool reuse_host = false) {
   tune.lean_task_bytes = (int64_t)c.lean_task_kb * 1024;
   MfOptions mo;
   mo.leaf = c.nd_leaf;
+  const bool timing = std::getenv("DG_SETUP_TIMING") != nullptr;
+  const double t1 = wall();
   try {
     if (c.fine_method == 1) mf_build_subdomains(h->S.A, h->S.sd_ptr, h->S.sd_nodes, mo, h->Bsub);
+    const double t2 = wall();
     if (c.levels > 1) mf_build_single(h->S.AC, mo, h->Bco);
+    if (timing)
+      fprintf(stderr, "[setup] host setup %.3f s, subdomain analysis %.3f s, coarse analysis %.3f s\n", t1 - t0,
+              t2 - t1, wall() - t2);
   } catch (const std::exception &ex) {
     return fail(h, DG_BAD_INPUT, std::string("symbolic analysis failed: ") + ex.what());
   }
@@ -1014,12 +1021,21 @@ dg_status do_solve_batch(dg_handle *h, const double *d_b, double *d_x, dg_stats 
       return fail(h, DG_SINGULAR, "a subdomain or coarse matrix is not positive definite");
     }
     h->factored = true;
-    auto iteration = [&](cudaStream_t q, int first, bool replace) -> int {
-      int nl = precondition(h, pl, q, false, nch, h->d_cb.p);
+    const bool prof = c.profile != 0;
+    double t_sub = 0, t_co = 0, t_sp = 0;
+    auto lap = [&](int a, int b) -> double {
+      float ms = 0;
+      CK(cudaEventElapsedTime(&ms, h->ev[a], h->ev[b]));
+      return ms * 1e-3;
+    };
+    auto iteration = [&](cudaStream_t q, int first, bool replace, bool profile) -> int {
+      int nl = precondition(h, pl, q, profile, nch, h->d_cb.p);
       bt_step(h, q, BT_RHO, first, mixed, tol2, h->part_rz.p, h->part_rzo.p);
+      if (profile) CK(cudaEventRecord(h->ev[6], q));
       bt_direction<<<nch, kVecThreads, 0, q>>>(h->d_cb.p, h->d_csys.p, h->d_state.p, h->bsc.p, h->z.p, h->p.p,
                                                first);
       bt_any(q, h, 0);
+      if (profile) CK(cudaEventRecord(h->ev[7], q));
       bt_step(h, q, BT_ALPHA, first, mixed, tol2, h->part_pq.p, nullptr);
       bt_update<<<nch, kVecThreads, 0, q>>>(h->d_cb.p, h->d_csys.p, h->d_state.p, h->bsc.p, h->p.p, h->q.p, h->x.p,
                                             h->r.p, h->part_rr.p);
@@ -1034,7 +1050,7 @@ dg_status do_solve_batch(dg_handle *h, const double *d_b, double *d_x, dg_stats 
     if (!h->iter_exec) {
       cudaGraph_t g = nullptr;
       CK(cudaStreamBeginCapture(h->s3, cudaStreamCaptureModeThreadLocal));
-      h->iter_nodes = iteration(h->s3, 0, false);
+      h->iter_nodes = iteration(h->s3, 0, false, false);
       CK(cudaStreamEndCapture(h->s3, &g));
       CK(cudaGraphInstantiate(&h->iter_exec, g, 0));
       CK(cudaGraphDestroy(g));
@@ -1045,14 +1061,19 @@ dg_status do_solve_batch(dg_handle *h, const double *d_b, double *d_x, dg_stats 
       it++;
       const int first = it == 1;
       const bool replace = pl.mixed && c.replace_every > 0 && it % c.replace_every == 0;
-      if (!first && !replace) {
+      if (!first && !replace && !prof) {
         CK(cudaGraphLaunch(h->iter_exec, s));
         launches += h->iter_nodes;
       } else {
-        launches += iteration(s, first, replace);
+        launches += iteration(s, first, replace, prof);
       }
       CK(cudaGetLastError());
       CK(cudaStreamSynchronize(s));
+      if (prof) {
+        t_sub += lap(3, 8);
+        if (pl.coarse) t_co += lap(4, 5);
+        t_sp += lap(6, 7);
+      }
       if (h->host_counts[1] > 0) {  // the FP64 true residual confirms the systems the recurrence stopped
         bt_any(s, h, 1, BT_CHECK, h->r.p);
         bt_step(h, s, BT_CONFIRM, 0, mixed, tol2, h->part_rr.p, nullptr);
@@ -1105,6 +1126,15 @@ dg_status do_solve_batch(dg_handle *h, const double *d_b, double *d_x, dg_stats 
     out.final_norm = std::sqrt(res_sum);
     out.true_rel_residual = worst;
     out.cond_num = 0.0;
+    out.t_subsolve_s = t_sub;
+    out.t_coarse_s = t_co;
+    out.t_spmv_s = t_sp;
+    {
+      const double tsz = pl.mixed ? 4.0 : 8.0;
+      out.subsolve_bytes = 2.0 * (double)h->Bsub.factor_nnz * tsz;
+      out.coarse_bytes = 2.0 * (double)h->Bco.factor_nnz * 8.0;
+      out.spmv_bytes = 12.0 * (double)h->S.A.nnz() + 8.0 * (n + 1) + 8.0 * n * 5.0;
+    }
     out.t_factor_s = ms_f * 1e-3;
     out.t_iterate_s = ms_i * 1e-3;
     out.t_total_s = out.t_factor_s + out.t_iterate_s;

@@ -80,6 +80,21 @@ def poisson2d_p1(nodes: int = 129, jitter: float = 0.2, seed: int = 0):
     return len(keep), rows1, cols1, vals, load[keep].copy(), coords
 
 
+def batched_poisson2d_p1(nsys: int = 256, n_min: int = 2000, n_max: int = 200000, seed: int = 0):
+    """Uneven independent systems: ``nsys`` jittered P1 Poisson problems as
+    poisson2d_p1, unknown counts drawn log-uniform in [n_min, n_max] (each
+    rounded to a square grid of interior nodes), each with its own seeded
+    jitter, diagonals and load.  Returns a list of (n, rows1, cols1, vals, rhs)."""
+    rng = np.random.default_rng(seed)
+    target = np.exp(rng.uniform(np.log(n_min), np.log(n_max), size=nsys))
+    out = []
+    for k, t in enumerate(target):
+        nodes = int(round(np.sqrt(t))) + 2
+        n, r, c, v, b, _ = poisson2d_p1(nodes, seed=seed * 100003 + k + 1)
+        out.append((n, r, c, v, b))
+    return out
+
+
 def poisson2d_p1_elements(nodes: int = 17, jitter: float = 0.2, seed: int = 0, kappa=None):
     """The P1 problem of ``poisson2d_p1`` as element matrices.
 
