@@ -459,8 +459,18 @@ def run_profile_solve(args):
 
     D.build_library()
     torch.cuda.set_device(0)
-    n, r, c, v, b, part = _problem(args.grid)
-    s = _solver(n, r, c, v, b, part, precision=args.precision)
+    if args.workload == "batched":
+        from doug_gb300 import problems as P
+        systems = P.batched_poisson2d_p1(BATCH_SYSTEMS, seed=SEED)
+        b = np.concatenate([t[4] for t in systems])
+        n = b.shape[0]
+        s = D.DougSolver(BATCH_CTL)
+        s.set_option("precision", args.precision)
+        s.set_systems([t[:4] for t in systems], [t[4] for t in systems])
+        s.setup()
+    else:
+        n, r, c, v, b, part = _problem(args.grid)
+        s = _solver(n, r, c, v, b, part, precision=args.precision)
     stream = torch.cuda.current_stream()
     bd = torch.tensor(b, dtype=torch.float64, device="cuda")
     xd = torch.empty_like(bd)
@@ -494,7 +504,7 @@ def main():
     args = ap.parse_args()
     if args.profile_solve:
         return run_profile_solve(args)
-    if args.workload == "batched" and args.impl == "gb300":
+    if args.workload == "batched" and args.impl == "gb300" and not args.profile_solve:
         import torch
         torch.cuda.set_device(0)
         with ClockSampler(0) as clk:

@@ -637,15 +637,24 @@ constexpr int kEThreads = 256;
 constexpr int kELeanThreads = 128;
 constexpr int kEUnroll = 8;        // independent E loads in flight per thread
 
+// Small fronts are solved by groups of G lanes (G = 8, 16 or 32; 32 / G
+// fronts per warp): a front of at most 4G rows, lane l of its group holding
+// the rows VN*l + G*VN*p.  Levels put their small fronts into three buckets
+// by size so that tiny fronts do not leave most of a warp idle.
+template <int G>
+__device__ __forceinline__ unsigned group_mask(int lane) {
+  return G == 32 ? 0xffffffffu : (((1u << G) - 1u) << (lane / G * G));
+}
+
 // E loads of one batch of kEUnroll columns [j0, j0 + kEUnroll) for the rows
-// of one lane; vectors wholly above the diagonal (r + VN <= j) are zero
-template <typename T, int PASS>
-__device__ __forceinline__ void load_e_batch(const T *Ef, int ld, int m, int k, int lane, int j0,
+// of one group lane; vectors wholly above the diagonal (r + VN <= j) are zero
+template <typename T, int PASS, int G>
+__device__ __forceinline__ void load_e_batch(const T *Ef, int ld, int m, int k, int sl, int j0,
                                              T (&e)[PASS][kEUnroll][Vec16<T>::N]) {
   constexpr int VN = Vec16<T>::N;
 #pragma unroll
   for (int p = 0; p < PASS; p++) {
-    const int r = VN * lane + 32 * VN * p;
+    const int r = VN * sl + G * VN * p;
 #pragma unroll
     for (int u = 0; u < kEUnroll; u++) {
       const int j = j0 + u;
@@ -658,33 +667,35 @@ __device__ __forceinline__ void load_e_batch(const T *Ef, int ld, int m, int k, 
   }
 }
 
-// small fronts, forward: one warp per front; lane l holds rows VN*l + 32*VN*p.
-// The first batch of E is loaded before the right-hand side is assembled.
-template <typename T>
+// small fronts, forward: the first batch of E is loaded before the
+// right-hand side is assembled
+template <typename T, int G>
 __global__ void __launch_bounds__(256, sizeof(T) == 8 ? 2 : 4)
 mf_fwd_small(MfView v, const int *__restrict__ fronts, int nf, const T *__restrict__ E,
              const T *__restrict__ xl, T *__restrict__ yl, T *__restrict__ uvec) {
-  constexpr int VN = Vec16<T>::N, PASS = kSolveSmall / (32 * VN);
-  __shared__ __align__(16) T wsh[8][kSolveSmall];
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  const int gw = blockIdx.x * nw + wid;
-  if (gw >= nf) return;  // warp-level kernel: no block barriers below
-  T *w = wsh[wid];
-  const int f = fronts[gw];
+  constexpr int VN = Vec16<T>::N, M = 4 * G, PASS = M / (G * VN), FPW = 32 / G;
+  __shared__ __align__(16) T wsh[8 * FPW][M];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int grp = lane / G, sl = lane % G;
+  const unsigned gm = group_mask<G>(lane);
+  const int gf = (blockIdx.x * 8 + wid) * FPW + grp;
+  if (gf >= nf) return;  // group-level kernel: no block barriers below
+  T *w = wsh[wid * FPW + grp];
+  const int f = fronts[gf];
   const int m = v.f_m[f], k = v.f_k[f], ld = round4(m);
   const int64_t xo = v.f_xoff[f] + v.f_p0[f];
   const T *Ef = E + v.e_off[f];
   T e[PASS][kEUnroll][VN];
-  load_e_batch<T, PASS>(Ef, ld, m, k, lane, 0, e);
-  for (int i = lane; i < m; i += 32) w[i] = i < k ? xl[xo + i] : T(0);
-  __syncwarp();
+  load_e_batch<T, PASS, G>(Ef, ld, m, k, sl, 0, e);
+  for (int i = sl; i < m; i += G) w[i] = i < k ? xl[xo + i] : T(0);
+  __syncwarp(gm);
   for (int ci = v.f_child_ptr[f]; ci < v.f_child_ptr[f + 1]; ci++) {
     const int c = v.f_children[ci];
     const int rc = v.f_m[c] - v.f_k[c];
     const int *rel = v.relmap + v.f_relmap[c];
     const T *u = uvec + v.f_uoff[c];
-    for (int a = lane; a < rc; a += 32) w[rel[a]] += u[a];
-    __syncwarp();
+    for (int a = sl; a < rc; a += G) w[rel[a]] += u[a];
+    __syncwarp(gm);
   }
   T acc[PASS][VN];
 #pragma unroll
@@ -692,7 +703,7 @@ mf_fwd_small(MfView v, const int *__restrict__ fronts, int nf, const T *__restri
 #pragma unroll
     for (int q = 0; q < VN; q++) acc[p][q] = T(0);
   for (int j0 = 0; j0 < k; j0 += kEUnroll) {
-    if (j0 > 0) load_e_batch<T, PASS>(Ef, ld, m, k, lane, j0, e);
+    if (j0 > 0) load_e_batch<T, PASS, G>(Ef, ld, m, k, sl, j0, e);
 #pragma unroll
     for (int u = 0; u < kEUnroll; u++) {
       const T bj = j0 + u < k ? w[j0 + u] : T(0);
@@ -707,45 +718,47 @@ mf_fwd_small(MfView v, const int *__restrict__ fronts, int nf, const T *__restri
   for (int p = 0; p < PASS; p++)
 #pragma unroll
     for (int q = 0; q < VN; q++) {
-      const int row = VN * lane + 32 * VN * p + q;
+      const int row = VN * sl + G * VN * p + q;
       if (row < k) yl[xo + row] = acc[p][q];
       else if (row < m) uf[row - k] = w[row] + acc[p][q];
     }
 }
 
-// small fronts, backward: one warp per front; the first batch of E is loaded
-// before v is gathered
-template <typename T>
+// small fronts, backward: the first batch of E is loaded before v is gathered
+template <typename T, int G>
 __global__ void __launch_bounds__(256, sizeof(T) == 8 ? 2 : 4)
 mf_bwd_small(MfView v, const int *__restrict__ fronts, int nf, const T *__restrict__ E,
              const T *__restrict__ yl, T *__restrict__ xl) {
-  constexpr int VN = Vec16<T>::N, PASS = kSolveSmall / (32 * VN);
-  __shared__ __align__(16) T wsh[8][kSolveSmall];
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  const int gw = blockIdx.x * nw + wid;
-  if (gw >= nf) return;
-  T *w = wsh[wid];
-  const int f = fronts[gw];
+  constexpr int VN = Vec16<T>::N, M = 4 * G, PASS = M / (G * VN), FPW = 32 / G;
+  static_assert(G >= kEUnroll, "a group stores one column sum per lane");
+  __shared__ __align__(16) T wsh[8 * FPW][M];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int grp = lane / G, sl = lane % G;
+  const unsigned gm = group_mask<G>(lane);
+  const int gf = (blockIdx.x * 8 + wid) * FPW + grp;
+  if (gf >= nf) return;
+  T *w = wsh[wid * FPW + grp];
+  const int f = fronts[gf];
   const int m = v.f_m[f], k = v.f_k[f], ld = round4(m);
   const int64_t xo = v.f_xoff[f] + v.f_p0[f];
   const T *Ef = E + v.e_off[f];
   T e[PASS][kEUnroll][VN];
-  load_e_batch<T, PASS>(Ef, ld, m, k, lane, 0, e);
+  load_e_batch<T, PASS, G>(Ef, ld, m, k, sl, 0, e);
   const T *xb = xl + v.f_xoff[f];
   const int *rows = v.rows + v.f_rows[f];
-  for (int i = lane; i < ld; i += 32) w[i] = i < k ? yl[xo + i] : (i < m ? xb[rows[i]] : T(0));
-  __syncwarp();
+  for (int i = sl; i < ld; i += G) w[i] = i < k ? yl[xo + i] : (i < m ? xb[rows[i]] : T(0));
+  __syncwarp(gm);
   T wr[PASS][VN];
 #pragma unroll
   for (int p = 0; p < PASS; p++)
 #pragma unroll
     for (int q = 0; q < VN; q++) {
-      const int r = VN * lane + 32 * VN * p + q;
+      const int r = VN * sl + G * VN * p + q;
       wr[p][q] = r < ld ? w[r] : T(0);
     }
-  // each column sum is reduced over the warp; lane u of the batch keeps column u
+  // each column sum is reduced over the group; lane u of the batch keeps column u
   for (int c0 = 0; c0 < k; c0 += kEUnroll) {
-    if (c0 > 0) load_e_batch<T, PASS>(Ef, ld, m, k, lane, c0, e);
+    if (c0 > 0) load_e_batch<T, PASS, G>(Ef, ld, m, k, sl, c0, e);
     T s[kEUnroll];
 #pragma unroll
     for (int u = 0; u < kEUnroll; u++) {
@@ -755,13 +768,13 @@ mf_bwd_small(MfView v, const int *__restrict__ fronts, int nf, const T *__restri
 #pragma unroll
         for (int q = 0; q < VN; q++) s[u] += e[p][u][q] * wr[p][q];
 #pragma unroll
-      for (int o = 16; o > 0; o >>= 1) s[u] += __shfl_xor_sync(0xffffffffu, s[u], o);
+      for (int o = G / 2; o > 0; o >>= 1) s[u] += __shfl_xor_sync(gm, s[u], o);
     }
-    if (lane < kEUnroll && c0 + lane < k) {
+    if (sl < kEUnroll && c0 + sl < k) {
       T out = s[0];
 #pragma unroll
-      for (int u = 1; u < kEUnroll; u++) if (lane == u) out = s[u];
-      xl[xo + c0 + lane] = out;
+      for (int u = 1; u < kEUnroll; u++) if (sl == u) out = s[u];
+      xl[xo + c0 + sl] = out;
     }
   }
 }
@@ -1074,10 +1087,13 @@ __global__ void restrict_to_coarse(const int64_t *__restrict__ Rp, const int *__
 
 // z_g = (sum of subdomain solutions at g, in subdomain order) + (P x_c)_g ;
 // partial sums of r.z (and of r.z_old for the flexible variant).  One thread
-// per node; Pcp holds coarse-vector positions (composed at setup).
+// per node; Pcp holds coarse-vector positions (composed at setup).  The loads
+// of a node are issued in three dependent rounds (row pointers, r and z_old;
+// the first two pull positions and the first four P entries; the gathers),
+// the rare longer rows finish in loops; the sums keep the entries' order.
 template <typename T, typename TP>
 __global__ void __launch_bounds__(kVecThreads)
-pull_prolong_dot(int n, const int64_t *__restrict__ pull_ptr, const int64_t *__restrict__ pull_idx,
+pull_prolong_dot(int n, const int *__restrict__ pull_ptr, const int *__restrict__ pull_idx,
                  const T *__restrict__ xl, const int64_t *__restrict__ Pp, const int *__restrict__ Pcp,
                  const TP *__restrict__ Pv, const double *__restrict__ xc,
                  int mode, const double *__restrict__ r, double *__restrict__ z,
@@ -1091,33 +1107,50 @@ pull_prolong_dot(int n, const int64_t *__restrict__ pull_ptr, const int64_t *__r
   const int g0 = cb ? cb[blockIdx.x] + threadIdx.x : blockIdx.x * kVecThreads + threadIdx.x;
   const int gend = cb ? cb[blockIdx.x + 1] : n;
   const int gstep = cb ? kVecThreads : gridDim.x * kVecThreads;
+  const bool pull = (mode & 5) == 1, prol = (mode & 2) != 0, flex = (mode & 8) != 0;
   for (int g = g0; g < gend; g += gstep) {
+    // round 1
+    const double rg = r[g];
+    const double zo = flex ? zold[g] : 0.0;
+    int q0 = 0, q1 = 0;
+    int64_t e0 = 0, e1 = 0;
+    if (pull) { q0 = pull_ptr[g]; q1 = pull_ptr[g + 1]; }
+    if (prol) { e0 = Pp[g]; e1 = Pp[g + 1]; }
+    // round 2
+    const int i0 = q0 < q1 ? pull_idx[q0] : -1;
+    const int i1 = q0 + 1 < q1 ? pull_idx[q0 + 1] : -1;
+    int pc[4];
+    TP pv[4];
+#pragma unroll
+    for (int u = 0; u < 4; u++) {
+      const bool on = e0 + u < e1;
+      pc[u] = on ? Pcp[e0 + u] : -1;
+      pv[u] = on ? Pv[e0 + u] : TP(0);
+    }
+    // round 3
+    const T x0 = i0 >= 0 ? xl[i0] : T(0);
+    const T x1 = i1 >= 0 ? xl[i1] : T(0);
+    TP xv[4];
+#pragma unroll
+    for (int u = 0; u < 4; u++) xv[u] = pc[u] >= 0 ? (TP)xc[pc[u]] : TP(0);
     double sv = 0.0;
     if (mode & 4) {
-      sv = r[g];
-    } else if (mode & 1) {
-      const int64_t q0 = pull_ptr[g], q1 = pull_ptr[g + 1];
-      for (int64_t q = q0; q < q1; q++) sv = sv + (double)xl[pull_idx[q]];
+      sv = rg;
+    } else if (pull) {
+      if (i0 >= 0) sv = sv + (double)x0;
+      if (i1 >= 0) sv = sv + (double)x1;
+      for (int q = q0 + 2; q < q1; q++) sv = sv + (double)xl[pull_idx[q]];
     }
-    if (mode & 2) {
-      const int64_t e0 = Pp[g], e1 = Pp[g + 1];
+    if (prol) {
       TP t = TP(0);
-      int64_t e = e0;
-      for (; e + 4 <= e1; e += 4) {  // independent loads in flight
-        const int c0 = Pcp[e], c1 = Pcp[e + 1], c2 = Pcp[e + 2], c3 = Pcp[e + 3];
-        const TP v0 = Pv[e], v1 = Pv[e + 1], v2 = Pv[e + 2], v3 = Pv[e + 3];
-        const TP x0 = (TP)xc[c0], x1 = (TP)xc[c1], x2 = (TP)xc[c2], x3 = (TP)xc[c3];
-        t += v0 * x0;
-        t += v1 * x1;
-        t += v2 * x2;
-        t += v3 * x3;
-      }
-      for (; e < e1; e++) t += Pv[e] * (TP)xc[Pcp[e]];
+#pragma unroll
+      for (int u = 0; u < 4; u++)
+        if (pc[u] >= 0) t += pv[u] * xv[u];
+      for (int64_t e = e0 + 4; e < e1; e++) t += Pv[e] * (TP)xc[Pcp[e]];
       sv = sv + (double)t;
     }
-    const double rg = r[g];
-    if (mode & 8) {
-      srzo += rg * zold[g];
+    if (flex) {
+      srzo += rg * zo;
       zold[g] = sv;
     }
     z[g] = sv;
@@ -1125,7 +1158,7 @@ pull_prolong_dot(int n, const int64_t *__restrict__ pull_ptr, const int64_t *__r
   }
   double b = block_sum<kVecThreads>(srz, sh);
   if (threadIdx.x == 0) part_rz[blockIdx.x] = b;
-  if (mode & 8) {
+  if (flex) {
     b = block_sum<kVecThreads>(srzo, sh);
     if (threadIdx.x == 0) part_rzo[blockIdx.x] = b;
   }

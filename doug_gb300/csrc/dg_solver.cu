@@ -101,7 +101,8 @@ struct MfDevice {
   std::vector<Level> levels;
   // per level: solve work lists
   struct SolveLevel {
-    int small_off, small_cnt, fwd_off, fwd_cnt, bwd_off, bwd_cnt;
+    int small_off[3], small_cnt[3];   // small fronts of <= 32, <= 64, <= 128 rows
+    int fwd_off, fwd_cnt, bwd_off, bwd_cnt;
     size_t fwd_smem, bwd_smem;
     bool fwd_lean, bwd_lean;      // 128-thread CTAs for levels of small tasks
   };
@@ -239,7 +240,7 @@ struct MfDevice {
     slevels.assign((size_t)nlevels, SolveLevel());
     for (int l = 0; l < nlevels; l++) {
       SolveLevel &L = slevels[(size_t)l];
-      L.small_off = (int)ss.size();
+      std::vector<std::pair<int, int>> sm[3];  // (k, front) per bucket
       L.fwd_off = (int)fw.size();
       L.bwd_off = (int)bw.size();
       L.fwd_smem = L.bwd_smem = 0;
@@ -248,7 +249,7 @@ struct MfDevice {
       for (int q = B.lvl_ptr[(size_t)l]; q < B.lvl_ptr[(size_t)l + 1]; q++) {
         int f = B.lvl_fronts[(size_t)q];
         int m = B.f_m[(size_t)f], k = B.f_k[(size_t)f];
-        if (m <= kSolveSmall) { ss.push_back(f); continue; }
+        if (m <= kSolveSmall) { sm[m <= 32 ? 0 : m <= 64 ? 1 : 2].push_back({k, f}); continue; }
         // forward tasks: runs of row chunks of at least tune.fwd_task_bytes of E each
         const int RC = FwdRows<T>::N, nch = (m + RC - 1) / RC;
         for (int c = 0; c < nch;) {
@@ -274,7 +275,14 @@ struct MfDevice {
       std::stable_sort(bl.begin(), bl.end(), [](const std::pair<int, int2> &a, const std::pair<int, int2> &b) { return a.first > b.first; });
       for (auto &e : fl) fw.push_back(e.second);
       for (auto &e : bl) bw.push_back(e.second);
-      L.small_cnt = (int)ss.size() - L.small_off;
+      // fronts of similar pivot counts share a warp
+      for (int bk = 0; bk < 3; bk++) {
+        std::stable_sort(sm[bk].begin(), sm[bk].end(),
+                         [](const std::pair<int, int> &a, const std::pair<int, int> &b) { return a.first > b.first; });
+        L.small_off[bk] = (int)ss.size();
+        for (auto &e : sm[bk]) ss.push_back(e.second);
+        L.small_cnt[bk] = (int)ss.size() - L.small_off[bk];
+      }
       L.fwd_cnt = (int)fw.size() - L.fwd_off;
       L.bwd_cnt = (int)bw.size() - L.bwd_off;
       L.fwd_lean = L.fwd_cnt && fwd_bytes / L.fwd_cnt < tune.lean_task_bytes;
@@ -346,9 +354,19 @@ struct MfDevice {
     int launches = 0;
     for (int l = 0; l < nlevels; l++) {
       const SolveLevel &L = slevels[(size_t)l];
-      if (L.small_cnt) {
-        mf_fwd_small<T><<<(L.small_cnt + 7) / 8, 256, 0, s>>>(view, solve_small.p + L.small_off, L.small_cnt,
-                                                              E.p, xl.p, yl.p, u.p);
+      if (L.small_cnt[0]) {
+        mf_fwd_small<T, 8><<<(L.small_cnt[0] + 31) / 32, 256, 0, s>>>(view, solve_small.p + L.small_off[0],
+                                                                     L.small_cnt[0], E.p, xl.p, yl.p, u.p);
+        launches++;
+      }
+      if (L.small_cnt[1]) {
+        mf_fwd_small<T, 16><<<(L.small_cnt[1] + 15) / 16, 256, 0, s>>>(view, solve_small.p + L.small_off[1],
+                                                                      L.small_cnt[1], E.p, xl.p, yl.p, u.p);
+        launches++;
+      }
+      if (L.small_cnt[2]) {
+        mf_fwd_small<T, 32><<<(L.small_cnt[2] + 7) / 8, 256, 0, s>>>(view, solve_small.p + L.small_off[2],
+                                                                    L.small_cnt[2], E.p, xl.p, yl.p, u.p);
         launches++;
       }
       if (L.fwd_cnt) {
@@ -372,9 +390,19 @@ struct MfDevice {
                                                                           yl.p, xl.p);
         launches++;
       }
-      if (L.small_cnt) {
-        mf_bwd_small<T><<<(L.small_cnt + 7) / 8, 256, 0, s>>>(view, solve_small.p + L.small_off, L.small_cnt,
-                                                              E.p, yl.p, xl.p);
+      if (L.small_cnt[0]) {
+        mf_bwd_small<T, 8><<<(L.small_cnt[0] + 31) / 32, 256, 0, s>>>(view, solve_small.p + L.small_off[0],
+                                                                     L.small_cnt[0], E.p, yl.p, xl.p);
+        launches++;
+      }
+      if (L.small_cnt[1]) {
+        mf_bwd_small<T, 16><<<(L.small_cnt[1] + 15) / 16, 256, 0, s>>>(view, solve_small.p + L.small_off[1],
+                                                                      L.small_cnt[1], E.p, yl.p, xl.p);
+        launches++;
+      }
+      if (L.small_cnt[2]) {
+        mf_bwd_small<T, 32><<<(L.small_cnt[2] + 7) / 8, 256, 0, s>>>(view, solve_small.p + L.small_off[2],
+                                                                    L.small_cnt[2], E.p, yl.p, xl.p);
         launches++;
       }
     }
@@ -519,7 +547,8 @@ struct dg_handle {
   int lanes = 8;
   // device
   int device = 0;
-  DBuf<int64_t> Ap, Rp, Pp, pull_ptr, pull_idx;
+  DBuf<int64_t> Ap, Rp, Pp;
+  DBuf<int> pull_ptr, pull_idx;   // per node: its positions in the subdomain arena
   DBuf<int> Ac, Rc, Pc, cpos, status;
   DBuf<double> Av, ACv, Rv, Pv, b, x, r, p, q, z, zold, hb, hx;
   DBuf<float> Rvf, Pvf;
@@ -837,12 +866,14 @@ dg_status do_setup(dg_handle *h, bool reuse_host = false) {
         h->sub64.reset(new MfDevice<double>()); h->sub64->upload(h->Bsub, tune);
       }
       // pull lists: subdomain arena positions of every node, subdomain order
-      std::vector<int64_t> pp((size_t)n + 1, 0);
+      if (arena_rows->size() >= (size_t)INT_MAX)
+        throw CudaError{cudaErrorInvalidValue, "subdomain arena beyond 32-bit positions"};
+      std::vector<int> pp((size_t)n + 1, 0);
       for (int g : *arena_rows) pp[(size_t)g + 1]++;
       for (int i = 0; i < n; i++) pp[(size_t)i + 1] += pp[(size_t)i];
-      std::vector<int64_t> idx((size_t)pp[(size_t)n]);
-      std::vector<int64_t> fill(pp.begin(), pp.end() - 1);
-      for (int64_t q = 0; q < (int64_t)arena_rows->size(); q++)
+      std::vector<int> idx((size_t)pp[(size_t)n]);
+      std::vector<int> fill(pp.begin(), pp.end() - 1);
+      for (int q = 0; q < (int)arena_rows->size(); q++)
         idx[(size_t)fill[(size_t)(*arena_rows)[(size_t)q]]++] = q;
       h->pull_ptr.upload(pp);
       h->pull_idx.upload(idx);
