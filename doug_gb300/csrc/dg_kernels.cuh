@@ -668,19 +668,18 @@ __device__ __forceinline__ void load_e_batch(const T *Ef, int ld, int m, int k, 
 }
 
 // small fronts, forward: the first batch of E is loaded before the
-// right-hand side is assembled
+// right-hand side is assembled.  cta: this CTA's index within its bucket.
 template <typename T, int G>
-__global__ void __launch_bounds__(256, sizeof(T) == 8 ? 2 : 4)
-mf_fwd_small(MfView v, const int *__restrict__ fronts, int nf, const T *__restrict__ E,
-             const T *__restrict__ xl, T *__restrict__ yl, T *__restrict__ uvec) {
+__device__ __forceinline__ void fwd_small_body(const MfView &v, const int *__restrict__ fronts, int nf,
+                                               const T *__restrict__ E, const T *__restrict__ xl,
+                                               T *__restrict__ yl, T *__restrict__ uvec, int cta, T *wsh) {
   constexpr int VN = Vec16<T>::N, M = 4 * G, PASS = M / (G * VN), FPW = 32 / G;
-  __shared__ __align__(16) T wsh[8 * FPW][M];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const int grp = lane / G, sl = lane % G;
   const unsigned gm = group_mask<G>(lane);
-  const int gf = (blockIdx.x * 8 + wid) * FPW + grp;
-  if (gf >= nf) return;  // group-level kernel: no block barriers below
-  T *w = wsh[wid * FPW + grp];
+  const int gf = (cta * 8 + wid) * FPW + grp;
+  if (gf >= nf) return;  // group-level work: no block barriers below
+  T *w = wsh + (wid * FPW + grp) * M;
   const int f = fronts[gf];
   const int m = v.f_m[f], k = v.f_k[f], ld = round4(m);
   const int64_t xo = v.f_xoff[f] + v.f_p0[f];
@@ -726,18 +725,17 @@ mf_fwd_small(MfView v, const int *__restrict__ fronts, int nf, const T *__restri
 
 // small fronts, backward: the first batch of E is loaded before v is gathered
 template <typename T, int G>
-__global__ void __launch_bounds__(256, sizeof(T) == 8 ? 2 : 4)
-mf_bwd_small(MfView v, const int *__restrict__ fronts, int nf, const T *__restrict__ E,
-             const T *__restrict__ yl, T *__restrict__ xl) {
+__device__ __forceinline__ void bwd_small_body(const MfView &v, const int *__restrict__ fronts, int nf,
+                                               const T *__restrict__ E, const T *__restrict__ yl,
+                                               T *__restrict__ xl, int cta, T *wsh) {
   constexpr int VN = Vec16<T>::N, M = 4 * G, PASS = M / (G * VN), FPW = 32 / G;
   static_assert(G >= kEUnroll, "a group stores one column sum per lane");
-  __shared__ __align__(16) T wsh[8 * FPW][M];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const int grp = lane / G, sl = lane % G;
   const unsigned gm = group_mask<G>(lane);
-  const int gf = (blockIdx.x * 8 + wid) * FPW + grp;
+  const int gf = (cta * 8 + wid) * FPW + grp;
   if (gf >= nf) return;
-  T *w = wsh[wid * FPW + grp];
+  T *w = wsh + (wid * FPW + grp) * M;
   const int f = fronts[gf];
   const int m = v.f_m[f], k = v.f_k[f], ld = round4(m);
   const int64_t xo = v.f_xoff[f] + v.f_p0[f];
@@ -777,6 +775,41 @@ mf_bwd_small(MfView v, const int *__restrict__ fronts, int nf, const T *__restri
       xl[xo + c0 + sl] = out;
     }
   }
+}
+
+// One launch per level for the three small-front buckets: the first
+// nb.x CTAs take the fronts of <= 32 rows (8 lanes each), the next nb.y those
+// of <= 64 rows (16 lanes), the rest those of <= 128 rows (32 lanes).
+// fronts: the level's small fronts, bucket after bucket; cnt: bucket sizes.
+struct SmallBuckets {
+  int cnt0, cnt1, cnt2;   // fronts per bucket
+  int nb0, nb1;           // CTAs of buckets 0 and 1
+};
+
+template <typename T>
+__global__ void __launch_bounds__(256, sizeof(T) == 8 ? 2 : 4)
+mf_fwd_small(MfView v, const int *__restrict__ fronts, SmallBuckets sb, const T *__restrict__ E,
+             const T *__restrict__ xl, T *__restrict__ yl, T *__restrict__ uvec) {
+  __shared__ __align__(16) T wsh[8 * kSolveSmall];
+  const int b = blockIdx.x;
+  if (b < sb.nb0) fwd_small_body<T, 8>(v, fronts, sb.cnt0, E, xl, yl, uvec, b, wsh);
+  else if (b < sb.nb0 + sb.nb1)
+    fwd_small_body<T, 16>(v, fronts + sb.cnt0, sb.cnt1, E, xl, yl, uvec, b - sb.nb0, wsh);
+  else
+    fwd_small_body<T, 32>(v, fronts + sb.cnt0 + sb.cnt1, sb.cnt2, E, xl, yl, uvec, b - sb.nb0 - sb.nb1, wsh);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256, sizeof(T) == 8 ? 2 : 4)
+mf_bwd_small(MfView v, const int *__restrict__ fronts, SmallBuckets sb, const T *__restrict__ E,
+             const T *__restrict__ yl, T *__restrict__ xl) {
+  __shared__ __align__(16) T wsh[8 * kSolveSmall];
+  const int b = blockIdx.x;
+  if (b < sb.nb0) bwd_small_body<T, 8>(v, fronts, sb.cnt0, E, yl, xl, b, wsh);
+  else if (b < sb.nb0 + sb.nb1)
+    bwd_small_body<T, 16>(v, fronts + sb.cnt0, sb.cnt1, E, yl, xl, b - sb.nb0, wsh);
+  else
+    bwd_small_body<T, 32>(v, fronts + sb.cnt0 + sb.cnt1, sb.cnt2, E, yl, xl, b - sb.nb0 - sb.nb1, wsh);
 }
 
 // large fronts, forward: task = {front, (first chunk << 16) | chunk count};

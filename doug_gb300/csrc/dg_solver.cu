@@ -73,6 +73,7 @@ struct MfTune {
   int panel_rows = 512;                  // fronts of at most this many rows may use mf_factor_panel
   int64_t fwd_task_bytes = 96 * 1024;    // E bytes per forward task of a large front
   int64_t lean_task_bytes = 80 * 1024;   // levels with smaller average tasks use 128-thread CTAs
+  int small_min_fronts = 304;            // levels with fewer small fronts solve them CTA-per-task
 };
 
 template <typename T>
@@ -101,7 +102,8 @@ struct MfDevice {
   std::vector<Level> levels;
   // per level: solve work lists
   struct SolveLevel {
-    int small_off[3], small_cnt[3];   // small fronts of <= 32, <= 64, <= 128 rows
+    int small_off, small_cta;     // small fronts of the level (three buckets)
+    SmallBuckets sb;
     int fwd_off, fwd_cnt, bwd_off, bwd_cnt;
     size_t fwd_smem, bwd_smem;
     bool fwd_lean, bwd_lean;      // 128-thread CTAs for levels of small tasks
@@ -246,10 +248,17 @@ struct MfDevice {
       L.fwd_smem = L.bwd_smem = 0;
       std::vector<std::pair<int, int2>> fl, bl;
       int64_t fwd_bytes = 0, bwd_bytes = 0;
+      // a level with few small fronts solves them with the CTA-per-task
+      // kernels too: a group of lanes per front leaves the GPU nearly idle
+      // while it walks the columns of a large-k front
+      int nsmall = 0;
+      for (int q = B.lvl_ptr[(size_t)l]; q < B.lvl_ptr[(size_t)l + 1]; q++)
+        nsmall += B.f_m[(size_t)B.lvl_fronts[(size_t)q]] <= kSolveSmall;
+      const bool thin = nsmall < tune.small_min_fronts;
       for (int q = B.lvl_ptr[(size_t)l]; q < B.lvl_ptr[(size_t)l + 1]; q++) {
         int f = B.lvl_fronts[(size_t)q];
         int m = B.f_m[(size_t)f], k = B.f_k[(size_t)f];
-        if (m <= kSolveSmall) { sm[m <= 32 ? 0 : m <= 64 ? 1 : 2].push_back({k, f}); continue; }
+        if (m <= kSolveSmall && !thin) { sm[m <= 32 ? 0 : m <= 64 ? 1 : 2].push_back({k, f}); continue; }
         // forward tasks: runs of row chunks of at least tune.fwd_task_bytes of E each
         const int RC = FwdRows<T>::N, nch = (m + RC - 1) / RC;
         for (int c = 0; c < nch;) {
@@ -276,13 +285,17 @@ struct MfDevice {
       for (auto &e : fl) fw.push_back(e.second);
       for (auto &e : bl) bw.push_back(e.second);
       // fronts of similar pivot counts share a warp
+      L.small_off = (int)ss.size();
+      int cnt[3];
       for (int bk = 0; bk < 3; bk++) {
         std::stable_sort(sm[bk].begin(), sm[bk].end(),
                          [](const std::pair<int, int> &a, const std::pair<int, int> &b) { return a.first > b.first; });
-        L.small_off[bk] = (int)ss.size();
         for (auto &e : sm[bk]) ss.push_back(e.second);
-        L.small_cnt[bk] = (int)ss.size() - L.small_off[bk];
+        cnt[bk] = (int)sm[bk].size();
       }
+      // 256-thread CTAs: 32 fronts of bucket 0, 16 of bucket 1, 8 of bucket 2
+      L.sb = SmallBuckets{cnt[0], cnt[1], cnt[2], (cnt[0] + 31) / 32, (cnt[1] + 15) / 16};
+      L.small_cta = L.sb.nb0 + L.sb.nb1 + (cnt[2] + 7) / 8;
       L.fwd_cnt = (int)fw.size() - L.fwd_off;
       L.bwd_cnt = (int)bw.size() - L.bwd_off;
       L.fwd_lean = L.fwd_cnt && fwd_bytes / L.fwd_cnt < tune.lean_task_bytes;
@@ -354,19 +367,8 @@ struct MfDevice {
     int launches = 0;
     for (int l = 0; l < nlevels; l++) {
       const SolveLevel &L = slevels[(size_t)l];
-      if (L.small_cnt[0]) {
-        mf_fwd_small<T, 8><<<(L.small_cnt[0] + 31) / 32, 256, 0, s>>>(view, solve_small.p + L.small_off[0],
-                                                                     L.small_cnt[0], E.p, xl.p, yl.p, u.p);
-        launches++;
-      }
-      if (L.small_cnt[1]) {
-        mf_fwd_small<T, 16><<<(L.small_cnt[1] + 15) / 16, 256, 0, s>>>(view, solve_small.p + L.small_off[1],
-                                                                      L.small_cnt[1], E.p, xl.p, yl.p, u.p);
-        launches++;
-      }
-      if (L.small_cnt[2]) {
-        mf_fwd_small<T, 32><<<(L.small_cnt[2] + 7) / 8, 256, 0, s>>>(view, solve_small.p + L.small_off[2],
-                                                                    L.small_cnt[2], E.p, xl.p, yl.p, u.p);
+      if (L.small_cta) {
+        mf_fwd_small<T><<<L.small_cta, 256, 0, s>>>(view, solve_small.p + L.small_off, L.sb, E.p, xl.p, yl.p, u.p);
         launches++;
       }
       if (L.fwd_cnt) {
@@ -390,19 +392,8 @@ struct MfDevice {
                                                                           yl.p, xl.p);
         launches++;
       }
-      if (L.small_cnt[0]) {
-        mf_bwd_small<T, 8><<<(L.small_cnt[0] + 31) / 32, 256, 0, s>>>(view, solve_small.p + L.small_off[0],
-                                                                     L.small_cnt[0], E.p, yl.p, xl.p);
-        launches++;
-      }
-      if (L.small_cnt[1]) {
-        mf_bwd_small<T, 16><<<(L.small_cnt[1] + 15) / 16, 256, 0, s>>>(view, solve_small.p + L.small_off[1],
-                                                                      L.small_cnt[1], E.p, yl.p, xl.p);
-        launches++;
-      }
-      if (L.small_cnt[2]) {
-        mf_bwd_small<T, 32><<<(L.small_cnt[2] + 7) / 8, 256, 0, s>>>(view, solve_small.p + L.small_off[2],
-                                                                    L.small_cnt[2], E.p, yl.p, xl.p);
+      if (L.small_cta) {
+        mf_bwd_small<T><<<L.small_cta, 256, 0, s>>>(view, solve_small.p + L.small_off, L.sb, E.p, yl.p, xl.p);
         launches++;
       }
     }
@@ -734,6 +725,7 @@ dg_status do_setup(dg_handle *h, bool reuse_host = false) {
   tune.panel_rows = c.panel_rows;
   tune.fwd_task_bytes = (int64_t)c.fwd_task_kb * 1024;
   tune.lean_task_bytes = (int64_t)c.lean_task_kb * 1024;
+  tune.small_min_fronts = c.thin_level_fronts;
   MfOptions mo;
   mo.leaf = c.nd_leaf;
   const bool timing = std::getenv("DG_SETUP_TIMING") != nullptr;
@@ -1377,10 +1369,11 @@ dg_status dg_set_option(dg_handle *h, const char *name, const char *value) {
     h->ctl.replace_every = v;
     return DG_OK;
   }
-  if (w1 == "panel_rows" || w1 == "fwd_task_kb" || w1 == "lean_task_kb") {
+  if (w1 == "panel_rows" || w1 == "fwd_task_kb" || w1 == "lean_task_kb" || w1 == "thin_level_fronts") {
     int v;
-    if (!parse_i10(w2, v) || v < 1) return fail(h, DG_BAD_INPUT, "bad " + w1);
-    (w1 == "panel_rows" ? h->ctl.panel_rows : w1 == "fwd_task_kb" ? h->ctl.fwd_task_kb : h->ctl.lean_task_kb) = v;
+    if (!parse_i10(w2, v) || v < (w1 == "thin_level_fronts" ? 0 : 1)) return fail(h, DG_BAD_INPUT, "bad " + w1);
+    (w1 == "panel_rows" ? h->ctl.panel_rows : w1 == "fwd_task_kb" ? h->ctl.fwd_task_kb
+     : w1 == "lean_task_kb" ? h->ctl.lean_task_kb : h->ctl.thin_level_fronts) = v;
     h->ready = false;
     return DG_OK;
   }

@@ -39,6 +39,7 @@ struct Controls {
   int panel_rows = 512;             // fronts up to this size (and panel + E <= 96 KB): one CTA each
   int fwd_task_kb = 96;             // KB of E per forward task of a large front
   int lean_task_kb = 80;            // levels with smaller average tasks use 128-thread CTAs
+  int thin_level_fronts = 304;      // levels with fewer small fronts solve them one CTA per task
 };
 
 // Parse one "name value" line the way util_actionOnCtrlArg does
