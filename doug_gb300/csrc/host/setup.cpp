@@ -19,6 +19,7 @@
 #include <cstdlib>
 #include <sstream>
 #include <atomic>
+#include <deque>
 #include <thread>
 
 namespace dg {
@@ -448,43 +449,78 @@ void assemble_elements(const ElementMesh &M, int &n, std::vector<int> &ii, std::
   for (int g = 1; g <= M.ngf; g++)
     if (gl[(size_t)g]) { lg_fmap.push_back(g); gl[(size_t)g] = (int)lg_fmap.size(); }
   n = (int)lg_fmap.size();
-  // pattern: per local row, the sorted distinct local columns with a non-zero
-  // element value somewhere
-  std::vector<int64_t> rp((size_t)n + 1, 0);
-  std::vector<std::pair<int, int>> pairs;
-  for (int e = 0; e < M.nell; e++) {
-    const int e0 = M.eptr[(size_t)e], nf = M.eptr[(size_t)e + 1] - e0;
-    const double *Ae = &M.emat[(size_t)M.emat_off[(size_t)e]];
-    for (int i = 0; i < nf; i++)
-      for (int j = 0; j < nf; j++)
-        if (Ae[(size_t)j * nf + i] != 0.0)
-          pairs.push_back({gl[(size_t)M.efree[(size_t)(e0 + i)]] - 1, gl[(size_t)M.efree[(size_t)(e0 + j)]] - 1});
-  }
-  std::sort(pairs.begin(), pairs.end());
-  pairs.erase(std::unique(pairs.begin(), pairs.end()), pairs.end());
-  std::vector<int> col(pairs.size());
-  for (size_t q = 0; q < pairs.size(); q++) {
-    rp[(size_t)pairs[q].first + 1]++;
-    col[q] = pairs[q].second;
-  }
-  for (int r = 0; r < n; r++) rp[(size_t)r + 1] += rp[(size_t)r];
-  // values: element order, then row i, column j within the element
-  std::vector<double> val(col.size(), 0.0);
-  b.assign((size_t)n, 0.0);
-  for (int e = 0; e < M.nell; e++) {
-    const int e0 = M.eptr[(size_t)e], nf = M.eptr[(size_t)e + 1] - e0;
-    const double *Ae = &M.emat[(size_t)M.emat_off[(size_t)e]];
-    for (int i = 0; i < nf; i++) {
-      const int li = gl[(size_t)M.efree[(size_t)(e0 + i)]] - 1;
-      for (int j = 0; j < nf; j++) {
-        const double a = Ae[(size_t)j * nf + i];
-        if (a == 0.0) continue;
-        const int lj = gl[(size_t)M.efree[(size_t)(e0 + j)]] - 1;
-        const int *c0 = &col[(size_t)rp[(size_t)li]], *c1 = &col[(size_t)rp[(size_t)li + 1] - 1] + 1;
-        val[(size_t)(std::lower_bound(c0, c1, lj) - &col[0])] += a;
+  // Every row is assembled on its own (rows split among host threads): its
+  // element occurrences are visited in element order, and for each column
+  // the non-zero contributions are summed in that order (element order, then
+  // row i, column j within the element), the entries sorted by column.  This
+  // is the serial element loop's arithmetic, row by row.
+  std::vector<int64_t> occ_ptr((size_t)n + 1, 0);
+  for (int64_t q = 0; q < (int64_t)M.efree.size(); q++) occ_ptr[(size_t)gl[(size_t)M.efree[(size_t)q]]]++;
+  for (int r = 0; r < n; r++) occ_ptr[(size_t)r + 1] += occ_ptr[(size_t)r];
+  std::vector<int> occ_e(M.efree.size()), occ_i(M.efree.size());
+  {
+    std::vector<int64_t> fill(occ_ptr.begin(), occ_ptr.end() - 1);
+    for (int e = 0; e < M.nell; e++)
+      for (int i = M.eptr[(size_t)e]; i < M.eptr[(size_t)e + 1]; i++) {
+        const int li = gl[(size_t)M.efree[(size_t)i]] - 1;
+        occ_e[(size_t)fill[(size_t)li]] = e;
+        occ_i[(size_t)fill[(size_t)li]++] = i - M.eptr[(size_t)e];
       }
-      b[(size_t)li] += M.erhs[(size_t)(e0 + i)];
+  }
+  const int nth = std::max(1, std::min(16, (int)std::thread::hardware_concurrency()));
+  std::vector<std::vector<int>> tcol((size_t)nth);
+  std::vector<std::vector<double>> tval((size_t)nth);
+  std::vector<int64_t> rcount((size_t)n, 0);
+  b.assign((size_t)n, 0.0);
+  auto work = [&](int t) {
+    const int r0 = (int)((int64_t)n * t / nth), r1 = (int)((int64_t)n * (t + 1) / nth);
+    std::vector<std::pair<int, double>> ent;
+    for (int r = r0; r < r1; r++) {
+      ent.clear();
+      double br = 0.0;
+      for (int64_t q = occ_ptr[(size_t)r]; q < occ_ptr[(size_t)r + 1]; q++) {
+        const int e = occ_e[(size_t)q], i = occ_i[(size_t)q];
+        const int e0 = M.eptr[(size_t)e], nf = M.eptr[(size_t)e + 1] - e0;
+        const double *Ae = &M.emat[(size_t)M.emat_off[(size_t)e]];
+        for (int j = 0; j < nf; j++) {
+          const double a = Ae[(size_t)j * nf + i];
+          if (a != 0.0) ent.push_back({gl[(size_t)M.efree[(size_t)(e0 + j)]] - 1, a});
+        }
+        br += M.erhs[(size_t)(e0 + i)];
+      }
+      b[(size_t)r] = br;
+      std::stable_sort(ent.begin(), ent.end(),
+                       [](const std::pair<int, double> &x, const std::pair<int, double> &y) { return x.first < y.first; });
+      int64_t cnt = 0;
+      for (size_t q = 0; q < ent.size();) {
+        double sv = 0.0;
+        size_t q1 = q;
+        for (; q1 < ent.size() && ent[q1].first == ent[q].first; q1++) sv += ent[q1].second;
+        tcol[(size_t)t].push_back(ent[q].first);
+        tval[(size_t)t].push_back(sv);
+        cnt++;
+        q = q1;
+      }
+      rcount[(size_t)r] = cnt;
     }
+  };
+  {
+    std::vector<std::thread> pool;
+    for (int t = 1; t < nth; t++) pool.emplace_back(work, t);
+    work(0);
+    for (auto &th : pool) th.join();
+  }
+  std::vector<int64_t> rp((size_t)n + 1, 0);
+  for (int r = 0; r < n; r++) rp[(size_t)r + 1] = rp[(size_t)r] + rcount[(size_t)r];
+  std::vector<int> col;
+  std::vector<double> val;
+  col.reserve((size_t)rp[(size_t)n]);
+  val.reserve((size_t)rp[(size_t)n]);
+  for (int t = 0; t < nth; t++) {
+    col.insert(col.end(), tcol[(size_t)t].begin(), tcol[(size_t)t].end());
+    val.insert(val.end(), tval[(size_t)t].begin(), tval[(size_t)t].end());
+    std::vector<int>().swap(tcol[(size_t)t]);
+    std::vector<double>().swap(tval[(size_t)t]);
   }
   // COO in row order with the reference's flipped indices (ElemMtxs_assemble.F90:262-266)
   ii.resize(col.size());
@@ -844,43 +880,52 @@ static bool aggregate(ScaledMatrix &S, int neighood, int minasize, int maxasize,
     // graphs; it is sized with room for that
     std::vector<int> stat((size_t)n, 0), dist((size_t)n, 0), nodes((size_t)4 * n + 64, 0);
     // nextgoodstart (1-based, length n): good seeds at the head, the outer
-    // layer of the newest aggregate at the tail, exactly as the reference
+    // layer of the newest aggregate at the tail, exactly as the reference.
+    // The reference compacts the head list before every seed choice (drops
+    // the seeds aggregated meanwhile) and then takes the first seed that
+    // repeats an earlier one, else the first.  Validity belongs to a node,
+    // not to a list position, so the same choice comes from an append-only
+    // list L: a cursor over its first valid entry and a queue of the
+    // positions where a node occurs for the second time (positions only
+    // grow).  The explicit array is rebuilt only for an iteration whose tail
+    // writes could reach the head, where the reference's overlapping use of
+    // the one array has to be replayed.
     std::vector<int> ngs((size_t)n + 1, 0);
-    int ngood = 0;
-    std::vector<int> seen((size_t)n, 0);
-    int seen_stamp = 0;
+    std::vector<int> L;
+    std::vector<int> occ((size_t)n, 0);
+    std::deque<size_t> rep;
+    size_t cur = 0;
+    int64_t nvalid = 0;  // entries of L whose node is not aggregated
+    auto append = [&](int v) {
+      L.push_back(v);
+      if (++occ[(size_t)v] == 2) rep.push_back(L.size() - 1);
+      nvalid++;
+    };
+    auto rebuild = [&](int cnt) {  // L = ngs[1..cnt]
+      for (int v : L) occ[(size_t)v] = 0;
+      L.clear();
+      rep.clear();
+      cur = 0;
+      nvalid = 0;
+      for (int q = 1; q <= cnt; q++) append(ngs[(size_t)q]);
+      for (int v : L)  // entries of aggregated nodes are not valid
+        if (stat[(size_t)v] >= kPending) nvalid--;
+    };
     maxasizelargest = coarse ? 3 * maxasize : maxasize + 4 * (2 * neighood);
     if (!coarse) st.beta = alpha / 4.0;
     Colourer col(S, neighood, maxasize, stat, dist, nodes, st);
     int first = 0;
     for (;;) {
-      // drop good starts that got aggregated meanwhile
-      if (ngood > 0) {
-        int w = 0;
-        for (int q = 1; q <= ngood; q++)
-          if (stat[(size_t)ngs[(size_t)q]] < kPending) {
-            w++;
-            if (w < q) ngs[(size_t)w] = ngs[(size_t)q];
-          }
-        ngood = w;
-      }
+      const int64_t valid_start = nvalid;  // the reference's compacted ngood
       int start;
-      if (ngood == 0) {
+      if (nvalid == 0) {
         while (first < n && stat[(size_t)first] >= kPending) first++;
         if (first >= n) break;
         start = first;
       } else {
-        // the first entry that repeats an earlier one (the reference scans all
-        // pairs, SpMtx_aggregation.F90:210-217; a stamp per pass gives the
-        // same answer in one sweep)
-        start = -1;
-        seen_stamp++;
-        for (int a = 1; a <= ngood; a++) {
-          int v = ngs[(size_t)a];
-          if (seen[(size_t)v] == seen_stamp) { start = v; break; }
-          seen[(size_t)v] = seen_stamp;
-        }
-        if (start < 0) start = ngs[1];
+        while (stat[(size_t)L[cur]] >= kPending) cur++;
+        while (!rep.empty() && stat[(size_t)L[rep.front()]] >= kPending) rep.pop_front();
+        start = rep.empty() ? L[cur] : L[rep.front()];
       }
       int nneigs = 0;
       int ok = col.colour(start, nneigs);
@@ -908,25 +953,49 @@ static bool aggregate(ScaledMatrix &S, int neighood, int minasize, int maxasize,
       } else {
         next_layer = 0;
       }
+      // the outer layer's size first: it decides whether the tail writes of
+      // the reference can reach its head list
+      int nouter_all = 0;
+      if (next_layer > neighood + 1)
+        for (int q = 0; q < nneigs; q++) {
+          int node = nodes[(size_t)q];
+          if (!(stat[(size_t)node] <= neighood + 1 && q + 1 <= maxasize) && stat[(size_t)node] == next_layer)
+            nouter_all++;
+        }
+      const bool replay = valid_start + 2 * (int64_t)nouter_all >= (int64_t)n;
+      int ngood = 0;
+      if (replay) {  // the reference's compacted head list in the array
+        for (size_t q = cur; q < L.size(); q++)
+          if (stat[(size_t)L[q]] < kPending) ngs[(size_t)++ngood] = L[q];
+      }
       int mindistance = INT_MAX, nouters = 0;
+      std::vector<int> outer;
       for (int q = 0; q < nneigs; q++) {
         int node = nodes[(size_t)q];
         if (stat[(size_t)node] <= neighood + 1 && q + 1 <= maxasize) {
           stat[(size_t)node] = kAggregated;
           aggrnum[(size_t)node] = nagrs;
+          nvalid -= occ[(size_t)node];
         } else if (next_layer > neighood + 1) {
           if (stat[(size_t)node] == next_layer) {
             mindistance = std::min(mindistance, dist[(size_t)node]);
             nouters++;
-            ngs[(size_t)(n - nouters + 1)] = node;
+            if (replay) ngs[(size_t)(n - nouters + 1)] = node;
+            else outer.push_back(node);
           }
         }
       }
-      for (int q = 1; q <= nouters; q++)
-        if (dist[(size_t)ngs[(size_t)(n - q + 1)]] == mindistance) {
-          ngood++;
-          ngs[(size_t)ngood] = ngs[(size_t)(n - q + 1)];
-        }
+      if (replay) {
+        for (int q = 1; q <= nouters; q++)
+          if (dist[(size_t)ngs[(size_t)(n - q + 1)]] == mindistance) {
+            ngood++;
+            ngs[(size_t)ngood] = ngs[(size_t)(n - q + 1)];
+          }
+        rebuild(ngood);
+      } else {
+        for (int v : outer)
+          if (dist[(size_t)v] == mindistance) append(v);
+      }
       for (int q = 0; q < nneigs; q++) {
         int node = nodes[(size_t)q];
         if (stat[(size_t)node] != kAggregated) { dist[(size_t)node] = 0; stat[(size_t)node] = 0; }

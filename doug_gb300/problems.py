@@ -151,6 +151,115 @@ def poisson2d_p1_elements(nodes: int = 17, jitter: float = 0.2, seed: int = 0, k
             np.array(erhs, np.float64), info)
 
 
+def _kuhn_tets(N: int):
+    """Node ids of the 6 Kuhn tetrahedra of every hex of an N^3 grid of
+    (N+1)^3 nodes (node id (i*(N+1) + j)*(N+1) + k; conforming across hexes)."""
+    n1 = N + 1
+    I, J, K = np.meshgrid(np.arange(N), np.arange(N), np.arange(N), indexing="ij")
+    base = ((I * n1 + J) * n1 + K).ravel()
+    step = np.array([n1 * n1, n1, 1])
+    tets = []
+    for perm in ((0, 1, 2), (0, 2, 1), (1, 0, 2), (1, 2, 0), (2, 0, 1), (2, 1, 0)):
+        a = step[perm[0]]
+        b = a + step[perm[1]]
+        c = b + step[perm[2]]
+        tets.append(np.stack([base, base + a, base + b, base + c], 1))
+    return np.concatenate(tets, 0)
+
+
+def elasticity3d_p1_elements(N: int = 64, jitter: float = 0.15, nboxes: int = 20, e_box: float = 1.0e3,
+                             nu: float = 0.3, seed: int = 0):
+    """3-D linear elasticity on P1 tetrahedra (element input, 3 freedoms per node).
+
+    The unit cube is an N^3 hex grid, every hex split into 6 Kuhn tetrahedra,
+    nodes off the boundary jittered uniformly by +-jitter*h (seeded).  Young's
+    modulus 1, except E = e_box in elements whose centroid lies in one of
+    ``nboxes`` seeded axis-aligned boxes; Poisson ratio nu.  The bottom face
+    (z = 0) is clamped (its freedoms are left out, as DOUG's freemap does);
+    body force (0, 0, -1) lumped to the vertices.  Freedom of node n (z > 0),
+    component c: 3*(index of n among the free nodes) + c + 1.
+
+    Returns (ngf, eptr, efree, emat, erhs, info) in the layout of
+    ``poisson2d_p1_elements`` (element matrices column by column, restricted
+    to the element's free freedoms), plus info["node_ijk"] (free node grid
+    indices, for box partitions).
+    """
+    rng = np.random.default_rng(seed)
+    n1 = N + 1
+    h = 1.0 / N
+    I, J, K = np.meshgrid(np.arange(n1), np.arange(n1), np.arange(n1), indexing="ij")
+    X = np.stack([I, J, K], -1).reshape(-1, 3) * h
+    inner = ((I > 0) & (I < N) & (J > 0) & (J < N) & (K > 0) & (K < N)).ravel()
+    X[inner] += rng.uniform(-jitter * h, jitter * h, size=(int(inner.sum()), 3))
+    tet = _kuhn_tets(N)
+    P = X[tet]                                          # (ne, 4, 3)
+    Jm = np.stack([P[:, 1] - P[:, 0], P[:, 2] - P[:, 0], P[:, 3] - P[:, 0]], 2)   # columns = edges
+    det = np.linalg.det(Jm)
+    vol = np.abs(det) / 6.0
+    Ji = np.linalg.inv(Jm)                              # rows: gradients of the barycentric coords 1..3
+    grad = np.concatenate([-Ji.sum(1, keepdims=True), Ji], 1)                  # (ne, 4, 3)
+    ne = tet.shape[0]
+    B = np.zeros((ne, 6, 12))
+    for a in range(4):
+        gx, gy, gz = grad[:, a, 0], grad[:, a, 1], grad[:, a, 2]
+        c = 3 * a
+        B[:, 0, c] = gx
+        B[:, 1, c + 1] = gy
+        B[:, 2, c + 2] = gz
+        B[:, 3, c] = gy
+        B[:, 3, c + 1] = gx
+        B[:, 4, c + 1] = gz
+        B[:, 4, c + 2] = gy
+        B[:, 5, c] = gz
+        B[:, 5, c + 2] = gx
+    lam = nu / ((1 + nu) * (1 - 2 * nu))
+    mu = 1.0 / (2 * (1 + nu))
+    D = np.zeros((6, 6))
+    D[:3, :3] = lam
+    D[[0, 1, 2], [0, 1, 2]] = lam + 2 * mu
+    D[[3, 4, 5], [3, 4, 5]] = mu
+    lo = rng.uniform(0.0, 0.85, size=(nboxes, 3))
+    hi = lo + rng.uniform(0.05, 0.25, size=(nboxes, 3))
+    cen = P.mean(1)
+    inbox = np.zeros(ne, dtype=bool)
+    for q in range(nboxes):
+        inbox |= np.all((cen >= lo[q]) & (cen <= hi[q]), axis=1)
+    E = np.where(inbox, e_box, 1.0)
+    Ke = np.matmul(np.matmul(B.transpose(0, 2, 1), D), B) * (E * vol)[:, None, None]   # (ne, 12, 12)
+    del B
+    # freedoms: nodes with k > 0
+    kz = K.ravel()
+    freenode = np.full(n1 ** 3, -1, dtype=np.int64)
+    freenode[kz > 0] = np.arange(int((kz > 0).sum()))
+    ngf = 3 * int((kz > 0).sum())
+    dof = (3 * freenode[tet])[:, :, None] + np.arange(3)[None, None, :] + 1        # (ne, 4, 3), 1-based
+    dof = np.where((freenode[tet] >= 0)[:, :, None], dof, 0).reshape(ne, 12)
+    mask = dof > 0
+    nf = mask.sum(1)
+    eptr = np.concatenate([[0], np.cumsum(nf)]).astype(np.int32)
+    efree = dof[mask].astype(np.int32)
+    m2 = mask[:, :, None] & mask[:, None, :]            # (e, j, i): column j, row i
+    emat = np.ascontiguousarray(Ke.transpose(0, 2, 1))[m2]
+    load = np.zeros((ne, 4, 3))
+    load[:, :, 2] = -(vol / 4.0)[:, None]
+    erhs = load.reshape(ne, 12)[mask]
+    fn = np.flatnonzero(kz > 0)
+    info = {"nell": ne, "ngf": ngf, "nsd": 3, "mfrelt": 12, "nnode": n1 ** 3,
+            "node_ijk": np.stack([I.ravel()[fn], J.ravel()[fn], kz[fn]], 1)}
+    return ngf, eptr, efree, emat, erhs, info
+
+
+def dof_box_partition(node_ijk, N: int, parts=(4, 4, 8), dofs_per_node: int = 3):
+    """1-based box-partition ids of the freedoms (``dofs_per_node`` per node)
+    from the free nodes' grid indices (i, j in 0..N, k in 1..N)."""
+    i, j, k = node_ijk[:, 0], node_ijk[:, 1], node_ijk[:, 2] - 1
+    bi = np.minimum(i * parts[0] // (N + 1), parts[0] - 1)
+    bj = np.minimum(j * parts[1] // (N + 1), parts[1] - 1)
+    bk = np.minimum(k * parts[2] // N, parts[2] - 1)
+    p = (bi * parts[1] + bj) * parts[2] + bk
+    return (np.repeat(p, dofs_per_node) + 1).astype(np.int32)
+
+
 def _fortran_record(fh, payload: bytes) -> None:
     n = np.array([len(payload)], dtype="<i4").tobytes()
     fh.write(n + payload + n)
