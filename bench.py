@@ -306,6 +306,12 @@ def run_gpu(args, rank, world):
             batched = run_batched(args, args.steps, args.warmup)
         except Exception as ex:  # reported in the line; the headline stands on its own
             batched = {"error": repr(ex)}
+    elasticity = None
+    if not args.no_elasticity:
+        try:
+            elasticity = run_elasticity(args, 1, 1)
+        except Exception as ex:
+            elasticity = {"error": repr(ex)}
 
     if rank != 0:
         return 0
@@ -349,6 +355,7 @@ def run_gpu(args, rank, world):
         "roofline": roofline, "cpu_baseline": cpu, "clocks": clocks,
         "gpu_launches": int(launches),
         "batched": batched,
+        "elasticity": elasticity,
     }
     print(json.dumps(line), flush=True)
     return 0
@@ -450,6 +457,78 @@ def run_batched(args, steps, warmup):
     return out
 
 
+ELAS_N = 64
+ELAS_CTL = dict(solver=2, method=1, fine_method=1, levels=2, overlap=1, smoothers=1, strong1="0.08",
+                radius1=2, maxasize1=100, solve_tolerance=TOL, solve_maxiters=5000)
+ELAS_WORKLOAD = ("3-D linear elasticity, P1 tetrahedra: 64^3 hexes x 6 tets (1,572,864 elements, 12x12 element "
+                 "matrices), nodes jittered +-0.15h, E = 1 with 20 seeded boxes of E = 1e3, nu = 0.3, bottom "
+                 "face clamped, body force (0,0,-1): 811,200 freedoms; elemental input; 128 box subdomains "
+                 "(4x4x8), overlap 1, the reference's scalar smoothed-aggregation coarse grid")
+
+
+def run_elasticity(args, steps, warmup):
+    """The elemental elasticity workload: mixed and FP64 solves with the
+    assembled products, and the mixed solve with the matrix-free element
+    products (elemental_matvec 1); every step is a full solve from the
+    element right-hand side in HBM."""
+    import torch
+    import doug_gb300 as D
+    from doug_gb300 import problems as P
+
+    D.build_library()
+    ngf, eptr, efree, emat, erhs, info = P.elasticity3d_p1_elements(ELAS_N, seed=SEED)
+    part = P.dof_box_partition(info["node_ijk"], ELAS_N)
+    stream = torch.cuda.current_stream()
+    sptr = stream.cuda_stream
+    out = {"config": {"workload": ELAS_WORKLOAD, "n": int(ngf), "elements": int(len(eptr) - 1),
+                      "element_values": int(len(emat)), "controls": ELAS_CTL}}
+    xs = {}
+    for name, prec, emv in (("mixed", 1, 0), ("fp64", 0, 0), ("mixed_matrix_free", 1, 1)):
+        s = D.DougSolver(ELAS_CTL)
+        s.set_option("precision", prec)
+        s.set_option("elemental_matvec", emv)
+        s.set_elements(ngf, eptr, efree, emat, erhs)
+        s.set_partition(part)
+        t0 = time.perf_counter()
+        s.setup()
+        setup_s = time.perf_counter() - t0
+        b = s.input_matrix()[4]
+        bd = torch.tensor(b, dtype=torch.float64, device="cuda")
+        xd = torch.empty_like(bd)
+        k = steps if name == "mixed" else 1
+        for _ in range(warmup if name == "mixed" else 1):
+            s.solve_device(bd.data_ptr(), xd.data_ptr(), sptr)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(k):
+            st = s.solve_device(bd.data_ptr(), xd.data_ptr(), sptr)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        t = e0.elapsed_time(e1) * 1e-3 / k
+        s.set_option("profile", 1)
+        pr = s.solve_device(bd.data_ptr(), xd.data_ptr(), sptr)
+        s.set_option("profile", 0)
+        xs[name] = xd.cpu().numpy()
+        res = {"solve_s": t, "iterations": st.iterations, "true_rel_residual": st.true_rel_residual,
+               "setup_host_s": setup_s, "gpu_launches": st.gpu_launches,
+               "phases": {"factor_s": pr.t_factor_s, "iterate_s": pr.t_iterate_s, "subsolve_s": pr.t_subsolve_s,
+                          "coarse_s": pr.t_coarse_s, "product_s": pr.t_spmv_s,
+                          "product_ms_per_iteration": 1e3 * pr.t_spmv_s / max(pr.iterations, 1)}}
+        if name == "mixed":
+            sz = s.sizes()
+            out["config"].update({"nnz": int(len(s.input_matrix()[3])), "subdomains": sz["nsubdomains"],
+                                  "coarse_unknowns": sz["nagr_fine"]})
+        out[name] = res
+        del s
+        torch.cuda.empty_cache()
+    x64 = xs["fp64"]
+    for name in ("mixed", "mixed_matrix_free"):
+        out[name]["rel_err_vs_fp64_solution"] = float(np.linalg.norm(xs[name] - x64) / np.linalg.norm(x64))
+    out["mixed_vs_fp64"] = out["mixed"]["solve_s"] / out["fp64"]["solve_s"]
+    return out
+
+
 def run_profile_solve(args):
     """One solve of the workload (grid args.grid^3) inside a
     cudaProfilerStart/Stop range, after one warm-up solve: the command the
@@ -459,7 +538,18 @@ def run_profile_solve(args):
 
     D.build_library()
     torch.cuda.set_device(0)
-    if args.workload == "batched":
+    if args.workload == "elasticity":
+        from doug_gb300 import problems as P
+        ngf, eptr, efree, emat, erhs, info = P.elasticity3d_p1_elements(args.grid, seed=SEED)
+        s = D.DougSolver(ELAS_CTL)
+        s.set_option("precision", args.precision)
+        s.set_option("elemental_matvec", 1)
+        s.set_elements(ngf, eptr, efree, emat, erhs)
+        s.set_partition(P.dof_box_partition(info["node_ijk"], args.grid))
+        s.setup()
+        b = s.input_matrix()[4]
+        n = b.shape[0]
+    elif args.workload == "batched":
         from doug_gb300 import problems as P
         systems = P.batched_poisson2d_p1(BATCH_SYSTEMS, seed=SEED)
         b = np.concatenate([t[4] for t in systems])
@@ -495,8 +585,9 @@ def main():
     ap.add_argument("--fp64-steps", type=int, default=1)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batched", action="store_true", help="skip the batched uneven-systems workload")
-    ap.add_argument("--workload", default="diffusion128", choices=["diffusion128", "batched"],
-                    help="batched: print only the batched uneven-systems line")
+    ap.add_argument("--no-elasticity", action="store_true", help="skip the elemental elasticity workload")
+    ap.add_argument("--workload", default="diffusion128", choices=["diffusion128", "batched", "elasticity"],
+                    help="batched / elasticity: print only that workload's line")
     ap.add_argument("--profile-solve", action="store_true",
                     help="one solve inside a profiler range (for ncu), no timing line")
     ap.add_argument("--grid", type=int, default=N, help="grid size of --profile-solve")
@@ -504,6 +595,19 @@ def main():
     args = ap.parse_args()
     if args.profile_solve:
         return run_profile_solve(args)
+    if args.workload == "elasticity" and args.impl == "gb300" and not args.profile_solve:
+        import torch
+        torch.cuda.set_device(0)
+        with ClockSampler(0) as clk:
+            el = run_elasticity(args, args.steps, args.warmup)
+        m = el["mixed"]
+        print(json.dumps({"metric": "time to rel. residual 1e-8 (s), elemental elasticity, 1 GB300",
+                          "value": m["solve_s"], "unit": "s", "n_gpus": 1, "steps": args.steps,
+                          "warmup": args.warmup, "ms_per_step": m["solve_s"] * 1e3, "higher_is_better": False,
+                          "scaling": "weak", "vs_baseline": None, "dtype": "f64 outer / f32 subdomain factors",
+                          "data": "synthetic (seeded generator, doug_gb300/problems.py)",
+                          "config": el["config"], "elasticity": el, "clocks": clk.summary()}), flush=True)
+        return 0
     if args.workload == "batched" and args.impl == "gb300" and not args.profile_solve:
         import torch
         torch.cuda.set_device(0)

@@ -1047,46 +1047,81 @@ __global__ void grad_elements(int nell, const int *__restrict__ eptr, const int 
 // contributions in element order (no atomics: the result is deterministic)
 // and the p.q partial sums.
 // ---------------------------------------------------------------------------
-constexpr int kElemChunk = 4096;  // doubles of element matrices per CTA stage (32 KB)
+constexpr int kElemChunk = 4096;  // matrix values per CTA stage (32 KB)
+constexpr int kElemFree = 512;    // element freedoms per CTA stage
+constexpr int kElemRun = 512;     // elements per CTA stage
 
-// task t = elements [erun[t], erun[t+1]) whose matrices total <= kElemChunk values
+// A(i, j) of an element matrix in shared memory: full column-major storage,
+// or (SYM) the lower triangle column by column, column c starting at
+// c*nf - c(c-1)/2 (for bitwise symmetric element matrices: the same values)
+template <bool SYM>
+__device__ __forceinline__ double elem_entry(const double *Me, int nf, int i, int j) {
+  if (!SYM) return Me[j * nf + i];
+  const int r = i >= j ? i : j, c = i >= j ? j : i;
+  return Me[c * nf - (c * (c - 1)) / 2 + (r - c)];
+}
+
+// task t = elements [erun[t], erun[t+1]); the CTA stages their matrices, their
+// offsets and the p values of their freedoms in shared memory (coalesced
+// loads; the p gathers all in flight at once), then one thread per
+// (element, column): c = sum_i A_e(i, j) p[f_i] in increasing i
+template <bool SYM>
 __global__ void __launch_bounds__(256)
 elem_contrib(const int *__restrict__ erun, const int *__restrict__ eptr, const int *__restrict__ efl,
              const int64_t *__restrict__ eoff, const double *__restrict__ emat, const double *__restrict__ p,
              double *__restrict__ c) {
   __shared__ double Ms[kElemChunk];
-  const int e0 = erun[blockIdx.x], e1 = erun[blockIdx.x + 1];
+  __shared__ double ps[kElemFree];
+  __shared__ int ep[kElemRun + 1], eo[kElemRun + 1];
+  const int e0 = erun[blockIdx.x], e1 = erun[blockIdx.x + 1], ne = e1 - e0;
+  const int f0 = eptr[e0], nfr = eptr[e1] - f0;
   const int64_t m0 = eoff[e0];
   const int len = (int)(eoff[e1] - m0);
   for (int q = threadIdx.x; q < len; q += blockDim.x) Ms[q] = emat[m0 + q];
+  for (int q = threadIdx.x; q <= ne; q += blockDim.x) {
+    ep[q] = eptr[e0 + q] - f0;
+    eo[q] = (int)(eoff[e0 + q] - m0);
+  }
+  for (int q = threadIdx.x; q < nfr; q += blockDim.x) ps[q] = p[efl[f0 + q]];
   __syncthreads();
-  // one thread per (element, column)
-  const int f0 = eptr[e0], nitems = eptr[e1] - f0;
-  for (int t = threadIdx.x; t < nitems; t += blockDim.x) {
-    int lo = e0, hi = e1 - 1;  // element of item t: the last e with eptr[e] <= f0 + t
+  for (int t = threadIdx.x; t < nfr; t += blockDim.x) {
+    int lo = 0, hi = ne - 1;  // element of item t: the last e with ep[e] <= t
     while (lo < hi) {
       const int mid = (lo + hi + 1) >> 1;
-      if (eptr[mid] <= f0 + t) lo = mid; else hi = mid - 1;
+      if (ep[mid] <= t) lo = mid; else hi = mid - 1;
     }
-    const int e = lo, fe = eptr[e], nf = eptr[e + 1] - fe, j = f0 + t - fe;
-    const double *Aj = Ms + (eoff[e] - m0) + (int64_t)j * nf;  // column j
+    const int fe = ep[lo], nf = ep[lo + 1] - fe, j = t - fe;
+    const double *Me = Ms + eo[lo];
+    const double *pe = ps + fe;
     double s = 0.0;
-    for (int i = 0; i < nf; i++) s = __dadd_rn(s, __dmul_rn(Aj[i], p[efl[fe + i]]));
+    for (int i = 0; i < nf; i++) s = __dadd_rn(s, __dmul_rn(elem_entry<SYM>(Me, nf, i, j), pe[i]));
     c[f0 + t] = s;
   }
 }
 
-// q[r] = sum of r's element contributions (element order); partial p.q
+// q[r] = sum of r's element contributions (element order); partial p.q.
+// Four contributions of a row are loaded before they are added.
 __global__ void __launch_bounds__(kVecThreads)
 elem_pull_pq(int n, const int64_t *__restrict__ rptr, const int *__restrict__ ridx, const double *__restrict__ c,
              const double *__restrict__ p, double *__restrict__ q, double *__restrict__ part_pq) {
   __shared__ double sh[32];
   double spq = 0.0;
   for (int r = blockIdx.x * kVecThreads + threadIdx.x; r < n; r += gridDim.x * kVecThreads) {
+    const int64_t t0 = rptr[r], t1 = rptr[r + 1];
+    const double pr = p[r];
     double s = 0.0;
-    for (int64_t t = rptr[r]; t < rptr[r + 1]; t++) s = __dadd_rn(s, c[ridx[t]]);
+    int64_t t = t0;
+    for (; t + 4 <= t1; t += 4) {
+      const int i0 = ridx[t], i1 = ridx[t + 1], i2 = ridx[t + 2], i3 = ridx[t + 3];
+      const double c0 = c[i0], c1 = c[i1], c2 = c[i2], c3 = c[i3];
+      s = __dadd_rn(s, c0);
+      s = __dadd_rn(s, c1);
+      s = __dadd_rn(s, c2);
+      s = __dadd_rn(s, c3);
+    }
+    for (; t < t1; t++) s = __dadd_rn(s, c[ridx[t]]);
     q[r] = s;
-    spq += p[r] * s;
+    spq += pr * s;
   }
   double b = block_sum<kVecThreads>(spq, sh);
   if (threadIdx.x == 0) part_pq[blockIdx.x] = b;

@@ -519,6 +519,9 @@ struct dg_handle {
   bool elem_mv = false;           // PCG products with the element matrices
   DBuf<int64_t> d_el_off;
   DBuf<double> d_el_mat;
+  bool el_sym = false;             // the matvec reads packed lower triangles
+  DBuf<int64_t> d_el_poff;
+  DBuf<double> d_el_pack;
   bool factored = false;          // the device holds factors of the current setup
   int nparts = 0;
   // batched independent systems (dg_set_systems): system k owns the rows
@@ -651,8 +654,12 @@ void spmv_any(int lanes, int grid, cudaStream_t s, dg_handle *h, int first, int 
   if (h->elem_mv) {  // matrix-free product with the element matrices
     cg_direction<<<grid, kVecThreads, 0, s>>>(h->n, h->z.p, h->p.p, h->part_rz.p, h->part_rzo.p, h->sc.p, first,
                                               flexible);
-    elem_contrib<<<h->el_nrun, 256, 0, s>>>(h->d_el_run.p, h->d_el_eptr.p, h->d_el_local.p, h->d_el_off.p,
-                                            h->d_el_mat.p, h->p.p, h->d_el_c.p);
+    if (h->el_sym)
+      elem_contrib<true><<<h->el_nrun, 256, 0, s>>>(h->d_el_run.p, h->d_el_eptr.p, h->d_el_local.p,
+                                                    h->d_el_poff.p, h->d_el_pack.p, h->p.p, h->d_el_c.p);
+    else
+      elem_contrib<false><<<h->el_nrun, 256, 0, s>>>(h->d_el_run.p, h->d_el_eptr.p, h->d_el_local.p,
+                                                     h->d_el_off.p, h->d_el_mat.p, h->p.p, h->d_el_c.p);
     elem_pull_pq<<<grid, kVecThreads, 0, s>>>(h->n, h->d_el_rptr.p, h->d_el_ridx.p, h->d_el_c.p, h->p.p, h->q.p,
                                               h->part_pq.p);
     return;
@@ -762,14 +769,49 @@ dg_status do_setup(dg_handle *h, bool reuse_host = false) {
         h->d_el_eptr.upload(h->el_eptr); h->d_el_local.upload(h->el_local);
         h->d_el_off.upload(h->el_off); h->d_el_mat.upload(h->el_mat);
         if (c.elemental_matvec == 1) {
-          // element runs of at most kElemChunk matrix values; per row, its
-          // contribution slots in element order
+          // bitwise symmetric element matrices are read as packed lower
+          // triangles (the same values, 46 % fewer bytes for 12 x 12)
           const int nell = (int)h->el_eptr.size() - 1;
+          bool sym = true;
+          for (int e = 0; e < nell && sym; e++) {
+            const int nf = h->el_eptr[(size_t)e + 1] - h->el_eptr[(size_t)e];
+            const double *A = &h->el_mat[(size_t)h->el_off[(size_t)e]];
+            for (int j = 0; j < nf && sym; j++)
+              for (int i = j + 1; i < nf; i++)
+                if (!(A[(size_t)j * nf + i] == A[(size_t)i * nf + j])) { sym = false; break; }
+          }
+          std::vector<int64_t> poff(1, 0);
+          if (sym) {
+            for (int e = 0; e < nell; e++) {
+              const int64_t nf = h->el_eptr[(size_t)e + 1] - h->el_eptr[(size_t)e];
+              poff.push_back(poff.back() + nf * (nf + 1) / 2);
+            }
+            std::vector<double> pack((size_t)poff.back());
+            for (int e = 0; e < nell; e++) {
+              const int nf = h->el_eptr[(size_t)e + 1] - h->el_eptr[(size_t)e];
+              const double *A = &h->el_mat[(size_t)h->el_off[(size_t)e]];
+              double *P = &pack[(size_t)poff[(size_t)e]];
+              for (int j = 0, o = 0; j < nf; j++)
+                for (int i = j; i < nf; i++) P[o++] = A[(size_t)j * nf + i];
+            }
+            h->d_el_poff.upload(poff);
+            h->d_el_pack.upload(pack);
+          }
+          h->el_sym = sym;
+          const std::vector<int64_t> &moff = sym ? poff : h->el_off;
+          // element runs of at most kElemChunk matrix values, kElemFree
+          // freedoms and kElemRun elements; per row, its contribution slots
+          // in element order
           std::vector<int> run(1, 0);
           for (int e = 0; e < nell; e++) {
-            const int64_t sz = h->el_off[(size_t)e + 1] - h->el_off[(size_t)e];
-            if (sz > kElemChunk) throw CudaError{cudaErrorInvalidValue, "element matrix larger than the matvec stage"};
-            if (h->el_off[(size_t)e + 1] - h->el_off[(size_t)run.back()] > kElemChunk) run.push_back(e);
+            const int64_t sz = moff[(size_t)e + 1] - moff[(size_t)e];
+            const int nf = h->el_eptr[(size_t)e + 1] - h->el_eptr[(size_t)e];
+            if (sz > kElemChunk || nf > kElemFree)
+              throw CudaError{cudaErrorInvalidValue, "element matrix larger than the matvec stage"};
+            const int r0 = run.back();
+            if (moff[(size_t)e + 1] - moff[(size_t)r0] > kElemChunk ||
+                h->el_eptr[(size_t)e + 1] - h->el_eptr[(size_t)r0] > kElemFree || e + 1 - r0 > kElemRun)
+              run.push_back(e);
           }
           run.push_back(nell);
           std::vector<int64_t> rptr((size_t)n + 1, 0);

@@ -156,11 +156,19 @@ def test_elements_p1_gpu_vs_oracle(precision):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("precision", [0, 1])
-def test_elemental_matvec_gpu(precision):
+@pytest.mark.parametrize("precision,asym", [(0, False), (1, False), (0, True)])
+def test_elemental_matvec_gpu(precision, asym):
     # PCG products with the stored element matrices (elemental_matvec 1) give the
-    # same solve as the assembled CSR products
+    # same solve as the assembled CSR products; bitwise symmetric element
+    # matrices are read as packed triangles, others (asym: one ulp off the
+    # diagonal) in full
     ngf, eptr, efree, emat, erhs, info = _p1_elements(nodes=65, seed=9, kappa=True)
+    if asym:
+        nf = np.diff(eptr)
+        off = np.concatenate([[0], np.cumsum(nf * nf)])
+        emat = emat.copy()
+        for e in np.flatnonzero(nf >= 2)[::3]:
+            emat[off[e] + 1] = np.nextafter(emat[off[e] + 1], np.inf)  # A(1, 0) only
     opts = dict(solver=2, method=1, fine_method=1, levels=2, smoothers=1, overlap=1, strong1="0.08",
                 radius1=2, solve_tolerance="1.0e-10", solve_maxiters=500)
     xs = []
