@@ -1094,7 +1094,8 @@ elem_contrib(const int *__restrict__ erun, const int *__restrict__ eptr, const i
     const double *Me = Ms + eo[lo];
     const double *pe = ps + fe;
     double s = 0.0;
-    for (int i = 0; i < nf; i++) s = __dadd_rn(s, __dmul_rn(elem_entry<SYM>(Me, nf, i, j), pe[i]));
+    // fused multiply-adds: FP64 issue, not DRAM, bounds this product on GB300
+    for (int i = 0; i < nf; i++) s = __fma_rn(elem_entry<SYM>(Me, nf, i, j), pe[i], s);
     c[f0 + t] = s;
   }
 }
@@ -1287,16 +1288,15 @@ spmv_pq(int n, const int64_t *__restrict__ Ap, const int *__restrict__ Ac, const
     if (i < n) {
       int64_t e = Ap[i] + sub;
       const int64_t e1 = Ap[i + 1];
-      if (LANES == 1) {  // short rows: all loads of a row issued before the sums
-        for (; e + 4 <= e1; e += 4) {
-          const int c0 = Ac[e], c1 = Ac[e + 1], c2 = Ac[e + 2], c3 = Ac[e + 3];
-          const double a0 = Av[e], a1 = Av[e + 1], a2 = Av[e + 2], a3 = Av[e + 3];
-          const double p0 = p[c0], p1 = p[c1], p2 = p[c2], p3 = p[c3];
-          s = __fma_rn(a0, p0, s);
-          s = __fma_rn(a1, p1, s);
-          s = __fma_rn(a2, p2, s);
-          s = __fma_rn(a3, p3, s);
-        }
+      // four entries of this lane's share loaded before they are summed
+      for (; e + 3 * LANES < e1; e += 4 * LANES) {
+        const int c0 = Ac[e], c1 = Ac[e + LANES], c2 = Ac[e + 2 * LANES], c3 = Ac[e + 3 * LANES];
+        const double a0 = Av[e], a1 = Av[e + LANES], a2 = Av[e + 2 * LANES], a3 = Av[e + 3 * LANES];
+        const double p0 = p[c0], p1 = p[c1], p2 = p[c2], p3 = p[c3];
+        s = __fma_rn(a0, p0, s);
+        s = __fma_rn(a1, p1, s);
+        s = __fma_rn(a2, p2, s);
+        s = __fma_rn(a3, p3, s);
       }
       for (; e < e1; e += LANES) s = __fma_rn(Av[e], p[Ac[e]], s);
     }
@@ -1436,16 +1436,14 @@ bt_spmv_pq(const int *__restrict__ cb, const int *__restrict__ csys, const int *
     if (i < i1) {
       int64_t e = Ap[i] + sub;
       const int64_t e1 = Ap[i + 1];
-      if (LANES == 1) {
-        for (; e + 4 <= e1; e += 4) {
-          const int c0 = Ac[e], c1 = Ac[e + 1], c2 = Ac[e + 2], c3 = Ac[e + 3];
-          const double a0 = Av[e], a1 = Av[e + 1], a2 = Av[e + 2], a3 = Av[e + 3];
-          const double p0 = p[c0], p1 = p[c1], p2 = p[c2], p3 = p[c3];
-          s = __fma_rn(a0, p0, s);
-          s = __fma_rn(a1, p1, s);
-          s = __fma_rn(a2, p2, s);
-          s = __fma_rn(a3, p3, s);
-        }
+      for (; e + 3 * LANES < e1; e += 4 * LANES) {
+        const int c0 = Ac[e], c1 = Ac[e + LANES], c2 = Ac[e + 2 * LANES], c3 = Ac[e + 3 * LANES];
+        const double a0 = Av[e], a1 = Av[e + LANES], a2 = Av[e + 2 * LANES], a3 = Av[e + 3 * LANES];
+        const double p0 = p[c0], p1 = p[c1], p2 = p[c2], p3 = p[c3];
+        s = __fma_rn(a0, p0, s);
+        s = __fma_rn(a1, p1, s);
+        s = __fma_rn(a2, p2, s);
+        s = __fma_rn(a3, p3, s);
       }
       for (; e < e1; e += LANES) s = __fma_rn(Av[e], p[Ac[e]], s);
     }

@@ -630,13 +630,14 @@ double tridiag_cond(const std::vector<double> &alpha, const std::vector<double> 
   return lmin != 0 ? lmax / lmin : 0.0;
 }
 
+// lanes per CSR row: about 12 entries per lane (each lane loads four at a time)
 int lanes_for(const Csr &A) {
   double avg = A.nrows ? (double)A.nnz() / A.nrows : 1;
-  if (avg <= 9) return 1;  // thread per row, loads unrolled
-  if (avg <= 3) return 2;
-  if (avg <= 6) return 4;
-  if (avg <= 12) return 8;
-  if (avg <= 24) return 16;
+  if (avg <= 12) return 1;
+  if (avg <= 24) return 2;
+  if (avg <= 48) return 4;
+  if (avg <= 96) return 8;
+  if (avg <= 192) return 16;
   return 32;
 }
 

@@ -226,6 +226,7 @@ def elasticity3d_p1_elements(N: int = 64, jitter: float = 0.15, nboxes: int = 20
         inbox |= np.all((cen >= lo[q]) & (cen <= hi[q]), axis=1)
     E = np.where(inbox, e_box, 1.0)
     Ke = np.matmul(np.matmul(B.transpose(0, 2, 1), D), B) * (E * vol)[:, None, None]   # (ne, 12, 12)
+    Ke = 0.5 * (Ke + Ke.transpose(0, 2, 1))            # symmetric to the last bit
     del B
     # freedoms: nodes with k > 0
     kz = K.ravel()
