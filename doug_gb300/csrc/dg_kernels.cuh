@@ -641,22 +641,25 @@ constexpr int kEUnroll = 8;        // independent E loads in flight per thread
 // fronts per warp): a front of at most 4G rows, lane l of its group holding
 // the rows VN*l + G*VN*p.  Levels put their small fronts into three buckets
 // by size so that tiny fronts do not leave most of a warp idle.
+constexpr int kSmallUnroll = 4;   // E columns per load batch of a small-front group
+template <typename T> struct SmallMinBlocks { static constexpr int N = sizeof(T) == 8 ? 3 : 6; };
+
 template <int G>
 __device__ __forceinline__ unsigned group_mask(int lane) {
   return G == 32 ? 0xffffffffu : (((1u << G) - 1u) << (lane / G * G));
 }
 
-// E loads of one batch of kEUnroll columns [j0, j0 + kEUnroll) for the rows
+// E loads of one batch of kSmallUnroll columns [j0, j0 + kSmallUnroll) for the rows
 // of one group lane; vectors wholly above the diagonal (r + VN <= j) are zero
 template <typename T, int PASS, int G>
 __device__ __forceinline__ void load_e_batch(const T *Ef, int ld, int m, int k, int sl, int j0,
-                                             T (&e)[PASS][kEUnroll][Vec16<T>::N]) {
+                                             T (&e)[PASS][kSmallUnroll][Vec16<T>::N]) {
   constexpr int VN = Vec16<T>::N;
 #pragma unroll
   for (int p = 0; p < PASS; p++) {
     const int r = VN * sl + G * VN * p;
 #pragma unroll
-    for (int u = 0; u < kEUnroll; u++) {
+    for (int u = 0; u < kSmallUnroll; u++) {
       const int j = j0 + u;
       if (r < m && j < k && r + VN > j) Vec16<T>::load(Ef + (int64_t)j * ld + r, e[p][u]);
       else {
@@ -684,7 +687,7 @@ __device__ __forceinline__ void fwd_small_body(const MfView &v, const int *__res
   const int m = v.f_m[f], k = v.f_k[f], ld = round4(m);
   const int64_t xo = v.f_xoff[f] + v.f_p0[f];
   const T *Ef = E + v.e_off[f];
-  T e[PASS][kEUnroll][VN];
+  T e[PASS][kSmallUnroll][VN];
   load_e_batch<T, PASS, G>(Ef, ld, m, k, sl, 0, e);
   for (int i = sl; i < m; i += G) w[i] = i < k ? xl[xo + i] : T(0);
   __syncwarp(gm);
@@ -701,10 +704,10 @@ __device__ __forceinline__ void fwd_small_body(const MfView &v, const int *__res
   for (int p = 0; p < PASS; p++)
 #pragma unroll
     for (int q = 0; q < VN; q++) acc[p][q] = T(0);
-  for (int j0 = 0; j0 < k; j0 += kEUnroll) {
+  for (int j0 = 0; j0 < k; j0 += kSmallUnroll) {
     if (j0 > 0) load_e_batch<T, PASS, G>(Ef, ld, m, k, sl, j0, e);
 #pragma unroll
-    for (int u = 0; u < kEUnroll; u++) {
+    for (int u = 0; u < kSmallUnroll; u++) {
       const T bj = j0 + u < k ? w[j0 + u] : T(0);
 #pragma unroll
       for (int p = 0; p < PASS; p++)
@@ -729,7 +732,7 @@ __device__ __forceinline__ void bwd_small_body(const MfView &v, const int *__res
                                                const T *__restrict__ E, const T *__restrict__ yl,
                                                T *__restrict__ xl, int cta, T *wsh) {
   constexpr int VN = Vec16<T>::N, M = 4 * G, PASS = M / (G * VN), FPW = 32 / G;
-  static_assert(G >= kEUnroll, "a group stores one column sum per lane");
+  static_assert(G >= kSmallUnroll, "a group stores one column sum per lane");
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const int grp = lane / G, sl = lane % G;
   const unsigned gm = group_mask<G>(lane);
@@ -740,7 +743,7 @@ __device__ __forceinline__ void bwd_small_body(const MfView &v, const int *__res
   const int m = v.f_m[f], k = v.f_k[f], ld = round4(m);
   const int64_t xo = v.f_xoff[f] + v.f_p0[f];
   const T *Ef = E + v.e_off[f];
-  T e[PASS][kEUnroll][VN];
+  T e[PASS][kSmallUnroll][VN];
   load_e_batch<T, PASS, G>(Ef, ld, m, k, sl, 0, e);
   const T *xb = xl + v.f_xoff[f];
   const int *rows = v.rows + v.f_rows[f];
@@ -755,11 +758,11 @@ __device__ __forceinline__ void bwd_small_body(const MfView &v, const int *__res
       wr[p][q] = r < ld ? w[r] : T(0);
     }
   // each column sum is reduced over the group; lane u of the batch keeps column u
-  for (int c0 = 0; c0 < k; c0 += kEUnroll) {
+  for (int c0 = 0; c0 < k; c0 += kSmallUnroll) {
     if (c0 > 0) load_e_batch<T, PASS, G>(Ef, ld, m, k, sl, c0, e);
-    T s[kEUnroll];
+    T s[kSmallUnroll];
 #pragma unroll
-    for (int u = 0; u < kEUnroll; u++) {
+    for (int u = 0; u < kSmallUnroll; u++) {
       s[u] = T(0);
 #pragma unroll
       for (int p = 0; p < PASS; p++)
@@ -768,10 +771,10 @@ __device__ __forceinline__ void bwd_small_body(const MfView &v, const int *__res
 #pragma unroll
       for (int o = G / 2; o > 0; o >>= 1) s[u] += __shfl_xor_sync(gm, s[u], o);
     }
-    if (sl < kEUnroll && c0 + sl < k) {
+    if (sl < kSmallUnroll && c0 + sl < k) {
       T out = s[0];
 #pragma unroll
-      for (int u = 1; u < kEUnroll; u++) if (sl == u) out = s[u];
+      for (int u = 1; u < kSmallUnroll; u++) if (sl == u) out = s[u];
       xl[xo + c0 + sl] = out;
     }
   }
@@ -787,7 +790,7 @@ struct SmallBuckets {
 };
 
 template <typename T>
-__global__ void __launch_bounds__(256, sizeof(T) == 8 ? 2 : 4)
+__global__ void __launch_bounds__(256, SmallMinBlocks<T>::N)
 mf_fwd_small(MfView v, const int *__restrict__ fronts, SmallBuckets sb, const T *__restrict__ E,
              const T *__restrict__ xl, T *__restrict__ yl, T *__restrict__ uvec) {
   __shared__ __align__(16) T wsh[8 * kSolveSmall];
@@ -800,7 +803,7 @@ mf_fwd_small(MfView v, const int *__restrict__ fronts, SmallBuckets sb, const T 
 }
 
 template <typename T>
-__global__ void __launch_bounds__(256, sizeof(T) == 8 ? 2 : 4)
+__global__ void __launch_bounds__(256, SmallMinBlocks<T>::N)
 mf_bwd_small(MfView v, const int *__restrict__ fronts, SmallBuckets sb, const T *__restrict__ E,
              const T *__restrict__ yl, T *__restrict__ xl) {
   __shared__ __align__(16) T wsh[8 * kSolveSmall];
@@ -822,7 +825,7 @@ mf_bwd_small(MfView v, const int *__restrict__ fronts, SmallBuckets sb, const T 
 template <typename T> struct FwdRows { static constexpr int N = 32 * Vec16<T>::N; };
 
 template <typename T, int NT>
-__global__ void __launch_bounds__(NT, NT == kELeanThreads ? 8 : 2)
+__global__ void __launch_bounds__(NT, NT == kELeanThreads ? 12 : 4)
 mf_fwd_big(MfView v, const int2 *__restrict__ tasks, const T *__restrict__ E, const T *__restrict__ xl,
            T *__restrict__ yl, T *__restrict__ uvec) {
   constexpr int VN = Vec16<T>::N, RC = FwdRows<T>::N, NW = NT / 32, UN = NT == kELeanThreads ? 4 : kEUnroll;
@@ -897,7 +900,7 @@ mf_fwd_big(MfView v, const int2 *__restrict__ tasks, const T *__restrict__ E, co
 // large fronts, backward: task = {front, column block J}; x[32J .. 32J+31] from
 // rows [32J, m) of E
 template <typename T, int NT>
-__global__ void __launch_bounds__(NT, NT == kELeanThreads ? 8 : 2)
+__global__ void __launch_bounds__(NT, NT == kELeanThreads ? 12 : 4)
 mf_bwd_big(MfView v, const int2 *__restrict__ tasks, const T *__restrict__ E, const T *__restrict__ yl,
            T *__restrict__ xl) {
   constexpr int VN = Vec16<T>::N, LPC = 32 / VN, NCS = NT / LPC, UN = NT == kELeanThreads ? 4 : kEUnroll;
