@@ -42,7 +42,7 @@ TOL = "1.0e-8"
 CTL = dict(solver=2, method=1, fine_method=1, levels=2, overlap=2, smoothers=1,
            strong1="0.08", radius1=5, maxasize1=400, solve_tolerance=TOL, solve_maxiters=2000)
 METRIC = "time to rel. residual 1e-8 (s), mixed+batched vs plain FP64 PCG, 1 GB300"
-SUBSOLVE_TRAFFIC_BYTES = 4.5975e9  # ncu, one PCG iteration of the 128^3 mixed solve
+SUBSOLVE_TRAFFIC_BYTES = 4.620e9  # ncu, one PCG iteration of the 128^3 mixed solve
 WORKLOAD = ("128^3 log-normal diffusion (sigma 1, corr. length 8), 7-point FV, 2,097,152 unknowns; "
             "PCG + 2-level additive Schwarz: 64 subdomains (4x4x4 boxes), overlap 2, "
             "smoothed-aggregation coarse grid")
