@@ -306,6 +306,12 @@ def run_gpu(args, rank, world):
             batched = run_batched(args, args.steps, args.warmup)
         except Exception as ex:  # reported in the line; the headline stands on its own
             batched = {"error": repr(ex)}
+    adjoint = None
+    if not args.no_adjoint:
+        try:
+            adjoint = run_adjoint(args, 0)
+        except Exception as ex:
+            adjoint = {"error": repr(ex)}
     elasticity = None
     if not args.no_elasticity:
         try:
@@ -356,6 +362,7 @@ def run_gpu(args, rank, world):
         "gpu_launches": int(launches),
         "batched": batched,
         "elasticity": elasticity,
+        "adjoint": adjoint,
     }
     print(json.dumps(line), flush=True)
     return 0
@@ -529,6 +536,77 @@ def run_elasticity(args, steps, warmup):
     return out
 
 
+ADJ_NODES = 513
+ADJ_RHS = 32
+ADJ_CTL = dict(solver=2, method=1, fine_method=1, levels=2, overlap=1, smoothers=1, strong1="0.08",
+               radius1=2, solve_tolerance="1.0e-10", solve_maxiters=3000)
+ADJ_WORKLOAD = ("2-D P1 diffusion on a 513x513 jittered node grid (261,121 unknowns, 524,288 triangles), one "
+                "conductivity per element (log-normal, sigma 0.5), 32 right-hand sides U[-1,1], loss "
+                "sum ||x - x_target||^2 with x_target from the conductivities perturbed by 10 %; mixed-precision "
+                "PCG to 1e-10, adjoint gradients dL/dkappa and dL/db")
+
+
+def run_adjoint(args, fd_elements):
+    """Forward solve of the 32 right-hand sides and the adjoint backward pass
+    (doug_gb300.autograd.element_solve); optional central finite differences
+    of the loss on seeded elements (each two full forward solves, FP64 to 1e-12)."""
+    import torch
+    import doug_gb300 as D
+    from doug_gb300 import problems as P
+    from doug_gb300.autograd import element_solve
+
+    D.build_library()
+    rng = np.random.default_rng(SEED + 4)
+    ntri = 2 * (ADJ_NODES - 1) ** 2
+    kappa = np.exp(0.5 * rng.standard_normal(ntri))
+    ngf, eptr, efree, Kb, erhs, _ = P.poisson2d_p1_elements(nodes=ADJ_NODES, seed=SEED + 4)
+    B = torch.tensor(rng.uniform(-1.0, 1.0, (ngf, ADJ_RHS)), device="cuda")
+    k_target = kappa * (1.0 + 0.1 * rng.uniform(-1.0, 1.0, ntri))
+    s = D.DougSolver(ADJ_CTL)
+    s.set_option("precision", 1)
+    with torch.no_grad():
+        Xt = element_solve(s, ngf, eptr, efree, Kb, erhs, torch.tensor(k_target), B).detach()
+    k = torch.tensor(kappa, requires_grad=True)
+    bt = B.clone().requires_grad_(True)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    X = element_solve(s, ngf, eptr, efree, Kb, erhs, k, bt)
+    L = ((X - Xt) ** 2).sum()
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    L.backward()
+    torch.cuda.synchronize()
+    t2 = time.perf_counter()
+    g = k.grad.numpy().copy()
+    out = {"config": {"workload": ADJ_WORKLOAD, "n": int(ngf), "elements": ntri, "rhs": ADJ_RHS,
+                      "controls": ADJ_CTL},
+           "forward_s": t1 - t0, "backward_s": t2 - t1, "loss": float(L.item()),
+           "note": "forward = element assembly + host setup + numeric factorisations + 32 PCG solves; "
+                   "backward = 32 adjoint solves with the kept factors + dg_grad_elements"}
+    if fd_elements:
+        sf = D.DougSolver(dict(ADJ_CTL, solve_tolerance="1.0e-12"))
+        sf.set_option("precision", 0)
+
+        def loss(kap):
+            with torch.no_grad():
+                Xk = element_solve(sf, ngf, eptr, efree, Kb, erhs, torch.tensor(kap), B)
+                return float(((Xk - Xt) ** 2).sum().item())
+
+        sel = rng.choice(ntri, fd_elements, replace=False)
+        errs = []
+        gmax = float(np.abs(g).max())
+        for e in sel:
+            h = 1e-4 * kappa[e]
+            kp, km = kappa.copy(), kappa.copy()
+            kp[e] += h
+            km[e] -= h
+            fd = (loss(kp) - loss(km)) / (2 * h)
+            errs.append(abs(fd - g[e]) / max(gmax, 1e-300))
+        out["fd_elements"] = int(fd_elements)
+        out["fd_max_err_rel_to_max_grad"] = float(max(errs))
+    return out
+
+
 def run_profile_solve(args):
     """One solve of the workload (grid args.grid^3) inside a
     cudaProfilerStart/Stop range, after one warm-up solve: the command the
@@ -586,8 +664,11 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batched", action="store_true", help="skip the batched uneven-systems workload")
     ap.add_argument("--no-elasticity", action="store_true", help="skip the elemental elasticity workload")
-    ap.add_argument("--workload", default="diffusion128", choices=["diffusion128", "batched", "elasticity"],
-                    help="batched / elasticity: print only that workload's line")
+    ap.add_argument("--no-adjoint", action="store_true", help="skip the differentiation workload")
+    ap.add_argument("--fd-elements", type=int, default=50, help="finite-difference checks of --workload adjoint")
+    ap.add_argument("--workload", default="diffusion128",
+                    choices=["diffusion128", "batched", "elasticity", "adjoint"],
+                    help="batched / elasticity / adjoint: print only that workload's line")
     ap.add_argument("--profile-solve", action="store_true",
                     help="one solve inside a profiler range (for ncu), no timing line")
     ap.add_argument("--grid", type=int, default=N, help="grid size of --profile-solve")
@@ -595,6 +676,18 @@ def main():
     args = ap.parse_args()
     if args.profile_solve:
         return run_profile_solve(args)
+    if args.workload == "adjoint" and args.impl == "gb300" and not args.profile_solve:
+        import torch
+        torch.cuda.set_device(0)
+        with ClockSampler(0) as clk:
+            ad = run_adjoint(args, args.fd_elements)
+        print(json.dumps({"metric": "forward + adjoint time (s), 32 right-hand sides, 1 GB300",
+                          "value": ad["forward_s"] + ad["backward_s"], "unit": "s", "n_gpus": 1, "steps": 1,
+                          "warmup": 0, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+                          "dtype": "f64 outer / f32 subdomain factors",
+                          "data": "synthetic (seeded generator, doug_gb300/problems.py)",
+                          "config": ad["config"], "adjoint": ad, "clocks": clk.summary()}), flush=True)
+        return 0
     if args.workload == "elasticity" and args.impl == "gb300" and not args.profile_solve:
         import torch
         torch.cuda.set_device(0)

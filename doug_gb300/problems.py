@@ -137,18 +137,15 @@ def poisson2d_p1_elements(nodes: int = 17, jitter: float = 0.2, seed: int = 0, k
     f = rng.uniform(-1.0, 1.0, size=nodes * nodes)
     free = np.zeros(nodes * nodes, dtype=np.int64)
     free[interior.ravel()] = np.arange(1, int(interior.sum()) + 1)
-    eptr = [0]
-    efree, emat, erhs = [], [], []
-    for e in range(len(tri)):
-        loc = [a for a in range(3) if free[tri[e, a]] > 0]
-        efree.extend(int(free[tri[e, a]]) for a in loc)
-        Ke = K[e][np.ix_(loc, loc)]
-        emat.extend(Ke.T.ravel())          # column by column
-        erhs.extend(f[tri[e, a]] * area[e] / 3.0 for a in loc)
-        eptr.append(len(efree))
+    ft = free[tri]                                    # (ne, 3), 0 = boundary vertex
+    mask = ft > 0
+    eptr = np.concatenate([[0], np.cumsum(mask.sum(1))]).astype(np.int32)
+    efree = ft[mask].astype(np.int32)
+    m2 = mask[:, :, None] & mask[:, None, :]          # (e, j, i): column j, row i
+    emat = np.ascontiguousarray(K.transpose(0, 2, 1))[m2]      # column by column
+    erhs = (f[tri] * area[:, None] / 3.0)[mask]
     info = {"nell": len(tri), "ngf": int(interior.sum()), "nsd": 2, "mfrelt": 3, "nnode": nodes * nodes}
-    return (info["ngf"], np.array(eptr, np.int32), np.array(efree, np.int32), np.array(emat, np.float64),
-            np.array(erhs, np.float64), info)
+    return info["ngf"], eptr, efree, np.asarray(emat, np.float64), np.asarray(erhs, np.float64), info
 
 
 def _kuhn_tets(N: int):
