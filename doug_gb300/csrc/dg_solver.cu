@@ -711,6 +711,140 @@ void bt_step(dg_handle *h, cudaStream_t s, int step, int first, int mixed, doubl
                                 h->d_state.p, h->d_iters.p, h->d_dit.p, h->d_host_counts);
 }
 
+// q = A r with L lanes per row and the r.q partials (any CSR on the device)
+void spmv_lanes(int lanes, cudaStream_t s, int n, const int64_t *Ap, const int *Ac, const double *Av,
+                const double *r, double *q, double *part) {
+  const int g = kRedBlocks;
+  switch (lanes) {
+    case 1: spmv_pq<1><<<g, kVecThreads, 0, s>>>(n, Ap, Ac, Av, r, q, part); break;
+    case 2: spmv_pq<2><<<g, kVecThreads, 0, s>>>(n, Ap, Ac, Av, r, q, part); break;
+    case 4: spmv_pq<4><<<g, kVecThreads, 0, s>>>(n, Ap, Ac, Av, r, q, part); break;
+    case 8: spmv_pq<8><<<g, kVecThreads, 0, s>>>(n, Ap, Ac, Av, r, q, part); break;
+    case 16: spmv_pq<16><<<g, kVecThreads, 0, s>>>(n, Ap, Ac, Av, r, q, part); break;
+    default: spmv_pq<32><<<g, kVecThreads, 0, s>>>(n, Ap, Ac, Av, r, q, part); break;
+  }
+}
+
+// Robust coarse space (coarse_method 2) on the GPU.  B p = sum_i R_i^T
+// A_i^-1 R_i p is one gather into the supports, one batched FP64
+// multifrontal solve of all support matrices A_i = A(S_i, S_i) and one pull
+// sum (supports in order).  B g = 1 is solved by CG preconditioned with A
+// itself (B is locally a multiple of A^-1), to ||r||/||r0|| <= 1e-14 or until
+// the residual stops falling: the reference's CG (pcg_forRCS,
+// pcg_robust.f90:37-120) asks for ||r||/||r0|| <= tol^2, so it too solves to
+// rounding level.  Then q_i = A_i^-1 g(S_i) (RobustRestrictMtxBuild,
+// RobustCoarseMtx.f90:175-202) with the same factors.
+bool robust_restriction_gpu(const Controls &c, const Csr &A, const std::vector<int64_t> &sp,
+                            const std::vector<int> &sn, std::vector<double> &q, std::string &err,
+                            bool &no_device) {
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+    no_device = true;
+    err = "no CUDA device is visible; the robust coarse space is built on the GPU";
+    return false;
+  }
+  cudaStream_t s = nullptr;
+  double *host_out = nullptr, *d_host_out = nullptr;
+  int *host_status = nullptr, *d_host_status = nullptr;
+  bool ok = false;
+  try {
+    const int n = A.nrows;
+    std::vector<int> sn1(sn.size());
+    for (size_t k = 0; k < sn.size(); k++) sn1[k] = sn[k] + 1;
+    MfBatch Bs;
+    MfOptions mo;
+    mo.leaf = c.nd_leaf;
+    mf_build_subdomains(A, sp, sn1, mo, Bs);
+    MfTune tune;
+    tune.panel_rows = c.panel_rows;
+    tune.fwd_task_bytes = (int64_t)c.fwd_task_kb * 1024;
+    tune.lean_task_bytes = (int64_t)c.lean_task_kb * 1024;
+    tune.small_min_fronts = c.thin_level_fronts;
+    CK(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+    CK(cudaHostAlloc(&host_out, 16 * sizeof(double), cudaHostAllocMapped));
+    CK(cudaHostAlloc(&host_status, sizeof(int), cudaHostAllocMapped));
+    CK(cudaHostGetDevicePointer(&d_host_out, host_out, 0));
+    CK(cudaHostGetDevicePointer(&d_host_status, host_status, 0));
+    MfDevice<double> dev;
+    dev.upload(Bs, tune);
+    DBuf<double> Av, x, r, z, p, qv, part_rz, part_pq, part_rr, sc;
+    DBuf<int64_t> Ap;
+    DBuf<int> Ac, status, pull_ptr, pull_idx;
+    Av.upload(A.val); Ap.upload(A.ptr); Ac.upload(A.col);
+    for (auto *v : {&x, &r, &z, &p, &qv}) v->alloc((size_t)n);
+    for (auto *v : {&part_rz, &part_pq, &part_rr}) v->alloc(kRedBlocks);
+    sc.alloc(8);
+    status.alloc(1);
+    CK(cudaMemset(sc.p, 0, 8 * sizeof(double)));
+    CK(cudaMemset(status.p, 0, sizeof(int)));
+    {  // pull lists: support arena positions of every node, supports in order
+      std::vector<int> pp((size_t)n + 1, 0);
+      for (int g : Bs.gidx) pp[(size_t)g + 1]++;
+      for (int i = 0; i < n; i++) pp[(size_t)i + 1] += pp[(size_t)i];
+      std::vector<int> idx((size_t)pp[(size_t)n]);
+      std::vector<int> fill(pp.begin(), pp.end() - 1);
+      for (int k = 0; k < (int)Bs.gidx.size(); k++) idx[(size_t)fill[(size_t)Bs.gidx[(size_t)k]]++] = k;
+      pull_ptr.upload(pp);
+      pull_idx.upload(idx);
+    }
+    dev.factor(Av.p, status.p, s);
+    int stv = 0;
+    CK(cudaMemcpyAsync(&stv, status.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    if (stv & ERR_NOT_SPD) throw CudaError{cudaSuccess, "robust coarse space: a support matrix is not positive definite"};
+    const std::vector<double> ones((size_t)n, 1.0);
+    CK(cudaMemcpy(r.p, ones.data(), (size_t)n * sizeof(double), cudaMemcpyHostToDevice));
+    CK(cudaMemset(x.p, 0, (size_t)n * sizeof(double)));
+    CK(cudaMemset(p.p, 0, (size_t)n * sizeof(double)));
+    const int lanes = lanes_for(A), grid = kRedBlocks;
+    const double init = (double)n;  // ||1||^2
+    double best = init;
+    int since_best = 0;
+    for (int it = 1; it <= 10000; it++) {
+      spmv_lanes(lanes, s, n, Ap.p, Ac.p, Av.p, r.p, z.p, part_rz.p);  // z = A r, r.z
+      cg_direction<<<grid, kVecThreads, 0, s>>>(n, z.p, p.p, part_rz.p, part_rz.p, sc.p, it == 1, 0);
+      gather_subdomains<double><<<grid, kVecThreads, 0, s>>>(p.p, dev.gidx.p, dev.xl.p, dev.xlen);
+      dev.solve(s);
+      pull_prolong_dot<double, double><<<grid, kVecThreads, 0, s>>>(
+          n, pull_ptr.p, pull_idx.p, dev.xl.p, nullptr, nullptr, nullptr, nullptr, 1, p.p, qv.p, nullptr,
+          part_pq.p, nullptr);  // q = B p, p.q
+      cg_update<<<grid, kVecThreads, 0, s>>>(n, p.p, qv.p, x.p, r.p, sc.p, part_pq.p, part_rr.p);
+      cg_finish<<<1, 32, 0, s>>>(sc.p, part_rr.p, 0, d_host_out, status.p, d_host_status);
+      CK(cudaGetLastError());
+      CK(cudaStreamSynchronize(s));
+      const double res = host_out[0];
+      if (!(res == res) || !(host_out[5] > 0.0))
+        throw CudaError{cudaSuccess, "robust coarse space: CG breakdown in B g = 1"};
+      if (res <= 1e-28 * init) break;
+      if (res < 0.25 * best) { best = res; since_best = 0; }
+      else if (++since_best >= 25) break;  // stagnated at rounding level
+    }
+    // q_i = A_i^-1 g(S_i), back in support order
+    gather_subdomains<double><<<grid, kVecThreads, 0, s>>>(x.p, dev.gidx.p, dev.xl.p, dev.xlen);
+    dev.solve(s);
+    std::vector<double> xl((size_t)dev.xlen);
+    CK(cudaMemcpyAsync(xl.data(), dev.xl.p, xl.size() * sizeof(double), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    q.assign(sn.size(), 0.0);
+    std::vector<int> posn((size_t)n, -1);
+    for (size_t i = 0; i + 1 < sp.size(); i++) {
+      for (int64_t k = sp[i]; k < sp[i + 1]; k++) posn[(size_t)sn[(size_t)k]] = (int)(k - sp[i]);
+      for (int64_t a = Bs.xoff[i]; a < Bs.xoff[i + 1]; a++)
+        q[(size_t)(sp[i] + posn[(size_t)Bs.gidx[(size_t)a]])] = xl[(size_t)a];
+      for (int64_t k = sp[i]; k < sp[i + 1]; k++) posn[(size_t)sn[(size_t)k]] = -1;
+    }
+    ok = true;
+  } catch (const CudaError &e) {
+    err = e.e == cudaSuccess ? std::string(e.what) : std::string("CUDA error in ") + e.what + ": " + cudaGetErrorString(e.e);
+  } catch (const std::exception &ex) {
+    err = std::string("robust coarse space: ") + ex.what();
+  }
+  if (s) cudaStreamDestroy(s);
+  if (host_out) cudaFreeHost(host_out);
+  if (host_status) cudaFreeHost(host_status);
+  return ok;
+}
+
 // host setup (aggregation, R, AC, subdomains; skipped with reuse_host when
 // it is current), symbolic analysis and device upload
 dg_status do_setup(dg_handle *h, bool reuse_host = false) {
@@ -724,9 +858,15 @@ dg_status do_setup(dg_handle *h, bool reuse_host = false) {
       if (!h->part.empty()) return fail(h, DG_BAD_INPUT, "a partition vector cannot be combined with batched systems");
       if (!build_setup_systems(c, h->sys_row, h->sys_tri, h->ii, h->jj, h->vv, h->S, err))
         return fail(h, DG_BAD_INPUT, err);
-    } else if (!build_setup(c, h->n, h->ii, h->jj, h->vv, h->part.empty() ? nullptr : &h->part, h->nparts, h->S,
-                            err)) {
-      return fail(h, DG_BAD_INPUT, err);
+    } else {
+      bool no_device = false;
+      const RobustHook hook = [&](const Csr &A, const std::vector<int64_t> &sp, const std::vector<int> &sn,
+                                  std::vector<double> &q, std::string &e) {
+        return robust_restriction_gpu(c, A, sp, sn, q, e, no_device);
+      };
+      if (!build_setup(c, h->n, h->ii, h->jj, h->vv, h->part.empty() ? nullptr : &h->part, h->nparts, h->S, err,
+                       &hook))
+        return fail(h, no_device ? DG_NO_DEVICE : DG_BAD_INPUT, err);
     }
   }
   MfTune tune;

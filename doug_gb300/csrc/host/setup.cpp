@@ -1167,7 +1167,7 @@ static Coo smoother(const Csr &A, const std::vector<char> &strong, double omega,
 
 bool build_setup(const Controls &c_in, int n, const std::vector<int> &ii, const std::vector<int> &jj,
                  const std::vector<double> &vv, const std::vector<int> *part, int nparts,
-                 SetupResult &out, std::string &err) {
+                 SetupResult &out, std::string &err, const RobustHook *robust) {
   Controls c = c_in;
   out = SetupResult();
   out.n = n;
@@ -1183,8 +1183,12 @@ bool build_setup(const Controls &c_in, int n, const std::vector<int> &ii, const 
           " restricts a residual the one-process reference never sets (pcg.F90:146-149)";
     return false;
   }
-  if (c.coarse_method > 1) {
-    err = "coarse_method " + std::to_string(c.coarse_method) + " is not the smoothed-aggregation path";
+  if (c.coarse_method > 2) {  // aggr.F90:155-165
+    err = "Wrong coarse method " + std::to_string(c.coarse_method);
+    return false;
+  }
+  if (c.coarse_method == 2 && !robust) {
+    err = "coarse_method 2 (robust coarse space) needs the device B-solve";
     return false;
   }
   size_t nnz = vv.size();
@@ -1251,6 +1255,28 @@ bool build_setup(const Controls &c_in, int n, const std::vector<int> &ii, const 
       else R = mul(Trows, cols_of(coo_of(SS)));  // 2 (and >8, performed as 2)
     }
     Rcoo = coo_of(R);
+  }
+  if (c.coarse_method == 2) {
+    // CoarsePreconditioner_robust_Init (CoarsePreconditioner_robust.F90:34-63): the
+    // supports are R's rows in R's entry order (CoarseProjectionMtxsBuild,
+    // RobustCoarseMtx.f90:85-103); the new R holds q_i on S_i, rows one after
+    // the other (RobustRestrictMtxBuild, :175-202)
+    const int na = Rcoo.nrows;
+    std::vector<int64_t> sp((size_t)na + 1, 0);
+    for (size_t k = 0; k < Rcoo.size(); k++) sp[(size_t)Rcoo.i[k] + 1]++;
+    for (int a = 0; a < na; a++) sp[(size_t)a + 1] += sp[(size_t)a];
+    std::vector<int> sn(Rcoo.size());
+    std::vector<int64_t> fp(sp.begin(), sp.end() - 1);
+    for (size_t k = 0; k < Rcoo.size(); k++) sn[(size_t)fp[(size_t)Rcoo.i[k]]++] = Rcoo.j[k];
+    std::vector<double> q;
+    if (!(*robust)(A, sp, sn, q, err)) return false;
+    Coo Rh;
+    Rh.nrows = na; Rh.ncols = Rcoo.ncols;
+    Rh.i.resize(sn.size()); Rh.j = sn; Rh.v = q;
+    for (int a = 0; a < na; a++)
+      for (int64_t k = sp[(size_t)a]; k < sp[(size_t)a + 1]; k++) Rh.i[(size_t)k] = a;
+    Rcoo = Rh;
+    tm.lap("robust coarse space");
   }
   // CoarseMtxBuild (CoarseMtx.F90:476-516): T = A R^T (R arranged by columns),
   // AC = R T with R's rows re-bucketed from that column order.

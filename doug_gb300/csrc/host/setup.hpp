@@ -7,6 +7,7 @@
 // it runs once per matrix, before the GPU solve.
 #pragma once
 #include <cstdint>
+#include <functional>
 #include <string>
 #include <vector>
 
@@ -130,13 +131,24 @@ struct SetupResult {
   std::vector<double> R_v, AC_v;
 };
 
+// Robust coarse space (coarse_method 2): given A and the supports S_i of the
+// coarse nodes (0-based node lists, support order), fill q (laid out as the
+// supports) with q_i = A_i^-1 g(S_i), A_i = A(S_i, S_i), where g solves
+// B g = 1 for B = sum_i R_i^T A_i^-1 R_i (RobustCoarseMtx.f90:53-210,
+// pcg_robust.f90:37-120).  The product computes it on the GPU.
+using RobustHook = std::function<bool(const Csr &A, const std::vector<int64_t> &supp_ptr,
+                                      const std::vector<int> &supp_nodes, std::vector<double> &q,
+                                      std::string &err)>;
+
 // Build everything from 1-based COO triplets (assembled semantics: header
 // swap and 0-based shift already applied by the caller).  part: optional
 // 1-based partition vector (length n) that replaces the coarse-aggregate
-// subdomains.  Returns false with err on a DOUG abort condition.
+// subdomains.  robust: the B-solve of coarse_method 2 (required for it).
+// Returns false with err on a DOUG abort condition.
 bool build_setup(const Controls &c_in, int n, const std::vector<int> &ii,
                  const std::vector<int> &jj, const std::vector<double> &vv,
-                 const std::vector<int> *part, int nparts, SetupResult &out, std::string &err);
+                 const std::vector<int> *part, int nparts, SetupResult &out, std::string &err,
+                 const RobustHook *robust = nullptr);
 
 // Batched independent systems: system k owns the rows [sys_row[k],
 // sys_row[k+1]) and the triplets [sys_tri[k], sys_tri[k+1]) of (ii, jj, vv),

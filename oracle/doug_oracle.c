@@ -1140,6 +1140,106 @@ static spm int_rest_build(const spm *A, const aggrs *ag, int smoothers) {
   return R;
 }
 
+/* Dense lower Cholesky in place (n x n, column-major, 0-based); 0 if not SPD. */
+static int dense_chol(int n, double *a) {
+  int i, j, k;
+  for (j = 0; j < n; j++) {
+    double d = a[(size_t)j * n + j];
+    for (k = 0; k < j; k++) d -= a[(size_t)k * n + j] * a[(size_t)k * n + j];
+    if (!(d > 0.0)) return 0;
+    d = sqrt(d);
+    a[(size_t)j * n + j] = d;
+    for (i = j + 1; i < n; i++) {
+      double v = a[(size_t)j * n + i];
+      for (k = 0; k < j; k++) v -= a[(size_t)k * n + i] * a[(size_t)k * n + j];
+      a[(size_t)j * n + i] = v / d;
+    }
+  }
+  return 1;
+}
+static void dense_chol_solve(int n, const double *l, double *x) {
+  int i, k;
+  for (i = 0; i < n; i++) {
+    double v = x[i];
+    for (k = 0; k < i; k++) v -= l[(size_t)k * n + i] * x[k];
+    x[i] = v / l[(size_t)i * n + i];
+  }
+  for (i = n - 1; i >= 0; i--) {
+    double v = x[i];
+    for (k = i + 1; k < n; k++) v -= l[(size_t)i * n + k] * x[k];
+    x[i] = v / l[(size_t)i * n + i];
+  }
+}
+
+/* Robust coarse space (coarse_method 2): CoarsePreconditioner_robust_Init
+ * (CoarsePreconditioner_robust.F90:34-63), CoarseProjectionMtxsBuild and
+ * RobustRestrictMtxBuild (RobustCoarseMtx.f90:53-210).  The support S_i of
+ * coarse node i is the column list of row i of the smoothed restriction R in
+ * R's entry order; A_i = A(S_i, S_i); g solves B g = 1 with
+ * B = sum_i R_i^T A_i^-1 R_i; row i of the new restriction holds
+ * q_i = A_i^-1 g(S_i) on S_i, rows one after the other.  The reference reaches
+ * g by preconditioned CG (pcg_forRCS, pcg_robust.f90:37-120, stopping on
+ * ||r||/||r0|| <= tol^2); here B is formed densely and factored, an exact
+ * solve for test-sized problems. */
+static spm robust_restriction(const spm *A, const spm *R) {
+  int n = A->nrows, nagr = R->nrows, k, i, j;
+  spm Ar = spm_copy(A);
+  spm_arrange(&Ar, ARR_ROWS, 0, 0, 0, 0);
+  int *cnt = (int *)xcalloc((size_t)nagr + 2, sizeof(int));
+  for (k = 1; k <= R->nnz; k++) cnt[R->indi[k]]++;
+  int *start = (int *)xcalloc((size_t)nagr + 2, sizeof(int));
+  for (i = 1; i <= nagr; i++) start[i + 1] = start[i] + cnt[i];
+  int *supp = (int *)xcalloc((size_t)R->nnz + 1, sizeof(int));
+  int *fill = (int *)xcalloc((size_t)nagr + 2, sizeof(int));
+  for (k = 1; k <= R->nnz; k++) { i = R->indi[k]; supp[start[i] + fill[i]++] = R->indj[k]; }
+  int *pos = (int *)xcalloc((size_t)n + 1, sizeof(int));
+  for (i = 1; i <= n; i++) pos[i] = -1;
+  double **Linv = (double **)xcalloc((size_t)nagr + 1, sizeof(double *));
+  double *B = (double *)xcalloc((size_t)n * n, sizeof(double));
+  for (i = 1; i <= nagr; i++) {
+    int m = cnt[i], a, b;
+    const int *S = supp + start[i];
+    for (a = 0; a < m; a++) pos[S[a]] = a;
+    double *Ai = (double *)xcalloc((size_t)m * m, sizeof(double));
+    for (a = 0; a < m; a++) {
+      int row = S[a];
+      for (k = Ar.mbound[row]; k < Ar.mbound[row + 1]; k++) {
+        int col = Ar.indj[k];
+        if (col <= n && pos[col] >= 0) Ai[(size_t)pos[col] * m + a] += Ar.val[k];
+      }
+    }
+    if (!dense_chol(m, Ai)) orc_abort("robust coarse space: a support matrix is not positive definite");
+    double *col = (double *)xcalloc((size_t)m, sizeof(double));
+    for (b = 0; b < m; b++) {  /* column b of A_i^-1 into B(S, S) */
+      for (a = 0; a < m; a++) col[a] = a == b ? 1.0 : 0.0;
+      dense_chol_solve(m, Ai, col);
+      for (a = 0; a < m; a++) B[(size_t)(S[b] - 1) * n + (S[a] - 1)] += col[a];
+    }
+    free(col);
+    Linv[i] = Ai;
+    for (a = 0; a < m; a++) pos[S[a]] = -1;
+  }
+  if (!dense_chol(n, B)) orc_abort("robust coarse space: B is not positive definite");
+  double *g = (double *)xcalloc((size_t)n, sizeof(double));
+  for (j = 0; j < n; j++) g[j] = 1.0;
+  dense_chol_solve(n, B, g);
+  spm Rh = spm_new(R->nnz, nagr, R->ncols);
+  int q = 0;
+  for (i = 1; i <= nagr; i++) {
+    int m = cnt[i], a;
+    const int *S = supp + start[i];
+    double *qi = (double *)xcalloc((size_t)m, sizeof(double));
+    for (a = 0; a < m; a++) qi[a] = g[S[a] - 1];
+    dense_chol_solve(m, Linv[i], qi);
+    for (a = 0; a < m; a++) { q++; Rh.indi[q] = i; Rh.indj[q] = S[a]; Rh.val[q] = qi[a]; }
+    free(qi);
+    free(Linv[i]);
+  }
+  free(Linv); free(B); free(g); free(pos); free(fill); free(supp); free(start); free(cnt);
+  spm_free(&Ar);
+  return Rh;
+}
+
 /* CoarseMtxBuild (CoarseMtx.F90:476-516), np=1: T=A*R^T, AC=R*T. It
  * re-arranges R by columns as a side effect, exactly as the reference. */
 static spm coarse_mtx_build(const spm *A, spm *R, int ninner) {
@@ -1506,9 +1606,14 @@ static void run_setup(state *s, const int *part, int nparts) {
   spm_aggregate(&s->A, &s->fine_inner, &s->fine_full, s->r1, s->min1, s->max1, s->strong1, 0);
   spm_unscale(&s->A);
   /* CoarsePreconditioner_smooth_Init (CoarsePreconditioner_smooth.F90:47-89) */
-  if (c->coarse_method > 1) orc_abort("coarse_method %d not supported", c->coarse_method);
+  if (c->coarse_method > 2) orc_abort("Wrong coarse method %d", c->coarse_method);
   if (c->smoothers > c->radius1) c->smoothers = c->radius1; /* CoarseMtx.F90:75-78 */
   s->R = int_rest_build(&s->A, &s->fine_inner, c->smoothers);
+  if (c->coarse_method == 2) { /* aggr.F90:158-160 */
+    spm Rh = robust_restriction(&s->A, &s->R);
+    spm_free(&s->R);
+    s->R = Rh;
+  }
   s->have_R = 1;
   s->AC = coarse_mtx_build(&s->A, &s->R, n);
   /* Partitionings_aggr_InitCoarse (Partitioning_aggr.F90:120-193) */
