@@ -40,6 +40,7 @@ EXPORTED_SYMBOLS = [
     "dg_get_subdomains", "dg_get_restriction", "dg_get_coarse_matrix", "dg_residual_csr",
     "dg_set_elements", "dg_get_input", "dg_grad_matrix", "dg_grad_elements",
     "dg_residual_csr_noalloc", "dg_autotune", "dg_set_systems", "dg_get_system_stats",
+    "dg_solve_multi", "dg_solve_multi_device",
 ]
 
 
@@ -115,6 +116,8 @@ def load_library(path: str | None = None):
     L.dg_set_systems.argtypes = [vp, C.c_int, P(C.c_int), P(C.c_longlong), P(C.c_int), P(C.c_int),
                                  P(C.c_double), P(C.c_double)]
     L.dg_get_system_stats.argtypes = [vp, P(C.c_int), P(C.c_int), P(C.c_double), P(C.c_double)]
+    L.dg_solve_multi.argtypes = [vp, C.c_int, P(C.c_double), P(C.c_double), P(_Stats)]
+    L.dg_solve_multi_device.argtypes = [vp, C.c_int, vp, vp, P(_Stats), vp]
     L.dg_set_elements.argtypes = [vp, C.c_int, C.c_int, P(C.c_int), P(C.c_int), P(C.c_double), P(C.c_double)]
     L.dg_get_input.argtypes = [vp, P(C.c_int), P(C.c_int), P(C.c_int), P(C.c_int), P(C.c_double),
                                P(C.c_double)]
@@ -266,8 +269,31 @@ class DougSolver:
                                            _ip(r), _ip(c), _dp(v), _dp(b) if b is not None else None))
         self._sys_n = ns
 
+    def solve_multi(self, B, allow_not_converged: bool = False):
+        """Solves A X = B for the columns of B (n x nrhs) together; returns
+        (X, stats).  Per right-hand side: system_stats()."""
+        B = np.asarray(B, dtype=np.float64)
+        n, k = B.shape
+        Bt = np.ascontiguousarray(B.T)            # right-hand sides one after the other
+        Xt = np.zeros_like(Bt)
+        st = _Stats()
+        rc = self._L.dg_solve_multi(self._h, k, _dp(Bt), _dp(Xt), C.byref(st))
+        self._check(rc, allow=(DG_NOT_CONVERGED,) if allow_not_converged else ())
+        self._sys_n = np.full(k, n, np.int32)
+        return Xt.T.copy(), self._stats(rc, st)
+
+    def solve_multi_device(self, nrhs: int, b_ptr: int, x_ptr: int, stream: int = 0, allow_not_converged=False):
+        """solve_multi with device pointers: nrhs vectors of n doubles one after the other."""
+        st = _Stats()
+        rc = self._L.dg_solve_multi_device(self._h, int(nrhs), C.c_void_p(b_ptr), C.c_void_p(x_ptr), C.byref(st),
+                                           C.c_void_p(stream))
+        self._check(rc, allow=(DG_NOT_CONVERGED,) if allow_not_converged else ())
+        self._sys_n = np.full(int(nrhs), self.sizes()["n"], np.int32)
+        return self._stats(rc, st)
+
     def system_stats(self) -> dict:
-        """Per-system results of the last batched solve (numpy arrays)."""
+        """Per-system results of the last batched solve, or per right-hand
+        side of the last solve_multi (numpy arrays)."""
         k = len(self._sys_n)
         it = np.zeros(k, np.int32)
         stt = np.zeros(k, np.int32)

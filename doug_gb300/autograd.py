@@ -1,8 +1,8 @@
 """Differentiable solves x = A^-1 b through the GB300 solver (torch.autograd).
 
-The forward pass solves A x = b with the library's preconditioned CG (one
-solve per right-hand side column; the numeric factors of the first solve are
-kept for the others and for the backward pass).  The backward pass is the
+The forward pass solves A x = b with the library's preconditioned CG (all
+right-hand side columns together, dg_solve_multi; the numeric factors are
+kept for the backward pass).  The backward pass is the
 adjoint: A is symmetric, so lambda = A^-1 dL/dx is one more solve with the
 same factors, and
 
@@ -29,12 +29,16 @@ def _as_cols(b: torch.Tensor) -> torch.Tensor:
 
 
 def _solve_cols(solver: DougSolver, B: torch.Tensor) -> torch.Tensor:
-    """Solves A X = B column by column on the current stream (B: n x r, FP64 CUDA)."""
+    """Solves A X = B on the current stream (B: n x r, FP64 CUDA): the r
+    right-hand sides together (one shared factorisation, every kernel over
+    all of them)."""
     stream = torch.cuda.current_stream().cuda_stream
     Bt = B.t().contiguous()                 # columns contiguous
     Xt = torch.empty_like(Bt)
-    for c in range(Bt.shape[0]):
-        solver.solve_device(Bt[c].data_ptr(), Xt[c].data_ptr(), stream)
+    if Bt.shape[0] == 1:
+        solver.solve_device(Bt[0].data_ptr(), Xt[0].data_ptr(), stream)
+    else:
+        solver.solve_multi_device(Bt.shape[0], Bt.data_ptr(), Xt.data_ptr(), stream)
     return Xt.t()
 
 

@@ -789,12 +789,19 @@ struct SmallBuckets {
   int nb0, nb1;           // CTAs of buckets 0 and 1
 };
 
+// Several right-hand sides (nrhs > 1): CTA x serves right-hand side x % nrhs
+// of the work unit x / nrhs, so the CTAs that read the same E are adjacent;
+// the vectors of right-hand side k start at k * xs (xl, yl) and k * us (u).
 template <typename T>
 __global__ void __launch_bounds__(256, SmallMinBlocks<T>::N)
 mf_fwd_small(MfView v, const int *__restrict__ fronts, SmallBuckets sb, const T *__restrict__ E,
-             const T *__restrict__ xl, T *__restrict__ yl, T *__restrict__ uvec) {
+             const T *__restrict__ xl, T *__restrict__ yl, T *__restrict__ uvec, int nrhs = 1, int64_t xs = 0,
+             int64_t us = 0) {
   __shared__ __align__(16) T wsh[8 * kSolveSmall];
-  const int b = blockIdx.x;
+  const int b = blockIdx.x / nrhs, rk = blockIdx.x % nrhs;
+  xl += rk * xs;
+  yl += rk * xs;
+  uvec += rk * us;
   if (b < sb.nb0) fwd_small_body<T, 8>(v, fronts, sb.cnt0, E, xl, yl, uvec, b, wsh);
   else if (b < sb.nb0 + sb.nb1)
     fwd_small_body<T, 16>(v, fronts + sb.cnt0, sb.cnt1, E, xl, yl, uvec, b - sb.nb0, wsh);
@@ -805,9 +812,11 @@ mf_fwd_small(MfView v, const int *__restrict__ fronts, SmallBuckets sb, const T 
 template <typename T>
 __global__ void __launch_bounds__(256, SmallMinBlocks<T>::N)
 mf_bwd_small(MfView v, const int *__restrict__ fronts, SmallBuckets sb, const T *__restrict__ E,
-             const T *__restrict__ yl, T *__restrict__ xl) {
+             const T *__restrict__ yl, T *__restrict__ xl, int nrhs = 1, int64_t xs = 0) {
   __shared__ __align__(16) T wsh[8 * kSolveSmall];
-  const int b = blockIdx.x;
+  const int b = blockIdx.x / nrhs, rk = blockIdx.x % nrhs;
+  yl += rk * xs;
+  xl += rk * xs;
   if (b < sb.nb0) bwd_small_body<T, 8>(v, fronts, sb.cnt0, E, yl, xl, b, wsh);
   else if (b < sb.nb0 + sb.nb1)
     bwd_small_body<T, 16>(v, fronts + sb.cnt0, sb.cnt1, E, yl, xl, b - sb.nb0, wsh);
@@ -827,13 +836,17 @@ template <typename T> struct FwdRows { static constexpr int N = 32 * Vec16<T>::N
 template <typename T, int NT>
 __global__ void __launch_bounds__(NT, NT == kELeanThreads ? 12 : 4)
 mf_fwd_big(MfView v, const int2 *__restrict__ tasks, const T *__restrict__ E, const T *__restrict__ xl,
-           T *__restrict__ yl, T *__restrict__ uvec) {
+           T *__restrict__ yl, T *__restrict__ uvec, int nrhs = 1, int64_t xs = 0, int64_t us = 0) {
   constexpr int VN = Vec16<T>::N, RC = FwdRows<T>::N, NW = NT / 32, UN = NT == kELeanThreads ? 4 : kEUnroll;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T *b = reinterpret_cast<T *>(smem_raw);  // b[0, m)
   __shared__ T red[NW][RC];
-  const int f = tasks[blockIdx.x].x;
-  const int ch0 = tasks[blockIdx.x].y >> 16, nch = tasks[blockIdx.x].y & 0xffff;
+  const int task = blockIdx.x / nrhs, rk = blockIdx.x % nrhs;
+  xl += rk * xs;
+  yl += rk * xs;
+  uvec += rk * us;
+  const int f = tasks[task].x;
+  const int ch0 = tasks[task].y >> 16, nch = tasks[task].y & 0xffff;
   const int m = v.f_m[f], k = v.f_k[f], ld = round4(m);
   const int64_t xo = v.f_xoff[f] + v.f_p0[f];
   const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
@@ -902,11 +915,14 @@ mf_fwd_big(MfView v, const int2 *__restrict__ tasks, const T *__restrict__ E, co
 template <typename T, int NT>
 __global__ void __launch_bounds__(NT, NT == kELeanThreads ? 12 : 4)
 mf_bwd_big(MfView v, const int2 *__restrict__ tasks, const T *__restrict__ E, const T *__restrict__ yl,
-           T *__restrict__ xl) {
+           T *__restrict__ xl, int nrhs = 1, int64_t xs = 0) {
   constexpr int VN = Vec16<T>::N, LPC = 32 / VN, NCS = NT / LPC, UN = NT == kELeanThreads ? 4 : kEUnroll;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T *w = reinterpret_cast<T *>(smem_raw);  // v[32J, ld)
-  const int f = tasks[blockIdx.x].x, J = tasks[blockIdx.x].y;
+  const int task = blockIdx.x / nrhs, rk = blockIdx.x % nrhs;
+  yl += rk * xs;
+  xl += rk * xs;
+  const int f = tasks[task].x, J = tasks[task].y;
   const int m = v.f_m[f], k = v.f_k[f], ld = round4(m);
   const int c0 = 32 * J, jb = min(32, k - c0);
   const int64_t xo = v.f_xoff[f] + v.f_p0[f];
@@ -1134,26 +1150,33 @@ elem_pull_pq(int n, const int64_t *__restrict__ rptr, const int *__restrict__ ri
 // ---------------------------------------------------------------------------
 // Schwarz gather / pull sum and coarse transfer
 // ---------------------------------------------------------------------------
+// nrhs right-hand sides: vector k at r + k * rs, local vector k at xl + k * len
 template <typename T>
 __global__ void gather_subdomains(const double *__restrict__ r, const int *__restrict__ gidx,
-                                  T *__restrict__ xl, int64_t len) {
+                                  T *__restrict__ xl, int64_t len, int nrhs = 1, int64_t rs = 0) {
   for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < len;
-       p += (int64_t)gridDim.x * blockDim.x)
-    xl[p] = (T)r[gidx[p]];
+       p += (int64_t)gridDim.x * blockDim.x) {
+    const int g = gidx[p];
+    for (int k = 0; k < nrhs; k++) xl[k * len + p] = (T)r[k * rs + g];
+  }
 }
 
 // crhs (in the coarse batch's local numbering) = R r
+// nrhs right-hand sides: r_k at r + k * rs, the coarse vector k at xc + k * xcs
 template <typename TR>
 __global__ void restrict_to_coarse(const int64_t *__restrict__ Rp, const int *__restrict__ Rc,
                                    const TR *__restrict__ Rv, const double *__restrict__ r,
-                                   const int *__restrict__ cpos, double *__restrict__ xc, int nc) {
+                                   const int *__restrict__ cpos, double *__restrict__ xc, int nc, int nrhs = 1,
+                                   int64_t rs = 0, int64_t xcs = 0) {
   const int lane = threadIdx.x & 31;
   const int warps = (gridDim.x * blockDim.x) >> 5;
   for (int a = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; a < nc; a += warps) {
-    double s = 0.0;
-    for (int64_t e = Rp[a] + lane; e < Rp[a + 1]; e += 32) s += (double)Rv[e] * r[Rc[e]];
-    s = warp_sum(s);
-    if (lane == 0) xc[cpos[a]] = s;
+    for (int k = 0; k < nrhs; k++) {
+      double s = 0.0;
+      for (int64_t e = Rp[a] + lane; e < Rp[a + 1]; e += 32) s += (double)Rv[e] * r[k * rs + Rc[e]];
+      s = warp_sum(s);
+      if (lane == 0) xc[k * xcs + cpos[a]] = s;
+    }
   }
 }
 
@@ -1170,24 +1193,34 @@ pull_prolong_dot(int n, const int *__restrict__ pull_ptr, const int *__restrict_
                  const TP *__restrict__ Pv, const double *__restrict__ xc,
                  int mode, const double *__restrict__ r, double *__restrict__ z,
                  double *__restrict__ zold, double *__restrict__ part_rz, double *__restrict__ part_rzo,
-                 const int *__restrict__ cb = nullptr) {
+                 const int *__restrict__ cb = nullptr, const int *__restrict__ csys = nullptr,
+                 int64_t vs = 0, int64_t xls = 0, int64_t xcs = 0) {
   // mode bit 0: fine subdomains on; bit 1: coarse on; bit 2: identity fine (z=r);
-  // bit 3: keep z_old and produce r.z_old.  cb (batched systems): CTA b owns
-  // the rows [cb[b], cb[b+1]) and its partial sums are that chunk's.
+  // bit 3: keep z_old and produce r.z_old.  cb (batched systems / right-hand
+  // sides): CTA b owns the positions [cb[b], cb[b+1]) of the stacked vectors
+  // and its partial sums are that chunk's; with csys, the chunk belongs to
+  // right-hand side k = csys[b]: rows g - k*vs of the matrix and the local
+  // vectors at k*xls (subdomains) and k*xcs (coarse).
   __shared__ double sh[32];
   double srz = 0.0, srzo = 0.0;
   const int g0 = cb ? cb[blockIdx.x] + threadIdx.x : blockIdx.x * kVecThreads + threadIdx.x;
   const int gend = cb ? cb[blockIdx.x + 1] : n;
   const int gstep = cb ? kVecThreads : gridDim.x * kVecThreads;
+  const int64_t rk = csys ? csys[blockIdx.x] : 0;
+  const int64_t voff = rk * vs;
+  if (xl) xl += rk * xls;
+  if (xc) xc += rk * xcs;
   const bool pull = (mode & 5) == 1, prol = (mode & 2) != 0, flex = (mode & 8) != 0;
-  for (int g = g0; g < gend; g += gstep) {
+  for (int gg = g0; gg < gend; gg += gstep) {
+    const int64_t g = gg;              // position in the stacked vectors
+    const int gl = (int)(g - voff);    // row of the matrix / pull lists
     // round 1
     const double rg = r[g];
     const double zo = flex ? zold[g] : 0.0;
     int q0 = 0, q1 = 0;
     int64_t e0 = 0, e1 = 0;
-    if (pull) { q0 = pull_ptr[g]; q1 = pull_ptr[g + 1]; }
-    if (prol) { e0 = Pp[g]; e1 = Pp[g + 1]; }
+    if (pull) { q0 = pull_ptr[gl]; q1 = pull_ptr[gl + 1]; }
+    if (prol) { e0 = Pp[gl]; e1 = Pp[gl + 1]; }
     // round 2
     const int i0 = q0 < q1 ? pull_idx[q0] : -1;
     const int i1 = q0 + 1 < q1 ? pull_idx[q0 + 1] : -1;
@@ -1423,8 +1456,11 @@ template <int LANES>
 __global__ void __launch_bounds__(kVecThreads)
 bt_spmv_pq(const int *__restrict__ cb, const int *__restrict__ csys, const int *__restrict__ state,
            const int64_t *__restrict__ Ap, const int *__restrict__ Ac, const double *__restrict__ Av,
-           const double *__restrict__ p, double *__restrict__ q, double *__restrict__ part_pq) {
+           const double *__restrict__ p, double *__restrict__ q, double *__restrict__ part_pq, int64_t vs = 0) {
+  // vs > 0 (right-hand sides of one matrix): position g of vector k is row g - k*vs
   __shared__ double sh[32];
+  const int64_t voff = (int64_t)csys[blockIdx.x] * vs;
+  const double *pc = p + voff;  // pc[c]: column c of this right-hand side
   if (state[csys[blockIdx.x]] != BT_ACTIVE) {
     if (threadIdx.x == 0) part_pq[blockIdx.x] = 0.0;
     return;
@@ -1437,18 +1473,18 @@ bt_spmv_pq(const int *__restrict__ cb, const int *__restrict__ csys, const int *
     const int i = row0 + threadIdx.x / LANES;
     double s = 0.0;
     if (i < i1) {
-      int64_t e = Ap[i] + sub;
-      const int64_t e1 = Ap[i + 1];
+      int64_t e = Ap[i - voff] + sub;
+      const int64_t e1 = Ap[i - voff + 1];
       for (; e + 3 * LANES < e1; e += 4 * LANES) {
         const int c0 = Ac[e], c1 = Ac[e + LANES], c2 = Ac[e + 2 * LANES], c3 = Ac[e + 3 * LANES];
         const double a0 = Av[e], a1 = Av[e + LANES], a2 = Av[e + 2 * LANES], a3 = Av[e + 3 * LANES];
-        const double p0 = p[c0], p1 = p[c1], p2 = p[c2], p3 = p[c3];
+        const double p0 = pc[c0], p1 = pc[c1], p2 = pc[c2], p3 = pc[c3];
         s = __fma_rn(a0, p0, s);
         s = __fma_rn(a1, p1, s);
         s = __fma_rn(a2, p2, s);
         s = __fma_rn(a3, p3, s);
       }
-      for (; e < e1; e += LANES) s = __fma_rn(Av[e], p[Ac[e]], s);
+      for (; e < e1; e += LANES) s = __fma_rn(Av[e], pc[Ac[e]], s);
     }
 #pragma unroll
     for (int o = LANES / 2; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o, LANES);
@@ -1491,8 +1527,10 @@ __global__ void __launch_bounds__(kVecThreads)
 bt_residual(const int *__restrict__ cb, const int *__restrict__ csys, const int *__restrict__ state, int want,
             const int64_t *__restrict__ Ap, const int *__restrict__ Ac, const double *__restrict__ Av,
             const double *__restrict__ x, const double *__restrict__ b, double *__restrict__ r,
-            double *__restrict__ part_rr) {
+            double *__restrict__ part_rr, int64_t vs = 0) {
   __shared__ double sh[32];
+  const int64_t voff = (int64_t)csys[blockIdx.x] * vs;
+  const double *xc = x + voff;  // xc[c]: column c of this right-hand side
   if (want >= 0 && state[csys[blockIdx.x]] != want) {
     if (threadIdx.x == 0) part_rr[blockIdx.x] = 0.0;
     return;
@@ -1505,7 +1543,7 @@ bt_residual(const int *__restrict__ cb, const int *__restrict__ csys, const int 
     const int i = row0 + threadIdx.x / LANES;
     double s = 0.0;
     if (i < i1)
-      for (int64_t e = Ap[i] + sub; e < Ap[i + 1]; e += LANES) s = __fma_rn(Av[e], x[Ac[e]], s);
+      for (int64_t e = Ap[i - voff] + sub; e < Ap[i - voff + 1]; e += LANES) s = __fma_rn(Av[e], xc[Ac[e]], s);
 #pragma unroll
     for (int o = LANES / 2; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o, LANES);
     if (i < i1 && sub == 0) {

@@ -140,6 +140,8 @@ struct MfDevice {
     xl.alloc((size_t)B.xlen);
     yl.alloc((size_t)B.xlen);
     u.alloc((size_t)std::max<int64_t>(B.ulen, 1));
+    ulen = B.ulen;
+    mk = 0;
     view = MfView{f_off.p, f_m.p, f_k.p, f_rows.p, f_xoff.p, f_p0.p, f_uoff.p, f_woff.p,
                   f_child_ptr.p, f_children.p, f_relmap.p, f_asm.p, rows.p, relmap.p,
                   asm_tgt.p, asm_sp.p, asm_src.p, e_off.p};
@@ -362,22 +364,38 @@ struct MfDevice {
     return launches;
   }
 
+  // several right-hand sides: local vectors k at k*xlen (xlm, ylm) and k*ulen (um)
+  DBuf<T> xlm, ylm, um;
+  int mk = 0;
+  int64_t ulen = 0;
+  void ensure_multi(int K) {
+    if (mk == K) return;
+    xlm.alloc((size_t)xlen * K);
+    ylm.alloc((size_t)xlen * K);
+    um.alloc((size_t)std::max<int64_t>(ulen, 1) * K);
+    mk = K;
+  }
+
   // forward + backward solve: right-hand side in xl, solution back in xl
-  int solve(cudaStream_t s) {
+  // (nrhs > 1: the nrhs right-hand sides in xlm, solutions back in xlm)
+  int solve(cudaStream_t s, int nrhs = 1) {
     int launches = 0;
+    T *xl_ = nrhs > 1 ? xlm.p : xl.p, *yl_ = nrhs > 1 ? ylm.p : yl.p, *u_ = nrhs > 1 ? um.p : u.p;
+    const int64_t xs = nrhs > 1 ? xlen : 0, us = nrhs > 1 ? std::max<int64_t>(ulen, 1) : 0;
     for (int l = 0; l < nlevels; l++) {
       const SolveLevel &L = slevels[(size_t)l];
       if (L.small_cta) {
-        mf_fwd_small<T><<<L.small_cta, 256, 0, s>>>(view, solve_small.p + L.small_off, L.sb, E.p, xl.p, yl.p, u.p);
+        mf_fwd_small<T><<<L.small_cta * nrhs, 256, 0, s>>>(view, solve_small.p + L.small_off, L.sb, E.p, xl_, yl_,
+                                                           u_, nrhs, xs, us);
         launches++;
       }
       if (L.fwd_cnt) {
         if (L.fwd_lean)
-          mf_fwd_big<T, kELeanThreads><<<L.fwd_cnt, kELeanThreads, L.fwd_smem, s>>>(view, fwd_tasks.p + L.fwd_off,
-                                                                                  E.p, xl.p, yl.p, u.p);
+          mf_fwd_big<T, kELeanThreads><<<L.fwd_cnt * nrhs, kELeanThreads, L.fwd_smem, s>>>(
+              view, fwd_tasks.p + L.fwd_off, E.p, xl_, yl_, u_, nrhs, xs, us);
         else
-          mf_fwd_big<T, kEThreads><<<L.fwd_cnt, kEThreads, L.fwd_smem, s>>>(view, fwd_tasks.p + L.fwd_off, E.p,
-                                                                          xl.p, yl.p, u.p);
+          mf_fwd_big<T, kEThreads><<<L.fwd_cnt * nrhs, kEThreads, L.fwd_smem, s>>>(
+              view, fwd_tasks.p + L.fwd_off, E.p, xl_, yl_, u_, nrhs, xs, us);
         launches++;
       }
     }
@@ -385,15 +403,16 @@ struct MfDevice {
       const SolveLevel &L = slevels[(size_t)l];
       if (L.bwd_cnt) {
         if (L.bwd_lean)
-          mf_bwd_big<T, kELeanThreads><<<L.bwd_cnt, kELeanThreads, L.bwd_smem, s>>>(view, bwd_tasks.p + L.bwd_off,
-                                                                                  E.p, yl.p, xl.p);
+          mf_bwd_big<T, kELeanThreads><<<L.bwd_cnt * nrhs, kELeanThreads, L.bwd_smem, s>>>(
+              view, bwd_tasks.p + L.bwd_off, E.p, yl_, xl_, nrhs, xs);
         else
-          mf_bwd_big<T, kEThreads><<<L.bwd_cnt, kEThreads, L.bwd_smem, s>>>(view, bwd_tasks.p + L.bwd_off, E.p,
-                                                                          yl.p, xl.p);
+          mf_bwd_big<T, kEThreads><<<L.bwd_cnt * nrhs, kEThreads, L.bwd_smem, s>>>(
+              view, bwd_tasks.p + L.bwd_off, E.p, yl_, xl_, nrhs, xs);
         launches++;
       }
       if (L.small_cta) {
-        mf_bwd_small<T><<<L.small_cta, 256, 0, s>>>(view, solve_small.p + L.small_off, L.sb, E.p, yl.p, xl.p);
+        mf_bwd_small<T><<<L.small_cta * nrhs, 256, 0, s>>>(view, solve_small.p + L.small_off, L.sb, E.p, yl_, xl_,
+                                                           nrhs, xs);
         launches++;
       }
     }
@@ -496,6 +515,60 @@ struct SgsDevice {
   }
 };
 
+// Per-system PCG state of stacked vectors: the systems of a batch
+// (dg_set_systems, vs = 0) or several right-hand sides of one matrix
+// (dg_solve_multi, vector k at k*vs).  Chunks of at most kBatchChunk
+// positions, none across two systems; one partial sum per chunk.
+struct BatchCtx {
+  int nsys = 0, nchunks = 0;
+  int64_t vs = 0;
+  DBuf<int> cb, csys, sys_cptr, state, iters, dit;
+  DBuf<double> bsc, part_rz, part_rzo, part_pq, part_rr;
+  int *host_counts = nullptr, *d_host_counts = nullptr;  // mapped pinned
+  cudaGraphExec_t exec = nullptr;
+  int exec_nodes = 0;
+  BatchCtx() = default;
+  BatchCtx(const BatchCtx &) = delete;
+  BatchCtx &operator=(const BatchCtx &) = delete;
+  ~BatchCtx() {
+    if (exec) cudaGraphExecDestroy(exec);
+    if (host_counts) cudaFreeHost(host_counts);
+  }
+  // row[k] .. row[k+1]: the positions of system k in the stacked vectors
+  void build(const std::vector<int64_t> &row, int64_t vstride) {
+    if (exec) { cudaGraphExecDestroy(exec); exec = nullptr; }
+    nsys = (int)row.size() - 1;
+    vs = vstride;
+    std::vector<int> hb(1, 0), hs, hp(1, 0);
+    for (int k = 0; k < nsys; k++) {
+      for (int64_t r = row[(size_t)k]; r < row[(size_t)k + 1]; r += kBatchChunk) {
+        hb.push_back((int)std::min<int64_t>(r + kBatchChunk, row[(size_t)k + 1]));
+        hs.push_back(k);
+      }
+      hp.push_back((int)hs.size());
+    }
+    nchunks = (int)hs.size();
+    cb.upload(hb); csys.upload(hs); sys_cptr.upload(hp);
+    state.alloc((size_t)nsys); iters.alloc((size_t)nsys); dit.alloc(1);
+    bsc.alloc((size_t)nsys * BS_N);
+    CK(cudaMemset(state.p, 0, (size_t)nsys * sizeof(int)));
+    CK(cudaMemset(bsc.p, 0, (size_t)nsys * BS_N * sizeof(double)));
+    for (auto *v : {&part_rz, &part_rzo, &part_pq, &part_rr}) {
+      v->alloc((size_t)nchunks);
+      CK(cudaMemset(v->p, 0, (size_t)nchunks * sizeof(double)));
+    }
+    if (!host_counts) {
+      CK(cudaHostAlloc(&host_counts, 4 * sizeof(int), cudaHostAllocMapped));
+      CK(cudaHostGetDevicePointer(&d_host_counts, host_counts, 0));
+    }
+  }
+};
+
+// the PCG vectors of one stacked solve
+struct Vecs {
+  double *b, *x, *r, *p, *q, *z, *zold;
+};
+
 struct dg_handle {
   Controls ctl;
   std::string ctl_text;           // words given through dg_set_option (applied first)
@@ -528,10 +601,12 @@ struct dg_handle {
   // [sys_row[k], sys_row[k+1]) and the triplets [sys_tri[k], sys_tri[k+1])
   int nsys = 0;
   std::vector<int64_t> sys_row, sys_tri;
-  int nchunks = 0;                // row chunks of the batched vector kernels
-  DBuf<int> d_cb, d_csys, d_sys_cptr, d_state, d_iters, d_dit;
-  DBuf<double> bsc;               // per-system CG scalars
-  int *host_counts = nullptr, *d_host_counts = nullptr;  // mapped pinned
+  BatchCtx bt;                    // the systems of a batch
+  // several right-hand sides of one matrix (dg_solve_multi): mr_k right-hand
+  // sides, stacked vectors
+  BatchCtx mr;
+  int mr_k = 0;
+  DBuf<double> mb, mx, mrr, mp, mq, mz, mzold;
   std::vector<int> sys_iters, sys_state;
   std::vector<double> sys_relres, sys_seconds;
   SetupResult S;
@@ -572,7 +647,6 @@ struct dg_handle {
     if (join_ev) cudaEventDestroy(join_ev);
     if (host_out) cudaFreeHost(host_out);
     if (host_status) cudaFreeHost(host_status);
-    if (host_counts) cudaFreeHost(host_counts);
     for (auto &e : ev) if (e) cudaEventDestroy(e);
   }
 };
@@ -685,30 +759,31 @@ void resid_any(int lanes, int grid, cudaStream_t s, dg_handle *h, const double *
   }
 }
 
-// batched systems: the chunked product and residual
+// stacked systems / right-hand sides: the chunked product and residual
 template <int L>
-void launch_bt(cudaStream_t s, dg_handle *h, int resid, int want, double *rr) {
+void launch_bt(cudaStream_t s, dg_handle *h, BatchCtx &c, const Vecs &v, int resid, int want, double *rr) {
   if (resid)
-    bt_residual<L><<<h->nchunks, kVecThreads, 0, s>>>(h->d_cb.p, h->d_csys.p, h->d_state.p, want, h->Ap.p, h->Ac.p,
-                                                      h->Av.p, h->x.p, h->b.p, rr, h->part_rr.p);
+    bt_residual<L><<<c.nchunks, kVecThreads, 0, s>>>(c.cb.p, c.csys.p, c.state.p, want, h->Ap.p, h->Ac.p, h->Av.p,
+                                                     v.x, v.b, rr, c.part_rr.p, c.vs);
   else
-    bt_spmv_pq<L><<<h->nchunks, kVecThreads, 0, s>>>(h->d_cb.p, h->d_csys.p, h->d_state.p, h->Ap.p, h->Ac.p, h->Av.p,
-                                                     h->p.p, h->q.p, h->part_pq.p);
+    bt_spmv_pq<L><<<c.nchunks, kVecThreads, 0, s>>>(c.cb.p, c.csys.p, c.state.p, h->Ap.p, h->Ac.p, h->Av.p, v.p, v.q,
+                                                    c.part_pq.p, c.vs);
 }
-void bt_any(cudaStream_t s, dg_handle *h, int resid, int want = -1, double *rr = nullptr) {
+void bt_any(cudaStream_t s, dg_handle *h, BatchCtx &c, const Vecs &v, int resid, int want = -1,
+            double *rr = nullptr) {
   switch (h->lanes) {
-    case 1: launch_bt<1>(s, h, resid, want, rr); break;
-    case 2: launch_bt<2>(s, h, resid, want, rr); break;
-    case 4: launch_bt<4>(s, h, resid, want, rr); break;
-    case 8: launch_bt<8>(s, h, resid, want, rr); break;
-    case 16: launch_bt<16>(s, h, resid, want, rr); break;
-    default: launch_bt<32>(s, h, resid, want, rr); break;
+    case 1: launch_bt<1>(s, h, c, v, resid, want, rr); break;
+    case 2: launch_bt<2>(s, h, c, v, resid, want, rr); break;
+    case 4: launch_bt<4>(s, h, c, v, resid, want, rr); break;
+    case 8: launch_bt<8>(s, h, c, v, resid, want, rr); break;
+    case 16: launch_bt<16>(s, h, c, v, resid, want, rr); break;
+    default: launch_bt<32>(s, h, c, v, resid, want, rr); break;
   }
 }
-void bt_step(dg_handle *h, cudaStream_t s, int step, int first, int mixed, double tol2, const double *pa,
+void bt_step(BatchCtx &c, cudaStream_t s, int step, int first, int mixed, double tol2, const double *pa,
              const double *pb) {
-  bt_scalars<<<1, 1024, 0, s>>>(h->nsys, h->d_sys_cptr.p, step, first, mixed, mixed, tol2, pa, pb, h->bsc.p,
-                                h->d_state.p, h->d_iters.p, h->d_dit.p, h->d_host_counts);
+  bt_scalars<<<1, 1024, 0, s>>>(c.nsys, c.sys_cptr.p, step, first, mixed, mixed, tol2, pa, pb, c.bsc.p, c.state.p,
+                                c.iters.p, c.dit.p, c.d_host_counts);
 }
 
 // q = A r with L lanes per row and the r.q partials (any CSR on the device)
@@ -973,31 +1048,12 @@ dg_status do_setup(dg_handle *h, bool reuse_host = false) {
     h->Ap.upload(S.A.ptr); h->Ac.upload(S.A.col); h->Av.upload(S.A.val);
     h->lanes = lanes_for(S.A);
     for (auto *v : {&h->b, &h->x, &h->r, &h->p, &h->q, &h->z, &h->zold, &h->hb, &h->hx}) v->alloc((size_t)n);
-    h->nchunks = 0;
-    if (h->nsys > 0) {  // chunks of at most kBatchChunk rows, none across two systems
-      std::vector<int> cb(1, 0), csys, cptr(1, 0);
-      for (int k = 0; k < h->nsys; k++) {
-        for (int64_t r = h->sys_row[(size_t)k]; r < h->sys_row[(size_t)k + 1]; r += kBatchChunk) {
-          cb.push_back((int)std::min<int64_t>(r + kBatchChunk, h->sys_row[(size_t)k + 1]));
-          csys.push_back(k);
-        }
-        cptr.push_back((int)csys.size());
-      }
-      h->nchunks = (int)csys.size();
-      h->d_cb.upload(cb); h->d_csys.upload(csys); h->d_sys_cptr.upload(cptr);
-      h->d_state.alloc((size_t)h->nsys); h->d_iters.alloc((size_t)h->nsys); h->d_dit.alloc(1);
-      h->bsc.alloc((size_t)h->nsys * BS_N);
-      CK(cudaMemset(h->d_state.p, 0, (size_t)h->nsys * sizeof(int)));
-      CK(cudaMemset(h->bsc.p, 0, (size_t)h->nsys * BS_N * sizeof(double)));
-      if (!h->host_counts) {
-        CK(cudaHostAlloc(&h->host_counts, 4 * sizeof(int), cudaHostAllocMapped));
-        CK(cudaHostGetDevicePointer(&h->d_host_counts, h->host_counts, 0));
-      }
-    }
-    const size_t nparts_sum = std::max<size_t>(kRedBlocks, (size_t)h->nchunks);
+    if (h->nsys > 0) h->bt.build(h->sys_row, 0);
+    h->mr_k = 0;  // the right-hand-side stacks are rebuilt on demand
+    if (h->mr.exec) { cudaGraphExecDestroy(h->mr.exec); h->mr.exec = nullptr; }
     for (auto *v : {&h->part_rz, &h->part_rzo, &h->part_pq, &h->part_rr}) {
-      v->alloc(nparts_sum);
-      CK(cudaMemset(v->p, 0, nparts_sum * sizeof(double)));
+      v->alloc(kRedBlocks);
+      CK(cudaMemset(v->p, 0, kRedBlocks * sizeof(double)));
     }
     h->sc.alloc(8);
     CK(cudaMemset(h->sc.p, 0, 8 * sizeof(double)));
@@ -1128,67 +1184,99 @@ int factor_all(dg_handle *h, const SolvePlan &pl, cudaStream_t s) {
 // stream beside the subdomain solves, then the pull sum with the
 // prolongation.  pg: grid of the pull kernel; cb: the chunk table of batched
 // systems (one chunk per CTA) or null.  Returns the number of kernels.
-int precondition(dg_handle *h, const SolvePlan &pl, cudaStream_t st, bool profile, int pg, const int *cb) {
+// The stacked vectors and partial sums of one solve: the handle's own
+// vectors for a single system; ctx's for stacked systems / right-hand sides.
+struct StackArgs {
+  Vecs v;
+  double *part_rz, *part_rzo;
+  int pg;                  // grid of the pull kernel
+  const int *cb = nullptr, *csys = nullptr;
+  int nrhs = 1;            // > 1: right-hand sides of one matrix
+};
+
+int precondition(dg_handle *h, const SolvePlan &pl, cudaStream_t st, bool profile, const StackArgs &a) {
   const int grid = kRedBlocks;
-  const int n = h->n;
+  const int n = h->n, K = a.nrhs;
+  const int64_t vs = K > 1 ? n : 0;
   int nl = 0;
+  MfDevice<double> *co = h->co64.get();
+  double *xc_buf = nullptr;
   if (pl.coarse) {  // restriction + coarse solve on the second stream
+    xc_buf = K > 1 ? co->xlm.p : co->xl.p;
+    const int64_t xcs = K > 1 ? co->xlen : 0;
     CK(cudaEventRecord(h->fork_ev, st));
     CK(cudaStreamWaitEvent(h->s2, h->fork_ev, 0));
     if (profile) CK(cudaEventRecord(h->ev[4], h->s2));
     if (pl.mixed)
-      restrict_to_coarse<float><<<grid, kVecThreads, 0, h->s2>>>(h->Rp.p, h->Rc.p, h->Rvf.p, h->r.p, h->cpos.p, h->co64->xl.p, h->S.R.nrows);
+      restrict_to_coarse<float><<<grid, kVecThreads, 0, h->s2>>>(h->Rp.p, h->Rc.p, h->Rvf.p, a.v.r, h->cpos.p, xc_buf,
+                                                                  h->S.R.nrows, K, vs, xcs);
     else
-      restrict_to_coarse<double><<<grid, kVecThreads, 0, h->s2>>>(h->Rp.p, h->Rc.p, h->Rv.p, h->r.p, h->cpos.p, h->co64->xl.p, h->S.R.nrows);
-    nl += 1 + h->co64->solve(h->s2);
+      restrict_to_coarse<double><<<grid, kVecThreads, 0, h->s2>>>(h->Rp.p, h->Rc.p, h->Rv.p, a.v.r, h->cpos.p, xc_buf,
+                                                                   h->S.R.nrows, K, vs, xcs);
+    nl += 1 + co->solve(h->s2, K);
     if (profile) CK(cudaEventRecord(h->ev[5], h->s2));
     CK(cudaEventRecord(h->join_ev, h->s2));
   }
   if (profile) CK(cudaEventRecord(h->ev[3], st));
+  const void *xl_fine = nullptr;
+  int64_t xls = 0;
   if (pl.fine && pl.sgs) {
-    sgs_subdomains<<<h->sgs->nsd, kSgsThreads, 0, st>>>(h->sgs->view, h->sgs->sd_ptr.p, pl.sgs_iters, h->r.p,
+    sgs_subdomains<<<h->sgs->nsd, kSgsThreads, 0, st>>>(h->sgs->view, h->sgs->sd_ptr.p, pl.sgs_iters, a.v.r,
                                                          h->sgs->x.p);
+    xl_fine = h->sgs->x.p;
     nl++;
   } else if (pl.fine) {
     if (pl.mixed) {
-      gather_subdomains<float><<<grid, kVecThreads, 0, st>>>(h->r.p, h->sub32->gidx.p, h->sub32->xl.p, h->sub32->xlen);
-      nl += 1 + h->sub32->solve(st);
+      MfDevice<float> *d = h->sub32.get();
+      float *xl = K > 1 ? d->xlm.p : d->xl.p;
+      gather_subdomains<float><<<grid, kVecThreads, 0, st>>>(a.v.r, d->gidx.p, xl, d->xlen, K, vs);
+      nl += 1 + d->solve(st, K);
+      xl_fine = xl;
+      xls = K > 1 ? d->xlen : 0;
     } else {
-      gather_subdomains<double><<<grid, kVecThreads, 0, st>>>(h->r.p, h->sub64->gidx.p, h->sub64->xl.p, h->sub64->xlen);
-      nl += 1 + h->sub64->solve(st);
+      MfDevice<double> *d = h->sub64.get();
+      double *xl = K > 1 ? d->xlm.p : d->xl.p;
+      gather_subdomains<double><<<grid, kVecThreads, 0, st>>>(a.v.r, d->gidx.p, xl, d->xlen, K, vs);
+      nl += 1 + d->solve(st, K);
+      xl_fine = xl;
+      xls = K > 1 ? d->xlen : 0;
     }
   }
   if (profile) CK(cudaEventRecord(h->ev[8], st));
   if (pl.coarse) CK(cudaStreamWaitEvent(st, h->join_ev, 0));
-  const double *xc = pl.coarse ? h->co64->xl.p : nullptr;
+  const double *xc = xc_buf;
+  const int64_t xcs = (pl.coarse && K > 1) ? co->xlen : 0;
   if (pl.sgs && pl.mixed)
-    pull_prolong_dot<double, float><<<pg, kVecThreads, 0, st>>>(
-        n, h->pull_ptr.p, h->pull_idx.p, pl.fine ? h->sgs->x.p : nullptr, h->Pp.p, h->Pc.p, h->Pvf.p, xc,
-        pl.mode, h->r.p, h->z.p, h->zold.p, h->part_rz.p, h->part_rzo.p, cb);
+    pull_prolong_dot<double, float><<<a.pg, kVecThreads, 0, st>>>(
+        n, h->pull_ptr.p, h->pull_idx.p, (const double *)xl_fine, h->Pp.p, h->Pc.p, h->Pvf.p, xc,
+        pl.mode, a.v.r, a.v.z, a.v.zold, a.part_rz, a.part_rzo, a.cb, a.csys, vs, xls, xcs);
   else if (pl.sgs)
-    pull_prolong_dot<double, double><<<pg, kVecThreads, 0, st>>>(
-        n, h->pull_ptr.p, h->pull_idx.p, pl.fine ? h->sgs->x.p : nullptr, h->Pp.p, h->Pc.p, h->Pv.p, xc,
-        pl.mode, h->r.p, h->z.p, h->zold.p, h->part_rz.p, h->part_rzo.p, cb);
+    pull_prolong_dot<double, double><<<a.pg, kVecThreads, 0, st>>>(
+        n, h->pull_ptr.p, h->pull_idx.p, (const double *)xl_fine, h->Pp.p, h->Pc.p, h->Pv.p, xc,
+        pl.mode, a.v.r, a.v.z, a.v.zold, a.part_rz, a.part_rzo, a.cb, a.csys, vs, xls, xcs);
   else if (pl.mixed)
-    pull_prolong_dot<float, float><<<pg, kVecThreads, 0, st>>>(
-        n, h->pull_ptr.p, h->pull_idx.p, pl.fine ? h->sub32->xl.p : nullptr, h->Pp.p, h->Pc.p, h->Pvf.p, xc,
-        pl.mode, h->r.p, h->z.p, h->zold.p, h->part_rz.p, h->part_rzo.p, cb);
+    pull_prolong_dot<float, float><<<a.pg, kVecThreads, 0, st>>>(
+        n, h->pull_ptr.p, h->pull_idx.p, (const float *)xl_fine, h->Pp.p, h->Pc.p, h->Pvf.p, xc,
+        pl.mode, a.v.r, a.v.z, a.v.zold, a.part_rz, a.part_rzo, a.cb, a.csys, vs, xls, xcs);
   else
-    pull_prolong_dot<double, double><<<pg, kVecThreads, 0, st>>>(
-        n, h->pull_ptr.p, h->pull_idx.p, pl.fine ? h->sub64->xl.p : nullptr, h->Pp.p, h->Pc.p, h->Pv.p, xc,
-        pl.mode, h->r.p, h->z.p, h->zold.p, h->part_rz.p, h->part_rzo.p, cb);
+    pull_prolong_dot<double, double><<<a.pg, kVecThreads, 0, st>>>(
+        n, h->pull_ptr.p, h->pull_idx.p, (const double *)xl_fine, h->Pp.p, h->Pc.p, h->Pv.p, xc,
+        pl.mode, a.v.r, a.v.z, a.v.zold, a.part_rz, a.part_rzo, a.cb, a.csys, vs, xls, xcs);
   return nl + 1;
 }
 
-// Batched independent systems: every system runs its own pcg_weigs
-// (pcg.F90:289-462) with its own scalars and stopping test; the
-// factorisations, preconditioner applications and products of all systems
-// share the launches.  A system that stops is frozen (its rows are skipped by
-// the direction, product and update kernels).
-dg_status do_solve_batch(dg_handle *h, const double *d_b, double *d_x, dg_stats *st, cudaStream_t s) {
+// Stacked solves: the independent systems of a batch (c = h->bt) or K
+// right-hand sides of one matrix (c = h->mr, nrhs = K).  Every system /
+// right-hand side runs its own pcg_weigs (pcg.F90:289-462) with its own
+// scalars and stopping test; the factorisations, preconditioner applications
+// and products share the launches.  A system that stops is frozen (its rows
+// are skipped by the direction, product and update kernels).  d_b, d_x: the
+// stacked vectors (length ntot).
+dg_status do_solve_stacked(dg_handle *h, BatchCtx &bc, const Vecs &V, int nrhs, int64_t ntot, const double *d_b,
+                           double *d_x, dg_stats *st, cudaStream_t s) {
   Controls c = h->ctl;
   ctl_finish(c);
-  const int n = h->n, K = h->nsys, nch = h->nchunks;
+  const int n = h->n, K = bc.nsys, nch = bc.nchunks;
   const SolvePlan pl = plan_of(h, c);
   const int mixed = pl.mixed ? 1 : 0;
   const double tol = c.solve_tolerance, tol2 = tol * tol;
@@ -1201,6 +1289,14 @@ dg_status do_solve_batch(dg_handle *h, const double *d_b, double *d_x, dg_stats 
   out.factor_nnz = h->Bsub.factor_nnz;
   out.factor_gflop = h->Bsub.factor_flops * 1e-9;
   out.t_setup_s = h->t_setup;
+  StackArgs sa;
+  sa.v = V;
+  sa.part_rz = bc.part_rz.p;
+  sa.part_rzo = bc.part_rzo.p;
+  sa.pg = nch;
+  sa.cb = bc.cb.p;
+  sa.csys = nrhs > 1 ? bc.csys.p : nullptr;
+  sa.nrhs = nrhs;
   try {
     const double t0 = wall();
     CK(cudaMemsetAsync(h->status.p, 0, sizeof(int), s));
@@ -1211,12 +1307,12 @@ dg_status do_solve_batch(dg_handle *h, const double *d_b, double *d_x, dg_stats 
       launches += factor_all(h, fp, s);
     }
     CK(cudaEventRecord(h->ev[1], s));
-    CK(cudaMemcpyAsync(h->b.p, d_b, (size_t)n * sizeof(double), cudaMemcpyDeviceToDevice, s));
-    CK(cudaMemsetAsync(h->x.p, 0, (size_t)n * sizeof(double), s));
-    CK(cudaMemsetAsync(h->p.p, 0, (size_t)n * sizeof(double), s));
-    CK(cudaMemsetAsync(h->zold.p, 0, (size_t)n * sizeof(double), s));
-    bt_any(s, h, 1, -1, h->r.p);  // r = b - A x0 for every system
-    bt_step(h, s, BT_INIT, 0, mixed, tol2, h->part_rr.p, nullptr);
+    CK(cudaMemcpyAsync(V.b, d_b, (size_t)ntot * sizeof(double), cudaMemcpyDeviceToDevice, s));
+    CK(cudaMemsetAsync(V.x, 0, (size_t)ntot * sizeof(double), s));
+    CK(cudaMemsetAsync(V.p, 0, (size_t)ntot * sizeof(double), s));
+    CK(cudaMemsetAsync(V.zold, 0, (size_t)ntot * sizeof(double), s));
+    bt_any(s, h, bc, V, 1, -1, V.r);  // r = b - A x0 for every system
+    bt_step(bc, s, BT_INIT, 0, mixed, tol2, bc.part_rr.p, nullptr);
     launches += 2;
     CK(cudaGetLastError());
     int stv = 0;
@@ -1235,30 +1331,29 @@ dg_status do_solve_batch(dg_handle *h, const double *d_b, double *d_x, dg_stats 
       return ms * 1e-3;
     };
     auto iteration = [&](cudaStream_t q, int first, bool replace, bool profile) -> int {
-      int nl = precondition(h, pl, q, profile, nch, h->d_cb.p);
-      bt_step(h, q, BT_RHO, first, mixed, tol2, h->part_rz.p, h->part_rzo.p);
+      int nl = precondition(h, pl, q, profile, sa);
+      bt_step(bc, q, BT_RHO, first, mixed, tol2, bc.part_rz.p, bc.part_rzo.p);
       if (profile) CK(cudaEventRecord(h->ev[6], q));
-      bt_direction<<<nch, kVecThreads, 0, q>>>(h->d_cb.p, h->d_csys.p, h->d_state.p, h->bsc.p, h->z.p, h->p.p,
-                                               first);
-      bt_any(q, h, 0);
+      bt_direction<<<nch, kVecThreads, 0, q>>>(bc.cb.p, bc.csys.p, bc.state.p, bc.bsc.p, V.z, V.p, first);
+      bt_any(q, h, bc, V, 0);
       if (profile) CK(cudaEventRecord(h->ev[7], q));
-      bt_step(h, q, BT_ALPHA, first, mixed, tol2, h->part_pq.p, nullptr);
-      bt_update<<<nch, kVecThreads, 0, q>>>(h->d_cb.p, h->d_csys.p, h->d_state.p, h->bsc.p, h->p.p, h->q.p, h->x.p,
-                                            h->r.p, h->part_rr.p);
+      bt_step(bc, q, BT_ALPHA, first, mixed, tol2, bc.part_pq.p, nullptr);
+      bt_update<<<nch, kVecThreads, 0, q>>>(bc.cb.p, bc.csys.p, bc.state.p, bc.bsc.p, V.p, V.q, V.x, V.r,
+                                            bc.part_rr.p);
       nl += 5;
       if (replace) {  // FP64 residual replacement, r = b - A x, of the iterating systems
-        bt_any(q, h, 1, BT_ACTIVE, h->r.p);
+        bt_any(q, h, bc, V, 1, BT_ACTIVE, V.r);
         nl++;
       }
-      bt_step(h, q, BT_FINISH, first, mixed, tol2, h->part_rr.p, nullptr);
+      bt_step(bc, q, BT_FINISH, first, mixed, tol2, bc.part_rr.p, nullptr);
       return nl + 1;
     };
-    if (!h->iter_exec) {
+    if (!bc.exec) {
       cudaGraph_t g = nullptr;
       CK(cudaStreamBeginCapture(h->s3, cudaStreamCaptureModeThreadLocal));
-      h->iter_nodes = iteration(h->s3, 0, false, false);
+      bc.exec_nodes = iteration(h->s3, 0, false, false);
       CK(cudaStreamEndCapture(h->s3, &g));
-      CK(cudaGraphInstantiate(&h->iter_exec, g, 0));
+      CK(cudaGraphInstantiate(&bc.exec, g, 0));
       CK(cudaGraphDestroy(g));
     }
     std::vector<double> t_end(1, wall() - t0);
@@ -1268,8 +1363,8 @@ dg_status do_solve_batch(dg_handle *h, const double *d_b, double *d_x, dg_stats 
       const int first = it == 1;
       const bool replace = pl.mixed && c.replace_every > 0 && it % c.replace_every == 0;
       if (!first && !replace && !prof) {
-        CK(cudaGraphLaunch(h->iter_exec, s));
-        launches += h->iter_nodes;
+        CK(cudaGraphLaunch(bc.exec, s));
+        launches += bc.exec_nodes;
       } else {
         launches += iteration(s, first, replace, prof);
       }
@@ -1280,28 +1375,28 @@ dg_status do_solve_batch(dg_handle *h, const double *d_b, double *d_x, dg_stats 
         if (pl.coarse) t_co += lap(4, 5);
         t_sp += lap(6, 7);
       }
-      if (h->host_counts[1] > 0) {  // the FP64 true residual confirms the systems the recurrence stopped
-        bt_any(s, h, 1, BT_CHECK, h->r.p);
-        bt_step(h, s, BT_CONFIRM, 0, mixed, tol2, h->part_rr.p, nullptr);
+      if (bc.host_counts[1] > 0) {  // the FP64 true residual confirms the systems the recurrence stopped
+        bt_any(s, h, bc, V, 1, BT_CHECK, V.r);
+        bt_step(bc, s, BT_CONFIRM, 0, mixed, tol2, bc.part_rr.p, nullptr);
         launches += 2;
         CK(cudaGetLastError());
         CK(cudaStreamSynchronize(s));
       }
       t_end.push_back(wall() - t0);
-      active = h->host_counts[0];
+      active = bc.host_counts[0];
     }
     CK(cudaEventRecord(h->ev[2], s));
     // true residuals for the report (into q, which is free now)
-    bt_any(s, h, 1, -1, h->q.p);
-    bt_step(h, s, BT_REPORT, 0, mixed, tol2, h->part_rr.p, nullptr);
+    bt_any(s, h, bc, V, 1, -1, V.q);
+    bt_step(bc, s, BT_REPORT, 0, mixed, tol2, bc.part_rr.p, nullptr);
     launches += 2;
-    CK(cudaMemcpyAsync(d_x, h->x.p, (size_t)n * sizeof(double), cudaMemcpyDeviceToDevice, s));
+    CK(cudaMemcpyAsync(d_x, V.x, (size_t)ntot * sizeof(double), cudaMemcpyDeviceToDevice, s));
     std::vector<double> bs((size_t)K * BS_N);
     h->sys_iters.assign((size_t)K, 0);
     h->sys_state.assign((size_t)K, 0);
-    CK(cudaMemcpyAsync(bs.data(), h->bsc.p, bs.size() * sizeof(double), cudaMemcpyDeviceToHost, s));
-    CK(cudaMemcpyAsync(h->sys_iters.data(), h->d_iters.p, (size_t)K * sizeof(int), cudaMemcpyDeviceToHost, s));
-    CK(cudaMemcpyAsync(h->sys_state.data(), h->d_state.p, (size_t)K * sizeof(int), cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(bs.data(), bc.bsc.p, bs.size() * sizeof(double), cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(h->sys_iters.data(), bc.iters.p, (size_t)K * sizeof(int), cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(h->sys_state.data(), bc.state.p, (size_t)K * sizeof(int), cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
     float ms_f = 0, ms_i = 0;
     CK(cudaEventElapsedTime(&ms_f, h->ev[0], h->ev[1]));
@@ -1352,10 +1447,45 @@ dg_status do_solve_batch(dg_handle *h, const double *d_b, double *d_x, dg_stats 
   }
 }
 
+// K right-hand sides of the handle's matrix solved together: the stacked
+// vectors (right-hand side k at k*n), per-right-hand-side CG scalars, one
+// factorisation, every solve kernel over all K (the CTAs reading the same E
+// are adjacent).
+dg_status do_solve_multi(dg_handle *h, int K, const double *d_b, double *d_x, dg_stats *st, cudaStream_t s) {
+  if (!h->ready) return fail(h, DG_NOT_READY, "dg_setup has not run");
+  if (h->nsys > 0) return fail(h, DG_BAD_INPUT, "several right-hand sides of batched systems: stack them as systems");
+  if (K < 1) return fail(h, DG_BAD_INPUT, "number of right-hand sides must be >= 1");
+  if ((int64_t)K * h->n >= (int64_t)INT_MAX) return fail(h, DG_BAD_INPUT, "too many right-hand sides for n");
+  Controls c = h->ctl;
+  ctl_finish(c);
+  if (c.fine_method == 2) return fail(h, DG_BAD_INPUT, "several right-hand sides: fine_method 2 is not supported");
+  if (h->elem_mv) return fail(h, DG_BAD_INPUT, "several right-hand sides: use the assembled products (elemental_matvec 0)");
+  try {
+    if (h->mr_k != K) {
+      const int64_t nt = (int64_t)K * h->n;
+      std::vector<int64_t> row((size_t)K + 1);
+      for (int k = 0; k <= K; k++) row[(size_t)k] = (int64_t)k * h->n;
+      h->mr.build(row, h->n);
+      for (auto *v : {&h->mb, &h->mx, &h->mrr, &h->mp, &h->mq, &h->mz, &h->mzold}) v->alloc((size_t)nt);
+      if (h->sub32) h->sub32->ensure_multi(K);
+      if (h->sub64) h->sub64->ensure_multi(K);
+      if (h->co64) h->co64->ensure_multi(K);
+      h->mr_k = K;
+    }
+  } catch (const CudaError &e) {
+    return cuda_fail(h, e);
+  }
+  const Vecs V{h->mb.p, h->mx.p, h->mrr.p, h->mp.p, h->mq.p, h->mz.p, h->mzold.p};
+  return do_solve_stacked(h, h->mr, V, K, (int64_t)K * h->n, d_b, d_x, st, s);
+}
+
 // the solve: numeric factorisation + PCG (pcg_weigs, pcg.F90:289-462)
 dg_status do_solve(dg_handle *h, const double *d_b, double *d_x, dg_stats *st, cudaStream_t s) {
   if (!h->ready) return fail(h, DG_NOT_READY, "dg_setup has not run");
-  if (h->nsys > 0) return do_solve_batch(h, d_b, d_x, st, s);
+  if (h->nsys > 0) {
+    const Vecs V{h->b.p, h->x.p, h->r.p, h->p.p, h->q.p, h->z.p, h->zold.p};
+    return do_solve_stacked(h, h->bt, V, 1, h->n, d_b, d_x, st, s);
+  }
   Controls c = h->ctl;
   ctl_finish(c);
   const int n = h->n;
@@ -1418,7 +1548,12 @@ dg_status do_solve(dg_handle *h, const double *d_b, double *d_x, dg_stats *st, c
     // one PCG iteration's launches on stream st (coarse branch forked to s2);
     // returns the number of kernels
     auto iteration = [&](cudaStream_t st, int first, bool replace, bool profile) -> int {
-      int nl = precondition(h, pl, st, profile, grid, nullptr);
+      StackArgs sa;
+      sa.v = Vecs{h->b.p, h->x.p, h->r.p, h->p.p, h->q.p, h->z.p, h->zold.p};
+      sa.part_rz = h->part_rz.p;
+      sa.part_rzo = h->part_rzo.p;
+      sa.pg = grid;
+      int nl = precondition(h, pl, st, profile, sa);
       if (profile) CK(cudaEventRecord(h->ev[6], st));
       spmv_any(h->lanes, grid, st, h, first, mixed ? 1 : 0);
       if (profile) CK(cudaEventRecord(h->ev[7], st));
@@ -1726,8 +1861,8 @@ dg_status dg_set_systems(dg_handle *h, int nsys, const int *n_sys, const long lo
 dg_status dg_get_system_stats(const dg_handle *h, int *iterations, int *status, double *rel_residual,
                               double *seconds) {
   if (!h) return DG_BAD_INPUT;
-  if (h->nsys <= 0 || (int)h->sys_iters.size() != h->nsys) return DG_NOT_READY;
-  for (int k = 0; k < h->nsys; k++) {
+  if (h->sys_iters.empty()) return DG_NOT_READY;
+  for (int k = 0; k < (int)h->sys_iters.size(); k++) {
     const int stt = h->sys_state[(size_t)k];
     if (iterations) iterations[k] = h->sys_iters[(size_t)k];
     if (status) status[k] = stt == BT_DONE ? DG_OK : stt == BT_BREAKDOWN ? DG_BREAKDOWN : DG_NOT_CONVERGED;
@@ -1832,6 +1967,38 @@ dg_status dg_autotune(dg_handle *h, double *best_seconds, int *chosen) {
     chosen[2] = pick.fwd_kb; chosen[3] = pick.lean_kb;
   }
   return st;
+}
+
+dg_status dg_solve_multi(dg_handle *h, int nrhs, const double *b, double *x, dg_stats *stats) {
+  if (!h || !x || nrhs < 1) return DG_BAD_INPUT;
+  if (!h->ready) return fail(h, DG_NOT_READY, "dg_setup has not run");
+  const size_t bytes = (size_t)h->n * (size_t)nrhs * sizeof(double);
+  double *db = nullptr, *dx = nullptr;
+  if (cudaMalloc(&db, bytes) != cudaSuccess || cudaMalloc(&dx, bytes) != cudaSuccess) {
+    cudaFree(db);
+    return fail(h, DG_CUDA_ERROR, "device memory for the right-hand sides");
+  }
+  dg_status st = DG_OK;
+  if (b) {
+    if (cudaMemcpy(db, b, bytes, cudaMemcpyHostToDevice) != cudaSuccess) st = fail(h, DG_CUDA_ERROR, "H2D copy failed");
+  } else {
+    for (int k = 0; k < nrhs && st == DG_OK; k++)
+      if (cudaMemcpy(db + (size_t)k * h->n, h->rhs.data(), (size_t)h->n * sizeof(double), cudaMemcpyHostToDevice) !=
+          cudaSuccess)
+        st = fail(h, DG_CUDA_ERROR, "H2D copy failed");
+  }
+  if (st == DG_OK) st = do_solve_multi(h, nrhs, db, dx, stats, 0);
+  if ((st == DG_OK || st == DG_NOT_CONVERGED) && cudaMemcpy(x, dx, bytes, cudaMemcpyDeviceToHost) != cudaSuccess)
+    st = fail(h, DG_CUDA_ERROR, "D2H copy failed");
+  cudaFree(db);
+  cudaFree(dx);
+  return st;
+}
+
+dg_status dg_solve_multi_device(dg_handle *h, int nrhs, const double *d_b, double *d_x, dg_stats *stats,
+                                void *stream) {
+  if (!h || !d_b || !d_x) return DG_BAD_INPUT;
+  return do_solve_multi(h, nrhs, d_b, d_x, stats, (cudaStream_t)stream);
 }
 
 dg_status dg_solve_device(dg_handle *h, const double *d_b, double *d_x, dg_stats *stats, void *stream) {

@@ -131,8 +131,8 @@ dg_status dg_set_rhs(dg_handle *h, const double *b);
  * A partition vector cannot be combined with it. */
 dg_status dg_set_systems(dg_handle *h, int nsys, const int *n_sys, const long long *nnz_sys, const int *rows,
                          const int *cols, const double *vals, const double *b);
-/* Per-system results of the last batched solve (each pointer may be NULL;
- * nsys entries each): iterations, status (DG_OK, DG_NOT_CONVERGED,
+/* Per-system results of the last batched solve, or per right-hand side of
+ * the last dg_solve_multi (each pointer may be NULL; one entry each): iterations, status (DG_OK, DG_NOT_CONVERGED,
  * DG_BREAKDOWN), true relative residual ||b - A x|| / ||b|| and the wall time
  * from the start of the solve to the end of the system's last iteration. */
 dg_status dg_get_system_stats(const dg_handle *h, int *iterations, int *status, double *rel_residual,
@@ -162,6 +162,18 @@ dg_status dg_solve(dg_handle *h, const double *b, double *x, dg_stats *stats);
 /* Same with device pointers on the given CUDA stream (NULL: default stream). */
 dg_status dg_solve_device(dg_handle *h, const double *d_b, double *d_x, dg_stats *stats,
                           void *cuda_stream);
+/* Several right-hand sides of the handle's matrix solved together (no
+ * reference counterpart: the reference solves one right-hand side per run).
+ * B and X hold nrhs vectors of n doubles one after the other (B may be NULL:
+ * the stored right-hand side for every vector).  Each right-hand side runs its
+ * own PCG (own scalars, stopping test and iteration count, as dg_solve); the
+ * factorisations are shared and every preconditioner, product and vector
+ * kernel covers all of them.  dg_get_system_stats reports per right-hand side;
+ * stats carries the largest iteration count and residual.  Not with batched
+ * systems, fine_method 2 or elemental_matvec 1. */
+dg_status dg_solve_multi(dg_handle *h, int nrhs, const double *B, double *X, dg_stats *stats);
+dg_status dg_solve_multi_device(dg_handle *h, int nrhs, const double *d_B, double *d_X, dg_stats *stats,
+                                void *cuda_stream);
 /* Write x with the control file's solution_file / solution_format. */
 dg_status dg_write_solution(dg_handle *h, const double *x);
 
