@@ -566,6 +566,9 @@ def run_adjoint(args, fd_elements):
     s.set_option("precision", 1)
     with torch.no_grad():
         Xt = element_solve(s, ngf, eptr, efree, Kb, erhs, torch.tensor(k_target), B).detach()
+    # one untimed forward + backward pass (first use of the torch kernels of the loss)
+    kw = torch.tensor(kappa, requires_grad=True)
+    ((element_solve(s, ngf, eptr, efree, Kb, erhs, kw, B) - Xt) ** 2).sum().backward()
     k = torch.tensor(kappa, requires_grad=True)
     bt = B.clone().requires_grad_(True)
     torch.cuda.synchronize()
