@@ -603,6 +603,115 @@ mf_update_big(MfView v, const int2 *__restrict__ tasks, int jl, int kw, T *__res
   }
 }
 
+// FP32 trailing update on the tensor cores: the same tiles as mf_update_big
+// (C -= L_I L_J^T, 128 x 128 per CTA, K in chunks of 8 double-buffered in
+// shared memory), each product as three TF32 products (split 3xTF32:
+// a = a_hi + a_lo with a_hi, a_lo TF32; a b ~ a_lo b_hi + a_hi b_lo + a_hi b_hi,
+// FP32 accumulation), which keeps the FP32 accuracy of the factorisation.
+// 8 warps, warp w owns rows 64*(w%2) .. +63 and columns 32*(w/2) .. +31 of the
+// tile: 4 x 4 mma.m16n8k8 tiles.  Operands are split when they are staged.
+__device__ __forceinline__ uint32_t tf32_of(float x) {
+  uint32_t r;
+  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+  return r;
+}
+__device__ __forceinline__ void mma_tf32(float (&d)[4], const uint32_t (&a)[4], const uint32_t (&b)[2]) {
+  asm volatile("mma.sync.aligned.m16n8k8.row.col.f32.tf32.tf32.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+               "{%0,%1,%2,%3};\n"
+               : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+               : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
+}
+
+constexpr int kTcPad = kBT + 8;  // row stride of the staged operands (conflict-free fragment loads)
+
+__global__ void __launch_bounds__(256, 2)
+mf_update_big_tf32(MfView v, const int2 *__restrict__ tasks, int jl, int kw, float *__restrict__ arena) {
+  __shared__ __align__(16) uint32_t Ah[2][kBK][kTcPad], Al[2][kBK][kTcPad];
+  __shared__ __align__(16) uint32_t Bh[2][kBK][kTcPad], Bl[2][kBK][kTcPad];
+  const int f = tasks[blockIdx.x].x;
+  const int ti = tasks[blockIdx.x].y >> 16, tj = tasks[blockIdx.x].y & 0xffff;
+  const int m = v.f_m[f], k = v.f_k[f];
+  const int K = min(kw, k - jl);
+  const int c0 = jl + K, r0 = c0 + ti * kBT, cc0 = c0 + tj * kBT;
+  float *F = arena + v.f_off[f];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int lt = tid >> 5, lr = (tid & 31) * 4;  // chunk column and first of 4 rows this thread stages
+  const int wm = (warp & 1) * 64, wn = (warp >> 1) * 32;
+  const int gid = lane >> 2, tig = lane & 3;
+  float pa[4], pb[4];
+  auto fetch = [&](int kc) {
+    const int t = kc + lt;
+#pragma unroll
+    for (int u = 0; u < 4; u++) {
+      const int ra = r0 + lr + u, rb = cc0 + lr + u;
+      pa[u] = (t < K && ra < m) ? F[(int64_t)(jl + t) * m + ra] : 0.f;
+      pb[u] = (t < K && rb < m) ? F[(int64_t)(jl + t) * m + rb] : 0.f;
+    }
+  };
+  auto stash = [&](int buf) {
+#pragma unroll
+    for (int u = 0; u < 4; u++) {
+      const uint32_t ah = tf32_of(pa[u]), bh = tf32_of(pb[u]);
+      Ah[buf][lt][lr + u] = ah;
+      Al[buf][lt][lr + u] = tf32_of(pa[u] - __uint_as_float(ah));
+      Bh[buf][lt][lr + u] = bh;
+      Bl[buf][lt][lr + u] = tf32_of(pb[u] - __uint_as_float(bh));
+    }
+  };
+  float acc[4][4][4];
+#pragma unroll
+  for (int a = 0; a < 4; a++)
+#pragma unroll
+    for (int b = 0; b < 4; b++)
+#pragma unroll
+      for (int q = 0; q < 4; q++) acc[a][b][q] = 0.f;
+  fetch(0);
+  stash(0);
+  __syncthreads();
+  int buf = 0;
+  for (int kc = 0; kc < K; kc += kBK) {
+    const bool more = kc + kBK < K;
+    if (more) fetch(kc + kBK);
+    // B fragments (hi and lo) of the warp's 4 column tiles
+    uint32_t bh[4][2], bl[4][2];
+#pragma unroll
+    for (int nt = 0; nt < 4; nt++) {
+      const int col = wn + nt * 8 + gid;
+      bh[nt][0] = Bh[buf][tig][col];
+      bh[nt][1] = Bh[buf][tig + 4][col];
+      bl[nt][0] = Bl[buf][tig][col];
+      bl[nt][1] = Bl[buf][tig + 4][col];
+    }
+#pragma unroll
+    for (int mt = 0; mt < 4; mt++) {
+      const int row = wm + mt * 16 + gid;
+      const uint32_t ah[4] = {Ah[buf][tig][row], Ah[buf][tig][row + 8], Ah[buf][tig + 4][row],
+                              Ah[buf][tig + 4][row + 8]};
+      const uint32_t al[4] = {Al[buf][tig][row], Al[buf][tig][row + 8], Al[buf][tig + 4][row],
+                              Al[buf][tig + 4][row + 8]};
+#pragma unroll
+      for (int nt = 0; nt < 4; nt++) {  // small terms first
+        mma_tf32(acc[mt][nt], al, bh[nt]);
+        mma_tf32(acc[mt][nt], ah, bl[nt]);
+        mma_tf32(acc[mt][nt], ah, bh[nt]);
+      }
+    }
+    if (more) stash(buf ^ 1);
+    __syncthreads();
+    buf ^= 1;
+  }
+#pragma unroll
+  for (int mt = 0; mt < 4; mt++)
+#pragma unroll
+    for (int nt = 0; nt < 4; nt++)
+#pragma unroll
+      for (int q = 0; q < 4; q++) {
+        const int row = r0 + wm + mt * 16 + gid + (q >= 2 ? 8 : 0);
+        const int col = cc0 + wn + nt * 8 + tig * 2 + (q & 1);
+        if (row < m && col < m && row >= col) F[(int64_t)col * m + row] -= acc[mt][nt][q];
+      }
+}
+
 // ---------------------------------------------------------------------------
 // multifrontal solves with the elimination matrices E
 //

@@ -350,7 +350,8 @@ struct MfDevice {
         }
         if (st.big) {
           if constexpr (sizeof(T) == 4) {  // planned for FP32 batches only
-            mf_update_big<T><<<st.upd_cnt, 256, 0, s>>>(view, upd_tasks.p + st.upd_off, st.j0, st.kw, arena.p);
+            mf_update_big_tf32<<<st.upd_cnt, 256, 0, s>>>(view, upd_tasks.p + st.upd_off, st.j0, st.kw,
+                                                          reinterpret_cast<float *>(arena.p));
             launches++;
           }
         } else if (st.upd_cnt + st.etile_cnt) {
