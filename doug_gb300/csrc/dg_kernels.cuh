@@ -524,88 +524,11 @@ mf_update(MfView v, const int2 *__restrict__ tasks, int nupd, const int2 *__rest
 // Trailing update of a super-panel with 128 x 128 tiles (FP32): C -= L_rows L_cols^T
 // for the L columns [jl, jl + K), K = min(kw, k - jl), rows and columns from
 // c0 = jl + K (task = {front, (ti << 16) | tj}, ti >= tj, 128-row units).
-// 256 threads, 8 x 8 outputs each (rows tx*4 + {0..3} and 64 + tx*4 + {0..3},
-// columns likewise with ty); K is walked in chunks of 8 columns, double
-// buffered in shared memory with the next chunk's global loads issued before
-// the current chunk is consumed.
 constexpr int kBT = 128, kBK = 8;
 
-template <typename T>
-__global__ void __launch_bounds__(256, 2)
-mf_update_big(MfView v, const int2 *__restrict__ tasks, int jl, int kw, T *__restrict__ arena) {
-  __shared__ __align__(16) T As[2][kBK][kBT];
-  __shared__ __align__(16) T Bs[2][kBK][kBT];
-  const int f = tasks[blockIdx.x].x;
-  const int ti = tasks[blockIdx.x].y >> 16, tj = tasks[blockIdx.x].y & 0xffff;
-  const int m = v.f_m[f], k = v.f_k[f];
-  const int K = min(kw, k - jl);
-  const int c0 = jl + K, r0 = c0 + ti * kBT, cc0 = c0 + tj * kBT;
-  T *F = arena + v.f_off[f];
-  const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
-  const int lt = tid >> 5, lr = (tid & 31) * 4;  // chunk column and first of 4 rows this thread loads
-  T pa[4], pb[4];
-  auto fetch = [&](int kc) {
-    const int t = kc + lt;
-#pragma unroll
-    for (int u = 0; u < 4; u++) {
-      const int ra = r0 + lr + u, rb = cc0 + lr + u;
-      pa[u] = (t < K && ra < m) ? F[(int64_t)(jl + t) * m + ra] : T(0);
-      pb[u] = (t < K && rb < m) ? F[(int64_t)(jl + t) * m + rb] : T(0);
-    }
-  };
-  auto stash = [&](int buf) {
-#pragma unroll
-    for (int u = 0; u < 4; u++) {
-      As[buf][lt][lr + u] = pa[u];
-      Bs[buf][lt][lr + u] = pb[u];
-    }
-  };
-  T acc[8][8];
-#pragma unroll
-  for (int a = 0; a < 8; a++)
-#pragma unroll
-    for (int b = 0; b < 8; b++) acc[a][b] = T(0);
-  fetch(0);
-  stash(0);
-  __syncthreads();
-  int buf = 0;
-  for (int kc = 0; kc < K; kc += kBK) {
-    const bool more = kc + kBK < K;
-    if (more) fetch(kc + kBK);
-#pragma unroll
-    for (int t = 0; t < kBK; t++) {
-      T ra[8], rb[8];
-#pragma unroll
-      for (int u = 0; u < 4; u++) {
-        ra[u] = As[buf][t][tx * 4 + u];
-        ra[4 + u] = As[buf][t][64 + tx * 4 + u];
-        rb[u] = Bs[buf][t][ty * 4 + u];
-        rb[4 + u] = Bs[buf][t][64 + ty * 4 + u];
-      }
-#pragma unroll
-      for (int a = 0; a < 8; a++)
-#pragma unroll
-        for (int b = 0; b < 8; b++) acc[a][b] += ra[a] * rb[b];
-    }
-    if (more) stash(buf ^ 1);
-    __syncthreads();
-    buf ^= 1;
-  }
-#pragma unroll
-  for (int b = 0; b < 8; b++) {
-    const int col = cc0 + (b < 4 ? ty * 4 + b : 64 + ty * 4 + b - 4);
-    if (col >= m) continue;
-#pragma unroll
-    for (int a = 0; a < 8; a++) {
-      const int row = r0 + (a < 4 ? tx * 4 + a : 64 + tx * 4 + a - 4);
-      if (row < m && row >= col) F[(int64_t)col * m + row] -= acc[a][b];
-    }
-  }
-}
-
-// FP32 trailing update on the tensor cores: the same tiles as mf_update_big
-// (C -= L_I L_J^T, 128 x 128 per CTA, K in chunks of 8 double-buffered in
-// shared memory), each product as three TF32 products (split 3xTF32:
+// It runs on the tensor cores (C -= L_I L_J^T, 128 x 128 per CTA, K walked
+// in chunks of 8 columns, double-buffered in shared memory with the next
+// chunk's global loads issued before the current chunk is consumed), each product as three TF32 products (split 3xTF32:
 // a = a_hi + a_lo with a_hi, a_lo TF32; a b ~ a_lo b_hi + a_hi b_lo + a_hi b_hi,
 // FP32 accumulation), which keeps the FP32 accuracy of the factorisation.
 // 8 warps, warp w owns rows 64*(w%2) .. +63 and columns 32*(w/2) .. +31 of the
