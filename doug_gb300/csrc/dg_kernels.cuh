@@ -22,7 +22,7 @@ constexpr int kRedBlocks = 1024;   // partial-sum slots of every reduction
 constexpr int kVecThreads = 256;
 
 // device error word bits
-enum : int { ERR_NOT_SPD = 1, ERR_NAN = 2, ERR_BREAKDOWN = 4 };
+enum : int { ERR_NOT_SPD = 1, ERR_NAN = 2, ERR_BREAKDOWN = 4, ERR_WAIT = 8 };
 
 struct MfView {  // device pointers of one multifrontal batch
   const int64_t *f_off;
@@ -728,7 +728,7 @@ __device__ __forceinline__ void fwd_small_body(const MfView &v, const int *__res
     const int rc = v.f_m[c] - v.f_k[c];
     const int *rel = v.relmap + v.f_relmap[c];
     const T *u = uvec + v.f_uoff[c];
-    for (int a = sl; a < rc; a += G) w[rel[a]] += u[a];
+    for (int a = sl; a < rc; a += G) w[rel[a]] += __ldcg(u + a);
     __syncwarp(gm);
   }
   T acc[PASS][VN];
@@ -779,7 +779,7 @@ __device__ __forceinline__ void bwd_small_body(const MfView &v, const int *__res
   load_e_batch<T, PASS, G>(Ef, ld, m, k, sl, 0, e);
   const T *xb = xl + v.f_xoff[f];
   const int *rows = v.rows + v.f_rows[f];
-  for (int i = sl; i < ld; i += G) w[i] = i < k ? yl[xo + i] : (i < m ? xb[rows[i]] : T(0));
+  for (int i = sl; i < ld; i += G) w[i] = i < k ? yl[xo + i] : (i < m ? __ldcg(xb + rows[i]) : T(0));
   __syncwarp(gm);
   T wr[PASS][VN];
 #pragma unroll
@@ -865,20 +865,15 @@ mf_bwd_small(MfView v, const int *__restrict__ fronts, SmallBuckets sb, const T 
 // of rows wholly above the diagonal of E is zero and not loaded.
 template <typename T> struct FwdRows { static constexpr int N = 32 * Vec16<T>::N; };
 
+// the task body; b: shared memory for the front's right-hand side (m
+// values), red: the warp sums of one chunk
 template <typename T, int NT>
-__global__ void __launch_bounds__(NT, NT == kELeanThreads ? 12 : 4)
-mf_fwd_big(MfView v, const int2 *__restrict__ tasks, const T *__restrict__ E, const T *__restrict__ xl,
-           T *__restrict__ yl, T *__restrict__ uvec, int nrhs = 1, int64_t xs = 0, int64_t us = 0) {
+__device__ __forceinline__ void fwd_big_body(const MfView &v, int2 tk, const T *__restrict__ E,
+                                             const T *__restrict__ xl, T *__restrict__ yl, T *__restrict__ uvec,
+                                             T *b, T (*red)[FwdRows<T>::N]) {
   constexpr int VN = Vec16<T>::N, RC = FwdRows<T>::N, NW = NT / 32, UN = NT == kELeanThreads ? 4 : kEUnroll;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  T *b = reinterpret_cast<T *>(smem_raw);  // b[0, m)
-  __shared__ T red[NW][RC];
-  const int task = blockIdx.x / nrhs, rk = blockIdx.x % nrhs;
-  xl += rk * xs;
-  yl += rk * xs;
-  uvec += rk * us;
-  const int f = tasks[task].x;
-  const int ch0 = tasks[task].y >> 16, nch = tasks[task].y & 0xffff;
+  const int f = tk.x;
+  const int ch0 = tk.y >> 16, nch = tk.y & 0xffff;
   const int m = v.f_m[f], k = v.f_k[f], ld = round4(m);
   const int64_t xo = v.f_xoff[f] + v.f_p0[f];
   const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
@@ -907,7 +902,7 @@ mf_fwd_big(MfView v, const int2 *__restrict__ tasks, const T *__restrict__ E, co
     const int rc = v.f_m[c] - v.f_k[c];
     const int *rel = v.relmap + v.f_relmap[c];
     const T *u = uvec + v.f_uoff[c];
-    for (int a = tid; a < rc; a += NT) b[rel[a]] += u[a];
+    for (int a = tid; a < rc; a += NT) b[rel[a]] += __ldcg(u + a);
     __syncthreads();
   }
   T *uf = uvec + v.f_uoff[f];
@@ -942,19 +937,24 @@ mf_fwd_big(MfView v, const int2 *__restrict__ tasks, const T *__restrict__ E, co
   }
 }
 
+template <typename T, int NT>
+__global__ void __launch_bounds__(NT, NT == kELeanThreads ? 12 : 4)
+mf_fwd_big(MfView v, const int2 *__restrict__ tasks, const T *__restrict__ E, const T *__restrict__ xl,
+           T *__restrict__ yl, T *__restrict__ uvec, int nrhs = 1, int64_t xs = 0, int64_t us = 0) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ T red[NT / 32][FwdRows<T>::N];
+  const int task = blockIdx.x / nrhs, rk = blockIdx.x % nrhs;
+  fwd_big_body<T, NT>(v, tasks[task], E, xl + rk * xs, yl + rk * xs, uvec + rk * us,
+                      reinterpret_cast<T *>(smem_raw), red);
+}
+
 // large fronts, backward: task = {front, column block J}; x[32J .. 32J+31] from
 // rows [32J, m) of E
 template <typename T, int NT>
-__global__ void __launch_bounds__(NT, NT == kELeanThreads ? 12 : 4)
-mf_bwd_big(MfView v, const int2 *__restrict__ tasks, const T *__restrict__ E, const T *__restrict__ yl,
-           T *__restrict__ xl, int nrhs = 1, int64_t xs = 0) {
+__device__ __forceinline__ void bwd_big_body(const MfView &v, int2 tk, const T *__restrict__ E,
+                                             const T *__restrict__ yl, T *__restrict__ xl, T *w) {
   constexpr int VN = Vec16<T>::N, LPC = 32 / VN, NCS = NT / LPC, UN = NT == kELeanThreads ? 4 : kEUnroll;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  T *w = reinterpret_cast<T *>(smem_raw);  // v[32J, ld)
-  const int task = blockIdx.x / nrhs, rk = blockIdx.x % nrhs;
-  yl += rk * xs;
-  xl += rk * xs;
-  const int f = tasks[task].x, J = tasks[task].y;
+  const int f = tk.x, J = tk.y;
   const int m = v.f_m[f], k = v.f_k[f], ld = round4(m);
   const int c0 = 32 * J, jb = min(32, k - c0);
   const int64_t xo = v.f_xoff[f] + v.f_p0[f];
@@ -978,7 +978,7 @@ mf_bwd_big(MfView v, const int2 *__restrict__ tasks, const T *__restrict__ E, co
     }
   };
   load_batch(c0 + cs, c0 + rq * VN);  // in flight while v is gathered
-  for (int i = c0 + tid; i < ld; i += NT) w[i - c0] = i < k ? yl[xo + i] : (i < m ? xb[rows[i]] : T(0));
+  for (int i = c0 + tid; i < ld; i += NT) w[i - c0] = i < k ? yl[xo + i] : (i < m ? __ldcg(xb + rows[i]) : T(0));
   __syncthreads();
   for (int cc = cs; cc < 32; cc += NCS) {  // uniform trip count: the shuffles below need whole groups
     const int c = c0 + cc;
@@ -999,6 +999,139 @@ mf_bwd_big(MfView v, const int2 *__restrict__ tasks, const T *__restrict__ E, co
 #pragma unroll
     for (int o = LPC / 2; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
     if (rq == 0 && cc < jb) xl[xo + c] = s;
+  }
+}
+
+template <typename T, int NT>
+__global__ void __launch_bounds__(NT, NT == kELeanThreads ? 12 : 4)
+mf_bwd_big(MfView v, const int2 *__restrict__ tasks, const T *__restrict__ E, const T *__restrict__ yl,
+           T *__restrict__ xl, int nrhs = 1, int64_t xs = 0) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int task = blockIdx.x / nrhs, rk = blockIdx.x % nrhs;
+  bwd_big_body<T, NT>(v, tasks[task], E, yl + rk * xs, xl + rk * xs, reinterpret_cast<T *>(smem_raw));
+}
+
+// ---------------------------------------------------------------------------
+// Dependency-driven solve (solve_schedule 1): one launch per direction.  The
+// tasks of all levels form one list (forward: leaves first; backward: roots
+// first; the level kernels' tasks and small-front CTAs, unchanged); a CTA
+// takes the next task with an atomic counter, waits until the tasks that
+// produce its fronts' inputs have published their done flags (forward: the
+// children's tasks, backward: the parent's), runs the task and publishes its
+// own flag.  A task's dependencies come earlier in the list, so they were
+// taken by CTAs that were running when they took them: no CTA waits on work
+// that has not started, whether or not all CTAs are resident.  The waits are
+// bounded (kQueueWaitCycles); on a timeout the CTA records ERR_WAIT and goes
+// on, and the host reports the error.  Data written by other CTAs of the same
+// launch (update vectors, ancestors' solutions) is read past L1 (__ldcg).
+// With nrhs right-hand sides, list entry g is task g / nrhs for right-hand
+// side g % nrhs and waits for the same right-hand side's producers.
+// ---------------------------------------------------------------------------
+constexpr long long kQueueWaitCycles = 1000000000LL;  // about 0.5 s at 2 GHz
+
+struct QueueView {
+  const int4 *tasks;   // {kind (0 small CTA, 1 large-front task), level, index, 0}
+  const int *dep_ptr;  // dependencies of task t: dep[dep_ptr[t] .. dep_ptr[t+1])
+  const int *dep;
+  int ntasks;
+};
+
+__device__ __forceinline__ int ld_volatile(const int *p) { return *(const volatile int *)p; }
+
+__device__ __forceinline__ void queue_wait(const QueueView &q, int t, int rk, int nrhs, const int *done,
+                                           int *status) {
+  for (int i = q.dep_ptr[t]; i < q.dep_ptr[t + 1]; i++) {
+    const int *flag = done + (int64_t)q.dep[i] * nrhs + rk;
+    const long long t0 = clock64();
+    while (ld_volatile(flag) == 0) {
+      if (clock64() - t0 > kQueueWaitCycles || (ld_volatile(status) & ERR_WAIT)) {
+        atomicOr(status, ERR_WAIT);  // after one timeout no CTA waits any more
+        return;
+      }
+      __nanosleep(100);
+    }
+  }
+  __threadfence();
+}
+
+template <typename T>
+__device__ __forceinline__ void queue_publish(int *done, int64_t idx) {
+  __threadfence();
+  atomicExch(done + idx, 1);
+}
+
+// forward; small tasks: level lv, CTA index c of the level's small-front
+// launch (fronts small_fronts + lvl_small_off[lv], buckets lvl_sb[lv])
+template <typename T>
+__global__ void __launch_bounds__(256, 4)
+mf_fwd_queue(MfView v, QueueView q, const int *__restrict__ small_fronts, const int *__restrict__ lvl_small_off,
+             const SmallBuckets *__restrict__ lvl_sb, const int2 *__restrict__ fwd_tasks, const T *__restrict__ E,
+             const T *__restrict__ xl, T *__restrict__ yl, T *__restrict__ uvec, int *counter, int *done,
+             int *status, int nrhs = 1, int64_t xs = 0, int64_t us = 0) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ T red[8][FwdRows<T>::N];
+  __shared__ int s_g;
+  T *sm = reinterpret_cast<T *>(smem_raw);
+  const int total = q.ntasks * nrhs;
+  for (;;) {
+    if (threadIdx.x == 0) s_g = atomicAdd(counter, 1);
+    __syncthreads();
+    const int g = s_g;
+    if (g >= total) return;
+    const int t = g / nrhs, rk = g % nrhs;
+    if (threadIdx.x == 0) queue_wait(q, t, rk, nrhs, done, status);
+    __syncthreads();
+    const int4 tk = q.tasks[t];
+    const T *xk = xl + rk * xs;
+    T *yk = yl + rk * xs, *uk = uvec + rk * us;
+    if (tk.x == 0) {
+      const SmallBuckets sb = lvl_sb[tk.y];
+      const int *fr = small_fronts + lvl_small_off[tk.y];
+      const int b = tk.z;
+      if (b < sb.nb0) fwd_small_body<T, 8>(v, fr, sb.cnt0, E, xk, yk, uk, b, sm);
+      else if (b < sb.nb0 + sb.nb1) fwd_small_body<T, 16>(v, fr + sb.cnt0, sb.cnt1, E, xk, yk, uk, b - sb.nb0, sm);
+      else fwd_small_body<T, 32>(v, fr + sb.cnt0 + sb.cnt1, sb.cnt2, E, xk, yk, uk, b - sb.nb0 - sb.nb1, sm);
+    } else {
+      fwd_big_body<T, 256>(v, fwd_tasks[tk.z], E, xk, yk, uk, sm, red);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) queue_publish<T>(done, g);
+  }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256, 4)
+mf_bwd_queue(MfView v, QueueView q, const int *__restrict__ small_fronts, const int *__restrict__ lvl_small_off,
+             const SmallBuckets *__restrict__ lvl_sb, const int2 *__restrict__ bwd_tasks, const T *__restrict__ E,
+             const T *__restrict__ yl, T *__restrict__ xl, int *counter, int *done, int *status, int nrhs = 1,
+             int64_t xs = 0) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ int s_g;
+  T *sm = reinterpret_cast<T *>(smem_raw);
+  const int total = q.ntasks * nrhs;
+  for (;;) {
+    if (threadIdx.x == 0) s_g = atomicAdd(counter, 1);
+    __syncthreads();
+    const int g = s_g;
+    if (g >= total) return;
+    const int t = g / nrhs, rk = g % nrhs;
+    if (threadIdx.x == 0) queue_wait(q, t, rk, nrhs, done, status);
+    __syncthreads();
+    const int4 tk = q.tasks[t];
+    const T *yk = yl + rk * xs;
+    T *xk = xl + rk * xs;
+    if (tk.x == 0) {
+      const SmallBuckets sb = lvl_sb[tk.y];
+      const int *fr = small_fronts + lvl_small_off[tk.y];
+      const int b = tk.z;
+      if (b < sb.nb0) bwd_small_body<T, 8>(v, fr, sb.cnt0, E, yk, xk, b, sm);
+      else if (b < sb.nb0 + sb.nb1) bwd_small_body<T, 16>(v, fr + sb.cnt0, sb.cnt1, E, yk, xk, b - sb.nb0, sm);
+      else bwd_small_body<T, 32>(v, fr + sb.cnt0 + sb.cnt1, sb.cnt2, E, yk, xk, b - sb.nb0 - sb.nb1, sm);
+    } else {
+      bwd_big_body<T, 256>(v, bwd_tasks[tk.z], E, yk, xk, sm);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) queue_publish<T>(done, g);
   }
 }
 

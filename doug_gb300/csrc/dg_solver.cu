@@ -74,6 +74,7 @@ struct MfTune {
   int64_t fwd_task_bytes = 96 * 1024;    // E bytes per forward task of a large front
   int64_t lean_task_bytes = 80 * 1024;   // levels with smaller average tasks use 128-thread CTAs
   int small_min_fronts = 304;            // levels with fewer small fronts solve them CTA-per-task
+  int schedule = 0;                      // solves: 0 one launch per level, 1 dependency-driven queue
 };
 
 template <typename T>
@@ -81,6 +82,13 @@ struct MfDevice {
   DBuf<int64_t> f_off, f_rows, f_xoff, f_uoff, f_woff, f_relmap, f_asm, asm_tgt, asm_sp, asm_src, e_off;
   DBuf<int> f_m, f_k, f_p0, f_child_ptr, f_children, rows, relmap, lvl_fronts, gidx;
   DBuf<int> pan_fronts, diag_fronts, solve_small;
+  // dependency-driven schedule of the solves (solve_schedule 1)
+  bool queue = false;
+  DBuf<int4> qf_tasks, qb_tasks;
+  DBuf<int> qf_dep_ptr, qf_dep, qb_dep_ptr, qb_dep, q_small_off, q_counter, q_done;
+  DBuf<SmallBuckets> q_sb;
+  int qf_n = 0, qb_n = 0, q_grid = 0, q_k = 0;
+  size_t q_smem = 0;
   DBuf<int2> asm_tasks, upd_tasks, panel_tasks, esc_tasks, etile_tasks, fwd_tasks, bwd_tasks;
   DBuf<T> arena, E, xl, yl, u;
   int64_t e_len = 0;
@@ -310,6 +318,8 @@ struct MfDevice {
     bwd_tasks.upload(bw);
     set_solve_attrs<kEThreads>(optin, fwd_smem_max, bwd_smem_max);
     set_solve_attrs<kELeanThreads>(optin, fwd_smem_max, bwd_smem_max);
+    queue = tune.schedule == 1;
+    if (queue) plan_queue(B, ss, fw, bw, fwd_smem_max, bwd_smem_max);
   }
 
   template <int NT>
@@ -365,6 +375,96 @@ struct MfDevice {
     return launches;
   }
 
+  // The task lists of the dependency-driven solves: the level plan's tasks in
+  // level order (forward leaves first, backward roots first; per level the
+  // large-front tasks, then the small-front CTAs), and for every task the
+  // tasks producing its inputs (forward: all tasks of the children of its
+  // fronts; backward: all tasks of their parents).
+  void plan_queue(const MfBatch &B, const std::vector<int> &ss, const std::vector<int2> &fw,
+                  const std::vector<int2> &bw, size_t fwd_smem_max, size_t bwd_smem_max) {
+    const int nf = B.nfronts;
+    std::vector<int4> qt[2];
+    std::vector<std::vector<int>> prod[2];   // per front: its tasks
+    std::vector<std::vector<int>> cover[2];  // per task: its fronts
+    for (int dir = 0; dir < 2; dir++) {
+      prod[dir].assign((size_t)nf, {});
+      for (int li = 0; li < nlevels; li++) {
+        const int l = dir == 0 ? li : nlevels - 1 - li;
+        const SolveLevel &L = slevels[(size_t)l];
+        const int boff = dir == 0 ? L.fwd_off : L.bwd_off, bcnt = dir == 0 ? L.fwd_cnt : L.bwd_cnt;
+        for (int i = boff; i < boff + bcnt; i++) {
+          const int f = dir == 0 ? fw[(size_t)i].x : bw[(size_t)i].x;
+          prod[dir][(size_t)f].push_back((int)qt[dir].size());
+          cover[dir].push_back({f});
+          qt[dir].push_back(make_int4(1, l, i, 0));
+        }
+        const SmallBuckets &sb = L.sb;
+        for (int c = 0; c < L.small_cta; c++) {
+          std::vector<int> fr;
+          int first, cnt, per;
+          if (c < sb.nb0) { first = c * 32; cnt = sb.cnt0; per = 32; }
+          else if (c < sb.nb0 + sb.nb1) { first = sb.cnt0 + (c - sb.nb0) * 16; cnt = sb.cnt0 + sb.cnt1; per = 16; }
+          else { first = sb.cnt0 + sb.cnt1 + (c - sb.nb0 - sb.nb1) * 8; cnt = sb.cnt0 + sb.cnt1 + sb.cnt2; per = 8; }
+          for (int q = first; q < std::min(first + per, cnt); q++) {
+            const int f = ss[(size_t)(L.small_off + q)];
+            fr.push_back(f);
+            prod[dir][(size_t)f].push_back((int)qt[dir].size());
+          }
+          cover[dir].push_back(fr);
+          qt[dir].push_back(make_int4(0, l, c, 0));
+        }
+      }
+    }
+    std::vector<int> dptr[2], dep[2];
+    for (int dir = 0; dir < 2; dir++) {
+      dptr[dir].assign(1, 0);
+      std::vector<int> d;
+      for (size_t t = 0; t < qt[dir].size(); t++) {
+        d.clear();
+        for (int f : cover[dir][t]) {
+          if (dir == 0) {
+            for (int ci = B.f_child_ptr[(size_t)f]; ci < B.f_child_ptr[(size_t)f + 1]; ci++)
+              for (int u : prod[0][(size_t)B.f_children[(size_t)ci]]) d.push_back(u);
+          } else if (B.f_parent[(size_t)f] >= 0) {
+            for (int u : prod[1][(size_t)B.f_parent[(size_t)f]]) d.push_back(u);
+          }
+        }
+        std::sort(d.begin(), d.end());
+        d.erase(std::unique(d.begin(), d.end()), d.end());
+        for (int u : d)
+          if (u >= (int)t) throw CudaError{cudaErrorInvalidValue, "solve queue: a dependency does not come first"};
+        dep[dir].insert(dep[dir].end(), d.begin(), d.end());
+        dptr[dir].push_back((int)dep[dir].size());
+      }
+    }
+    qf_tasks.upload(qt[0]); qb_tasks.upload(qt[1]);
+    qf_dep_ptr.upload(dptr[0]); qf_dep.upload(dep[0]);
+    qb_dep_ptr.upload(dptr[1]); qb_dep.upload(dep[1]);
+    qf_n = (int)qt[0].size();
+    qb_n = (int)qt[1].size();
+    std::vector<int> so((size_t)nlevels);
+    std::vector<SmallBuckets> sbv((size_t)nlevels);
+    for (int l = 0; l < nlevels; l++) { so[(size_t)l] = slevels[(size_t)l].small_off; sbv[(size_t)l] = slevels[(size_t)l].sb; }
+    q_small_off.upload(so);
+    q_sb.upload(sbv);
+    q_counter.alloc(2);
+    q_smem = std::max({(size_t)8 * kSolveSmall * sizeof(T), fwd_smem_max, bwd_smem_max});
+    CK(cudaFuncSetAttribute(mf_fwd_queue<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)q_smem));
+    CK(cudaFuncSetAttribute(mf_bwd_queue<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)q_smem));
+    int dev = 0, nsm = 0, occ_f = 0, occ_b = 0;
+    CK(cudaGetDevice(&dev));
+    CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_f, mf_fwd_queue<T>, 256, q_smem));
+    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_b, mf_bwd_queue<T>, 256, q_smem));
+    q_grid = nsm * std::max(1, std::min(occ_f, occ_b));
+    q_k = 0;
+  }
+  void ensure_queue(int K) {
+    if (q_k == K) return;
+    q_done.alloc((size_t)(qf_n + qb_n) * K);
+    q_k = K;
+  }
+
   // several right-hand sides: local vectors k at k*xlen (xlm, ylm) and k*ulen (um)
   DBuf<T> xlm, ylm, um;
   int mk = 0;
@@ -379,10 +479,22 @@ struct MfDevice {
 
   // forward + backward solve: right-hand side in xl, solution back in xl
   // (nrhs > 1: the nrhs right-hand sides in xlm, solutions back in xlm)
-  int solve(cudaStream_t s, int nrhs = 1) {
+  int solve(cudaStream_t s, int nrhs = 1, int *status = nullptr) {
     int launches = 0;
     T *xl_ = nrhs > 1 ? xlm.p : xl.p, *yl_ = nrhs > 1 ? ylm.p : yl.p, *u_ = nrhs > 1 ? um.p : u.p;
     const int64_t xs = nrhs > 1 ? xlen : 0, us = nrhs > 1 ? std::max<int64_t>(ulen, 1) : 0;
+    if (queue && status) {
+      ensure_queue(nrhs);
+      CK(cudaMemsetAsync(q_counter.p, 0, 2 * sizeof(int), s));
+      CK(cudaMemsetAsync(q_done.p, 0, (size_t)(qf_n + qb_n) * nrhs * sizeof(int), s));
+      mf_fwd_queue<T><<<q_grid, 256, q_smem, s>>>(view, QueueView{qf_tasks.p, qf_dep_ptr.p, qf_dep.p, qf_n},
+                                                  solve_small.p, q_small_off.p, q_sb.p, fwd_tasks.p, E.p, xl_, yl_,
+                                                  u_, q_counter.p, q_done.p, status, nrhs, xs, us);
+      mf_bwd_queue<T><<<q_grid, 256, q_smem, s>>>(view, QueueView{qb_tasks.p, qb_dep_ptr.p, qb_dep.p, qb_n},
+                                                  solve_small.p, q_small_off.p, q_sb.p, bwd_tasks.p, E.p, yl_, xl_,
+                                                  q_counter.p + 1, q_done.p + (size_t)qf_n * nrhs, status, nrhs, xs);
+      return 2;
+    }
     for (int l = 0; l < nlevels; l++) {
       const SolveLevel &L = slevels[(size_t)l];
       if (L.small_cta) {
@@ -950,6 +1062,7 @@ dg_status do_setup(dg_handle *h, bool reuse_host = false) {
   tune.fwd_task_bytes = (int64_t)c.fwd_task_kb * 1024;
   tune.lean_task_bytes = (int64_t)c.lean_task_kb * 1024;
   tune.small_min_fronts = c.thin_level_fronts;
+  tune.schedule = c.solve_schedule;
   MfOptions mo;
   mo.leaf = c.nd_leaf;
   const bool timing = std::getenv("DG_SETUP_TIMING") != nullptr;
@@ -1214,7 +1327,7 @@ int precondition(dg_handle *h, const SolvePlan &pl, cudaStream_t st, bool profil
     else
       restrict_to_coarse<double><<<grid, kVecThreads, 0, h->s2>>>(h->Rp.p, h->Rc.p, h->Rv.p, a.v.r, h->cpos.p, xc_buf,
                                                                    h->S.R.nrows, K, vs, xcs);
-    nl += 1 + co->solve(h->s2, K);
+    nl += 1 + co->solve(h->s2, K, h->status.p);
     if (profile) CK(cudaEventRecord(h->ev[5], h->s2));
     CK(cudaEventRecord(h->join_ev, h->s2));
   }
@@ -1231,14 +1344,14 @@ int precondition(dg_handle *h, const SolvePlan &pl, cudaStream_t st, bool profil
       MfDevice<float> *d = h->sub32.get();
       float *xl = K > 1 ? d->xlm.p : d->xl.p;
       gather_subdomains<float><<<grid, kVecThreads, 0, st>>>(a.v.r, d->gidx.p, xl, d->xlen, K, vs);
-      nl += 1 + d->solve(st, K);
+      nl += 1 + d->solve(st, K, h->status.p);
       xl_fine = xl;
       xls = K > 1 ? d->xlen : 0;
     } else {
       MfDevice<double> *d = h->sub64.get();
       double *xl = K > 1 ? d->xlm.p : d->xl.p;
       gather_subdomains<double><<<grid, kVecThreads, 0, st>>>(a.v.r, d->gidx.p, xl, d->xlen, K, vs);
-      nl += 1 + d->solve(st, K);
+      nl += 1 + d->solve(st, K, h->status.p);
       xl_fine = xl;
       xls = K > 1 ? d->xlen : 0;
     }
@@ -1398,7 +1511,10 @@ dg_status do_solve_stacked(dg_handle *h, BatchCtx &bc, const Vecs &V, int nrhs, 
     CK(cudaMemcpyAsync(bs.data(), bc.bsc.p, bs.size() * sizeof(double), cudaMemcpyDeviceToHost, s));
     CK(cudaMemcpyAsync(h->sys_iters.data(), bc.iters.p, (size_t)K * sizeof(int), cudaMemcpyDeviceToHost, s));
     CK(cudaMemcpyAsync(h->sys_state.data(), bc.state.p, (size_t)K * sizeof(int), cudaMemcpyDeviceToHost, s));
+    int stw = 0;
+    CK(cudaMemcpyAsync(&stw, h->status.p, sizeof(int), cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
+    if (stw & ERR_WAIT) return fail(h, DG_CUDA_ERROR, "a dependency wait of the subdomain solve timed out");
     float ms_f = 0, ms_i = 0;
     CK(cudaEventElapsedTime(&ms_f, h->ev[0], h->ev[1]));
     CK(cudaEventElapsedTime(&ms_i, h->ev[1], h->ev[2]));
@@ -1590,6 +1706,7 @@ dg_status do_solve(dg_handle *h, const double *d_b, double *d_x, dg_stats *st, c
       }
       CK(cudaGetLastError());  // a failed launch must not pass as a converged step
       CK(cudaStreamSynchronize(s));
+      if (*h->host_status & ERR_WAIT) return fail(h, DG_CUDA_ERROR, "a dependency wait of the subdomain solve timed out");
       if (prof) {
         t_sub += lap(3, 8);
         if (coarse) t_co += lap(4, 5);
@@ -1686,6 +1803,13 @@ dg_status dg_set_option(dg_handle *h, const char *name, const char *value) {
     int v;
     if (!parse_i10(w2, v)) return fail(h, DG_BAD_INPUT, "bad replace_every");
     h->ctl.replace_every = v;
+    return DG_OK;
+  }
+  if (w1 == "solve_schedule") {
+    int v;
+    if (!parse_i10(w2, v) || v < 0 || v > 1) return fail(h, DG_BAD_INPUT, "solve_schedule must be 0 or 1");
+    h->ctl.solve_schedule = v;
+    h->ready = false;
     return DG_OK;
   }
   if (w1 == "panel_rows" || w1 == "fwd_task_kb" || w1 == "lean_task_kb" || w1 == "thin_level_fronts") {

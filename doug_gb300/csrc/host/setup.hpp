@@ -41,6 +41,7 @@ struct Controls {
   int fwd_task_kb = 96;             // KB of E per forward task of a large front
   int lean_task_kb = 80;            // levels with smaller average tasks use 128-thread CTAs
   int thin_level_fronts = 304;      // levels with fewer small fronts solve them one CTA per task
+  int solve_schedule = 0;           // multifrontal solves: 0 one launch per level, 1 dependency-driven queue
 };
 
 // Parse one "name value" line the way util_actionOnCtrlArg does

@@ -23,11 +23,12 @@ def _ctl_text(d):
     return "".join(f"{k} {v}\n" for k, v in d.items())
 
 
-@pytest.mark.parametrize("word", ["panel_rows", "fwd_task_kb", "lean_task_kb", "thin_level_fronts"])
+@pytest.mark.parametrize("word", ["panel_rows", "fwd_task_kb", "lean_task_kb", "thin_level_fronts", "solve_schedule"])
 def test_tuning_words_reject_bad_values(word):
     s = D.DougSolver({})
-    s.set_option(word, 64)
-    for bad in ((-3, "x") if word == "thin_level_fronts" else (0, -3, "x")):
+    s.set_option(word, 1 if word == "solve_schedule" else 64)
+    for bad in ((-3, "x") if word == "thin_level_fronts" else (2, -1, "x") if word == "solve_schedule"
+                else (0, -3, "x")):
         with pytest.raises(D.DougError):
             s.set_option(word, bad)
 
@@ -43,7 +44,8 @@ def diffusion24():
 @pytest.mark.gpu
 @pytest.mark.parametrize("words", [dict(panel_rows=16), dict(panel_rows=48, fwd_task_kb=4, lean_task_kb=1),
                                    dict(fwd_task_kb=1024, lean_task_kb=4096), dict(nd_leaf=8),
-                                   dict(thin_level_fronts=0), dict(thin_level_fronts=100000)])
+                                   dict(thin_level_fronts=0), dict(thin_level_fronts=100000),
+                                   dict(solve_schedule=1), dict(solve_schedule=1, thin_level_fronts=0)])
 @pytest.mark.parametrize("precision", [0, 1])
 def test_batch_parameters_keep_the_solution(diffusion24, words, precision):
     n, r, c, v, b, ro = diffusion24

@@ -59,12 +59,14 @@ def test_multi_rhs_matches_oracle(precision):
 
 
 @pytest.mark.gpu
-def test_multi_rhs_3d_with_partition():
+@pytest.mark.parametrize("schedule", [0, 1])
+def test_multi_rhs_3d_with_partition(schedule):
     N = 14
     n, r, c, v, b = P.diffusion3d_fv(N, seed=9)
     part = P.block_partition(N, 2)
     opts = dict(OPTS, overlap=2)
     s = D.DougSolver(opts)
+    s.set_option("solve_schedule", schedule)
     s.set_matrix_coo(n, r, c, v)
     s.set_partition(part)
     s.setup()
