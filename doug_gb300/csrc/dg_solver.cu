@@ -457,12 +457,8 @@ struct MfDevice {
     CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_f, mf_fwd_queue<T>, 256, q_smem));
     CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_b, mf_bwd_queue<T>, 256, q_smem));
     q_grid = nsm * std::max(1, std::min(occ_f, occ_b));
-    q_k = 0;
-  }
-  void ensure_queue(int K) {
-    if (q_k == K) return;
-    q_done.alloc((size_t)(qf_n + qb_n) * K);
-    q_k = K;
+    q_done.alloc((size_t)(qf_n + qb_n));  // one right-hand side; ensure_multi grows it
+    q_k = 1;
   }
 
   // several right-hand sides: local vectors k at k*xlen (xlm, ylm) and k*ulen (um)
@@ -471,6 +467,10 @@ struct MfDevice {
   int64_t ulen = 0;
   void ensure_multi(int K) {
     if (mk == K) return;
+    if (queue && q_k < K) {
+      q_done.alloc((size_t)(qf_n + qb_n) * K);
+      q_k = K;
+    }
     xlm.alloc((size_t)xlen * K);
     ylm.alloc((size_t)xlen * K);
     um.alloc((size_t)std::max<int64_t>(ulen, 1) * K);
@@ -483,8 +483,7 @@ struct MfDevice {
     int launches = 0;
     T *xl_ = nrhs > 1 ? xlm.p : xl.p, *yl_ = nrhs > 1 ? ylm.p : yl.p, *u_ = nrhs > 1 ? um.p : u.p;
     const int64_t xs = nrhs > 1 ? xlen : 0, us = nrhs > 1 ? std::max<int64_t>(ulen, 1) : 0;
-    if (queue && status) {
-      ensure_queue(nrhs);
+    if (queue && status && q_k >= nrhs) {
       CK(cudaMemsetAsync(q_counter.p, 0, 2 * sizeof(int), s));
       CK(cudaMemsetAsync(q_done.p, 0, (size_t)(qf_n + qb_n) * nrhs * sizeof(int), s));
       mf_fwd_queue<T><<<q_grid, 256, q_smem, s>>>(view, QueueView{qf_tasks.p, qf_dep_ptr.p, qf_dep.p, qf_n},
