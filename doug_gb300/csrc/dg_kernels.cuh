@@ -1327,20 +1327,37 @@ __global__ void gather_subdomains(const double *__restrict__ r, const int *__res
 }
 
 // crhs (in the coarse batch's local numbering) = R r
-// nrhs right-hand sides: r_k at r + k * rs, the coarse vector k at xc + k * xcs
-template <typename TR>
-__global__ void restrict_to_coarse(const int64_t *__restrict__ Rp, const int *__restrict__ Rc,
-                                   const TR *__restrict__ Rv, const double *__restrict__ r,
-                                   const int *__restrict__ cpos, double *__restrict__ xc, int nc, int nrhs = 1,
-                                   int64_t rs = 0, int64_t xcs = 0) {
-  const int lane = threadIdx.x & 31;
-  const int warps = (gridDim.x * blockDim.x) >> 5;
-  for (int a = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; a < nc; a += warps) {
+// nrhs right-hand sides: r_k at r + k * rs, the coarse vector k at xc + k * xcs.
+// L lanes per coarse row (chosen for about 12 entries per lane), four loads
+// in flight per lane, the lane sums added by a shuffle tree.
+template <typename TR, int L>
+__global__ void __launch_bounds__(kVecThreads)
+restrict_to_coarse(const int64_t *__restrict__ Rp, const int *__restrict__ Rc, const TR *__restrict__ Rv,
+                   const double *__restrict__ r, const int *__restrict__ cpos, double *__restrict__ xc, int nc,
+                   int nrhs = 1, int64_t rs = 0, int64_t xcs = 0) {
+  const int sub = threadIdx.x % L;
+  const int rows_per_grid = gridDim.x * (kVecThreads / L);
+  for (int a0 = blockIdx.x * (kVecThreads / L); a0 < nc; a0 += rows_per_grid) {
+    const int a = a0 + threadIdx.x / L;
+    const bool on = a < nc;
+    const int64_t e0 = on ? Rp[a] : 0, e1 = on ? Rp[a + 1] : 0;
     for (int k = 0; k < nrhs; k++) {
+      const double *rk = r + k * rs;
       double s = 0.0;
-      for (int64_t e = Rp[a] + lane; e < Rp[a + 1]; e += 32) s += (double)Rv[e] * r[k * rs + Rc[e]];
-      s = warp_sum(s);
-      if (lane == 0) xc[k * xcs + cpos[a]] = s;
+      int64_t e = e0 + sub;
+      for (; e + 3 * L < e1; e += 4 * L) {
+        const int c0 = Rc[e], c1 = Rc[e + L], c2 = Rc[e + 2 * L], c3 = Rc[e + 3 * L];
+        const double v0 = (double)Rv[e], v1 = (double)Rv[e + L], v2 = (double)Rv[e + 2 * L], v3 = (double)Rv[e + 3 * L];
+        const double x0 = rk[c0], x1 = rk[c1], x2 = rk[c2], x3 = rk[c3];
+        s += v0 * x0;
+        s += v1 * x1;
+        s += v2 * x2;
+        s += v3 * x3;
+      }
+      for (; e < e1; e += L) s += (double)Rv[e] * rk[Rc[e]];
+#pragma unroll
+      for (int o = L / 2; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o, L);
+      if (on && sub == 0) xc[k * xcs + cpos[a]] = s;
     }
   }
 }
@@ -1597,7 +1614,7 @@ __global__ void cg_finish(double *__restrict__ sc, const double *__restrict__ pa
 // frozen while the others go on, which makes each system's iterates those of
 // its own PCG.
 // ---------------------------------------------------------------------------
-constexpr int kBatchChunk = 2048;  // rows per CTA of the batched vector kernels
+constexpr int kBatchChunk = 1024;  // rows per CTA of the batched vector kernels
 enum { BS_RHO_PREV = 0, BS_RHO = 1, BS_ALPHA = 2, BS_RES = 3, BS_INIT = 4, BS_BETA = 5, BS_PQ = 6,
        BS_TRUE = 7, BS_N = 8 };
 // per-system state

@@ -726,6 +726,7 @@ struct dg_handle {
   double t_setup = 0;
   int precision = 0;
   int lanes = 8;
+  int r_lanes = 32;               // lanes per row of the restriction R
   // device
   int device = 0;
   DBuf<int64_t> Ap, Rp, Pp;
@@ -868,6 +869,20 @@ void resid_any(int lanes, int grid, cudaStream_t s, dg_handle *h, const double *
     case 8: launch_resid<8>(grid, s, h, xx, bb, rr); break;
     case 16: launch_resid<16>(grid, s, h, xx, bb, rr); break;
     default: launch_resid<32>(grid, s, h, xx, bb, rr); break;
+  }
+}
+
+// x_c = R r with L lanes per coarse row
+template <typename TR>
+void restrict_any(int lanes, int grid, cudaStream_t s, const int64_t *Rp, const int *Rc, const TR *Rv, const double *r,
+                  const int *cpos, double *xc, int nc, int K, int64_t rs, int64_t xcs) {
+  switch (lanes) {
+    case 1: restrict_to_coarse<TR, 1><<<grid, kVecThreads, 0, s>>>(Rp, Rc, Rv, r, cpos, xc, nc, K, rs, xcs); break;
+    case 2: restrict_to_coarse<TR, 2><<<grid, kVecThreads, 0, s>>>(Rp, Rc, Rv, r, cpos, xc, nc, K, rs, xcs); break;
+    case 4: restrict_to_coarse<TR, 4><<<grid, kVecThreads, 0, s>>>(Rp, Rc, Rv, r, cpos, xc, nc, K, rs, xcs); break;
+    case 8: restrict_to_coarse<TR, 8><<<grid, kVecThreads, 0, s>>>(Rp, Rc, Rv, r, cpos, xc, nc, K, rs, xcs); break;
+    case 16: restrict_to_coarse<TR, 16><<<grid, kVecThreads, 0, s>>>(Rp, Rc, Rv, r, cpos, xc, nc, K, rs, xcs); break;
+    default: restrict_to_coarse<TR, 32><<<grid, kVecThreads, 0, s>>>(Rp, Rc, Rv, r, cpos, xc, nc, K, rs, xcs); break;
   }
 }
 
@@ -1192,6 +1207,7 @@ dg_status do_setup(dg_handle *h, bool reuse_host = false) {
     if (h->iter_exec) { cudaGraphExecDestroy(h->iter_exec); h->iter_exec = nullptr; }
     // transfer operators
     h->Rp.upload(S.R.ptr); h->Rc.upload(S.R.col); h->Rv.upload(S.R.val);
+    h->r_lanes = lanes_for(S.R);
     h->Pp.upload(S.P.ptr); h->Pv.upload(S.P.val);
     std::vector<float> rf(S.R.val.begin(), S.R.val.end()), pf(S.P.val.begin(), S.P.val.end());
     h->Rvf.upload(rf); h->Pvf.upload(pf);
@@ -1320,12 +1336,10 @@ int precondition(dg_handle *h, const SolvePlan &pl, cudaStream_t st, bool profil
     CK(cudaEventRecord(h->fork_ev, st));
     CK(cudaStreamWaitEvent(h->s2, h->fork_ev, 0));
     if (profile) CK(cudaEventRecord(h->ev[4], h->s2));
-    if (pl.mixed)
-      restrict_to_coarse<float><<<grid, kVecThreads, 0, h->s2>>>(h->Rp.p, h->Rc.p, h->Rvf.p, a.v.r, h->cpos.p, xc_buf,
-                                                                  h->S.R.nrows, K, vs, xcs);
-    else
-      restrict_to_coarse<double><<<grid, kVecThreads, 0, h->s2>>>(h->Rp.p, h->Rc.p, h->Rv.p, a.v.r, h->cpos.p, xc_buf,
-                                                                   h->S.R.nrows, K, vs, xcs);
+    if (pl.mixed) restrict_any<float>(h->r_lanes, grid, h->s2, h->Rp.p, h->Rc.p, h->Rvf.p, a.v.r, h->cpos.p, xc_buf,
+                                       h->S.R.nrows, K, vs, xcs);
+    else restrict_any<double>(h->r_lanes, grid, h->s2, h->Rp.p, h->Rc.p, h->Rv.p, a.v.r, h->cpos.p, xc_buf,
+                              h->S.R.nrows, K, vs, xcs);
     nl += 1 + co->solve(h->s2, K, h->status.p);
     if (profile) CK(cudaEventRecord(h->ev[5], h->s2));
     CK(cudaEventRecord(h->join_ev, h->s2));
