@@ -15,6 +15,7 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libdouggpu.so")
+CLI = os.path.join(OUT, "doug_gpu")       # command-line driver (flags of the reference's executables)
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 
 HOST_SRC = ["host/setup.cpp", "host/mf_symbolic.cpp"]
@@ -70,6 +71,10 @@ def build(force: bool = False, verbose: bool = False) -> str:
             print(l)
     if force or jobs or not os.path.exists(LIB):
         _run([nvcc, ARCH, "-shared", "-o", LIB] + objs + ["-lpthread"])
+    cli_src = os.path.join(CSRC, "doug_gpu_main.cpp")
+    if force or _stale(CLI, [cli_src, LIB, os.path.join(ROOT, "include", "doug_gpu.h")]):
+        _run(["g++", "-std=c++17", "-O2", "-Wall", cli_src, "-o", CLI, "-L" + OUT, "-ldouggpu",
+              "-Wl,-rpath,$ORIGIN"])
     return LIB
 
 
