@@ -75,6 +75,8 @@ struct MfTune {
   int64_t lean_task_bytes = 80 * 1024;   // levels with smaller average tasks use 128-thread CTAs
   int small_min_fronts = 304;            // levels with fewer small fronts solve them CTA-per-task
   int schedule = 0;                      // solves: 0 one launch per level, 1 dependency-driven queue
+  int tiny_rows = 64;                    // panel fronts of at most this many rows: tiny_threads per CTA
+  int tiny_threads = 64;
 };
 
 template <typename T>
@@ -82,6 +84,7 @@ struct MfDevice {
   DBuf<int64_t> f_off, f_rows, f_xoff, f_uoff, f_woff, f_relmap, f_asm, asm_tgt, asm_sp, asm_src, e_off;
   DBuf<int> f_m, f_k, f_p0, f_child_ptr, f_children, rows, relmap, lvl_fronts, gidx;
   DBuf<int> pan_fronts, diag_fronts, solve_small;
+  int tiny_threads = 64;
   // dependency-driven schedule of the solves (solve_schedule 1)
   bool queue = false;
   DBuf<int4> qf_tasks, qb_tasks;
@@ -104,6 +107,8 @@ struct MfDevice {
   };
   struct Level {
     int pan_off, pan_cnt, asm_off, asm_cnt, pan_maxm;
+    int tiny_off, tiny_cnt;        // panel fronts of at most tune.tiny_rows rows: narrow CTAs
+    size_t tiny_smem;
     size_t pan_smem;
     std::vector<Step> steps;
   };
@@ -162,24 +167,32 @@ struct MfDevice {
     levels.assign((size_t)nlevels, Level());
     for (int l = 0; l < nlevels; l++) {
       Level &L = levels[(size_t)l];
-      L.pan_off = (int)pn.size();
       L.pan_smem = 0;
       L.pan_maxm = 0;
+      L.tiny_smem = 0;
       L.asm_off = (int)at.size();
-      std::vector<int> large;
+      std::vector<int> large, tiny, pan;
       for (int q = B.lvl_ptr[(size_t)l]; q < B.lvl_ptr[(size_t)l + 1]; q++) {
         int f = B.lvl_fronts[(size_t)q];
         int m = B.f_m[(size_t)f], k = B.f_k[(size_t)f];
         const size_t smem = (size_t)2 * m * k * sizeof(T);
-        if (m <= tune.panel_rows && smem <= kPanelSmem) {
-          pn.push_back(f);
+        if (m <= tune.tiny_rows) {
+          tiny.push_back(f);
+          L.tiny_smem = std::max(L.tiny_smem, smem);
+        } else if (m <= tune.panel_rows && smem <= kPanelSmem) {
+          pan.push_back(f);
           L.pan_smem = std::max(L.pan_smem, smem);
           L.pan_maxm = std::max(L.pan_maxm, m);
         } else {
           large.push_back(f);
         }
       }
-      L.pan_cnt = (int)pn.size() - L.pan_off;
+      L.tiny_off = (int)pn.size();
+      pn.insert(pn.end(), tiny.begin(), tiny.end());
+      L.tiny_cnt = (int)tiny.size();
+      L.pan_off = (int)pn.size();
+      pn.insert(pn.end(), pan.begin(), pan.end());
+      L.pan_cnt = (int)pan.size();
       int kmax = 0;
       for (int f : large) {
         int m = B.f_m[(size_t)f];
@@ -319,6 +332,7 @@ struct MfDevice {
     set_solve_attrs<kEThreads>(optin, fwd_smem_max, bwd_smem_max);
     set_solve_attrs<kELeanThreads>(optin, fwd_smem_max, bwd_smem_max);
     queue = tune.schedule == 1;
+    tiny_threads = tune.tiny_threads;
     if (queue) plan_queue(B, ss, fw, bw, fwd_smem_max, bwd_smem_max);
   }
 
@@ -339,6 +353,11 @@ struct MfDevice {
     int launches = 0;
     for (int l = 0; l < nlevels; l++) {
       const Level &L = levels[(size_t)l];
+      if (L.tiny_cnt) {  // small fronts: narrow CTAs, more of them per SM
+        mf_factor_panel<T><<<L.tiny_cnt, tiny_threads, L.tiny_smem, s>>>(view, pan_fronts.p + L.tiny_off, vals,
+                                                                         arena.p, E.p, status);
+        launches++;
+      }
       if (L.pan_cnt) {
         mf_factor_panel<T><<<L.pan_cnt, L.pan_maxm > kPanWideRows ? kPanThreadsWide : kPanThreads, L.pan_smem, s>>>(view, pan_fronts.p + L.pan_off, vals,
                                                                       arena.p, E.p, status);
