@@ -746,6 +746,7 @@ struct dg_handle {
   int precision = 0;
   int lanes = 8;
   int r_lanes = 32;               // lanes per row of the restriction R
+  int pull_grid = kRedBlocks;     // CTAs of the single-system pull kernel: one wave
   // device
   int device = 0;
   DBuf<int64_t> Ap, Rp, Pp;
@@ -1227,6 +1228,16 @@ dg_status do_setup(dg_handle *h, bool reuse_host = false) {
     // transfer operators
     h->Rp.upload(S.R.ptr); h->Rc.upload(S.R.col); h->Rv.upload(S.R.val);
     h->r_lanes = lanes_for(S.R);
+    {  // the pull kernel holds 64 registers: a 1024-CTA grid would be 1.7 waves
+      int dev = 0, nsm = 0, occ = 0;
+      CK(cudaGetDevice(&dev));
+      CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+      if (c.precision == 1)
+        CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, pull_prolong_dot<float, float>, kVecThreads, 0));
+      else
+        CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, pull_prolong_dot<double, double>, kVecThreads, 0));
+      h->pull_grid = std::max(1, std::min(kRedBlocks, nsm * std::max(occ, 1)));
+    }
     h->Pp.upload(S.P.ptr); h->Pv.upload(S.P.val);
     std::vector<float> rf(S.R.val.begin(), S.R.val.end()), pf(S.P.val.begin(), S.P.val.end());
     h->Rvf.upload(rf); h->Pvf.upload(pf);
@@ -1701,7 +1712,7 @@ dg_status do_solve(dg_handle *h, const double *d_b, double *d_x, dg_stats *st, c
       sa.v = Vecs{h->b.p, h->x.p, h->r.p, h->p.p, h->q.p, h->z.p, h->zold.p};
       sa.part_rz = h->part_rz.p;
       sa.part_rzo = h->part_rzo.p;
-      sa.pg = grid;
+      sa.pg = h->pull_grid;
       int nl = precondition(h, pl, st, profile, sa);
       if (profile) CK(cudaEventRecord(h->ev[6], st));
       spmv_any(h->lanes, grid, st, h, first, mixed ? 1 : 0);
