@@ -40,7 +40,7 @@ EXPORTED_SYMBOLS = [
     "dg_get_subdomains", "dg_get_restriction", "dg_get_coarse_matrix", "dg_residual_csr",
     "dg_set_elements", "dg_get_input", "dg_grad_matrix", "dg_grad_elements",
     "dg_residual_csr_noalloc", "dg_autotune", "dg_set_systems", "dg_get_system_stats",
-    "dg_solve_multi", "dg_solve_multi_device",
+    "dg_solve_multi", "dg_solve_multi_device", "dg_set_node_geometry", "dg_get_coarse_coords",
 ]
 
 
@@ -119,6 +119,8 @@ def load_library(path: str | None = None):
     L.dg_solve_multi.argtypes = [vp, C.c_int, P(C.c_double), P(C.c_double), P(_Stats)]
     L.dg_solve_multi_device.argtypes = [vp, C.c_int, vp, vp, P(_Stats), vp]
     L.dg_set_elements.argtypes = [vp, C.c_int, C.c_int, P(C.c_int), P(C.c_int), P(C.c_double), P(C.c_double)]
+    L.dg_set_node_geometry.argtypes = [vp, C.c_int, C.c_int, P(C.c_double), P(C.c_int)]
+    L.dg_get_coarse_coords.argtypes = [vp, P(C.c_int), P(C.c_int), P(C.c_double)]
     L.dg_get_input.argtypes = [vp, P(C.c_int), P(C.c_int), P(C.c_int), P(C.c_int), P(C.c_double),
                                P(C.c_double)]
     L.dg_set_partition.argtypes = [vp, P(C.c_int), C.c_int]
@@ -215,6 +217,22 @@ class DougSolver:
         em = np.ascontiguousarray(emat, dtype=np.float64)
         er = np.ascontiguousarray(erhs, dtype=np.float64)
         self._check(self._L.dg_set_elements(self._h, len(ep) - 1, int(ngf), _ip(ep), _ip(ef), _dp(em), _dp(er)))
+
+    def set_node_geometry(self, coords, freemap) -> None:
+        """Node coordinates (nnode x nsd, nsd 2 or 3) and the 1-based node of
+        every global freedom, after set_elements: the input of doug_geom's
+        geometric coarse grid (control word executable geom, levels 2)."""
+        xyz = np.ascontiguousarray(coords, dtype=np.float64)
+        fm = np.ascontiguousarray(freemap, dtype=np.int32)
+        self._check(self._L.dg_set_node_geometry(self._h, xyz.shape[1], xyz.shape[0], _dp(xyz), _ip(fm)))
+
+    def coarse_coords(self):
+        """Coordinates of the geometric coarse grid's coarse freedoms, one row each."""
+        nsd, nc = C.c_int(), C.c_int()
+        self._check(self._L.dg_get_coarse_coords(self._h, C.byref(nsd), C.byref(nc), None))
+        buf = np.zeros(nsd.value * nc.value, dtype=np.float64)
+        self._check(self._L.dg_get_coarse_coords(self._h, None, None, _dp(buf)))
+        return buf.reshape(nc.value, nsd.value)
 
     def grad_matrix(self, d_lambda: int, d_x: int, d_grad: int, stream: int = 0) -> None:
         """d_grad[k] = -lambda[row_k] x[col_k] per input triplet (device pointers)."""

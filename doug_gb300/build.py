@@ -18,7 +18,7 @@ LIB = os.path.join(OUT, "libdouggpu.so")
 CLI = os.path.join(OUT, "doug_gpu")       # command-line driver (flags of the reference's executables)
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 
-HOST_SRC = ["host/setup.cpp", "host/mf_symbolic.cpp"]
+HOST_SRC = ["host/setup.cpp", "host/geom.cpp", "host/mf_symbolic.cpp"]
 CUDA_SRC = ["dg_solver.cu", "dg_residual.cu"]
 
 

@@ -714,6 +714,11 @@ struct dg_handle {
   // every element freedom, element offsets, matrices
   bool have_elements = false;
   std::vector<int> el_eptr, el_local;
+  std::vector<int> el_free, el_lg;  // global freedoms of the elements; global freedom of every unknown
+  int el_ngf = 0;
+  // node coordinates of elemental input (the geometric coarse grid of doug_geom)
+  bool have_geometry = false;
+  NodeGeometry geo;
   std::vector<int64_t> el_off;
   std::vector<double> el_mat;
   DBuf<int> d_el_eptr, d_el_local, d_gi, d_gj, d_el_run, d_el_ridx;
@@ -1076,7 +1081,13 @@ dg_status do_setup(dg_handle *h, bool reuse_host = false) {
   ctl_finish(c);
   double t0 = wall();
   if (!(reuse_host && h->S.n == h->n && h->S.n > 0)) {
-    if (h->nsys > 0) {
+    if (c.executable == 1) {  // doug_geom (geom.F90:62-116)
+      if (h->nsys > 0) return fail(h, DG_BAD_INPUT, "batched systems run the doug_aggr setup only");
+      if (!build_setup_geom(c, h->n, h->ii, h->jj, h->vv, h->part.empty() ? nullptr : &h->part, h->nparts,
+                            h->have_elements ? &h->el_free : nullptr, h->have_elements ? &h->el_lg : nullptr,
+                            h->have_geometry ? &h->geo : nullptr, h->S, err))
+        return fail(h, DG_BAD_INPUT, err);
+    } else if (h->nsys > 0) {
       if (!h->part.empty()) return fail(h, DG_BAD_INPUT, "a partition vector cannot be combined with batched systems");
       if (!build_setup_systems(c, h->sys_row, h->sys_tri, h->ii, h->jj, h->vv, h->S, err))
         return fail(h, DG_BAD_INPUT, err);
@@ -1920,7 +1931,11 @@ static dg_status set_elements(dg_handle *h, const ElementMesh &M) {
   for (size_t q = 0; q < M.efree.size(); q++) h->el_local[q] = gl[(size_t)M.efree[q]];
   h->el_off = M.emat_off;
   h->el_mat = M.emat;
+  h->el_free = M.efree;
+  h->el_lg = lg;
+  h->el_ngf = M.ngf;
   h->have_elements = true;
+  h->have_geometry = false;
   return DG_OK;
 }
 
@@ -1942,7 +1957,16 @@ dg_status dg_load_ctl(dg_handle *h, const char *path) {
     if (!read_elemental(resolve(h->ctl_dir, c.info_file), resolve(h->ctl_dir, c.freedom_lists_file),
                         resolve(h->ctl_dir, c.elemmat_rhs_file), c.number_of_blocks, M, err))
       return fail(h, DG_BAD_INPUT, err);
-    return set_elements(h, M);
+    dg_status st = set_elements(h, M);
+    if (st != DG_OK || c.coords_file.empty() || c.freemap_file.empty()) return st;
+    // Mesh_readFileCoords / Mesh_readFileFreemap (Mesh.F90:470-520)
+    NodeGeometry G;
+    if (!read_geometry(resolve(h->ctl_dir, c.coords_file), resolve(h->ctl_dir, c.freemap_file), M.nsd, M.nnode,
+                       M.ngf, G, err))
+      return fail(h, DG_BAD_INPUT, err);
+    h->geo = std::move(G);
+    h->have_geometry = true;
+    return DG_OK;
   }
   if (c.input_type == 3) {  // generated structured problem (Distribution.F90:67-70)
     int n = 0;
@@ -2063,6 +2087,34 @@ dg_status dg_set_elements(dg_handle *h, int nell, int ngf, const int *eptr, cons
   std::string err;
   if (!check_elements(M, err)) return fail(h, DG_BAD_INPUT, err);
   return set_elements(h, M);
+}
+
+dg_status dg_set_node_geometry(dg_handle *h, int nsd, int nnode, const double *coords, const int *freemap) {
+  if (!h || nsd < 2 || nsd > 3 || nnode <= 0 || !coords || !freemap) return DG_BAD_INPUT;
+  if (!h->have_elements) return fail(h, DG_NOT_READY, "node geometry: give the elements first");
+  NodeGeometry G;
+  G.nsd = nsd;
+  G.nnode = nnode;
+  G.coords.assign(coords, coords + (size_t)nsd * nnode);
+  G.freemap.assign(freemap, freemap + h->el_ngf);
+  for (int f = 0; f < h->el_ngf; f++)
+    if (G.freemap[(size_t)f] < 1 || G.freemap[(size_t)f] > nnode)
+      return fail(h, DG_BAD_INPUT, "freemap: freedom " + std::to_string(f + 1) + " maps to node " +
+                                       std::to_string(G.freemap[(size_t)f]));
+  h->geo = std::move(G);
+  h->have_geometry = true;
+  h->S.n = 0;
+  h->ready = false;
+  return DG_OK;
+}
+
+dg_status dg_get_coarse_coords(const dg_handle *h, int *nsd, int *ncoarse, double *xyz) {
+  if (!h || h->S.coarse_xyz.empty() || !h->have_geometry) return DG_NOT_READY;
+  const int d = h->geo.nsd;
+  if (nsd) *nsd = d;
+  if (ncoarse) *ncoarse = (int)(h->S.coarse_xyz.size() / (size_t)d);
+  if (xyz) std::copy(h->S.coarse_xyz.begin(), h->S.coarse_xyz.end(), xyz);
+  return DG_OK;
 }
 
 dg_status dg_set_rhs(dg_handle *h, const double *b) {

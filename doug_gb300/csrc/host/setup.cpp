@@ -139,7 +139,14 @@ bool ctl_apply(Controls &c, const std::string &w1, const std::string &w2, std::s
   TRY(S("freemap_file", c.freemap_file))
   TRY(S("solution_file", c.solution_file)) TRY(I("solution_format", c.solution_format))
   TRY(I("start_vec_type", c.start_vec_type))
+  TRY(I("maxcie", c.maxcie)) TRY(I("maxnd", c.maxnd)) TRY(I("cutbal", c.cutbal))
+  TRY(I("center_type", c.center_type)) TRY(L("hanging_nodes", c.hanging_nodes))
 #undef TRY
+  if (w1 == "executable") {  // not a reference word: doug_aggr (aggr) or doug_geom (geom)
+    if (w2 != "aggr" && w2 != "geom") { err = "executable must be aggr or geom: '" + w2 + "'"; return false; }
+    if (c.executable == -1) c.executable = w2 == "geom" ? 1 : 0;
+    return true;
+  }
   return true;  // unknown words are ignored
 }
 
@@ -174,6 +181,7 @@ bool ctl_parse_text(Controls &c, const std::string &text, std::string &err) {
 
 void ctl_finish(Controls &c) {
   if (c.solve_maxiters == -1) c.solve_maxiters = 100;
+  if (c.executable == 1) c.fine_method = 1;
 }
 
 // ---------------------------------------------------------------------------
@@ -416,6 +424,35 @@ bool read_elemental(const std::string &info, const std::string &freelists, const
   return check_elements(M, err);
 }
 
+bool read_geometry(const std::string &coords_path, const std::string &freemap_path, int nsd, int nnode, int ngf,
+                   NodeGeometry &G, std::string &err) {
+  if (nsd < 1 || nsd > 3 || nnode < 1 || ngf < 1) { err = "node geometry: bad sizes in the info file"; return false; }
+  std::vector<unsigned char> b, rec;
+  size_t pos = 0;
+  if (!slurp(coords_path, b) || !fortran_record(b, pos, rec) || rec.size() < (size_t)8 * nsd * nnode) {
+    err = "cannot read node coordinates from " + coords_path;
+    return false;
+  }
+  G.nsd = nsd;
+  G.nnode = nnode;
+  G.coords.resize((size_t)nsd * nnode);
+  for (size_t q = 0; q < G.coords.size(); q++) G.coords[q] = rd_led(rec.data() + 8 * q);
+  pos = 0;
+  if (!slurp(freemap_path, b) || !fortran_record(b, pos, rec) || rec.size() < (size_t)4 * ngf) {
+    err = "cannot read the freedom map from " + freemap_path;
+    return false;
+  }
+  G.freemap.resize((size_t)ngf);
+  for (int f = 0; f < ngf; f++) {
+    G.freemap[(size_t)f] = (int32_t)rd_le32(rec.data() + 4 * f);
+    if (G.freemap[(size_t)f] < 1 || G.freemap[(size_t)f] > nnode) {
+      err = "freemap: freedom " + std::to_string(f + 1) + " maps to node " + std::to_string(G.freemap[(size_t)f]);
+      return false;
+    }
+  }
+  return true;
+}
+
 bool check_elements(const ElementMesh &M, std::string &err) {
   if (M.nell <= 0 || M.ngf <= 0 || (int)M.eptr.size() != M.nell + 1 || M.eptr[0] != 0) {
     err = "elements: bad element count or freedom list offsets";
@@ -567,13 +604,6 @@ bool write_solution(const std::string &path, int format, const double *x, int n,
 // ---------------------------------------------------------------------------
 // sparse helpers with DOUG's ordering semantics
 // ---------------------------------------------------------------------------
-struct Coo {  // triplets in a definite order, 0-based
-  int nrows = 0, ncols = 0;
-  std::vector<int> i, j;
-  std::vector<double> v;
-  size_t size() const { return v.size(); }
-};
-
 // stable bucketing by row (SpMtx_arrange ROWS, sort=.false.)
 static Csr rows_of(const Coo &m) {
   Csr c;
@@ -1165,6 +1195,164 @@ static Coo smoother(const Csr &A, const std::vector<char> &strong, double omega,
   return S;
 }
 
+// CoarseMtxBuild (CoarseMtx.F90:476-516): T = A R^T (R arranged by columns),
+// AC = R T with R's rows re-bucketed from that column order.  Fills out.R
+// (rows = coarse freedoms, columns ascending), out.P (= R^T, coarse freedoms
+// ascending per fine node) and R's final COO order in out.R_i/R_j/R_v.
+static Csr galerkin(const Csr &A, const Coo &Rcoo, int n, SetupResult &out) {
+  Csr Rcols = cols_of(Rcoo);                 // column view: for each fine node, coarse freedoms ascending
+  Csr Tm = spgemm_first_touch(A, Rcols);     // n x ncoarse
+  Coo RcolOrder;                             // R's COO after arrangement by columns
+  RcolOrder.nrows = Rcoo.nrows; RcolOrder.ncols = Rcoo.ncols;
+  RcolOrder.i.reserve(Rcoo.size()); RcolOrder.j.reserve(Rcoo.size()); RcolOrder.v.reserve(Rcoo.size());
+  for (int col = 0; col < Rcols.nrows; col++)
+    for (int64_t k = Rcols.ptr[(size_t)col]; k < Rcols.ptr[(size_t)col + 1]; k++) {
+      RcolOrder.i.push_back(Rcols.col[(size_t)k]);
+      RcolOrder.j.push_back(col);
+      RcolOrder.v.push_back(Rcols.val[(size_t)k]);
+    }
+  out.R = rows_of(RcolOrder);
+  out.P = Rcols;
+  out.P.nrows = n; out.P.ncols = Rcoo.nrows;
+  Csr AC = spgemm_first_touch(out.R, Tm);
+  out.R_i.clear(); out.R_j.clear(); out.R_v.clear();
+  out.R_i.reserve(RcolOrder.size()); out.R_j.reserve(RcolOrder.size()); out.R_v.reserve(RcolOrder.size());
+  for (size_t k = 0; k < RcolOrder.size(); k++) {
+    out.R_i.push_back(RcolOrder.i[k] + 1); out.R_j.push_back(RcolOrder.j[k] + 1);
+    out.R_v.push_back(RcolOrder.v[k]);
+  }
+  return AC;
+}
+
+// Add_layers (Decomposition.f90:56-99) for every node list in turn: each
+// subdomain is its list grown by `overlap` breadth-first layers over the
+// pattern of A; appended to out.sd_ptr / out.sd_nodes (1-based ids)
+static void grow_subdomains(const Csr &A, const std::vector<std::vector<int>> &lists, int overlap, SetupResult &out) {
+  const int n = A.nrows;
+  out.sd_ptr.assign(1, 0);
+  out.sd_nodes.clear();
+  std::vector<int> onfront((size_t)n, 0), nodes;
+  for (const auto &base : lists) {
+    nodes = base;
+    for (int v : nodes) onfront[(size_t)v] = -1;
+    size_t lo = 0, hi = nodes.size();
+    for (int layer = 1; layer <= overlap; layer++) {
+      for (size_t q = lo; q < hi; q++) {
+        int v = nodes[q];
+        for (int64_t k = A.ptr[(size_t)v]; k < A.ptr[(size_t)v + 1]; k++) {
+          int w = A.col[(size_t)k];
+          if (onfront[(size_t)w] == 0) { onfront[(size_t)w] = layer; nodes.push_back(w); }
+        }
+      }
+      lo = hi;
+      hi = nodes.size();
+    }
+    for (int v : nodes) { onfront[(size_t)v] = 0; out.sd_nodes.push_back(v + 1); }
+    out.sd_ptr.push_back((int64_t)out.sd_nodes.size());
+  }
+}
+
+// 1-based triplets (0-based accepted, SpMtx_class.F90:441-444) to 0-based COO
+static bool triplets(int n, const std::vector<int> &ii, const std::vector<int> &jj, const std::vector<double> &vv,
+                     Coo &A0, std::string &err) {
+  size_t nnz = vv.size();
+  int shift = (nnz > 0 && ii[0] == 0) ? 1 : 0;
+  A0 = Coo();
+  A0.nrows = n; A0.ncols = n;
+  A0.i.resize(nnz); A0.j.resize(nnz); A0.v = vv;
+  for (size_t k = 0; k < nnz; k++) {
+    int a = ii[k] + shift - 1, b = jj[k] + shift - 1;
+    if (a < 0 || a >= n || b < 0 || b >= n) {
+      err = "matrix entry " + std::to_string(k + 1) + " out of range";
+      return false;
+    }
+    A0.i[k] = a; A0.j[k] = b;
+  }
+  return true;
+}
+
+bool build_setup_geom(const Controls &c_in, int n, const std::vector<int> &ii, const std::vector<int> &jj,
+                      const std::vector<double> &vv, const std::vector<int> *part, int nparts,
+                      const std::vector<int> *efree, const std::vector<int> *lg_fmap, const NodeGeometry *G,
+                      SetupResult &out, std::string &err) {
+  Controls c = c_in;
+  out = SetupResult();
+  out.n = n;
+  PhaseTimer tm;
+  if (c.method == 2 || c.method == 3) {
+    err = "method " + std::to_string(c.method) +
+          " restricts a residual the one-process reference never sets (pcg.F90:146-149)";
+    return false;
+  }
+  if (c.levels > 2) { err = "doug_geom builds no coarse level for levels " + std::to_string(c.levels); return false; }
+  if (c.levels == 2 && (c.input_type != 1 || !efree || !lg_fmap || !G)) {
+    err = "the geometric coarse grid needs elemental input with node coordinates (coords_file, freemap_file)";
+    return false;
+  }
+  Coo A0;
+  if (!triplets(n, ii, jj, vv, A0, err)) return false;
+  const Csr A = rows_of(A0);  // FinePreconditioner_Init arranges A by rows (Preconditioner_base.F90:109)
+  out.fine.num.assign((size_t)n, 0);
+  out.fine_full.num.assign((size_t)n, 0);
+  out.overlap = c.overlap < 0 ? std::max(c.smoothers, 0) : c.overlap;  // geom.F90:96-100, before the coarse init
+  out.levels = c.levels;
+  std::vector<std::vector<int>> lists;
+  if (part) {
+    lists.resize((size_t)nparts);
+    for (int i = 0; i < n; i++) lists[(size_t)(*part)[(size_t)i] - 1].push_back(i);
+  } else {
+    lists.resize(1);
+    for (int i = 0; i < n; i++) lists[0].push_back(i);
+  }
+  grow_subdomains(A, lists, out.overlap, out);
+  tm.lap("subdomains + overlap");
+  out.smoothers = c.smoothers;
+  if (c.levels == 2) {
+    out.smoothers = 0;  // CoarsePreconditioner_geometric.F90:53
+    Coo Rcoo;
+    std::vector<double> cxyz;
+    if (!geometric_restriction(c, *efree, *G, *lg_fmap, Rcoo, cxyz, err)) return false;
+    tm.lap("geometric coarse grid");
+    Csr AC = galerkin(A, Rcoo, n, out);
+    out.AC_i.reserve(AC.col.size()); out.AC_j.reserve(AC.col.size()); out.AC_v.reserve(AC.col.size());
+    for (int r = 0; r < AC.nrows; r++)
+      for (int64_t k = AC.ptr[(size_t)r]; k < AC.ptr[(size_t)r + 1]; k++) {
+        out.AC_i.push_back(r + 1); out.AC_j.push_back(AC.col[(size_t)k] + 1); out.AC_v.push_back(AC.val[(size_t)k]);
+      }
+    out.coarse_xyz = cxyz;
+    const std::vector<int> keep = independent_coarse(AC);
+    const int nk = keep.empty() ? 0 : *std::max_element(keep.begin(), keep.end());
+    if (nk < AC.nrows) {  // the solve uses the independent coarse freedoms only
+      Coo Rs, ACs;
+      Rs.nrows = nk; Rs.ncols = n;
+      for (size_t k = 0; k < Rcoo.size(); k++)
+        if (keep[(size_t)Rcoo.i[k]]) { Rs.i.push_back(keep[(size_t)Rcoo.i[k]] - 1); Rs.j.push_back(Rcoo.j[k]); Rs.v.push_back(Rcoo.v[k]); }
+      ACs.nrows = ACs.ncols = nk;
+      for (int r = 0; r < AC.nrows; r++)
+        for (int64_t k = AC.ptr[(size_t)r]; k < AC.ptr[(size_t)r + 1]; k++)
+          if (keep[(size_t)r] && keep[(size_t)AC.col[(size_t)k]]) {
+            ACs.i.push_back(keep[(size_t)r] - 1); ACs.j.push_back(keep[(size_t)AC.col[(size_t)k]] - 1);
+            ACs.v.push_back(AC.val[(size_t)k]);
+          }
+      Csr Rcols = cols_of(Rs);
+      out.P = Rcols;
+      out.P.nrows = n; out.P.ncols = nk;
+      Coo Rc;  // by columns, then rows
+      Rc.nrows = nk; Rc.ncols = n;
+      for (int col = 0; col < Rcols.nrows; col++)
+        for (int64_t k = Rcols.ptr[(size_t)col]; k < Rcols.ptr[(size_t)col + 1]; k++) {
+          Rc.i.push_back(Rcols.col[(size_t)k]); Rc.j.push_back(col); Rc.v.push_back(Rcols.val[(size_t)k]);
+        }
+      out.R = rows_of(Rc);
+      AC = rows_of(ACs);
+    }
+    out.AC = AC;
+    tm.lap("restriction + Galerkin");
+  }
+  out.A = A;
+  return true;
+}
+
 bool build_setup(const Controls &c_in, int n, const std::vector<int> &ii, const std::vector<int> &jj,
                  const std::vector<double> &vv, const std::vector<int> *part, int nparts,
                  SetupResult &out, std::string &err, const RobustHook *robust) {
@@ -1191,19 +1379,8 @@ bool build_setup(const Controls &c_in, int n, const std::vector<int> &ii, const 
     err = "coarse_method 2 (robust coarse space) needs the device B-solve";
     return false;
   }
-  size_t nnz = vv.size();
-  int shift = (nnz > 0 && ii[0] == 0) ? 1 : 0;  // 0-based files (SpMtx_class.F90:441-444)
   Coo A0;
-  A0.nrows = n; A0.ncols = n;
-  A0.i.resize(nnz); A0.j.resize(nnz); A0.v = vv;
-  for (size_t k = 0; k < nnz; k++) {
-    int a = ii[k] + shift - 1, b = jj[k] + shift - 1;
-    if (a < 0 || a >= n || b < 0 || b >= n) {
-      err = "matrix entry " + std::to_string(k + 1) + " out of range";
-      return false;
-    }
-    A0.i[k] = a; A0.j[k] = b;
-  }
+  if (!triplets(n, ii, jj, vv, A0, err)) return false;
   // Partitionings_aggr_InitFine (Partitioning_aggr.F90:33-117)
   out.strong1 = (c.strong1 != 0.0) ? c.strong1 : 0.67;
   out.r1 = c.radius1 > 0 ? c.radius1 : 2;
@@ -1278,29 +1455,8 @@ bool build_setup(const Controls &c_in, int n, const std::vector<int> &ii, const 
     Rcoo = Rh;
     tm.lap("robust coarse space");
   }
-  // CoarseMtxBuild (CoarseMtx.F90:476-516): T = A R^T (R arranged by columns),
-  // AC = R T with R's rows re-bucketed from that column order.
-  Csr Rcols = cols_of(Rcoo);                 // column view: for each fine node, aggregates ascending
-  Csr Tm = spgemm_first_touch(A, Rcols);     // n x nagr
-  Coo RcolOrder;                             // R's COO after arrangement by columns
-  RcolOrder.nrows = Rcoo.nrows; RcolOrder.ncols = Rcoo.ncols;
-  RcolOrder.i.reserve(Rcoo.size()); RcolOrder.j.reserve(Rcoo.size()); RcolOrder.v.reserve(Rcoo.size());
-  for (int col = 0; col < Rcols.nrows; col++)
-    for (int64_t k = Rcols.ptr[(size_t)col]; k < Rcols.ptr[(size_t)col + 1]; k++) {
-      RcolOrder.i.push_back(Rcols.col[(size_t)k]);
-      RcolOrder.j.push_back(col);
-      RcolOrder.v.push_back(Rcols.val[(size_t)k]);
-    }
-  out.R = rows_of(RcolOrder);                // rows = aggregates, columns ascending
-  out.P = Rcols;                             // rows = fine nodes, aggregates ascending
-  out.P.nrows = n; out.P.ncols = Rcoo.nrows;
-  Csr AC = spgemm_first_touch(out.R, Tm);
+  Csr AC = galerkin(A, Rcoo, n, out);
   tm.lap("restriction + Galerkin");
-  out.R_i.reserve(RcolOrder.size()); out.R_j.reserve(RcolOrder.size()); out.R_v.reserve(RcolOrder.size());
-  for (size_t k = 0; k < RcolOrder.size(); k++) {
-    out.R_i.push_back(RcolOrder.i[k] + 1); out.R_j.push_back(RcolOrder.j[k] + 1);
-    out.R_v.push_back(RcolOrder.v[k]);
-  }
   // Partitionings_aggr_InitCoarse (Partitioning_aggr.F90:120-193)
   out.strong2 = c.strong2 > 0 ? c.strong2 : out.strong1 / 2.0;
   ScaledMatrix SC;
@@ -1334,20 +1490,14 @@ bool build_setup(const Controls &c_in, int n, const std::vector<int> &ii, const 
   out.smoothers = c.smoothers;
   out.levels = c.levels;
   int np = part ? nparts : out.coarse_full.nagr;
-  out.sd_ptr.assign(1, 0);
-  std::vector<std::vector<int>> part_nodes;
+  std::vector<std::vector<int>> lists((size_t)np);
   if (part) {  // Get_nodes (Decomposition.f90:35-53) for every part in one sweep
-    part_nodes.resize((size_t)np);
-    for (int i = 0; i < n; i++) part_nodes[(size_t)(*part)[(size_t)i] - 1].push_back(i);
-  }
-  std::vector<int> onfront((size_t)n, 0), nodes;
-  std::vector<int> loc((size_t)n, 0);
-  for (int p = 1; p <= np; p++) {
-    nodes.clear();
-    if (part) {
-      nodes = part_nodes[(size_t)p - 1];
-    } else {  // Get_aggregate_nodes (Aggregate_mod.F90:162-190)
-      const Aggregates &ca = out.coarse_full, &fa = out.fine_full;
+    for (int i = 0; i < n; i++) lists[(size_t)(*part)[(size_t)i] - 1].push_back(i);
+  } else {  // Get_aggregate_nodes (Aggregate_mod.F90:162-190)
+    std::vector<int> loc((size_t)n, 0);
+    const Aggregates &ca = out.coarse_full, &fa = out.fine_full;
+    for (int p = 1; p <= np; p++) {
+      std::vector<int> &nodes = lists[(size_t)p - 1];
       for (int q = ca.starts[(size_t)p - 1]; q < ca.starts[(size_t)p]; q++) {
         int f = ca.nodes[(size_t)q];
         for (int t = fa.starts[(size_t)f - 1]; t < fa.starts[(size_t)f]; t++) {
@@ -1357,24 +1507,10 @@ bool build_setup(const Controls &c_in, int n, const std::vector<int> &ii, const 
       }
       for (int v : nodes) loc[(size_t)v] = 0;
     }
-    for (int v : nodes) onfront[(size_t)v] = -1;
-    size_t lo = 0, hi = nodes.size();
-    for (int layer = 1; layer <= out.overlap; layer++) {
-      // the reference restarts each layer one entry early; that entry's
-      // neighbours are already marked, so the visited order is unchanged
-      for (size_t q = lo; q < hi; q++) {
-        int v = nodes[q];
-        for (int64_t k = A.ptr[(size_t)v]; k < A.ptr[(size_t)v + 1]; k++) {
-          int w = A.col[(size_t)k];
-          if (onfront[(size_t)w] == 0) { onfront[(size_t)w] = layer; nodes.push_back(w); }
-        }
-      }
-      lo = hi;
-      hi = nodes.size();
-    }
-    for (int v : nodes) { onfront[(size_t)v] = 0; out.sd_nodes.push_back(v + 1); }
-    out.sd_ptr.push_back((int64_t)out.sd_nodes.size());
   }
+  // the reference restarts each overlap layer one entry early; that entry's
+  // neighbours are already marked, so the visited order is unchanged
+  grow_subdomains(A, lists, out.overlap, out);
   tm.lap("subdomains + overlap");
   out.A = A;
   return true;

@@ -24,6 +24,8 @@ struct Controls {
   int solve_maxiters = -1;
   bool symmstruct = false, symmnumeric = false;
   int interpolation_type = -1;
+  int maxcie = -1, maxnd = -1, cutbal = -1, center_type = -1;  // geometric coarse grid (globals.F90:149-153)
+  bool hanging_nodes = false;
   std::string assembled_mtx_file, assembled_rhs_file, solution_file;
   std::string info_file, elemmat_rhs_file, freedom_lists_file, coords_file, freemap_file;
   int assembled_mtx_format = -1, assembled_rhs_format = -1, solution_format = -1;
@@ -42,13 +44,16 @@ struct Controls {
   int lean_task_kb = 80;            // levels with smaller average tasks use 128-thread CTAs
   int thin_level_fronts = 304;      // levels with fewer small fronts solve them one CTA per task
   int solve_schedule = 0;           // multifrontal solves: 0 one launch per level, 1 dependency-driven queue
+  int executable = -1;              // which reference driver: -1/0 doug_aggr, 1 doug_geom
 };
 
 // Parse one "name value" line the way util_actionOnCtrlArg does
 // (DOUG_utils.F90:703-1150).  Returns false and fills err on a malformed value.
 bool ctl_apply(Controls &c, const std::string &name, const std::string &value, std::string &err);
 bool ctl_parse_text(Controls &c, const std::string &text, std::string &err);
-void ctl_finish(Controls &c);  // solve_maxiters default (DOUG_utils.F90:676-678)
+// solve_maxiters default (DOUG_utils.F90:676-678); doug_geom always applies
+// exact subdomain solves (geom.F90:101-102), whatever fine_method says
+void ctl_finish(Controls &c);
 bool parse_i10(const std::string &s, int &out);
 bool parse_f10_5(const std::string &s, double &out);
 bool parse_l1(const std::string &s, bool &out);
@@ -99,6 +104,27 @@ bool check_elements(const ElementMesh &M, std::string &err);
 void assemble_elements(const ElementMesh &M, int &n, std::vector<int> &ii, std::vector<int> &jj,
                        std::vector<double> &vv, std::vector<double> &b, std::vector<int> &lg_fmap);
 
+// Node coordinates for the geometric coarse grid (Mesh.F90:470-520):
+// coordinate d of node v (1-based) at coords[(v-1)*nsd + d], and the node of
+// global freedom f (1-based) at freemap[f-1].
+struct NodeGeometry {
+  int nsd = 0, nnode = 0;
+  std::vector<double> coords;
+  std::vector<int> freemap;
+};
+// coords_file: one record of nsd*nnode real64; freemap_file: one record of
+// ngf int32 (Mesh_readFileCoords / Mesh_readFileFreemap)
+bool read_geometry(const std::string &coords_path, const std::string &freemap_path, int nsd, int nnode, int ngf,
+                   NodeGeometry &G, std::string &err);
+
+// triplets in a definite order, 0-based
+struct Coo {
+  int nrows = 0, ncols = 0;
+  std::vector<int> i, j;
+  std::vector<double> v;
+  size_t size() const { return v.size(); }
+};
+
 // CSR with DOUG's stable row arrangement (entries of a row keep their input order).
 struct Csr {
   int nrows = 0, ncols = 0;
@@ -130,6 +156,7 @@ struct SetupResult {
   // R and AC in the reference's final COO order (for pattern export)
   std::vector<int> R_i, R_j, AC_i, AC_j;
   std::vector<double> R_v, AC_v;
+  std::vector<double> coarse_xyz;       // geometric coarse grid: coordinates of R's coarse freedoms
 };
 
 // Robust coarse space (coarse_method 2): given A and the supports S_i of the
@@ -150,6 +177,29 @@ bool build_setup(const Controls &c_in, int n, const std::vector<int> &ii,
                  const std::vector<int> &jj, const std::vector<double> &vv,
                  const std::vector<int> *part, int nparts, SetupResult &out, std::string &err,
                  const RobustHook *robust = nullptr);
+
+// doug_geom's setup on one process (geom.F90:62-116): subdomains = all
+// unknowns (or the imported parts) with the overlap layers; levels 2 with
+// elemental input (efree: the elements' global freedoms, lg_fmap: global
+// freedom of every unknown, G: the node coordinates) adds the geometric
+// coarse grid: R from geometric_restriction, AC = R A R^T.  R_i/R_j/R_v and
+// AC_i/AC_j/AC_v hold them whole; the R, P and AC the solve uses keep only
+// the coarse freedoms independent_coarse accepts.
+bool build_setup_geom(const Controls &c, int n, const std::vector<int> &ii, const std::vector<int> &jj,
+                      const std::vector<double> &vv, const std::vector<int> *part, int nparts,
+                      const std::vector<int> *efree, const std::vector<int> *lg_fmap, const NodeGeometry *G,
+                      SetupResult &out, std::string &err);
+// The geometric coarse grid's restriction (coarse freedoms x unknowns,
+// 0-based, the reference's entry order: unknown after unknown) and the
+// coordinates of its coarse freedoms (nsd per freedom).
+bool geometric_restriction(const Controls &c, const std::vector<int> &efree, const NodeGeometry &G,
+                           const std::vector<int> &lg_fmap, Coo &R, std::vector<double> &coarse_xyz,
+                           std::string &err);
+// Coarse freedoms kept for the solve: a Cholesky of AC in natural order
+// that skips pivots at or below 1e-10 of their diagonal (basis functions
+// that depend on earlier ones); keep[i] = new 1-based number or 0.  More
+// than 4000 coarse freedoms: all kept.
+std::vector<int> independent_coarse(const Csr &AC);
 
 // Batched independent systems: system k owns the rows [sys_row[k],
 // sys_row[k+1]) and the triplets [sys_tri[k], sys_tri[k+1]) of (ii, jj, vv),

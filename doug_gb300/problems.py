@@ -102,7 +102,9 @@ def poisson2d_p1_elements(nodes: int = 17, jitter: float = 0.2, seed: int = 0, k
     nodes carry no freedom, as in DOUG's freemap); element e lists its interior
     vertices.  kappa (one value per triangle, default 1) scales the element
     stiffness.  Returns (ngf, eptr, efree, emat, erhs, info) with emat the
-    element matrices column by column and info a dict of the mesh sizes.
+    element matrices column by column and info a dict of the mesh sizes,
+    the node coordinates info["coords"] (nnode x 2) and the node of every
+    freedom info["freemap"] (1-based).
     """
     rng = np.random.default_rng(seed)
     h = 1.0 / (nodes - 1)
@@ -144,7 +146,8 @@ def poisson2d_p1_elements(nodes: int = 17, jitter: float = 0.2, seed: int = 0, k
     m2 = mask[:, :, None] & mask[:, None, :]          # (e, j, i): column j, row i
     emat = np.ascontiguousarray(K.transpose(0, 2, 1))[m2]      # column by column
     erhs = (f[tri] * area[:, None] / 3.0)[mask]
-    info = {"nell": len(tri), "ngf": int(interior.sum()), "nsd": 2, "mfrelt": 3, "nnode": nodes * nodes}
+    info = {"nell": len(tri), "ngf": int(interior.sum()), "nsd": 2, "mfrelt": 3, "nnode": nodes * nodes,
+            "coords": np.stack([X, Y], 1), "freemap": (np.flatnonzero(interior.ravel()) + 1).astype(np.int32)}
     return info["ngf"], eptr, efree, np.asarray(emat, np.float64), np.asarray(erhs, np.float64), info
 
 
@@ -179,7 +182,8 @@ def elasticity3d_p1_elements(N: int = 64, jitter: float = 0.15, nboxes: int = 20
     Returns (ngf, eptr, efree, emat, erhs, info) in the layout of
     ``poisson2d_p1_elements`` (element matrices column by column, restricted
     to the element's free freedoms), plus info["node_ijk"] (free node grid
-    indices, for box partitions).
+    indices, for box partitions), info["coords"] (nnode x 3) and
+    info["freemap"] (the 1-based node of every freedom).
     """
     rng = np.random.default_rng(seed)
     n1 = N + 1
@@ -243,7 +247,8 @@ def elasticity3d_p1_elements(N: int = 64, jitter: float = 0.15, nboxes: int = 20
     erhs = load.reshape(ne, 12)[mask]
     fn = np.flatnonzero(kz > 0)
     info = {"nell": ne, "ngf": ngf, "nsd": 3, "mfrelt": 12, "nnode": n1 ** 3,
-            "node_ijk": np.stack([I.ravel()[fn], J.ravel()[fn], kz[fn]], 1)}
+            "node_ijk": np.stack([I.ravel()[fn], J.ravel()[fn], kz[fn]], 1),
+            "coords": X, "freemap": (np.repeat(fn, 3) + 1).astype(np.int32)}
     return ngf, eptr, efree, emat, erhs, info
 
 
@@ -265,8 +270,10 @@ def _fortran_record(fh, payload: bytes) -> None:
 
 def write_elemental_files(folder: str, ngf, eptr, efree, emat, erhs, info) -> dict:
     """Writes DOUG's elemental input files (Fortran unformatted sequential,
-    little-endian): info, freedom lists and element matrices + RHS.  Returns
-    the control-file words that name them."""
+    little-endian): info, freedom lists and element matrices + RHS, and when
+    info has "coords" and "freemap" the node coordinates (one record,
+    coordinate after coordinate of every node) and the freedom-to-node map
+    (one record).  Returns the control-file words that name them."""
     import os
     eptr = np.asarray(eptr)
     files = {"info_file": "doug_info.dat", "freedom_lists_file": "doug_element.dat",
@@ -286,6 +293,13 @@ def write_elemental_files(folder: str, ngf, eptr, efree, emat, erhs, info) -> di
                 _fortran_record(fh, np.asarray(emat[off + j * nf: off + (j + 1) * nf], dtype="<f8").tobytes())
             off += nf * nf
             _fortran_record(fh, np.asarray(erhs[eptr[e]:eptr[e + 1]], dtype="<f8").tobytes())
+    if "coords" in info and "freemap" in info:
+        files["coords_file"] = "doug_coord.dat"
+        files["freemap_file"] = "doug_freemap.dat"
+        with open(os.path.join(folder, files["coords_file"]), "wb") as fh:
+            _fortran_record(fh, np.ascontiguousarray(info["coords"], dtype="<f8").tobytes())
+        with open(os.path.join(folder, files["freemap_file"]), "wb") as fh:
+            _fortran_record(fh, np.ascontiguousarray(info["freemap"], dtype="<i4").tobytes())
     return files
 
 

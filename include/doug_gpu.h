@@ -117,6 +117,14 @@ dg_status dg_set_matrix_coo(dg_handle *h, int n, int nnz, const int *rows, const
  * elements' non-zero values in element order, b sums the elements' RHS. */
 dg_status dg_set_elements(dg_handle *h, int nell, int ngf, const int *eptr, const int *efree,
                           const double *emat, const double *erhs);
+/* Node coordinates of the elements' mesh (after dg_set_elements; dg_load_ctl
+ * reads them from coords_file / freemap_file): coordinate d of node v
+ * (1-based) at coords[(v-1)*nsd + d], nsd 2 or 3, and the node of every
+ * global freedom f (1-based) at freemap[f-1] (ngf entries).  Replaces the
+ * reference's Mesh_readFileCoords / Mesh_readFileFreemap
+ * (src/datatypes/Mesh.F90:470-520); the geometric coarse grid of doug_geom
+ * (control word "executable geom" with levels 2) is built from them. */
+dg_status dg_set_node_geometry(dg_handle *h, int nsd, int nnode, const double *coords, const int *freemap);
 /* Right-hand side (n values); without one, b = 1 as in the reference. */
 dg_status dg_set_rhs(dg_handle *h, const double *b);
 /* Batched independent systems (no reference counterpart: one reference run
@@ -229,6 +237,10 @@ dg_status dg_get_subdomains(const dg_handle *h, long long *starts /* nsubd+1 */,
 /* R and AC in the reference's final entry order (COO, 1-based). */
 dg_status dg_get_restriction(const dg_handle *h, int *ri, int *rj, double *rv);
 dg_status dg_get_coarse_matrix(const dg_handle *h, int *ci, int *cj, double *cv);
+/* doug_geom with levels 2: the coordinates of the ncoarse coarse freedoms
+ * that R and AC number (nsd per freedom, freedom after freedom; xyz may be
+ * NULL to ask for the sizes); DG_NOT_READY otherwise. */
+dg_status dg_get_coarse_coords(const dg_handle *h, int *nsd, int *ncoarse, double *xyz);
 /* The matrix and right-hand side the handle holds (after dg_set_matrix_coo,
  * dg_set_elements or dg_load_ctl), as given or as assembled from elements:
  * 1-based COO in entry order.  NULL arrays are skipped (ask for n, nnz first). */

@@ -77,6 +77,8 @@ typedef struct {
   int solve_maxiters;
   int symmstruct, symmnumeric;
   int interpolation_type;
+  int maxcie, maxnd, cutbal, center_type, hanging_nodes;
+  int executable; /* extension word: -1/0 doug_aggr, 1 doug_geom */
   /* master data */
   char assembled_mtx_file[300];
   int assembled_mtx_format;
@@ -86,6 +88,7 @@ typedef struct {
   int solution_format;
   int start_vec_type;
   char info_file[300], freedom_lists_file[300], elemmat_rhs_file[300];
+  char coords_file[300], freemap_file[300];
 } ctl_t;
 
 static void ctl_defaults(ctl_t *c) {
@@ -99,6 +102,9 @@ static void ctl_defaults(ctl_t *c) {
   c->strong1 = c->strong2 = c->solve_tolerance = -1.0;
   c->solve_maxiters = -1;
   c->interpolation_type = -1;
+  c->maxcie = c->maxnd = c->cutbal = c->center_type = -1;
+  c->hanging_nodes = 0;
+  c->executable = -1;
   c->assembled_mtx_format = -1;
   c->assembled_rhs_format = -1;
   c->solution_format = -1;
@@ -211,6 +217,16 @@ static void ctl_action(ctl_t *c, const char *w1, const char *w2) {
   SETS(assembled_rhs_file) SETI(assembled_rhs_format)
   SETS(solution_file) SETI(solution_format) SETI(start_vec_type)
   SETS(info_file) SETS(freedom_lists_file) SETS(elemmat_rhs_file)
+  SETS(coords_file) SETS(freemap_file)
+  SETI(maxcie) SETI(maxnd) SETI(cutbal) SETI(center_type) SETL(hanging_nodes)
+  if (!strcmp(w1, "executable")) { /* not a reference word: which of the reference's drivers */
+    if (c->executable == -1) {
+      if (!strcmp(w2, "aggr")) c->executable = 0;
+      else if (!strcmp(w2, "geom")) c->executable = 1;
+      else orc_abort("executable must be aggr or geom: '%s'", w2);
+    }
+    return;
+  }
 }
 
 /* CtrlData_initFromFile (DOUG_utils.F90:629-696), on text. */
@@ -1241,13 +1257,14 @@ static spm robust_restriction(const spm *A, const spm *R) {
 }
 
 /* CoarseMtxBuild (CoarseMtx.F90:476-516), np=1: T=A*R^T, AC=R*T. It
- * re-arranges R by columns as a side effect, exactly as the reference. */
-static spm coarse_mtx_build(const spm *A, spm *R, int ninner) {
+ * re-arranges R by columns as a side effect, exactly as the reference.
+ * keep: assembled / structured input restrict R to the inner columns. */
+static spm coarse_mtx_build(const spm *A, spm *R, int ninner, int keep) {
   spm TT = spm_copy(A);
   spm T = spm_AB(&TT, R, 0, 1);
   spm_free(&TT);
   spm RT = spm_copy(R);
-  keep_columns_upto(&RT, ninner, 1);
+  if (keep) keep_columns_upto(&RT, ninner, 1);
   spm AC = spm_AB(&RT, &T, 0, 0);
   spm_free(&RT); spm_free(&T);
   return AC;
@@ -1565,6 +1582,845 @@ static double calc_cond(int it, const double *alpha, const double *beta) {
 }
 
 /* ------------------------------------------------------------------ */
+/* geometric coarse grid of doug_geom on one process                    */
+/* (CoarsePreconditioner_geometric.F90:34-115): CreateCoarse           */
+/* (coarse/geom/CreateCoarse.f90), the master's own part of SendCoarse  */
+/* (coarse/geom/TransmitCoarse.F90:574-799), CreateRestrict             */
+/* (coarse/geom/CreateRestrict.F90, GeomInterp.f90) and CleanCoarse     */
+/* (CoarseAllgathers.F90:331-507).  One coarse freedom per coarse node  */
+/* (CreateCoarseFreemap); no hanging nodes (hanging_nodes .false., the  */
+/* default); center_type 1 (box centre) and 2 (clamped mean); the       */
+/* random median of center_type 3 is not restated.                     */
+/* ------------------------------------------------------------------ */
+typedef struct {
+  int nsd, nnode, ngf, nell, mfrelt;
+  double *coords;       /* coords(d, node) at [(node-1)*nsd + d-1] */
+  int *freemap;         /* freemap(f) at [f], 1-based node numbers */
+  int *nfrelt;          /* [e], e 1-based */
+  int *mhead;           /* mhead(j, e) at [(e-1)*mfrelt + j-1] */
+  int nlf, *lg_fmap;    /* local freedom -> global freedom, [l] */
+} geom_mesh;
+
+typedef struct { int nfs, n[8], nref, rbeg, lbeg; } cg_elem;           /* CoarseGridElem */
+typedef struct { int level, node, next, parent, lbeg, lend; } cg_ref;  /* RefinedElem */
+typedef struct {
+  int nsd, ncti, nct, elnum, refnum, ngfc, nlfc, mlvl;
+  int nc[3];
+  double h0[3], minvg[3], maxvg[3];
+  double *coords;       /* [(node-1)*nsd + d] */
+  cg_elem *els;         /* [1..elnum] */
+  cg_ref *refels;       /* [1..refnum] */
+  int *elmap;           /* [1..] fine nodes */
+} cgrid;
+
+static void cgrid_free(cgrid *C) {
+  free(C->coords ? C->coords - 1 : NULL); free(C->els); free(C->refels); free(C->elmap);
+  memset(C, 0, sizeof *C);
+}
+
+/* BHeap.f90: max-heap of (by, ind); heapify never looks at a lone left child */
+typedef struct { int size, cap; int *by, *inds; } bheap;
+static void bh_insert(bheap *B, int val, int ind) {
+  if (B->size < B->cap) {
+    int cur = ++B->size;
+    while (cur > 1) {
+      if (B->by[cur / 2] >= val) break;
+      B->by[cur] = B->by[cur / 2];
+      B->inds[cur] = B->inds[cur / 2];
+      cur /= 2;
+    }
+    B->by[cur] = val;
+    B->inds[cur] = ind;
+  }
+}
+static void bh_heapify(bheap *B, int cur) {
+  int val = B->by[cur], ind = B->inds[cur], bt = cur;
+  for (;;) {
+    int l = 2 * cur, r = 2 * cur + 1;
+    if (r <= B->size) {
+      if (B->by[bt] < B->by[l]) bt = l;
+      if (B->by[bt] < B->by[r]) bt = r;
+    } else if (l < B->size) {
+      if (B->by[bt] < B->by[l]) bt = l;
+    }
+    if (bt == cur) break;
+    B->by[cur] = B->by[bt];
+    B->inds[cur] = B->inds[bt];
+    cur = bt;
+    B->by[cur] = val;
+  }
+  B->inds[cur] = ind;
+}
+static void bh_delmax(bheap *B) {
+  if (B->size >= 1) {
+    B->by[1] = B->by[B->size];
+    B->inds[1] = B->inds[B->size];
+    B->size--;
+    bh_heapify(B, 1);
+  }
+}
+
+#define CGX(C, node) ((C)->coords + (size_t)((node) - 1) * (C)->nsd)
+#define MGX(M, node) ((M)->coords + (size_t)((node) - 1) * (M)->nsd)
+
+/* getelem (CoarseGrid.F90:403-424) */
+static int cg_getelem(const double *x, const cgrid *C) {
+  double rx[3] = {0.0, 0.0, 0.0};
+  int i, ind;
+  for (i = 0; i < C->nsd; i++) rx[i] = (x[i] - C->minvg[i]) / C->h0[i];
+  ind = (int)trunc(rx[0]);
+  for (i = 1; i < C->nsd; i++) ind = (int)((double)(ind * (C->nc[i] - 1)) + trunc(rx[i]));
+  return ind + 1;
+}
+
+/* getDir (CoarseGrid.F90:498-509) on ds = x - c */
+static int cg_getdir(const double *x, const double *c, int nsd) {
+  int n = 1;
+  if (x[0] - c[0] < 0) n += 1;
+  if (x[1] - c[1] < 0) n += 2;
+  if (nsd == 3 && x[2] - c[2] < 0) n += 4;
+  return n;
+}
+
+/* getRefBounds (CoarseGrid.F90:427-473) */
+static void cg_refbounds(const cgrid *C, int refi, double *minv, double *maxv) {
+  int mi[3] = {0, 0, 0}, ma[3] = {0, 0, 0}, k, i;
+  const cg_ref *ref = &C->refels[refi];
+  const double *ct = CGX(C, ref->node);
+  for (k = 0; k < C->nsd; k++) minv[k] = maxv[k] = ct[k];
+  while (ref->parent > 0) {
+    ref = &C->refels[ref->parent];
+    ct = CGX(C, ref->node);
+    for (k = 0; k < C->nsd; k++) {
+      if (!ma[k] && ct[k] > maxv[k]) { maxv[k] = ct[k]; ma[k] = 1; }
+      else if (!mi[k] && ct[k] <= minv[k]) { minv[k] = ct[k]; mi[k] = 1; }
+    }
+  }
+  const cg_elem *el = &C->els[-ref->parent];
+  for (i = 0; i < (1 << C->nsd); i++) {
+    const double *p = CGX(C, el->n[i]);
+    for (k = 0; k < C->nsd; k++) {
+      if (!mi[k] && p[k] < minv[k]) { minv[k] = p[k]; mi[k] = 1; }
+      else if (!ma[k] && p[k] > maxv[k]) { maxv[k] = p[k]; ma[k] = 1; }
+    }
+  }
+}
+
+/* ChooseGeometricCenter / ChooseMeanCenter with meanpow 1 (CreateCoarse.f90) */
+static void cg_center(int type, double *pt, const geom_mesh *M, const int *elmap, int lo, int hi,
+                      const double *minv, const double *maxv) {
+  int d, i, nsd = M->nsd;
+  if (type == 1) {
+    for (d = 0; d < nsd; d++) pt[d] = (maxv[d] + minv[d]) / 2.0;
+    return;
+  }
+  for (d = 0; d < nsd; d++) pt[d] = 0.0;
+  for (i = lo; i <= hi; i++)
+    for (d = 0; d < nsd; d++) pt[d] = pt[d] + MGX(M, elmap[i])[d];
+  for (d = 0; d < nsd; d++) pt[d] = pt[d] / (double)(hi - lo + 1);
+  for (d = 0; d < nsd; d++) {
+    double bval = 0.25 * (maxv[d] - minv[d]);
+    if (pt[d] > maxv[d] - bval) pt[d] = maxv[d] - bval;
+    else if (pt[d] < minv[d] + bval) pt[d] = minv[d] + bval;
+  }
+}
+
+/* CreateCoarseMesh + CreateCoarseFreemap (CreateCoarse.f90) */
+static void cg_create(const geom_mesh *M, cgrid *C, int maxcie, int maxnd, int cutbal, int ctype) {
+  int nsd = M->nsd, tn = 1 << nsd, i, j, k, e, nd, d;
+  memset(C, 0, sizeof *C);
+  C->nsd = nsd;
+  char *inuse = (char *)xcalloc((size_t)M->nnode + 1, 1);
+  for (e = 1; e <= M->nell; e++)
+    for (j = 1; j <= M->nfrelt[e]; j++) inuse[M->freemap[M->mhead[(size_t)(e - 1) * M->mfrelt + j - 1]]] = 1;
+  double ln[3];
+  for (d = 0; d < nsd; d++) {
+    int first = 1;
+    double mn = 0, mx = 0;
+    for (nd = 1; nd <= M->nnode; nd++)
+      if (inuse[nd]) {
+        double v = MGX(M, nd)[d];
+        if (first || v < mn) mn = v;
+        if (first || v > mx) mx = v;
+        first = 0;
+      }
+    C->minvg[d] = mn;
+    C->maxvg[d] = mx;
+    ln[d] = C->maxvg[d] - C->minvg[d];
+    C->minvg[d] = C->minvg[d] - ln[d] * 0.005;
+    C->maxvg[d] = C->maxvg[d] + ln[d] * 0.005;
+    ln[d] = ln[d] * 1.01;
+  }
+  if (nsd == 2) {
+    C->nc[0] = (int)round(pow((double)maxcie * (ln[0] / ln[1]), 0.5));
+    C->nc[1] = (int)round(pow((double)maxcie * (ln[1] / ln[0]), 0.5));
+  } else {
+    C->nc[0] = (int)round(pow((double)maxcie * ln[0] * ln[0] / (ln[1] * ln[2]), 0.33));
+    C->nc[1] = (int)round(pow((double)maxcie * ln[1] * ln[1] / (ln[0] * ln[2]), 0.33));
+    C->nc[2] = (int)round(pow((double)maxcie * ln[2] * ln[2] / (ln[0] * ln[1]), 0.33));
+  }
+  C->elnum = 1;
+  for (d = 0; d < nsd; d++) {
+    if (C->nc[d] < 1) C->nc[d] = 1;
+    C->h0[d] = ln[d] / (double)C->nc[d];
+    C->elnum *= C->nc[d];
+  }
+  C->ncti = 1;
+  for (d = 0; d < nsd; d++) { C->nc[d] += 1; C->ncti *= C->nc[d]; }
+  int refmax = maxnd - C->ncti > 0 ? maxnd - C->ncti : 0;
+  C->nct = maxnd > C->ncti ? maxnd : C->ncti;
+  double *coords = NEWD((size_t)C->nct * nsd);
+  C->coords = coords + 1;
+  C->els = (cg_elem *)xcalloc((size_t)C->elnum + 1, sizeof(cg_elem));
+  C->refels = (cg_ref *)xcalloc((size_t)refmax + 1, sizeof(cg_ref));
+  C->elmap = NEWI(M->nnode);
+  nd = 1;
+  if (nsd == 2) {
+    for (i = 0; i <= C->nc[0] - 1; i++)
+      for (j = 0; j <= C->nc[1] - 1; j++, nd++) {
+        CGX(C, nd)[0] = i * C->h0[0] + C->minvg[0];
+        CGX(C, nd)[1] = j * C->h0[1] + C->minvg[1];
+      }
+  } else {
+    for (i = 0; i <= C->nc[0] - 1; i++)
+      for (j = 0; j <= C->nc[1] - 1; j++)
+        for (k = 0; k <= C->nc[2] - 1; k++, nd++) {
+          CGX(C, nd)[0] = i * C->h0[0] + C->minvg[0];
+          CGX(C, nd)[1] = j * C->h0[1] + C->minvg[1];
+          CGX(C, nd)[2] = k * C->h0[2] + C->minvg[2];
+        }
+  }
+  int el = 1;
+  if (nsd == 2) {
+    for (i = 1; i <= C->nc[0] - 1; i++)
+      for (j = 1; j <= C->nc[1] - 1; j++, el++) {
+        cg_elem *E = &C->els[el];
+        int nb = (i - 1) * C->nc[1] + j;
+        E->nfs = 0; E->nref = 0; E->rbeg = -1;
+        E->n[0] = nb; E->n[1] = nb + 1; E->n[2] = nb + C->nc[1]; E->n[3] = nb + C->nc[1] + 1;
+      }
+  } else {
+    for (i = 1; i <= C->nc[0] - 1; i++)
+      for (j = 1; j <= C->nc[1] - 1; j++)
+        for (k = 1; k <= C->nc[2] - 1; k++, el++) {
+          cg_elem *E = &C->els[el];
+          int nb = ((i - 1) * C->nc[1] + (j - 1)) * C->nc[2] + k, c3 = C->nc[2], c2 = C->nc[1];
+          E->nfs = 0; E->nref = 0; E->rbeg = -1;
+          E->n[0] = nb; E->n[1] = nb + 1; E->n[2] = nb + c3; E->n[3] = nb + c3 + 1;
+          E->n[4] = nb + c3 * c2; E->n[5] = nb + c3 * c2 + 1;
+          E->n[6] = nb + c3 * (c2 + 1); E->n[7] = nb + c3 * (c2 + 1) + 1;
+        }
+  }
+  for (nd = 1; nd <= M->nnode; nd++)
+    if (inuse[nd]) C->els[cg_getelem(MGX(M, nd), C)].nfs++;
+  C->els[1].lbeg = 1;
+  for (i = 2; i <= C->elnum; i++) C->els[i].lbeg = C->els[i - 1].lbeg + C->els[i - 1].nfs;
+  for (nd = 1; nd <= M->nnode; nd++)
+    if (inuse[nd]) {
+      cg_elem *E = &C->els[cg_getelem(MGX(M, nd), C)];
+      C->elmap[E->lbeg] = nd;
+      E->lbeg++;
+    }
+  bheap B;
+  B.size = 0;
+  B.cap = C->elnum + refmax;
+  B.by = NEWI(B.cap);
+  B.inds = NEWI(B.cap);
+  double buf = sqrt((double)nsd);
+  C->els[1].lbeg = 1;
+  if (C->els[1].nfs > 0) bh_insert(&B, (int)lround(buf * C->els[1].nfs), 1);
+  for (i = 2; i <= C->elnum; i++) {
+    C->els[i].lbeg = C->els[i - 1].lbeg + C->els[i - 1].nfs;
+    if (C->els[i].nfs > 0) bh_insert(&B, (int)lround(buf * C->els[i].nfs), i);
+  }
+  C->mlvl = 1;
+  int refpt = 1, hangpt = C->nct;
+  double pt[3], pt2[3], minv[3], maxv[3];
+  while (C->ncti + refpt <= hangpt) {
+    el = B.inds[1];
+    int pcnt = B.by[1];
+    bh_delmax(&B);
+    if (pcnt <= 2 * cutbal) break;
+    if (el <= C->elnum) { /* refine an initial grid element */
+      cg_ref *nw = &C->refels[refpt];
+      cg_elem *E = &C->els[el];
+      nw->level = 1;
+      nw->node = C->ncti + refpt;
+      nw->parent = -el;
+      nw->next = -1;
+      nw->lbeg = E->lbeg;
+      nw->lend = E->lbeg + E->nfs - 1;
+      for (d = 0; d < nsd; d++) { minv[d] = CGX(C, E->n[0])[d]; maxv[d] = CGX(C, E->n[tn - 1])[d]; }
+      cg_center(ctype, pt, M, C->elmap, nw->lbeg, nw->lend, minv, maxv);
+      for (d = 0; d < nsd; d++) CGX(C, nw->node)[d] = pt[d];
+      E->rbeg = refpt;
+      bh_insert(&B, E->nfs, C->elnum + refpt);
+      refpt++;
+    } else { /* refine a refined element */
+      int er = el - C->elnum, counts[9] = {0}, flags, cnt;
+      cg_ref *nw = &C->refels[refpt], *cur = &C->refels[er];
+      nw->level = cur->level + 1;
+      nw->node = C->ncti + refpt;
+      nw->parent = er;
+      for (d = 0; d < nsd; d++) pt[d] = CGX(C, cur->node)[d];
+      cg_refbounds(C, er, minv, maxv);
+      for (i = cur->lbeg; i <= cur->lend; i++) counts[cg_getdir(MGX(M, C->elmap[i]), pt, nsd)]++;
+      flags = 1;
+      for (i = 2; i <= tn; i++) if (counts[i] > counts[flags]) flags = i;
+      cnt = counts[flags];
+      if (cnt <= cutbal) break;
+      i = cur->lbeg;
+      k = cur->lend;
+      for (;;) {
+        for (; i <= k; i++) if (cg_getdir(MGX(M, C->elmap[i]), pt, nsd) == flags) break;
+        for (; k >= i; k--) if (cg_getdir(MGX(M, C->elmap[k]), pt, nsd) != flags) break;
+        if (i >= k) break;
+        j = C->elmap[k]; C->elmap[k] = C->elmap[i]; C->elmap[i] = j;
+      }
+      nw->lbeg = i;
+      nw->lend = cur->lend;
+      nw->next = cur->next;
+      cur->next = refpt;
+      cur->lend = i - 1;
+      for (d = 0; d < nsd; d++) pt2[d] = MGX(M, C->elmap[nw->lbeg])[d];
+      for (d = 0; d < nsd; d++) { /* adjustBounds (CoarseGrid.F90:477-491) */
+        if (pt[d] <= pt2[d]) minv[d] = pt[d];
+        else maxv[d] = pt[d];
+      }
+      cg_center(ctype, pt, M, C->elmap, nw->lbeg, nw->lend, minv, maxv);
+      for (d = 0; d < nsd; d++) CGX(C, nw->node)[d] = pt[d];
+      bh_insert(&B, cnt, C->elnum + refpt);
+      bh_insert(&B, pcnt - cnt, C->elnum + er);
+      if (C->mlvl < nw->level) C->mlvl = nw->level;
+      refpt++;
+    }
+  }
+  free(B.by); free(B.inds);
+  C->refnum = refpt - 1;
+  C->nct = C->ncti + C->refnum;
+  /* drop the grid nodes of empty elements, then number the refinement
+   * centres element by element in list order */
+  int *remap = (int *)xcalloc((size_t)C->ncti + 1, sizeof(int));
+  for (i = 1; i <= C->elnum; i++)
+    if (C->els[i].nfs != 0)
+      for (k = 0; k < tn; k++) remap[C->els[i].n[k]] = 1;
+  int pc = -1;
+  for (i = 0; i <= C->ncti; i++) if (remap[i] == 0) pc++;
+  C->nct -= pc;
+  double *nco = NEWD((size_t)C->nct * nsd);
+  double *ncoords = nco + 1;
+  if (pc > 0) {
+    for (i = 1; i <= C->ncti; i++) {
+      if (remap[i] == 1) {
+        remap[i] = remap[i - 1] + 1;
+        memcpy(ncoords + (size_t)(remap[i] - 1) * nsd, CGX(C, i), sizeof(double) * (size_t)nsd);
+      } else {
+        remap[i] = remap[i - 1];
+      }
+    }
+    C->ncti -= pc;
+    for (i = 1; i <= C->elnum; i++)
+      for (k = 0; k < tn; k++) C->els[i].n[k] = C->els[i].nfs > 0 ? remap[C->els[i].n[k]] : 0;
+  } else {
+    memcpy(ncoords, C->coords, sizeof(double) * (size_t)C->ncti * nsd);
+  }
+  free(remap);
+  k = C->ncti + 1;
+  for (i = 1; i <= C->elnum; i++) {
+    C->els[i].nref = k;
+    j = C->els[i].rbeg;
+    while (j != -1) {
+      memcpy(ncoords + (size_t)(k - 1) * nsd, CGX(C, C->refels[j].node), sizeof(double) * (size_t)nsd);
+      C->refels[j].node = k;
+      k++;
+      j = C->refels[j].next;
+    }
+    C->els[i].nref = k - C->els[i].nref;
+  }
+  free(C->coords - 1);
+  C->coords = ncoords;
+  C->ngfc = C->nct;
+  C->nlfc = C->ngfc;
+  free(inuse);
+}
+
+/* the master's own part of SendCoarse (TransmitCoarse.F90:574-799) on one
+ * process: the local grid LC holds the elements and refinements that own
+ * local fine nodes, in the order the local freedoms first reach them.
+ * lfreemap[l] (out) = fine node of local freedom l. */
+static void cg_local(const geom_mesh *M, const cgrid *C, cgrid *LC, int *lfreemap) {
+  int nsd = C->nsd, tn = 1 << nsd, i, j, k, f, nd;
+  int *ndtoel = NEWI(M->nnode);
+  for (int el = 1; el <= C->elnum; el++) {
+    const cg_elem *E = &C->els[el];
+    if (E->rbeg <= 0) {
+      for (j = E->lbeg; j <= E->lbeg + E->nfs - 1; j++) ndtoel[C->elmap[j]] = -el;
+    } else {
+      for (j = E->rbeg; j > 0; j = C->refels[j].next)
+        for (k = C->refels[j].lbeg; k <= C->refels[j].lend; k++) ndtoel[C->elmap[k]] = j;
+    }
+  }
+  char *refmask = (char *)xcalloc((size_t)C->refnum + 1, 1), *elmask = (char *)xcalloc((size_t)C->elnum + 1, 1);
+  char *have = (char *)xcalloc((size_t)M->nnode + 1, 1);
+  int *ellist = NEWI(C->elnum);
+  memset(LC, 0, sizeof *LC);
+  LC->nsd = nsd;
+  int lnnode = 0;
+  for (i = 1; i <= M->nlf; i++) {
+    f = M->lg_fmap[i];
+    nd = M->freemap[f];
+    if (ndtoel[nd] != 0) {
+      lfreemap[i] = nd;
+      if (!have[nd]) { lnnode++; have[nd] = 1; }
+      k = ndtoel[nd];
+      while (k > 0) {
+        if (refmask[k]) break;
+        refmask[k] = 1;
+        LC->refnum++;
+        k = C->refels[k].parent;
+      }
+      if (k < 0 && !elmask[-k]) {
+        ellist[++LC->elnum] = -k;
+        elmask[-k] = 1;
+      }
+    } else {
+      lfreemap[i] = 0;
+    }
+  }
+  int *gl_c = NEWI(C->nct), *lg_c = NEWI(C->nct);
+  LC->ncti = 0;
+  for (i = 1; i <= LC->elnum; i++)
+    for (j = 0; j < tn; j++) {
+      int cn = C->els[ellist[i]].n[j];
+      if (gl_c[cn] == 0) { gl_c[cn] = ++LC->ncti; lg_c[LC->ncti] = cn; }
+    }
+  k = LC->ncti + 1;
+  for (i = 1; i <= LC->elnum; i++)
+    for (j = C->els[ellist[i]].rbeg; j != -1; j = C->refels[j].next)
+      if (refmask[j]) { gl_c[C->refels[j].node] = k; lg_c[k] = C->refels[j].node; k++; }
+  LC->nct = LC->ncti + LC->refnum;
+  LC->ngfc = C->ngfc;
+  LC->mlvl = C->mlvl;
+  LC->nlfc = LC->nct; /* one freedom per coarse node */
+  double *co = NEWD((size_t)LC->nct * nsd);
+  LC->coords = co + 1;
+  for (i = 1; i <= LC->nct; i++) memcpy(CGX(LC, i), CGX(C, lg_c[i]), sizeof(double) * (size_t)nsd);
+  LC->els = (cg_elem *)xcalloc((size_t)LC->elnum + 1, sizeof(cg_elem));
+  LC->refels = (cg_ref *)xcalloc((size_t)LC->refnum + 1, sizeof(cg_ref));
+  LC->elmap = NEWI(lnnode);
+  nd = 1;
+  int rel = 1, pstack[64];
+  for (f = 1; f <= LC->elnum; f++) {
+    const cg_elem *E = &C->els[ellist[f]];
+    cg_elem *L = &LC->els[f];
+    L->nref = E->nref;
+    for (j = 0; j < tn; j++) L->n[j] = gl_c[E->n[j]];
+    L->lbeg = nd;
+    L->nfs = 0;
+    i = E->rbeg;
+    if (i == -1) {
+      L->rbeg = -1;
+      for (j = E->lbeg; j <= E->lbeg + E->nfs - 1; j++)
+        if (have[C->elmap[j]]) { L->nfs++; LC->elmap[nd++] = C->elmap[j]; }
+    } else {
+      int last = 0;
+      L->rbeg = rel;
+      pstack[0] = -f;
+      while (i != -1) {
+        const cg_ref *old = &C->refels[i];
+        if (refmask[i]) {
+          cg_ref *r = &LC->refels[rel];
+          if (old->level >= 64) orc_abort("refinement deeper than 63 levels");
+          r->level = old->level;
+          r->node = gl_c[old->node];
+          r->parent = pstack[r->level - 1];
+          r->next = rel + 1;
+          r->lbeg = nd;
+          for (j = old->lbeg; j <= old->lend; j++)
+            if (have[C->elmap[j]]) { L->nfs++; LC->elmap[nd++] = C->elmap[j]; }
+          r->lend = nd - 1;
+          pstack[r->level] = rel;
+          last = rel;
+          rel++;
+        }
+        i = old->next;
+      }
+      LC->refels[last].next = -1;
+    }
+  }
+  free(ndtoel); free(refmask); free(elmask); free(have); free(ellist); free(gl_c); free(lg_c);
+}
+
+/* BuildMults (GeomInterp.f90:472-560): coefficients of the multilinear
+ * polynomial of every coarse node over the box [minv, maxv].
+ * coefs(corner, col) at [(col-1)*tn + corner-1]; mults(row, col) likewise. */
+static void cg_buildmults(const double *minv, const double *maxv, const double *coefs, int csz, int nsd,
+                          int ncols, double *mults) {
+  int tn = 1 << nsd, i, r, c;
+  double mbuf[8], prd = 1.0, fm[8];
+  for (i = 0; i < tn * ncols; i++) mults[i] = 0.0;
+  for (i = 0; i < nsd; i++) prd = prd * (maxv[i] - minv[i]);
+  prd = 1.0 / prd;
+  for (c = 1; c <= tn; c++) {
+    if (nsd == 2) {
+      switch (c) {
+        case 1: mbuf[0] = minv[0] * minv[1]; mbuf[1] = -minv[1]; mbuf[2] = -minv[0]; mbuf[3] = 1.0; break;
+        case 2: mbuf[0] = -(maxv[0] * minv[1]); mbuf[1] = minv[1]; mbuf[2] = maxv[0]; mbuf[3] = -1.0; break;
+        case 3: mbuf[0] = -(minv[0] * maxv[1]); mbuf[1] = maxv[1]; mbuf[2] = minv[0]; mbuf[3] = -1.0; break;
+        default: mbuf[0] = maxv[0] * maxv[1]; mbuf[1] = -maxv[1]; mbuf[2] = -maxv[0]; mbuf[3] = 1.0; break;
+      }
+    } else {
+      /* corner c: signs of the factors (x - bound) and the sign of the term */
+      static const int usemax[8][3] = {{0, 0, 0}, {1, 0, 0}, {0, 1, 0}, {1, 1, 0},
+                                       {0, 0, 1}, {1, 0, 1}, {0, 1, 1}, {1, 1, 1}};
+      static const int negf[8] = {1, 0, 0, 1, 0, 1, 1, 0}; /* factors negated, quotients kept */
+      for (i = 0; i < 3; i++) {
+        double b = usemax[c - 1][i] ? maxv[i] : minv[i];
+        fm[i] = negf[c - 1] ? -b : b;
+      }
+      mbuf[4] = fm[0]; mbuf[5] = fm[1]; mbuf[6] = fm[2];
+      mbuf[0] = mbuf[4] * mbuf[5] * mbuf[6];
+      if (negf[c - 1]) {
+        for (i = 0; i < 3; i++) mbuf[1 + i] = mbuf[0] / mbuf[4 + i];
+        mbuf[7] = 1.0;
+      } else {
+        for (i = 0; i < 3; i++) mbuf[1 + i] = -mbuf[0] / mbuf[4 + i];
+        mbuf[7] = -1.0;
+      }
+    }
+    for (r = 0; r < tn; r++) mbuf[r] = mbuf[r] * prd;
+    for (i = 1; i <= csz; i++)
+      for (r = 0; r < tn; r++)
+        mults[(size_t)(i - 1) * tn + r] = mults[(size_t)(i - 1) * tn + r] + coefs[(size_t)(i - 1) * tn + c - 1] * mbuf[r];
+  }
+}
+
+/* MlinInterpolate (GeomInterp.f90:563-582) */
+static double cg_interp(const double *p, int nsd, const double *m) {
+  if (nsd == 2) return m[0] + m[1] * p[0] + m[2] * p[1] + m[3] * p[0] * p[1];
+  return m[0] + m[1] * p[0] + m[2] * p[1] + m[3] * p[2] + m[4] * p[1] * p[2] + m[5] * p[0] * p[2] +
+         m[6] * p[0] * p[1] + m[7] * p[0] * p[1] * p[2];
+}
+
+/* CalcNextCoefs (GeomInterp.f90:244-468) without hanging nodes: corner
+ * coefficients of the sub-box of [minv, maxv] cut at the centre ct towards
+ * pt, in terms of the coarse nodes cinds (+ the centre ci). */
+static void cg_nextcoefs(const double *ct, int ci, const double *minv, const double *maxv, const double *coefs,
+                         const int *cinds, int csz, int nsd, const double *pt, double *cfout, int *ciout,
+                         int *ncsz_out) {
+  int tn = 1 << nsd, i, k, r, ncnt = 1, ncsz, dir = 1, drev = 1, rev[3], nc[8], ni[8];
+  double m[3];
+#define CF(a, col) coefs[(size_t)((col) - 1) * tn + (a) - 1]
+#define CO(a, col) cfout[(size_t)((col) - 1) * tn + (a) - 1]
+  for (i = 0; i < nsd; i++) m[i] = (maxv[i] - ct[i]) / (maxv[i] - minv[i]);
+  ncsz = csz;
+  for (i = 1; i <= csz; i++) ciout[i - 1] = cinds[i - 1];
+  k = 1;
+  for (i = 0; i < nsd; i++) {
+    if (pt[i] < ct[i]) { dir += k; rev[i] = -k; }
+    else { drev += k; rev[i] = k; }
+    k *= 2;
+  }
+  for (i = 1; i <= csz; i++) CO(dir, i) = CF(dir, i);
+  for (i = 1; i <= csz; i++) CO(drev, i) = 0.0;
+  nc[0] = drev;
+  ni[0] = ci;
+  if (nsd == 2) {
+    for (r = 0; r < 2; r++) {
+      int a = drev - rev[r];
+      for (i = 1; i <= csz; i++) {
+        if (rev[r] > 0) CO(a, i) = m[r] * CF(a, i) + (1 - m[r]) * CF(dir, i);
+        else CO(a, i) = m[r] * CF(dir, i) + (1 - m[r]) * CF(a, i);
+      }
+    }
+  } else {
+    for (r = 0; r < 3; r++) {
+      int a = dir + rev[r];
+      for (i = 1; i <= csz; i++) {
+        if (rev[r] > 0) CO(a, i) = m[r] * CF(a, i) + (1 - m[r]) * CF(dir, i);
+        else CO(a, i) = m[r] * CF(dir, i) + (1 - m[r]) * CF(a, i);
+      }
+    }
+    /* face centres: bilinear in the two other directions */
+    static const int o1[3] = {1, 0, 0}, o2[3] = {2, 2, 1}, s1[3] = {2, 1, 1}, s2[3] = {4, 4, 2};
+    for (r = 0; r < 3; r++) {
+      int a = drev - rev[r], kk = (-rev[r] > 0 ? -rev[r] : 0) + 1;
+      double p = m[o1[r]], q = m[o2[r]];
+      for (i = 1; i <= csz; i++)
+        CO(a, i) = p * q * CF(kk, i) + p * (1 - q) * CF(kk + s2[r], i) + (1 - p) * q * CF(kk + s1[r], i) +
+                   (1 - p) * (1 - q) * CF(kk + s1[r] + s2[r], i);
+    }
+  }
+  /* put the new centre into a column whose coefficients all vanished, or
+   * close the gap with the last column */
+  int n0 = ncsz;
+  for (i = n0; i >= 1; i--) {
+    int allz = 1;
+    for (r = 1; r <= tn; r++) if (CO(r, i) != 0.0) { allz = 0; break; }
+    if (!allz) continue;
+    if (ncnt > 0) {
+      CO(nc[ncnt - 1], i) = 1.0;
+      ciout[i - 1] = ni[ncnt - 1];
+      ncnt--;
+    } else {
+      for (r = 1; r <= tn; r++) CO(r, i) = CO(r, ncsz);
+      ciout[i - 1] = ciout[ncsz - 1];
+      ncsz--;
+    }
+  }
+  for (i = 1; i <= ncnt; i++) {
+    ncsz++;
+    for (r = 1; r <= tn; r++) CO(r, ncsz) = 0.0;
+    CO(nc[i - 1], ncsz) = 1.0;
+    ciout[ncsz - 1] = ni[i - 1];
+  }
+  *ncsz_out = ncsz;
+#undef CF
+#undef CO
+}
+
+typedef struct { int n, cap; int *i, *j; double *v; } coo_buf;
+static void coo_push(coo_buf *b, int i, int j, double v) {
+  if (b->n == b->cap) {
+    b->cap = b->cap ? 2 * b->cap : 1024;
+    b->i = (int *)realloc(b->i, sizeof(int) * (size_t)(b->cap + 1));
+    b->j = (int *)realloc(b->j, sizeof(int) * (size_t)(b->cap + 1));
+    b->v = (double *)realloc(b->v, sizeof(double) * (size_t)(b->cap + 1));
+    if (!b->i || !b->j || !b->v) orc_abort("out of memory");
+  }
+  b->n++;
+  b->i[b->n] = i; b->j[b->n] = j; b->v[b->n] = v;
+}
+
+/* CalcMlinearInterp (GeomInterp.f90:585-825): node prolongation entries
+ * (fine node, coarse node, value), fine node after fine node in element and
+ * list order */
+static void cg_mlinear(const cgrid *C, const geom_mesh *M, coo_buf *NP) {
+  int nsd = C->nsd, tn = 1 << nsd, L = C->mlvl, maxc = tn + C->mlvl + nsd, i, j, k, l, d;
+  double *mins = NEWD((size_t)nsd * (L + 1)), *maxs = NEWD((size_t)nsd * (L + 1));
+  double *coefs = NEWD((size_t)tn * maxc * L), *curcfs = NEWD((size_t)tn * maxc * tn);
+  double *finals = NEWD((size_t)tn * maxc * tn), *mults = NEWD((size_t)tn * maxc);
+  int *cinds = NEWI((size_t)maxc * L), *cszs = NEWI(L), *curcis = NEWI((size_t)maxc * tn), curcsz[9];
+  char have[9];
+#define MN(lv) (mins + 1 + (size_t)((lv) - 1) * nsd)
+#define MX(lv) (maxs + 1 + (size_t)((lv) - 1) * nsd)
+#define COEF(lv) (coefs + 1 + (size_t)((lv) - 1) * tn * maxc)
+#define CIND(lv) (cinds + 1 + (size_t)((lv) - 1) * maxc)
+#define CURC(dd) (curcfs + 1 + (size_t)((dd) - 1) * tn * maxc)
+#define CURI(dd) (curcis + 1 + (size_t)((dd) - 1) * maxc)
+#define FIN(dd) (finals + 1 + (size_t)((dd) - 1) * tn * maxc)
+  static const int c2[4] = {4, 2, 3, 1}, c3[8] = {8, 4, 6, 2, 7, 3, 5, 1};
+  for (i = 1; i <= C->elnum; i++) {
+    const cg_elem *E = &C->els[i];
+    for (d = 0; d < nsd; d++) { MN(1)[d] = CGX(C, E->n[0])[d]; MX(1)[d] = CGX(C, E->n[tn - 1])[d]; }
+    cszs[1] = tn;
+    for (l = 0; l < tn; l++) CIND(1)[l] = E->n[l];
+    for (l = 0; l < tn * tn; l++) COEF(1)[l] = 0.0;
+    /* corner a of the box is the coarse node in column c(a) (getDir order) */
+    for (l = 0; l < tn; l++) {
+      int col = nsd == 2 ? c2[l] : c3[l];
+      COEF(1)[(size_t)(col - 1) * tn + l] = 1.0;
+    }
+    if (E->rbeg == -1) {
+      cg_buildmults(MN(1), MX(1), COEF(1), cszs[1], nsd, maxc, mults + 1);
+      for (j = E->lbeg; j <= E->lbeg + E->nfs - 1; j++) {
+        int pn = C->elmap[j];
+        for (l = 1; l <= cszs[1]; l++)
+          coo_push(NP, pn, CIND(1)[l - 1], cg_interp(MGX(M, pn), nsd, mults + 1 + (size_t)(l - 1) * tn));
+      }
+      continue;
+    }
+    for (j = E->rbeg; j != -1; j = C->refels[j].next) {
+      const cg_ref *R = &C->refels[j];
+      int lvl;
+      if (R->parent > 0) {
+        int ci = C->refels[R->parent].node;
+        const double *ct = CGX(C, ci), *pt = CGX(C, R->node);
+        lvl = R->level - 1;
+        cg_nextcoefs(ct, ci, MN(lvl), MX(lvl), COEF(lvl), CIND(lvl), cszs[lvl], nsd, pt, COEF(lvl + 1),
+                     CIND(lvl + 1), &cszs[lvl + 1]);
+        for (d = 0; d < nsd; d++) {
+          if (ct[d] <= pt[d]) { MN(lvl + 1)[d] = ct[d]; MX(lvl + 1)[d] = MX(lvl)[d]; }
+          else { MN(lvl + 1)[d] = MN(lvl)[d]; MX(lvl + 1)[d] = ct[d]; }
+        }
+      }
+      int ci = R->node;
+      const double *ct = CGX(C, ci);
+      lvl = R->level;
+      if (R->lbeg > R->lend) continue;
+      memset(have, 0, sizeof have);
+      for (k = R->lbeg; k <= R->lend; k++) {
+        int pn = C->elmap[k];
+        const double *pt = MGX(M, pn);
+        int dd = cg_getdir(pt, ct, nsd);
+        if (!have[dd]) {
+          cg_nextcoefs(ct, ci, MN(lvl), MX(lvl), COEF(lvl), CIND(lvl), cszs[lvl], nsd, pt, CURC(dd), CURI(dd),
+                       &curcsz[dd]);
+          for (d = 0; d < nsd; d++) {
+            if (ct[d] <= pt[d]) { MN(lvl + 1)[d] = ct[d]; MX(lvl + 1)[d] = MX(lvl)[d]; }
+            else { MN(lvl + 1)[d] = MN(lvl)[d]; MX(lvl + 1)[d] = ct[d]; }
+          }
+          cg_buildmults(MN(lvl + 1), MX(lvl + 1), CURC(dd), curcsz[dd], nsd, maxc, FIN(dd));
+          have[dd] = 1;
+        }
+        for (l = 1; l <= curcsz[dd]; l++)
+          coo_push(NP, pn, CURI(dd)[l - 1], cg_interp(pt, nsd, FIN(dd) + (size_t)(l - 1) * tn));
+      }
+    }
+  }
+#undef MN
+#undef MX
+#undef COEF
+#undef CIND
+#undef CURC
+#undef CURI
+#undef FIN
+  free(mins); free(maxs); free(coefs); free(curcfs); free(finals); free(mults);
+  free(cinds); free(cszs); free(curcis);
+}
+
+/* CreatePathRestrict's node prolongation (CreateRestrict.F90:95-213) for
+ * interpolation_type 2 (inverse distance) and 3 (the reference's kriging,
+ * which returns the distances themselves): rows by fine node number, every
+ * node weighted against its element's corners and the refinement centres
+ * on its path. */
+static void cg_path(const cgrid *C, const geom_mesh *M, int itype, coo_buf *NP) {
+  int nsd = C->nsd, tn = 1 << nsd, i, j, k, q, d;
+  int *start = NEWI(M->nnode + 1);
+  for (i = 1; i <= C->elnum; i++)
+    if (C->els[i].rbeg == -1)
+      for (j = C->els[i].lbeg; j <= C->els[i].lbeg + C->els[i].nfs - 1; j++) start[C->elmap[j] + 1] = tn;
+  for (i = 1; i <= C->refnum; i++)
+    for (j = C->refels[i].lbeg; j <= C->refels[i].lend; j++) start[C->elmap[j] + 1] = tn + C->refels[i].level;
+  start[1] = 1;
+  for (i = 1; i <= M->nnode; i++) start[i + 1] = start[i] + start[i + 1];
+  int tot = start[M->nnode + 1] - 1;
+  NP->n = NP->cap = tot;
+  NP->i = NEWI(tot); NP->j = NEWI(tot); NP->v = NEWD(tot);
+  double *pts = NEWD((size_t)nsd * (tn + C->mlvl));
+  int *pinds = NEWI(tn + C->mlvl);
+  double *w = NEWD(tn + C->mlvl);
+  for (i = 1; i <= C->elnum; i++) {
+    const cg_elem *E = &C->els[i];
+    for (k = 0; k < tn; k++) {
+      memcpy(pts + 1 + (size_t)k * nsd, CGX(C, E->n[k]), sizeof(double) * (size_t)nsd);
+      pinds[k + 1] = E->n[k];
+    }
+    int lo0 = E->lbeg, hi0 = E->lbeg + E->nfs - 1, csz = tn, rj = E->rbeg;
+    for (;;) {
+      int lo, hi;
+      if (E->rbeg == -1) { lo = lo0; hi = hi0; }
+      else {
+        if (rj == -1) break;
+        const cg_ref *R = &C->refels[rj];
+        csz = tn + R->level;
+        memcpy(pts + 1 + (size_t)(csz - 1) * nsd, CGX(C, R->node), sizeof(double) * (size_t)nsd);
+        pinds[csz] = R->node;
+        lo = R->lbeg; hi = R->lend;
+        rj = R->next;
+      }
+      for (j = lo; j <= hi; j++) {
+        int pn = C->elmap[j];
+        const double *x = MGX(M, pn);
+        for (q = 1; q <= csz; q++) {
+          double s = 0.0;
+          for (d = 0; d < nsd; d++) {
+            double t = pts[1 + (size_t)(q - 1) * nsd + d] - x[d];
+            s = s + t * t;
+          }
+          w[q] = pow(s, 0.5);
+        }
+        if (itype == 2) { /* getInvDistVals (CreateRestrict.F90:232-251) */
+          for (q = 1; q <= csz; q++) {
+            if (w[q] <= 1.0e-9) {
+              for (k = 1; k <= csz; k++) w[k] = 0.0;
+              w[q] = 1.0;
+              break;
+            }
+            w[q] = 1.0 / w[q];
+          }
+          double sum = 0.0;
+          for (q = 1; q <= csz; q++) sum = sum + w[q];
+          for (q = 1; q <= csz; q++) w[q] = w[q] / sum;
+        }
+        for (q = 1; q <= csz; q++) {
+          int at = start[pn] + q - 1;
+          NP->i[at] = pn; NP->j[at] = pinds[q]; NP->v[at] = w[q];
+        }
+      }
+      if (E->rbeg == -1) break;
+    }
+  }
+  free(start); free(pts); free(pinds); free(w);
+}
+
+/* CoarsePreconditioner_geometric_Init (CoarsePreconditioner_geometric.F90:
+ * 34-115) up to CoarseMtxBuild, one process: the restriction R (local coarse
+ * freedoms x local fine freedoms) in the reference's entry order, arranged
+ * by columns; entries <= eps = 1e-9 dropped (GeomInterp.f90:200-214). */
+static spm geom_restriction(const geom_mesh *M, const ctl_t *c, double **cxyz) {
+  int maxcie = c->maxcie == -1 ? 75 : c->maxcie, maxnd = c->maxnd == -1 ? 500 : c->maxnd;
+  int cutbal = c->cutbal <= 0 ? 1 : c->cutbal, ctype = c->center_type == -1 ? 1 : c->center_type;
+  int itype = c->interpolation_type == -1 ? 1 : c->interpolation_type, i, j, k;
+  if (M->nsd != 2 && M->nsd != 3) orc_abort("the geometric coarse grid needs 2-D or 3-D coordinates (nsd %d)", M->nsd);
+  if (c->hanging_nodes) orc_abort("hanging_nodes: not restated");
+  if (ctype != 1 && ctype != 2) orc_abort("No such center choosing method");
+  if (itype < 1 || itype > 3) orc_abort("interpolation_type %d", itype);
+  cgrid C, LC;
+  cg_create(M, &C, maxcie, maxnd, cutbal, ctype);
+  int *lfreemap = NEWI(M->nlf);
+  cg_local(M, &C, &LC, lfreemap);
+  cgrid_free(&C);
+  coo_buf NP;
+  memset(&NP, 0, sizeof NP);
+  int *lb = NEWI(M->nnode), *ub = NEWI(M->nnode);
+  if (itype == 1) { /* CreateGeneralRestrict (GeomInterp.f90:77-241) */
+    cg_mlinear(&LC, M, &NP);
+    if (NP.n > 0) {
+      lb[NP.i[1]] = 1;
+      for (k = 2; k <= NP.n; k++)
+        if (NP.i[k - 1] != NP.i[k]) {
+          if (ub[NP.i[k - 1]] != 0 || lb[NP.i[k]] != 0) orc_abort("Node restriction matrix not consolidated");
+          ub[NP.i[k - 1]] = k - 1;
+          lb[NP.i[k]] = k;
+        }
+      ub[NP.i[NP.n]] = NP.n;
+    }
+  } else { /* CreatePathRestrict: rows by fine node number */
+    cg_path(&LC, M, itype, &NP);
+    for (i = 1; i <= M->nnode; i++) { lb[i] = 0; ub[i] = -1; }
+    for (k = 1; k <= NP.n; k++) {
+      if (lb[NP.i[k]] == 0) lb[NP.i[k]] = k;
+      ub[NP.i[k]] = k;
+    }
+  }
+  coo_buf Rb;
+  memset(&Rb, 0, sizeof Rb);
+  for (i = 1; i <= M->nlf; i++) {
+    int nd = lfreemap[i];
+    if (nd == 0) continue;
+    for (j = lb[nd]; j <= ub[nd] && j >= 1; j++)
+      if (NP.v[j] > 1.0e-9) coo_push(&Rb, NP.j[j], i, NP.v[j]);
+  }
+  free(NP.i); free(NP.j); free(NP.v); free(lb); free(ub); free(lfreemap);
+  /* CleanCoarse (CoarseAllgathers.F90:331-507), one process: coarse
+   * freedoms that no entry of R uses are dropped, the rest renumbered in
+   * order */
+  int *used = NEWI(LC.nlfc);
+  for (k = 1; k <= Rb.n; k++) used[Rb.i[k]] = 1;
+  int nk = 0;
+  for (i = 1; i <= LC.nlfc; i++) used[i] = used[i] ? ++nk : 0;
+  spm R = spm_new(Rb.n, nk, M->nlf);
+  for (k = 1; k <= Rb.n; k++) { R.indi[k] = used[Rb.i[k]]; R.indj[k] = Rb.j[k]; R.val[k] = Rb.v[k]; }
+  *cxyz = (double *)xcalloc((size_t)nk * M->nsd + 1, sizeof(double));
+  for (i = 1; i <= LC.nlfc; i++)
+    if (used[i]) memcpy(*cxyz + (size_t)(used[i] - 1) * M->nsd, CGX(&LC, i), sizeof(double) * (size_t)M->nsd);
+  free(used); free(Rb.i); free(Rb.j); free(Rb.v);
+  cgrid_free(&LC);
+  return R;
+}
+
+/* ------------------------------------------------------------------ */
 /* the whole np=1 path                                                  */
 /* ------------------------------------------------------------------ */
 typedef struct {
@@ -1581,6 +2437,11 @@ typedef struct {
   int ol;
   double strong1, strong2;
   int r1, r2, min1, max1, min2, max2;
+  const geom_mesh *geom; /* node coordinates of elemental input, or NULL */
+  spm Rs, ACs;            /* the coarse level the solve uses when it differs from R, AC */
+  int have_sub;
+  int cnsd;
+  double *cxyz;           /* coarse freedom coordinates (doug_geom) */
 } state;
 
 static void state_free(state *s) {
@@ -1588,13 +2449,119 @@ static void state_free(state *s) {
   aggrs_free(&s->fine_inner); aggrs_free(&s->fine_full);
   aggrs_free(&s->coarse_inner); aggrs_free(&s->coarse_full);
   spm_free(&s->R); spm_free(&s->AC);
+  spm_free(&s->Rs); spm_free(&s->ACs); free(s->cxyz);
   free(s->sd_start); free(s->sd_nodes);
+}
+
+/* The multilinear basis functions of a geometric coarse grid can be
+ * linearly dependent on the fine nodes (a coarse element whose fine nodes
+ * lie on one line): AC is then singular but consistent, and the
+ * reference's LU solve (UMFPACK with pivoting) returns one of its
+ * solutions, whose prolongation R^T y is the same for all of them.  The
+ * solve here keeps the coarse freedoms whose Cholesky pivot (natural order,
+ * dependent ones skipped) stays above 1e-10 of their diagonal and solves on
+ * those: the same projection onto the range of R^T.  Coarse levels of more
+ * than 4000 freedoms are kept whole. */
+static void geom_independent_coarse(state *s) {
+  int nc = s->AC.nrows, i, j, k;
+  if (nc <= 0 || nc > 4000) return;
+  double *a = (double *)xcalloc((size_t)nc * nc, sizeof(double));
+  for (k = 1; k <= s->AC.nnz; k++)
+    a[(size_t)(s->AC.indi[k] - 1) * nc + (s->AC.indj[k] - 1)] = a[(size_t)(s->AC.indi[k] - 1) * nc + (s->AC.indj[k] - 1)] + s->AC.val[k];
+  int *keep = NEWI(nc), nk = 0;
+  for (j = 0; j < nc; j++) {
+    double d = a[(size_t)j * nc + j], d0 = d;
+    for (k = 0; k < j; k++) if (keep[k + 1]) d = d - a[(size_t)j * nc + k] * a[(size_t)j * nc + k];
+    if (!(d > 1.0e-10 * d0)) {
+      for (i = j; i < nc; i++) a[(size_t)i * nc + j] = 0.0;
+      continue;
+    }
+    keep[j + 1] = ++nk;
+    double l = sqrt(d);
+    a[(size_t)j * nc + j] = l;
+    for (i = j + 1; i < nc; i++) {
+      double t = a[(size_t)i * nc + j];
+      for (k = 0; k < j; k++) if (keep[k + 1]) t = t - a[(size_t)i * nc + k] * a[(size_t)j * nc + k];
+      a[(size_t)i * nc + j] = t / l;
+    }
+  }
+  free(a);
+  if (nk == nc) { free(keep); return; }
+  int nr = 0, na = 0;
+  for (k = 1; k <= s->R.nnz; k++) if (keep[s->R.indi[k]]) nr++;
+  for (k = 1; k <= s->AC.nnz; k++) if (keep[s->AC.indi[k]] && keep[s->AC.indj[k]]) na++;
+  s->Rs = spm_new(nr, nk, s->R.ncols);
+  s->ACs = spm_new(na, nk, nk);
+  nr = na = 0;
+  for (k = 1; k <= s->R.nnz; k++)
+    if (keep[s->R.indi[k]]) { nr++; s->Rs.indi[nr] = keep[s->R.indi[k]]; s->Rs.indj[nr] = s->R.indj[k]; s->Rs.val[nr] = s->R.val[k]; }
+  for (k = 1; k <= s->AC.nnz; k++)
+    if (keep[s->AC.indi[k]] && keep[s->AC.indj[k]]) {
+      na++;
+      s->ACs.indi[na] = keep[s->AC.indi[k]]; s->ACs.indj[na] = keep[s->AC.indj[k]]; s->ACs.val[na] = s->AC.val[k];
+    }
+  s->have_sub = 1;
+  free(keep);
+}
+
+/* main_geom (geom.F90:62-116) on one process: no aggregation; one
+ * subdomain of all nodes (Partitionings_full_InitCoarse,
+ * Partitioning_full.F90:32-47) or the imported parts, with ol layers
+ * (FinePreconditioner_Init arranges A by rows); with elemental input and
+ * levels 2 the geometric coarse grid gives R, and AC = R A R^T in the local
+ * coarse numbering (the one-process allgather only renumbers it). */
+static void run_setup_geom(state *s, const int *part, int nparts) {
+  ctl_t *c = &s->ctl;
+  int n = s->n, i, ip;
+  s->fine_inner.n = s->fine_full.n = n;
+  s->fine_inner.num = NEWI(n);
+  s->fine_full.num = NEWI(n);
+  s->ol = (c->overlap < 0) ? (c->smoothers > 0 ? c->smoothers : 0) : c->overlap;
+  c->fine_method = 1; /* main_geom always applies exact subdomain solves (geom.F90:101-102) */
+  if (c->levels > 2) orc_abort("doug_geom builds no coarse level for levels %d", c->levels);
+  if (c->levels == 2 && (c->input_type != 1 || !s->geom))
+    orc_abort("the geometric coarse grid needs elemental input with node coordinates");
+  spm_arrange(&s->A, ARR_ROWS, 0, 0, 0, 0);
+  int *nodes = NEWI(n);
+  int np = part ? nparts : 1;
+  s->nsubd = np;
+  s->sd_start = (int *)xcalloc((size_t)np + 2, sizeof(int));
+  long cap = 4L * n + 16, fill = 0;
+  s->sd_nodes = (int *)xcalloc((size_t)cap, sizeof(int));
+  for (ip = 1; ip <= np; ip++) {
+    int nnodes = 0;
+    for (i = 1; i <= n; i++)
+      if (!part || part[i - 1] == ip) nodes[++nnodes] = i;
+    int nexp = add_layers(s->A.mbound, s->A.indj, nodes, nnodes, s->ol, n);
+    if (fill + nexp > cap) {
+      cap = 2 * (fill + nexp);
+      s->sd_nodes = (int *)realloc(s->sd_nodes, sizeof(int) * (size_t)cap);
+      if (!s->sd_nodes) orc_abort("out of memory");
+    }
+    s->sd_start[ip - 1] = (int)fill;
+    memcpy(s->sd_nodes + fill, nodes + 1, sizeof(int) * (size_t)nexp);
+    fill += nexp;
+  }
+  s->sd_start[np] = (int)fill;
+  free(nodes);
+  if (c->levels == 2) {
+    c->smoothers = 0; /* CoarsePreconditioner_geometric.F90:53 */
+    s->R = geom_restriction(s->geom, c, &s->cxyz);
+    s->cnsd = s->geom->nsd;
+    s->have_R = 1;
+    s->AC = coarse_mtx_build(&s->A, &s->R, n, 0);
+    geom_independent_coarse(s);
+  }
 }
 
 /* aggr.F90:131-215 for numprocs==1 (or an imported partition). */
 static void run_setup(state *s, const int *part, int nparts) {
   ctl_t *c = &s->ctl;
   int n = s->n, i;
+  if (c->executable == 1) {
+    run_setup_geom(s, part, nparts);
+    return;
+  }
   /* Partitionings_aggr_InitFine (Partitioning_aggr.F90:33-117) */
   s->strong1 = (c->strong1 != 0.0) ? c->strong1 : 0.67;
   s->r1 = (c->radius1 > 0) ? c->radius1 : 2;
@@ -1615,7 +2582,7 @@ static void run_setup(state *s, const int *part, int nparts) {
     s->R = Rh;
   }
   s->have_R = 1;
-  s->AC = coarse_mtx_build(&s->A, &s->R, n);
+  s->AC = coarse_mtx_build(&s->A, &s->R, n, c->input_type != 1);
   /* Partitionings_aggr_InitCoarse (Partitioning_aggr.F90:120-193) */
   s->strong2 = (c->strong2 > 0) ? c->strong2 : s->strong1 / 2.0;
   spm_find_strong(&s->AC, s->strong2);
@@ -1748,13 +2715,14 @@ static void run_pcg(state *s, orc_result *res) {
   }
   profchol cfact;
   memset(&cfact, 0, sizeof cfact);
-  int nc = s->AC.nrows;
+  const spm *ACp = s->have_sub ? &s->ACs : &s->AC, *Rp = s->have_sub ? &s->Rs : &s->R;
+  int nc = ACp->nrows;
   if (levels > 1) {
-    int *ci = (int *)xcalloc((size_t)s->AC.nnz + 1, sizeof(int));
-    int *cj = (int *)xcalloc((size_t)s->AC.nnz + 1, sizeof(int));
+    int *ci = (int *)xcalloc((size_t)ACp->nnz + 1, sizeof(int));
+    int *cj = (int *)xcalloc((size_t)ACp->nnz + 1, sizeof(int));
     int k;
-    for (k = 0; k < s->AC.nnz; k++) { ci[k] = s->AC.indi[k + 1] - 1; cj[k] = s->AC.indj[k + 1] - 1; }
-    pc_factor(&cfact, nc, s->AC.nnz, ci, cj, s->AC.val + 1);
+    for (k = 0; k < ACp->nnz; k++) { ci[k] = ACp->indi[k + 1] - 1; cj[k] = ACp->indj[k + 1] - 1; }
+    pc_factor(&cfact, nc, ACp->nnz, ci, cj, ACp->val + 1);
     free(ci); free(cj);
   }
   double t1 = now_s();
@@ -1825,9 +2793,9 @@ static void run_pcg(state *s, orc_result *res) {
         }
       }
       if (levels > 1) { /* prec2Level (pcg.F90:144-209), method 1 */
-        spmv_R(&s->R, r, crhs, 0, nc);
+        spmv_R(Rp, r, crhs, 0, nc);
         pc_solve(&cfact, crhs + 1, csol + 1, cw);
-        spmv_R(&s->R, csol, tmpsol, 1, n);
+        spmv_R(Rp, csol, tmpsol, 1, n);
         if (method == 1 || method == 5) /* pcg.F90:191-193, 205-208 */
           for (i = 1; i <= n; i++) z[i] = z[i] + tmpsol[i];
       }
@@ -1905,6 +2873,11 @@ static void export_setup(const state *s, orc_result *r) {
   r->minasize1 = s->min1; r->maxasize1 = s->max1;
   r->minasize2 = s->min2; r->maxasize2 = s->max2;
   r->tol = s->ctl.solve_tolerance; r->maxit = s->ctl.solve_maxiters;
+  if (s->cxyz) {
+    r->cnsd = s->cnsd;
+    r->cxyz = (double *)xcalloc((size_t)s->cnsd * s->AC.nrows + 1, sizeof(double));
+    memcpy(r->cxyz, s->cxyz, sizeof(double) * (size_t)s->cnsd * s->AC.nrows);
+  }
 }
 
 static void load_coo(state *s, int n, int nnz, const int *ii, const int *jj,
@@ -1929,10 +2902,11 @@ static void load_coo(state *s, int n, int nnz, const int *ii, const int *jj,
 
 static int run_common(int n, int nnz, const int *ii, const int *jj, const double *vv,
                       const double *rhs, const char *ctl_text, const int *part,
-                      int nparts, int do_solve, orc_result **out) {
+                      int nparts, int do_solve, const geom_mesh *G, orc_result **out) {
   orc_result *r = (orc_result *)calloc(1, sizeof(orc_result));
   state *s = (state *)calloc(1, sizeof(state));
   *out = r;
+  s->geom = G;
   if (setjmp(g_jmp)) {
     r->status = -1;
     snprintf(r->errmsg, sizeof r->errmsg, "%s", g_err);
@@ -1960,13 +2934,13 @@ static int run_common(int n, int nnz, const int *ii, const int *jj, const double
 int orc_run_coo(int n, int nnz, const int *ii, const int *jj, const double *vv,
                 const double *rhs, const char *ctl_text, const int *part,
                 int nparts, orc_result **out) {
-  return run_common(n, nnz, ii, jj, vv, rhs, ctl_text, part, nparts, 1, out);
+  return run_common(n, nnz, ii, jj, vv, rhs, ctl_text, part, nparts, 1, NULL, out);
 }
 
 int orc_setup_coo(int n, int nnz, const int *ii, const int *jj, const double *vv,
                   const char *ctl_text, const int *part, int nparts,
                   orc_result **out) {
-  return run_common(n, nnz, ii, jj, vv, NULL, ctl_text, part, nparts, 0, out);
+  return run_common(n, nnz, ii, jj, vv, NULL, ctl_text, part, nparts, 0, NULL, out);
 }
 
 void orc_free(orc_result *r) {
@@ -1974,7 +2948,7 @@ void orc_free(orc_result *r) {
   free(r->x); free(r->b); free(r->res_hist); free(r->aggr_fine);
   free(r->aggr_fine_full); free(r->aggr_coarse); free(r->aggr_coarse_full);
   free(r->subd_starts); free(r->subd_nodes); free(r->R_i); free(r->R_j);
-  free(r->R_v); free(r->AC_i); free(r->AC_j); free(r->AC_v);
+  free(r->R_v); free(r->AC_i); free(r->AC_j); free(r->AC_v); free(r->cxyz);
   free(r);
 }
 
@@ -2353,7 +3327,94 @@ int orc_read_elemental(const char *info, const char *freel, const char *elemmat,
 
 void orc_free_buffers(void *a, void *b, void *c, void *d) { free(a); free(b); free(c); free(d); }
 
+static void geom_mesh_free(geom_mesh *G) {
+  free(G->coords); free(G->freemap); free(G->nfrelt); free(G->mhead); free(G->lg_fmap);
+  memset(G, 0, sizeof *G);
+}
+
+/* Mesh_readFromFile for doug_geom (Mesh.F90:293-552): info (nell, ngf,
+ * nsd, mfrelt, nnode), the freedom lists, coords(nsd, nnode) in one record
+ * and freemap(ngf) in one record; local freedoms = the used freedoms in
+ * increasing order (one process).  Returns 0 or a negative error code. */
+static int read_geom_mesh(const char *info, const char *freel, const char *coords, const char *freemap,
+                          int nblocks, geom_mesh *G) {
+  long len, pos, rl;
+  unsigned char *own;
+  const unsigned char *r;
+  unsigned char *buf = slurp(info, &len);
+  if (!buf) return -1;
+  pos = 0;
+  r = fort_record(buf, len, &pos, &rl, &own);
+  if (!r || rl < 20) { free(buf); free(own); return -2; }
+  G->nell = (int32_t)le32(r); G->ngf = (int32_t)le32(r + 4); G->nsd = (int32_t)le32(r + 8);
+  G->mfrelt = (int32_t)le32(r + 12); G->nnode = (int32_t)le32(r + 16);
+  free(own); free(buf);
+  if (G->nell <= 0 || G->ngf <= 0 || G->nsd <= 0 || G->nsd > 3 || G->mfrelt <= 0 || G->nnode <= 0) return -2;
+  G->nfrelt = (int *)xcalloc((size_t)G->nell + 1, sizeof(int));
+  G->mhead = (int *)xcalloc((size_t)G->nell * G->mfrelt, sizeof(int));
+  buf = slurp(freel, &len);
+  if (!buf) return -3;
+  pos = 0;
+  for (int e = 1; e <= G->nell; e++) {
+    r = fort_record(buf, len, &pos, &rl, &own);
+    if (!r || rl < 4) { free(own); free(buf); return -3; }
+    int nf = (int32_t)le32(r);
+    if (nf < 0 || nf > G->mfrelt || rl < 4 + 4L * nf) { free(own); free(buf); return -3; }
+    G->nfrelt[e] = nf;
+    for (int i = 0; i < nf; i++) G->mhead[(size_t)(e - 1) * G->mfrelt + i] = (int32_t)le32(r + 4 + 4 * i);
+    free(own);
+  }
+  free(buf);
+  if (nblocks > 1) {
+    int mx = 0;
+    for (int e = 1; e <= G->nell; e++)
+      for (int i = 0; i < G->nfrelt[e]; i++) if (G->mhead[(size_t)(e - 1) * G->mfrelt + i] > mx) mx = G->mhead[(size_t)(e - 1) * G->mfrelt + i];
+    G->ngf = mx;
+  }
+  buf = slurp(coords, &len);
+  if (!buf) return -4;
+  pos = 0;
+  r = fort_record(buf, len, &pos, &rl, &own);
+  if (!r || rl < 8L * G->nsd * G->nnode) { free(own); free(buf); return -4; }
+  G->coords = (double *)xcalloc((size_t)G->nsd * G->nnode, sizeof(double));
+  for (long q = 0; q < (long)G->nsd * G->nnode; q++) G->coords[q] = led(r + 8 * q);
+  free(own); free(buf);
+  buf = slurp(freemap, &len);
+  if (!buf) return -5;
+  pos = 0;
+  r = fort_record(buf, len, &pos, &rl, &own);
+  if (!r || rl < 4L * G->ngf) { free(own); free(buf); return -5; }
+  G->freemap = (int *)xcalloc((size_t)G->ngf + 1, sizeof(int));
+  for (int f = 1; f <= G->ngf; f++) {
+    G->freemap[f] = (int32_t)le32(r + 4 * (f - 1));
+    if (G->freemap[f] < 1 || G->freemap[f] > G->nnode) { free(own); free(buf); return -6; }
+  }
+  free(own); free(buf);
+  char *usedf = (char *)xcalloc((size_t)G->ngf + 1, 1);
+  for (int e = 1; e <= G->nell; e++)
+    for (int i = 0; i < G->nfrelt[e]; i++) {
+      int g = G->mhead[(size_t)(e - 1) * G->mfrelt + i];
+      if (g < 1 || g > G->ngf) { free(usedf); return -7; }
+      usedf[g] = 1;
+    }
+  G->lg_fmap = (int *)xcalloc((size_t)G->ngf + 1, sizeof(int));
+  G->nlf = 0;
+  for (int g = 1; g <= G->ngf; g++) if (usedf[g]) G->lg_fmap[++G->nlf] = g;
+  free(usedf);
+  return 0;
+}
+
+static int run_ctl_common(const char *ctl_path, const char *overrides, const int *part, int nparts,
+                          orc_result **out);
 int orc_run_ctl(const char *ctl_path, const char *overrides, orc_result **out) {
+  return run_ctl_common(ctl_path, overrides, NULL, 0, out);
+}
+int orc_run_ctl_part(const char *ctl_path, const char *overrides, const int *part, int nparts,
+                     orc_result **out) {
+  return run_ctl_common(ctl_path, overrides, part, nparts, out);
+}
+static int run_ctl_common(const char *ctl_path, const char *overrides, const int *part, int nparts,
+                          orc_result **out) {
   *out = NULL;
   long len = 0;
   unsigned char *txt = slurp(ctl_path, &len);
@@ -2399,7 +3460,21 @@ int orc_run_ctl(const char *ctl_path, const char *overrides, orc_result **out) {
     double *vv, *rhs;
     rc = orc_read_elemental(ip, fp, ep, c.number_of_blocks, &n, &nnz, &ii, &jj, &vv, &rhs);
     if (rc) orc_abort("Unable to read elemental input (%d)", rc);
-    rc = orc_run_coo(n, nnz, ii, jj, vv, rhs, all, NULL, 0, &r);
+    geom_mesh G;
+    memset(&G, 0, sizeof G);
+    int have_geom = 0;
+    if (c.executable == 1 && c.coords_file[0] && c.freemap_file[0]) {
+      char cp[1400], mp[1400];
+#define ORC_PATH(dst, name) \
+      if (name[0] == '/') snprintf(dst, sizeof dst, "%s", name); else snprintf(dst, sizeof dst, "%s/%s", dir, name);
+      ORC_PATH(cp, c.coords_file) ORC_PATH(mp, c.freemap_file)
+#undef ORC_PATH
+      rc = read_geom_mesh(ip, fp, cp, mp, c.number_of_blocks, &G);
+      if (rc) orc_abort("Unable to read the node coordinates / freemap (%d)", rc);
+      have_geom = 1;
+    }
+    rc = run_common(n, nnz, ii, jj, vv, rhs, all, part, nparts, 1, have_geom ? &G : NULL, &r);
+    geom_mesh_free(&G);
     free(ii); free(jj); free(vv); free(rhs); free(all);
     *out = r;
     return rc;
@@ -2419,7 +3494,7 @@ int orc_run_ctl(const char *ctl_path, const char *overrides, orc_result **out) {
         if (ri < g) { ii[nnz] = mri; jj[nnz] = mri + g; vv[nnz++] = -1; } /* down */
       }
     for (int i = 0; i < n; i++) rhs[i] = -1;
-    rc = orc_run_coo(n, nnz, ii, jj, vv, rhs, all, NULL, 0, &r);
+    rc = orc_run_coo(n, nnz, ii, jj, vv, rhs, all, part, nparts, &r);
     free(ii); free(jj); free(vv); free(rhs); free(all);
     *out = r;
     return rc;
@@ -2443,7 +3518,7 @@ int orc_run_ctl(const char *ctl_path, const char *overrides, orc_result **out) {
     if (rc) orc_abort("Unable to read rhs file: %s (%d)", rpath, rc);
   }
   int nz2 = n > nnz ? n : nnz;
-  rc = orc_run_coo(nn, nz2, ii, jj, vv, rhs, all, NULL, 0, &r);
+  rc = orc_run_coo(nn, nz2, ii, jj, vv, rhs, all, part, nparts, &r);
   free(ii); free(jj); free(vv); free(rhs); free(all);
   *out = r;
   return rc;

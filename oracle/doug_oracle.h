@@ -59,6 +59,10 @@ typedef struct orc_result {
   double tol;
   int maxit;
   double t_setup, t_factor, t_solve;
+  /* doug_geom with levels 2: coordinates of the coarse freedoms that R and
+   * AC number (cnsd x AC_n, coordinate after coordinate of each freedom) */
+  int cnsd;
+  double *cxyz;
 } orc_result;
 
 /* Run the full path from a DOUG control file.  `overrides` is a string of
@@ -66,6 +70,10 @@ typedef struct orc_result {
  * repeated word, so overrides win).  `workdir` resolves relative file names
  * (NULL: directory of the control file). */
 int orc_run_ctl(const char *ctl_path, const char *overrides, orc_result **out);
+/* The same with an imported partition of the unknowns (1-based part ids,
+ * length n, nparts parts) in place of the default subdomains. */
+int orc_run_ctl_part(const char *ctl_path, const char *overrides, const int *part, int nparts,
+                     orc_result **out);
 /* Elemental input files (input_type 1) assembled as one DOUG process does;
  * 1-based COO with the reference's flipped indices, malloc'ed (free with
  * orc_free_buffers). */

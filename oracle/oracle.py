@@ -41,6 +41,7 @@ class _Result(C.Structure):
         ("minasize2", C.c_int), ("maxasize2", C.c_int),
         ("tol", C.c_double), ("maxit", C.c_int),
         ("t_setup", C.c_double), ("t_factor", C.c_double), ("t_solve", C.c_double),
+        ("cnsd", C.c_int), ("cxyz", C.POINTER(C.c_double)),
     ]
 
 
@@ -65,6 +66,7 @@ def lib():
             L.orc_setup_coo.argtypes = [C.c_int, C.c_int, P(C.c_int), P(C.c_int), P(C.c_double),
                                         C.c_char_p, P(C.c_int), C.c_int, P(P(_Result))]
             L.orc_run_ctl.argtypes = [C.c_char_p, C.c_char_p, P(P(_Result))]
+            L.orc_run_ctl_part.argtypes = [C.c_char_p, C.c_char_p, P(C.c_int), C.c_int, P(P(_Result))]
             L.orc_free.argtypes = [P(_Result)]
             L.orc_read_assembled.argtypes = [C.c_char_p, C.c_int, P(C.c_int), P(C.c_int),
                                              P(P(C.c_int)), P(P(C.c_int)), P(P(C.c_double))]
@@ -128,6 +130,8 @@ def _convert(res_p) -> OracleResult:
                 _arr(r.R_j, r.R_nnz, np.int32), _arr(r.R_v, r.R_nnz, np.float64))
     out["AC"] = (r.AC_n, _arr(r.AC_i, r.AC_nnz, np.int32), _arr(r.AC_j, r.AC_nnz, np.int32),
                  _arr(r.AC_v, r.AC_nnz, np.float64))
+    out["coarse_xyz"] = (_arr(r.cxyz, r.cnsd * r.AC_n, np.float64).reshape(r.AC_n, r.cnsd)
+                         if r.cnsd > 0 else None)
     for k in ("overlap", "smoothers", "levels", "method", "strong1", "strong2", "radius1",
               "radius2", "minasize1", "maxasize1", "minasize2", "maxasize2", "tol", "maxit",
               "t_setup", "t_factor", "t_solve"):
@@ -167,10 +171,16 @@ def run_coo(n, rows1, cols1, vals, rhs=None, ctl="", part=None, setup_only=False
     return out
 
 
-def run_ctl(path, overrides=""):
+def run_ctl(path, overrides="", part=None):
+    """Run the oracle on a control file; part: optional 1-based partition of
+    the unknowns replacing the default subdomains."""
     L = lib()
     res = C.POINTER(_Result)()
-    L.orc_run_ctl(path.encode(), overrides.encode(), C.byref(res))
+    if part is None:
+        L.orc_run_ctl(path.encode(), overrides.encode(), C.byref(res))
+    else:
+        pp = np.ascontiguousarray(part, dtype=np.int32)
+        L.orc_run_ctl_part(path.encode(), overrides.encode(), _ip(pp), int(pp.max()), C.byref(res))
     out = _convert(res)
     L.orc_free(res)
     return out
