@@ -16,6 +16,7 @@ CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libdouggpu.so")
 CLI = os.path.join(OUT, "doug_gpu")       # command-line driver (flags of the reference's executables)
+CLI_GEOM = os.path.join(OUT, "doug_geom_gpu")  # the same driver with doug_geom's setup
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 
 HOST_SRC = ["host/setup.cpp", "host/geom.cpp", "host/mf_symbolic.cpp"]
@@ -72,9 +73,10 @@ def build(force: bool = False, verbose: bool = False) -> str:
     if force or jobs or not os.path.exists(LIB):
         _run([nvcc, ARCH, "-shared", "-o", LIB] + objs + ["-lpthread"])
     cli_src = os.path.join(CSRC, "doug_gpu_main.cpp")
-    if force or _stale(CLI, [cli_src, LIB, os.path.join(ROOT, "include", "doug_gpu.h")]):
-        _run(["g++", "-std=c++17", "-O2", "-Wall", cli_src, "-o", CLI, "-L" + OUT, "-ldouggpu",
-              "-Wl,-rpath,$ORIGIN"])
+    for exe, defs in ((CLI, []), (CLI_GEOM, ["-DDG_DRIVER_GEOM"])):
+        if force or _stale(exe, [cli_src, LIB, os.path.join(ROOT, "include", "doug_gpu.h")]):
+            _run(["g++", "-std=c++17", "-O2", "-Wall"] + defs + [cli_src, "-o", exe, "-L" + OUT, "-ldouggpu",
+                  "-Wl,-rpath,$ORIGIN"])
     return LIB
 
 

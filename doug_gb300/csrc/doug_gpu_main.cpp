@@ -1,5 +1,7 @@
-// doug_gpu: the command-line driver of the GB300 solve path, with the flags
-// of the reference's executables (util_parseArgs, DOUG_utils.F90:485-566):
+// doug_gpu / doug_geom_gpu: the command-line drivers of the GB300 solve path
+// (doug_aggr's setup, aggr.F90, and doug_geom's, geom.F90; the second is this
+// file built with DG_DRIVER_GEOM), with the flags of the reference's
+// executables (util_parseArgs, DOUG_utils.F90:485-566):
 //   -f file.name    control file (default DOUG.dat)
 //   -q [file.name]  quiet: the driver's messages go to file.name (default log.DOUG)
 //   -p [prefix]     profile: phase times to prefix.00 (default prof)
@@ -32,11 +34,16 @@ const char *kReferenceWords[] = {
     "submeth", "gmres_max_it", "gmrestarts"};
 const char *kExtensionWords[] = {"precision", "replace_every", "omega", "nd_leaf", "profile", "reuse_factors",
                                  "elemental_matvec", "panel_rows", "fwd_task_kb", "lean_task_kb",
-                                 "thin_level_fronts", "solve_schedule"};
+                                 "thin_level_fronts", "solve_schedule", "executable"};
+#ifdef DG_DRIVER_GEOM
+const char *kName = "doug_geom_gpu";
+#else
+const char *kName = "doug_gpu";
+#endif
 
 void usage(FILE *o) {
   fprintf(o, " Usage: \n");
-  fprintf(o, " ./doug_gpu [[-f file.name] [-q [file.name]] [-p [file.prefix]] or [-i][-v][-h]]\n");
+  fprintf(o, " ./%s [[-f file.name] [-q [file.name]] [-p [file.prefix]] or [-i][-v][-h]]\n", kName);
   fprintf(o, "                 : w/o any parameter assumes control file is DOUG.dat\n");
   fprintf(o, " -f file.name    : specifies DOUG control file name\n");
   fprintf(o, " -q [file.name]  : quiet mode - the driver logs to log.DOUG or to file.name\n");
@@ -110,6 +117,9 @@ int main(int argc, char **argv) {
     return 1;
   }
   if (prof) dg_set_option(h, "profile", "1");  // phase times (event pairs, no iteration graph)
+#ifdef DG_DRIVER_GEOM
+  dg_set_option(h, "executable", "geom");  // the first value of a word wins: the control file cannot undo it
+#endif
   dg_status st = dg_load_ctl(h, ctl.c_str());
   if (st != DG_OK) {
     rc = fail("control file", st);
