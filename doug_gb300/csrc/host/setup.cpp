@@ -635,50 +635,76 @@ static Coo coo_of(const Csr &c) {
   return m;
 }
 
+// Rows [0, n) in contiguous blocks on up to 16 host threads (one block
+// below 4096 rows): fn(lo, hi) must only write rows lo..hi-1, so the result
+// is the same for any thread count.
+template <class F>
+static void parallel_rows(int n, F fn) {
+  const int nt = std::max(1, std::min(16, (int)std::thread::hardware_concurrency()));
+  if (n < 4096 || nt < 2) {
+    fn(0, n);
+    return;
+  }
+  const int chunk = (n + nt - 1) / nt;
+  std::vector<std::thread> th;
+  for (int t = 1; t < nt; t++) {
+    const int lo = t * chunk, hi = std::min(n, lo + chunk);
+    if (lo < hi) th.emplace_back([&fn, lo, hi] { fn(lo, hi); });
+  }
+  fn(0, std::min(n, chunk));
+  for (auto &x : th) x.join();
+}
+
 // SpMtx_AB (SpMtx_op_AB.f90:39-200): A given as a row view, B as a row view
 // (of B, or of B^T).  Output row i lists its columns in first-touch order;
 // each value is summed in the order A's row entries, then B's row entries,
-// are visited; explicit zeros are kept.
+// are visited; explicit zeros are kept.  Rows are independent: counted and
+// filled in parallel blocks.
 static Csr spgemm_first_touch(const Csr &A, const Csr &B) {
   Csr C;
   C.nrows = A.nrows; C.ncols = B.ncols;
   C.ptr.assign((size_t)A.nrows + 1, 0);
-  std::vector<int> mark((size_t)B.ncols, -1);
-  std::vector<int64_t> pos((size_t)B.ncols, 0);
-  for (int i = 0; i < A.nrows; i++) {
-    int64_t cnt = 0;
-    for (int64_t k = A.ptr[(size_t)i]; k < A.ptr[(size_t)i + 1]; k++) {
-      int kk = A.col[(size_t)k];
-      for (int64_t j = B.ptr[(size_t)kk]; j < B.ptr[(size_t)kk + 1]; j++) {
-        int jj = B.col[(size_t)j];
-        if (mark[(size_t)jj] != i) { mark[(size_t)jj] = i; cnt++; }
+  parallel_rows(A.nrows, [&](int lo, int hi) {
+    std::vector<int> mark((size_t)B.ncols, -1);
+    for (int i = lo; i < hi; i++) {
+      int64_t cnt = 0;
+      for (int64_t k = A.ptr[(size_t)i]; k < A.ptr[(size_t)i + 1]; k++) {
+        int kk = A.col[(size_t)k];
+        for (int64_t j = B.ptr[(size_t)kk]; j < B.ptr[(size_t)kk + 1]; j++) {
+          int jj = B.col[(size_t)j];
+          if (mark[(size_t)jj] != i) { mark[(size_t)jj] = i; cnt++; }
+        }
       }
+      C.ptr[(size_t)i + 1] = cnt;
     }
-    C.ptr[(size_t)i + 1] = C.ptr[(size_t)i] + cnt;
-  }
+  });
+  for (int i = 0; i < A.nrows; i++) C.ptr[(size_t)i + 1] += C.ptr[(size_t)i];
   C.col.resize((size_t)C.ptr.back());
   C.val.resize((size_t)C.ptr.back());
-  std::fill(mark.begin(), mark.end(), -1);
-  for (int i = 0; i < A.nrows; i++) {
-    int64_t base = C.ptr[(size_t)i], nind = 0;
-    for (int64_t k = A.ptr[(size_t)i]; k < A.ptr[(size_t)i + 1]; k++) {
-      int kk = A.col[(size_t)k];
-      double av = A.val[(size_t)k];
-      for (int64_t j = B.ptr[(size_t)kk]; j < B.ptr[(size_t)kk + 1]; j++) {
-        int jj = B.col[(size_t)j];
-        double prod = av * B.val[(size_t)j];
-        if (mark[(size_t)jj] != i) {
-          mark[(size_t)jj] = i;
-          pos[(size_t)jj] = base + nind;
-          C.col[(size_t)(base + nind)] = jj;
-          C.val[(size_t)(base + nind)] = prod;
-          nind++;
-        } else {
-          C.val[(size_t)pos[(size_t)jj]] = C.val[(size_t)pos[(size_t)jj]] + prod;
+  parallel_rows(A.nrows, [&](int lo, int hi) {
+    std::vector<int> mark((size_t)B.ncols, -1);
+    std::vector<int64_t> pos((size_t)B.ncols, 0);
+    for (int i = lo; i < hi; i++) {
+      int64_t base = C.ptr[(size_t)i], nind = 0;
+      for (int64_t k = A.ptr[(size_t)i]; k < A.ptr[(size_t)i + 1]; k++) {
+        int kk = A.col[(size_t)k];
+        double av = A.val[(size_t)k];
+        for (int64_t j = B.ptr[(size_t)kk]; j < B.ptr[(size_t)kk + 1]; j++) {
+          int jj = B.col[(size_t)j];
+          double prod = av * B.val[(size_t)j];
+          if (mark[(size_t)jj] != i) {
+            mark[(size_t)jj] = i;
+            pos[(size_t)jj] = base + nind;
+            C.col[(size_t)(base + nind)] = jj;
+            C.val[(size_t)(base + nind)] = prod;
+            nind++;
+          } else {
+            C.val[(size_t)pos[(size_t)jj]] = C.val[(size_t)pos[(size_t)jj]] + prod;
+          }
         }
       }
     }
-  }
+  });
   return C;
 }
 
@@ -741,33 +767,41 @@ static void unscale_rows(ScaledMatrix &S) {
 // adjacency SpMtx_build_refs_symm(sortdown) (SpMtx_arrangement.F90:461-568).
 static void find_strong(ScaledMatrix &S, double alpha) {
   const Csr &M = S.M;
+  const int n = M.nrows;
   S.strong.assign(M.col.size(), 0);
-  for (int r = 0; r < M.nrows; r++) {
-    double mx = (double)(-1.0e15f);
-    for (int64_t k = M.ptr[(size_t)r]; k < M.ptr[(size_t)r + 1]; k++)
-      if (M.col[(size_t)k] != r) mx = std::max(mx, std::fabs(M.val[(size_t)k]));
-    mx = mx * alpha;
-    for (int64_t k = M.ptr[(size_t)r]; k < M.ptr[(size_t)r + 1]; k++) {
-      if (M.col[(size_t)k] != r) S.strong[(size_t)k] = std::fabs(M.val[(size_t)k]) > mx;
-      else S.strong[(size_t)k] = S.diag[(size_t)r] > mx;  // unscaled diagonal
+  S.sptr.assign((size_t)n + 1, 0);
+  parallel_rows(n, [&](int lo, int hi) {
+    for (int r = lo; r < hi; r++) {
+      double mx = (double)(-1.0e15f);
+      for (int64_t k = M.ptr[(size_t)r]; k < M.ptr[(size_t)r + 1]; k++)
+        if (M.col[(size_t)k] != r) mx = std::max(mx, std::fabs(M.val[(size_t)k]));
+      mx = mx * alpha;
+      int64_t cnt = 0;
+      for (int64_t k = M.ptr[(size_t)r]; k < M.ptr[(size_t)r + 1]; k++) {
+        if (M.col[(size_t)k] != r) S.strong[(size_t)k] = std::fabs(M.val[(size_t)k]) > mx;
+        else S.strong[(size_t)k] = S.diag[(size_t)r] > mx;  // unscaled diagonal
+        if (S.strong[(size_t)k] && M.col[(size_t)k] != r && M.col[(size_t)k] < n) cnt++;
+      }
+      S.sptr[(size_t)r + 1] = cnt;
     }
-  }
+  });
+  for (int r = 0; r < n; r++) S.sptr[(size_t)r + 1] += S.sptr[(size_t)r];
   // strong off-diagonal neighbours of each row, by |value| descending; equal
   // magnitudes keep their entry order (stable)
-  int n = M.nrows;
-  S.sptr.assign((size_t)n + 1, 0);
-  std::vector<int64_t> tmp;
-  S.scol.clear();
-  for (int r = 0; r < n; r++) {
-    tmp.clear();
-    for (int64_t k = M.ptr[(size_t)r]; k < M.ptr[(size_t)r + 1]; k++)
-      if (S.strong[(size_t)k] && M.col[(size_t)k] != r && M.col[(size_t)k] < n) tmp.push_back(k);
-    std::stable_sort(tmp.begin(), tmp.end(), [&](int64_t a, int64_t b) {
-      return std::fabs(M.val[(size_t)a]) > std::fabs(M.val[(size_t)b]);
-    });
-    for (int64_t k : tmp) S.scol.push_back(M.col[(size_t)k]);
-    S.sptr[(size_t)r + 1] = (int64_t)S.scol.size();
-  }
+  S.scol.assign((size_t)S.sptr.back(), 0);
+  parallel_rows(n, [&](int lo, int hi) {
+    std::vector<int64_t> tmp;
+    for (int r = lo; r < hi; r++) {
+      tmp.clear();
+      for (int64_t k = M.ptr[(size_t)r]; k < M.ptr[(size_t)r + 1]; k++)
+        if (S.strong[(size_t)k] && M.col[(size_t)k] != r && M.col[(size_t)k] < n) tmp.push_back(k);
+      std::stable_sort(tmp.begin(), tmp.end(), [&](int64_t a, int64_t b) {
+        return std::fabs(M.val[(size_t)a]) > std::fabs(M.val[(size_t)b]);
+      });
+      int64_t q = S.sptr[(size_t)r];
+      for (int64_t k : tmp) S.scol[(size_t)q++] = M.col[(size_t)k];
+    }
+  });
 }
 
 // Persistent state of the reference's aggregation (SAVE variables):
@@ -1199,9 +1233,11 @@ static Coo smoother(const Csr &A, const std::vector<char> &strong, double omega,
 // AC = R T with R's rows re-bucketed from that column order.  Fills out.R
 // (rows = coarse freedoms, columns ascending), out.P (= R^T, coarse freedoms
 // ascending per fine node) and R's final COO order in out.R_i/R_j/R_v.
-static Csr galerkin(const Csr &A, const Coo &Rcoo, int n, SetupResult &out) {
+static Csr galerkin(const Csr &A, const Coo &Rcoo, int n, SetupResult &out, PhaseTimer *tm = nullptr) {
   Csr Rcols = cols_of(Rcoo);                 // column view: for each fine node, coarse freedoms ascending
+  if (tm) tm->lap("R by columns");
   Csr Tm = spgemm_first_touch(A, Rcols);     // n x ncoarse
+  if (tm) tm->lap("T = A R^T");
   Coo RcolOrder;                             // R's COO after arrangement by columns
   RcolOrder.nrows = Rcoo.nrows; RcolOrder.ncols = Rcoo.ncols;
   RcolOrder.i.reserve(Rcoo.size()); RcolOrder.j.reserve(Rcoo.size()); RcolOrder.v.reserve(Rcoo.size());
@@ -1214,6 +1250,7 @@ static Csr galerkin(const Csr &A, const Coo &Rcoo, int n, SetupResult &out) {
   out.R = rows_of(RcolOrder);
   out.P = Rcols;
   out.P.nrows = n; out.P.ncols = Rcoo.nrows;
+  if (tm) tm->lap("R by rows");
   Csr AC = spgemm_first_touch(out.R, Tm);
   out.R_i.clear(); out.R_j.clear(); out.R_v.clear();
   out.R_i.reserve(RcolOrder.size()); out.R_j.reserve(RcolOrder.size()); out.R_v.reserve(RcolOrder.size());
@@ -1389,8 +1426,10 @@ bool build_setup(const Controls &c_in, int n, const std::vector<int> &ii, const 
   AggState st;
   ScaledMatrix SA;
   SA.M = rows_of(A0);
+  tm.lap("arrange by rows");
   SA.symmetric = c.symmstruct && c.symmnumeric;
   scale_rows(SA);
+  tm.lap("scale");
   find_strong(SA, out.strong1);
   tm.lap("fine strength");
   if (!aggregate(SA, out.r1, out.min1, out.max1, out.strong1, false, st, out.fine, out.fine_full, err))
@@ -1416,8 +1455,10 @@ bool build_setup(const Controls &c_in, int n, const std::vector<int> &ii, const 
     Rcoo = T;
   } else {
     Coo S = smoother(A, SA.strong, c.omega, false);
+    tm.lap("smoother");
     if (sm == 1) {
       R = spgemm_first_touch(Trows, cols_of(S));
+      tm.lap("R = T S^T");
     } else {
       Coo S2 = smoother(A, SA.strong, c.omega, true);
       Csr SS = spgemm_first_touch(rows_of(S2), rows_of(S));
@@ -1455,8 +1496,9 @@ bool build_setup(const Controls &c_in, int n, const std::vector<int> &ii, const 
     Rcoo = Rh;
     tm.lap("robust coarse space");
   }
-  Csr AC = galerkin(A, Rcoo, n, out);
-  tm.lap("restriction + Galerkin");
+  tm.lap("restriction");
+  Csr AC = galerkin(A, Rcoo, n, out, &tm);
+  tm.lap("Galerkin");
   // Partitionings_aggr_InitCoarse (Partitioning_aggr.F90:120-193)
   out.strong2 = c.strong2 > 0 ? c.strong2 : out.strong1 / 2.0;
   ScaledMatrix SC;
