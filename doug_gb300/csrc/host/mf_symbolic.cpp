@@ -366,6 +366,47 @@ void append(const Local &L, const std::vector<int> &gid_of_local, MfBatch &B) {
   B.nfronts += nf;
 }
 
+// Appends batch P (built by append from an empty batch) to B: the result is
+// what appending P's matrices to B directly gives (offsets shifted by B's
+// sizes; the flop count is summed per piece).
+void merge(const MfBatch &P, MfBatch &B) {
+  const int base_front = B.nfronts;
+  const int64_t arena = B.arena, xlen = B.xlen, ulen = B.ulen, wlen = B.wlen;
+  const int64_t nrows = (int64_t)B.rows.size(), nrel = (int64_t)B.relmap.size();
+  const int64_t nasm = (int64_t)B.asm_tgt.size(), nsrc = (int64_t)B.asm_src.size();
+  const int nchild = (int)B.f_children.size();
+  for (int64_t v : P.xoff) B.xoff.push_back(v + xlen);
+  B.gidx.insert(B.gidx.end(), P.gidx.begin(), P.gidx.end());
+  for (int64_t v : P.f_off) B.f_off.push_back(v + arena);
+  B.f_m.insert(B.f_m.end(), P.f_m.begin(), P.f_m.end());
+  B.f_k.insert(B.f_k.end(), P.f_k.begin(), P.f_k.end());
+  for (int64_t v : P.f_rows) B.f_rows.push_back(v + nrows);
+  for (int64_t v : P.f_xoff) B.f_xoff.push_back(v + xlen);
+  B.f_p0.insert(B.f_p0.end(), P.f_p0.begin(), P.f_p0.end());
+  for (int64_t v : P.f_uoff) B.f_uoff.push_back(v + ulen);
+  for (int64_t v : P.f_woff) B.f_woff.push_back(v + wlen);
+  for (int v : P.f_child_ptr) B.f_child_ptr.push_back(v + nchild);
+  for (int v : P.f_children) B.f_children.push_back(v + base_front);
+  for (int64_t v : P.f_relmap) B.f_relmap.push_back(v + nrel);
+  for (int64_t v : P.f_asm) B.f_asm.push_back(v + nasm);
+  for (int v : P.f_parent) B.f_parent.push_back(v < 0 ? -1 : v + base_front);
+  B.f_level.insert(B.f_level.end(), P.f_level.begin(), P.f_level.end());
+  B.rows.insert(B.rows.end(), P.rows.begin(), P.rows.end());
+  B.relmap.insert(B.relmap.end(), P.relmap.begin(), P.relmap.end());
+  for (int64_t v : P.asm_tgt) B.asm_tgt.push_back(v + arena);
+  for (int64_t v : P.asm_sp) B.asm_sp.push_back(v + nsrc);
+  B.asm_src.insert(B.asm_src.end(), P.asm_src.begin(), P.asm_src.end());
+  B.nmat += P.nmat;
+  B.nfronts += P.nfronts;
+  B.arena += P.arena;
+  B.xlen += P.xlen;
+  B.ulen += P.ulen;
+  B.wlen += P.wlen;
+  B.factor_nnz += P.factor_nnz;
+  B.factor_flops += P.factor_flops;
+  B.max_m = std::max(B.max_m, P.max_m);
+}
+
 void finalize(MfBatch &B) {
   B.xoff.push_back(B.xlen);
   B.arena += 16;  // slack: staging copies round the last front up to 16 bytes
@@ -417,12 +458,12 @@ void mf_build_subdomains(const Csr &A, const std::vector<int64_t> &sd_ptr,
                          const std::vector<int> &sd_nodes, const MfOptions &opt, MfBatch &out) {
   out = MfBatch();
   int nsd = (int)sd_ptr.size() - 1;
-  std::vector<Local> locs((size_t)nsd);
-  std::vector<std::vector<int>> gids((size_t)nsd);
+  // every subdomain is analysed and laid out as its own batch on a host
+  // thread; the pieces are then joined in subdomain order
+  std::vector<MfBatch> pieces((size_t)nsd);
   parallel_for(nsd, [&](int s) {
     int64_t b0 = sd_ptr[(size_t)s], m = sd_ptr[(size_t)s + 1] - b0;
-    std::vector<int> &gid = gids[(size_t)s];
-    gid.resize((size_t)m);
+    std::vector<int> gid((size_t)m);
     // local position of each global node (sorted lookup keeps memory per subdomain small)
     std::vector<std::pair<int, int>> lut((size_t)m);
     for (int64_t t = 0; t < m; t++) {
@@ -444,26 +485,31 @@ void mf_build_subdomains(const Csr &A, const std::vector<int64_t> &sd_ptr,
         if (h >= 0) { lr.push_back((int)t); lc.push_back(h); src.push_back(e); }
       }
     }
-    analyse((int)m, lr, lc, src, opt.leaf, locs[(size_t)s]);
+    Local L;
+    analyse((int)m, lr, lc, src, opt.leaf, L);
+    append(L, gid, pieces[(size_t)s]);
   });
   // reserve the batch arrays once (they are large for big subdomains)
   {
-    size_t nf = 0, nr = 0, ne = 0;
-    for (const Local &L : locs) {
-      nf += L.p0.size();
-      for (const auto &r : L.rows) nr += r.size();
-      ne += L.er.size();
+    size_t nf = 0, nr = 0, ne = 0, nsrc = 0, nx = 0;
+    for (const MfBatch &P : pieces) {
+      nf += (size_t)P.nfronts;
+      nr += P.rows.size();
+      ne += P.asm_tgt.size();
+      nsrc += P.asm_src.size();
+      nx += P.gidx.size();
     }
     out.f_off.reserve(nf); out.f_m.reserve(nf); out.f_k.reserve(nf); out.f_rows.reserve(nf);
     out.f_xoff.reserve(nf); out.f_p0.reserve(nf); out.f_uoff.reserve(nf); out.f_woff.reserve(nf);
     out.f_parent.reserve(nf); out.f_level.reserve(nf); out.f_relmap.reserve(nf); out.f_asm.reserve(nf + 1);
     out.f_child_ptr.reserve(nf + 1); out.f_children.reserve(nf);
     out.rows.reserve(nr); out.relmap.reserve(nr);
-    out.asm_tgt.reserve(ne); out.asm_sp.reserve(ne + 1); out.asm_src.reserve(ne);
+    out.asm_tgt.reserve(ne); out.asm_sp.reserve(ne + 1); out.asm_src.reserve(nsrc);
+    out.gidx.reserve(nx);
   }
   for (int s = 0; s < nsd; s++) {
-    append(locs[(size_t)s], gids[(size_t)s], out);
-    Local().rows.swap(locs[(size_t)s].rows);  // release as we go
+    merge(pieces[(size_t)s], out);
+    MfBatch().rows.swap(pieces[(size_t)s].rows);  // release as we go
   }
   finalize(out);
 }
