@@ -90,6 +90,27 @@ def test_oracle_e4x4_fixture(words):
     assert len(r["subdomains"]) == 1 and len(r["subdomains"][0]) == 9
 
 
+# the reference harness's doug_geom runs on the e4x4 fixture
+# (tests/tests_all.conf:34-62): e1lev = levels 1, fine_methods 1,2, smoothers 0,
+# overlaps -1,0,1,2; e2lev = levels 2, fine_methods 1,2, smoothers 0,1,2, overlaps -1,0
+HARNESS = ([(1, f, 0, o) for f in (1, 2) for o in (-1, 0, 1, 2)] +
+           [(2, f, sm, o) for f in (1, 2) for sm in (0, 1, 2) for o in (-1, 0)])
+
+
+def _harness_words(levels, fine, smoothers, overlap):
+    return (f"executable geom\nlevels {levels}\nfine_method {fine}\nsmoothers {smoothers}\n"
+            f"overlap {overlap}\n")
+
+
+@pytest.mark.parametrize("levels,fine,smoothers,overlap", HARNESS)
+def test_oracle_e4x4_harness_matrix(levels, fine, smoothers, overlap):
+    r = O.run_ctl(os.path.join(E4, "DOUG.ctl"), _harness_words(levels, fine, smoothers, overlap))
+    assert r["status"] == 0, r["errmsg"]
+    ref = O.read_vector(os.path.join(E4, "csolution.xdr"), 2, 9)
+    assert np.linalg.norm(r["x"] - ref) <= 1e-9   # the harness accepts 1e-6
+    assert r["smoothers"] == (0 if levels == 2 else smoothers)
+
+
 @pytest.mark.parametrize("mesh", ["p1", "elas"])
 @pytest.mark.parametrize("words", WORDS)
 def test_host_setup_equals_oracle(request, mesh, words):
@@ -200,7 +221,8 @@ def test_geom_gpu_matches_oracle(request, precision, mesh, words, parts):
 
 @pytest.mark.gpu
 @pytest.mark.parametrize("words", ["executable geom\nlevels 1\n", GEOM, GEOM + "interpolation_type 2\n",
-                                   GEOM + "center_type 2\nmaxcie 9\ncutbal 1\n"])
+                                   GEOM + "center_type 2\nmaxcie 9\ncutbal 1\n"] +
+                         [_harness_words(*h) for h in HARNESS])
 def test_geom_gpu_e4x4_fixture(words):
     s = _product(os.path.join(E4, "DOUG.ctl"), words)
     s.setup()
