@@ -704,6 +704,24 @@ __device__ __forceinline__ void load_e_batch(const T *Ef, int ld, int m, int k, 
 
 // small fronts, forward: the first batch of E is loaded before the
 // right-hand side is assembled.  cta: this CTA's index within its bucket.
+// Programmatic dependent launch of the level solves.  pdl_trigger (at the
+// start of a CTA) lets the next kernel of the stream start its CTAs once
+// every CTA of this one has started; pdl_wait returns once the previous
+// kernel has completed and its writes are visible.  The solve bodies issue
+// their first loads of E (written by the factorisation, before any of these
+// kernels) and only then wait, before they read a vector that the previous
+// level wrote.  Without the launch attribute both instructions do nothing.
+__device__ __forceinline__ void pdl_trigger() {
+#if defined(__CUDA_ARCH__) && __CUDA_ARCH__ >= 900
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+#endif
+}
+__device__ __forceinline__ void pdl_wait() {
+#if defined(__CUDA_ARCH__) && __CUDA_ARCH__ >= 900
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+#endif
+}
+
 template <typename T, int G>
 __device__ __forceinline__ void fwd_small_body(const MfView &v, const int *__restrict__ fronts, int nf,
                                                const T *__restrict__ E, const T *__restrict__ xl,
@@ -721,6 +739,7 @@ __device__ __forceinline__ void fwd_small_body(const MfView &v, const int *__res
   const T *Ef = E + v.e_off[f];
   T e[PASS][kSmallUnroll][VN];
   load_e_batch<T, PASS, G>(Ef, ld, m, k, sl, 0, e);
+  pdl_wait();
   for (int i = sl; i < m; i += G) w[i] = i < k ? xl[xo + i] : T(0);
   __syncwarp(gm);
   for (int ci = v.f_child_ptr[f]; ci < v.f_child_ptr[f + 1]; ci++) {
@@ -777,6 +796,7 @@ __device__ __forceinline__ void bwd_small_body(const MfView &v, const int *__res
   const T *Ef = E + v.e_off[f];
   T e[PASS][kSmallUnroll][VN];
   load_e_batch<T, PASS, G>(Ef, ld, m, k, sl, 0, e);
+  pdl_wait();
   const T *xb = xl + v.f_xoff[f];
   const int *rows = v.rows + v.f_rows[f];
   for (int i = sl; i < ld; i += G) w[i] = i < k ? yl[xo + i] : (i < m ? __ldcg(xb + rows[i]) : T(0));
@@ -821,6 +841,7 @@ struct SmallBuckets {
   int nb0, nb1;           // CTAs of buckets 0 and 1
 };
 
+
 // Several right-hand sides (nrhs > 1): CTA x serves right-hand side x % nrhs
 // of the work unit x / nrhs, so the CTAs that read the same E are adjacent;
 // the vectors of right-hand side k start at k * xs (xl, yl) and k * us (u).
@@ -830,6 +851,7 @@ mf_fwd_small(MfView v, const int *__restrict__ fronts, SmallBuckets sb, const T 
              const T *__restrict__ xl, T *__restrict__ yl, T *__restrict__ uvec, int nrhs = 1, int64_t xs = 0,
              int64_t us = 0) {
   __shared__ __align__(16) T wsh[8 * kSolveSmall];
+  pdl_trigger();
   const int b = blockIdx.x / nrhs, rk = blockIdx.x % nrhs;
   xl += rk * xs;
   yl += rk * xs;
@@ -846,6 +868,7 @@ __global__ void __launch_bounds__(256, SmallMinBlocks<T>::N)
 mf_bwd_small(MfView v, const int *__restrict__ fronts, SmallBuckets sb, const T *__restrict__ E,
              const T *__restrict__ yl, T *__restrict__ xl, int nrhs = 1, int64_t xs = 0) {
   __shared__ __align__(16) T wsh[8 * kSolveSmall];
+  pdl_trigger();
   const int b = blockIdx.x / nrhs, rk = blockIdx.x % nrhs;
   yl += rk * xs;
   xl += rk * xs;
@@ -895,6 +918,7 @@ __device__ __forceinline__ void fwd_big_body(const MfView &v, int2 tk, const T *
   };
   auto chunk_cols = [&](int r0) { return r0 < k ? min(k, r0 + RC) : k; };
   load_batch(ch0 * RC, chunk_cols(ch0 * RC), wid);  // in flight while b is assembled
+  pdl_wait();
   for (int i = tid; i < m; i += NT) b[i] = i < k ? xl[xo + i] : T(0);
   __syncthreads();
   for (int ci = v.f_child_ptr[f]; ci < v.f_child_ptr[f + 1]; ci++) {
@@ -943,6 +967,7 @@ mf_fwd_big(MfView v, const int2 *__restrict__ tasks, const T *__restrict__ E, co
            T *__restrict__ yl, T *__restrict__ uvec, int nrhs = 1, int64_t xs = 0, int64_t us = 0) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ T red[NT / 32][FwdRows<T>::N];
+  pdl_trigger();
   const int task = blockIdx.x / nrhs, rk = blockIdx.x % nrhs;
   fwd_big_body<T, NT>(v, tasks[task], E, xl + rk * xs, yl + rk * xs, uvec + rk * us,
                       reinterpret_cast<T *>(smem_raw), red);
@@ -978,6 +1003,7 @@ __device__ __forceinline__ void bwd_big_body(const MfView &v, int2 tk, const T *
     }
   };
   load_batch(c0 + cs, c0 + rq * VN);  // in flight while v is gathered
+  pdl_wait();
   for (int i = c0 + tid; i < ld; i += NT) w[i - c0] = i < k ? yl[xo + i] : (i < m ? __ldcg(xb + rows[i]) : T(0));
   __syncthreads();
   for (int cc = cs; cc < 32; cc += NCS) {  // uniform trip count: the shuffles below need whole groups
@@ -1007,6 +1033,7 @@ __global__ void __launch_bounds__(NT, NT == kELeanThreads ? 12 : 4)
 mf_bwd_big(MfView v, const int2 *__restrict__ tasks, const T *__restrict__ E, const T *__restrict__ yl,
            T *__restrict__ xl, int nrhs = 1, int64_t xs = 0) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
+  pdl_trigger();
   const int task = blockIdx.x / nrhs, rk = blockIdx.x % nrhs;
   bwd_big_body<T, NT>(v, tasks[task], E, yl + rk * xs, xl + rk * xs, reinterpret_cast<T *>(smem_raw));
 }

@@ -75,9 +75,32 @@ struct MfTune {
   int64_t lean_task_bytes = 80 * 1024;   // levels with smaller average tasks use 128-thread CTAs
   int small_min_fronts = 304;            // levels with fewer small fronts solve them CTA-per-task
   int schedule = 0;                      // solves: 0 one launch per level, 1 dependency-driven queue
+  int pdl = 0;                           // 1: level launches with programmatic dependent launch
   int tiny_rows = 64;                    // panel fronts of at most this many rows: tiny_threads per CTA
   int tiny_threads = 64;
 };
+
+// Launch k with programmatic stream serialisation when pdl is set: its CTAs
+// may start while the previous kernel of the stream drains (the kernels call
+// pdl_enter before reading anything); otherwise an ordinary launch.
+template <typename... P, typename... A>
+void launch_level(bool pdl, void (*k)(P...), int grid, int block, size_t smem, cudaStream_t s, A... args) {
+  if (!pdl) {
+    k<<<grid, block, smem, s>>>(args...);
+    return;
+  }
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)grid);
+  cfg.blockDim = dim3((unsigned)block);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  CK(cudaLaunchKernelEx(&cfg, k, args...));
+}
 
 template <typename T>
 struct MfDevice {
@@ -87,6 +110,7 @@ struct MfDevice {
   int tiny_threads = 64;
   // dependency-driven schedule of the solves (solve_schedule 1)
   bool queue = false;
+  bool pdl = false;
   DBuf<int4> qf_tasks, qb_tasks;
   DBuf<int> qf_dep_ptr, qf_dep, qb_dep_ptr, qb_dep, q_small_off, q_counter, q_done;
   DBuf<SmallBuckets> q_sb;
@@ -332,6 +356,7 @@ struct MfDevice {
     set_solve_attrs<kEThreads>(optin, fwd_smem_max, bwd_smem_max);
     set_solve_attrs<kELeanThreads>(optin, fwd_smem_max, bwd_smem_max);
     queue = tune.schedule == 1;
+    pdl = tune.pdl == 1;
     tiny_threads = tune.tiny_threads;
     if (queue) plan_queue(B, ss, fw, bw, fwd_smem_max, bwd_smem_max);
   }
@@ -516,34 +541,29 @@ struct MfDevice {
     for (int l = 0; l < nlevels; l++) {
       const SolveLevel &L = slevels[(size_t)l];
       if (L.small_cta) {
-        mf_fwd_small<T><<<L.small_cta * nrhs, 256, 0, s>>>(view, solve_small.p + L.small_off, L.sb, E.p, xl_, yl_,
-                                                           u_, nrhs, xs, us);
+        launch_level(pdl, mf_fwd_small<T>, L.small_cta * nrhs, 256, 0, s, view,
+                     (const int *)(solve_small.p + L.small_off), L.sb, (const T *)E.p, (const T *)xl_, yl_, u_, nrhs,
+                     xs, us);
         launches++;
       }
       if (L.fwd_cnt) {
-        if (L.fwd_lean)
-          mf_fwd_big<T, kELeanThreads><<<L.fwd_cnt * nrhs, kELeanThreads, L.fwd_smem, s>>>(
-              view, fwd_tasks.p + L.fwd_off, E.p, xl_, yl_, u_, nrhs, xs, us);
-        else
-          mf_fwd_big<T, kEThreads><<<L.fwd_cnt * nrhs, kEThreads, L.fwd_smem, s>>>(
-              view, fwd_tasks.p + L.fwd_off, E.p, xl_, yl_, u_, nrhs, xs, us);
+        launch_level(pdl, L.fwd_lean ? mf_fwd_big<T, kELeanThreads> : mf_fwd_big<T, kEThreads>, L.fwd_cnt * nrhs,
+                     L.fwd_lean ? kELeanThreads : kEThreads, L.fwd_smem, s, view,
+                     (const int2 *)(fwd_tasks.p + L.fwd_off), (const T *)E.p, (const T *)xl_, yl_, u_, nrhs, xs, us);
         launches++;
       }
     }
     for (int l = nlevels - 1; l >= 0; l--) {
       const SolveLevel &L = slevels[(size_t)l];
       if (L.bwd_cnt) {
-        if (L.bwd_lean)
-          mf_bwd_big<T, kELeanThreads><<<L.bwd_cnt * nrhs, kELeanThreads, L.bwd_smem, s>>>(
-              view, bwd_tasks.p + L.bwd_off, E.p, yl_, xl_, nrhs, xs);
-        else
-          mf_bwd_big<T, kEThreads><<<L.bwd_cnt * nrhs, kEThreads, L.bwd_smem, s>>>(
-              view, bwd_tasks.p + L.bwd_off, E.p, yl_, xl_, nrhs, xs);
+        launch_level(pdl, L.bwd_lean ? mf_bwd_big<T, kELeanThreads> : mf_bwd_big<T, kEThreads>, L.bwd_cnt * nrhs,
+                     L.bwd_lean ? kELeanThreads : kEThreads, L.bwd_smem, s, view,
+                     (const int2 *)(bwd_tasks.p + L.bwd_off), (const T *)E.p, (const T *)yl_, xl_, nrhs, xs);
         launches++;
       }
       if (L.small_cta) {
-        mf_bwd_small<T><<<L.small_cta * nrhs, 256, 0, s>>>(view, solve_small.p + L.small_off, L.sb, E.p, yl_, xl_,
-                                                           nrhs, xs);
+        launch_level(pdl, mf_bwd_small<T>, L.small_cta * nrhs, 256, 0, s, view,
+                     (const int *)(solve_small.p + L.small_off), L.sb, (const T *)E.p, (const T *)yl_, xl_, nrhs, xs);
         launches++;
       }
     }
@@ -1108,6 +1128,7 @@ dg_status do_setup(dg_handle *h, bool reuse_host = false) {
   tune.lean_task_bytes = (int64_t)c.lean_task_kb * 1024;
   tune.small_min_fronts = c.thin_level_fronts;
   tune.schedule = c.solve_schedule;
+  tune.pdl = c.solve_pdl;
   MfOptions mo;
   mo.leaf = c.nd_leaf;
   const bool timing = std::getenv("DG_SETUP_TIMING") != nullptr;
@@ -1857,6 +1878,13 @@ dg_status dg_set_option(dg_handle *h, const char *name, const char *value) {
     int v;
     if (!parse_i10(w2, v)) return fail(h, DG_BAD_INPUT, "bad replace_every");
     h->ctl.replace_every = v;
+    return DG_OK;
+  }
+  if (w1 == "solve_pdl") {
+    int v;
+    if (!parse_i10(w2, v) || v < 0 || v > 1) return fail(h, DG_BAD_INPUT, "solve_pdl must be 0 or 1");
+    h->ctl.solve_pdl = v;
+    h->ready = false;
     return DG_OK;
   }
   if (w1 == "solve_schedule") {

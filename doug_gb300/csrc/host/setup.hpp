@@ -44,6 +44,7 @@ struct Controls {
   int lean_task_kb = 80;            // levels with smaller average tasks use 128-thread CTAs
   int thin_level_fronts = 304;      // levels with fewer small fronts solve them one CTA per task
   int solve_schedule = 0;           // multifrontal solves: 0 one launch per level, 1 dependency-driven queue
+  int solve_pdl = 1;                // 1: the level launches overlap through programmatic dependent launch
   int executable = -1;              // which reference driver: -1/0 doug_aggr, 1 doug_geom
 };
 
