@@ -23,12 +23,13 @@ def _ctl_text(d):
     return "".join(f"{k} {v}\n" for k, v in d.items())
 
 
-@pytest.mark.parametrize("word", ["panel_rows", "fwd_task_kb", "lean_task_kb", "thin_level_fronts", "solve_schedule"])
+@pytest.mark.parametrize("word", ["panel_rows", "fwd_task_kb", "lean_task_kb", "thin_level_fronts", "solve_schedule",
+                                  "solve_pdl"])
 def test_tuning_words_reject_bad_values(word):
     s = D.DougSolver({})
-    s.set_option(word, 1 if word == "solve_schedule" else 64)
-    for bad in ((-3, "x") if word == "thin_level_fronts" else (2, -1, "x") if word == "solve_schedule"
-                else (0, -3, "x")):
+    binary = word in ("solve_schedule", "solve_pdl")
+    s.set_option(word, 1 if binary else 64)
+    for bad in ((-3, "x") if word == "thin_level_fronts" else (2, -1, "x") if binary else (0, -3, "x")):
         with pytest.raises(D.DougError):
             s.set_option(word, bad)
 
@@ -45,7 +46,8 @@ def diffusion24():
 @pytest.mark.parametrize("words", [dict(panel_rows=16), dict(panel_rows=48, fwd_task_kb=4, lean_task_kb=1),
                                    dict(fwd_task_kb=1024, lean_task_kb=4096), dict(nd_leaf=8),
                                    dict(thin_level_fronts=0), dict(thin_level_fronts=100000),
-                                   dict(solve_schedule=1), dict(solve_schedule=1, thin_level_fronts=0)])
+                                   dict(solve_schedule=1), dict(solve_schedule=1, thin_level_fronts=0),
+                                   dict(solve_pdl=0)])
 @pytest.mark.parametrize("precision", [0, 1])
 def test_batch_parameters_keep_the_solution(diffusion24, words, precision):
     n, r, c, v, b, ro = diffusion24
@@ -78,3 +80,23 @@ def test_autotune_picks_a_grid_point_and_solves(diffusion24):
     x, st = s.solve()
     assert st.true_rel_residual <= 1.01e-10
     assert np.linalg.norm(x - ro["x"]) <= 1e-7 * np.linalg.norm(ro["x"])
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision", [0, 1])
+def test_pdl_launches_give_identical_results(diffusion24, precision):
+    """The programmatic dependent launch of the level solves changes when CTAs
+    start, not what they compute: the solutions are bit-identical."""
+    n, r, c, v, b, ro = diffusion24
+    xs = []
+    for pdl in (0, 1):
+        s = D.DougSolver(OPTS)
+        s.set_option("precision", precision)
+        s.set_option("solve_pdl", pdl)
+        s.set_matrix_coo(n, r, c, v)
+        s.set_rhs(b)
+        s.setup()
+        x, st = s.solve()
+        xs.append((x, st.iterations))
+    assert xs[0][1] == xs[1][1]
+    assert np.array_equal(xs[0][0].view(np.int64), xs[1][0].view(np.int64))
