@@ -300,6 +300,12 @@ def run_gpu(args, rank, world):
     err_mixed_vs_fp64 = float(np.linalg.norm(x_mixed - x64) / np.linalg.norm(x64))
     del sf
     torch.cuda.empty_cache()
+    small = None
+    if not args.no_small:
+        try:
+            small = run_small(args, max(args.steps, 3), max(args.warmup, 3))
+        except Exception as ex:
+            small = {"error": repr(ex)}
     batched = None
     if not args.no_batched:
         try:
@@ -360,6 +366,7 @@ def run_gpu(args, rank, world):
                 "api": "dg_solve (host buffers, pinned)"},
         "roofline": roofline, "cpu_baseline": cpu, "clocks": clocks,
         "gpu_launches": int(launches),
+        "small": small,
         "batched": batched,
         "elasticity": elasticity,
         "adjoint": adjoint,
@@ -375,6 +382,70 @@ BATCH_WORKLOAD = ("256 independent jittered 2-D P1 Poisson systems, unknowns log
                   "(seeded), each with its own two-level additive Schwarz (its own aggregation, "
                   "coarse-aggregate subdomains with overlap 1, smoothed-aggregation coarse grid), all "
                   "solved in one batch")
+
+
+SMALL_NODES = 129
+SMALL_CTL = dict(solver=2, method=1, fine_method=1, levels=2, overlap=1, smoothers=1, strong1="0.08",
+                 radius1=2, solve_tolerance=TOL, solve_maxiters=1000, omega=repr(2.0 / 3.0))
+SMALL_WORKLOAD = ("2-D P1 Poisson on a 129x129 jittered node grid (16,129 unknowns), 4 subdomains (2x2 quadrants, "
+                  "imported), overlap 1, smoothed-aggregation coarse grid with omega 2/3")
+
+
+def run_small(args, steps, warmup):
+    """The small plain case: the whole solve on the GPU (FP64 and mixed) and
+    the oracle's whole setup + solve on one host core beside it."""
+    import torch
+    import doug_gb300 as D
+    from doug_gb300 import problems as P
+
+    D.build_library()
+    n, r, c, v, b, xy = P.poisson2d_p1(SMALL_NODES, seed=SEED)
+    part = (1 + (xy[:, 0] >= 0.5) * 2 + (xy[:, 1] >= 0.5)).astype(np.int32)
+    stream = torch.cuda.current_stream()
+    sptr = stream.cuda_stream
+    bd = torch.tensor(b, dtype=torch.float64, device="cuda")
+    xd = torch.empty_like(bd)
+    out = {"config": {"workload": SMALL_WORKLOAD, "n": n, "nnz": int(len(v)), "subdomains": 4,
+                      "controls": SMALL_CTL}}
+    xs = {}
+    for prec, key in ((0, "fp64"), (1, "mixed")):
+        s = D.DougSolver(SMALL_CTL)
+        s.set_option("precision", prec)
+        s.set_matrix_coo(n, r, c, v)
+        s.set_rhs(b)
+        s.set_partition(part)
+        t0 = time.perf_counter()
+        s.setup()
+        setup_s = time.perf_counter() - t0
+        for _ in range(warmup):
+            st = s.solve_device(bd.data_ptr(), xd.data_ptr(), sptr)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(steps):
+            st = s.solve_device(bd.data_ptr(), xd.data_ptr(), sptr)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        xs[key] = xd.cpu().numpy()
+        out[key] = {"solve_s": e0.elapsed_time(e1) * 1e-3 / steps, "iterations": st.iterations,
+                    "true_rel_residual": st.true_rel_residual, "setup_host_s": setup_s}
+        del s
+    out["mixed_rel_err_vs_fp64_solution"] = float(np.linalg.norm(xs["mixed"] - xs["fp64"]) / np.linalg.norm(xs["fp64"]))
+    if not args.no_cpu_baseline:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle as O
+        ctl = "".join(f"{k} {v_}\n" for k, v_ in SMALL_CTL.items())
+        t0 = time.perf_counter()
+        ro = O.run_coo(n, r, c, v, rhs=b, ctl=ctl, part=part)
+        wall = time.perf_counter() - t0
+        out["cpu_reference_port"] = {"value": wall, "unit": "s", "cores": 1, "kind": "port",
+                                     "sample": "the whole workload: the oracle's setup, exact subdomain and "
+                                               "coarse factorisations and PCG to 1e-8, one host core",
+                                     "iterations": ro["iterations"], "setup_s": ro["t_setup"],
+                                     "factor_s": ro["t_factor"], "solve_s": ro["t_solve"],
+                                     "gpu_fp64_rel_err_vs_oracle": float(np.linalg.norm(xs["fp64"] - ro["x"]) /
+                                                                         np.linalg.norm(ro["x"]))}
+    return out
 
 
 def run_batched(args, steps, warmup):
@@ -666,6 +737,7 @@ def main():
     ap.add_argument("--fp64-steps", type=int, default=1)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batched", action="store_true", help="skip the batched uneven-systems workload")
+    ap.add_argument("--no-small", action="store_true", help="skip the small 129x129 P1 workload")
     ap.add_argument("--no-elasticity", action="store_true", help="skip the elemental elasticity workload")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the differentiation workload")
     ap.add_argument("--fd-elements", type=int, default=50, help="finite-difference checks of --workload adjoint")

@@ -79,6 +79,7 @@ typedef struct {
   int interpolation_type;
   int maxcie, maxnd, cutbal, center_type, hanging_nodes;
   int executable; /* extension word: -1/0 doug_aggr, 1 doug_geom */
+  double omega;   /* extension word: prolongator smoother weight (the reference's 1/3 when unset) */
   /* master data */
   char assembled_mtx_file[300];
   int assembled_mtx_format;
@@ -105,6 +106,7 @@ static void ctl_defaults(ctl_t *c) {
   c->maxcie = c->maxnd = c->cutbal = c->center_type = -1;
   c->hanging_nodes = 0;
   c->executable = -1;
+  c->omega = -1.0;
   c->assembled_mtx_format = -1;
   c->assembled_rhs_format = -1;
   c->solution_format = -1;
@@ -219,6 +221,15 @@ static void ctl_action(ctl_t *c, const char *w1, const char *w2) {
   SETS(info_file) SETS(freedom_lists_file) SETS(elemmat_rhs_file)
   SETS(coords_file) SETS(freemap_file)
   SETI(maxcie) SETI(maxnd) SETI(cutbal) SETI(center_type) SETL(hanging_nodes)
+  if (!strcmp(w1, "omega")) { /* not a reference word: parsed as a C double, first value wins */
+    if (c->omega == -1.0) {
+      char *end = NULL;
+      double v = strtod(w2, &end);
+      if (!end || *end || !(v > 0)) orc_abort("bad omega: '%s'", w2);
+      c->omega = v;
+    }
+    return;
+  }
   if (!strcmp(w1, "executable")) { /* not a reference word: which of the reference's drivers */
     if (c->executable == -1) {
       if (!strcmp(w2, "aggr")) c->executable = 0;
@@ -1098,9 +1109,9 @@ static spm build_smoother(const spm *A, double omega, int assign_diag) {
 }
 
 /* IntRestBuild (CoarseMtx.F90:50-474), np=1 (no ghost matrix). */
-static spm int_rest_build(const spm *A, const aggrs *ag, int smoothers) {
-  const double omega = 0.33333333333333;  /* :64 */
-  const double omega2 = 0.33333333333333; /* :67 */
+static spm int_rest_build(const spm *A, const aggrs *ag, int smoothers, double w) {
+  const double omega = w > 0 ? w : 0.33333333333333;   /* :64 */
+  const double omega2 = w > 0 ? w : 0.33333333333333;  /* :67 */
   int Tnrows = A->nrows, i, j, k;
   int nz = ag->starts[ag->nagr + 1] - 1, nagr = ag->nagr;
   spm T = spm_new(nz, nagr, Tnrows);
@@ -2575,7 +2586,7 @@ static void run_setup(state *s, const int *part, int nparts) {
   /* CoarsePreconditioner_smooth_Init (CoarsePreconditioner_smooth.F90:47-89) */
   if (c->coarse_method > 2) orc_abort("Wrong coarse method %d", c->coarse_method);
   if (c->smoothers > c->radius1) c->smoothers = c->radius1; /* CoarseMtx.F90:75-78 */
-  s->R = int_rest_build(&s->A, &s->fine_inner, c->smoothers);
+  s->R = int_rest_build(&s->A, &s->fine_inner, c->smoothers, c->omega);
   if (c->coarse_method == 2) { /* aggr.F90:158-160 */
     spm Rh = robust_restriction(&s->A, &s->R);
     spm_free(&s->R);
