@@ -190,6 +190,17 @@ def cpu_sample(n, r, c, v, part, iterations, workers=1):
     return est, {"factor_s": tf, "solves_s": ts, "wall_s": wall}, sample
 
 
+def max_over_ranks(t, world, device="cuda"):
+    """The slowest rank's time: with N GPUs every rank solves its own replica
+    of the workload, and the step takes as long as the slowest one."""
+    if world <= 1:
+        return t
+    import torch
+    tt = torch.tensor([t], device=device, dtype=torch.float64)
+    torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+    return float(tt.item())
+
+
 def run_reference(args, rank, world):
     if rank != 0:
         return 0
@@ -252,11 +263,7 @@ def run_gpu(args, rank, world):
         torch.cuda.synchronize()
     if world > 1:
         torch.distributed.barrier()
-    t_mixed = e0.elapsed_time(e1) * 1e-3 / args.steps
-    if world > 1:
-        tt = torch.tensor([t_mixed], device="cuda", dtype=torch.float64)
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        t_mixed = float(tt.item())
+    t_mixed = max_over_ranks(e0.elapsed_time(e1) * 1e-3 / args.steps, world)
     last = st
     # accuracy of the mixed solve against the FP64 path (below)
     x_mixed = xd.cpu().numpy()
