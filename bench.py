@@ -131,63 +131,59 @@ def _solver(n, r, c, v, b, part, precision):
     return s
 
 
-def _subdomain_sample(n, r, c, v, part, box=(1, 1, 1)):
-    """Index set of one interior subdomain (its box plus two overlap layers)
-    and its principal submatrix, 0-based COO."""
-    import scipy.sparse as sp
-    A = sp.csr_matrix((v, (r - 1, c - 1)), shape=(n, n))
-    pid = (box[0] * PARTS_PER_DIM + box[1]) * PARTS_PER_DIM + box[2] + 1
-    inds = np.flatnonzero(part == pid)
-    mask = np.zeros(n, bool)
-    mask[inds] = True
-    pat = A.copy()
-    pat.data[:] = 1.0
-    for _ in range(int(CTL["overlap"])):  # overlap layers over the matrix graph (Add_layers)
-        mask = mask | ((pat @ mask.astype(np.float64)) != 0)
-    idx = np.flatnonzero(mask)
-    S = A[idx][:, idx].tocoo()
-    return len(idx), S.row, S.col, S.data
+def _ctl_text(ctl):
+    return "".join(f"{k} {v}\n" for k, v in ctl.items())
 
 
-def _oracle_sample_worker(args):
-    m, rows, cols, vals, nsolves = args
+def _config(n, nnz, nsub, ncoarse):
+    """The workload description both arms print (the same dict)."""
+    return {"workload": WORKLOAD, "n": int(n), "nnz": int(nnz), "subdomains": int(nsub),
+            "coarse_unknowns": int(ncoarse), "controls": CTL,
+            "l2": "working set (factors ~2 GB) far larger than the 129 MB L2; no flush needed"}
+
+
+def host_threads():
+    """Host threads the CPU legs use: every core of this process's affinity set."""
+    try:
+        return max(1, len(os.sched_getaffinity(0)))
+    except AttributeError:
+        return max(1, os.cpu_count() or 1)
+
+
+def oracle_whole_run(n, r, c, v, b, part, threads, steps, warmup):
+    """The oracle's whole solve of the workload on `threads` host threads:
+    its setup once (aggregation, R, AC, subdomains), then per step what a GPU
+    step does: numeric factorisations of every subdomain matrix and of the
+    coarse matrix (exact nested-dissection multifrontal Cholesky, standing in
+    for the reference's UMFPACK) and the two-level PCG to 1e-8."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as O
-    rng = np.random.default_rng(0)
-    b = rng.uniform(-1, 1, m)
+    O.set_threads(threads)
     t0 = time.perf_counter()
-    f = O.SpdFactor(m, rows, cols, vals)
-    t1 = time.perf_counter()
-    for _ in range(nsolves):
-        f.solve(b)
-    t2 = time.perf_counter()
-    return t1 - t0, t2 - t1
+    sess = O.Session(n, r, c, v, _ctl_text(CTL), part)
+    setup_s = time.perf_counter() - t0
+    for _ in range(warmup):
+        sess.solve(b)
+    times, res = [], None
+    for _ in range(steps):
+        t = time.perf_counter()
+        res = sess.solve(b)
+        times.append(time.perf_counter() - t)
+        if res["status"] != 0:
+            raise RuntimeError("oracle solve failed: " + res["errmsg"])
+    info = {"setup_s": setup_s, "factor_s": res["t_factor"], "pcg_s": res["t_solve"],
+            "iterations": res["iterations"], "subdomains": len(sess.setup["subdomains"]),
+            "coarse_unknowns": sess.setup["AC"][0]}
+    sess.close()
+    return times, res, info
 
 
-def cpu_sample(n, r, c, v, part, iterations, workers=1):
-    """Time the oracle's exact subdomain factor + `iterations` subdomain solves
-    for `workers` subdomains in parallel processes, and scale to the 64
-    subdomains of the workload."""
-    import multiprocessing as mp
-    m, sr, sc, sv = _subdomain_sample(n, r, c, v, part)
-    nsd = PARTS_PER_DIM ** 3
-    t0 = time.perf_counter()
-    if workers <= 1:
-        tf, ts = _oracle_sample_worker((m, sr, sc, sv, iterations))
-        wall = tf + ts
-    else:
-        ctx = mp.get_context("spawn")
-        with ctx.Pool(workers) as pool:
-            res = pool.map(_oracle_sample_worker, [(m, sr, sc, sv, iterations)] * workers)
-        wall = time.perf_counter() - t0
-        tf = max(x[0] for x in res)
-        ts = max(x[1] for x in res)
-    est = wall * (-(-nsd // workers))
-    sample = (f"interior subdomain (box + 2 overlap layers, {m} unknowns) of the 64: oracle "
-              f"exact factorisation + {iterations} subdomain solves on {workers} core(s) "
-              f"{'in parallel' if workers > 1 else ''}, x{-(-nsd // workers)} for 64 subdomains; "
-              f"coarse solve, SpMV and vector work omitted (a lower bound of the CPU solve)")
-    return est, {"factor_s": tf, "solves_s": ts, "wall_s": wall}, sample
+def _oracle_sample(threads, info):
+    return (f"the whole workload every step: numeric factorisations of the {info['subdomains']} subdomain "
+            f"matrices and the coarse matrix ({info['coarse_unknowns']} unknowns) by the oracle's exact "
+            f"nested-dissection multifrontal Cholesky, then its two-level PCG to 1e-8 "
+            f"({info['iterations']} iterations), on {threads} host threads; the oracle's setup "
+            f"(aggregation, R, AC, subdomains: {info['setup_s']:.2f} s) once before, like the GPU's")
 
 
 def max_over_ranks(t, world, device="cuda"):
@@ -202,27 +198,24 @@ def max_over_ranks(t, world, device="cuda"):
 
 
 def run_reference(args, rank, world):
+    """The CPU arm: the oracle's restatement of DOUG's solve (the reference
+    itself needs gfortran, MPI, METIS and UMFPACK, none of which the GPU host
+    has) on the same workload, one whole solve per step on all host threads."""
     if rank != 0:
         return 0
     n, r, c, v, b, part = _problem()
-    iterations = int(os.environ.get("DG_REF_ITERS", "62"))  # the GPU solves take 62 iterations here
-    workers = max(1, min(os.cpu_count() or 1, 16))
-    # warm-up: a small sample (loads and builds the oracle)
-    for _ in range(max(1, min(args.warmup, 1))):
-        cpu_sample_small = _oracle_sample_worker((8, np.arange(8), np.arange(8), np.ones(8), 1))
-        del cpu_sample_small
-    vals = []
-    info = None
-    for _ in range(args.steps):
-        est, info, sample = cpu_sample(n, r, c, v, part, iterations, workers)
-        vals.append(est)
-    value = float(np.mean(vals))
+    threads = host_threads()
+    times, res, info = oracle_whole_run(n, r, c, v, b, part, threads, args.steps, args.warmup)
+    value = float(np.mean(times))
     line = {"metric": METRIC, "value": value, "unit": "s", "impl": "reference", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": value * 1e3,
             "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic (seeded)", "config": {"workload": WORKLOAD, "sample": "see cpu_baseline"},
-            "cpu_baseline": {"value": value, "unit": "s", "cores": workers, "kind": "port",
-                             "sample": sample, "detail": info},
+            "data": "synthetic (seeded generator, doug_gb300/problems.py)",
+            "config": _config(n, len(v), info["subdomains"], info["coarse_unknowns"]),
+            "iterations": info["iterations"], "setup_s": info["setup_s"],
+            "phases": {"factor_s": info["factor_s"], "pcg_s": info["pcg_s"]},
+            "cpu_baseline": {"value": value, "unit": "s", "cores": threads, "kind": "port",
+                             "sample": _oracle_sample(threads, info)},
             "e2e": {"value": value, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
     return 0
@@ -352,20 +345,27 @@ def run_gpu(args, rank, world):
               "subsolve_s": prof.t_subsolve_s, "coarse_s": prof.t_coarse_s, "spmv_s": prof.t_spmv_s,
               "spmv_GBps": (prof.spmv_bytes * prof.iterations / prof.t_spmv_s / 1e9) if prof.t_spmv_s else None}
     cpu = None
+    vs_oracle = None
     if not args.no_cpu_baseline:
-        est, info, sample = cpu_sample(n, r, c, v, part, last.iterations, workers=1)
-        cpu = {"value": est, "unit": "s", "cores": 1, "kind": "port", "sample": sample, "detail": info}
+        threads = host_threads()
+        times, ores, info = oracle_whole_run(n, r, c, v, b, part, threads, 1, 0)
+        cpu = {"value": times[0], "unit": "s", "cores": threads, "kind": "port",
+               "sample": _oracle_sample(threads, info), "detail": info}
+        xo = ores["x"]
+        vs_oracle = {"fp64_rel_err": float(np.linalg.norm(x64 - xo) / np.linalg.norm(xo)),
+                     "fp64_iterations": stf.iterations,
+                     "mixed_rel_err": float(np.linalg.norm(x_mixed - xo) / np.linalg.norm(xo)),
+                     "mixed_iterations": last.iterations, "oracle_iterations": ores["iterations"]}
     clocks = clk.summary()
     line = {
         "metric": METRIC, "value": t_mixed, "unit": "s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": t_mixed * 1e3, "higher_is_better": False,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64 outer / f32 subdomain factors",
         "data": "synthetic (seeded generator, doug_gb300/problems.py)",
-        "config": {"workload": WORKLOAD, "n": n, "nnz": int(len(v)), "subdomains": last.nsubdomains,
-                   "coarse_unknowns": last.ncoarse, "controls": CTL,
-                   "l2": "working set (factors ~2 GB) far larger than the 129 MB L2; no flush needed",
-                   "parallelism": "replicas" if world > 1 else "1 GPU"},
+        "config": _config(n, len(v), last.nsubdomains, last.ncoarse),
+        "parallelism": "replicas" if world > 1 else "1 GPU",
         "iterations": last.iterations, "true_rel_residual": last.true_rel_residual,
+        "vs_oracle": vs_oracle,
         "fp64_s": t_fp64, "fp64_iterations": stf.iterations, "mixed_vs_fp64": t_mixed / t_fp64,
         "mixed_rel_err_vs_fp64_solution": err_mixed_vs_fp64,
         "setup_host_s": setup_s, "phases_mixed": phases,

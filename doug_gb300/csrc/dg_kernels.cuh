@@ -11,7 +11,12 @@
 //   * CSR SpMV fused with the CG direction update and the p.q partial sums;
 //   * fused PCG vector updates with deterministic two-pass reductions.
 //
-// All waits are __syncthreads barriers; no kernel spins on memory.
+// The level kernels wait only at hardware barriers (__syncthreads,
+// __syncwarp, griddepcontrol.wait).  The optional dependency-driven solve
+// schedule (mf_fwd_queue / mf_bwd_queue, option solve_schedule 1) polls the
+// done flags of its producer tasks with clock64 + __nanosleep; every such
+// wait is bounded, and on timeout it sets ERR_WAIT in the error word, skips
+// the task's remaining waits and returns, and the host reports DG_CUDA_ERROR.
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>

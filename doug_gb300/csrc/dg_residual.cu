@@ -116,10 +116,42 @@ static __device__ __align__(256) double g_noalloc_partials[kNoAllocMaxPartials];
 
 // Host code may not use g_noalloc_partials as an address: on the host the
 // name refers to a stand-in variable, not to device memory.  The device
-// address is looked up once per device (with that device current) and cached.
+// address is looked up with the device current and cached per device,
+// together with the id of the CUDA context it belongs to: after a
+// cudaDeviceReset the device gets a new primary context, into which the
+// library's module (and the array) is loaded again, possibly elsewhere, so a
+// changed context id makes the next call look the address up again.
 constexpr int kMaxDevices = 128;
 static double *g_noalloc_ptr[kMaxDevices];
+static unsigned long long g_noalloc_ctx[kMaxDevices];
 static std::mutex g_noalloc_mu;
+
+// cuCtxGetCurrent / cuCtxGetId through the runtime's driver entry points,
+// so that the library does not link the driver library itself.
+typedef int (*ctx_get_current_fn)(void **ctx);
+typedef int (*ctx_get_id_fn)(void *ctx, unsigned long long *id);
+static ctx_get_current_fn g_ctx_get_current;
+static ctx_get_id_fn g_ctx_get_id;
+
+// The id of the calling thread's current context (0: none yet).
+static cudaError_t current_context_id(unsigned long long *id) {
+  *id = 0;
+  if (!g_ctx_get_current || !g_ctx_get_id) {
+    cudaDriverEntryPointQueryResult q1, q2;
+    void *f1 = nullptr, *f2 = nullptr;
+    cudaError_t e = cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f1, 12000, cudaEnableDefault, &q1);
+    if (e != cudaSuccess || q1 != cudaDriverEntryPointSuccess) return e != cudaSuccess ? e : cudaErrorNotSupported;
+    e = cudaGetDriverEntryPointByVersion("cuCtxGetId", &f2, 12000, cudaEnableDefault, &q2);
+    if (e != cudaSuccess || q2 != cudaDriverEntryPointSuccess) return e != cudaSuccess ? e : cudaErrorNotSupported;
+    g_ctx_get_current = reinterpret_cast<ctx_get_current_fn>(f1);
+    g_ctx_get_id = reinterpret_cast<ctx_get_id_fn>(f2);
+  }
+  void *ctx = nullptr;
+  if (g_ctx_get_current(&ctx) != 0) return cudaErrorUnknown;
+  if (!ctx) return cudaSuccess;
+  if (g_ctx_get_id(ctx, id) != 0) return cudaErrorUnknown;
+  return cudaSuccess;
+}
 
 static cudaError_t noalloc_scratch(double **out) {
   int dev = 0;
@@ -127,11 +159,18 @@ static cudaError_t noalloc_scratch(double **out) {
   if (e != cudaSuccess) return e;
   if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
   std::lock_guard<std::mutex> lk(g_noalloc_mu);
-  if (!g_noalloc_ptr[dev]) {
+  unsigned long long ctx = 0;
+  e = current_context_id(&ctx);
+  if (e != cudaSuccess) return e;
+  if (!g_noalloc_ptr[dev] || ctx == 0 || ctx != g_noalloc_ctx[dev]) {
     double *p = nullptr;
+    // loads the module into the device's primary context if it is not yet
     e = cudaGetSymbolAddress(reinterpret_cast<void **>(&p), g_noalloc_partials);
     if (e != cudaSuccess) return e;
+    e = current_context_id(&ctx);
+    if (e != cudaSuccess) return e;
     g_noalloc_ptr[dev] = p;
+    g_noalloc_ctx[dev] = ctx;
   }
   *out = g_noalloc_ptr[dev];
   return cudaSuccess;

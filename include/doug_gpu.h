@@ -64,7 +64,8 @@ typedef struct {
   double init_norm;           /* ||b - A x0||_2 */
   double final_norm;          /* ||r_k||_2 of the recurrence */
   double true_rel_residual;   /* ||b - A x||_2 / ||b - A x0||_2 (FP64 recomputed) */
-  double cond_num;            /* Lanczos estimate lambda_max / lambda_min */
+  double cond_num;            /* Lanczos estimate lambda_max / lambda_min (FP64 path; 0 when the
+                                 tridiagonal is degenerate: a zero alpha or a negative beta) */
   double t_setup_s;           /* host setup: aggregation, R, AC, symbolic analysis */
   double t_factor_s;          /* GPU numeric factorisations (subdomains + coarse) */
   double t_iterate_s;         /* GPU PCG iterations */
@@ -205,6 +206,8 @@ dg_status dg_residual_csr(int n, const long long *d_rowptr, const int *d_col, co
  * rows), larger n returns DG_BAD_INPUT.  The first call on each device looks
  * up the array's device address (the calling thread's current device must be
  * the stream's device), so make that first call before any stream capture.
+ * The address is kept per device and CUDA context: after a cudaDeviceReset
+ * the next call (again outside any capture) looks it up in the new context.
  * All calls share the array: calls that overlap on the GPU (other streams,
  * other threads) race and must be serialised by the caller. */
 dg_status dg_residual_csr_noalloc(int n, const long long *d_rowptr, const int *d_col,

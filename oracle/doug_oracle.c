@@ -16,6 +16,7 @@
  * fixtures tests/assembled/lap4x4 and tests/assembled/lap16x16.
  */
 #include "doug_oracle.h"
+#include "spchol.h"
 
 #include <ctype.h>
 #include <limits.h>
@@ -26,6 +27,9 @@
 #include <stdlib.h>
 #include <string.h>
 #include <time.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
 
 /* ------------------------------------------------------------------ */
 /* error handling: DOUG_abort (DOUG_utils.F90:254-286) becomes a longjmp */
@@ -674,18 +678,21 @@ static int lets_colour(colour_ctx *c, int innode, int *nneigs) {
   *nneigs = 0;
   long virt = 2L * c->maxasize * c->maxasize;
   if (virt > 50000000L) orc_abort("maxasize too large");
-  c->cap = (int)virt;
-  c->rcap = c->maxasize;
-  c->inlayer = NEWI(c->cap);
-  c->newlayer = NEWI(c->cap);
-  c->roundernodes = NEWI(c->rcap);
+  if (!c->inlayer) { /* the reference's work arrays (Aggregate_mod.F90:305-310), allocated
+                      * once per aggregation here and kept across calls: every entry is
+                      * written before it is read */
+    c->cap = (int)virt;
+    c->rcap = c->maxasize;
+    c->inlayer = (int *)malloc(sizeof(int) * ((size_t)c->cap + 1));
+    c->newlayer = (int *)malloc(sizeof(int) * ((size_t)c->cap + 1));
+    c->roundernodes = (int *)malloc(sizeof(int) * ((size_t)c->rcap + 1));
+    if (!c->inlayer || !c->newlayer || !c->roundernodes) orc_abort("out of memory");
+  }
   c->stat[innode] = 1;
   c->distance[innode] = 0;
   int ninnodes = 1;
   c->inlayer[1] = innode;
-  int ok = can_add_roundlayer(c, 0, &ninnodes, nneigs);
-  free(c->inlayer); free(c->newlayer); free(c->roundernodes);
-  return ok;
+  return can_add_roundlayer(c, 0, &ninnodes, nneigs);
 }
 
 /* SpMtx_aggregate (SpMtx_aggregation.F90:49-641), numprocs==1. */
@@ -713,6 +720,7 @@ static void spm_aggregate(spm *A, aggrs *inner, aggrs *full, int neighood,
     if (!coarse) g_beta = alpha / 4.0;
     int ngoodstarts = 0;
     int *nextgoodstart = NEWI(n);
+    int *seen = NEWI(n), seen_stamp = 0;
     int firstwocol = 1;
     colour_ctx c;
     memset(&c, 0, sizeof c);
@@ -739,10 +747,14 @@ static void spm_aggregate(spm *A, aggrs *inner, aggrs *full, int neighood,
         if (done) break;
         startnode = firstwocol;
       } else {
+        /* the first entry that repeats an earlier one (SpMtx_aggregation.F90:206-218), found with
+         * a marker per node instead of the pairwise scan */
         startnode = 0;
-        for (i = 2; i <= ngoodstarts && !startnode; i++)
-          for (j = 1; j <= i - 1; j++)
-            if (nextgoodstart[i] == nextgoodstart[j]) { startnode = nextgoodstart[i]; break; }
+        seen_stamp++;
+        for (i = 1; i <= ngoodstarts; i++) {
+          if (seen[nextgoodstart[i]] == seen_stamp) { startnode = nextgoodstart[i]; break; }
+          seen[nextgoodstart[i]] = seen_stamp;
+        }
         if (startnode == 0) startnode = nextgoodstart[1];
       }
       ok = lets_colour(&c, startnode, &nneigs);
@@ -795,6 +807,8 @@ static void spm_aggregate(spm *A, aggrs *inner, aggrs *full, int neighood,
         if (stat[node] != D_AGGREGATED) { distance[node] = 0; stat[node] = 0; }
       }
     }
+    free(c.inlayer); free(c.newlayer); free(c.roundernodes);
+    free(seen);
     free(nextgoodstart); free(distance); free(nodes); free(stat);
   } else {
     /* Cartesian aggregates (:332-346); a radius below 1 is an integer
@@ -1312,184 +1326,34 @@ static int add_layers(const int *adjBounds, const int *adjValues, int *nodes,
 }
 
 /* ------------------------------------------------------------------ */
-/* exact SPD solver: reverse Cuthill-McKee + profile (envelope)         */
-/* Cholesky.  Stands in for UMFPACK's exact LU (Fact.F90:102-159); both */
+/* exact SPD solves: spchol.c (nested dissection + multifrontal         */
+/* Cholesky) stands in for UMFPACK's exact LU (Fact.F90:102-159); both   */
 /* are exact solves, so results agree to rounding.                      */
 /* ------------------------------------------------------------------ */
-typedef struct {
-  int n;
-  int *perm;      /* new -> old (0-based) */
-  int *iperm;     /* old -> new */
-  long *rowptr;   /* start of row i in env (0-based), n+1 */
-  int *first;     /* first column of row i */
-  double *env;    /* row i holds L(i, first[i]..i) */
-} profchol;
-
-static void pc_free(profchol *f) {
-  free(f->perm); free(f->iperm); free(f->rowptr); free(f->first); free(f->env);
-  memset(f, 0, sizeof *f);
-}
-
-/* Build a factor from 0-based COO (duplicates summed, as umf4triplet2col). */
-static void pc_factor(profchol *f, int n, int nnz, const int *ii, const int *jj,
-                      const double *vv) {
-  int i, k;
-  memset(f, 0, sizeof *f);
-  f->n = n;
-  /* symmetric adjacency (CSR, deduplicated) for RCM */
-  int *deg = (int *)xcalloc((size_t)n + 1, sizeof(int));
-  for (k = 0; k < nnz; k++)
-    if (ii[k] != jj[k]) { deg[ii[k]]++; deg[jj[k]]++; }
-  int *adjp = (int *)xcalloc((size_t)n + 1, sizeof(int));
-  for (i = 0; i < n; i++) adjp[i + 1] = adjp[i] + deg[i];
-  int *adj = (int *)xcalloc((size_t)adjp[n] + 1, sizeof(int));
-  int *fill = (int *)xcalloc((size_t)n + 1, sizeof(int));
-  for (k = 0; k < nnz; k++)
-    if (ii[k] != jj[k]) {
-      adj[adjp[ii[k]] + fill[ii[k]]++] = jj[k];
-      adj[adjp[jj[k]] + fill[jj[k]]++] = ii[k];
-    }
-  /* dedupe each list */
-  int *mark = (int *)xcalloc((size_t)n + 1, sizeof(int));
-  for (i = 0; i < n; i++) mark[i] = -1;
-  int *udeg = (int *)xcalloc((size_t)n + 1, sizeof(int));
-  for (i = 0; i < n; i++) {
-    int w = adjp[i];
-    for (k = adjp[i]; k < adjp[i] + fill[i]; k++)
-      if (mark[adj[k]] != i) { mark[adj[k]] = i; adj[w++] = adj[k]; }
-    udeg[i] = w - adjp[i];
-  }
-  /* RCM: BFS from a minimum-degree unvisited node, neighbours by degree */
-  int *order = (int *)xcalloc((size_t)n + 1, sizeof(int));
-  char *vis = (char *)xcalloc((size_t)n + 1, 1);
-  int head = 0, tail = 0;
-  int *tmp = (int *)xcalloc((size_t)n + 1, sizeof(int));
-  while (tail < n) {
-    int s = -1, bestd = INT_MAX;
-    for (i = 0; i < n; i++)
-      if (!vis[i] && udeg[i] < bestd) { bestd = udeg[i]; s = i; }
-    /* one pseudo-peripheral refinement: farthest node of a BFS */
-    {
-      int h = tail, t = tail, last = s;
-      order[t++] = s; vis[s] = 1;
-      while (h < t) {
-        int v = order[h++]; last = v;
-        for (k = adjp[v]; k < adjp[v] + udeg[v]; k++)
-          if (!vis[adj[k]]) { vis[adj[k]] = 1; order[t++] = adj[k]; }
-      }
-      for (k = tail; k < t; k++) vis[order[k]] = 0;
-      s = last;
-    }
-    order[tail++] = s; vis[s] = 1; head = tail - 1;
-    while (head < tail) {
-      int v = order[head++], nt = 0;
-      for (k = adjp[v]; k < adjp[v] + udeg[v]; k++)
-        if (!vis[adj[k]]) { vis[adj[k]] = 1; tmp[nt++] = adj[k]; }
-      /* insertion sort by degree (stable) */
-      int a, b;
-      for (a = 1; a < nt; a++) {
-        int x = tmp[a];
-        for (b = a - 1; b >= 0 && udeg[tmp[b]] > udeg[x]; b--) tmp[b + 1] = tmp[b];
-        tmp[b + 1] = x;
-      }
-      for (a = 0; a < nt; a++) order[tail++] = tmp[a];
-    }
-  }
-  f->perm = (int *)xcalloc((size_t)n + 1, sizeof(int));
-  f->iperm = (int *)xcalloc((size_t)n + 1, sizeof(int));
-  for (i = 0; i < n; i++) f->perm[i] = order[n - 1 - i];
-  for (i = 0; i < n; i++) f->iperm[f->perm[i]] = i;
-  /* envelope */
-  f->first = (int *)xcalloc((size_t)n + 1, sizeof(int));
-  for (i = 0; i < n; i++) f->first[i] = i;
-  for (k = 0; k < nnz; k++) {
-    int r = f->iperm[ii[k]], c = f->iperm[jj[k]];
-    if (c > r) { int t2 = r; r = c; c = t2; }
-    if (c < f->first[r]) f->first[r] = c;
-  }
-  f->rowptr = (long *)xcalloc((size_t)n + 1, sizeof(long));
-  for (i = 0; i < n; i++) f->rowptr[i + 1] = f->rowptr[i] + (i - f->first[i] + 1);
-  f->env = (double *)xcalloc((size_t)f->rowptr[n] + 1, sizeof(double));
-  for (k = 0; k < nnz; k++) {
-    int r = f->iperm[ii[k]], c = f->iperm[jj[k]];
-    if (c > r) continue; /* lower triangle only (matrix is symmetric) */
-    f->env[f->rowptr[r] + (c - f->first[r])] += vv[k];
-  }
-  /* row-oriented Cholesky on the envelope */
-  for (i = 0; i < n; i++) {
-    double *Li = f->env + f->rowptr[i];
-    int fi = f->first[i], j;
-    for (j = fi; j < i; j++) {
-      double *Lj = f->env + f->rowptr[j];
-      int fj = f->first[j];
-      int k0 = fi > fj ? fi : fj;
-      double s = Li[j - fi];
-      for (k = k0; k < j; k++) s -= Li[k - fi] * Lj[k - fj];
-      Li[j - fi] = s / Lj[j - fj];
-    }
-    double s = Li[i - fi];
-    for (k = fi; k < i; k++) s -= Li[k - fi] * Li[k - fi];
-    if (!(s > 0.0)) orc_abort("matrix not positive definite (pivot %d: %g)", i, s);
-    Li[i - fi] = sqrt(s);
-  }
-  free(deg); free(adjp); free(adj); free(fill); free(mark); free(udeg);
-  free(order); free(vis); free(tmp);
-}
-
-/* x = A^-1 b (0-based vectors in the original numbering) */
-static void pc_solve(const profchol *f, const double *b, double *x, double *w) {
-  int n = f->n, i, k;
-  for (i = 0; i < n; i++) w[i] = b[f->perm[i]];
-  for (i = 0; i < n; i++) {
-    const double *Li = f->env + f->rowptr[i];
-    int fi = f->first[i];
-    double s = w[i];
-    for (k = fi; k < i; k++) s -= Li[k - fi] * w[k];
-    w[i] = s / Li[i - fi];
-  }
-  for (i = n - 1; i >= 0; i--) {
-    const double *Li = f->env + f->rowptr[i];
-    int fi = f->first[i];
-    w[i] = w[i] / Li[i - fi];
-    double wi = w[i];
-    for (k = fi; k < i; k++) w[k] -= Li[k - fi] * wi;
-  }
-  for (i = 0; i < n; i++) x[f->perm[i]] = w[i];
-}
-
-/* factor once, solve many (used by the CPU timing of the benchmark) */
 void *orc_spd_factor(int n, int nnz, const int *ii, const int *jj, const double *vv) {
-  if (setjmp(g_jmp)) return NULL;
-  profchol *f = (profchol *)xcalloc(1, sizeof(profchol));
-  pc_factor(f, n, nnz, ii, jj, vv);
-  return f;
+  char err[256];
+  return spchol_factor(n, nnz, ii, jj, vv, err, sizeof err);
 }
 
 int orc_spd_solve_factored(void *fact, const double *b, double *x) {
-  profchol *f = (profchol *)fact;
+  spchol *f = (spchol *)fact;
   if (!f) return -1;
-  double *w = (double *)malloc(sizeof(double) * (size_t)(f->n + 1));
+  double *w = (double *)malloc(sizeof(double) * (size_t)spchol_work_size(f));
   if (!w) return -1;
-  pc_solve(f, b, x, w);
+  spchol_solve(f, b, x, w);
   free(w);
   return 0;
 }
 
-void orc_spd_free(void *fact) {
-  profchol *f = (profchol *)fact;
-  if (f) { pc_free(f); free(f); }
-}
+void orc_spd_free(void *fact) { spchol_free((spchol *)fact); }
 
 int orc_spd_solve(int n, int nnz, const int *ii, const int *jj, const double *vv,
                   const double *b, double *x) {
-  if (setjmp(g_jmp)) return -1;
-  profchol f;
-  pc_factor(&f, n, nnz, ii, jj, vv);
-  double *w = (double *)xcalloc((size_t)n + 1, sizeof(double));
-  pc_solve(&f, b, x, w);
-  free(w);
-  pc_free(&f);
-  return 0;
+  void *f = orc_spd_factor(n, nnz, ii, jj, vv);
+  if (!f) return -1;
+  int rc = orc_spd_solve_factored(f, b, x);
+  orc_spd_free(f);
+  return rc;
 }
 
 /* ------------------------------------------------------------------ */
@@ -2680,6 +2544,137 @@ static double dotp(const double *a, const double *b, int n) {
   return s;
 }
 
+/* Host threads of the oracle's factorisations, subdomain solves and vector
+ * loops (orc_set_threads).  Every parallel loop is over independent
+ * subdomains, rows or entries, and the subdomain results are summed in
+ * subdomain order afterwards, so the results do not depend on the count. */
+static int g_threads = 1;
+
+void orc_set_threads(int t) { g_threads = t > 0 ? t : 1; }
+
+typedef struct {
+  spchol **sd;     /* per subdomain (fine_method 1) */
+  spchol *coarse;  /* levels > 1 */
+  int nsd;
+  long work;       /* doubles of work a subdomain solve needs */
+} factors;
+
+static void factors_free(factors *F) {
+  if (F->sd) {
+    int sd;
+    for (sd = 0; sd < F->nsd; sd++) spchol_free(F->sd[sd]);
+    free(F->sd);
+  }
+  spchol_free(F->coarse);
+  memset(F, 0, sizeof *F);
+}
+
+/* Factorise_subdomains (subsolvers.F90:78-163): the principal submatrix
+ * A(inds, inds) of every subdomain, and the coarse matrix, which the
+ * reference factorises lazily on the first coarse solve (pcg.F90:166-178).
+ * Task 0 is the coarse matrix, tasks 1..nsd the subdomains. */
+static void factor_all(state *s, factors *F) {
+  ctl_t *c = &s->ctl;
+  int n = s->n;
+  const spm *ACp = s->have_sub ? &s->ACs : &s->AC;
+  F->nsd = c->fine_method == 1 ? s->nsubd : 0;
+  F->sd = (spchol **)xcalloc((size_t)F->nsd + 1, sizeof(spchol *));
+  int have_coarse = c->levels > 1;
+  int ntask = F->nsd + 1, failed = 0, t;
+  char msg[256];
+  msg[0] = 0;
+#pragma omp parallel num_threads(g_threads) if (g_threads > 1)
+  {
+    int *floc = (int *)calloc((size_t)n + 2, sizeof(int));
+    if (!floc) {
+#pragma omp atomic write
+      failed = 1;
+    }
+#pragma omp for schedule(dynamic, 1)
+    for (t = 0; t < ntask; t++) {
+      char err[256];
+      err[0] = 0;
+      if (!floc || failed) continue;
+      if (t == 0) {
+        if (!have_coarse) continue;
+        long nz = ACp->nnz, k;
+        int *ci = (int *)malloc(sizeof(int) * ((size_t)nz + 1));
+        int *cj = (int *)malloc(sizeof(int) * ((size_t)nz + 1));
+        spchol *f = NULL;
+        if (ci && cj) {
+          for (k = 0; k < nz; k++) { ci[k] = ACp->indi[k + 1] - 1; cj[k] = ACp->indj[k + 1] - 1; }
+          f = spchol_factor(ACp->nrows, nz, ci, cj, ACp->val + 1, err, sizeof err);
+        } else {
+          snprintf(err, sizeof err, "out of memory");
+        }
+        free(ci); free(cj);
+        if (!f) {
+#pragma omp critical(orc_fail)
+          { failed = 1; snprintf(msg, sizeof msg, "coarse factorisation: %s", err); }
+        }
+        F->coarse = f;
+        continue;
+      }
+      int sd = t - 1;
+      int b0 = s->sd_start[sd], m = s->sd_start[sd + 1] - b0, k;
+      const int *nodes = s->sd_nodes + b0;
+      long cnt = 0, q;
+      for (k = 0; k < m; k++) floc[nodes[k]] = k + 1;
+      for (k = 0; k < m; k++) {
+        int i = nodes[k];
+        for (q = s->A.mbound[i]; q <= s->A.mbound[i + 1] - 1; q++)
+          if (floc[s->A.indj[q]] > 0) cnt++;
+      }
+      int *si = (int *)malloc(sizeof(int) * ((size_t)cnt + 1));
+      int *sj = (int *)malloc(sizeof(int) * ((size_t)cnt + 1));
+      double *sv = (double *)malloc(sizeof(double) * ((size_t)cnt + 1));
+      spchol *f = NULL;
+      if (si && sj && sv) {
+        cnt = 0;
+        for (k = 0; k < m; k++) {
+          int i = nodes[k];
+          for (q = s->A.mbound[i]; q <= s->A.mbound[i + 1] - 1; q++) {
+            int l = floc[s->A.indj[q]];
+            if (l > 0) { si[cnt] = k; sj[cnt] = l - 1; sv[cnt] = s->A.val[q]; cnt++; }
+          }
+        }
+        f = spchol_factor(m, cnt, si, sj, sv, err, sizeof err);
+      } else {
+        snprintf(err, sizeof err, "out of memory");
+      }
+      free(si); free(sj); free(sv);
+      for (k = 0; k < m; k++) floc[nodes[k]] = 0;
+      if (!f) {
+#pragma omp critical(orc_fail)
+        { failed = 1; snprintf(msg, sizeof msg, "subdomain %d: %s", sd + 1, err); }
+      }
+      F->sd[sd] = f;
+    }
+    free(floc);
+  }
+  if (failed) {
+    factors_free(F);
+    orc_abort("%s", msg[0] ? msg : "out of memory");
+  }
+  F->work = 1;
+  for (t = 0; t < F->nsd; t++) {
+    long w = spchol_work_size(F->sd[t]);
+    if (w > F->work) F->work = w;
+  }
+}
+
+/* y = A x over row blocks (the same per-row sums as spmv_rows) */
+static void spmv_rows_par(const spm *A, const double *x, double *y) {
+  int i;
+#pragma omp parallel for num_threads(g_threads) if (g_threads > 1) schedule(static)
+  for (i = 1; i <= A->nrows; i++) {
+    double s = 0.0;
+    int j;
+    for (j = A->mbound[i]; j <= A->mbound[i + 1] - 1; j++) s = s + A->val[j] * x[A->indj[j]];
+    y[i] = s;
+  }
+}
+
 /* pcg_weigs (pcg.F90:289-462) with preconditioner (pcg.F90:216-270). */
 static void run_pcg(state *s, orc_result *res) {
   ctl_t *c = &s->ctl;
@@ -2694,60 +2689,27 @@ static void run_pcg(state *s, orc_result *res) {
   unsigned char *sgs_in = (unsigned char *)xcalloc((size_t)n + 1, 1);
   double *sgs_diag = NEWD(n), *sgs_x = NEWD(n);
   double t0 = now_s();
-  /* Factorise_subdomains (subsolvers.F90:78-163) */
-  profchol *fact = NULL;
-  int maxsd = 1;
-  if (c->fine_method == 1) {
-    fact = (profchol *)xcalloc((size_t)s->nsubd + 1, sizeof(profchol));
-    int *floc = NEWI(n);
-    for (sd = 0; sd < s->nsubd; sd++) {
-      int b0 = s->sd_start[sd], m = s->sd_start[sd + 1] - b0, k;
-      if (m > maxsd) maxsd = m;
-      for (k = 0; k < m; k++) floc[s->sd_nodes[b0 + k]] = k + 1;
-      int cnt = 0;
-      for (k = 1; k <= s->A.nnz; k++)
-        if (floc[s->A.indi[k]] > 0 && floc[s->A.indj[k]] > 0) cnt++;
-      int *si = (int *)xcalloc((size_t)cnt + 1, sizeof(int));
-      int *sj = (int *)xcalloc((size_t)cnt + 1, sizeof(int));
-      double *sv = (double *)xcalloc((size_t)cnt + 1, sizeof(double));
-      cnt = 0;
-      for (k = 1; k <= s->A.nnz; k++)
-        if (floc[s->A.indi[k]] > 0 && floc[s->A.indj[k]] > 0) {
-          si[cnt] = floc[s->A.indi[k]] - 1;
-          sj[cnt] = floc[s->A.indj[k]] - 1;
-          sv[cnt] = s->A.val[k];
-          cnt++;
-        }
-      pc_factor(&fact[sd], m, cnt, si, sj, sv);
-      free(si); free(sj); free(sv);
-      for (k = 0; k < m; k++) floc[s->sd_nodes[b0 + k]] = 0;
-    }
-    free(floc);
-  }
-  profchol cfact;
-  memset(&cfact, 0, sizeof cfact);
+  factors F;
+  memset(&F, 0, sizeof F);
+  factor_all(s, &F);
   const spm *ACp = s->have_sub ? &s->ACs : &s->AC, *Rp = s->have_sub ? &s->Rs : &s->R;
   int nc = ACp->nrows;
-  if (levels > 1) {
-    int *ci = (int *)xcalloc((size_t)ACp->nnz + 1, sizeof(int));
-    int *cj = (int *)xcalloc((size_t)ACp->nnz + 1, sizeof(int));
-    int k;
-    for (k = 0; k < ACp->nnz; k++) { ci[k] = ACp->indi[k + 1] - 1; cj[k] = ACp->indj[k + 1] - 1; }
-    pc_factor(&cfact, nc, ACp->nnz, ci, cj, ACp->val + 1);
-    free(ci); free(cj);
-  }
   double t1 = now_s();
   res->t_factor = t1 - t0;
 
+  int nthr = g_threads > 1 ? g_threads : 1;
   double *x = NEWD(n), *r = NEWD(n), *p = NEWD(n), *q = NEWD(n), *z = NEWD(n);
-  double *subrhs = NEWD(maxsd), *subsol = NEWD(maxsd), *work = NEWD(maxsd);
-  double *crhs = NEWD(nc), *csol = NEWD(nc), *cw = NEWD(nc), *tmpsol = NEWD(n);
+  long sdtot = s->sd_start[s->nsubd];
+  double *subsol = NEWD(sdtot);
+  double *works = (double *)xcalloc((size_t)F.work * nthr + 1, sizeof(double));
+  double *crhs = NEWD(nc), *csol = NEWD(nc), *tmpsol = NEWD(n);
+  double *cw = levels > 1 ? NEWD(spchol_work_size(F.coarse)) : NEWD(1);
   double tol = c->solve_tolerance;
   int maxit = c->solve_maxiters;
   if (maxit == -1) maxit = 100000;
   double *alpha = NEWD(maxit + 1), *beta = NEWD(maxit + 1);
   res->res_hist = (double *)xcalloc((size_t)maxit + 1, sizeof(double));
-  spmv_rows(&s->A, x, r);
+  spmv_rows_par(&s->A, x, r);
   for (i = 1; i <= n; i++) r[i] = s->rhs[i - 1] - r[i];
   double init_norm = dotp(r, r, n);
   if (init_norm == 0.0) init_norm = 1.0;
@@ -2795,33 +2757,56 @@ static void run_pcg(state *s, orc_result *res) {
           for (k = 0; k < m; k++) z[s->sd_nodes[b0 + k]] = z[s->sd_nodes[b0 + k]] + sgs_x[s->sd_nodes[b0 + k]];
           for (k = 0; k < m; k++) sgs_in[s->sd_nodes[b0 + k]] = 0;
         }
-      } else { /* Solve_subdomains (subsolvers.F90:54-76) */
-        for (sd = 0; sd < s->nsubd; sd++) {
-          int b0 = s->sd_start[sd], m = s->sd_start[sd + 1] - b0, k;
-          for (k = 0; k < m; k++) subrhs[k] = r[s->sd_nodes[b0 + k]];
-          pc_solve(&fact[sd], subrhs, subsol, work);
-          for (k = 0; k < m; k++) z[s->sd_nodes[b0 + k]] = z[s->sd_nodes[b0 + k]] + subsol[k];
+      }
+      /* Solve_subdomains (subsolvers.F90:54-76) beside prec2Level's coarse
+       * solve (pcg.F90:144-209): task 0 restricts, solves the coarse system
+       * and prolongs; task sd+1 solves subdomain sd into its own slice */
+      int nsolve = c->fine_method == 1 ? s->nsubd : 0, t;
+#pragma omp parallel for num_threads(g_threads) if (g_threads > 1) schedule(dynamic, 1)
+      for (t = 0; t < nsolve + 1; t++) {
+        if (t == 0) {
+          if (levels > 1) {
+            spmv_R(Rp, r, crhs, 0, nc);
+            spchol_solve(F.coarse, crhs + 1, csol + 1, cw);
+            spmv_R(Rp, csol, tmpsol, 1, n);
+          }
+          continue;
         }
+        int sdi = t - 1, b0 = s->sd_start[sdi], m = s->sd_start[sdi + 1] - b0, k;
+#ifdef _OPENMP
+        double *w = works + (size_t)F.work * (size_t)omp_get_thread_num();
+#else
+        double *w = works;
+#endif
+        double *v = subsol + 1 + b0;
+        for (k = 0; k < m; k++) v[k] = r[s->sd_nodes[b0 + k]];
+        spchol_solve(F.sd[sdi], v, v, w);
       }
-      if (levels > 1) { /* prec2Level (pcg.F90:144-209), method 1 */
-        spmv_R(Rp, r, crhs, 0, nc);
-        pc_solve(&cfact, crhs + 1, csol + 1, cw);
-        spmv_R(Rp, csol, tmpsol, 1, n);
-        if (method == 1 || method == 5) /* pcg.F90:191-193, 205-208 */
-          for (i = 1; i <= n; i++) z[i] = z[i] + tmpsol[i];
+      for (sd = 0; sd < nsolve; sd++) {
+        int b0 = s->sd_start[sd], m = s->sd_start[sd + 1] - b0, k;
+        const double *v = subsol + 1 + b0;
+        for (k = 0; k < m; k++) z[s->sd_nodes[b0 + k]] = z[s->sd_nodes[b0 + k]] + v[k];
       }
+      if (levels > 1 && (method == 1 || method == 5)) /* pcg.F90:191-193, 205-208 */
+        for (i = 1; i <= n; i++) z[i] = z[i] + tmpsol[i];
     }
     double rho_curr = dotp(r, z, n);
     if (it == 1) {
       for (i = 1; i <= n; i++) p[i] = z[i];
     } else {
-      beta[it] = rho_curr / rho_prev;
-      for (i = 1; i <= n; i++) p[i] = z[i] + beta[it] * p[i];
+      double bt = rho_curr / rho_prev;
+      beta[it] = bt;
+#pragma omp parallel for num_threads(g_threads) if (g_threads > 1) schedule(static)
+      for (i = 1; i <= n; i++) p[i] = z[i] + bt * p[i];
     }
-    spmv_rows(&s->A, p, q);
-    alpha[it] = rho_curr / dotp(p, q, n);
-    for (i = 1; i <= n; i++) x[i] = x[i] + alpha[it] * p[i];
-    for (i = 1; i <= n; i++) r[i] = r[i] - alpha[it] * q[i];
+    spmv_rows_par(&s->A, p, q);
+    double al = rho_curr / dotp(p, q, n);
+    alpha[it] = al;
+#pragma omp parallel for num_threads(g_threads) if (g_threads > 1) schedule(static)
+    for (i = 1; i <= n; i++) {
+      x[i] = x[i] + al * p[i];
+      r[i] = r[i] - al * q[i];
+    }
     rho_prev = rho_curr;
     double res_norm = dotp(r, r, n);
     ratio_norm = res_norm / init_norm;
@@ -2832,12 +2817,8 @@ static void run_pcg(state *s, orc_result *res) {
   res->cond_num = calc_cond(it, alpha, beta);
   res->x = (double *)xcalloc((size_t)n, sizeof(double));
   memcpy(res->x, x + 1, sizeof(double) * (size_t)n);
-  if (fact) {
-    for (sd = 0; sd < s->nsubd; sd++) pc_free(&fact[sd]);
-    free(fact);
-  }
-  pc_free(&cfact);
-  free(x); free(r); free(p); free(q); free(z); free(subrhs); free(subsol); free(work);
+  factors_free(&F);
+  free(x); free(r); free(p); free(q); free(z); free(subsol); free(works);
   free(crhs); free(csol); free(cw); free(tmpsol); free(alpha); free(beta);
   free(sgs_in); free(sgs_diag); free(sgs_x);
 }
@@ -2952,6 +2933,63 @@ int orc_setup_coo(int n, int nnz, const int *ii, const int *jj, const double *vv
                   const char *ctl_text, const int *part, int nparts,
                   orc_result **out) {
   return run_common(n, nnz, ii, jj, vv, NULL, ctl_text, part, nparts, 0, NULL, out);
+}
+
+/* A setup kept for repeated factorisations + solves (the benchmark's CPU
+ * timing: the setup once, then per step what the GPU step does). */
+struct orc_session {
+  state s;
+};
+
+int orc_session_new(int n, int nnz, const int *ii, const int *jj, const double *vv,
+                    const char *ctl_text, const int *part, int nparts, orc_session **sess,
+                    orc_result **out) {
+  orc_result *r = (orc_result *)calloc(1, sizeof(orc_result));
+  orc_session *S = (orc_session *)calloc(1, sizeof(orc_session));
+  *out = r;
+  *sess = NULL;
+  state *s = &S->s;
+  if (setjmp(g_jmp)) {
+    r->status = -1;
+    snprintf(r->errmsg, sizeof r->errmsg, "%s", g_err);
+    state_free(s); free(S);
+    return -1;
+  }
+  ctl_defaults(&s->ctl);
+  ctl_parse_text(&s->ctl, ctl_text ? ctl_text : "");
+  ctl_finish(&s->ctl);
+  load_coo(s, n, nnz, ii, jj, vv);
+  s->rhs = (double *)xcalloc((size_t)s->n + 1, sizeof(double));
+  double t0 = now_s();
+  run_setup(s, part, nparts);
+  r->t_setup = now_s() - t0;
+  export_setup(s, r);
+  *sess = S;
+  return 0;
+}
+
+int orc_session_solve(orc_session *S, const double *rhs, orc_result **out) {
+  orc_result *r = (orc_result *)calloc(1, sizeof(orc_result));
+  *out = r;
+  state *s = &S->s;
+  if (setjmp(g_jmp)) {
+    r->status = -1;
+    snprintf(r->errmsg, sizeof r->errmsg, "%s", g_err);
+    return -1;
+  }
+  int i;
+  for (i = 0; i < s->n; i++) s->rhs[i] = rhs ? rhs[i] : 1.0;
+  r->n = s->n;
+  r->b = (double *)xcalloc((size_t)s->n + 1, sizeof(double));
+  memcpy(r->b, s->rhs, sizeof(double) * (size_t)s->n);
+  run_pcg(s, r);
+  return 0;
+}
+
+void orc_session_free(orc_session *S) {
+  if (!S) return;
+  state_free(&S->s);
+  free(S);
 }
 
 void orc_free(orc_result *r) {

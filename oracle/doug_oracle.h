@@ -10,8 +10,8 @@
  * input, strength of connection, aggregation, smoothed-aggregation
  * restriction, Galerkin coarse matrix, overlapping subdomains and PCG with the
  * two-level additive Schwarz preconditioner.  Exact subdomain / coarse solves
- * (UMFPACK LU in the reference) are done here by a profile Cholesky after
- * reverse Cuthill-McKee ordering.
+ * (UMFPACK LU in the reference) are done here by a nested-dissection
+ * multifrontal Cholesky (spchol.h).
  *
  * Parity pin: the reference's fixtures tests/assembled/lap4x4 and
  * tests/assembled/lap16x16 (final solutions; see tests/test_oracle.py).
@@ -103,7 +103,23 @@ int orc_read_assembled(const char *path, int format, int *n, int *nnz,
 int orc_read_vector(const char *path, int format, int n, double *x);
 int orc_write_solution(const char *path, int format, int n, const double *x);
 
-/* Exact solve of a sparse SPD system (profile Cholesky after RCM). */
+/* A setup kept for repeated solves: orc_session_new runs the setup (its
+ * result carries the setup arrays and t_setup); each orc_session_solve runs
+ * the numeric factorisations and the PCG on rhs (NULL -> b = 1), filling
+ * x, iterations, res_hist, t_factor and t_solve. */
+typedef struct orc_session orc_session;
+int orc_session_new(int n, int nnz, const int *ii, const int *jj, const double *vv,
+                    const char *ctl_text, const int *part, int nparts, orc_session **sess,
+                    orc_result **out);
+int orc_session_solve(orc_session *sess, const double *rhs, orc_result **out);
+void orc_session_free(orc_session *sess);
+
+/* Host threads for the factorisations, subdomain solves and vector loops
+ * (default 1).  The results do not depend on the count. */
+void orc_set_threads(int threads);
+
+/* Exact solve of a sparse SPD system (nested dissection + multifrontal
+ * Cholesky, spchol.h). */
 int orc_spd_solve(int n, int nnz, const int *ii, const int *jj, const double *vv,
                   const double *b, double *x);
 

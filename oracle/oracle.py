@@ -47,8 +47,9 @@ class _Result(C.Structure):
 
 def build(force: bool = False) -> str:
     """Compile the oracle with its Makefile (gcc)."""
-    src = os.path.join(_HERE, "doug_oracle.c")
-    if force or not os.path.exists(_SO) or os.path.getmtime(_SO) < os.path.getmtime(src):
+    srcs = [os.path.join(_HERE, f) for f in ("doug_oracle.c", "doug_oracle.h", "spchol.c", "spchol.h",
+                                               "Makefile")]
+    if force or not os.path.exists(_SO) or os.path.getmtime(_SO) < max(os.path.getmtime(f) for f in srcs):
         subprocess.run(["make", "-s", "-C", _HERE], check=True)
     return _SO
 
@@ -82,6 +83,12 @@ def lib():
             L.orc_spd_factor.restype = C.c_void_p
             L.orc_spd_solve_factored.argtypes = [C.c_void_p, P(C.c_double), P(C.c_double)]
             L.orc_spd_free.argtypes = [C.c_void_p]
+            L.orc_session_new.argtypes = [C.c_int, C.c_int, P(C.c_int), P(C.c_int), P(C.c_double),
+                                          C.c_char_p, P(C.c_int), C.c_int, P(C.c_void_p),
+                                          P(P(_Result))]
+            L.orc_session_solve.argtypes = [C.c_void_p, P(C.c_double), P(P(_Result))]
+            L.orc_session_free.argtypes = [C.c_void_p]
+            L.orc_set_threads.argtypes = [C.c_int]
             for nm in ("orc_parse_i10", "orc_parse_l1"):
                 getattr(L, nm).argtypes = [C.c_char_p, P(C.c_int)]
             L.orc_parse_f10_5.argtypes = [C.c_char_p, P(C.c_double)]
@@ -267,7 +274,7 @@ def parse_value(kind, text):
 
 
 class SpdFactor:
-    """Exact SPD factorisation of the oracle (profile Cholesky after RCM)."""
+    """Exact SPD factorisation of the oracle (nested dissection + multifrontal Cholesky)."""
 
     def __init__(self, n, rows0, cols0, vals):
         L = lib()
@@ -291,5 +298,61 @@ class SpdFactor:
             if self._f:
                 self._L.orc_spd_free(self._f)
                 self._f = None
+        except Exception:
+            pass
+
+
+def set_threads(n):
+    """Host threads of the oracle's factorisations, subdomain solves and
+    vector loops (results do not depend on the count)."""
+    lib().orc_set_threads(int(n))
+
+
+class Session:
+    """The oracle's setup kept for repeated solves: ``setup`` holds the setup
+    result (aggregates, subdomains, R, AC, t_setup); ``solve(b)`` runs the
+    numeric factorisations and the PCG and returns the solve result."""
+
+    def __init__(self, n, rows1, cols1, vals, ctl="", part=None):
+        L = lib()
+        self._L = L
+        ii = np.ascontiguousarray(rows1, dtype=np.int32)
+        jj = np.ascontiguousarray(cols1, dtype=np.int32)
+        vv = np.ascontiguousarray(vals, dtype=np.float64)
+        pp, npart = None, 0
+        if part is not None:
+            pp = np.ascontiguousarray(part, dtype=np.int32)
+            npart = int(pp.max())
+        res = C.POINTER(_Result)()
+        self._s = C.c_void_p()
+        L.orc_session_new(n, len(vv), _ip(ii), _ip(jj), _dp(vv), ctl.encode(),
+                          _ip(pp) if pp is not None else None, npart, C.byref(self._s), C.byref(res))
+        self.setup = _convert(res)
+        L.orc_free(res)
+        if self.setup["status"] != 0:
+            raise RuntimeError("oracle setup failed: " + self.setup["errmsg"])
+        self.n = n
+
+    def solve(self, b=None):
+        res = C.POINTER(_Result)()
+        bb = None if b is None else np.ascontiguousarray(b, dtype=np.float64)
+        self._L.orc_session_solve(self._s, _dp(bb) if bb is not None else None, C.byref(res))
+        r = res.contents
+        out = {"status": r.status, "errmsg": r.errmsg.decode(errors="replace")}
+        if r.status == 0:
+            out.update(x=_arr(r.x, self.n, np.float64), iterations=r.iterations, cond_num=r.cond_num,
+                       init_norm=r.init_norm, res_hist=_arr(r.res_hist, r.iterations, np.float64),
+                       t_factor=r.t_factor, t_solve=r.t_solve)
+        self._L.orc_free(res)
+        return out
+
+    def close(self):
+        if self._s:
+            self._L.orc_session_free(self._s)
+            self._s = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
         except Exception:
             pass

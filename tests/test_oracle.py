@@ -118,3 +118,55 @@ def test_oracle_method5_is_additive_and_2_3_are_rejected():
     for m in (2, 3):
         r = O.run_ctl(path, f"method {m}\n" + base)
         assert r["status"] != 0 and "residual" in r["errmsg"]
+
+
+def test_sparse_cholesky_is_an_exact_solve():
+    # the oracle's exact subdomain / coarse solver (nested dissection +
+    # multifrontal Cholesky, standing in for UMFPACK) against a dense solve
+    from doug_gb300 import problems as P
+    for N, seed in ((9, 1), (14, 2)):
+        n, r, c, v, b = P.diffusion3d_fv(N, seed=seed)
+        A = np.zeros((n, n))
+        np.add.at(A, (r - 1, c - 1), v)
+        x = O.spd_solve(n, r - 1, c - 1, v, b)
+        xd = np.linalg.solve(A, b)
+        assert np.linalg.norm(x - xd) <= 1e-12 * np.linalg.norm(xd)
+    # a non-SPD matrix is refused
+    with pytest.raises(RuntimeError):
+        O.spd_solve(2, np.array([0, 1, 0, 1]), np.array([0, 1, 1, 0]), np.array([1.0, 1.0, 2.0, 2.0]),
+                    np.ones(2))
+
+
+def test_oracle_threads_do_not_change_results():
+    # subdomain factorisations and solves in parallel, summed in subdomain
+    # order afterwards: bit-identical solutions for any thread count
+    from doug_gb300 import problems as P
+    n, r, c, v, b = P.diffusion3d_fv(12, seed=3)
+    part = P.block_partition(12, 2)
+    ctl = ("solver 2\nmethod 1\nfine_method 1\nlevels 2\noverlap 2\nsmoothers 1\nstrong1 0.08\n"
+           "radius1 2\nsolve_tolerance 1.0e-10\n")
+    out = []
+    for t in (1, 3):
+        O.set_threads(t)
+        try:
+            ro = O.run_coo(n, r, c, v, rhs=b, ctl=ctl, part=part)
+        finally:
+            O.set_threads(1)
+        assert ro["status"] == 0, ro["errmsg"]
+        out.append(ro)
+    assert out[0]["iterations"] == out[1]["iterations"]
+    assert np.array_equal(out[0]["x"], out[1]["x"])
+
+
+def test_session_repeats_the_one_shot_run():
+    from doug_gb300 import problems as P
+    n, r, c, v, b, _ = P.poisson2d_p1(33, seed=2)
+    ctl = "solver 2\nmethod 1\nfine_method 1\nlevels 2\noverlap 1\nsmoothers 1\nstrong1 0.08\nradius1 2\n"
+    ro = O.run_coo(n, r, c, v, rhs=b, ctl=ctl)
+    S = O.Session(n, r, c, v, ctl)
+    for _ in range(2):
+        rs = S.solve(b)
+        assert rs["status"] == 0
+        assert rs["iterations"] == ro["iterations"]
+        assert np.array_equal(rs["x"], ro["x"])
+    S.close()
