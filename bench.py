@@ -455,6 +455,34 @@ def run_small(args, steps, warmup):
     return out
 
 
+def _batched_vs_oracle(systems, x64, xmixed, gpu_iters, sample=8):
+    """The oracle's own solve of a seeded sample of the systems (the smallest,
+    the largest and six drawn at random), each against its slice of the GPU
+    batch: FP64 and mixed relative errors and FP64 iteration counts."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    ns = np.array([t[0] for t in systems])
+    rng = np.random.default_rng(1)
+    pick = sorted(set([int(ns.argmin()), int(ns.argmax())]
+                      + [int(i) for i in rng.choice(len(systems), sample, replace=False)]))[:sample]
+    O.set_threads(host_threads())
+    rows = []
+    try:
+        for i in pick:
+            n, r, c, v, b = systems[i]
+            ro = O.run_coo(n, r, c, v, rhs=b, ctl=_ctl_text(BATCH_CTL))
+            xo = ro["x"]
+            rows.append({"system": i, "n": int(n), "oracle_iterations": ro["iterations"],
+                         "fp64_iterations": int(gpu_iters[i]),
+                         "fp64_rel_err": float(np.linalg.norm(x64[i] - xo) / np.linalg.norm(xo)),
+                         "mixed_rel_err": float(np.linalg.norm(xmixed[i] - xo) / np.linalg.norm(xo))})
+    finally:
+        O.set_threads(1)
+    return {"systems": rows, "fp64_rel_err_max": max(r["fp64_rel_err"] for r in rows),
+            "mixed_rel_err_max": max(r["mixed_rel_err"] for r in rows),
+            "iterations_max_diff": max(abs(r["oracle_iterations"] - r["fp64_iterations"]) for r in rows)}
+
+
 def run_batched(args, steps, warmup):
     """The batched uneven-systems workload: every step solves all systems
     (factorisations + per-system PCG to 1e-8) from right-hand sides in HBM."""
@@ -536,6 +564,8 @@ def run_batched(args, steps, warmup):
             out["fp64"] = res
             err = [np.linalg.norm(a - c) / np.linalg.norm(c) for a, c in zip(s.split(x_mixed), s.split(x64))]
             out["mixed_rel_err_vs_fp64_solution_max"] = float(max(err))
+            if not args.no_cpu_baseline:
+                out["vs_oracle"] = _batched_vs_oracle(systems, s.split(x64), s.split(x_mixed), ss["iterations"])
         del s
         torch.cuda.empty_cache()
     out["mixed_vs_fp64"] = out["mixed"]["batch_s"] / out["fp64"]["batch_s"]

@@ -183,3 +183,34 @@ def test_elemental_matvec_gpu(precision, asym):
     assert abs(s0.iterations - s1.iterations) <= 1
     assert s1.true_rel_residual <= 1.01e-10
     assert np.linalg.norm(x1 - x0) <= (1e-10 if precision == 0 else 1e-7) * np.linalg.norm(x0)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision,emv", [(0, 1), (1, 1), (0, 0)])
+def test_elasticity_reduced_grid_vs_oracle(precision, emv):
+    # the elasticity workload's controls (box subdomains, overlap 1, strong1
+    # 0.08, radius1 2, maxasize1 100) on a 10^3-hex grid: the GPU solve with
+    # matrix-free element products (elemental_matvec 1) or assembled products
+    # against the oracle's FP64 PCG on the assembled input
+    from doug_gb300 import problems as P
+    N = 10
+    ngf, eptr, efree, emat, erhs, info = P.elasticity3d_p1_elements(N, seed=3)
+    part = P.dof_box_partition(info["node_ijk"], N, parts=(2, 2, 2))
+    opts = dict(solver=2, method=1, fine_method=1, levels=2, overlap=1, smoothers=1, strong1="0.08",
+                radius1=2, maxasize1=100, solve_tolerance="1.0e-8", solve_maxiters=5000)
+    s = D.DougSolver(opts)
+    s.set_option("precision", precision)
+    s.set_option("elemental_matvec", emv)
+    s.set_elements(ngf, eptr, efree, emat, erhs)
+    s.set_partition(part)
+    n, r, c, v, b = s.input_matrix()
+    s.setup()
+    x, st = s.solve(allow_not_converged=False)
+    ro = O.run_coo(n, r, c, v, rhs=b, ctl=_ctl_text(opts), part=part)
+    assert ro["status"] == 0, ro["errmsg"]
+    err = np.linalg.norm(x - ro["x"]) / np.linalg.norm(ro["x"])
+    if precision == 0:
+        assert abs(st.iterations - ro["iterations"]) <= 1, (st.iterations, ro["iterations"])
+        assert err <= 1e-10, err
+    else:
+        assert err <= 1e-7, err

@@ -175,3 +175,25 @@ def test_true_residual_entry_matches_numpy():
     ref = b - A @ x
     assert np.allclose(res.cpu().numpy(), ref, rtol=0, atol=1e-12 * np.abs(ref).max())
     assert abs(nrm.item() - ref @ ref) <= 1e-12 * (ref @ ref)
+
+
+@pytest.mark.parametrize("case", ["lap16x16", "cfg0"])
+def test_condition_estimate_matches_oracle_tql1(case):
+    # dg_stats.cond_num (bisection on the Lanczos tridiagonal of the FP64 CG
+    # coefficients) against the oracle's restatement of CalculateEigenvalues /
+    # tql1 (pcg.F90:465-641) on the same solve
+    if case == "lap16x16":
+        opts = dict(solver=2, method=1, fine_method=1, levels=2, smoothers=1, overlap=1)
+        s = D.DougSolver(opts)
+        s.load_ctl(os.path.join(GOLDEN, "lap16x16", "DOUG.ctl"))
+        s.setup()
+        x, st = s.solve()
+        ro = O.run_ctl(os.path.join(GOLDEN, "lap16x16", "DOUG.ctl"), _ctl_text(opts))
+    else:
+        n, r, c, v, b, _ = P.poisson2d_p1(129, seed=0)
+        x, st = _solve(n, r, c, v, b, CFG0)
+        ro = O.run_coo(n, r, c, v, rhs=b, ctl=_ctl_text(CFG0))
+    assert ro["status"] == 0
+    assert st.iterations == ro["iterations"]
+    assert ro["cond_num"] > 1.0
+    assert abs(st.cond_num - ro["cond_num"]) <= 1e-8 * ro["cond_num"], (st.cond_num, ro["cond_num"])
