@@ -578,7 +578,8 @@ ELAS_CTL = dict(solver=2, method=1, fine_method=1, levels=2, overlap=1, smoother
 ELAS_WORKLOAD = ("3-D linear elasticity, P1 tetrahedra: 64^3 hexes x 6 tets (1,572,864 elements, 12x12 element "
                  "matrices), nodes jittered +-0.15h, E = 1 with 20 seeded boxes of E = 1e3, nu = 0.3, bottom "
                  "face clamped, body force (0,0,-1): 811,200 freedoms; elemental input; 128 box subdomains "
-                 "(4x4x8), overlap 1, the reference's scalar smoothed-aggregation coarse grid")
+                 "(4x4x8), overlap 1, the reference's scalar smoothed-aggregation coarse grid (and, as *_rbm, "
+                 "smoothed aggregation over nodal blocks with the six rigid-body modes, coarse_method 3)")
 
 
 def run_elasticity(args, steps, warmup):
@@ -598,11 +599,15 @@ def run_elasticity(args, steps, warmup):
     out = {"config": {"workload": ELAS_WORKLOAD, "n": int(ngf), "elements": int(len(eptr) - 1),
                       "element_values": int(len(emat)), "controls": ELAS_CTL}}
     xs = {}
-    for name, prec, emv in (("mixed", 1, 0), ("fp64", 0, 0), ("mixed_matrix_free", 1, 1)):
-        s = D.DougSolver(ELAS_CTL)
+    runs = (("mixed", 1, 0, 1), ("fp64", 0, 0, 1), ("mixed_matrix_free", 1, 1, 1), ("mixed_rbm", 1, 0, 3),
+            ("fp64_rbm", 0, 0, 3))
+    for name, prec, emv, cm in runs:
+        s = D.DougSolver(dict(ELAS_CTL, coarse_method=cm))
         s.set_option("precision", prec)
         s.set_option("elemental_matvec", emv)
         s.set_elements(ngf, eptr, efree, emat, erhs)
+        if cm == 3:  # smoothed aggregation over nodal blocks with rigid-body modes
+            s.set_node_geometry(info["coords"], info["freemap"])
         s.set_partition(part)
         t0 = time.perf_counter()
         s.setup()
@@ -626,7 +631,7 @@ def run_elasticity(args, steps, warmup):
         s.set_option("profile", 0)
         xs[name] = xd.cpu().numpy()
         res = {"solve_s": t, "iterations": st.iterations, "true_rel_residual": st.true_rel_residual,
-               "setup_host_s": setup_s, "gpu_launches": st.gpu_launches,
+               "setup_host_s": setup_s, "gpu_launches": st.gpu_launches, "coarse_unknowns": st.ncoarse,
                "phases": {"factor_s": pr.t_factor_s, "iterate_s": pr.t_iterate_s, "subsolve_s": pr.t_subsolve_s,
                           "coarse_s": pr.t_coarse_s, "product_s": pr.t_spmv_s,
                           "product_ms_per_iteration": 1e3 * pr.t_spmv_s / max(pr.iterations, 1)}}
@@ -638,9 +643,10 @@ def run_elasticity(args, steps, warmup):
         del s
         torch.cuda.empty_cache()
     x64 = xs["fp64"]
-    for name in ("mixed", "mixed_matrix_free"):
+    for name in ("mixed", "mixed_matrix_free", "mixed_rbm", "fp64_rbm"):
         out[name]["rel_err_vs_fp64_solution"] = float(np.linalg.norm(xs[name] - x64) / np.linalg.norm(x64))
     out["mixed_vs_fp64"] = out["mixed"]["solve_s"] / out["fp64"]["solve_s"]
+    out["rbm_vs_scalar_coarse"] = out["mixed_rbm"]["solve_s"] / out["mixed"]["solve_s"]
     return out
 
 

@@ -1107,6 +1107,17 @@ dg_status do_setup(dg_handle *h, bool reuse_host = false) {
                             h->have_elements ? &h->el_free : nullptr, h->have_elements ? &h->el_lg : nullptr,
                             h->have_geometry ? &h->geo : nullptr, h->S, err))
         return fail(h, DG_BAD_INPUT, err);
+    } else if (c.coarse_method == 3 && h->nsys == 0) {
+      // smoothed aggregation over nodal blocks with rigid-body modes: the node
+      // of every unknown from the freedom map of the element mesh
+      if (!h->have_elements || !h->have_geometry)
+        return fail(h, DG_BAD_INPUT, "coarse_method 3 needs elemental input with node coordinates "
+                                     "(coords_file / freemap_file or dg_set_node_geometry)");
+      std::vector<int> unode((size_t)h->n);
+      for (int u = 0; u < h->n; u++) unode[(size_t)u] = h->geo.freemap[(size_t)h->el_lg[(size_t)u] - 1] - 1;
+      if (!build_setup_rbm(c, h->n, h->ii, h->jj, h->vv, h->part.empty() ? nullptr : &h->part, h->nparts, unode,
+                           h->geo.nsd, h->geo.coords, h->S, err))
+        return fail(h, DG_BAD_INPUT, err);
     } else if (h->nsys > 0) {
       if (!h->part.empty()) return fail(h, DG_BAD_INPUT, "a partition vector cannot be combined with batched systems");
       if (!build_setup_systems(c, h->sys_row, h->sys_tri, h->ii, h->jj, h->vv, h->S, err))

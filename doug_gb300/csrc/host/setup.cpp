@@ -1408,8 +1408,10 @@ bool build_setup(const Controls &c_in, int n, const std::vector<int> &ii, const 
           " restricts a residual the one-process reference never sets (pcg.F90:146-149)";
     return false;
   }
-  if (c.coarse_method > 2) {  // aggr.F90:155-165
-    err = "Wrong coarse method " + std::to_string(c.coarse_method);
+  if (c.coarse_method > 2) {  // aggr.F90:155-165 (3: build_setup_rbm, with node coordinates)
+    err = c.coarse_method == 3 ? std::string("coarse_method 3 needs node coordinates (elemental input with "
+                                             "coords_file / freemap_file or dg_set_node_geometry)")
+                               : "Wrong coarse method " + std::to_string(c.coarse_method);
     return false;
   }
   if (c.coarse_method == 2 && !robust) {
@@ -1552,6 +1554,279 @@ bool build_setup(const Controls &c_in, int n, const std::vector<int> &ii, const 
   }
   // the reference restarts each overlap layer one entry early; that entry's
   // neighbours are already marked, so the visited order is unchanged
+  grow_subdomains(A, lists, out.overlap, out);
+  tm.lap("subdomains + overlap");
+  out.A = A;
+  return true;
+}
+
+// ---------------------------------------------------------------------------
+// Smoothed aggregation over nodal blocks with a rigid-body near-nullspace
+// (coarse_method 3; no counterpart in the reference, whose aggregation is
+// scalar: SpMtx_aggregation.F90:49-641).  The method is the smoothed
+// aggregation of Vanek, Mandel and Brezina (Computing 56 (1996) 179-196) for
+// systems: aggregates of mesh nodes from the block strength ||A_IJ||_F >
+// theta sqrt(||A_II||_F ||A_JJ||_F); per aggregate the rigid-body modes
+// (nsd translations, 1 or 3 rotations about the aggregate's centroid)
+// orthonormalised by twice-repeated modified Gram-Schmidt (columns that
+// vanish are dropped) form the tentative prolongator; Jacobi smoothing
+// P = (I - omega D^-1 A) P_tent with omega = 4 / (3 rho(D^-1 A)), rho by 20
+// power steps; R = P^T and AC = R A P.  Every loop runs in a fixed order, so
+// the oracle's restatement gives the same bits.
+// ---------------------------------------------------------------------------
+bool build_setup_rbm(const Controls &c_in, int n, const std::vector<int> &ii, const std::vector<int> &jj,
+                     const std::vector<double> &vv, const std::vector<int> *part, int nparts,
+                     const std::vector<int> &unode, int nsd, const std::vector<double> &xyz, SetupResult &out,
+                     std::string &err) {
+  Controls c = c_in;
+  out = SetupResult();
+  out.n = n;
+  PhaseTimer tm;
+  if (c.method == 2 || c.method == 3) {
+    err = "method " + std::to_string(c.method) +
+          " restricts a residual the one-process reference never sets (pcg.F90:146-149)";
+    return false;
+  }
+  if (c.fine_method < 0 || c.fine_method > 2) {
+    err = "Wrong fine method " + std::to_string(c.fine_method);
+    return false;
+  }
+  if (!part) {
+    err = "coarse_method 3 builds no coarse aggregates for subdomains: give a partition (dg_set_partition)";
+    return false;
+  }
+  if (nsd != 2 && nsd != 3) { err = "coarse_method 3 needs 2-D or 3-D node coordinates"; return false; }
+  if ((int)unode.size() != n) { err = "coarse_method 3: the node of every unknown is needed"; return false; }
+  Coo A0;
+  if (!triplets(n, ii, jj, vv, A0, err)) return false;
+  const Csr A = rows_of(A0);
+  tm.lap("arrange by rows");
+  out.strong1 = (c.strong1 != 0.0) ? c.strong1 : 0.67;
+  const double theta = out.strong1;
+  // nodes in order of first appearance; a node's unknowns ascending are its
+  // components 1..nsd
+  std::vector<int> nid(xyz.size() / (size_t)nsd + 1, -1), node_of((size_t)n), comp((size_t)n);
+  std::vector<int> node_glob, ncomp;
+  for (int u = 0; u < n; u++) {
+    const int g = unode[(size_t)u];
+    if (g < 0 || (size_t)g >= nid.size() - 1) { err = "coarse_method 3: node of unknown out of range"; return false; }
+    if (nid[(size_t)g] < 0) { nid[(size_t)g] = (int)node_glob.size(); node_glob.push_back(g); ncomp.push_back(0); }
+    const int k = nid[(size_t)g];
+    node_of[(size_t)u] = k;
+    comp[(size_t)u] = ncomp[(size_t)k]++;
+  }
+  const int nn = (int)node_glob.size();
+  for (int k = 0; k < nn; k++)
+    if (ncomp[(size_t)k] != nsd) {
+      err = "coarse_method 3 needs all " + std::to_string(nsd) + " freedoms of every node (node " +
+            std::to_string(node_glob[(size_t)k] + 1) + " has " + std::to_string(ncomp[(size_t)k]) + ")";
+      return false;
+    }
+  std::vector<std::vector<int>> node_unk((size_t)nn);
+  for (int u = 0; u < n; u++) node_unk[(size_t)node_of[(size_t)u]].push_back(u);
+  // block norms ||A_IJ||_F^2, neighbours in first-touch order
+  std::vector<int64_t> nptr((size_t)nn + 1, 0);
+  std::vector<int> ncol;
+  std::vector<double> nval;
+  {
+    std::vector<int> pos((size_t)nn, -1);
+    for (int I = 0; I < nn; I++) {
+      const int64_t base = (int64_t)ncol.size();
+      for (int u : node_unk[(size_t)I])
+        for (int64_t k = A.ptr[(size_t)u]; k < A.ptr[(size_t)u + 1]; k++) {
+          const int J = node_of[(size_t)A.col[(size_t)k]];
+          const double a = A.val[(size_t)k];
+          if (pos[(size_t)J] < 0) { pos[(size_t)J] = (int)ncol.size(); ncol.push_back(J); nval.push_back(a * a); }
+          else nval[(size_t)pos[(size_t)J]] = nval[(size_t)pos[(size_t)J]] + a * a;
+        }
+      for (int64_t q = base; q < (int64_t)ncol.size(); q++) pos[(size_t)ncol[(size_t)q]] = -1;
+      nptr[(size_t)I + 1] = (int64_t)ncol.size();
+    }
+  }
+  std::vector<double> dnorm((size_t)nn, 0.0);
+  for (size_t q = 0; q < nval.size(); q++) nval[q] = std::sqrt(nval[q]);
+  for (int I = 0; I < nn; I++)
+    for (int64_t q = nptr[(size_t)I]; q < nptr[(size_t)I + 1]; q++)
+      if (ncol[(size_t)q] == I) dnorm[(size_t)I] = nval[(size_t)q];
+  std::vector<char> strong(ncol.size(), 0);
+  for (int I = 0; I < nn; I++)
+    for (int64_t q = nptr[(size_t)I]; q < nptr[(size_t)I + 1]; q++) {
+      const int J = ncol[(size_t)q];
+      strong[(size_t)q] = J != I && nval[(size_t)q] > theta * std::sqrt(dnorm[(size_t)I] * dnorm[(size_t)J]);
+    }
+  tm.lap("block strength");
+  // aggregation: (1) a node whose strong neighbours are all free starts an
+  // aggregate with them; (2) a free node joins the phase-1 aggregate of its
+  // strongest aggregated strong neighbour; (3) the rest start aggregates
+  // with their free strong neighbours
+  std::vector<int> agg((size_t)nn, -1);
+  int na = 0;
+  for (int I = 0; I < nn; I++) {
+    if (agg[(size_t)I] >= 0) continue;
+    bool free_all = true;
+    for (int64_t q = nptr[(size_t)I]; q < nptr[(size_t)I + 1] && free_all; q++)
+      if (strong[(size_t)q] && agg[(size_t)ncol[(size_t)q]] >= 0) free_all = false;
+    if (!free_all) continue;
+    agg[(size_t)I] = na;
+    for (int64_t q = nptr[(size_t)I]; q < nptr[(size_t)I + 1]; q++)
+      if (strong[(size_t)q]) agg[(size_t)ncol[(size_t)q]] = na;
+    na++;
+  }
+  {
+    const std::vector<int> agg1 = agg;
+    for (int I = 0; I < nn; I++) {
+      if (agg1[(size_t)I] >= 0) continue;
+      int best = -1;
+      double bv = 0.0;
+      for (int64_t q = nptr[(size_t)I]; q < nptr[(size_t)I + 1]; q++)
+        if (strong[(size_t)q] && agg1[(size_t)ncol[(size_t)q]] >= 0 && (best < 0 || nval[(size_t)q] > bv)) {
+          best = agg1[(size_t)ncol[(size_t)q]];
+          bv = nval[(size_t)q];
+        }
+      if (best >= 0) agg[(size_t)I] = best;
+    }
+  }
+  for (int I = 0; I < nn; I++) {
+    if (agg[(size_t)I] >= 0) continue;
+    agg[(size_t)I] = na;
+    for (int64_t q = nptr[(size_t)I]; q < nptr[(size_t)I + 1]; q++)
+      if (strong[(size_t)q] && agg[(size_t)ncol[(size_t)q]] < 0) agg[(size_t)ncol[(size_t)q]] = na;
+    na++;
+  }
+  tm.lap("node aggregation");
+  // tentative prolongator: rigid-body modes per aggregate, orthonormalised
+  std::vector<std::vector<int>> agg_nodes((size_t)na);
+  for (int I = 0; I < nn; I++) agg_nodes[(size_t)agg[(size_t)I]].push_back(I);
+  const int nmodes = nsd == 3 ? 6 : 3;
+  std::vector<int> cfirst((size_t)na + 1, 0);   // coarse freedoms of aggregate a: [cfirst[a], cfirst[a+1])
+  std::vector<std::vector<double>> Q((size_t)na);
+  for (int a = 0; a < na; a++) {
+    const std::vector<int> &nodes = agg_nodes[(size_t)a];
+    const int m = (int)nodes.size(), rows = m * nsd;
+    double cen[3] = {0.0, 0.0, 0.0};
+    for (int d = 0; d < nsd; d++) {
+      for (int I : nodes) cen[d] = cen[d] + xyz[(size_t)node_glob[(size_t)I] * nsd + d];
+      cen[d] = cen[d] / (double)m;
+    }
+    std::vector<double> B((size_t)rows * nmodes, 0.0);  // column-major rows x nmodes
+    for (int t = 0; t < m; t++) {
+      const int g = node_glob[(size_t)nodes[(size_t)t]];
+      const double x = xyz[(size_t)g * nsd] - cen[0], y = xyz[(size_t)g * nsd + 1] - cen[1];
+      const double z = nsd == 3 ? xyz[(size_t)g * nsd + 2] - cen[2] : 0.0;
+      for (int d = 0; d < nsd; d++) B[(size_t)d * rows + (size_t)t * nsd + d] = 1.0;
+      double *r = &B[(size_t)nsd * rows + (size_t)t * nsd];
+      if (nsd == 2) {
+        r[0] = -y; r[1] = x;
+      } else {
+        r[1] = -z; r[2] = y;                       // about x: (0, -z, y)
+        r[(size_t)rows] = z; r[(size_t)rows + 2] = -x;   // about y: (z, 0, -x)
+        r[2 * (size_t)rows] = -y; r[2 * (size_t)rows + 1] = x;  // about z: (-y, x, 0)
+      }
+    }
+    std::vector<double> &q = Q[(size_t)a];
+    int kept = 0;
+    for (int col = 0; col < nmodes; col++) {
+      std::vector<double> v(B.begin() + (size_t)col * rows, B.begin() + (size_t)(col + 1) * rows);
+      double n0 = 0.0;
+      for (int i = 0; i < rows; i++) n0 = n0 + v[(size_t)i] * v[(size_t)i];
+      n0 = std::sqrt(n0);
+      for (int pass = 0; pass < 2; pass++)
+        for (int p2 = 0; p2 < kept; p2++) {
+          const double *qp = &q[(size_t)p2 * rows];
+          double h = 0.0;
+          for (int i = 0; i < rows; i++) h = h + qp[i] * v[(size_t)i];
+          for (int i = 0; i < rows; i++) v[(size_t)i] = v[(size_t)i] - h * qp[i];
+        }
+      double nv = 0.0;
+      for (int i = 0; i < rows; i++) nv = nv + v[(size_t)i] * v[(size_t)i];
+      nv = std::sqrt(nv);
+      if (!(nv > 1e-8 * n0)) continue;
+      for (int i = 0; i < rows; i++) q.push_back(v[(size_t)i] / nv);
+      kept++;
+    }
+    cfirst[(size_t)a + 1] = cfirst[(size_t)a] + kept;
+  }
+  const int nc = cfirst[(size_t)na];
+  // P_tent by rows: unknown u of node t (position t in its aggregate), component d
+  std::vector<int> pos_in_agg((size_t)nn, 0);
+  for (int a = 0; a < na; a++)
+    for (size_t t = 0; t < agg_nodes[(size_t)a].size(); t++) pos_in_agg[(size_t)agg_nodes[(size_t)a][t]] = (int)t;
+  Coo Pt;
+  Pt.nrows = n; Pt.ncols = nc;
+  for (int u = 0; u < n; u++) {
+    const int I = node_of[(size_t)u], a = agg[(size_t)I];
+    const int rows = (int)agg_nodes[(size_t)a].size() * nsd;
+    const int r = pos_in_agg[(size_t)I] * nsd + comp[(size_t)u];
+    for (int col = cfirst[(size_t)a]; col < cfirst[(size_t)a + 1]; col++) {
+      Pt.i.push_back(u); Pt.j.push_back(col);
+      Pt.v.push_back(Q[(size_t)a][(size_t)(col - cfirst[(size_t)a]) * rows + r]);
+    }
+  }
+  const Csr Ptr = rows_of(Pt);
+  tm.lap("tentative prolongator");
+  // omega = 4 / (3 rho(D^-1 A)), rho from 20 power steps
+  std::vector<double> dg((size_t)n, 0.0);
+  for (int u = 0; u < n; u++)
+    for (int64_t k = A.ptr[(size_t)u]; k < A.ptr[(size_t)u + 1]; k++)
+      if (A.col[(size_t)k] == u) dg[(size_t)u] = A.val[(size_t)k];
+  for (int u = 0; u < n; u++)
+    if (!(dg[(size_t)u] > 0.0)) { err = "coarse_method 3: non-positive diagonal at unknown " + std::to_string(u + 1); return false; }
+  std::vector<double> xv((size_t)n), yv((size_t)n);
+  for (int u = 0; u < n; u++) xv[(size_t)u] = 1.0 + (double)(u % 7) / 7.0;
+  double rho = 0.0;
+  for (int it = 0; it < 20; it++) {
+    parallel_rows(n, [&](int lo, int hi) {
+      for (int u = lo; u < hi; u++) {
+        double sacc = 0.0;
+        for (int64_t k = A.ptr[(size_t)u]; k < A.ptr[(size_t)u + 1]; k++)
+          sacc = sacc + A.val[(size_t)k] * xv[(size_t)A.col[(size_t)k]];
+        yv[(size_t)u] = sacc / dg[(size_t)u];
+      }
+    });
+    double ny = 0.0, nx = 0.0;
+    for (int u = 0; u < n; u++) { ny = ny + yv[(size_t)u] * yv[(size_t)u]; nx = nx + xv[(size_t)u] * xv[(size_t)u]; }
+    ny = std::sqrt(ny);
+    rho = ny / std::sqrt(nx);
+    for (int u = 0; u < n; u++) xv[(size_t)u] = yv[(size_t)u] / ny;
+  }
+  const double omega = 4.0 / (3.0 * rho);
+  tm.lap("spectral radius");
+  // P = P_tent - omega D^-1 (A P_tent), the pattern of A P_tent
+  Csr AP = spgemm_first_touch(A, Ptr);
+  Coo Rcoo;  // R = P^T as coarse x fine, unknown after unknown
+  Rcoo.nrows = nc; Rcoo.ncols = n;
+  {
+    std::vector<double> ptv((size_t)nc, 0.0);
+    for (int u = 0; u < n; u++) {
+      for (int64_t k = Ptr.ptr[(size_t)u]; k < Ptr.ptr[(size_t)u + 1]; k++) ptv[(size_t)Ptr.col[(size_t)k]] = Ptr.val[(size_t)k];
+      const double w = omega / dg[(size_t)u];
+      for (int64_t k = AP.ptr[(size_t)u]; k < AP.ptr[(size_t)u + 1]; k++) {
+        const int col = AP.col[(size_t)k];
+        Rcoo.i.push_back(col); Rcoo.j.push_back(u); Rcoo.v.push_back(ptv[(size_t)col] - w * AP.val[(size_t)k]);
+      }
+      for (int64_t k = Ptr.ptr[(size_t)u]; k < Ptr.ptr[(size_t)u + 1]; k++) ptv[(size_t)Ptr.col[(size_t)k]] = 0.0;
+    }
+  }
+  tm.lap("smoothed prolongator");
+  Csr AC = galerkin(A, Rcoo, n, out, &tm);
+  tm.lap("Galerkin");
+  out.AC = AC;
+  out.AC_i.reserve(AC.col.size()); out.AC_j.reserve(AC.col.size()); out.AC_v.reserve(AC.col.size());
+  for (int r = 0; r < AC.nrows; r++)
+    for (int64_t k = AC.ptr[(size_t)r]; k < AC.ptr[(size_t)r + 1]; k++) {
+      out.AC_i.push_back(r + 1); out.AC_j.push_back(AC.col[(size_t)k] + 1); out.AC_v.push_back(AC.val[(size_t)k]);
+    }
+  // unknowns' aggregates (1-based) for export; no coarse aggregates
+  std::vector<int> num((size_t)n);
+  for (int u = 0; u < n; u++) num[(size_t)u] = agg[(size_t)node_of[(size_t)u]] + 1;
+  form_aggr(out.fine, na, n, num);
+  out.fine_full = out.fine;
+  out.coarse.num.clear();
+  out.overlap = c.overlap < 0 ? std::max(c.smoothers, 0) : c.overlap;
+  out.smoothers = c.smoothers;
+  out.levels = c.levels;
+  std::vector<std::vector<int>> lists((size_t)nparts);
+  for (int i = 0; i < n; i++) lists[(size_t)(*part)[(size_t)i] - 1].push_back(i);
   grow_subdomains(A, lists, out.overlap, out);
   tm.lap("subdomains + overlap");
   out.A = A;

@@ -202,6 +202,16 @@ bool geometric_restriction(const Controls &c, const std::vector<int> &efree, con
 // than 4000 coarse freedoms: all kept.
 std::vector<int> independent_coarse(const Csr &AC);
 
+// Smoothed aggregation over nodal blocks with a rigid-body near-nullspace
+// (coarse_method 3, no reference counterpart): unode[u] is the 0-based mesh
+// node of unknown u (its unknowns ascending are the node's components), xyz
+// the node coordinates (nsd per node, indexed by that node id).  Needs an
+// imported partition for the subdomains.
+bool build_setup_rbm(const Controls &c, int n, const std::vector<int> &ii, const std::vector<int> &jj,
+                     const std::vector<double> &vv, const std::vector<int> *part, int nparts,
+                     const std::vector<int> &unode, int nsd, const std::vector<double> &xyz, SetupResult &out,
+                     std::string &err);
+
 // Batched independent systems: system k owns the rows [sys_row[k],
 // sys_row[k+1]) and the triplets [sys_tri[k], sys_tri[k+1]) of (ii, jj, vv),
 // whose indices are 1-based in the combined numbering.  Every system gets the

@@ -2430,11 +2430,297 @@ static void run_setup_geom(state *s, const int *part, int nparts) {
 }
 
 /* aggr.F90:131-215 for numprocs==1 (or an imported partition). */
+/* Node geometry for coarse_method 3 (orc_set_geometry): the 1-based mesh
+ * node of every unknown and the node coordinates (nsd per node). */
+static int g_geo_nsd = 0, g_geo_n = 0, g_geo_nnode = 0;
+static int *g_geo_unode = NULL;
+static double *g_geo_xyz = NULL;
+
+void orc_set_geometry(int nsd, int nnode, const double *coords, int n, const int *unode) {
+  free(g_geo_unode); free(g_geo_xyz);
+  g_geo_unode = NULL; g_geo_xyz = NULL;
+  g_geo_nsd = 0; g_geo_n = 0; g_geo_nnode = 0;
+  if (nsd <= 0 || !coords || !unode) return;
+  g_geo_nsd = nsd; g_geo_n = n; g_geo_nnode = nnode;
+  g_geo_unode = (int *)malloc(sizeof(int) * ((size_t)n + 1));
+  g_geo_xyz = (double *)malloc(sizeof(double) * ((size_t)nsd * nnode + 1));
+  memcpy(g_geo_unode + 1, unode, sizeof(int) * (size_t)n);
+  memcpy(g_geo_xyz, coords, sizeof(double) * (size_t)nsd * nnode);
+}
+
+/* coarse_method 3 (no counterpart in the reference, whose aggregation is
+ * scalar): smoothed aggregation over mesh nodes with the rigid-body modes as
+ * near-nullspace (Vanek, Mandel & Brezina, Computing 56 (1996) 179-196).
+ * Nodes in order of first appearance over the unknowns, a node's unknowns
+ * ascending being its components; block strength ||A_IJ||_F > theta *
+ * sqrt(||A_II||_F ||A_JJ||_F); three aggregation passes (whole free
+ * neighbourhoods, then joining the strongest phase-1 neighbour aggregate,
+ * then new aggregates of the rest); per aggregate the translations and
+ * rotations about its centroid, orthonormalised by modified Gram-Schmidt
+ * applied twice, columns below 1e-8 of their norm dropped; P = P_tent -
+ * omega D^-1 A P_tent, omega = 4 / (3 rho(D^-1 A)) with rho from 20 power
+ * steps; R = P^T and AC = R A R^T.  Subdomains: the imported parts with the
+ * overlap layers. */
+static void run_setup_rbm(state *s, const int *part, int nparts) {
+  ctl_t *c = &s->ctl;
+  int n = s->n, nsd = g_geo_nsd, i, k, u;
+  if (!part) orc_abort("coarse_method 3 needs an imported partition");
+  if (nsd != 2 && nsd != 3) orc_abort("coarse_method 3 needs node coordinates (orc_set_geometry)");
+  if (g_geo_n != n) orc_abort("coarse_method 3: geometry for %d unknowns, matrix has %d", g_geo_n, n);
+  if (c->method == 2 || c->method == 3)
+    orc_abort("method %d restricts a residual the one-process reference never sets (pcg.F90:146-149)", c->method);
+  s->strong1 = (c->strong1 != 0.0) ? c->strong1 : 0.67;
+  double theta = s->strong1;
+  spm_arrange(&s->A, ARR_ROWS, 0, 0, 0, 0);
+  const spm *A = &s->A;
+  /* nodes by first appearance */
+  int *nid = NEWI(g_geo_nnode), *node_of = NEWI(n), *comp = NEWI(n);
+  int *node_glob = NEWI(n), *ncomp = NEWI(n), nn = 0;
+  for (u = 1; u <= n; u++) {
+    int g = g_geo_unode[u];
+    if (g < 1 || g > g_geo_nnode) orc_abort("coarse_method 3: node %d of unknown %d out of range", g, u);
+    if (nid[g] == 0) { nn++; nid[g] = nn; node_glob[nn] = g; ncomp[nn] = 0; }
+    node_of[u] = nid[g];
+    comp[u] = ncomp[nid[g]]++;
+  }
+  for (k = 1; k <= nn; k++)
+    if (ncomp[k] != nsd) orc_abort("coarse_method 3 needs all %d freedoms of every node", nsd);
+  /* unknowns per node, ascending */
+  int *nu_ptr = NEWI(nn + 1), *nu = NEWI(n), *fillp = NEWI(nn + 1);
+  for (u = 1; u <= n; u++) nu_ptr[node_of[u] + 1]++;
+  nu_ptr[1] = 1;
+  for (k = 1; k <= nn; k++) nu_ptr[k + 1] += nu_ptr[k];
+  for (k = 1; k <= nn; k++) fillp[k] = nu_ptr[k];
+  for (u = 1; u <= n; u++) nu[fillp[node_of[u]]++] = u;
+  /* block norms, neighbours in first-touch order */
+  long cap = (long)A->nnz + 1;
+  int *bptr = NEWI(nn + 1), *bcol = NEWI(cap);
+  double *bval = NEWD(cap);
+  int *posn = NEWI(nn), nb = 0;
+  for (k = 1; k <= nn; k++) posn[k] = 0;
+  bptr[1] = 1;
+  for (k = 1; k <= nn; k++) {
+    int q0 = nb + 1, t;
+    for (t = nu_ptr[k]; t < nu_ptr[k + 1]; t++) {
+      int uu = nu[t], e;
+      for (e = A->mbound[uu]; e <= A->mbound[uu + 1] - 1; e++) {
+        int J = node_of[A->indj[e]];
+        double a = A->val[e];
+        if (posn[J] == 0) { nb++; posn[J] = nb; bcol[nb] = J; bval[nb] = a * a; }
+        else bval[posn[J]] = bval[posn[J]] + a * a;
+      }
+    }
+    for (t = q0; t <= nb; t++) posn[bcol[t]] = 0;
+    bptr[k + 1] = nb + 1;
+  }
+  double *dn = NEWD(nn);
+  for (i = 1; i <= nb; i++) bval[i] = sqrt(bval[i]);
+  for (k = 1; k <= nn; k++)
+    for (i = bptr[k]; i < bptr[k + 1]; i++)
+      if (bcol[i] == k) dn[k] = bval[i];
+  char *strong = NEWB(nb);
+  for (k = 1; k <= nn; k++)
+    for (i = bptr[k]; i < bptr[k + 1]; i++) {
+      int J = bcol[i];
+      strong[i] = (J != k && bval[i] > theta * sqrt(dn[k] * dn[J])) ? 1 : 0;
+    }
+  /* aggregation: 1-based aggregate per node, 0 = free */
+  int *agg = NEWI(nn), *agg1 = NEWI(nn), na = 0;
+  for (k = 1; k <= nn; k++) {
+    int freeall = 1;
+    if (agg[k]) continue;
+    for (i = bptr[k]; i < bptr[k + 1]; i++)
+      if (strong[i] && agg[bcol[i]]) { freeall = 0; break; }
+    if (!freeall) continue;
+    na++;
+    agg[k] = na;
+    for (i = bptr[k]; i < bptr[k + 1]; i++)
+      if (strong[i]) agg[bcol[i]] = na;
+  }
+  for (k = 1; k <= nn; k++) agg1[k] = agg[k];
+  for (k = 1; k <= nn; k++) {
+    int best = 0;
+    double bv = 0.0;
+    if (agg1[k]) continue;
+    for (i = bptr[k]; i < bptr[k + 1]; i++)
+      if (strong[i] && agg1[bcol[i]] && (best == 0 || bval[i] > bv)) { best = agg1[bcol[i]]; bv = bval[i]; }
+    if (best) agg[k] = best;
+  }
+  for (k = 1; k <= nn; k++) {
+    if (agg[k]) continue;
+    na++;
+    agg[k] = na;
+    for (i = bptr[k]; i < bptr[k + 1]; i++)
+      if (strong[i] && agg[bcol[i]] == 0) agg[bcol[i]] = na;
+  }
+  /* nodes per aggregate, ascending */
+  int *ag_ptr = NEWI(na + 1), *ag_nodes = NEWI(nn), *pos_in = NEWI(nn);
+  for (k = 1; k <= nn; k++) ag_ptr[agg[k] + 1]++;
+  ag_ptr[1] = 1;
+  for (i = 1; i <= na; i++) ag_ptr[i + 1] += ag_ptr[i];
+  {
+    int *f2 = NEWI(na + 1);
+    for (i = 1; i <= na; i++) f2[i] = ag_ptr[i];
+    for (k = 1; k <= nn; k++) { pos_in[k] = f2[agg[k]] - ag_ptr[agg[k]]; ag_nodes[f2[agg[k]]++] = k; }
+    free(f2);
+  }
+  /* rigid-body modes, orthonormalised */
+  int nmodes = nsd == 3 ? 6 : 3;
+  int *cfirst = NEWI(na + 1);
+  double **Q = (double **)xcalloc((size_t)na + 1, sizeof(double *));
+  cfirst[1] = 1;
+  for (int a = 1; a <= na; a++) {
+    int m = ag_ptr[a + 1] - ag_ptr[a], rows = m * nsd, t, d, col, kept = 0;
+    double cen[3] = {0.0, 0.0, 0.0};
+    for (d = 0; d < nsd; d++) {
+      for (t = ag_ptr[a]; t < ag_ptr[a + 1]; t++) cen[d] = cen[d] + g_geo_xyz[(size_t)(node_glob[ag_nodes[t]] - 1) * nsd + d];
+      cen[d] = cen[d] / (double)m;
+    }
+    double *B = (double *)xcalloc((size_t)rows * nmodes + 1, sizeof(double));
+    for (t = 0; t < m; t++) {
+      int g = node_glob[ag_nodes[ag_ptr[a] + t]] - 1;
+      double x = g_geo_xyz[(size_t)g * nsd] - cen[0], y = g_geo_xyz[(size_t)g * nsd + 1] - cen[1];
+      double z = nsd == 3 ? g_geo_xyz[(size_t)g * nsd + 2] - cen[2] : 0.0;
+      for (d = 0; d < nsd; d++) B[(size_t)d * rows + t * nsd + d] = 1.0;
+      if (nsd == 2) {
+        B[(size_t)2 * rows + t * 2] = -y; B[(size_t)2 * rows + t * 2 + 1] = x;
+      } else {
+        B[(size_t)3 * rows + t * 3 + 1] = -z; B[(size_t)3 * rows + t * 3 + 2] = y;
+        B[(size_t)4 * rows + t * 3] = z; B[(size_t)4 * rows + t * 3 + 2] = -x;
+        B[(size_t)5 * rows + t * 3] = -y; B[(size_t)5 * rows + t * 3 + 1] = x;
+      }
+    }
+    double *q = (double *)xcalloc((size_t)rows * nmodes + 1, sizeof(double));
+    double *v = (double *)xcalloc((size_t)rows + 1, sizeof(double));
+    for (col = 0; col < nmodes; col++) {
+      int r, pass, p2;
+      double n0 = 0.0, nv = 0.0;
+      for (r = 0; r < rows; r++) v[r] = B[(size_t)col * rows + r];
+      for (r = 0; r < rows; r++) n0 = n0 + v[r] * v[r];
+      n0 = sqrt(n0);
+      for (pass = 0; pass < 2; pass++)
+        for (p2 = 0; p2 < kept; p2++) {
+          const double *qp = q + (size_t)p2 * rows;
+          double h = 0.0;
+          for (r = 0; r < rows; r++) h = h + qp[r] * v[r];
+          for (r = 0; r < rows; r++) v[r] = v[r] - h * qp[r];
+        }
+      for (r = 0; r < rows; r++) nv = nv + v[r] * v[r];
+      nv = sqrt(nv);
+      if (!(nv > 1e-8 * n0)) continue;
+      for (r = 0; r < rows; r++) q[(size_t)kept * rows + r] = v[r] / nv;
+      kept++;
+    }
+    free(B); free(v);
+    Q[a] = q;
+    cfirst[a + 1] = cfirst[a] + kept;
+  }
+  int nc = cfirst[na + 1] - 1;
+  /* tentative prolongator, unknown after unknown (n x nc) */
+  spm Pt = spm_new(n * nmodes, n, nc);
+  int np = 0;
+  for (u = 1; u <= n; u++) {
+    int K = node_of[u], a = agg[K], rows = (ag_ptr[a + 1] - ag_ptr[a]) * nsd, col;
+    int r = pos_in[K] * nsd + comp[u];
+    for (col = cfirst[a]; col < cfirst[a + 1]; col++) {
+      np++;
+      Pt.indi[np] = u; Pt.indj[np] = col; Pt.val[np] = Q[a][(size_t)(col - cfirst[a]) * rows + r];
+    }
+  }
+  Pt.nnz = np;
+  /* omega from the power method on D^-1 A */
+  double *dg = NEWD(n), *xv = NEWD(n), *yv = NEWD(n), rho = 0.0;
+  for (u = 1; u <= n; u++)
+    for (k = A->mbound[u]; k <= A->mbound[u + 1] - 1; k++)
+      if (A->indj[k] == u) dg[u] = A->val[k];
+  for (u = 1; u <= n; u++)
+    if (!(dg[u] > 0.0)) orc_abort("coarse_method 3: non-positive diagonal at unknown %d", u);
+  for (u = 1; u <= n; u++) xv[u] = 1.0 + (double)((u - 1) % 7) / 7.0;
+  for (int it = 0; it < 20; it++) {
+    double ny = 0.0, nx = 0.0;
+    for (u = 1; u <= n; u++) {
+      double sacc = 0.0;
+      for (k = A->mbound[u]; k <= A->mbound[u + 1] - 1; k++) sacc = sacc + A->val[k] * xv[A->indj[k]];
+      yv[u] = sacc / dg[u];
+    }
+    for (u = 1; u <= n; u++) { ny = ny + yv[u] * yv[u]; nx = nx + xv[u] * xv[u]; }
+    ny = sqrt(ny);
+    rho = ny / sqrt(nx);
+    for (u = 1; u <= n; u++) xv[u] = yv[u] / ny;
+  }
+  double omega = 4.0 / (3.0 * rho);
+  /* A P_tent (first-touch), then P = P_tent - omega D^-1 A P_tent as R = P^T */
+  spm AA = spm_copy(A);
+  spm AP = spm_AB(&AA, &Pt, 0, 0);
+  spm_free(&AA);
+  spm_arrange(&AP, ARR_ROWS, 0, 0, 0, 0);
+  spm_arrange(&Pt, ARR_ROWS, 0, 0, 0, 0);
+  spm R = spm_new(AP.nnz, nc, n);
+  {
+    double *ptv = NEWD(nc);
+    int nr = 0;
+    for (u = 1; u <= n; u++) {
+      for (k = Pt.mbound[u]; k <= Pt.mbound[u + 1] - 1; k++) ptv[Pt.indj[k]] = Pt.val[k];
+      double w = omega / dg[u];
+      for (k = AP.mbound[u]; k <= AP.mbound[u + 1] - 1; k++) {
+        int col = AP.indj[k];
+        nr++;
+        R.indi[nr] = col; R.indj[nr] = u; R.val[nr] = ptv[col] - w * AP.val[k];
+      }
+      for (k = Pt.mbound[u]; k <= Pt.mbound[u + 1] - 1; k++) ptv[Pt.indj[k]] = 0.0;
+    }
+    R.nnz = nr;
+    free(ptv);
+  }
+  s->R = R;
+  s->have_R = 1;
+  s->AC = coarse_mtx_build(&s->A, &s->R, n, 0);
+  /* aggregates per unknown for export */
+  int *num = NEWI(n);
+  for (u = 1; u <= n; u++) num[u] = agg[node_of[u]];
+  form_aggr(&s->fine_inner, na, n, 0, 0, num);
+  form_aggr(&s->fine_full, na, n, 0, 0, num);
+  free(num);
+  s->have_coarse = 0;
+  /* subdomains: imported parts + overlap (Get_nodes, Add_layers) */
+  s->ol = (c->overlap < 0) ? (c->smoothers > 0 ? c->smoothers : 0) : c->overlap;
+  spm_arrange(&s->A, ARR_ROWS, 0, 0, 0, 0);
+  int *nodes = NEWI(n);
+  s->nsubd = nparts;
+  s->sd_start = (int *)xcalloc((size_t)nparts + 2, sizeof(int));
+  long scap = 16L * n + 16, fill = 0;
+  s->sd_nodes = (int *)xcalloc((size_t)scap, sizeof(int));
+  for (int ip = 1; ip <= nparts; ip++) {
+    int nnodes = 0;
+    for (i = 1; i <= n; i++) if (part[i - 1] == ip) nodes[++nnodes] = i;
+    int nexp = add_layers(s->A.mbound, s->A.indj, nodes, nnodes, s->ol, n);
+    if (fill + nexp > scap) {
+      scap = 2 * (fill + nexp);
+      s->sd_nodes = (int *)realloc(s->sd_nodes, sizeof(int) * (size_t)scap);
+      if (!s->sd_nodes) orc_abort("out of memory");
+    }
+    s->sd_start[ip - 1] = (int)fill;
+    memcpy(s->sd_nodes + fill, nodes + 1, sizeof(int) * (size_t)nexp);
+    fill += nexp;
+  }
+  s->sd_start[nparts] = (int)fill;
+  free(nodes);
+  for (int a = 1; a <= na; a++) free(Q[a]);
+  free(Q); free(cfirst); spm_free(&Pt); spm_free(&AP);
+  free(dg); free(xv); free(yv); free(agg); free(agg1); free(ag_ptr); free(ag_nodes); free(pos_in);
+  free(bptr); free(bcol); free(bval); free(posn); free(dn); free(strong);
+  free(nu_ptr); free(nu); free(fillp); free(nid); free(node_of); free(comp); free(node_glob); free(ncomp);
+}
+
 static void run_setup(state *s, const int *part, int nparts) {
   ctl_t *c = &s->ctl;
   int n = s->n, i;
   if (c->executable == 1) {
     run_setup_geom(s, part, nparts);
+    return;
+  }
+  if (c->coarse_method == 3) {
+    run_setup_rbm(s, part, nparts);
     return;
   }
   /* Partitionings_aggr_InitFine (Partitioning_aggr.F90:33-117) */

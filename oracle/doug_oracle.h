@@ -95,6 +95,12 @@ int orc_setup_coo(int n, int nnz, const int *ii, const int *jj, const double *vv
                   const char *ctl_text, const int *part, int nparts,
                   orc_result **out);
 
+/* Node geometry for coarse_method 3 (smoothed aggregation over nodal blocks
+ * with rigid-body modes), used by the following runs: nsd coordinates per
+ * node (nnode nodes) and the 1-based node of each of the n unknowns (a
+ * node's unknowns ascending are its components).  nsd 0 clears it. */
+void orc_set_geometry(int nsd, int nnode, const double *coords, int n, const int *unode);
+
 void orc_free(orc_result *r);
 
 /* File-format helpers (restated readers/writers). Return 0 on success. */

@@ -89,6 +89,7 @@ def lib():
             L.orc_session_solve.argtypes = [C.c_void_p, P(C.c_double), P(P(_Result))]
             L.orc_session_free.argtypes = [C.c_void_p]
             L.orc_set_threads.argtypes = [C.c_int]
+            L.orc_set_geometry.argtypes = [C.c_int, C.c_int, P(C.c_double), C.c_int, P(C.c_int)]
             for nm in ("orc_parse_i10", "orc_parse_l1"):
                 getattr(L, nm).argtypes = [C.c_char_p, P(C.c_int)]
             L.orc_parse_f10_5.argtypes = [C.c_char_p, P(C.c_double)]
@@ -300,6 +301,19 @@ class SpdFactor:
                 self._f = None
         except Exception:
             pass
+
+
+def set_geometry(coords=None, unode=None):
+    """Node geometry for coarse_method 3 (used by the following runs):
+    coords (nnode x nsd) and the 1-based node of every unknown.  No
+    arguments: clear it."""
+    L = lib()
+    if coords is None:
+        L.orc_set_geometry(0, 0, None, 0, None)
+        return
+    xyz = np.ascontiguousarray(coords, dtype=np.float64)
+    un = np.ascontiguousarray(unode, dtype=np.int32)
+    L.orc_set_geometry(xyz.shape[1], xyz.shape[0], _dp(xyz), len(un), _ip(un))
 
 
 def set_threads(n):
