@@ -36,14 +36,17 @@ def test_oracle_robust_lap16x16_matches_fixture():
 
 
 def test_coarse_method_words():
+    # coarse_method 4 is unknown (aggr.F90:155-165: "Wrong coarse method");
+    # 3 (the rigid-body coarse space, an extension) needs node coordinates
     n, r, c, v, b = P.laplace2d(8)
-    s = D.DougSolver(dict(solver=2, method=1, fine_method=1, levels=2, coarse_method=3))
-    s.set_matrix_coo(n, r, c, v)
-    with pytest.raises(D.DougError) as ei:
-        s.setup_host_only()
-    assert "coarse method" in str(ei.value)
-    ro = O.run_coo(n, r, c, v, rhs=b, ctl="solver 2\nmethod 1\nfine_method 1\nlevels 2\ncoarse_method 3\n")
-    assert ro["status"] != 0
+    for cm, msg in ((4, "coarse method"), (3, "node coordinates")):
+        s = D.DougSolver(dict(solver=2, method=1, fine_method=1, levels=2, coarse_method=cm))
+        s.set_matrix_coo(n, r, c, v)
+        with pytest.raises(D.DougError) as ei:
+            s.setup_host_only()
+        assert msg in str(ei.value)
+        ro = O.run_coo(n, r, c, v, rhs=b, ctl=f"solver 2\nmethod 1\nfine_method 1\nlevels 2\ncoarse_method {cm}\n")
+        assert ro["status"] != 0
 
 
 CASES = {
