@@ -1560,6 +1560,51 @@ bool build_setup(const Controls &c_in, int n, const std::vector<int> &ii, const 
   return true;
 }
 
+// The three aggregation passes of smoothed aggregation on a weighted graph
+// (vertex v's neighbours col[ptr[v]..ptr[v+1]) with weights val, strong
+// flags): (1) a vertex whose strong neighbours are all free starts an
+// aggregate with them; (2) a free vertex joins the phase-1 aggregate of its
+// strongest aggregated strong neighbour (first on ties); (3) every vertex
+// still free starts an aggregate with its free strong neighbours.  Vertices
+// in order; agg[v] = 0-based aggregate; returns the number of aggregates.
+static int three_phase_aggregate(int nv, const std::vector<int64_t> &ptr, const std::vector<int> &col,
+                                 const std::vector<double> &val, const std::vector<char> &strong,
+                                 std::vector<int> &agg) {
+  agg.assign((size_t)nv, -1);
+  int na = 0;
+  for (int I = 0; I < nv; I++) {
+    if (agg[(size_t)I] >= 0) continue;
+    bool free_all = true;
+    for (int64_t q = ptr[(size_t)I]; q < ptr[(size_t)I + 1] && free_all; q++)
+      if (strong[(size_t)q] && col[(size_t)q] != I && agg[(size_t)col[(size_t)q]] >= 0) free_all = false;
+    if (!free_all) continue;
+    agg[(size_t)I] = na;
+    for (int64_t q = ptr[(size_t)I]; q < ptr[(size_t)I + 1]; q++)
+      if (strong[(size_t)q]) agg[(size_t)col[(size_t)q]] = na;
+    na++;
+  }
+  const std::vector<int> agg1 = agg;
+  for (int I = 0; I < nv; I++) {
+    if (agg1[(size_t)I] >= 0) continue;
+    int best = -1;
+    double bv = 0.0;
+    for (int64_t q = ptr[(size_t)I]; q < ptr[(size_t)I + 1]; q++)
+      if (strong[(size_t)q] && agg1[(size_t)col[(size_t)q]] >= 0 && (best < 0 || val[(size_t)q] > bv)) {
+        best = agg1[(size_t)col[(size_t)q]];
+        bv = val[(size_t)q];
+      }
+    if (best >= 0) agg[(size_t)I] = best;
+  }
+  for (int I = 0; I < nv; I++) {
+    if (agg[(size_t)I] >= 0) continue;
+    agg[(size_t)I] = na;
+    for (int64_t q = ptr[(size_t)I]; q < ptr[(size_t)I + 1]; q++)
+      if (strong[(size_t)q] && agg[(size_t)col[(size_t)q]] < 0) agg[(size_t)col[(size_t)q]] = na;
+    na++;
+  }
+  return na;
+}
+
 // ---------------------------------------------------------------------------
 // Smoothed aggregation over nodal blocks with a rigid-body near-nullspace
 // (coarse_method 3; no counterpart in the reference, whose aggregation is
@@ -1569,7 +1614,9 @@ bool build_setup(const Controls &c_in, int n, const std::vector<int> &ii, const 
 // theta sqrt(||A_II||_F ||A_JJ||_F); per aggregate the rigid-body modes
 // (nsd translations, 1 or 3 rotations about the aggregate's centroid)
 // orthonormalised by twice-repeated modified Gram-Schmidt (columns that
-// vanish are dropped) form the tentative prolongator; Jacobi smoothing
+// vanish are dropped) form the tentative prolongator; radius1 rounds of
+// aggregation (the later ones over the previous round's aggregates) set
+// the aggregate size; Jacobi smoothing
 // P = (I - omega D^-1 A) P_tent with omega = 4 / (3 rho(D^-1 A)), rho by 20
 // power steps; R = P^T and AC = R A P.  Every loop runs in a fixed order, so
 // the oracle's restatement gives the same bits.
@@ -1655,43 +1702,38 @@ bool build_setup_rbm(const Controls &c_in, int n, const std::vector<int> &ii, co
       strong[(size_t)q] = J != I && nval[(size_t)q] > theta * std::sqrt(dnorm[(size_t)I] * dnorm[(size_t)J]);
     }
   tm.lap("block strength");
-  // aggregation: (1) a node whose strong neighbours are all free starts an
-  // aggregate with them; (2) a free node joins the phase-1 aggregate of its
-  // strongest aggregated strong neighbour; (3) the rest start aggregates
-  // with their free strong neighbours
-  std::vector<int> agg((size_t)nn, -1);
-  int na = 0;
-  for (int I = 0; I < nn; I++) {
-    if (agg[(size_t)I] >= 0) continue;
-    bool free_all = true;
-    for (int64_t q = nptr[(size_t)I]; q < nptr[(size_t)I + 1] && free_all; q++)
-      if (strong[(size_t)q] && agg[(size_t)ncol[(size_t)q]] >= 0) free_all = false;
-    if (!free_all) continue;
-    agg[(size_t)I] = na;
-    for (int64_t q = nptr[(size_t)I]; q < nptr[(size_t)I + 1]; q++)
-      if (strong[(size_t)q]) agg[(size_t)ncol[(size_t)q]] = na;
-    na++;
-  }
-  {
-    const std::vector<int> agg1 = agg;
-    for (int I = 0; I < nn; I++) {
-      if (agg1[(size_t)I] >= 0) continue;
-      int best = -1;
-      double bv = 0.0;
-      for (int64_t q = nptr[(size_t)I]; q < nptr[(size_t)I + 1]; q++)
-        if (strong[(size_t)q] && agg1[(size_t)ncol[(size_t)q]] >= 0 && (best < 0 || nval[(size_t)q] > bv)) {
-          best = agg1[(size_t)ncol[(size_t)q]];
-          bv = nval[(size_t)q];
+  // aggregation rounds: round 1 aggregates the nodes over the strong block
+  // graph; every further round (radius1 rounds in all, at least 1)
+  // aggregates the previous round's aggregates over the graph of their
+  // strong connections (weight: the sum of the block norms between them)
+  std::vector<int> agg;
+  int na = three_phase_aggregate(nn, nptr, ncol, nval, strong, agg);
+  const int rounds = c.radius1 > 0 ? c.radius1 : 1;
+  for (int round = 2; round <= rounds && na > 1; round++) {
+    std::vector<int64_t> gptr((size_t)na + 1, 0);
+    std::vector<int> gcol;
+    std::vector<double> gval;
+    std::vector<std::vector<int>> members((size_t)na);
+    for (int I = 0; I < nn; I++) members[(size_t)agg[(size_t)I]].push_back(I);
+    std::vector<int> pos((size_t)na, -1);
+    for (int a = 0; a < na; a++) {
+      const int64_t base = (int64_t)gcol.size();
+      for (int I : members[(size_t)a])
+        for (int64_t q = nptr[(size_t)I]; q < nptr[(size_t)I + 1]; q++) {
+          if (!strong[(size_t)q]) continue;
+          const int b = agg[(size_t)ncol[(size_t)q]];
+          if (b == a) continue;
+          if (pos[(size_t)b] < 0) { pos[(size_t)b] = (int)gcol.size(); gcol.push_back(b); gval.push_back(nval[(size_t)q]); }
+          else gval[(size_t)pos[(size_t)b]] = gval[(size_t)pos[(size_t)b]] + nval[(size_t)q];
         }
-      if (best >= 0) agg[(size_t)I] = best;
+      for (int64_t q = base; q < (int64_t)gcol.size(); q++) pos[(size_t)gcol[(size_t)q]] = -1;
+      gptr[(size_t)a + 1] = (int64_t)gcol.size();
     }
-  }
-  for (int I = 0; I < nn; I++) {
-    if (agg[(size_t)I] >= 0) continue;
-    agg[(size_t)I] = na;
-    for (int64_t q = nptr[(size_t)I]; q < nptr[(size_t)I + 1]; q++)
-      if (strong[(size_t)q] && agg[(size_t)ncol[(size_t)q]] < 0) agg[(size_t)ncol[(size_t)q]] = na;
-    na++;
+    std::vector<char> gstrong(gcol.size(), 1);
+    std::vector<int> agg2;
+    const int na2 = three_phase_aggregate(na, gptr, gcol, gval, gstrong, agg2);
+    for (int I = 0; I < nn; I++) agg[(size_t)I] = agg2[(size_t)agg[(size_t)I]];
+    na = na2;
   }
   tm.lap("node aggregation");
   // tentative prolongator: rigid-body modes per aggregate, orthonormalised

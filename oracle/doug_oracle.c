@@ -2448,6 +2448,48 @@ void orc_set_geometry(int nsd, int nnode, const double *coords, int n, const int
   memcpy(g_geo_xyz, coords, sizeof(double) * (size_t)nsd * nnode);
 }
 
+/* The three aggregation passes of smoothed aggregation on a weighted graph
+ * (1-based: vertex v's neighbours col[ptr[v]..ptr[v+1]-1], weights val,
+ * strong flags): (1) a vertex whose strong neighbours are all free starts an
+ * aggregate with them; (2) a free vertex joins the phase-1 aggregate of its
+ * strongest aggregated strong neighbour (first on ties); (3) the vertices
+ * still free start aggregates with their free strong neighbours.  agg[v]:
+ * 1-based aggregate; returns their number. */
+static int three_phase(int nv, const int *ptr, const int *col, const double *val, const char *strong, int *agg) {
+  int k, i, na = 0;
+  int *agg1 = NEWI(nv);
+  for (k = 1; k <= nv; k++) agg[k] = 0;
+  for (k = 1; k <= nv; k++) {
+    int freeall = 1;
+    if (agg[k]) continue;
+    for (i = ptr[k]; i < ptr[k + 1]; i++)
+      if (strong[i] && col[i] != k && agg[col[i]]) { freeall = 0; break; }
+    if (!freeall) continue;
+    na++;
+    agg[k] = na;
+    for (i = ptr[k]; i < ptr[k + 1]; i++)
+      if (strong[i]) agg[col[i]] = na;
+  }
+  for (k = 1; k <= nv; k++) agg1[k] = agg[k];
+  for (k = 1; k <= nv; k++) {
+    int best = 0;
+    double bv = 0.0;
+    if (agg1[k]) continue;
+    for (i = ptr[k]; i < ptr[k + 1]; i++)
+      if (strong[i] && agg1[col[i]] && (best == 0 || val[i] > bv)) { best = agg1[col[i]]; bv = val[i]; }
+    if (best) agg[k] = best;
+  }
+  for (k = 1; k <= nv; k++) {
+    if (agg[k]) continue;
+    na++;
+    agg[k] = na;
+    for (i = ptr[k]; i < ptr[k + 1]; i++)
+      if (strong[i] && agg[col[i]] == 0) agg[col[i]] = na;
+  }
+  free(agg1);
+  return na;
+}
+
 /* coarse_method 3 (no counterpart in the reference, whose aggregation is
  * scalar): smoothed aggregation over mesh nodes with the rigid-body modes as
  * near-nullspace (Vanek, Mandel & Brezina, Computing 56 (1996) 179-196).
@@ -2457,7 +2499,8 @@ void orc_set_geometry(int nsd, int nnode, const double *coords, int n, const int
  * neighbourhoods, then joining the strongest phase-1 neighbour aggregate,
  * then new aggregates of the rest); per aggregate the translations and
  * rotations about its centroid, orthonormalised by modified Gram-Schmidt
- * applied twice, columns below 1e-8 of their norm dropped; P = P_tent -
+ * applied twice, columns below 1e-8 of their norm dropped; radius1 rounds
+ * of aggregation, the later ones over the previous aggregates; P = P_tent -
  * omega D^-1 A P_tent, omega = 4 / (3 rho(D^-1 A)) with rho from 20 power
  * steps; R = P^T and AC = R A R^T.  Subdomains: the imported parts with the
  * overlap layers. */
@@ -2524,34 +2567,47 @@ static void run_setup_rbm(state *s, const int *part, int nparts) {
       int J = bcol[i];
       strong[i] = (J != k && bval[i] > theta * sqrt(dn[k] * dn[J])) ? 1 : 0;
     }
-  /* aggregation: 1-based aggregate per node, 0 = free */
-  int *agg = NEWI(nn), *agg1 = NEWI(nn), na = 0;
-  for (k = 1; k <= nn; k++) {
-    int freeall = 1;
-    if (agg[k]) continue;
-    for (i = bptr[k]; i < bptr[k + 1]; i++)
-      if (strong[i] && agg[bcol[i]]) { freeall = 0; break; }
-    if (!freeall) continue;
-    na++;
-    agg[k] = na;
-    for (i = bptr[k]; i < bptr[k + 1]; i++)
-      if (strong[i]) agg[bcol[i]] = na;
-  }
-  for (k = 1; k <= nn; k++) agg1[k] = agg[k];
-  for (k = 1; k <= nn; k++) {
-    int best = 0;
-    double bv = 0.0;
-    if (agg1[k]) continue;
-    for (i = bptr[k]; i < bptr[k + 1]; i++)
-      if (strong[i] && agg1[bcol[i]] && (best == 0 || bval[i] > bv)) { best = agg1[bcol[i]]; bv = bval[i]; }
-    if (best) agg[k] = best;
-  }
-  for (k = 1; k <= nn; k++) {
-    if (agg[k]) continue;
-    na++;
-    agg[k] = na;
-    for (i = bptr[k]; i < bptr[k + 1]; i++)
-      if (strong[i] && agg[bcol[i]] == 0) agg[bcol[i]] = na;
+  /* aggregation: round 1 over the nodes, then radius1 - 1 rounds over the
+   * previous aggregates (edges: strong node pairs between them, weight the
+   * sum of their block norms); 1-based aggregate per node */
+  int *agg = NEWI(nn), na;
+  na = three_phase(nn, bptr, bcol, bval, strong, agg);
+  {
+    int rounds = c->radius1 > 0 ? c->radius1 : 1, round;
+    for (round = 2; round <= rounds && na > 1; round++) {
+      int *mptr = NEWI(na + 1), *mem = NEWI(nn), *f3 = NEWI(na + 1);
+      for (k = 1; k <= nn; k++) mptr[agg[k] + 1]++;
+      mptr[1] = 1;
+      for (i = 1; i <= na; i++) mptr[i + 1] += mptr[i];
+      for (i = 1; i <= na; i++) f3[i] = mptr[i];
+      for (k = 1; k <= nn; k++) mem[f3[agg[k]]++] = k;
+      int *gptr = NEWI(na + 1), *gcol = NEWI(nb), *gpos = NEWI(na), ng = 0, aa;
+      double *gval = NEWD(nb);
+      gptr[1] = 1;
+      for (aa = 1; aa <= na; aa++) {
+        int q0 = ng + 1, t, q;
+        for (t = mptr[aa]; t < mptr[aa + 1]; t++) {
+          int I = mem[t];
+          for (q = bptr[I]; q < bptr[I + 1]; q++) {
+            int bb;
+            if (!strong[q]) continue;
+            bb = agg[bcol[q]];
+            if (bb == aa) continue;
+            if (gpos[bb] == 0) { ng++; gpos[bb] = ng; gcol[ng] = bb; gval[ng] = bval[q]; }
+            else gval[gpos[bb]] = gval[gpos[bb]] + bval[q];
+          }
+        }
+        for (t = q0; t <= ng; t++) gpos[gcol[t]] = 0;
+        gptr[aa + 1] = ng + 1;
+      }
+      char *gstrong = NEWB(ng);
+      for (i = 1; i <= ng; i++) gstrong[i] = 1;
+      int *agg2 = NEWI(na);
+      int na2 = three_phase(na, gptr, gcol, gval, gstrong, agg2);
+      for (k = 1; k <= nn; k++) agg[k] = agg2[agg[k]];
+      na = na2;
+      free(mptr); free(mem); free(f3); free(gptr); free(gcol); free(gpos); free(gval); free(gstrong); free(agg2);
+    }
   }
   /* nodes per aggregate, ascending */
   int *ag_ptr = NEWI(na + 1), *ag_nodes = NEWI(nn), *pos_in = NEWI(nn);
@@ -2707,7 +2763,7 @@ static void run_setup_rbm(state *s, const int *part, int nparts) {
   free(nodes);
   for (int a = 1; a <= na; a++) free(Q[a]);
   free(Q); free(cfirst); spm_free(&Pt); spm_free(&AP);
-  free(dg); free(xv); free(yv); free(agg); free(agg1); free(ag_ptr); free(ag_nodes); free(pos_in);
+  free(dg); free(xv); free(yv); free(agg); free(ag_ptr); free(ag_nodes); free(pos_in);
   free(bptr); free(bcol); free(bval); free(posn); free(dn); free(strong);
   free(nu_ptr); free(nu); free(fillp); free(nid); free(node_of); free(comp); free(node_glob); free(ncomp);
 }
