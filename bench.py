@@ -236,6 +236,7 @@ def run_gpu(args, rank, world):
     t0 = time.perf_counter()
     sm = _solver(n, r, c, v, b, part, precision=1)
     setup_s = time.perf_counter() - t0
+    setup_phases = sm.setup_phases()
     bd = torch.tensor(b, dtype=torch.float64, device="cuda")
     xd = torch.empty_like(bd)
     for _ in range(args.warmup):
@@ -368,7 +369,7 @@ def run_gpu(args, rank, world):
         "vs_oracle": vs_oracle,
         "fp64_s": t_fp64, "fp64_iterations": stf.iterations, "mixed_vs_fp64": t_mixed / t_fp64,
         "mixed_rel_err_vs_fp64_solution": err_mixed_vs_fp64,
-        "setup_host_s": setup_s, "phases_mixed": phases,
+        "setup_host_s": setup_s, "setup_phases": setup_phases, "phases_mixed": phases,
         "e2e": {"value": t_e2e, "unit": "s", "h2d_bytes_per_step": 8 * n, "d2h_bytes_per_step": 8 * n,
                 "api": "dg_solve (host buffers, pinned)"},
         "roofline": roofline, "cpu_baseline": cpu, "clocks": clocks,

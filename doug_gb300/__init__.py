@@ -41,6 +41,7 @@ EXPORTED_SYMBOLS = [
     "dg_set_elements", "dg_get_input", "dg_grad_matrix", "dg_grad_elements",
     "dg_residual_csr_noalloc", "dg_autotune", "dg_set_systems", "dg_get_system_stats",
     "dg_solve_multi", "dg_solve_multi_device", "dg_set_node_geometry", "dg_get_coarse_coords",
+    "dg_get_setup_phases",
 ]
 
 
@@ -120,6 +121,7 @@ def load_library(path: str | None = None):
     L.dg_solve_multi_device.argtypes = [vp, C.c_int, vp, vp, P(_Stats), vp]
     L.dg_set_elements.argtypes = [vp, C.c_int, C.c_int, P(C.c_int), P(C.c_int), P(C.c_double), P(C.c_double)]
     L.dg_set_node_geometry.argtypes = [vp, C.c_int, C.c_int, P(C.c_double), P(C.c_int)]
+    L.dg_get_setup_phases.argtypes = [vp, P(C.c_double), P(C.c_double), P(C.c_int), P(C.c_double)]
     L.dg_get_coarse_coords.argtypes = [vp, P(C.c_int), P(C.c_int), P(C.c_double)]
     L.dg_get_input.argtypes = [vp, P(C.c_int), P(C.c_int), P(C.c_int), P(C.c_int), P(C.c_double),
                                P(C.c_double)]
@@ -370,6 +372,15 @@ class DougSolver:
                           st.coarse_bytes, st.t_spmv_s, st.spmv_bytes)
 
     # --- parity export ----------------------------------------------------
+    def setup_phases(self) -> dict:
+        """Seconds of the last setup: host part up to the fine aggregates,
+        restriction + Galerkin product (device time when on the GPU), total."""
+        a, c, t = C.c_double(), C.c_double(), C.c_double()
+        d = C.c_int()
+        self._check(self._L.dg_get_setup_phases(self._h, C.byref(a), C.byref(c), C.byref(d), C.byref(t)))
+        return {"aggregation_s": a.value, "coarse_s": c.value, "coarse_on_device": bool(d.value),
+                "total_s": t.value}
+
     def sizes(self) -> dict:
         v = [C.c_int() for _ in range(4)]
         tot = C.c_longlong()

@@ -20,7 +20,7 @@ CLI_GEOM = os.path.join(OUT, "doug_geom_gpu")  # the same driver with doug_geom'
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 
 HOST_SRC = ["host/setup.cpp", "host/geom.cpp", "host/mf_symbolic.cpp"]
-CUDA_SRC = ["dg_solver.cu", "dg_residual.cu"]
+CUDA_SRC = ["dg_solver.cu", "dg_residual.cu", "dg_coarse_setup.cu"]
 
 
 def _nvcc() -> str:

@@ -1128,8 +1128,10 @@ dg_status do_setup(dg_handle *h, bool reuse_host = false) {
                                   std::vector<double> &q, std::string &e) {
         return robust_restriction_gpu(c, A, sp, sn, q, e, no_device);
       };
+      int ndev_setup = 0;
+      const bool on_device = cudaGetDeviceCount(&ndev_setup) == cudaSuccess && ndev_setup > 0;
       if (!build_setup(c, h->n, h->ii, h->jj, h->vv, h->part.empty() ? nullptr : &h->part, h->nparts, h->S, err,
-                       &hook))
+                       &hook, on_device))
         return fail(h, no_device ? DG_NO_DEVICE : DG_BAD_INPUT, err);
     }
   }
@@ -1898,6 +1900,14 @@ dg_status dg_set_option(dg_handle *h, const char *name, const char *value) {
     h->ready = false;
     return DG_OK;
   }
+  if (w1 == "device_setup") {
+    int v;
+    if (!parse_i10(w2, v) || v < 0 || v > 1) return fail(h, DG_BAD_INPUT, "device_setup must be 0 or 1");
+    h->ctl.device_setup = v;
+    h->S.n = 0;  // the host setup runs again
+    h->ready = false;
+    return DG_OK;
+  }
   if (w1 == "solve_schedule") {
     int v;
     if (!parse_i10(w2, v) || v < 0 || v > 1) return fail(h, DG_BAD_INPUT, "solve_schedule must be 0 or 1");
@@ -2285,6 +2295,17 @@ dg_status dg_write_solution(dg_handle *h, const double *x) {
   if (h->ctl.solution_file.empty()) return fail(h, DG_BAD_INPUT, "no solution_file in the control words");
   if (!write_solution(resolve(h->ctl_dir, h->ctl.solution_file), h->ctl.solution_format, x, h->n, err))
     return fail(h, DG_BAD_INPUT, err);
+  return DG_OK;
+}
+
+dg_status dg_get_setup_phases(const dg_handle *h, double *aggregation_s, double *coarse_s, int *on_device,
+                              double *total_s) {
+  if (!h) return DG_BAD_INPUT;
+  if (h->S.n == 0) return DG_NOT_READY;
+  if (aggregation_s) *aggregation_s = h->S.t_aggregation;
+  if (coarse_s) *coarse_s = h->S.t_coarse;
+  if (on_device) *on_device = h->S.coarse_on_device ? 1 : 0;
+  if (total_s) *total_s = h->t_setup;
   return DG_OK;
 }
 

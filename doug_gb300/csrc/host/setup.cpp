@@ -28,10 +28,15 @@ namespace dg {
 struct PhaseTimer {
   bool on = std::getenv("DG_SETUP_TIMING") != nullptr;
   std::chrono::steady_clock::time_point t = std::chrono::steady_clock::now();
-  void lap(const char *what) {
+  double total = 0;
+  // seconds since the previous lap, also added to total
+  double lap(const char *what) {
     auto now = std::chrono::steady_clock::now();
-    if (on) fprintf(stderr, "[setup] %-28s %8.3f s\n", what, std::chrono::duration<double>(now - t).count());
+    const double dt = std::chrono::duration<double>(now - t).count();
+    if (on) fprintf(stderr, "[setup] %-28s %8.3f s\n", what, dt);
     t = now;
+    total += dt;
+    return dt;
   }
 };
 
@@ -1392,7 +1397,7 @@ bool build_setup_geom(const Controls &c_in, int n, const std::vector<int> &ii, c
 
 bool build_setup(const Controls &c_in, int n, const std::vector<int> &ii, const std::vector<int> &jj,
                  const std::vector<double> &vv, const std::vector<int> *part, int nparts,
-                 SetupResult &out, std::string &err, const RobustHook *robust) {
+                 SetupResult &out, std::string &err, const RobustHook *robust, bool on_device) {
   Controls c = c_in;
   out = SetupResult();
   out.n = n;
@@ -1438,11 +1443,19 @@ bool build_setup(const Controls &c_in, int n, const std::vector<int> &ii, const 
     return false;
   unscale_rows(SA);
   tm.lap("fine aggregation");
+  out.t_aggregation = tm.total;
   const Csr &A = SA.M;
   // IntRestBuild (CoarseMtx.F90:50-474); smoothers are capped at radius1
   if (c.smoothers > c.radius1) c.smoothers = c.radius1;
   int sm = c.smoothers;
   if (sm < 0) { err = "smoothers must be >= 0 for the smoothed-aggregation coarse space"; return false; }
+  Csr AC;
+  if (on_device && c.device_setup == 1 && c.coarse_method <= 1 && sm <= 1) {
+    // smoother, re-bucketing and the three first-touch products on the GPU
+    if (!device_restriction_galerkin(A, SA.strong, out.fine, sm, c.omega, out, AC, out.t_coarse, err)) return false;
+    out.coarse_on_device = true;
+    tm.lap("restriction + Galerkin (GPU)");
+  } else {
   Coo T;  // tentative prolongator as restriction rows
   T.nrows = out.fine.nagr; T.ncols = n;
   T.i.reserve((size_t)n); T.j.reserve((size_t)n); T.v.reserve((size_t)n);
@@ -1499,8 +1512,9 @@ bool build_setup(const Controls &c_in, int n, const std::vector<int> &ii, const 
     tm.lap("robust coarse space");
   }
   tm.lap("restriction");
-  Csr AC = galerkin(A, Rcoo, n, out, &tm);
-  tm.lap("Galerkin");
+  AC = galerkin(A, Rcoo, n, out, &tm);
+  out.t_coarse = tm.lap("Galerkin");
+  }
   // Partitionings_aggr_InitCoarse (Partitioning_aggr.F90:120-193)
   out.strong2 = c.strong2 > 0 ? c.strong2 : out.strong1 / 2.0;
   ScaledMatrix SC;

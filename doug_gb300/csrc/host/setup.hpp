@@ -46,6 +46,7 @@ struct Controls {
   int solve_schedule = 0;           // multifrontal solves: 0 one launch per level, 1 dependency-driven queue
   int solve_pdl = 1;                // 1: the level launches overlap through programmatic dependent launch
   int executable = -1;              // which reference driver: -1/0 doug_aggr, 1 doug_geom
+  int device_setup = 1;             // 1: smoothing, re-bucketing and Galerkin products on the GPU when one is visible
 };
 
 // Parse one "name value" line the way util_actionOnCtrlArg does
@@ -158,6 +159,10 @@ struct SetupResult {
   std::vector<int> R_i, R_j, AC_i, AC_j;
   std::vector<double> R_v, AC_v;
   std::vector<double> coarse_xyz;       // geometric coarse grid: coordinates of R's coarse freedoms
+  // setup phases (seconds): fine aggregation on the host (strength, aggregation),
+  // restriction + Galerkin product (device time when they ran on the GPU)
+  double t_aggregation = 0, t_coarse = 0;
+  bool coarse_on_device = false;
 };
 
 // Robust coarse space (coarse_method 2): given A and the supports S_i of the
@@ -173,11 +178,13 @@ using RobustHook = std::function<bool(const Csr &A, const std::vector<int64_t> &
 // swap and 0-based shift already applied by the caller).  part: optional
 // 1-based partition vector (length n) that replaces the coarse-aggregate
 // subdomains.  robust: the B-solve of coarse_method 2 (required for it).
+// on_device: a GPU is visible, so with device_setup 1 (and coarse_method
+// <= 1, smoothers <= 1) the restriction and Galerkin product run there.
 // Returns false with err on a DOUG abort condition.
 bool build_setup(const Controls &c_in, int n, const std::vector<int> &ii,
                  const std::vector<int> &jj, const std::vector<double> &vv,
                  const std::vector<int> *part, int nparts, SetupResult &out, std::string &err,
-                 const RobustHook *robust = nullptr);
+                 const RobustHook *robust = nullptr, bool on_device = false);
 
 // doug_geom's setup on one process (geom.F90:62-116): subdomains = all
 // unknowns (or the imported parts) with the overlap layers; levels 2 with
@@ -211,6 +218,16 @@ bool build_setup_rbm(const Controls &c, int n, const std::vector<int> &ii, const
                      const std::vector<double> &vv, const std::vector<int> *part, int nparts,
                      const std::vector<int> &unode, int nsd, const std::vector<double> &xyz, SetupResult &out,
                      std::string &err);
+
+// IntRestBuild with smoothers 0 or 1 (CoarseMtx.F90:50-233, 418-427) and
+// CoarseMtxBuild (CoarseMtx.F90:476-516) on the GPU (dg_coarse_setup.cu):
+// from the fine matrix A (row-arranged), its strong flags and the fine
+// aggregates, fills out.R, out.P, out.R_i/R_j/R_v and AC with the same bits
+// as the host path; seconds = the device time.  False with err on a CUDA
+// error or when no device is visible.
+bool device_restriction_galerkin(const Csr &A, const std::vector<char> &strong, const Aggregates &fine,
+                                 int smoothers, double omega, SetupResult &out, Csr &AC, double &seconds,
+                                 std::string &err);
 
 // Batched independent systems: system k owns the rows [sys_row[k],
 // sys_row[k+1]) and the triplets [sys_tri[k], sys_tri[k+1]) of (ii, jj, vv),

@@ -230,6 +230,15 @@ dg_status dg_grad_matrix(dg_handle *h, const double *d_lambda, const double *d_x
 dg_status dg_grad_elements(dg_handle *h, const double *d_lambda, const double *d_x, double *d_grad,
                            void *cuda_stream);
 
+/* Setup phases of the last dg_setup, in seconds (no reference counterpart;
+ * the reference prints its total setup time, src/main/aggr.F90:253-258):
+ * the host part up to the fine aggregates (arrangement, scaling, strength,
+ * aggregation), the restriction + Galerkin product (device time when they
+ * ran on the GPU: *on_device = 1), and the whole dg_setup (host setup,
+ * symbolic analysis and upload).  NULL pointers are skipped. */
+dg_status dg_get_setup_phases(const dg_handle *h, double *aggregation_s, double *coarse_s, int *on_device,
+                              double *total_s);
+
 /* Size queries and parity export (1-based ids as in the reference). */
 dg_status dg_get_sizes(const dg_handle *h, int *n, int *nagr_fine, int *nagr_coarse,
                        int *nsubdomains, long long *subdomain_total, int *R_nnz, int *AC_nnz);
