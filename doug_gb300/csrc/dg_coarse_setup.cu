@@ -449,6 +449,7 @@ void spgemm(const DCsr &A, const DCsr &B, bool b_repeats, DCsr &C, cudaStream_t 
   bound.alloc((size_t)A.nrows);
   row_bounds<<<nblocks(A.nrows), kThreads, 0, s>>>(A.nrows, A.ptr.p, A.col.p, B.ptr.p, bound.p);
   CSK(cudaGetLastError());
+  CSK(cudaStreamSynchronize(s));
   std::vector<int64_t> hb;
   bound.download(hb, (size_t)A.nrows);
   RowClasses rc;
@@ -538,7 +539,9 @@ bool device_restriction_galerkin(const Csr &A, const std::vector<char> &strong, 
   }
   cudaStream_t s = nullptr;
   try {
-    CSK(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+    // a blocking stream: the synchronous copies (legacy default stream) of
+    // the helpers above are ordered with the kernels launched on it
+    CSK(cudaStreamCreate(&s));
     cudaEvent_t e0, e1;
     CSK(cudaEventCreate(&e0));
     CSK(cudaEventCreate(&e1));
@@ -585,6 +588,7 @@ bool device_restriction_galerkin(const Csr &A, const std::vector<char> &strong, 
     spgemm(dRs, dTm, false, dAC, s);
     CSK(cudaEventRecord(e1, s));
     CSK(cudaEventSynchronize(e1));
+    CSK(cudaStreamSynchronize(s));
     float ms = 0;
     CSK(cudaEventElapsedTime(&ms, e0, e1));
     seconds = ms * 1e-3;
