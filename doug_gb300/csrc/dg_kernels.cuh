@@ -21,6 +21,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "dg_tc.cuh"
+
 namespace dg {
 
 constexpr int kRedBlocks = 1024;   // partial-sum slots of every reduction
@@ -638,6 +640,136 @@ mf_update_big_tf32(MfView v, const int2 *__restrict__ tasks, int jl, int kw, flo
         const int col = cc0 + wn + nt * 8 + tig * 2 + (q & 1);
         if (row < m && col < m && row >= col) F[(int64_t)col * m + row] -= acc[mt][nt][q];
       }
+}
+
+// The same update on the fifth-generation tensor cores: tcgen05.mma
+// kind::tf32 with the 128 x 128 FP32 accumulator in tensor memory.  The CTA
+// (8 warps) stages K in chunks of 32 columns: every thread loads rows of the
+// two column blocks of L (coalesced along the column), splits them into
+// TF32 hi and lo parts and writes them into four 16 KB shared-memory tiles
+// in the 128-byte-swizzled K-major layout (dg_tc.cuh); one thread issues the
+// 3 x 4 MMAs of the chunk (lo*hi, hi*lo, hi*hi per K step of 8) and commits
+// them to an mbarrier that all threads wait on (bounded: on a timeout the
+// CTA sets ERR_WAIT, waits once more and frees its tensor memory) before
+// the tiles are refilled.  The epilogue reads the accumulator back with
+// tcgen05.ld (warp w: lanes 32 (w % 4) .., columns 64 (w / 4) ..) and
+// subtracts it from the lower part of the front.  A diagonal tile (ti == tj)
+// stages one block and uses it as both operands.
+constexpr int kTcChunk = 32;
+constexpr size_t kTcTileBytes = 128 * kTcChunk * sizeof(float);  // 16 KB
+constexpr size_t kTcSmem = 4 * kTcTileBytes + 1024;                // + alignment to 1024 bytes
+constexpr long long kTcWaitPolls = 1LL << 24;
+
+__global__ void __launch_bounds__(256, 3)
+mf_update_big_tc(MfView v, const int2 *__restrict__ tasks, int jl, int kw, float *__restrict__ arena,
+                 int *__restrict__ status) {
+  extern __shared__ unsigned char tc_raw[];
+  unsigned char *base = reinterpret_cast<unsigned char *>((reinterpret_cast<uintptr_t>(tc_raw) + 1023) &
+                                                          ~static_cast<uintptr_t>(1023));
+  unsigned char *Ahi = base, *Alo = base + kTcTileBytes, *Bhi = base + 2 * kTcTileBytes,
+                *Blo = base + 3 * kTcTileBytes;
+  __shared__ __align__(8) uint64_t bar;
+  __shared__ uint32_t tmem_slot;
+  const int f = tasks[blockIdx.x].x;
+  const int ti = tasks[blockIdx.x].y >> 16, tj = tasks[blockIdx.x].y & 0xffff;
+  const int m = v.f_m[f], k = v.f_k[f];
+  const int K = min(kw, k - jl);
+  const int c0 = jl + K, r0 = c0 + ti * kBT, cc0 = c0 + tj * kBT;
+  const bool diag = ti == tj;
+  float *F = arena + v.f_off[f];
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  if (warp == 0) tc::tmem_alloc(&tmem_slot, 128);
+  if (tid == 0) tc::mbar_init(&bar, 1);
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  const uint32_t tmem = tmem_slot;
+  constexpr uint32_t idesc = tc::idesc_tf32(128, 128);
+  // this thread stages rows (tid & 127) and columns kk = (tid >> 7) + 2 q of
+  // every chunk: 16 values of each operand, loaded together
+  constexpr int NQ = 128 * kTcChunk / 256;
+  const int r = tid & 127, kk0 = tid >> 7;
+  const int ra = r0 + r, rb = cc0 + r;
+  float pa[NQ], pb[NQ];
+  auto fetch = [&](int kc) {
+#pragma unroll
+    for (int q = 0; q < NQ; q++) {
+      const int t = kc + kk0 + 2 * q;
+      pa[q] = (t < K && ra < m) ? F[(int64_t)(jl + t) * m + ra] : 0.f;
+      pb[q] = (!diag && t < K && rb < m) ? F[(int64_t)(jl + t) * m + rb] : 0.f;
+    }
+  };
+  auto stash = [&]() {
+#pragma unroll
+    for (int q = 0; q < NQ; q++) {
+      const uint32_t off = tc::sw128_offset(r, kk0 + 2 * q);
+      const uint32_t ah = tf32_of(pa[q]);
+      *reinterpret_cast<uint32_t *>(Ahi + off) = ah;
+      *reinterpret_cast<uint32_t *>(Alo + off) = tf32_of(pa[q] - __uint_as_float(ah));
+      if (!diag) {
+        const uint32_t bh = tf32_of(pb[q]);
+        *reinterpret_cast<uint32_t *>(Bhi + off) = bh;
+        *reinterpret_cast<uint32_t *>(Blo + off) = tf32_of(pb[q] - __uint_as_float(bh));
+      }
+    }
+  };
+  uint32_t parity = 0;
+  bool bad = false;
+  fetch(0);
+  for (int kc = 0; kc < K; kc += kTcChunk) {
+    stash();
+    tc::fence_async_smem();
+    __syncthreads();
+    if (tid == 0) {
+      tc::fence_after_sync();
+      const uint64_t dAh = tc::sw128_desc(tc::smem_u32(Ahi)), dAl = tc::sw128_desc(tc::smem_u32(Alo));
+      const uint64_t dBh = diag ? dAh : tc::sw128_desc(tc::smem_u32(Bhi));
+      const uint64_t dBl = diag ? dAl : tc::sw128_desc(tc::smem_u32(Blo));
+#pragma unroll
+      for (int ks = 0; ks < kTcChunk / 8; ks++) {  // 8 TF32 values (32 bytes) per MMA
+        const uint64_t o = (uint64_t)((ks * 32) >> 4);
+        tc::mma_tf32(tmem, dAl + o, dBh + o, idesc, (kc > 0 || ks > 0) ? 1u : 0u);
+        tc::mma_tf32(tmem, dAh + o, dBl + o, idesc, 1u);
+        tc::mma_tf32(tmem, dAh + o, dBh + o, idesc, 1u);
+      }
+      tc::mma_commit(tc::smem_u32(&bar));
+    }
+    // the next chunk's loads are in flight while the tensor cores work
+    if (kc + kTcChunk < K) fetch(kc + kTcChunk);
+    const bool ok = tc::mbar_wait(&bar, parity, kTcWaitPolls);
+    parity ^= 1;
+    if (__syncthreads_or(!ok)) { bad = true; break; }
+  }
+  if (bad) {
+    if (tid == 0) atomicOr(status, ERR_WAIT);
+    tc::mbar_wait(&bar, parity ^ 1, kTcWaitPolls);  // its MMAs in flight, once more (bounded)
+  } else {
+    tc::fence_after_sync();
+    const int lg = warp & 3, ch = warp >> 2;
+    const int row = r0 + 32 * lg + lane;
+#pragma unroll 1
+    for (int h = 0; h < 4; h++) {
+      float d[16];
+      tc::tmem_load16(tmem + ((uint32_t)(32 * lg) << 16) + (uint32_t)(ch * 64 + 16 * h), d);
+      if (row < m) {
+        const int colb = cc0 + ch * 64 + 16 * h;
+        float cur[16];
+#pragma unroll
+        for (int c = 0; c < 16; c++) {
+          const int col = colb + c;
+          cur[c] = (col < m && row >= col) ? F[(int64_t)col * m + row] : 0.f;
+        }
+#pragma unroll
+        for (int c = 0; c < 16; c++) {
+          const int col = colb + c;
+          if (col < m && row >= col) F[(int64_t)col * m + row] = cur[c] - d[c];
+        }
+      }
+    }
+  }
+  tc::fence_before_sync();
+  __syncthreads();
+  if (warp == 0) tc::tmem_free(tmem, 128);
 }
 
 // ---------------------------------------------------------------------------

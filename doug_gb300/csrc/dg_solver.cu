@@ -67,7 +67,7 @@ static double wall() {
 // fronts of at most panel_rows rows whose panel and E fit in kPanelSmem
 // bytes are factored by one CTA each; the others by the multi-CTA pipeline
 constexpr size_t kPanelSmem = 96 * 1024;
-constexpr int kSuperPanel = 128;      // columns of L per trailing update of a large front
+constexpr int kSuperPanel = 128;      // default columns of L per trailing update of a large front
 // tunable batch parameters (control words panel_rows, fwd_task_kb, lean_task_kb)
 struct MfTune {
   int panel_rows = 512;                  // fronts of at most this many rows may use mf_factor_panel
@@ -78,6 +78,8 @@ struct MfTune {
   int pdl = 0;                           // 1: level launches with programmatic dependent launch
   int tiny_rows = 64;                    // panel fronts of at most this many rows: tiny_threads per CTA
   int tiny_threads = 64;
+  int tensor_update = 1;                 // FP32 super-panel updates: 1 tcgen05 (TMEM), 0 mma.sync
+  int super_panel = kSuperPanel;         // columns of L per trailing update of a large front (multiple of 32)
 };
 
 // Launch k with programmatic stream serialisation when pdl is set: its CTAs
@@ -108,6 +110,7 @@ struct MfDevice {
   DBuf<int> f_m, f_k, f_p0, f_child_ptr, f_children, rows, relmap, lvl_fronts, gidx;
   DBuf<int> pan_fronts, diag_fronts, solve_small;
   int tiny_threads = 64;
+  int tensor_update = 1;   // FP32 super-panel updates: 1 tcgen05 + TMEM, 0 mma.sync
   // dependency-driven schedule of the solves (solve_schedule 1)
   bool queue = false;
   bool pdl = false;
@@ -227,10 +230,11 @@ struct MfDevice {
       // right-looking by super-panels of kSuperPanel columns: each 32-column
       // panel updates only the rest of its super-panel; the trailing matrix
       // receives one update with up to kSuperPanel columns of L per super-panel
-      for (int S0 = 0; S0 < kmax; S0 += kSuperPanel) {
-        for (int j0 = S0; j0 < std::min(S0 + kSuperPanel, kmax); j0 += kNB) {
+      const int SP = tune.super_panel;
+      for (int S0 = 0; S0 < kmax; S0 += SP) {
+        for (int j0 = S0; j0 < std::min(S0 + SP, kmax); j0 += kNB) {
           Step st{j0, (int)df.size(), 0, (int)pf.size(), 0, (int)es.size(), 0,
-                  (int)ut.size(), 0, (int)et.size(), 0, kNB, S0 + kSuperPanel, false};
+                  (int)ut.size(), 0, (int)et.size(), 0, kNB, S0 + SP, false};
           for (int f : large) {
             int m = B.f_m[(size_t)f], k = B.f_k[(size_t)f];
             if (j0 >= k) continue;
@@ -239,7 +243,7 @@ struct MfDevice {
             for (int r0 = c0; r0 < m; r0 += kPanelRows) pf.push_back(make_int2(f, r0));
             for (int e0 = 0; e0 < c0; e0 += EscCols<T>::N) es.push_back(make_int2(f, e0));
             const int nt = (m - c0 + kTile - 1) / kTile;
-            const int cend = std::min(S0 + kSuperPanel, k);
+            const int cend = std::min(S0 + SP, k);
             const int ntc = cend > c0 ? (cend - c0 + kTile - 1) / kTile : 0;
             for (int tj = 0; tj < ntc; tj++)
               for (int ti = tj; ti < nt; ti++) ut.push_back(make_int2(f, (ti << 16) | tj));
@@ -257,11 +261,11 @@ struct MfDevice {
         const bool bigt = sizeof(T) == 4;  // FP32: 128 x 128 tiles; FP64 keeps 64 x 64 (FP64-pipe bound)
         const int tile = bigt ? kBT : kTile;
         Step st{S0, (int)df.size(), 0, (int)pf.size(), 0, (int)es.size(), 0,
-                (int)ut.size(), 0, (int)et.size(), 0, kSuperPanel, 0, bigt};
+                (int)ut.size(), 0, (int)et.size(), 0, SP, 0, bigt};
         for (int f : large) {
           int m = B.f_m[(size_t)f], k = B.f_k[(size_t)f];
           if (S0 >= k) continue;
-          const int c1 = S0 + std::min(kSuperPanel, k - S0);
+          const int c1 = S0 + std::min(SP, k - S0);
           const int nt = (m - c1 + tile - 1) / tile;
           for (int tj = 0; tj < nt; tj++)
             for (int ti = tj; ti < nt; ti++) ut.push_back(make_int2(f, (ti << 16) | tj));
@@ -358,6 +362,10 @@ struct MfDevice {
     queue = tune.schedule == 1;
     pdl = tune.pdl == 1;
     tiny_threads = tune.tiny_threads;
+    tensor_update = tune.tensor_update;
+    if constexpr (sizeof(T) == 4)
+      if (tensor_update == 1)
+        CK(cudaFuncSetAttribute(mf_update_big_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTcSmem));
     if (queue) plan_queue(B, ss, fw, bw, fwd_smem_max, bwd_smem_max);
   }
 
@@ -404,8 +412,12 @@ struct MfDevice {
         }
         if (st.big) {
           if constexpr (sizeof(T) == 4) {  // planned for FP32 batches only
-            mf_update_big_tf32<<<st.upd_cnt, 256, 0, s>>>(view, upd_tasks.p + st.upd_off, st.j0, st.kw,
-                                                          reinterpret_cast<float *>(arena.p));
+            if (tensor_update == 1)
+              mf_update_big_tc<<<st.upd_cnt, 256, kTcSmem, s>>>(view, upd_tasks.p + st.upd_off, st.j0, st.kw,
+                                                                 reinterpret_cast<float *>(arena.p), status);
+            else
+              mf_update_big_tf32<<<st.upd_cnt, 256, 0, s>>>(view, upd_tasks.p + st.upd_off, st.j0, st.kw,
+                                                            reinterpret_cast<float *>(arena.p));
             launches++;
           }
         } else if (st.upd_cnt + st.etile_cnt) {
@@ -1007,6 +1019,8 @@ bool robust_restriction_gpu(const Controls &c, const Csr &A, const std::vector<i
     tune.fwd_task_bytes = (int64_t)c.fwd_task_kb * 1024;
     tune.lean_task_bytes = (int64_t)c.lean_task_kb * 1024;
     tune.small_min_fronts = c.thin_level_fronts;
+    tune.tensor_update = c.tensor_update;
+    tune.super_panel = c.super_panel;
     CK(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
     CK(cudaHostAlloc(&host_out, 16 * sizeof(double), cudaHostAllocMapped));
     CK(cudaHostAlloc(&host_status, sizeof(int), cudaHostAllocMapped));
@@ -1140,6 +1154,8 @@ dg_status do_setup(dg_handle *h, bool reuse_host = false) {
   tune.fwd_task_bytes = (int64_t)c.fwd_task_kb * 1024;
   tune.lean_task_bytes = (int64_t)c.lean_task_kb * 1024;
   tune.small_min_fronts = c.thin_level_fronts;
+  tune.tensor_update = c.tensor_update;
+  tune.super_panel = c.super_panel;
   tune.schedule = c.solve_schedule;
   tune.pdl = c.solve_pdl;
   MfOptions mo;
@@ -1897,6 +1913,21 @@ dg_status dg_set_option(dg_handle *h, const char *name, const char *value) {
     int v;
     if (!parse_i10(w2, v) || v < 0 || v > 1) return fail(h, DG_BAD_INPUT, "solve_pdl must be 0 or 1");
     h->ctl.solve_pdl = v;
+    h->ready = false;
+    return DG_OK;
+  }
+  if (w1 == "super_panel") {
+    int v;
+    if (!parse_i10(w2, v) || v < 32 || v % 32 != 0 || v > 1024)
+      return fail(h, DG_BAD_INPUT, "super_panel must be a multiple of 32 in [32, 1024]");
+    h->ctl.super_panel = v;
+    h->ready = false;
+    return DG_OK;
+  }
+  if (w1 == "tensor_update") {
+    int v;
+    if (!parse_i10(w2, v) || v < 0 || v > 1) return fail(h, DG_BAD_INPUT, "tensor_update must be 0 or 1");
+    h->ctl.tensor_update = v;
     h->ready = false;
     return DG_OK;
   }

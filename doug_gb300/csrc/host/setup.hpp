@@ -47,6 +47,8 @@ struct Controls {
   int solve_pdl = 1;                // 1: the level launches overlap through programmatic dependent launch
   int executable = -1;              // which reference driver: -1/0 doug_aggr, 1 doug_geom
   int device_setup = 1;             // 1: smoothing, re-bucketing and Galerkin products on the GPU when one is visible
+  int tensor_update = 1;            // FP32 super-panel trailing updates: 1 tcgen05 (TMEM accumulator), 0 mma.sync
+  int super_panel = 128;           // columns of L per trailing update of a large front (multiple of 32)
 };
 
 // Parse one "name value" line the way util_actionOnCtrlArg does
