@@ -1074,7 +1074,7 @@ __device__ __forceinline__ void fwd_big_body(const MfView &v, int2 tk, const T *
 #pragma unroll
     for (int q = 0; q < VN; q++) acc[q] = T(0);
     for (int j = wid; j < K; j += UN * NW) {
-      if (ch != ch0 || j != wid) load_batch(r0, K, j);
+      if (j != wid) load_batch(r0, K, j);  // every chunk's first batch was loaded ahead
 #pragma unroll
       for (int u = 0; u < UN; u++) {
         const int jj = j + u * NW;
@@ -1083,6 +1083,8 @@ __device__ __forceinline__ void fwd_big_body(const MfView &v, int2 tk, const T *
         for (int q = 0; q < VN; q++) acc[q] += e[u][q] * bj;
       }
     }
+    // the next chunk's first batch is in flight during this chunk's reduction
+    if (ch + 1 < ch0 + nch) load_batch((ch + 1) * RC, chunk_cols((ch + 1) * RC), wid);
 #pragma unroll
     for (int q = 0; q < VN; q++) red[wid][lane * VN + q] = acc[q];
     __syncthreads();
@@ -1148,7 +1150,7 @@ __device__ __forceinline__ void bwd_big_body(const MfView &v, int2 tk, const T *
     T s = T(0);
     if (cc < jb) {
       for (int i = c0 + rq * VN; i < m; i += UN * 32) {
-        if (cc != cs || i != c0 + rq * VN) load_batch(c, i);
+        if (i != c0 + rq * VN) load_batch(c, i);  // every column's first batch was loaded ahead
 #pragma unroll
         for (int u = 0; u < UN; u++) {
           const int ii = i + u * 32;  // w holds rows [c0, ld): rows past m are not read
@@ -1159,6 +1161,8 @@ __device__ __forceinline__ void bwd_big_body(const MfView &v, int2 tk, const T *
         }
       }
     }
+    // the next column's first batch is in flight during this column's reduction
+    if (cc + NCS < 32) load_batch(c + NCS, c0 + rq * VN);
 #pragma unroll
     for (int o = LPC / 2; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
     if (rq == 0 && cc < jb) xl[xo + c] = s;
