@@ -1195,13 +1195,15 @@ mf_bwd_big(MfView v, const int2 *__restrict__ tasks, const T *__restrict__ E, co
 // With nrhs right-hand sides, list entry g is task g / nrhs for right-hand
 // side g % nrhs and waits for the same right-hand side's producers.
 // ---------------------------------------------------------------------------
-constexpr long long kQueueWaitCycles = 1000000000LL;  // about 0.5 s at 2 GHz
+constexpr long long kQueueWaitCycles = 1000000000LL;  // default wait limit, about 0.5 s at 2 GHz
 
 struct QueueView {
   const int4 *tasks;   // {kind (0 small CTA, 1 large-front task), level, index, 0}
   const int *dep_ptr;  // dependencies of task t: dep[dep_ptr[t] .. dep_ptr[t+1])
   const int *dep;
   int ntasks;
+  long long wait_cycles;  // limit of one dependency wait (clock64 cycles)
+  int skip_publish;       // list entry whose done flag is never published (-1: none; failure tests)
 };
 
 __device__ __forceinline__ int ld_volatile(const int *p) { return *(const volatile int *)p; }
@@ -1212,7 +1214,7 @@ __device__ __forceinline__ void queue_wait(const QueueView &q, int t, int rk, in
     const int *flag = done + (int64_t)q.dep[i] * nrhs + rk;
     const long long t0 = clock64();
     while (ld_volatile(flag) == 0) {
-      if (clock64() - t0 > kQueueWaitCycles || (ld_volatile(status) & ERR_WAIT)) {
+      if (clock64() - t0 > q.wait_cycles || (ld_volatile(status) & ERR_WAIT)) {
         atomicOr(status, ERR_WAIT);  // after one timeout no CTA waits any more
         return;
       }
@@ -1223,8 +1225,9 @@ __device__ __forceinline__ void queue_wait(const QueueView &q, int t, int rk, in
 }
 
 template <typename T>
-__device__ __forceinline__ void queue_publish(int *done, int64_t idx) {
+__device__ __forceinline__ void queue_publish(const QueueView &q, int *done, int64_t idx) {
   __threadfence();
+  if (idx == q.skip_publish) return;  // a producer that never finishes (failure tests)
   atomicExch(done + idx, 1);
 }
 
@@ -1263,7 +1266,7 @@ mf_fwd_queue(MfView v, QueueView q, const int *__restrict__ small_fronts, const 
       fwd_big_body<T, 256>(v, fwd_tasks[tk.z], E, xk, yk, uk, sm, red);
     }
     __syncthreads();
-    if (threadIdx.x == 0) queue_publish<T>(done, g);
+    if (threadIdx.x == 0) queue_publish<T>(q, done, g);
   }
 }
 
@@ -1299,7 +1302,7 @@ mf_bwd_queue(MfView v, QueueView q, const int *__restrict__ small_fronts, const 
       bwd_big_body<T, 256>(v, bwd_tasks[tk.z], E, yk, xk, sm);
     }
     __syncthreads();
-    if (threadIdx.x == 0) queue_publish<T>(done, g);
+    if (threadIdx.x == 0) queue_publish<T>(q, done, g);
   }
 }
 

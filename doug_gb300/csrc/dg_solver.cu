@@ -20,6 +20,7 @@
 #include <cstdio>
 #include <cstring>
 #include <memory>
+#include <stdexcept>
 #include <string>
 #include <vector>
 
@@ -80,6 +81,8 @@ struct MfTune {
   int tiny_threads = 64;
   int tensor_update = 1;                 // FP32 super-panel updates: 1 tcgen05 (TMEM), 0 mma.sync
   int super_panel = kSuperPanel;         // columns of L per trailing update of a large front (multiple of 32)
+  long long queue_wait_cycles = kQueueWaitCycles;  // solve_schedule 1: limit of one dependency wait
+  int queue_skip_publish = -1;           // solve_schedule 1: forward entry whose done flag is withheld (tests)
 };
 
 // Launch k with programmatic stream serialisation when pdl is set: its CTAs
@@ -111,6 +114,8 @@ struct MfDevice {
   DBuf<int> pan_fronts, diag_fronts, solve_small;
   int tiny_threads = 64;
   int tensor_update = 1;   // FP32 super-panel updates: 1 tcgen05 + TMEM, 0 mma.sync
+  long long q_wait_cycles = kQueueWaitCycles;  // queue schedule: limit of one dependency wait
+  int q_skip_publish = -1;  // queue schedule: forward list entry whose done flag is withheld (tests)
   // dependency-driven schedule of the solves (solve_schedule 1)
   bool queue = false;
   bool pdl = false;
@@ -363,6 +368,8 @@ struct MfDevice {
     pdl = tune.pdl == 1;
     tiny_threads = tune.tiny_threads;
     tensor_update = tune.tensor_update;
+    q_wait_cycles = tune.queue_wait_cycles;
+    q_skip_publish = tune.queue_skip_publish;
     if constexpr (sizeof(T) == 4)
       if (tensor_update == 1)
         CK(cudaFuncSetAttribute(mf_update_big_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTcSmem));
@@ -542,10 +549,12 @@ struct MfDevice {
     if (queue && status && q_k >= nrhs) {
       CK(cudaMemsetAsync(q_counter.p, 0, 2 * sizeof(int), s));
       CK(cudaMemsetAsync(q_done.p, 0, (size_t)(qf_n + qb_n) * nrhs * sizeof(int), s));
-      mf_fwd_queue<T><<<q_grid, 256, q_smem, s>>>(view, QueueView{qf_tasks.p, qf_dep_ptr.p, qf_dep.p, qf_n},
+      mf_fwd_queue<T><<<q_grid, 256, q_smem, s>>>(view, QueueView{qf_tasks.p, qf_dep_ptr.p, qf_dep.p, qf_n,
+                                                                   q_wait_cycles, q_skip_publish},
                                                   solve_small.p, q_small_off.p, q_sb.p, fwd_tasks.p, E.p, xl_, yl_,
                                                   u_, q_counter.p, q_done.p, status, nrhs, xs, us);
-      mf_bwd_queue<T><<<q_grid, 256, q_smem, s>>>(view, QueueView{qb_tasks.p, qb_dep_ptr.p, qb_dep.p, qb_n},
+      mf_bwd_queue<T><<<q_grid, 256, q_smem, s>>>(view, QueueView{qb_tasks.p, qb_dep_ptr.p, qb_dep.p, qb_n,
+                                                                   q_wait_cycles, -1},
                                                   solve_small.p, q_small_off.p, q_sb.p, bwd_tasks.p, E.p, yl_, xl_,
                                                   q_counter.p + 1, q_done.p + (size_t)qf_n * nrhs, status, nrhs, xs);
       return 2;
@@ -1021,6 +1030,8 @@ bool robust_restriction_gpu(const Controls &c, const Csr &A, const std::vector<i
     tune.small_min_fronts = c.thin_level_fronts;
     tune.tensor_update = c.tensor_update;
     tune.super_panel = c.super_panel;
+    tune.queue_wait_cycles = c.queue_wait_cycles;
+    tune.queue_skip_publish = c.queue_skip_publish;
     CK(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
     CK(cudaHostAlloc(&host_out, 16 * sizeof(double), cudaHostAllocMapped));
     CK(cudaHostAlloc(&host_status, sizeof(int), cudaHostAllocMapped));
@@ -1156,6 +1167,8 @@ dg_status do_setup(dg_handle *h, bool reuse_host = false) {
   tune.small_min_fronts = c.thin_level_fronts;
   tune.tensor_update = c.tensor_update;
   tune.super_panel = c.super_panel;
+  tune.queue_wait_cycles = c.queue_wait_cycles;
+  tune.queue_skip_publish = c.queue_skip_publish;
   tune.schedule = c.solve_schedule;
   tune.pdl = c.solve_pdl;
   MfOptions mo;
@@ -1913,6 +1926,27 @@ dg_status dg_set_option(dg_handle *h, const char *name, const char *value) {
     int v;
     if (!parse_i10(w2, v) || v < 0 || v > 1) return fail(h, DG_BAD_INPUT, "solve_pdl must be 0 or 1");
     h->ctl.solve_pdl = v;
+    h->ready = false;
+    return DG_OK;
+  }
+  if (w1 == "queue_wait_cycles" || w1 == "queue_skip_publish") {
+    // failure tests of the dependency-driven schedule: a short wait limit and
+    // a forward task whose done flag is never published
+    long long v = 0;
+    try {
+      size_t used = 0;
+      v = std::stoll(w2, &used);
+      if (used != w2.size()) throw std::invalid_argument(w2);
+    } catch (const std::exception &) {
+      return fail(h, DG_BAD_INPUT, "bad " + w1);
+    }
+    if (w1 == "queue_wait_cycles") {
+      if (v < 1) return fail(h, DG_BAD_INPUT, "queue_wait_cycles must be positive");
+      h->ctl.queue_wait_cycles = v;
+    } else {
+      if (v < -1 || v > INT_MAX) return fail(h, DG_BAD_INPUT, "bad queue_skip_publish");
+      h->ctl.queue_skip_publish = (int)v;
+    }
     h->ready = false;
     return DG_OK;
   }

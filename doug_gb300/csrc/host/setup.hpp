@@ -49,6 +49,8 @@ struct Controls {
   int device_setup = 1;             // 1: smoothing, re-bucketing and Galerkin products on the GPU when one is visible
   int tensor_update = 1;            // FP32 super-panel trailing updates: 1 tcgen05 (TMEM accumulator), 0 mma.sync
   int super_panel = 128;           // columns of L per trailing update of a large front (multiple of 32)
+  long long queue_wait_cycles = 1000000000LL;  // solve_schedule 1: limit of one dependency wait (cycles)
+  int queue_skip_publish = -1;      // solve_schedule 1: forward entry whose done flag is withheld (failure tests)
 };
 
 // Parse one "name value" line the way util_actionOnCtrlArg does

@@ -76,3 +76,34 @@ def test_multi_rhs_3d_with_partition(schedule):
     for k in range(3):
         ro = O.run_coo(n, r, c, v, rhs=B[:, k], ctl=_ctl_text(opts), part=part)
         assert np.linalg.norm(X[:, k] - ro["x"]) <= 1e-10 * np.linalg.norm(ro["x"]), k
+
+
+@pytest.mark.gpu
+def test_queue_wait_times_out_and_the_handle_recovers():
+    # The dependency-driven schedule (solve_schedule 1) with a forward task
+    # whose done flag is never published (queue_skip_publish, a failure-test
+    # word) and a short wait limit (2e6 cycles, about 1 ms): the tasks waiting
+    # on it give up, the kernels finish, and dg_solve reports DG_CUDA_ERROR
+    # with the timeout message.  The same handle, set up again without the
+    # withheld flag, then solves correctly.
+    N = 14
+    n, r, c, v, b = P.diffusion3d_fv(N, seed=9)
+    part = P.block_partition(N, 2)
+    opts = dict(OPTS, overlap=2)
+    s = D.DougSolver(opts)
+    s.set_option("solve_schedule", 1)
+    s.set_option("queue_wait_cycles", 2000000)
+    s.set_option("queue_skip_publish", 0)
+    s.set_matrix_coo(n, r, c, v)
+    s.set_rhs(b)
+    s.set_partition(part)
+    s.setup()
+    with pytest.raises(D.DougError) as ei:
+        s.solve()
+    assert ei.value.status == D.DG_CUDA_ERROR
+    assert "timed out" in str(ei.value)
+    s.set_option("queue_skip_publish", -1)
+    s.setup()
+    x, st = s.solve(allow_not_converged=False)
+    ro = O.run_coo(n, r, c, v, rhs=b, ctl=_ctl_text(opts), part=part)
+    assert np.linalg.norm(x - ro["x"]) <= 1e-10 * np.linalg.norm(ro["x"])
