@@ -162,14 +162,14 @@ mf_factor_panel(MfView v, const int *__restrict__ fronts, const double *__restri
   T *F = arena + off;
   const int tid = threadIdx.x, nt = blockDim.x;
   // 1. zero: panel and E = [I ; 0] in shared memory, update block in the arena
-  for (int q = tid; q < m * k; q += nt) {
-    P[q] = T(0);
-    Es[q] = q / m == q % m ? T(1) : T(0);
-  }
-  for (int q = tid; q < r * r; q += nt) {
-    const int c = q / r, i = q % r;
-    if (i >= c) F[(int64_t)(k + c) * m + k + i] = T(0);
-  }
+  //    (column loops over thread-strided rows: no integer division per element)
+  for (int c = 0; c < k; c++)
+    for (int i = tid; i < m; i += nt) {
+      P[c * m + i] = T(0);
+      Es[c * m + i] = i == c ? T(1) : T(0);
+    }
+  for (int c = 0; c < r; c++)
+    for (int i = c + tid; i < r; i += nt) F[(int64_t)(k + c) * m + k + i] = T(0);
   __syncthreads();
   // 2. original entries (each target once, duplicates summed in order)
   for (int64_t e = v.f_asm[f] + tid; e < v.f_asm[f + 1]; e += nt) {
@@ -207,14 +207,13 @@ mf_factor_panel(MfView v, const int *__restrict__ fronts, const double *__restri
     for (int i = j + 1 + tid; i < m; i += nt) P[j * m + i] /= p;
     for (int c = tid; c <= j; c += nt) Es[c * m + j] /= p;
     __syncthreads();
-    const int rj = m - j - 1;
-    for (int q = tid; q < rj * (k - j - 1); q += nt) {  // panel columns c in (j, k), rows i >= c
-      const int c = j + 1 + q / rj, i = j + 1 + q % rj;
-      if (i >= c) P[c * m + i] -= P[j * m + i] * P[j * m + c];
+    for (int c = j + 1; c < k; c++) {  // panel columns c in (j, k), rows i >= c
+      const T lc = P[j * m + c];
+      for (int i = c + tid; i < m; i += nt) P[c * m + i] -= P[j * m + i] * lc;
     }
-    for (int q = tid; q < rj * (j + 1); q += nt) {  // E rows i > j, columns c <= j
-      const int c = q / rj, i = j + 1 + q % rj;
-      Es[c * m + i] -= P[j * m + i] * Es[c * m + j];
+    for (int c = 0; c <= j; c++) {  // E rows i > j, columns c <= j
+      const T ec = Es[c * m + j];
+      for (int i = j + 1 + tid; i < m; i += nt) Es[c * m + i] -= P[j * m + i] * ec;
     }
     __syncthreads();
   }
@@ -222,7 +221,8 @@ mf_factor_panel(MfView v, const int *__restrict__ fronts, const double *__restri
   {
     const int ld = round4(m);
     T *Eg = E + v.e_off[f];
-    for (int q = tid; q < m * k; q += nt) Eg[(int64_t)(q / m) * ld + q % m] = Es[q];
+    for (int c = 0; c < k; c++)
+      for (int i = tid; i < m; i += nt) Eg[(int64_t)c * ld + i] = Es[c * m + i];
   }
   // 6. update block: F[k:m, k:m] -= L21 L21^T (lower), 4x4 blocks per thread
   const int nb4 = (r + 3) / 4;
