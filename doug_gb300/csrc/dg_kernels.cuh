@@ -144,6 +144,7 @@ __device__ __forceinline__ void extend_add_column(T *__restrict__ Dst, const int
 // memory, the update block in the arena; the panel is factored and E formed
 // in shared memory, E is written out, and the update block receives
 // -L21 L21^T in 4x4 register blocks.
+constexpr int kPanBatch = 8;           // columns per batch of a thread's row updates
 constexpr int kPanThreads = 128;       // fronts of up to kPanWideRows rows
 constexpr int kPanThreadsWide = 256;   // larger fronts
 constexpr int kPanWideRows = 160;
@@ -153,7 +154,6 @@ __global__ void __launch_bounds__(kPanThreadsWide)
 mf_factor_panel(MfView v, const int *__restrict__ fronts, const double *__restrict__ vals,
                 T *__restrict__ arena, T *__restrict__ E, int *__restrict__ status) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  __shared__ T piv;
   const int f = fronts[blockIdx.x];
   const int m = v.f_m[f], k = v.f_k[f], r = m - k;
   T *P = reinterpret_cast<T *>(smem_raw);  // m x k pivot columns, ld m
@@ -194,26 +194,52 @@ mf_factor_panel(MfView v, const int *__restrict__ fronts, const double *__restri
     }
     __syncthreads();
   }
-  // 4. factor the panel and eliminate E
+  // 4. factor the panel and eliminate E.  Every thread takes the pivot from
+  //    shared memory itself (one barrier per step fewer); the updates of a
+  //    step go row by row, kPanBatch columns at a time with all their loads
+  //    issued before the stores, so a thread's read-modify-writes of
+  //    different columns overlap instead of waiting on each other.  Each
+  //    element still receives the updates of the pivots in increasing order.
   for (int j = 0; j < k; j++) {
-    if (tid == 0) {
-      T d = P[j * m + j];
-      if (!(d > T(0))) { atomicOr(status, ERR_NOT_SPD); d = T(1); }
-      piv = tsqrt<T>(d);
-      P[j * m + j] = piv;
+    T d = P[j * m + j];
+    if (!(d > T(0))) {
+      if (tid == 0) atomicOr(status, ERR_NOT_SPD);
+      d = T(1);
     }
-    __syncthreads();
-    const T p = piv;
+    const T p = tsqrt<T>(d);
     for (int i = j + 1 + tid; i < m; i += nt) P[j * m + i] /= p;
     for (int c = tid; c <= j; c += nt) Es[c * m + j] /= p;
     __syncthreads();
-    for (int c = j + 1; c < k; c++) {  // panel columns c in (j, k), rows i >= c
-      const T lc = P[j * m + c];
-      for (int i = c + tid; i < m; i += nt) P[c * m + i] -= P[j * m + i] * lc;
-    }
-    for (int c = 0; c <= j; c++) {  // E rows i > j, columns c <= j
-      const T ec = Es[c * m + j];
-      for (int i = j + 1 + tid; i < m; i += nt) Es[c * m + i] -= P[j * m + i] * ec;
+    if (tid == 0) P[j * m + j] = p;  // read by no thread before the next step
+    for (int i = j + 1 + tid; i < m; i += nt) {
+      const T lij = P[j * m + i];
+      // panel columns c in (j, min(k, i + 1))
+      const int c1 = min(k, i + 1);
+      for (int c0 = j + 1; c0 < c1; c0 += kPanBatch) {
+        T lc[kPanBatch], pv[kPanBatch];
+#pragma unroll
+        for (int u = 0; u < kPanBatch; u++) {
+          const int c = c0 + u;
+          lc[u] = c < c1 ? P[j * m + c] : T(0);
+          pv[u] = c < c1 ? P[c * m + i] : T(0);
+        }
+#pragma unroll
+        for (int u = 0; u < kPanBatch; u++)
+          if (c0 + u < c1) P[(c0 + u) * m + i] = pv[u] - lij * lc[u];
+      }
+      // E columns c <= j
+      for (int c0 = 0; c0 <= j; c0 += kPanBatch) {
+        T ec[kPanBatch], ev[kPanBatch];
+#pragma unroll
+        for (int u = 0; u < kPanBatch; u++) {
+          const int c = c0 + u;
+          ec[u] = c <= j ? Es[c * m + j] : T(0);
+          ev[u] = c <= j ? Es[c * m + i] : T(0);
+        }
+#pragma unroll
+        for (int u = 0; u < kPanBatch; u++)
+          if (c0 + u <= j) Es[(c0 + u) * m + i] = ev[u] - lij * ec[u];
+      }
     }
     __syncthreads();
   }
@@ -441,9 +467,12 @@ mf_panel(MfView v, const int2 *__restrict__ tasks, int npanel, const int2 *__res
 // only columns below cend = min(cend_base, k) when cend_base > 0 (the update
 // inside a 128-column super-panel), all columns otherwise (the trailing update
 // of the whole super-panel, K up to 128, staged 32 columns at a time).  For
-// blockIdx.x >= nupd (single-panel steps only) the tile belongs to the E update
+// blockIdx.x >= nupd the tile belongs to the E update
 // E[c0:m, 0:c0] -= L[c0:m, J] E_J (task = {front, (ti << 16) | tc}, columns
-// from 0); the columns of block J are assigned, the earlier ones accumulated.
+// from 0; J = [jl, c0)); the columns of block J are assigned, the earlier
+// ones accumulated.  A panel step (cend_base > 0) updates the E rows below
+// cend only, the rest of its super-panel; the super-panel's own launch
+// (cend_base 0, J = the super-panel) updates the rows below it.
 template <typename T>
 __global__ void __launch_bounds__(kMfThreads)
 mf_update(MfView v, const int2 *__restrict__ tasks, int nupd, const int2 *__restrict__ etasks, int jl, int kw,
@@ -502,6 +531,7 @@ mf_update(MfView v, const int2 *__restrict__ tasks, int nupd, const int2 *__rest
   }
   const int j0 = jl;
   if (etile) {
+    const int rend = cend_base > 0 ? cend : m;
 #pragma unroll
     for (int b = 0; b < 4; b++) {
       const int col = cc0 + ty + 16 * b;
@@ -509,7 +539,7 @@ mf_update(MfView v, const int2 *__restrict__ tasks, int nupd, const int2 *__rest
 #pragma unroll
       for (int a = 0; a < 4; a++) {
         const int row = r0 + tx + 16 * a;
-        if (row >= m) continue;
+        if (row >= rend) continue;
         T *dst = Eg + (int64_t)col * ld + row;
         *dst = col >= j0 ? -acc[a][b] : *dst - acc[a][b];
       }

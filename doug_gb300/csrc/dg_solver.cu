@@ -77,6 +77,7 @@ struct MfTune {
   int small_min_fronts = 304;            // levels with fewer small fronts solve them CTA-per-task
   int schedule = 0;                      // solves: 0 one launch per level, 1 dependency-driven queue
   int pdl = 0;                           // 1: level launches with programmatic dependent launch
+  int factor_overlap = 1;                // 1: a level's one-CTA fronts beside its large-front steps
   int tiny_rows = 64;                    // panel fronts of at most this many rows: tiny_threads per CTA
   int tiny_threads = 64;
   int tensor_update = 1;                 // FP32 super-panel updates: 1 tcgen05 (TMEM), 0 mma.sync
@@ -119,6 +120,20 @@ struct MfDevice {
   // dependency-driven schedule of the solves (solve_schedule 1)
   bool queue = false;
   bool pdl = false;
+  // factor_overlap: a side stream for the one-CTA fronts of a level while
+  // the calling stream runs the level's large-front steps (the fronts of a
+  // level have disjoint arena regions and their children are finished)
+  bool overlap = false;
+  cudaStream_t aux = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+  MfDevice() = default;
+  MfDevice(const MfDevice &) = delete;
+  MfDevice &operator=(const MfDevice &) = delete;
+  ~MfDevice() {
+    if (aux) cudaStreamDestroy(aux);
+    if (ev_fork) cudaEventDestroy(ev_fork);
+    if (ev_join) cudaEventDestroy(ev_join);
+  }
   DBuf<int4> qf_tasks, qb_tasks;
   DBuf<int> qf_dep_ptr, qf_dep, qb_dep_ptr, qb_dep, q_small_off, q_counter, q_done;
   DBuf<SmallBuckets> q_sb;
@@ -252,8 +267,11 @@ struct MfDevice {
             const int ntc = cend > c0 ? (cend - c0 + kTile - 1) / kTile : 0;
             for (int tj = 0; tj < ntc; tj++)
               for (int ti = tj; ti < nt; ti++) ut.push_back(make_int2(f, (ti << 16) | tj));
+            // E rows of the rest of the super-panel only (rows below cend
+            // receive the super-panel's update at once, planned below)
             const int nte = (c0 + kTile - 1) / kTile;
-            for (int ti = 0; ti < nt; ti++)
+            const int ntr = cend > c0 ? (cend - c0 + kTile - 1) / kTile : 0;
+            for (int ti = 0; ti < ntr; ti++)
               for (int tc = 0; tc < nte; tc++) et.push_back(make_int2(f, (ti << 16) | tc));
           }
           st.diag_cnt = (int)df.size() - st.diag_off;
@@ -274,9 +292,15 @@ struct MfDevice {
           const int nt = (m - c1 + tile - 1) / tile;
           for (int tj = 0; tj < nt; tj++)
             for (int ti = tj; ti < nt; ti++) ut.push_back(make_int2(f, (ti << 16) | tj));
+          // E rows below the super-panel, all its columns at once:
+          // E[c1:m, 0:c1] -= L[c1:m, S0:c1] E[S0:c1, 0:c1] (64 x 64 tiles)
+          const int nte = (c1 + kTile - 1) / kTile, ntr = (m - c1 + kTile - 1) / kTile;
+          for (int ti = 0; ti < ntr; ti++)
+            for (int tc = 0; tc < nte; tc++) et.push_back(make_int2(f, (ti << 16) | tc));
         }
         st.upd_cnt = (int)ut.size() - st.upd_off;
-        if (st.upd_cnt) L.steps.push_back(st);
+        st.etile_cnt = (int)et.size() - st.etile_off;
+        if (st.upd_cnt || st.etile_cnt) L.steps.push_back(st);
       }
     }
     pan_fronts.upload(pn);
@@ -366,6 +390,14 @@ struct MfDevice {
     set_solve_attrs<kELeanThreads>(optin, fwd_smem_max, bwd_smem_max);
     queue = tune.schedule == 1;
     pdl = tune.pdl == 1;
+    overlap = tune.factor_overlap == 1;
+    if (overlap && !aux) {
+      int prio_lo = 0, prio_hi = 0;
+      CK(cudaDeviceGetStreamPriorityRange(&prio_lo, &prio_hi));
+      CK(cudaStreamCreateWithPriority(&aux, cudaStreamNonBlocking, prio_hi));
+      CK(cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming));
+      CK(cudaEventCreateWithFlags(&ev_join, cudaEventDisableTiming));
+    }
     tiny_threads = tune.tiny_threads;
     tensor_update = tune.tensor_update;
     q_wait_cycles = tune.queue_wait_cycles;
@@ -393,16 +425,26 @@ struct MfDevice {
     int launches = 0;
     for (int l = 0; l < nlevels; l++) {
       const Level &L = levels[(size_t)l];
+      // the one-CTA fronts on the side stream when the level also has large
+      // fronts, joined before the next level
+      const bool fork = overlap && (L.tiny_cnt || L.pan_cnt) && (L.asm_cnt || !L.steps.empty());
+      cudaStream_t sp = s;
+      if (fork) {
+        CK(cudaEventRecord(ev_fork, s));
+        CK(cudaStreamWaitEvent(aux, ev_fork, 0));
+        sp = aux;
+      }
       if (L.tiny_cnt) {  // small fronts: narrow CTAs, more of them per SM
-        mf_factor_panel<T><<<L.tiny_cnt, tiny_threads, L.tiny_smem, s>>>(view, pan_fronts.p + L.tiny_off, vals,
-                                                                         arena.p, E.p, status);
+        mf_factor_panel<T><<<L.tiny_cnt, tiny_threads, L.tiny_smem, sp>>>(view, pan_fronts.p + L.tiny_off, vals,
+                                                                          arena.p, E.p, status);
         launches++;
       }
       if (L.pan_cnt) {
-        mf_factor_panel<T><<<L.pan_cnt, L.pan_maxm > kPanWideRows ? kPanThreadsWide : kPanThreads, L.pan_smem, s>>>(view, pan_fronts.p + L.pan_off, vals,
-                                                                      arena.p, E.p, status);
+        mf_factor_panel<T><<<L.pan_cnt, L.pan_maxm > kPanWideRows ? kPanThreadsWide : kPanThreads, L.pan_smem, sp>>>(
+            view, pan_fronts.p + L.pan_off, vals, arena.p, E.p, status);
         launches++;
       }
+      if (fork) CK(cudaEventRecord(ev_join, aux));
       if (L.asm_cnt) {
         mf_assemble_large<T><<<L.asm_cnt, kMfThreads, 0, s>>>(view, asm_tasks.p + L.asm_off, vals, arena.p);
         launches++;
@@ -419,13 +461,21 @@ struct MfDevice {
         }
         if (st.big) {
           if constexpr (sizeof(T) == 4) {  // planned for FP32 batches only
-            if (tensor_update == 1)
-              mf_update_big_tc<<<st.upd_cnt, 256, kTcSmem, s>>>(view, upd_tasks.p + st.upd_off, st.j0, st.kw,
-                                                                 reinterpret_cast<float *>(arena.p), status);
-            else
-              mf_update_big_tf32<<<st.upd_cnt, 256, 0, s>>>(view, upd_tasks.p + st.upd_off, st.j0, st.kw,
-                                                            reinterpret_cast<float *>(arena.p));
-            launches++;
+            if (st.upd_cnt) {
+              if (tensor_update == 1)
+                mf_update_big_tc<<<st.upd_cnt, 256, kTcSmem, s>>>(view, upd_tasks.p + st.upd_off, st.j0, st.kw,
+                                                                   reinterpret_cast<float *>(arena.p), status);
+              else
+                mf_update_big_tf32<<<st.upd_cnt, 256, 0, s>>>(view, upd_tasks.p + st.upd_off, st.j0, st.kw,
+                                                              reinterpret_cast<float *>(arena.p));
+              launches++;
+            }
+            if (st.etile_cnt) {  // the super-panel's E update
+              mf_update<T><<<st.etile_cnt, kMfThreads, 0, s>>>(view, upd_tasks.p + st.upd_off, 0,
+                                                               etile_tasks.p + st.etile_off, st.j0, st.kw, 0,
+                                                               arena.p, E.p);
+              launches++;
+            }
           }
         } else if (st.upd_cnt + st.etile_cnt) {
           mf_update<T><<<st.upd_cnt + st.etile_cnt, kMfThreads, 0, s>>>(
@@ -434,6 +484,7 @@ struct MfDevice {
           launches++;
         }
       }
+      if (fork) CK(cudaStreamWaitEvent(s, ev_join, 0));
     }
     return launches;
   }
@@ -1171,6 +1222,7 @@ dg_status do_setup(dg_handle *h, bool reuse_host = false) {
   tune.queue_skip_publish = c.queue_skip_publish;
   tune.schedule = c.solve_schedule;
   tune.pdl = c.solve_pdl;
+  tune.factor_overlap = c.factor_overlap;
   MfOptions mo;
   mo.leaf = c.nd_leaf;
   const bool timing = std::getenv("DG_SETUP_TIMING") != nullptr;
@@ -1926,6 +1978,13 @@ dg_status dg_set_option(dg_handle *h, const char *name, const char *value) {
     int v;
     if (!parse_i10(w2, v) || v < 0 || v > 1) return fail(h, DG_BAD_INPUT, "solve_pdl must be 0 or 1");
     h->ctl.solve_pdl = v;
+    h->ready = false;
+    return DG_OK;
+  }
+  if (w1 == "factor_overlap") {
+    int v;
+    if (!parse_i10(w2, v) || v < 0 || v > 1) return fail(h, DG_BAD_INPUT, "factor_overlap must be 0 or 1");
+    h->ctl.factor_overlap = v;
     h->ready = false;
     return DG_OK;
   }

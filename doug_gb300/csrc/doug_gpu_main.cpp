@@ -34,7 +34,7 @@ const char *kReferenceWords[] = {
     "submeth", "gmres_max_it", "gmrestarts"};
 const char *kExtensionWords[] = {"precision", "replace_every", "omega", "nd_leaf", "profile", "reuse_factors",
                                  "elemental_matvec", "panel_rows", "fwd_task_kb", "lean_task_kb",
-                                 "thin_level_fronts", "solve_schedule", "solve_pdl", "executable"};
+                                 "thin_level_fronts", "solve_schedule", "solve_pdl", "factor_overlap", "executable"};
 #ifdef DG_DRIVER_GEOM
 const char *kName = "doug_geom_gpu";
 #else

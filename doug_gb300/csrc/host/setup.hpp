@@ -45,6 +45,7 @@ struct Controls {
   int thin_level_fronts = 304;      // levels with fewer small fronts solve them one CTA per task
   int solve_schedule = 0;           // multifrontal solves: 0 one launch per level, 1 dependency-driven queue
   int solve_pdl = 1;                // 1: the level launches overlap through programmatic dependent launch
+  int factor_overlap = 1;           // 1: a level's one-CTA fronts factored on a side stream beside its large fronts
   int executable = -1;              // which reference driver: -1/0 doug_aggr, 1 doug_geom
   int device_setup = 1;             // 1: smoothing, re-bucketing and Galerkin products on the GPU when one is visible
   int tensor_update = 1;            // FP32 super-panel trailing updates: 1 tcgen05 (TMEM accumulator), 0 mma.sync

@@ -24,10 +24,10 @@ def _ctl_text(d):
 
 
 @pytest.mark.parametrize("word", ["panel_rows", "fwd_task_kb", "lean_task_kb", "thin_level_fronts", "solve_schedule",
-                                  "solve_pdl"])
+                                  "solve_pdl", "factor_overlap"])
 def test_tuning_words_reject_bad_values(word):
     s = D.DougSolver({})
-    binary = word in ("solve_schedule", "solve_pdl")
+    binary = word in ("solve_schedule", "solve_pdl", "factor_overlap")
     s.set_option(word, 1 if binary else 64)
     for bad in ((-3, "x") if word == "thin_level_fronts" else (2, -1, "x") if binary else (0, -3, "x")):
         with pytest.raises(D.DougError):
@@ -47,7 +47,7 @@ def diffusion24():
                                    dict(fwd_task_kb=1024, lean_task_kb=4096), dict(nd_leaf=8),
                                    dict(thin_level_fronts=0), dict(thin_level_fronts=100000),
                                    dict(solve_schedule=1), dict(solve_schedule=1, thin_level_fronts=0),
-                                   dict(solve_pdl=0)])
+                                   dict(solve_pdl=0), dict(factor_overlap=0)])
 @pytest.mark.parametrize("precision", [0, 1])
 def test_batch_parameters_keep_the_solution(diffusion24, words, precision):
     n, r, c, v, b, ro = diffusion24
@@ -83,16 +83,21 @@ def test_autotune_picks_a_grid_point_and_solves(diffusion24):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("word", ["solve_pdl", "factor_overlap"])
 @pytest.mark.parametrize("precision", [0, 1])
-def test_pdl_launches_give_identical_results(diffusion24, precision):
-    """The programmatic dependent launch of the level solves changes when CTAs
-    start, not what they compute: the solutions are bit-identical."""
+def test_launch_overlap_gives_identical_results(diffusion24, precision, word):
+    """The programmatic dependent launch of the level solves (solve_pdl) and
+    the side stream of the one-CTA fronts in the factorisation
+    (factor_overlap) change when CTAs start, not what they compute: the
+    solutions are bit-identical.  panel_rows 48 gives the factorisation
+    levels with both one-CTA and large fronts."""
     n, r, c, v, b, ro = diffusion24
     xs = []
-    for pdl in (0, 1):
+    for on in (0, 1):
         s = D.DougSolver(OPTS)
         s.set_option("precision", precision)
-        s.set_option("solve_pdl", pdl)
+        s.set_option("panel_rows", 48)
+        s.set_option(word, on)
         s.set_matrix_coo(n, r, c, v)
         s.set_rhs(b)
         s.setup()
