@@ -343,52 +343,62 @@ mf_assemble_large(MfView v, const int2 *__restrict__ tasks, const double *__rest
 }
 
 // Panel at column j0 of a large front in two launches: mf_diag factors the
-// jb x jb diagonal block of every listed front (one CTA each, in shared
-// memory); mf_panel then solves L21 = A21 L11^-T for row chunks of kPanelRows
-// rows (task = {front, first row of the chunk}), many CTAs per front.
+// jb x jb diagonal block of every listed front (one warp each, in
+// registers); mf_panel then solves L21 = A21 L11^-T for row chunks of
+// kPanelRows rows (task = {front, first row of the chunk}), many CTAs per
+// front, or forms E rows of the panel (escale tasks, below).
 constexpr int kPanelRows = 256;
 
+// Right-looking Cholesky of the lower triangle of D[0..jb)[0..jb) by one
+// warp: lane i keeps row i in registers, column j of L is broadcast by
+// shuffles.  Per element the same operations in the same order as the
+// column-by-column algorithm (scale by the pivot's square root, then
+// D[i][c] -= D[i][j] D[c][j] for j = 0, 1, ...).
 template <typename T>
-__device__ __forceinline__ void chol_small_smem(T (*D)[kNB + 1], int jb, int *status) {
-  // right-looking Cholesky of D[0..jb)[0..jb) (lower, D[row][col]) by one CTA
-  const int tid = threadIdx.x;
-  for (int j = 0; j < jb; j++) {
-    if (tid == 0) {
-      T d = D[j][j];
-      if (!(d > T(0))) { atomicOr(status, ERR_NOT_SPD); d = T(1); }
-      D[j][j] = tsqrt<T>(d);
+__device__ __forceinline__ void chol_warp(T (*D)[kNB + 1], int jb, int *status) {
+  const int lane = threadIdx.x & 31;
+  T a[kNB];
+#pragma unroll
+  for (int c = 0; c < kNB; c++) a[c] = D[lane][c];
+#pragma unroll
+  for (int j = 0; j < kNB; j++) {
+    if (j < jb) {
+      T d = __shfl_sync(0xffffffffu, a[j], j);
+      if (!(d > T(0))) {
+        if (lane == 0) atomicOr(status, ERR_NOT_SPD);
+        d = T(1);
+      }
+      const T p = tsqrt<T>(d);
+      if (lane == j) a[j] = p;
+      else if (lane > j) a[j] /= p;
+      const T lij = a[j];
+#pragma unroll
+      for (int c = j + 1; c < kNB; c++) {
+        const T lcj = __shfl_sync(0xffffffffu, lij, c);
+        if (c < jb && lane >= c) a[c] -= lij * lcj;
+      }
     }
-    __syncthreads();
-    const T p = D[j][j];
-    for (int i = j + 1 + tid; i < jb; i += blockDim.x) D[i][j] /= p;
-    __syncthreads();
-    for (int q = tid; q < (jb - j - 1) * (jb - j - 1); q += blockDim.x) {
-      int i = j + 1 + q / (jb - j - 1), c = j + 1 + q % (jb - j - 1);
-      if (i >= c) D[i][c] -= D[i][j] * D[c][j];
-    }
-    __syncthreads();
   }
+#pragma unroll
+  for (int c = 0; c < kNB; c++) D[lane][c] = a[c];
 }
 
 template <typename T>
-__global__ void __launch_bounds__(kMfThreads)
+__global__ void __launch_bounds__(32)
 mf_diag(MfView v, const int *__restrict__ fronts, int j0, T *__restrict__ arena, int *__restrict__ status) {
   __shared__ T D[kNB][kNB + 1];
   const int f = fronts[blockIdx.x];
   const int m = v.f_m[f], k = v.f_k[f];
   const int jb = min(kNB, k - j0);
   T *F = arena + v.f_off[f];
-  const int tid = threadIdx.x;
-  for (int q = tid; q < jb * jb; q += kMfThreads) {
-    int c = q / jb, i = q % jb;  // column-major walk: coalesced over i
-    D[i][c] = i >= c ? F[(int64_t)(j0 + c) * m + j0 + i] : T(0);
-  }
-  __syncthreads();
-  chol_small_smem<T>(D, jb, status);
-  for (int q = tid; q < jb * jb; q += kMfThreads) {
-    int c = q / jb, i = q % jb;
-    if (i >= c) F[(int64_t)(j0 + c) * m + j0 + i] = D[i][c];
-  }
+  const int lane = threadIdx.x;
+  for (int c = 0; c < kNB; c++)  // lower part of the block, zeros elsewhere (coalesced over rows)
+    D[lane][c] = (lane >= c && lane < jb) ? F[(int64_t)(j0 + c) * m + j0 + lane] : T(0);
+  __syncwarp();
+  chol_warp<T>(D, jb, status);
+  __syncwarp();
+  for (int c = 0; c < jb; c++)
+    if (lane >= c && lane < jb) F[(int64_t)(j0 + c) * m + j0 + lane] = D[lane][c];
 }
 
 // E rows of the panel (escale task = {front, first column}): E_J <- L_JJ^-1 E_J
@@ -442,7 +452,11 @@ mf_panel(MfView v, const int2 *__restrict__ tasks, int npanel, const int2 *__res
   __syncthreads();
   const int r0 = task.y;
   const int rb = max(r0, j0 + jb), re = min(r0 + kPanelRows, m);
-  for (int i = rb + tid; i < re; i += kMfThreads) {
+  // one row per thread (no row loop: the diagonal block is read inside the
+  // solve instead of being held in registers across rows)
+  static_assert(kPanelRows == kMfThreads, "a row chunk has one row per thread");
+  const int i = rb + tid;
+  if (i < re) {
     T x[kNB];
 #pragma unroll
     for (int t = 0; t < kNB; t++) x[t] = t < jb ? F[(int64_t)(j0 + t) * m + i] : T(0);

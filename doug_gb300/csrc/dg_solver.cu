@@ -391,13 +391,6 @@ struct MfDevice {
     queue = tune.schedule == 1;
     pdl = tune.pdl == 1;
     overlap = tune.factor_overlap == 1;
-    if (overlap && !aux) {
-      int prio_lo = 0, prio_hi = 0;
-      CK(cudaDeviceGetStreamPriorityRange(&prio_lo, &prio_hi));
-      CK(cudaStreamCreateWithPriority(&aux, cudaStreamNonBlocking, prio_hi));
-      CK(cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming));
-      CK(cudaEventCreateWithFlags(&ev_join, cudaEventDisableTiming));
-    }
     tiny_threads = tune.tiny_threads;
     tensor_update = tune.tensor_update;
     q_wait_cycles = tune.queue_wait_cycles;
@@ -423,6 +416,13 @@ struct MfDevice {
 
   int factor(const double *vals, int *status, cudaStream_t s) {
     int launches = 0;
+    if (overlap && !aux) {  // the side stream takes the calling stream's priority
+      int prio = 0;
+      CK(cudaStreamGetPriority(s, &prio));
+      CK(cudaStreamCreateWithPriority(&aux, cudaStreamNonBlocking, prio));
+      CK(cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming));
+      CK(cudaEventCreateWithFlags(&ev_join, cudaEventDisableTiming));
+    }
     for (int l = 0; l < nlevels; l++) {
       const Level &L = levels[(size_t)l];
       // the one-CTA fronts on the side stream when the level also has large
@@ -451,7 +451,7 @@ struct MfDevice {
       }
       for (const Step &st : L.steps) {
         if (st.diag_cnt) {
-          mf_diag<T><<<st.diag_cnt, kMfThreads, 0, s>>>(view, diag_fronts.p + st.diag_off, st.j0, arena.p, status);
+          mf_diag<T><<<st.diag_cnt, 32, 0, s>>>(view, diag_fronts.p + st.diag_off, st.j0, arena.p, status);
           launches++;
         }
         if (st.panel_cnt + st.esc_cnt) {
@@ -861,7 +861,8 @@ struct dg_handle {
   int *d_host_status = nullptr;
   cudaEvent_t ev[10]{};
   cudaStream_t s2 = nullptr;        // coarse-level stream (runs beside the subdomain solves)
-  cudaStream_t sf = nullptr;        // high-priority stream of the subdomain factorisation
+  cudaStream_t s2f = nullptr;       // high-priority stream of the coarse factorisation
+  cudaStream_t sf = nullptr;        // low-priority stream of the subdomain factorisation
   cudaEvent_t fine_ev = nullptr;
   cudaStream_t s3 = nullptr;        // capture stream of the iteration graph
   cudaGraphExec_t iter_exec = nullptr;
@@ -870,6 +871,7 @@ struct dg_handle {
   ~dg_handle() {
     if (iter_exec) cudaGraphExecDestroy(iter_exec);
     if (s2) cudaStreamDestroy(s2);
+    if (s2f) cudaStreamDestroy(s2f);
     if (sf) cudaStreamDestroy(sf);
     if (fine_ev) cudaEventDestroy(fine_ev);
     if (s3) cudaStreamDestroy(s3);
@@ -1339,12 +1341,16 @@ dg_status do_setup(dg_handle *h, bool reuse_host = false) {
       CK(cudaHostGetDevicePointer(&h->d_host_out, h->host_out, 0));
       CK(cudaHostGetDevicePointer(&h->d_host_status, h->host_status, 0));
       for (auto &e : h->ev) CK(cudaEventCreate(&e));
-      // the subdomain factorisation is the longer of the two factorisation
-      // chains: its stream gets the highest priority, the coarse stream the lowest
+      // factorisations: the coarse chain (a few fronts per level, one long
+      // chain of panel steps at the top) gets the highest priority, so that
+      // its CTAs start as soon as an SM has room; the subdomain chain, wide
+      // enough to fill the rest, the lowest.  In the iterations the coarse
+      // solve's stream has the lowest priority beside the subdomain solves.
       int prio_lo = 0, prio_hi = 0;
       CK(cudaDeviceGetStreamPriorityRange(&prio_lo, &prio_hi));
       CK(cudaStreamCreateWithPriority(&h->s2, cudaStreamNonBlocking, prio_lo));
-      CK(cudaStreamCreateWithPriority(&h->sf, cudaStreamNonBlocking, prio_hi));
+      CK(cudaStreamCreateWithPriority(&h->s2f, cudaStreamNonBlocking, prio_hi));
+      CK(cudaStreamCreateWithPriority(&h->sf, cudaStreamNonBlocking, prio_lo));
       CK(cudaEventCreateWithFlags(&h->fine_ev, cudaEventDisableTiming));
       CK(cudaStreamCreateWithFlags(&h->s3, cudaStreamNonBlocking));
       CK(cudaEventCreateWithFlags(&h->fork_ev, cudaEventDisableTiming));
@@ -1443,15 +1449,15 @@ SolvePlan plan_of(const dg_handle *h, const Controls &c) {
 
 // numeric factorisations (the reference factorises lazily in the first
 // preconditioner call, subsolvers.F90:78-101, pcg.F90:166-178): the coarse
-// factorisation on the low-priority stream beside the subdomain
-// factorisations on the high-priority one.  Returns the number of kernels.
+// factorisation on the high-priority stream beside the subdomain
+// factorisations on the low-priority one.  Returns the number of kernels.
 int factor_all(dg_handle *h, const SolvePlan &pl, cudaStream_t s) {
   int launches = 0;
   if (pl.coarse) {
     CK(cudaEventRecord(h->fork_ev, s));
-    CK(cudaStreamWaitEvent(h->s2, h->fork_ev, 0));
-    launches += h->co64->factor(h->ACv.p, h->status.p, h->s2);
-    CK(cudaEventRecord(h->join_ev, h->s2));
+    CK(cudaStreamWaitEvent(h->s2f, h->fork_ev, 0));
+    launches += h->co64->factor(h->ACv.p, h->status.p, h->s2f);
+    CK(cudaEventRecord(h->join_ev, h->s2f));
   }
   if (pl.fine && !pl.sgs) {
     CK(cudaEventRecord(h->fork_ev, s));
