@@ -112,22 +112,24 @@ constexpr int kTile = 64;    // trailing-update tile (64 x 64 per CTA step, 4x4 
 // for the parent's extend-add.
 
 // Extend-add of column b of a child's update block into column pb of the
-// parent (Dst = the parent's column base): rows a >= b, by the lanes of one
-// warp.  kEaBatch rows per lane are loaded (child values, target rows, old
-// target values) before any is stored, so a warp keeps many independent
-// loads in flight; the targets of one child column are distinct.
+// parent (Dst = the parent's column base; row r of the column at
+// Dst[r * stride]): rows a >= b, by the lanes of one warp.  kEaBatch rows
+// per lane are loaded (child values, target rows, old target values) before
+// any is stored, so a warp keeps many independent loads in flight; the
+// targets of one child column are distinct.
 constexpr int kEaBatch = 4;
 
 template <typename T>
 __device__ __forceinline__ void extend_add_column(T *__restrict__ Dst, const int *__restrict__ rel,
-                                                  const T *__restrict__ Ucol, int b, int rc, int lane) {
+                                                  const T *__restrict__ Ucol, int b, int rc, int lane,
+                                                  int stride = 1) {
   for (int a0 = b + lane; a0 < rc; a0 += 32 * kEaBatch) {
     int row[kEaBatch];
     T val[kEaBatch], old[kEaBatch];
 #pragma unroll
     for (int u = 0; u < kEaBatch; u++) {
       const int a = a0 + 32 * u;
-      row[u] = a < rc ? rel[a] : 0;
+      row[u] = a < rc ? rel[a] * stride : 0;
       val[u] = a < rc ? Ucol[a] : T(0);
     }
 #pragma unroll
@@ -139,12 +141,46 @@ __device__ __forceinline__ void extend_add_column(T *__restrict__ Dst, const int
   }
 }
 
+// 16-byte vectors of T in shared memory
+template <typename T> struct SVec;
+template <> struct SVec<float> {
+  static constexpr int N = 4;
+  using V = float4;
+  __device__ static __forceinline__ float get(const V &v, int q) { return q == 0 ? v.x : q == 1 ? v.y : q == 2 ? v.z : v.w; }
+  __device__ static __forceinline__ void set(V &v, int q, float x) {
+    if (q == 0) v.x = x; else if (q == 1) v.y = x; else if (q == 2) v.z = x; else v.w = x;
+  }
+};
+template <> struct SVec<double> {
+  static constexpr int N = 2;
+  using V = double2;
+  __device__ static __forceinline__ double get(const V &v, int q) { return q == 0 ? v.x : v.y; }
+  __device__ static __forceinline__ void set(V &v, int q, double x) { if (q == 0) v.x = x; else v.y = x; }
+};
+
+// Row stride (elements) of the one-CTA kernel's panel and E in shared
+// memory: whole 16-byte vectors, an odd number of them, so that the vectors
+// of 8 consecutive rows fall into 8 different bank groups.
+template <typename T> __host__ __device__ constexpr int pan_ld(int k) {
+  const int vn = 16 / (int)sizeof(T);
+  int nv = (k + vn - 1) / vn;
+  if ((nv & 1) == 0) nv++;
+  return nv * vn;
+}
+// shared memory of one front: panel and E (m x pan_ld(k) each), the
+// multiplier row (pan_ld(k))
+template <typename T> __host__ __device__ constexpr size_t pan_smem(int m, int k) {
+  return ((size_t)2 * m + 1) * pan_ld<T>(k) * sizeof(T);
+}
+
 // Fronts whose pivot panel (m x k) and E (m x k) fit in shared memory: one
 // CTA per front.  The pivot columns are assembled straight into shared
 // memory, the update block in the arena; the panel is factored and E formed
 // in shared memory, E is written out, and the update block receives
-// -L21 L21^T in 4x4 register blocks.
-constexpr int kPanBatch = 8;           // columns per batch of a thread's row updates
+// -L21 L21^T in 4x4 register blocks.  Panel and E are row-major in shared
+// memory (row i at i * pan_ld(k)): a thread updates its rows 16 bytes at a
+// time against the broadcast multiplier row, and the update block reads
+// 16-byte pieces of two rows per step.
 constexpr int kPanThreads = 128;       // fronts of up to kPanWideRows rows
 constexpr int kPanThreadsWide = 256;   // larger fronts
 constexpr int kPanWideRows = 160;
@@ -153,21 +189,36 @@ template <typename T>
 __global__ void __launch_bounds__(kPanThreadsWide)
 mf_factor_panel(MfView v, const int *__restrict__ fronts, const double *__restrict__ vals,
                 T *__restrict__ arena, T *__restrict__ E, int *__restrict__ status) {
+  using SV = SVec<T>;
+  using V = typename SV::V;
+  constexpr int VN = SV::N;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int f = fronts[blockIdx.x];
   const int m = v.f_m[f], k = v.f_k[f], r = m - k;
-  T *P = reinterpret_cast<T *>(smem_raw);  // m x k pivot columns, ld m
-  T *Es = P + m * k;                         // m x k elimination matrix, ld m
+  const int ldk = pan_ld<T>(k), nv = ldk / VN;
+  T *P = reinterpret_cast<T *>(smem_raw);  // m x k panel, row-major, row stride ldk
+  T *Es = P + (size_t)m * ldk;              // m x k elimination matrix, row-major
+  T *lmul = Es + (size_t)m * ldk;           // step j: L(c, j) for j < c < k, zero elsewhere
   const int64_t off = v.f_off[f];
   T *F = arena + off;
   const int tid = threadIdx.x, nt = blockDim.x;
-  // 1. zero: panel and E = [I ; 0] in shared memory, update block in the arena
-  //    (column loops over thread-strided rows: no integer division per element)
-  for (int c = 0; c < k; c++)
-    for (int i = tid; i < m; i += nt) {
-      P[c * m + i] = T(0);
-      Es[c * m + i] = i == c ? T(1) : T(0);
+  // 1. zero: panel, E = [I ; 0] and the multiplier row in shared memory,
+  //    update block in the arena
+  for (int i = tid; i < m; i += nt) {
+    V *pr = reinterpret_cast<V *>(P + (size_t)i * ldk);
+    V *er = reinterpret_cast<V *>(Es + (size_t)i * ldk);
+    for (int q = 0; q < nv; q++) {
+      V z, e;
+#pragma unroll
+      for (int u = 0; u < VN; u++) {
+        SV::set(z, u, T(0));
+        SV::set(e, u, (q * VN + u == i && i < k) ? T(1) : T(0));
+      }
+      pr[q] = z;
+      er[q] = e;
     }
+  }
+  for (int c = tid; c < ldk; c += nt) lmul[c] = T(0);
   for (int c = 0; c < r; c++)
     for (int i = c + tid; i < r; i += nt) F[(int64_t)(k + c) * m + k + i] = T(0);
   __syncthreads();
@@ -176,8 +227,12 @@ mf_factor_panel(MfView v, const int *__restrict__ fronts, const double *__restri
     double sv = 0.0;
     for (int64_t q = v.asm_sp[e]; q < v.asm_sp[e + 1]; q++) sv += vals[v.asm_src[q]];
     const int64_t t = v.asm_tgt[e] - off;
-    if (t < (int64_t)m * k) P[t] = (T)sv;
-    else F[t] = (T)sv;
+    if (t < (int64_t)m * k) {
+      const int col = (int)(t / m), row = (int)(t - (int64_t)col * m);
+      P[(size_t)row * ldk + col] = (T)sv;
+    } else {
+      F[t] = (T)sv;
+    }
   }
   __syncthreads();
   // 3. extend-add of the children's update matrices, children in order
@@ -189,68 +244,75 @@ mf_factor_panel(MfView v, const int *__restrict__ fronts, const double *__restri
     const int lane = tid & 31, wid = tid >> 5, nw = nt / 32;
     for (int b = wid; b < rc; b += nw) {
       const int col = rel[b];
-      T *Dst = col < k ? P + col * m : F + (int64_t)col * m;
-      extend_add_column<T>(Dst, rel, U + (int64_t)b * mc, b, rc, lane);
+      if (col < k) extend_add_column<T>(P + col, rel, U + (int64_t)b * mc, b, rc, lane, ldk);
+      else extend_add_column<T>(F + (int64_t)col * m, rel, U + (int64_t)b * mc, b, rc, lane);
     }
     __syncthreads();
   }
   // 4. factor the panel and eliminate E.  Every thread takes the pivot from
-  //    shared memory itself (one barrier per step fewer); the updates of a
-  //    step go row by row, kPanBatch columns at a time with all their loads
-  //    issued before the stores, so a thread's read-modify-writes of
-  //    different columns overlap instead of waiting on each other.  Each
-  //    element still receives the updates of the pivots in increasing order.
+  //    shared memory itself; the scaled column j goes to the multiplier row
+  //    (panel rows) beside the panel.  A thread then updates each of its
+  //    rows i > j 16 bytes at a time: panel columns (j, k) against the
+  //    multiplier row, E columns [0, j] against E's row j.  Entries left of
+  //    column j + 1 (panel) or right of column j (E) inside a vector keep
+  //    their values; upper-triangle and padding entries of the panel are
+  //    never read.  Each element receives the updates of the pivots in
+  //    increasing order.
   for (int j = 0; j < k; j++) {
-    T d = P[j * m + j];
+    T d = P[(size_t)j * ldk + j];
     if (!(d > T(0))) {
       if (tid == 0) atomicOr(status, ERR_NOT_SPD);
       d = T(1);
     }
     const T p = tsqrt<T>(d);
-    for (int i = j + 1 + tid; i < m; i += nt) P[j * m + i] /= p;
-    for (int c = tid; c <= j; c += nt) Es[c * m + j] /= p;
-    __syncthreads();
-    if (tid == 0) P[j * m + j] = p;  // read by no thread before the next step
     for (int i = j + 1 + tid; i < m; i += nt) {
-      const T lij = P[j * m + i];
-      // panel columns c in (j, min(k, i + 1))
-      const int c1 = min(k, i + 1);
-      for (int c0 = j + 1; c0 < c1; c0 += kPanBatch) {
-        T lc[kPanBatch], pv[kPanBatch];
+      const T x = P[(size_t)i * ldk + j] / p;
+      P[(size_t)i * ldk + j] = x;
+      if (i < k) lmul[i] = x;
+    }
+    for (int c = tid; c <= j; c += nt) Es[(size_t)j * ldk + c] /= p;
+    if (tid == 0) lmul[j] = T(0);  // held L(j, j-1); column j is no multiplier of step j
+    __syncthreads();
+    if (tid == 0) P[(size_t)j * ldk + j] = p;  // read by no thread before the next step
+    const V *lm = reinterpret_cast<const V *>(lmul);
+    const V *ej = reinterpret_cast<const V *>(Es + (size_t)j * ldk);
+    const int qp0 = (j + 1) / VN, qp1 = (k + VN - 1) / VN, qe1 = j / VN;
+    for (int i = j + 1 + tid; i < m; i += nt) {
+      const T lij = P[(size_t)i * ldk + j];
+      V *pr = reinterpret_cast<V *>(P + (size_t)i * ldk);
+      V *er = reinterpret_cast<V *>(Es + (size_t)i * ldk);
+      for (int q = qp0; q < qp1; q++) {
+        const V a = pr[q], b = lm[q];
+        V o;
 #pragma unroll
-        for (int u = 0; u < kPanBatch; u++) {
-          const int c = c0 + u;
-          lc[u] = c < c1 ? P[j * m + c] : T(0);
-          pv[u] = c < c1 ? P[c * m + i] : T(0);
+        for (int u = 0; u < VN; u++) {
+          const T nvl = SV::get(a, u) - lij * SV::get(b, u);
+          SV::set(o, u, q * VN + u > j ? nvl : SV::get(a, u));
         }
-#pragma unroll
-        for (int u = 0; u < kPanBatch; u++)
-          if (c0 + u < c1) P[(c0 + u) * m + i] = pv[u] - lij * lc[u];
+        pr[q] = o;
       }
-      // E columns c <= j
-      for (int c0 = 0; c0 <= j; c0 += kPanBatch) {
-        T ec[kPanBatch], ev[kPanBatch];
+      for (int q = 0; q <= qe1; q++) {
+        const V a = er[q], b = ej[q];
+        V o;
 #pragma unroll
-        for (int u = 0; u < kPanBatch; u++) {
-          const int c = c0 + u;
-          ec[u] = c <= j ? Es[c * m + j] : T(0);
-          ev[u] = c <= j ? Es[c * m + i] : T(0);
+        for (int u = 0; u < VN; u++) {
+          const T nvl = SV::get(a, u) - lij * SV::get(b, u);
+          SV::set(o, u, q * VN + u <= j ? nvl : SV::get(a, u));
         }
-#pragma unroll
-        for (int u = 0; u < kPanBatch; u++)
-          if (c0 + u <= j) Es[(c0 + u) * m + i] = ev[u] - lij * ec[u];
+        er[q] = o;
       }
     }
     __syncthreads();
   }
-  // 5. E -> global (ld round4(m)); the padding rows stay zero
+  // 5. E -> global (column-major, ld round4(m)); the padding rows stay zero
   {
     const int ld = round4(m);
     T *Eg = E + v.e_off[f];
     for (int c = 0; c < k; c++)
-      for (int i = tid; i < m; i += nt) Eg[(int64_t)c * ld + i] = Es[c * m + i];
+      for (int i = tid; i < m; i += nt) Eg[(int64_t)c * ld + i] = Es[(size_t)i * ldk + c];
   }
-  // 6. update block: F[k:m, k:m] -= L21 L21^T (lower), 4x4 blocks per thread
+  // 6. update block: F[k:m, k:m] -= L21 L21^T (lower), 4x4 blocks per thread;
+  //    L21 rows read VN columns at a time (padding columns are zero)
   const int nb4 = (r + 3) / 4;
   for (int q = tid; q < nb4 * nb4; q += nt) {
     const int bi = q % nb4, bc = q / nb4;
@@ -261,17 +323,29 @@ mf_factor_panel(MfView v, const int *__restrict__ fronts, const double *__restri
     for (int a = 0; a < 4; a++)
 #pragma unroll
       for (int b = 0; b < 4; b++) acc[a][b] = T(0);
-    for (int j = 0; j < k; j++) {
-      T li[4], lc[4];
+    const V *li[4], *lc[4];
+#pragma unroll
+    for (int a = 0; a < 4; a++) {
+      li[a] = reinterpret_cast<const V *>(P + (size_t)min(i0 + a, m - 1) * ldk);
+      lc[a] = reinterpret_cast<const V *>(P + (size_t)min(c0 + a, m - 1) * ldk);
+    }
+    const int qk = (k + VN - 1) / VN;
+    for (int qq = 0; qq < qk; qq++) {
+      V xi[4], xc[4];
 #pragma unroll
       for (int a = 0; a < 4; a++) {
-        li[a] = i0 + a < m ? P[j * m + i0 + a] : T(0);
-        lc[a] = c0 + a < m ? P[j * m + c0 + a] : T(0);
+        xi[a] = li[a][qq];
+        xc[a] = lc[a][qq];
       }
 #pragma unroll
-      for (int a = 0; a < 4; a++)
+      for (int u = 0; u < VN; u++) {
+        if (qq * VN + u < k) {
 #pragma unroll
-        for (int b = 0; b < 4; b++) acc[a][b] += li[a] * lc[b];
+          for (int a = 0; a < 4; a++)
+#pragma unroll
+            for (int b = 0; b < 4; b++) acc[a][b] += SV::get(xi[a], u) * SV::get(xc[b], u);
+        }
+      }
     }
 #pragma unroll
     for (int b = 0; b < 4; b++) {
@@ -343,8 +417,8 @@ mf_assemble_large(MfView v, const int2 *__restrict__ tasks, const double *__rest
 }
 
 // Panel at column j0 of a large front in two launches: mf_diag factors the
-// jb x jb diagonal block of every listed front (one warp each, in
-// registers); mf_panel then solves L21 = A21 L11^-T for row chunks of
+// jb x jb diagonal block of every listed front (one CTA each: one warp in
+// registers for FP32, a whole CTA for FP64); mf_panel then solves L21 = A21 L11^-T for row chunks of
 // kPanelRows rows (task = {front, first row of the chunk}), many CTAs per
 // front, or forms E rows of the panel (escale tasks, below).
 constexpr int kPanelRows = 256;
@@ -383,22 +457,55 @@ __device__ __forceinline__ void chol_warp(T (*D)[kNB + 1], int jb, int *status) 
   for (int c = 0; c < kNB; c++) D[lane][c] = a[c];
 }
 
+// The same right-looking Cholesky by a whole CTA in shared memory, one
+// pivot per step: for FP64, whose square roots and divisions are too slow
+// for one warp's chain on the FP64 pipe
 template <typename T>
-__global__ void __launch_bounds__(32)
+__device__ __forceinline__ void chol_cta(T (*D)[kNB + 1], int jb, int *status) {
+  const int tid = threadIdx.x;
+  for (int j = 0; j < jb; j++) {
+    if (tid == 0) {
+      T d = D[j][j];
+      if (!(d > T(0))) { atomicOr(status, ERR_NOT_SPD); d = T(1); }
+      D[j][j] = tsqrt<T>(d);
+    }
+    __syncthreads();
+    const T p = D[j][j];
+    for (int i = j + 1 + tid; i < jb; i += blockDim.x) D[i][j] /= p;
+    __syncthreads();
+    const int w = jb - j - 1;
+    for (int q = tid; q < w * w; q += blockDim.x) {
+      const int i = j + 1 + q / w, c = j + 1 + q % w;
+      if (i >= c) D[i][c] -= D[i][j] * D[c][j];
+    }
+    __syncthreads();
+  }
+}
+
+// FP32: one warp per front (chol_warp); FP64: kMfThreads per front (chol_cta)
+template <typename T> __host__ __device__ constexpr int diag_threads() { return sizeof(T) == 4 ? 32 : kMfThreads; }
+
+template <typename T>
+__global__ void __launch_bounds__(diag_threads<T>())
 mf_diag(MfView v, const int *__restrict__ fronts, int j0, T *__restrict__ arena, int *__restrict__ status) {
   __shared__ T D[kNB][kNB + 1];
   const int f = fronts[blockIdx.x];
   const int m = v.f_m[f], k = v.f_k[f];
   const int jb = min(kNB, k - j0);
   T *F = arena + v.f_off[f];
-  const int lane = threadIdx.x;
-  for (int c = 0; c < kNB; c++)  // lower part of the block, zeros elsewhere (coalesced over rows)
-    D[lane][c] = (lane >= c && lane < jb) ? F[(int64_t)(j0 + c) * m + j0 + lane] : T(0);
-  __syncwarp();
-  chol_warp<T>(D, jb, status);
-  __syncwarp();
-  for (int c = 0; c < jb; c++)
-    if (lane >= c && lane < jb) F[(int64_t)(j0 + c) * m + j0 + lane] = D[lane][c];
+  const int tid = threadIdx.x;
+  for (int q = tid; q < kNB * kNB; q += diag_threads<T>()) {  // lower part, zeros elsewhere
+    const int c = q / kNB, i = q % kNB;  // column-major walk: coalesced over rows
+    D[i][c] = (i >= c && i < jb) ? F[(int64_t)(j0 + c) * m + j0 + i] : T(0);
+  }
+  __syncthreads();
+  if constexpr (sizeof(T) == 4) chol_warp<T>(D, jb, status);
+  else chol_cta<T>(D, jb, status);
+  __syncthreads();
+  for (int q = tid; q < jb * jb; q += diag_threads<T>()) {
+    const int c = q / jb, i = q % jb;
+    if (i >= c) F[(int64_t)(j0 + c) * m + j0 + i] = D[i][c];
+  }
 }
 
 // E rows of the panel (escale task = {front, first column}): E_J <- L_JJ^-1 E_J

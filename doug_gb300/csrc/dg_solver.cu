@@ -222,7 +222,7 @@ struct MfDevice {
       for (int q = B.lvl_ptr[(size_t)l]; q < B.lvl_ptr[(size_t)l + 1]; q++) {
         int f = B.lvl_fronts[(size_t)q];
         int m = B.f_m[(size_t)f], k = B.f_k[(size_t)f];
-        const size_t smem = (size_t)2 * m * k * sizeof(T);
+        const size_t smem = pan_smem<T>(m, k);
         if (m <= tune.tiny_rows) {
           tiny.push_back(f);
           L.tiny_smem = std::max(L.tiny_smem, smem);
@@ -451,7 +451,8 @@ struct MfDevice {
       }
       for (const Step &st : L.steps) {
         if (st.diag_cnt) {
-          mf_diag<T><<<st.diag_cnt, 32, 0, s>>>(view, diag_fronts.p + st.diag_off, st.j0, arena.p, status);
+          mf_diag<T><<<st.diag_cnt, diag_threads<T>(), 0, s>>>(view, diag_fronts.p + st.diag_off, st.j0, arena.p,
+                                                                status);
           launches++;
         }
         if (st.panel_cnt + st.esc_cnt) {
