@@ -74,7 +74,7 @@ struct MfTune {
   int panel_rows = 512;                  // fronts of at most this many rows may use mf_factor_panel
   int64_t fwd_task_bytes = 96 * 1024;    // E bytes per forward task of a large front
   int64_t lean_task_bytes = 80 * 1024;   // levels with smaller average tasks use 128-thread CTAs
-  int small_min_fronts = 304;            // levels with fewer small fronts solve them CTA-per-task
+  int small_min_fronts = 1500;           // levels with fewer small fronts solve them CTA-per-task
   int schedule = 0;                      // solves: 0 one launch per level, 1 dependency-driven queue
   int pdl = 0;                           // 1: level launches with programmatic dependent launch
   int factor_overlap = 1;                // 1: a level's one-CTA fronts beside its large-front steps

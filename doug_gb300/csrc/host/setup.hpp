@@ -42,7 +42,7 @@ struct Controls {
   int panel_rows = 512;             // fronts up to this size (and panel + E <= 96 KB): one CTA each
   int fwd_task_kb = 96;             // KB of E per forward task of a large front
   int lean_task_kb = 80;            // levels with smaller average tasks use 128-thread CTAs
-  int thin_level_fronts = 304;      // levels with fewer small fronts solve them one CTA per task
+  int thin_level_fronts = 1500;     // levels with fewer small fronts solve them one CTA per task
   int solve_schedule = 0;           // multifrontal solves: 0 one launch per level, 1 dependency-driven queue
   int solve_pdl = 1;                // 1: the level launches overlap through programmatic dependent launch
   int factor_overlap = 1;           // 1: a level's one-CTA fronts factored on a side stream beside its large fronts
