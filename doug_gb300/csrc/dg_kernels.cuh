@@ -812,8 +812,8 @@ constexpr size_t kTcSmem = 4 * kTcTileBytes + 1024;                // + alignmen
 constexpr long long kTcWaitPolls = 1LL << 24;
 
 __global__ void __launch_bounds__(256, 3)
-mf_update_big_tc(MfView v, const int2 *__restrict__ tasks, int jl, int kw, float *__restrict__ arena,
-                 int *__restrict__ status) {
+mf_update_big_tc(MfView v, const int2 *__restrict__ tasks, int nupd, const int2 *__restrict__ etasks, int jl,
+                 int kw, float *__restrict__ arena, float *__restrict__ E, int *__restrict__ status) {
   extern __shared__ unsigned char tc_raw[];
   unsigned char *base = reinterpret_cast<unsigned char *>((reinterpret_cast<uintptr_t>(tc_raw) + 1023) &
                                                           ~static_cast<uintptr_t>(1023));
@@ -821,13 +821,17 @@ mf_update_big_tc(MfView v, const int2 *__restrict__ tasks, int jl, int kw, float
                 *Blo = base + 3 * kTcTileBytes;
   __shared__ __align__(8) uint64_t bar;
   __shared__ uint32_t tmem_slot;
-  const int f = tasks[blockIdx.x].x;
-  const int ti = tasks[blockIdx.x].y >> 16, tj = tasks[blockIdx.x].y & 0xffff;
+  const bool etile = (int)blockIdx.x >= nupd;
+  const int2 task = etile ? etasks[blockIdx.x - nupd] : tasks[blockIdx.x];
+  const int f = task.x;
+  const int ti = task.y >> 16, tj = task.y & 0xffff;
   const int m = v.f_m[f], k = v.f_k[f];
   const int K = min(kw, k - jl);
-  const int c0 = jl + K, r0 = c0 + ti * kBT, cc0 = c0 + tj * kBT;
-  const bool diag = ti == tj;
+  const int c0 = jl + K, r0 = c0 + ti * kBT, cc0 = etile ? tj * kBT : c0 + tj * kBT;
+  const bool diag = !etile && ti == tj;
   float *F = arena + v.f_off[f];
+  const int ld = round4(m);
+  float *Eg = E + v.e_off[f];
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   if (warp == 0) tc::tmem_alloc(&tmem_slot, 128);
   if (tid == 0) tc::mbar_init(&bar, 1);
@@ -841,13 +845,29 @@ mf_update_big_tc(MfView v, const int2 *__restrict__ tasks, int jl, int kw, float
   constexpr int NQ = 128 * kTcChunk / 256;
   const int r = tid & 127, kk0 = tid >> 7;
   const int ra = r0 + r, rb = cc0 + r;
+  // E tiles: B row rr is E column cc0 + rr, 16 consecutive K values of it
+  // (E rows jl + kc + te ..), read as four 16-byte vectors
+  const int rr = tid >> 1, te = (tid & 1) * 16;
+  const bool eok = etile && cc0 + rr < c0;
   float pa[NQ], pb[NQ];
   auto fetch = [&](int kc) {
 #pragma unroll
     for (int q = 0; q < NQ; q++) {
       const int t = kc + kk0 + 2 * q;
       pa[q] = (t < K && ra < m) ? F[(int64_t)(jl + t) * m + ra] : 0.f;
-      pb[q] = (!diag && t < K && rb < m) ? F[(int64_t)(jl + t) * m + rb] : 0.f;
+      if (!etile) pb[q] = (!diag && t < K && rb < m) ? F[(int64_t)(jl + t) * m + rb] : 0.f;
+    }
+    if (etile) {
+#pragma unroll
+      for (int u = 0; u < 4; u++) {
+        const int t = kc + te + 4 * u;
+        float4 x = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (eok && t < K) x = *reinterpret_cast<const float4 *>(Eg + (int64_t)(cc0 + rr) * ld + jl + t);
+        pb[4 * u] = x.x;
+        pb[4 * u + 1] = t + 1 < K ? x.y : 0.f;
+        pb[4 * u + 2] = t + 2 < K ? x.z : 0.f;
+        pb[4 * u + 3] = t + 3 < K ? x.w : 0.f;
+      }
     }
   };
   auto stash = [&]() {
@@ -857,10 +877,23 @@ mf_update_big_tc(MfView v, const int2 *__restrict__ tasks, int jl, int kw, float
       const uint32_t ah = tf32_of(pa[q]);
       *reinterpret_cast<uint32_t *>(Ahi + off) = ah;
       *reinterpret_cast<uint32_t *>(Alo + off) = tf32_of(pa[q] - __uint_as_float(ah));
-      if (!diag) {
+      if (!diag && !etile) {
         const uint32_t bh = tf32_of(pb[q]);
         *reinterpret_cast<uint32_t *>(Bhi + off) = bh;
         *reinterpret_cast<uint32_t *>(Blo + off) = tf32_of(pb[q] - __uint_as_float(bh));
+      }
+    }
+    if (etile) {
+#pragma unroll
+      for (int u = 0; u < 4; u++) {
+        const uint32_t off = tc::sw128_offset(rr, te + 4 * u);  // 4 values in one 16-byte chunk
+        uint4 h, l;
+        h.x = tf32_of(pb[4 * u]);     l.x = tf32_of(pb[4 * u] - __uint_as_float(h.x));
+        h.y = tf32_of(pb[4 * u + 1]); l.y = tf32_of(pb[4 * u + 1] - __uint_as_float(h.y));
+        h.z = tf32_of(pb[4 * u + 2]); l.z = tf32_of(pb[4 * u + 2] - __uint_as_float(h.z));
+        h.w = tf32_of(pb[4 * u + 3]); l.w = tf32_of(pb[4 * u + 3] - __uint_as_float(h.w));
+        *reinterpret_cast<uint4 *>(Bhi + off) = h;
+        *reinterpret_cast<uint4 *>(Blo + off) = l;
       }
     }
   };
@@ -902,7 +935,24 @@ mf_update_big_tc(MfView v, const int2 *__restrict__ tasks, int jl, int kw, float
     for (int h = 0; h < 4; h++) {
       float d[16];
       tc::tmem_load16(tmem + ((uint32_t)(32 * lg) << 16) + (uint32_t)(ch * 64 + 16 * h), d);
-      if (row < m) {
+      if (etile) {
+        // E[row, col] for col < c0: the super-panel's own columns (>= jl)
+        // are assigned, the earlier ones accumulated
+        if (row < m) {
+          const int colb = cc0 + ch * 64 + 16 * h;
+          float cur[16];
+#pragma unroll
+          for (int c = 0; c < 16; c++) {
+            const int col = colb + c;
+            cur[c] = (col < jl) ? Eg[(int64_t)col * ld + row] : 0.f;
+          }
+#pragma unroll
+          for (int c = 0; c < 16; c++) {
+            const int col = colb + c;
+            if (col < c0) Eg[(int64_t)col * ld + row] = cur[c] - d[c];
+          }
+        }
+      } else if (row < m) {
         const int colb = cc0 + ch * 64 + 16 * h;
         float cur[16];
 #pragma unroll

@@ -293,8 +293,11 @@ struct MfDevice {
           for (int tj = 0; tj < nt; tj++)
             for (int ti = tj; ti < nt; ti++) ut.push_back(make_int2(f, (ti << 16) | tj));
           // E rows below the super-panel, all its columns at once:
-          // E[c1:m, 0:c1] -= L[c1:m, S0:c1] E[S0:c1, 0:c1] (64 x 64 tiles)
-          const int nte = (c1 + kTile - 1) / kTile, ntr = (m - c1 + kTile - 1) / kTile;
+          // E[c1:m, 0:c1] -= L[c1:m, S0:c1] E[S0:c1, 0:c1] (FP32 with tcgen05:
+          // 128 x 128 tiles in the trailing update's launch; else 64 x 64
+          // tiles of mf_update)
+          const int etw = bigt && tune.tensor_update == 1 ? kBT : kTile;
+          const int nte = (c1 + etw - 1) / etw, ntr = (m - c1 + etw - 1) / etw;
           for (int ti = 0; ti < ntr; ti++)
             for (int tc = 0; tc < nte; tc++) et.push_back(make_int2(f, (ti << 16) | tc));
         }
@@ -462,16 +465,19 @@ struct MfDevice {
         }
         if (st.big) {
           if constexpr (sizeof(T) == 4) {  // planned for FP32 batches only
-            if (st.upd_cnt) {
-              if (tensor_update == 1)
-                mf_update_big_tc<<<st.upd_cnt, 256, kTcSmem, s>>>(view, upd_tasks.p + st.upd_off, st.j0, st.kw,
-                                                                   reinterpret_cast<float *>(arena.p), status);
-              else
-                mf_update_big_tf32<<<st.upd_cnt, 256, 0, s>>>(view, upd_tasks.p + st.upd_off, st.j0, st.kw,
-                                                              reinterpret_cast<float *>(arena.p));
+            if (tensor_update == 1) {  // trailing-update tiles, then the super-panel's E tiles
+              if (st.upd_cnt + st.etile_cnt) {
+                mf_update_big_tc<<<st.upd_cnt + st.etile_cnt, 256, kTcSmem, s>>>(
+                    view, upd_tasks.p + st.upd_off, st.upd_cnt, etile_tasks.p + st.etile_off, st.j0, st.kw,
+                    reinterpret_cast<float *>(arena.p), reinterpret_cast<float *>(E.p), status);
+                launches++;
+              }
+            } else if (st.upd_cnt) {
+              mf_update_big_tf32<<<st.upd_cnt, 256, 0, s>>>(view, upd_tasks.p + st.upd_off, st.j0, st.kw,
+                                                            reinterpret_cast<float *>(arena.p));
               launches++;
             }
-            if (st.etile_cnt) {  // the super-panel's E update
+            if (tensor_update != 1 && st.etile_cnt) {  // the super-panel's E update
               mf_update<T><<<st.etile_cnt, kMfThreads, 0, s>>>(view, upd_tasks.p + st.upd_off, 0,
                                                                etile_tasks.p + st.etile_off, st.j0, st.kw, 0,
                                                                arena.p, E.p);
