@@ -382,47 +382,6 @@ __device__ __forceinline__ int lower_bound32(const int *a, int lo, int hi, int k
   return lo;
 }
 
-// task = {front, first column of the chunk}
-template <typename T>
-__global__ void __launch_bounds__(kMfThreads)
-mf_assemble_large(MfView v, const int2 *__restrict__ tasks, const double *__restrict__ vals,
-                  T *__restrict__ arena) {
-  const int f = tasks[blockIdx.x].x, c0 = tasks[blockIdx.x].y;
-  const int m = v.f_m[f];
-  const int c1 = min(c0 + kAsmCols, m);
-  const int64_t off = v.f_off[f];
-  T *F = arena + off;
-  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5, nw = kMfThreads / 32;
-  for (int c = c0 + wid; c < c1; c += nw)
-    for (int i = c + lane; i < m; i += 32) F[(int64_t)c * m + i] = T(0);
-  __syncthreads();
-  const int64_t lo = lower_bound64(v.asm_tgt, v.f_asm[f], v.f_asm[f + 1], off + (int64_t)c0 * m);
-  const int64_t hi = lower_bound64(v.asm_tgt, lo, v.f_asm[f + 1], off + (int64_t)c1 * m);
-  for (int64_t e = lo + tid; e < hi; e += kMfThreads) {
-    double s = 0.0;
-    for (int64_t q = v.asm_sp[e]; q < v.asm_sp[e + 1]; q++) s += vals[v.asm_src[q]];
-    arena[v.asm_tgt[e]] = (T)s;
-  }
-  __syncthreads();
-  for (int ci = v.f_child_ptr[f]; ci < v.f_child_ptr[f + 1]; ci++) {
-    const int c = v.f_children[ci];
-    const int mc = v.f_m[c], kc = v.f_k[c], rc = mc - kc;
-    const T *U = arena + v.f_off[c] + (int64_t)kc * mc + kc;
-    const int *rel = v.relmap + v.f_relmap[c];
-    const int blo = lower_bound32(rel, 0, rc, c0), bhi = lower_bound32(rel, blo, rc, c1);
-    for (int b = blo + wid; b < bhi; b += nw)
-      extend_add_column<T>(F + (int64_t)rel[b] * m, rel, U + (int64_t)b * mc, b, rc, lane);
-    __syncthreads();
-  }
-}
-
-// Panel at column j0 of a large front in two launches: mf_diag factors the
-// jb x jb diagonal block of every listed front (one CTA each: one warp in
-// registers for FP32, a whole CTA for FP64); mf_panel then solves L21 = A21 L11^-T for row chunks of
-// kPanelRows rows (task = {front, first row of the chunk}), many CTAs per
-// front, or forms E rows of the panel (escale tasks, below).
-constexpr int kPanelRows = 256;
-
 // Right-looking Cholesky of the lower triangle of D[0..jb)[0..jb) by one
 // warp: lane i keeps row i in registers, column j of L is broadcast by
 // shuffles.  Per element the same operations in the same order as the
@@ -485,28 +444,85 @@ __device__ __forceinline__ void chol_cta(T (*D)[kNB + 1], int jb, int *status) {
 // FP32: one warp per front (chol_warp); FP64: kMfThreads per front (chol_cta)
 template <typename T> __host__ __device__ constexpr int diag_threads() { return sizeof(T) == 4 ? 32 : kMfThreads; }
 
+// Factor the jb x jb diagonal block at column j0 of a front in place (F: the
+// front's arena block, ld m): its lower part into shared memory, FP32 by one
+// warp in registers, FP64 by the whole CTA; every thread of the CTA calls it,
+// after a barrier that makes the block's final values visible.
 template <typename T>
-__global__ void __launch_bounds__(diag_threads<T>())
-mf_diag(MfView v, const int *__restrict__ fronts, int j0, T *__restrict__ arena, int *__restrict__ status) {
+__device__ __forceinline__ void factor_diag_block(T *__restrict__ F, int m, int j0, int jb, int *status) {
   __shared__ T D[kNB][kNB + 1];
-  const int f = fronts[blockIdx.x];
-  const int m = v.f_m[f], k = v.f_k[f];
-  const int jb = min(kNB, k - j0);
-  T *F = arena + v.f_off[f];
-  const int tid = threadIdx.x;
-  for (int q = tid; q < kNB * kNB; q += diag_threads<T>()) {  // lower part, zeros elsewhere
+  const int tid = threadIdx.x, nt = blockDim.x;
+  for (int q = tid; q < kNB * kNB; q += nt) {  // lower part, zeros elsewhere
     const int c = q / kNB, i = q % kNB;  // column-major walk: coalesced over rows
     D[i][c] = (i >= c && i < jb) ? F[(int64_t)(j0 + c) * m + j0 + i] : T(0);
   }
   __syncthreads();
-  if constexpr (sizeof(T) == 4) chol_warp<T>(D, jb, status);
-  else chol_cta<T>(D, jb, status);
+  if constexpr (sizeof(T) == 4) {
+    if (tid < 32) chol_warp<T>(D, jb, status);
+  } else {
+    chol_cta<T>(D, jb, status);
+  }
   __syncthreads();
-  for (int q = tid; q < jb * jb; q += diag_threads<T>()) {
+  for (int q = tid; q < jb * jb; q += nt) {
     const int c = q / jb, i = q % jb;
     if (i >= c) F[(int64_t)(j0 + c) * m + j0 + i] = D[i][c];
   }
 }
+
+// The diagonal block of a panel step in a launch of its own: only where no
+// earlier kernel of the chain finishes the block (the first step of an FP32
+// super-panel after the mma.sync trailing update, tensor_update 0)
+template <typename T>
+__global__ void __launch_bounds__(diag_threads<T>())
+mf_diag(MfView v, const int *__restrict__ fronts, int j0, T *__restrict__ arena, int *__restrict__ status) {
+  const int f = fronts[blockIdx.x];
+  const int m = v.f_m[f], k = v.f_k[f];
+  factor_diag_block<T>(arena + v.f_off[f], m, j0, min(kNB, k - j0), status);
+}
+
+// task = {front, first column of the chunk}.  The CTA of chunk 0 then
+// factors the front's first diagonal block (the first panel step's).
+template <typename T>
+__global__ void __launch_bounds__(kMfThreads)
+mf_assemble_large(MfView v, const int2 *__restrict__ tasks, const double *__restrict__ vals,
+                  T *__restrict__ arena, int *__restrict__ status) {
+  const int f = tasks[blockIdx.x].x, c0 = tasks[blockIdx.x].y;
+  const int m = v.f_m[f];
+  const int c1 = min(c0 + kAsmCols, m);
+  const int64_t off = v.f_off[f];
+  T *F = arena + off;
+  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5, nw = kMfThreads / 32;
+  for (int c = c0 + wid; c < c1; c += nw)
+    for (int i = c + lane; i < m; i += 32) F[(int64_t)c * m + i] = T(0);
+  __syncthreads();
+  const int64_t lo = lower_bound64(v.asm_tgt, v.f_asm[f], v.f_asm[f + 1], off + (int64_t)c0 * m);
+  const int64_t hi = lower_bound64(v.asm_tgt, lo, v.f_asm[f + 1], off + (int64_t)c1 * m);
+  for (int64_t e = lo + tid; e < hi; e += kMfThreads) {
+    double s = 0.0;
+    for (int64_t q = v.asm_sp[e]; q < v.asm_sp[e + 1]; q++) s += vals[v.asm_src[q]];
+    arena[v.asm_tgt[e]] = (T)s;
+  }
+  __syncthreads();
+  for (int ci = v.f_child_ptr[f]; ci < v.f_child_ptr[f + 1]; ci++) {
+    const int c = v.f_children[ci];
+    const int mc = v.f_m[c], kc = v.f_k[c], rc = mc - kc;
+    const T *U = arena + v.f_off[c] + (int64_t)kc * mc + kc;
+    const int *rel = v.relmap + v.f_relmap[c];
+    const int blo = lower_bound32(rel, 0, rc, c0), bhi = lower_bound32(rel, blo, rc, c1);
+    for (int b = blo + wid; b < bhi; b += nw)
+      extend_add_column<T>(F + (int64_t)rel[b] * m, rel, U + (int64_t)b * mc, b, rc, lane);
+    __syncthreads();
+  }
+  if (c0 == 0) factor_diag_block<T>(F, m, 0, min(kNB, v.f_k[f]), status);
+}
+
+// Panel at column j0 of a large front: its diagonal block was factored by
+// the kernel that finished it (factor_diag_block: the assembly, the previous
+// step's update tile (0, 0) or the super-panel's trailing-update tile (0, 0));
+// mf_panel solves L21 = A21 L11^-T for row chunks of kPanelRows rows (task =
+// {front, first row of the chunk}), many CTAs per front, or forms E rows of
+// the panel (escale tasks, below).
+constexpr int kPanelRows = 256;
 
 // E rows of the panel (escale task = {front, first column}): E_J <- L_JJ^-1 E_J
 // on kEscCols columns of [0, j0 + jb); the columns of block J start as the
@@ -597,7 +613,7 @@ mf_panel(MfView v, const int2 *__restrict__ tasks, int npanel, const int2 *__res
 template <typename T>
 __global__ void __launch_bounds__(kMfThreads)
 mf_update(MfView v, const int2 *__restrict__ tasks, int nupd, const int2 *__restrict__ etasks, int jl, int kw,
-          int cend_base, T *__restrict__ arena, T *__restrict__ E) {
+          int cend_base, T *__restrict__ arena, T *__restrict__ E, int *__restrict__ status) {
   __shared__ T As[kNB][kTile];
   __shared__ T Bs[kNB][kTile + 1];
   const bool etile = (int)blockIdx.x >= nupd;
@@ -676,6 +692,12 @@ mf_update(MfView v, const int2 *__restrict__ tasks, int nupd, const int2 *__rest
       const int row = r0 + tx + 16 * a;
       if (row < m && row >= col) F[(int64_t)col * m + row] -= acc[a][b];
     }
+  }
+  // tile (0, 0) holds the next panel step's diagonal block (columns c0 ..,
+  // inside the super-panel for a panel step): this was its last update
+  if (ti == 0 && tj == 0 && c0 < (cend_base > 0 ? min(cend_base, k) : k)) {
+    __syncthreads();
+    factor_diag_block<T>(F, m, c0, min(kNB, k - c0), status);
   }
 }
 
@@ -813,7 +835,8 @@ constexpr long long kTcWaitPolls = 1LL << 24;
 
 __global__ void __launch_bounds__(256, 3)
 mf_update_big_tc(MfView v, const int2 *__restrict__ tasks, int nupd, const int2 *__restrict__ etasks, int jl,
-                 int kw, float *__restrict__ arena, float *__restrict__ E, int *__restrict__ status) {
+                 int kw, float *__restrict__ arena, float *__restrict__ E, int *__restrict__ status,
+                 int fuse_diag) {
   extern __shared__ unsigned char tc_raw[];
   unsigned char *base = reinterpret_cast<unsigned char *>((reinterpret_cast<uintptr_t>(tc_raw) + 1023) &
                                                           ~static_cast<uintptr_t>(1023));
@@ -971,6 +994,10 @@ mf_update_big_tc(MfView v, const int2 *__restrict__ tasks, int nupd, const int2 
   tc::fence_before_sync();
   __syncthreads();
   if (warp == 0) tc::tmem_free(tmem, 128);
+  // trailing-update tile (0, 0) holds the next super-panel's first diagonal
+  // block: this was its last update
+  if (fuse_diag && !bad && !etile && ti == 0 && tj == 0 && c0 < k)
+    factor_diag_block<float>(F, m, c0, min(kNB, k - c0), status);
 }
 
 // ---------------------------------------------------------------------------

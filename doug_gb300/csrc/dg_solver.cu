@@ -258,7 +258,9 @@ struct MfDevice {
           for (int f : large) {
             int m = B.f_m[(size_t)f], k = B.f_k[(size_t)f];
             if (j0 >= k) continue;
-            df.push_back(f);
+            // the diagonal block is factored by the kernel that finishes it,
+            // except after the mma.sync trailing update (tensor_update 0)
+            if (j0 > 0 && j0 == S0 && sizeof(T) == 4 && tune.tensor_update != 1) df.push_back(f);
             const int c0 = j0 + std::min(kNB, k - j0);
             for (int r0 = c0; r0 < m; r0 += kPanelRows) pf.push_back(make_int2(f, r0));
             for (int e0 = 0; e0 < c0; e0 += EscCols<T>::N) es.push_back(make_int2(f, e0));
@@ -449,7 +451,8 @@ struct MfDevice {
       }
       if (fork) CK(cudaEventRecord(ev_join, aux));
       if (L.asm_cnt) {
-        mf_assemble_large<T><<<L.asm_cnt, kMfThreads, 0, s>>>(view, asm_tasks.p + L.asm_off, vals, arena.p);
+        mf_assemble_large<T><<<L.asm_cnt, kMfThreads, 0, s>>>(view, asm_tasks.p + L.asm_off, vals, arena.p,
+                                                              status);
         launches++;
       }
       for (const Step &st : L.steps) {
@@ -469,7 +472,7 @@ struct MfDevice {
               if (st.upd_cnt + st.etile_cnt) {
                 mf_update_big_tc<<<st.upd_cnt + st.etile_cnt, 256, kTcSmem, s>>>(
                     view, upd_tasks.p + st.upd_off, st.upd_cnt, etile_tasks.p + st.etile_off, st.j0, st.kw,
-                    reinterpret_cast<float *>(arena.p), reinterpret_cast<float *>(E.p), status);
+                    reinterpret_cast<float *>(arena.p), reinterpret_cast<float *>(E.p), status, 1);
                 launches++;
               }
             } else if (st.upd_cnt) {
@@ -480,14 +483,14 @@ struct MfDevice {
             if (tensor_update != 1 && st.etile_cnt) {  // the super-panel's E update
               mf_update<T><<<st.etile_cnt, kMfThreads, 0, s>>>(view, upd_tasks.p + st.upd_off, 0,
                                                                etile_tasks.p + st.etile_off, st.j0, st.kw, 0,
-                                                               arena.p, E.p);
+                                                               arena.p, E.p, status);
               launches++;
             }
           }
         } else if (st.upd_cnt + st.etile_cnt) {
           mf_update<T><<<st.upd_cnt + st.etile_cnt, kMfThreads, 0, s>>>(
               view, upd_tasks.p + st.upd_off, st.upd_cnt, etile_tasks.p + st.etile_off, st.j0, st.kw,
-              st.cend_base, arena.p, E.p);
+              st.cend_base, arena.p, E.p, status);
           launches++;
         }
       }

@@ -47,7 +47,9 @@ def diffusion24():
                                    dict(fwd_task_kb=1024, lean_task_kb=4096), dict(nd_leaf=8),
                                    dict(thin_level_fronts=0), dict(thin_level_fronts=100000),
                                    dict(solve_schedule=1), dict(solve_schedule=1, thin_level_fronts=0),
-                                   dict(solve_pdl=0), dict(factor_overlap=0)])
+                                   dict(solve_pdl=0), dict(factor_overlap=0),
+                                   dict(panel_rows=16, tensor_update=0), dict(panel_rows=16, super_panel=32),
+                                   dict(panel_rows=16, super_panel=64, factor_overlap=0)])
 @pytest.mark.parametrize("precision", [0, 1])
 def test_batch_parameters_keep_the_solution(diffusion24, words, precision):
     n, r, c, v, b, ro = diffusion24
