@@ -31,6 +31,14 @@ constexpr int kVecThreads = 256;
 // device error word bits
 enum : int { ERR_NOT_SPD = 1, ERR_NAN = 2, ERR_BREAKDOWN = 4, ERR_WAIT = 8 };
 
+// one entry of a front's child list (child ci of f_children): the child's
+// relative-row map offset, update-vector offset and update-row count, for
+// the forward solves' right-hand-side assembly in one load
+struct ChildEdge {
+  int64_t relmap, uoff;
+  int rc, pad;
+};
+
 struct MfView {  // device pointers of one multifrontal batch
   const int64_t *f_off;
   const int *f_m, *f_k;
@@ -42,6 +50,7 @@ struct MfView {  // device pointers of one multifrontal batch
   const int *rows, *relmap;
   const int64_t *asm_tgt, *asm_sp, *asm_src;
   const int64_t *e_off;        // offset of the front's elimination matrix E (m x k, ld round4(m))
+  const ChildEdge *ch_edge;    // per child-list entry: see ChildEdge
 };
 
 __host__ __device__ __forceinline__ int round4(int x) { return (x + 3) & ~3; }
@@ -1104,15 +1113,17 @@ __device__ __forceinline__ void fwd_small_body(const MfView &v, const int *__res
   const T *Ef = E + v.e_off[f];
   T e[PASS][kSmallUnroll][VN];
   load_e_batch<T, PASS, G>(Ef, ld, m, k, sl, 0, e);
+  // the child list is static: its first entry is read before the wait
+  const int cb = v.f_child_ptr[f], ce = v.f_child_ptr[f + 1];
+  ChildEdge ed = cb < ce ? v.ch_edge[cb] : ChildEdge{0, 0, 0, 0};
   pdl_wait();
   for (int i = sl; i < m; i += G) w[i] = i < k ? xl[xo + i] : T(0);
   __syncwarp(gm);
-  for (int ci = v.f_child_ptr[f]; ci < v.f_child_ptr[f + 1]; ci++) {
-    const int c = v.f_children[ci];
-    const int rc = v.f_m[c] - v.f_k[c];
-    const int *rel = v.relmap + v.f_relmap[c];
-    const T *u = uvec + v.f_uoff[c];
-    for (int a = sl; a < rc; a += G) w[rel[a]] += __ldcg(u + a);
+  for (int ci = cb; ci < ce; ci++) {
+    if (ci > cb) ed = v.ch_edge[ci];
+    const int *rel = v.relmap + ed.relmap;
+    const T *u = uvec + ed.uoff;
+    for (int a = sl; a < ed.rc; a += G) w[rel[a]] += __ldcg(u + a);
     __syncwarp(gm);
   }
   T acc[PASS][VN];
@@ -1283,16 +1294,20 @@ __device__ __forceinline__ void fwd_big_body(const MfView &v, int2 tk, const T *
   };
   auto chunk_cols = [&](int r0) { return r0 < k ? min(k, r0 + RC) : k; };
   load_batch(ch0 * RC, chunk_cols(ch0 * RC), wid);  // in flight while b is assembled
+  // the child list is static: its first entry is read before the wait, and
+  // each entry's successor while the entry is added
+  const int cb = v.f_child_ptr[f], ce = v.f_child_ptr[f + 1];
+  ChildEdge ed = cb < ce ? v.ch_edge[cb] : ChildEdge{0, 0, 0, 0};
   pdl_wait();
   for (int i = tid; i < m; i += NT) b[i] = i < k ? xl[xo + i] : T(0);
   __syncthreads();
-  for (int ci = v.f_child_ptr[f]; ci < v.f_child_ptr[f + 1]; ci++) {
-    const int c = v.f_children[ci];
-    const int rc = v.f_m[c] - v.f_k[c];
-    const int *rel = v.relmap + v.f_relmap[c];
-    const T *u = uvec + v.f_uoff[c];
-    for (int a = tid; a < rc; a += NT) b[rel[a]] += __ldcg(u + a);
+  for (int ci = cb; ci < ce; ci++) {
+    const ChildEdge nx = ci + 1 < ce ? v.ch_edge[ci + 1] : ed;
+    const int *rel = v.relmap + ed.relmap;
+    const T *u = uvec + ed.uoff;
+    for (int a = tid; a < ed.rc; a += NT) b[rel[a]] += __ldcg(u + a);
     __syncthreads();
+    ed = nx;
   }
   T *uf = uvec + v.f_uoff[f];
   for (int ch = ch0; ch < ch0 + nch; ch++) {

@@ -111,6 +111,7 @@ void launch_level(bool pdl, void (*k)(P...), int grid, int block, size_t smem, c
 template <typename T>
 struct MfDevice {
   DBuf<int64_t> f_off, f_rows, f_xoff, f_uoff, f_woff, f_relmap, f_asm, asm_tgt, asm_sp, asm_src, e_off;
+  DBuf<ChildEdge> ch_edge;
   DBuf<int> f_m, f_k, f_p0, f_child_ptr, f_children, rows, relmap, lvl_fronts, gidx;
   DBuf<int> pan_fronts, diag_fronts, solve_small;
   int tiny_threads = 64;
@@ -180,6 +181,14 @@ struct MfDevice {
     asm_src.upload(B.asm_src);
     f_m.upload(B.f_m); f_k.upload(B.f_k); f_p0.upload(B.f_p0);
     f_child_ptr.upload(B.f_child_ptr); f_children.upload(B.f_children);
+    {
+      std::vector<ChildEdge> ce(B.f_children.size());
+      for (size_t ci = 0; ci < B.f_children.size(); ci++) {
+        const int c = B.f_children[ci];
+        ce[ci] = ChildEdge{B.f_relmap[(size_t)c], B.f_uoff[(size_t)c], B.f_m[(size_t)c] - B.f_k[(size_t)c], 0};
+      }
+      ch_edge.upload(ce);
+    }
     rows.upload(B.rows); relmap.upload(B.relmap); lvl_fronts.upload(B.lvl_fronts);
     gidx.upload(B.gidx);
     nlevels = B.nlevels;
@@ -204,7 +213,7 @@ struct MfDevice {
     mk = 0;
     view = MfView{f_off.p, f_m.p, f_k.p, f_rows.p, f_xoff.p, f_p0.p, f_uoff.p, f_woff.p,
                   f_child_ptr.p, f_children.p, f_relmap.p, f_asm.p, rows.p, relmap.p,
-                  asm_tgt.p, asm_sp.p, asm_src.p, e_off.p};
+                  asm_tgt.p, asm_sp.p, asm_src.p, e_off.p, ch_edge.p};
     int dev = 0, optin = 0;
     CK(cudaGetDevice(&dev));
     CK(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
