@@ -1172,10 +1172,22 @@ __device__ __forceinline__ void bwd_small_body(const MfView &v, const int *__res
   const T *Ef = E + v.e_off[f];
   T e[PASS][kSmallUnroll][VN];
   load_e_batch<T, PASS, G>(Ef, ld, m, k, sl, 0, e);
+  // the ancestor rows' positions are static: read before the wait (a lane
+  // has at most 4 of the front's ld <= 4G rows)
+  const int *rows = v.rows + v.f_rows[f];
+  int rw[4];
+#pragma unroll
+  for (int q = 0; q < 4; q++) {
+    const int i = sl + q * G;
+    rw[q] = (i >= k && i < m) ? rows[i] : 0;
+  }
   pdl_wait();
   const T *xb = xl + v.f_xoff[f];
-  const int *rows = v.rows + v.f_rows[f];
-  for (int i = sl; i < ld; i += G) w[i] = i < k ? yl[xo + i] : (i < m ? __ldcg(xb + rows[i]) : T(0));
+#pragma unroll
+  for (int q = 0; q < 4; q++) {
+    const int i = sl + q * G;
+    if (i < ld) w[i] = i < k ? yl[xo + i] : (i < m ? __ldcg(xb + rw[q]) : T(0));
+  }
   __syncwarp(gm);
   T wr[PASS][VN];
 #pragma unroll
@@ -1385,8 +1397,23 @@ __device__ __forceinline__ void bwd_big_body(const MfView &v, int2 tk, const T *
     }
   };
   load_batch(c0 + cs, c0 + rq * VN);  // in flight while v is gathered
+  // the ancestor rows' positions are static: the first kRowsAhead of this
+  // thread are read before the wait
+  constexpr int kRowsAhead = 4;
+  int rw[kRowsAhead];
+#pragma unroll
+  for (int q = 0; q < kRowsAhead; q++) {
+    const int i = c0 + tid + q * NT;
+    rw[q] = (i >= k && i < m) ? rows[i] : 0;
+  }
   pdl_wait();
-  for (int i = c0 + tid; i < ld; i += NT) w[i - c0] = i < k ? yl[xo + i] : (i < m ? __ldcg(xb + rows[i]) : T(0));
+#pragma unroll
+  for (int q = 0; q < kRowsAhead; q++) {
+    const int i = c0 + tid + q * NT;
+    if (i < ld) w[i - c0] = i < k ? yl[xo + i] : (i < m ? __ldcg(xb + rw[q]) : T(0));
+  }
+  for (int i = c0 + tid + kRowsAhead * NT; i < ld; i += NT)
+    w[i - c0] = i < k ? yl[xo + i] : (i < m ? __ldcg(xb + rows[i]) : T(0));
   __syncthreads();
   for (int cc = cs; cc < 32; cc += NCS) {  // uniform trip count: the shuffles below need whole groups
     const int c = c0 + cc;
