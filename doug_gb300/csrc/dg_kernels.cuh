@@ -39,6 +39,13 @@ struct ChildEdge {
   int rc, pad;
 };
 
+// the front of a large-front solve task, stored beside the task so that the
+// task's first E loads need one load of the task list only
+struct __align__(16) TaskFront {
+  int m, k;
+  int64_t e_off;
+};
+
 struct MfView {  // device pointers of one multifrontal batch
   const int64_t *f_off;
   const int *f_m, *f_k;
@@ -1279,16 +1286,16 @@ template <typename T> struct FwdRows { static constexpr int N = 32 * Vec16<T>::N
 // the task body; b: shared memory for the front's right-hand side (m
 // values), red: the warp sums of one chunk
 template <typename T, int NT>
-__device__ __forceinline__ void fwd_big_body(const MfView &v, int2 tk, const T *__restrict__ E,
+__device__ __forceinline__ void fwd_big_body(const MfView &v, int2 tk, TaskFront tf, const T *__restrict__ E,
                                              const T *__restrict__ xl, T *__restrict__ yl, T *__restrict__ uvec,
                                              T *b, T (*red)[FwdRows<T>::N]) {
   constexpr int VN = Vec16<T>::N, RC = FwdRows<T>::N, NW = NT / 32, UN = NT == kELeanThreads ? 4 : kEUnroll;
   const int f = tk.x;
   const int ch0 = tk.y >> 16, nch = tk.y & 0xffff;
-  const int m = v.f_m[f], k = v.f_k[f], ld = round4(m);
+  const int m = tf.m, k = tf.k, ld = round4(m);
   const int64_t xo = v.f_xoff[f] + v.f_p0[f];
   const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
-  const T *Ef = E + v.e_off[f];
+  const T *Ef = E + tf.e_off;
   // one batch: columns j + u*NW (u < UN) of the chunk's rows of this lane;
   // a vector wholly above E's diagonal (rb + VN <= column) is zero
   T e[UN][VN];
@@ -1357,24 +1364,25 @@ __device__ __forceinline__ void fwd_big_body(const MfView &v, int2 tk, const T *
 
 template <typename T, int NT>
 __global__ void __launch_bounds__(NT, NT == kELeanThreads ? 12 : 4)
-mf_fwd_big(MfView v, const int2 *__restrict__ tasks, const T *__restrict__ E, const T *__restrict__ xl,
-           T *__restrict__ yl, T *__restrict__ uvec, int nrhs = 1, int64_t xs = 0, int64_t us = 0) {
+mf_fwd_big(MfView v, const int2 *__restrict__ tasks, const TaskFront *__restrict__ tmeta, const T *__restrict__ E,
+           const T *__restrict__ xl, T *__restrict__ yl, T *__restrict__ uvec, int nrhs = 1, int64_t xs = 0,
+           int64_t us = 0) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ T red[NT / 32][FwdRows<T>::N];
   pdl_trigger();
   const int task = blockIdx.x / nrhs, rk = blockIdx.x % nrhs;
-  fwd_big_body<T, NT>(v, tasks[task], E, xl + rk * xs, yl + rk * xs, uvec + rk * us,
+  fwd_big_body<T, NT>(v, tasks[task], tmeta[task], E, xl + rk * xs, yl + rk * xs, uvec + rk * us,
                       reinterpret_cast<T *>(smem_raw), red);
 }
 
 // large fronts, backward: task = {front, column block J}; x[32J .. 32J+31] from
 // rows [32J, m) of E
 template <typename T, int NT>
-__device__ __forceinline__ void bwd_big_body(const MfView &v, int2 tk, const T *__restrict__ E,
+__device__ __forceinline__ void bwd_big_body(const MfView &v, int2 tk, TaskFront tf, const T *__restrict__ E,
                                              const T *__restrict__ yl, T *__restrict__ xl, T *w) {
   constexpr int VN = Vec16<T>::N, LPC = 32 / VN, NCS = NT / LPC, UN = NT == kELeanThreads ? 4 : kEUnroll;
   const int f = tk.x, J = tk.y;
-  const int m = v.f_m[f], k = v.f_k[f], ld = round4(m);
+  const int m = tf.m, k = tf.k, ld = round4(m);
   const int c0 = 32 * J, jb = min(32, k - c0);
   const int64_t xo = v.f_xoff[f] + v.f_p0[f];
   const T *xb = xl + v.f_xoff[f];
@@ -1385,7 +1393,7 @@ __device__ __forceinline__ void bwd_big_body(const MfView &v, int2 tk, const T *
   // wholly above E's diagonal (i + VN <= c) is zero
   T e[UN][VN];
   auto load_batch = [&](int c, int i) {
-    const T *Ec = E + v.e_off[f] + (int64_t)c * ld;
+    const T *Ec = E + tf.e_off + (int64_t)c * ld;
 #pragma unroll
     for (int u = 0; u < UN; u++) {
       const int ii = i + u * 32;
@@ -1441,12 +1449,12 @@ __device__ __forceinline__ void bwd_big_body(const MfView &v, int2 tk, const T *
 
 template <typename T, int NT>
 __global__ void __launch_bounds__(NT, NT == kELeanThreads ? 12 : 4)
-mf_bwd_big(MfView v, const int2 *__restrict__ tasks, const T *__restrict__ E, const T *__restrict__ yl,
-           T *__restrict__ xl, int nrhs = 1, int64_t xs = 0) {
+mf_bwd_big(MfView v, const int2 *__restrict__ tasks, const TaskFront *__restrict__ tmeta, const T *__restrict__ E,
+           const T *__restrict__ yl, T *__restrict__ xl, int nrhs = 1, int64_t xs = 0) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   pdl_trigger();
   const int task = blockIdx.x / nrhs, rk = blockIdx.x % nrhs;
-  bwd_big_body<T, NT>(v, tasks[task], E, yl + rk * xs, xl + rk * xs, reinterpret_cast<T *>(smem_raw));
+  bwd_big_body<T, NT>(v, tasks[task], tmeta[task], E, yl + rk * xs, xl + rk * xs, reinterpret_cast<T *>(smem_raw));
 }
 
 // ---------------------------------------------------------------------------
@@ -1506,7 +1514,8 @@ __device__ __forceinline__ void queue_publish(const QueueView &q, int *done, int
 template <typename T>
 __global__ void __launch_bounds__(256, 4)
 mf_fwd_queue(MfView v, QueueView q, const int *__restrict__ small_fronts, const int *__restrict__ lvl_small_off,
-             const SmallBuckets *__restrict__ lvl_sb, const int2 *__restrict__ fwd_tasks, const T *__restrict__ E,
+             const SmallBuckets *__restrict__ lvl_sb, const int2 *__restrict__ fwd_tasks,
+             const TaskFront *__restrict__ fwd_tmeta, const T *__restrict__ E,
              const T *__restrict__ xl, T *__restrict__ yl, T *__restrict__ uvec, int *counter, int *done,
              int *status, int nrhs = 1, int64_t xs = 0, int64_t us = 0) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -1533,7 +1542,7 @@ mf_fwd_queue(MfView v, QueueView q, const int *__restrict__ small_fronts, const 
       else if (b < sb.nb0 + sb.nb1) fwd_small_body<T, 16>(v, fr + sb.cnt0, sb.cnt1, E, xk, yk, uk, b - sb.nb0, sm);
       else fwd_small_body<T, 32>(v, fr + sb.cnt0 + sb.cnt1, sb.cnt2, E, xk, yk, uk, b - sb.nb0 - sb.nb1, sm);
     } else {
-      fwd_big_body<T, 256>(v, fwd_tasks[tk.z], E, xk, yk, uk, sm, red);
+      fwd_big_body<T, 256>(v, fwd_tasks[tk.z], fwd_tmeta[tk.z], E, xk, yk, uk, sm, red);
     }
     __syncthreads();
     if (threadIdx.x == 0) queue_publish<T>(q, done, g);
@@ -1543,7 +1552,8 @@ mf_fwd_queue(MfView v, QueueView q, const int *__restrict__ small_fronts, const 
 template <typename T>
 __global__ void __launch_bounds__(256, 4)
 mf_bwd_queue(MfView v, QueueView q, const int *__restrict__ small_fronts, const int *__restrict__ lvl_small_off,
-             const SmallBuckets *__restrict__ lvl_sb, const int2 *__restrict__ bwd_tasks, const T *__restrict__ E,
+             const SmallBuckets *__restrict__ lvl_sb, const int2 *__restrict__ bwd_tasks,
+             const TaskFront *__restrict__ bwd_tmeta, const T *__restrict__ E,
              const T *__restrict__ yl, T *__restrict__ xl, int *counter, int *done, int *status, int nrhs = 1,
              int64_t xs = 0) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -1569,7 +1579,7 @@ mf_bwd_queue(MfView v, QueueView q, const int *__restrict__ small_fronts, const 
       else if (b < sb.nb0 + sb.nb1) bwd_small_body<T, 16>(v, fr + sb.cnt0, sb.cnt1, E, yk, xk, b - sb.nb0, sm);
       else bwd_small_body<T, 32>(v, fr + sb.cnt0 + sb.cnt1, sb.cnt2, E, yk, xk, b - sb.nb0 - sb.nb1, sm);
     } else {
-      bwd_big_body<T, 256>(v, bwd_tasks[tk.z], E, yk, xk, sm);
+      bwd_big_body<T, 256>(v, bwd_tasks[tk.z], bwd_tmeta[tk.z], E, yk, xk, sm);
     }
     __syncthreads();
     if (threadIdx.x == 0) queue_publish<T>(q, done, g);

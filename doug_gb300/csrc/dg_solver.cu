@@ -141,6 +141,7 @@ struct MfDevice {
   int qf_n = 0, qb_n = 0, q_grid = 0, q_k = 0;
   size_t q_smem = 0;
   DBuf<int2> asm_tasks, upd_tasks, panel_tasks, esc_tasks, etile_tasks, fwd_tasks, bwd_tasks;
+  DBuf<TaskFront> fwd_tmeta, bwd_tmeta;  // each solve task's front (m, k, E offset)
   DBuf<T> arena, E, xl, yl, u;
   int64_t e_len = 0;
   // per level: small-front range, assembly-task range, steps
@@ -332,6 +333,7 @@ struct MfDevice {
     // longest first
     std::vector<int> ss;
     std::vector<int2> fw, bw;
+    std::vector<TaskFront> fwm, bwm;
     size_t fwd_smem_max = 0, bwd_smem_max = 0;
     slevels.assign((size_t)nlevels, SolveLevel());
     for (int l = 0; l < nlevels; l++) {
@@ -378,6 +380,14 @@ struct MfDevice {
       std::stable_sort(bl.begin(), bl.end(), [](const std::pair<int, int2> &a, const std::pair<int, int2> &b) { return a.first > b.first; });
       for (auto &e : fl) fw.push_back(e.second);
       for (auto &e : bl) bw.push_back(e.second);
+      for (auto &e : fl) {
+        const int f = e.second.x;
+        fwm.push_back(TaskFront{B.f_m[(size_t)f], B.f_k[(size_t)f], eo[(size_t)f]});
+      }
+      for (auto &e : bl) {
+        const int f = e.second.x;
+        bwm.push_back(TaskFront{B.f_m[(size_t)f], B.f_k[(size_t)f], eo[(size_t)f]});
+      }
       // fronts of similar pivot counts share a warp
       L.small_off = (int)ss.size();
       int cnt[3];
@@ -400,6 +410,8 @@ struct MfDevice {
     solve_small.upload(ss);
     fwd_tasks.upload(fw);
     bwd_tasks.upload(bw);
+    fwd_tmeta.upload(fwm);
+    bwd_tmeta.upload(bwm);
     set_solve_attrs<kEThreads>(optin, fwd_smem_max, bwd_smem_max);
     set_solve_attrs<kELeanThreads>(optin, fwd_smem_max, bwd_smem_max);
     queue = tune.schedule == 1;
@@ -621,11 +633,13 @@ struct MfDevice {
       CK(cudaMemsetAsync(q_done.p, 0, (size_t)(qf_n + qb_n) * nrhs * sizeof(int), s));
       mf_fwd_queue<T><<<q_grid, 256, q_smem, s>>>(view, QueueView{qf_tasks.p, qf_dep_ptr.p, qf_dep.p, qf_n,
                                                                    q_wait_cycles, q_skip_publish},
-                                                  solve_small.p, q_small_off.p, q_sb.p, fwd_tasks.p, E.p, xl_, yl_,
+                                                  solve_small.p, q_small_off.p, q_sb.p, fwd_tasks.p, fwd_tmeta.p, E.p,
+                                                  xl_, yl_,
                                                   u_, q_counter.p, q_done.p, status, nrhs, xs, us);
       mf_bwd_queue<T><<<q_grid, 256, q_smem, s>>>(view, QueueView{qb_tasks.p, qb_dep_ptr.p, qb_dep.p, qb_n,
                                                                    q_wait_cycles, -1},
-                                                  solve_small.p, q_small_off.p, q_sb.p, bwd_tasks.p, E.p, yl_, xl_,
+                                                  solve_small.p, q_small_off.p, q_sb.p, bwd_tasks.p, bwd_tmeta.p, E.p,
+                                                  yl_, xl_,
                                                   q_counter.p + 1, q_done.p + (size_t)qf_n * nrhs, status, nrhs, xs);
       return 2;
     }
@@ -640,7 +654,8 @@ struct MfDevice {
       if (L.fwd_cnt) {
         launch_level(pdl, L.fwd_lean ? mf_fwd_big<T, kELeanThreads> : mf_fwd_big<T, kEThreads>, L.fwd_cnt * nrhs,
                      L.fwd_lean ? kELeanThreads : kEThreads, L.fwd_smem, s, view,
-                     (const int2 *)(fwd_tasks.p + L.fwd_off), (const T *)E.p, (const T *)xl_, yl_, u_, nrhs, xs, us);
+                     (const int2 *)(fwd_tasks.p + L.fwd_off), (const TaskFront *)(fwd_tmeta.p + L.fwd_off),
+                     (const T *)E.p, (const T *)xl_, yl_, u_, nrhs, xs, us);
         launches++;
       }
     }
@@ -649,7 +664,8 @@ struct MfDevice {
       if (L.bwd_cnt) {
         launch_level(pdl, L.bwd_lean ? mf_bwd_big<T, kELeanThreads> : mf_bwd_big<T, kEThreads>, L.bwd_cnt * nrhs,
                      L.bwd_lean ? kELeanThreads : kEThreads, L.bwd_smem, s, view,
-                     (const int2 *)(bwd_tasks.p + L.bwd_off), (const T *)E.p, (const T *)yl_, xl_, nrhs, xs);
+                     (const int2 *)(bwd_tasks.p + L.bwd_off), (const TaskFront *)(bwd_tmeta.p + L.bwd_off),
+                     (const T *)E.p, (const T *)yl_, xl_, nrhs, xs);
         launches++;
       }
       if (L.small_cta) {
